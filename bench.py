@@ -1,0 +1,292 @@
+#!/usr/bin/env python3
+"""Benchmark: V1 neuron-steps/s of the patchV1 hot path on GB300.
+
+Workload (the full-patch configuration): 32 blocks x 1024 = 32,768 V1 neurons (80% LIF E /
+20% AdEx I), 16,384 ON/OFF magno LGN cells on 128x128 drifting-grating frames at 120 Hz,
+~400 far partners per neuron with distance delays, dense within-block connectivity,
+dt = 0.125 ms, fp32, seeded synthetic data.
+
+One bench step = `--sim-steps` simulation steps (default 800 = 100 ms simulated) of the whole
+loop (LGN convolution + LGN spikes + V1 step + near and far delivery).  Between timed bench
+steps L2 is flushed by writing a 512 MiB buffer.  `value` is device time (CUDA events on the
+plan's stream); `e2e` runs the same bench step through the public API from host buffers:
+stimulus upload (H2D) + the steps + spike-raster download (D2H), wall-clock timed.
+
+`--impl reference` times the CPU implementation of the path (the oracle's restatement of the
+reference's kernels and host far delivery, OpenMP on all host cores) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "V1 neuron-steps/s fwd and fwd+adjoint, batched vs plain on one GB300 at tol"
+UNIT = "neuron-steps/s"
+L2_FLUSH = 512 << 20
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_dev{device}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["active", "hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names[1:], parts[5:9]):
+                if v.lower() in ("active", "1", "0x1"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(kernel: str):
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            t = json.load(f)
+        return t.get(kernel)
+    return None
+
+
+def algorithmic_bytes_per_neuron_step(wl, rate_hz: float) -> float:
+    """Bytes per V1 neuron-step the step kernel must move (state read+write, LGN synapses,
+    LGN spike words, and the per-spike conMat column and far fan-out)."""
+    s = wl.spec
+    S = 3 + 2 * (s.ngFF + s.ngE + s.ngI)
+    m = float(np.mean(wl.net.nLGNperV1))
+    nlgn_over_n = wl.lgn.nLGN / s.nV1
+    k_far = float(np.mean(wl.net.nVec)) if wl.net.nVec.size else 0.0
+    n_nb = float(np.mean(wl.net.nNearNB))
+    r_dt = rate_hz * s.dt * 1e-3
+    return 8 * S + 12 + 8 * m + 8 * nlgn_over_n + r_dt * (4 * s.blockSize * n_nb + 16 * k_far)
+
+
+def build_workload(name: str):
+    from visual_cortex_gb300 import synth
+    if name == "C1":
+        return synth.config1(seed=0)
+    return synth.config2(seed=0)
+
+
+def run_gb300(args):
+    rank, world, local = dist_env()
+    from visual_cortex_gb300.build import build_native
+    build_native()
+    from visual_cortex_gb300 import _native as N
+    from visual_cortex_gb300.model import Simulation
+
+    N.check(None, N.lib.pv1_set_device(local), "pv1_set_device")
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as td
+        torch.cuda.set_device(local)
+        td.init_process_group("nccl")
+        dist = td
+
+    wl = build_workload(args.config)
+    S = args.sim_steps
+    sim = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    for _ in range(args.warmup):
+        sim.run_timed(S, L2_FLUSH)
+    if dist:
+        dist.barrier()
+    times = []
+    launches = 0
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            times.append(sim.run_timed(S, L2_FLUSH))
+            launches += sim.launches()
+    total_ms = float(np.sum(times))
+    if dist:
+        import torch
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    neuron_steps = wl.spec.nV1 * S * args.steps * world
+    value = neuron_steps / (total_ms * 1e-3)
+
+    # per-kernel device time (direct launches, events around each launch)
+    v1_ms, lgn_ms, chunk = sim.time_kernels(320)
+
+    # end to end through the public API from host buffers
+    sim.set_record(N.REC_SPIKES, S + 1)
+    e2e_times, spikes = [], 0
+    for q in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        sim.load_stimulus(wl.stim)
+        step0 = sim.step
+        sim.run(S, sync=False)
+        sp = sim.fetch_spikes(step0, S)
+        e2e_times.append(time.perf_counter() - t0)
+        spikes += int((sp >= 1).sum())
+    e2e_s = float(np.sum(e2e_times))
+    e2e_value = wl.spec.nV1 * S * len(e2e_times) * world / e2e_s
+    rate_hz = spikes / (wl.spec.nV1 * S * len(e2e_times) * wl.spec.dt * 1e-3)
+    sim.close()
+
+    peak, peak_kind = load_peaks()
+    bpn = algorithmic_bytes_per_neuron_step(wl, rate_hz)
+    bytes_per_launch = bpn * wl.spec.nV1
+    achieved = bytes_per_launch / (v1_ms * 1e-3) / 1e9
+    traffic = load_traffic("v1_step_kernel")
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": ("32x1024 V1 (80% LIF E / 20% AdEx I), 16384 magno LGN, 128x128 "
+                                "grating 120 Hz, ~400 far partners/neuron, dt 0.125 ms")
+                   if args.config == "C2" else "1x1024 V1, 512 LGN, 64x64 grating, dt 0.125 ms",
+                   "sim_steps_per_bench_step": S, "nV1": wl.spec.nV1, "nLGN": wl.lgn.nLGN,
+                   "mode": "plain forward", "l2": "flushed (512 MiB write) before each timed bench step",
+                   "v1_rate_hz": rate_hz},
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": int(wl.stim.frames.nbytes),
+                "d2h_bytes_per_step": int(S * wl.spec.nV1 * 4)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "v1_step_kernel", "peak_source": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes_per_launch": bytes_per_launch,
+                     "launch_ms": v1_ms, "lgn_chunk_ms": lgn_ms, "lgn_chunk_steps": chunk},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(wl, args.cpu_sample_steps)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def cpu_baseline(wl, nsteps: int):
+    import oracle
+    from oracle.baseline import CpuPatch, cpu_model, host_threads
+    oracle.build()
+    cp = CpuPatch(wl)
+    cp.step(2)
+    dt = cp.time_steps(nsteps)
+    return {"value": wl.spec.nV1 * nsteps / dt, "unit": UNIT, "cores": cp.threads, "kind": "port",
+            "sample": f"{nsteps} steps of the same workload ({wl.spec.nV1} neurons), "
+                      f"CPU restatement with OpenMP on {cp.threads} threads ({cpu_model()})",
+            "seconds": dt}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return None
+    import oracle
+    from oracle.baseline import CpuPatch, cpu_model
+    oracle.build()
+    wl = build_workload(args.config)
+    cp = CpuPatch(wl)
+    n = args.cpu_sample_steps
+    for _ in range(args.warmup):
+        cp.step(max(1, n // 4))
+    times = [cp.time_steps(n) for _ in range(args.steps)]
+    total = float(np.sum(times))
+    value = wl.spec.nV1 * n * args.steps / total
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "same as the GB300 arm", "sim_steps_per_bench_step": n,
+                   "nV1": wl.spec.nV1},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cp.threads, "kind": "port",
+                         "sample": f"{n} simulation steps per bench step, CPU restatement of the "
+                                   f"reference kernels + host far delivery ({cpu_model()})"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="C2", choices=["C1", "C2"])
+    ap.add_argument("--sim-steps", type=int, default=800)
+    ap.add_argument("--cpu-sample-steps", type=int, default=40)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    out = run_reference(args) if args.impl == "reference" else run_gb300(args)
+    if out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

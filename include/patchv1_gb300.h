@@ -1,0 +1,257 @@
+/*
+ * patchv1_gb300.h -- C ABI of the GB300 (sm_103a) simulation hot path of patchV1.
+ *
+ * The reference (`patch`, src/patch.cu) has no library interface: its hot path is a set of
+ * CUDA kernels and one host function driven from main().  Each entry point below replaces
+ * one of those pieces; the comment on each cites the reference code it stands in for
+ * (paths relative to the reference project root).
+ *
+ * Conventions
+ *   - Every function returns 0 on success and a negative PV1_E* code on failure; the text of
+ *     the last failure of a plan is returned by pv1_last_error().  Nothing here calls exit()
+ *     or traps the GPU (the reference exits on any CUDA error, src/CUDA_MACRO.h:23-31).
+ *   - All arrays are host arrays owned by the caller and copied; the plan owns every device
+ *     buffer and its CUDA stream.  Calls on one plan are not thread safe; plans are
+ *     independent of each other.
+ *   - Float is 32-bit IEEE (the reference's Float, src/types.h:6), Size is uint32_t.
+ *   - Neuron ids are block-major (id = block*blockSize + local), excitatory types first within
+ *     a block (typeAcc), exactly as in the reference's files.
+ */
+#ifndef PATCHV1_GB300_H
+#define PATCHV1_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PV1_OK              0
+#define PV1_E_ARG          -1   /* bad argument / inconsistent sizes            */
+#define PV1_E_CUDA         -2   /* a CUDA runtime call failed                    */
+#define PV1_E_STATE        -3   /* call out of order (e.g. run before setup)     */
+#define PV1_E_UNSUPPORTED  -4   /* option of the reference not built here        */
+#define PV1_E_DEVICE       -5   /* a kernel raised its error word                */
+#define PV1_E_NOMEM        -6   /* device allocation failed                      */
+
+#define PV1_MAX_NTYPE 2         /* reference MAX_NTYPE, src/CONST.h:12            */
+#define PV1_MAX_NG    2         /* reference MAX_NGTYPE_*, src/CONST.h:24-28      */
+
+typedef struct pv1_plan pv1_plan;
+
+/* V1 model description: the option table entries of src/patch.cu:181-288 that the step,
+ * the delivery and the conductance kinetics read, after the per-type expansion done in
+ * src/patch.cu:890-1000 (size-1 vectors broadcast to nType; vT := vThres for iModel 0). */
+typedef struct pv1_v1_config {
+    uint32_t nblock, blockSize;             /* V1_allpos header, src/patch.cu:697-703     */
+    uint32_t nType, nTypeE;                 /* connectome_cfg, src/patch.cu:636-645       */
+    uint32_t typeAcc[PV1_MAX_NTYPE];        /* typeAccCount (cumulative, last == blockSize)*/
+    uint32_t ngFF, ngE, ngI;                /* sizes of riseTime{FF,E,I}                  */
+    float dt;                               /* ms                                         */
+    float riseFF[PV1_MAX_NG], decayFF[PV1_MAX_NG];
+    float riseE[PV1_MAX_NG],  decayE[PV1_MAX_NG];
+    float riseI[PV1_MAX_NG],  decayI[PV1_MAX_NG];
+    float vE, vI, vL;                       /* reversal potentials; the reference fixes them
+                                               at compile time to 0, -75, -65 (src/CONST.h:7-9) */
+    float vR[PV1_MAX_NTYPE], vThres[PV1_MAX_NTYPE], gL[PV1_MAX_NTYPE], C[PV1_MAX_NTYPE];
+    float tRef[PV1_MAX_NTYPE], vT[PV1_MAX_NTYPE], deltaT[PV1_MAX_NTYPE];
+    float tau_w[PV1_MAX_NTYPE], a[PV1_MAX_NTYPE], b[PV1_MAX_NTYPE];
+    float pFF[PV1_MAX_NTYPE * PV1_MAX_NG];  /* [nType][ngFF]                               */
+    float pE[PV1_MAX_NTYPE * PV1_MAX_NG];   /* [nType][ngE]                                */
+    float pI[PV1_MAX_NTYPE * PV1_MAX_NG];   /* [nType][ngI]                                */
+    float synFail[PV1_MAX_NTYPE * PV1_MAX_NTYPE];    /* [pre type][post type]              */
+    float synPerCon[PV1_MAX_NTYPE * PV1_MAX_NTYPE];
+    float synFailFF[PV1_MAX_NTYPE], synPerConFF[PV1_MAX_NTYPE];
+    float noisyDep[PV1_MAX_NTYPE];
+    float tau_noise;
+    int32_t noiseOnTonic;
+    int32_t iModel;                         /* 0: LIF (w held at 0), 1: AdEx              */
+    int32_t noDelay;                        /* 1 only (distance-free near delivery)       */
+    int32_t noFarDelay;                     /* 0: delayed far delivery; 1: reference drops
+                                               far input (src/coredynamics.cu:218-220)    */
+    float speedOfThought;                   /* mm/ms                                      */
+    int32_t hWrite;                         /* rawData carries h as well as g             */
+} pv1_v1_config;
+
+/* Magnocellular (ON/OFF DoG) LGN description: the stimulus/kernel-sampling bookkeeping of
+ * src/patch.cu:4950-5030 and 5395-5412 and the geometry of src/patch.cu:1604-1630. */
+typedef struct pv1_lgn_config {
+    uint32_t nLGN;              /* all LGN cells (parvo + magno); V1 synapses index these */
+    uint32_t nParvo_I, nMagno_I, nParvo_C, nMagno_C;  /* cell order in the LGN files      */
+    uint32_t mSample1D;         /* mSpatialSample1D (<= 32)                                */
+    uint32_t nKernelSample;     /* mKernelSample                                           */
+    uint32_t kernelSampleInterval, iKernelSampleT0;   /* in steps                          */
+    uint32_t denorm, ntPerFrame, maxFrame;            /* frame phase bookkeeping           */
+    uint32_t magnoComp, frameOffset;  /* frameOffset = pLongerThanM*dFrame                  */
+    float dt;
+    float kernelSampleDt, kernelSampleT0;             /* ms                                */
+    float convolRatio, frRatio;
+    float normViewDistance, L_x0, L_y0, R_x0, R_y0;
+    float nsig;
+    int32_t flat_retina;
+} pv1_lgn_config;
+
+/* Per-cell LGN parameters as stored in the `LGN` file (src/patch.cu:2505-2534): arrays of
+ * 2*nLGN hold [center][nLGN] then [surround][nLGN]. */
+typedef struct pv1_lgn_params {
+    const float *polar, *ecc, *rw, *rh, *orient, *k;        /* 2*nLGN each */
+    const float *ratio, *tauR, *tauD, *nR, *nD, *delay;     /* 2*nLGN each */
+    const float *spont, *c50, *sharpness;                   /* nLGN each   */
+    const uint32_t *coneType;                               /* 2*nLGN      */
+} pv1_lgn_params;
+
+/* ---- plan lifetime ------------------------------------------------------------------ */
+
+/* Makes `device` the current CUDA device of the calling thread for this library (the
+ * reference picks the device with the most free memory, src/patch.cu:9-24; here the caller
+ * chooses).  Plans are created on the current device. */
+int pv1_set_device(int device);
+
+/* Creates a plan on the current CUDA device.  Replaces the allocation part of main()
+ * (src/patch.cu:3898-4070). */
+int pv1_plan_create(const pv1_v1_config *cfg, pv1_plan **out);
+void pv1_plan_destroy(pv1_plan *plan);
+const char *pv1_last_error(const pv1_plan *plan);
+/* ABI version of this header (bumped on any signature change). */
+int pv1_abi_version(void);
+
+/* ---- LGN -------------------------------------------------------------------------- */
+
+/* Builds the temporal weights (time reversed, L1 normalised), the DoG spatial weights, the
+ * texture coordinates and max_convol of every magno cell on the device, and seeds the LGN
+ * Poisson generators.  Replaces store_PM(PM=1) (src/discrete_input_convol.cu:427-744, with
+ * store_temporalWeight :230-305), hStatic_nonlinear (src/LGN_props.h:143-170) and
+ * logRand_init (src/coredynamics.cu:148-177) called with `seed` (src/patch.cu:2685). */
+int pv1_lgn_setup(pv1_plan *plan, const pv1_lgn_config *lcfg, const pv1_lgn_params *p,
+                  uint64_t seed);
+
+/* Copies the setup tables back: TW [nMagno][nKernelSample], SW [nMagno][mSample],
+ * SC [2][nMagno][mSample], maxConvol [nLGN].  Any pointer may be NULL. */
+int pv1_lgn_get_tables(pv1_plan *plan, float *TW, float *SW, float *SC, float *maxConvol);
+
+/* Loads the stimulus movie (stimulus.bin body: nFrame frames of L,M,S planes [h][w]) and the
+ * initial luminance (init_L,M,S of the stimulus header), and runs the per-frame spatial stage
+ * of LGN_convol_magno (src/discrete_input_convol.cu:1474-1532) once per distinct frame.
+ * Frames loop at the end of the movie as in src/patch.cu:5987-5993. */
+int pv1_stimulus_load(pv1_plan *plan, uint32_t nFrame, uint32_t height, uint32_t width,
+                      const float init_LMS[3], const float *frames);
+
+/* Reads the spatial-stage table S [nFrame+1][nMagno] (row nFrame: the initial luminance). */
+int pv1_lgn_get_spatial(pv1_plan *plan, float *S);
+
+/* ---- V1 --------------------------------------------------------------------------- */
+
+/* LGN->V1 feed-forward synapses, transposed [maxLGN][nV1] as the reference keeps them in
+ * device memory (read_LGN, src/patch.h:30-77; getLGN_V1_surface, src/stats.cu:99-112).
+ * sLGN already carries sRatioLGN. */
+int pv1_v1_set_lgn_synapses(pv1_plan *plan, uint32_t maxLGN, const uint32_t *nLGNperV1,
+                            const uint32_t *lgnId, const float *sLGN);
+
+/* Near-neighbour connectivity: conMat [nblock][nearNeighborBlock][blockSize pre][blockSize
+ * post], neighborBlockId [nblock][nearNeighborBlock], nNearNeighborBlock [nblock]
+ * (src/patch.cu:3442-3497).  Strengths already carry sRatioV1. */
+int pv1_v1_set_near(pv1_plan *plan, uint32_t nearNeighborBlock, const uint32_t *nNearNB,
+                    const uint32_t *neighborBlockId, const float *conMat);
+
+/* Far connectivity as read from V1_vec (src/patch.cu:3313-3352): for post neuron i, nVec[i]
+ * entries of (vecID, conVec, delayVec) stored back to back.  Strengths already carry
+ * sRatioV1.  Builds the outgoing (by pre-neuron) event lists used on the device; replaces
+ * the host loop recal_G_vec (src/coredynamics.cu:181-372) with fill_fSpikeTrain
+ * (src/stats.cu:114-126) and sum_G (src/coredynamics.cu:2312-2349). */
+int pv1_v1_set_far(pv1_plan *plan, const uint32_t *nVec, const uint32_t *vecID,
+                   const float *conVec, const float *delayVec);
+
+/* Initial state (host-generated as in src/patch.cu:4405-4560).  Layouts: [nV1] or
+ * [ng][nV1]; w may be NULL for iModel 0. */
+int pv1_v1_set_state(pv1_plan *plan, const float *v, const float *w, const float *gFF,
+                     const float *hFF, const float *gE, const float *hE, const float *gI,
+                     const float *hI, const float *tonicDep);
+
+/* Seeds the per-neuron device generators and advances them as rand_spInit does
+ * (src/coredynamics.cu:5-146) for a network without initial spikes (spE0 = spI0 = 0). */
+int pv1_v1_init_rng(pv1_plan *plan, uint64_t seed, uint32_t trainDepth);
+
+/* Host initial-state generator of src/patch.cu:4405-4560 (libstdc++ default_random_engine
+ * and normal/uniform distributions, same call order).  v0/w0/g0 arrays as in the cfg:
+ * v0 [nType][2], w0 [nType][2], gFF0 [nType][ngFF][4], gE0 [nType][ngE][4],
+ * gI0 [nType][ngI][4].  Outputs [nV1] / [ng][nV1]. */
+int pv1_host_init_state(const pv1_v1_config *cfg, uint64_t seed, const float *tonicDep,
+                        const uint32_t *nLGNperV1, int use_v0, float tonicMax,
+                        const float *w0, const float *gFF0, const float *gE0,
+                        const float *gI0, float *v, float *w, float *gFF, float *hFF,
+                        float *gE, float *hE, float *gI, float *hI);
+
+/* ---- stepping --------------------------------------------------------------------- */
+
+#define PV1_REC_RAW    1   /* rawData records (src/patch.cu:6138-6165, 6255-6261)        */
+#define PV1_REC_LGN_SP 2   /* LGN_sp records (src/patch.cu:6423)                         */
+#define PV1_REC_LGN_FR 4   /* LGN_fr records                                             */
+#define PV1_REC_SPIKES 8   /* spike words only: the first field of each rawData record   */
+
+/* Sets which per-step records the device keeps, in a ring of `slots` steps. */
+int pv1_set_record(pv1_plan *plan, int flags, uint32_t slots);
+/* Bytes of one rawData record (after the file header). */
+int64_t pv1_raw_record_floats(const pv1_plan *plan);
+
+/* Runs `nsteps` steps of the hot loop (src/patch.cu:5966-6880): LGN convolution, LGN spikes,
+ * V1 step, near and far delivery.  Work is issued as CUDA graphs on the plan's stream.
+ * Returns after the work is queued when `sync` is 0. */
+int pv1_run(pv1_plan *plan, uint32_t nsteps, int sync);
+
+/* Copies finished records [step0, step0+n) to host buffers (any may be NULL):
+ * raw: n * pv1_raw_record_floats floats; lgn_sp, lgn_fr: n * nLGN floats. */
+int pv1_fetch_records(pv1_plan *plan, uint64_t step0, uint32_t n, float *raw,
+                      float *lgn_sp, float *lgn_fr);
+
+#define PV1_ST_V      0
+#define PV1_ST_W      1
+#define PV1_ST_TBACK  2
+#define PV1_ST_DEP    3
+#define PV1_ST_GFF    4   /* [ngFF][nV1] */
+#define PV1_ST_HFF    5
+#define PV1_ST_GE     6   /* [ngE][nV1], after the last step's delivery */
+#define PV1_ST_HE     7
+#define PV1_ST_GI     8
+#define PV1_ST_HI     9
+#define PV1_ST_SINFO 10   /* last step's spike word per neuron */
+#define PV1_ST_LGN_LTR 11 /* [nLGN] leftTimeRate  */
+#define PV1_ST_LGN_LNL 12 /* [nLGN] lastNegLogRand */
+#define PV1_ST_LGN_SINFO 13 /* [nLGN] last step's LGN spike word */
+/* Copies one state array to the host (waits for queued work). */
+int pv1_get_state(pv1_plan *plan, int which, float *out);
+/* Overwrites one state array (PV1_ST_* above). */
+int pv1_put_state(pv1_plan *plan, int which, const float *in);
+
+/* Draw recording for parity tests: when enabled, every uniform/normal the kernels draw is
+ * written to per-step buffers so that a CPU restatement can consume the same draws.
+ * capacity = draws kept per entity per step (LGN Poisson, V1 noise, FF failure, near
+ * failure).  0 disables. */
+int pv1_set_draw_record(pv1_plan *plan, uint32_t steps, uint32_t capacity);
+/* kind: 0 LGN uniforms [steps][nLGN][cap], 1 V1 noise normals [steps][nV1],
+ * 2 FF-failure normals [steps][nV1][cap], 3 near-failure normals [steps][nV1][cap]
+ * (indexed by the step whose spikes were delivered).  counts (may be NULL) receives
+ * the number of draws per entity per step, same leading shape. */
+int pv1_fetch_draws(pv1_plan *plan, int kind, float *draws, int32_t *counts);
+
+/* Spike words of steps [step0, step0+n) into out [n][nV1] (PV1_REC_SPIKES ring). */
+int pv1_fetch_spikes(pv1_plan *plan, uint64_t step0, uint32_t n, float *out);
+
+/* Number of kernel launches issued by the last pv1_run (for launch accounting). */
+int64_t pv1_last_launch_count(const pv1_plan *plan);
+
+/* ---- measurement (no counterpart in the reference, which has no timers) ------------- */
+
+/* Writes flush_bytes of a scratch buffer (to evict L2), then runs nsteps between two CUDA
+ * events on the plan's stream; *ms receives the device time of the run alone. */
+int pv1_run_timed(pv1_plan *plan, uint32_t nsteps, uint64_t flush_bytes, float *ms);
+
+/* Runs nsteps with one direct launch per kernel, each bracketed by CUDA events on the plan's
+ * stream; returns the mean device time per launch of the V1 step kernel and of the LGN
+ * rate+spike pair (per chunk of `chunk` steps; one chunk per `chunk` steps). */
+int pv1_time_kernels(pv1_plan *plan, uint32_t nsteps, float *v1_ms, float *lgn_ms, int *chunk);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PATCHV1_GB300_H */

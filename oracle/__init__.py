@@ -1,0 +1,207 @@
+"""CPU oracle of the patchV1 hot path -- TEST INFRASTRUCTURE, not part of the product.
+
+Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py use this package,
+as the checker.  pv1_oracle.c restates the reference's kernels on the CPU; this module builds
+it with gcc and drives it in the reference's own per-step order
+(src/patch.cu:5966-6880): LGN convolution -> LGN spikes -> V1 step -> near delivery -> far
+delivery.  Random draws are supplied by the caller (recorded from the GPU run under test):
+cuRAND is not re-derived here.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE.parent / "_build" / "oracle"
+LIB = BUILD / "liboracle.so"
+f32 = np.float32
+
+
+def build(force: bool = False) -> Path:
+    src = HERE / "pv1_oracle.c"
+    hdr = HERE.parent / "include" / "patchv1_gb300.h"
+    if not force and LIB.exists() and LIB.stat().st_mtime > max(src.stat().st_mtime, hdr.stat().st_mtime):
+        return LIB
+    BUILD.mkdir(parents=True, exist_ok=True)
+    tmp = LIB.with_suffix(".tmp.so")
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-std=c11",
+           "-D_GNU_SOURCE", "-o", str(tmp), str(src), "-lm"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + res.stderr)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        P = C.c_void_p
+        FP = C.POINTER(C.c_float)
+        UP = C.POINTER(C.c_uint32)
+        IP = C.POINTER(C.c_int32)
+        L.orc_lgn_setup.argtypes = [P, P, FP, FP, FP, FP, FP, FP, FP]
+        L.orc_lgn_spatial.argtypes = [C.c_int, C.c_int, FP, FP, UP, FP, C.c_int, C.c_int, C.c_int, C.c_int, FP]
+        L.orc_lgn_convol.argtypes = [P, C.c_int, C.c_int, C.c_longlong, FP, FP, FP, FP]
+        L.orc_lgn_nonlinear.argtypes = [P, FP, FP, FP, FP, FP, FP, FP, FP, FP, IP, C.c_int, FP, FP]
+        L.orc_v1_create.argtypes = [P, C.c_uint32, UP, UP, FP, C.c_uint32, UP, UP, FP, UP, UP, FP, FP, FP]
+        L.orc_v1_create.restype = P
+        L.orc_v1_destroy.argtypes = [P]
+        L.orc_v1_get.argtypes = [P, C.c_int, FP]
+        L.orc_v1_put.argtypes = [P, C.c_int, FP]
+        L.orc_v1_compute_v.argtypes = [P, FP, FP, FP, C.c_int]
+        L.orc_v1_deliver_near.argtypes = [P, FP, C.c_int]
+        L.orc_v1_deliver_far.argtypes = [P]
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_num_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def fp(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags.c_contiguous, (a.dtype, a.flags)
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def up(a):
+    if a is None:
+        return None
+    assert a.dtype == np.uint32 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_uint32))
+
+
+def ip(a):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+ST = dict(v=0, w=1, tBack=2, dep=3, gFF=4, hFF=5, gE=6, hE=7, gI=8, hI=9, sInfo=10)
+
+
+class LgnOracle:
+    """store_PM + per-frame spatial stage + per-step convolution and spikes for magno cells."""
+
+    def __init__(self, lgn, stim, wbits: int = 8):
+        self.lgn = lgn
+        self.cfg = lgn.to_struct()
+        self.params, self._keep = lgn.params_struct()
+        nm, ns, nks = lgn.nMagno, lgn.mSample1D ** 2, lgn.sched.mKernelSample
+        self.TW = np.empty((nm, nks), f32)
+        self.SW = np.empty((nm, ns), f32)
+        self.SC = np.empty((2, nm, ns), f32)
+        self.maxConvol = np.empty(lgn.nLGN, f32)
+        self.absk = np.empty(nm, f32)
+        self.la = np.empty(lgn.nLGN, f32)
+        self.lb = np.empty(lgn.nLGN, f32)
+        L = lib()
+        L.orc_lgn_setup(C.byref(self.cfg), C.byref(self.params), fp(self.TW), fp(self.SW), fp(self.SC),
+                        fp(self.maxConvol), fp(self.absk), fp(self.la), fp(self.lb))
+        self.nFrame = stim.frames.shape[0]
+        self.stim = stim
+        self.wbits = wbits
+        self.S = None
+        self.c50 = np.ascontiguousarray(lgn.c50, f32)
+        self.sharp = np.ascontiguousarray(lgn.sharpness, f32)
+        self.ltr = np.zeros(lgn.nLGN, f32)
+        self.lnl = np.zeros(lgn.nLGN, f32)
+
+    def spatial(self, SW=None, SC=None):
+        """S [nFrame+1][nMagno]; by default from this oracle's own SW/SC tables."""
+        lgn = self.lgn
+        fr = self.stim.frames
+        nF, _, h, w = fr.shape
+        layers = np.empty((nF + 1, 3, h, w), f32)
+        layers[:nF] = fr
+        for ch in range(3):
+            layers[nF, ch] = self.stim.init_LMS[ch]
+        SW = self.SW if SW is None else np.ascontiguousarray(SW, f32)
+        SC = self.SC if SC is None else np.ascontiguousarray(SC, f32)
+        cone = np.ascontiguousarray(np.asarray(lgn.coneType, np.uint32)[lgn.magno_ids()])
+        S = np.empty((nF + 1, lgn.nMagno), f32)
+        lib().orc_lgn_spatial(lgn.nMagno, lgn.mSample1D ** 2, fp(SW), fp(SC), up(cone), fp(layers), nF + 1,
+                              h, w, self.wbits, fp(S))
+        self.S = S
+        return S
+
+    def convol(self, it: int, S=None, TW=None):
+        S = self.S if S is None else S
+        TW = self.TW if TW is None else TW
+        out = np.empty(self.lgn.nMagno, f32)
+        lib().orc_lgn_convol(C.byref(self.cfg), self.lgn.nMagno, self.nFrame, int(it), fp(TW), fp(S),
+                             fp(self.absk), fp(out))
+        return out
+
+    def nonlinear(self, convol, u, ucount, cap):
+        sInfo = np.zeros(self.lgn.nLGN, f32)
+        fr = np.zeros(self.lgn.nLGN, f32)
+        mism = lib().orc_lgn_nonlinear(C.byref(self.cfg), fp(convol), fp(self.maxConvol), fp(self.c50),
+                                       fp(self.sharp), fp(self.la), fp(self.lb), fp(self.ltr), fp(self.lnl),
+                                       fp(u), ip(ucount), int(cap), fp(sInfo), fp(fr))
+        return sInfo, fr, mism
+
+
+class V1Oracle:
+    def __init__(self, spec, net):
+        self.spec = spec
+        self.cfg = spec.to_struct()
+        c = lambda a, t: np.ascontiguousarray(a, dtype=t)
+        self._keep = [c(net.nLGNperV1, np.uint32), c(net.lgnId, np.uint32), c(net.sLGN, f32),
+                      c(net.nNearNB, np.uint32), c(net.nbId, np.uint32), c(net.conMat, f32),
+                      c(net.nVec, np.uint32), c(net.vecID, np.uint32), c(net.conVec, f32),
+                      c(net.delayVec, f32), c(net.tonicDep, f32)]
+        k = self._keep
+        self.h = lib().orc_v1_create(C.byref(self.cfg), net.maxLGN, up(k[0]), up(k[1]), fp(k[2]), net.nnb,
+                                     up(k[3]), up(k[4]), fp(k[5]), up(k[6]), up(k[7]), fp(k[8]), fp(k[9]),
+                                     fp(k[10]))
+
+    def put(self, name, arr):
+        lib().orc_v1_put(self.h, ST[name], fp(np.ascontiguousarray(arr, f32)))
+
+    def get(self, name):
+        s = self.spec
+        n = s.nV1
+        size = dict(gFF=s.ngFF * n, hFF=s.ngFF * n, gE=s.ngE * n, hE=s.ngE * n, gI=s.ngI * n,
+                    hI=s.ngI * n).get(name, n)
+        out = np.empty(size, f32)
+        lib().orc_v1_get(self.h, ST[name], fp(out))
+        return out
+
+    def set_state(self, init):
+        for name in ("v", "gFF", "hFF", "gE", "hE", "gI", "hI"):
+            self.put(name, getattr(init, name))
+        if init.w is not None:
+            self.put("w", init.w)
+
+    def step(self, lgn_sInfo, noise=None, ff=None, near=None, cap=0):
+        L = lib()
+        nerr = L.orc_v1_compute_v(self.h, fp(np.ascontiguousarray(lgn_sInfo, f32)),
+                                  fp(None if noise is None else np.ascontiguousarray(noise, f32)),
+                                  fp(None if ff is None else np.ascontiguousarray(ff, f32)), int(cap))
+        L.orc_v1_deliver_near(self.h, fp(None if near is None else np.ascontiguousarray(near, f32)), int(cap))
+        L.orc_v1_deliver_far(self.h)
+        return nerr
+
+    def close(self):
+        if self.h:
+            lib().orc_v1_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

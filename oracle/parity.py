@@ -1,0 +1,200 @@
+"""GPU-vs-oracle parity runs (test infrastructure).
+
+`run_parity` steps one synthetic workload on the GPU with every random draw recorded, then
+replays the same steps with the CPU oracle in the reference's order, feeding it the recorded
+draws, and returns both sides' per-step records for comparison.
+
+Two modes for the LGN tables: `own_tables=True` makes the oracle use its own restated
+store_PM tables and its own emulation of the texture sampling (an end-to-end check, where the
+9-bit texture weights can move a few LGN spikes); `own_tables=False` feeds it the GPU's
+tables after they were compared separately, so that the V1 dynamics can be compared spike for
+spike.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import LgnOracle, V1Oracle
+
+f32 = np.float32
+
+
+def record_layout(spec):
+    """Offsets of the fields inside one rawData record."""
+    n = spec.nV1
+    h = 1 if spec.hWrite else 0
+    o = {"sInfo": 0, "dep": n}
+    off = 2 * n
+    if spec.iModel == 1:
+        o["w"] = off
+        off += n
+    o["v"] = off
+    off += n
+    o["gFF"] = off
+    off += spec.ngFF * n
+    if h:
+        o["hFF"] = off
+        off += spec.ngFF * n
+    o["gE"] = off
+    off += spec.ngE * n
+    o["gI"] = off
+    off += spec.ngI * n
+    if h:
+        o["hE"] = off
+        off += spec.ngE * n
+        o["hI"] = off
+        off += spec.ngI * n
+    return o
+
+
+def split_record(spec, rec):
+    o = record_layout(spec)
+    n = spec.nV1
+    sizes = dict(sInfo=n, dep=n, w=n, v=n, gFF=spec.ngFF * n, hFF=spec.ngFF * n, gE=spec.ngE * n,
+                 gI=spec.ngI * n, hE=spec.ngE * n, hI=spec.ngI * n)
+    return {k: rec[..., v:v + sizes[k]] for k, v in o.items()}
+
+
+def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None):
+    from visual_cortex_gb300.model import Simulation
+    from visual_cortex_gb300 import _native as N
+
+    close = sim is None
+    if sim is None:
+        sim = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        gpu_tables = sim.lgn_tables()
+        gpu_S = sim.lgn_spatial()
+        lnl0 = sim.state("lgn_lnl")
+        ltr0 = sim.state("lgn_ltr")
+        sim.set_record(N.REC_RAW | N.REC_LGN_SP | N.REC_LGN_FR, nsteps + 1)
+        sim.set_draw_record(nsteps, cap)
+        sim.run(nsteps)
+        raw, lsp, lfr = sim.fetch_records(0, nsteps, raw=True, lgn_sp=True, lgn_fr=True)
+        U, Uc = sim.fetch_draws(0)
+        noise, _ = sim.fetch_draws(1)
+        ff, _ = sim.fetch_draws(2)
+        near, _ = sim.fetch_draws(3)
+        final = {k: sim.state(k) for k in ("v", "gE", "gI", "gFF", "tBack")}
+        launches = sim.launches()
+    finally:
+        if close:
+            sim.close()
+
+    lo = LgnOracle(wl.lgn, wl.stim)
+    ora_tables = (lo.TW.copy(), lo.SW.copy(), lo.SC.copy(), lo.maxConvol.copy())
+    ora_S = lo.spatial()
+    if not own_tables:
+        TW, SW, SC, mc = gpu_tables
+        lo.TW[:] = TW
+        lo.maxConvol[:] = mc
+        lo.S = np.ascontiguousarray(gpu_S)
+    lo.lnl[:] = lnl0
+    lo.ltr[:] = ltr0
+    vo = V1Oracle(wl.spec, wl.net)
+    vo.set_state(wl.init)
+    nV1 = wl.spec.nV1
+    o_raw = np.zeros_like(raw)
+    o_lsp = np.zeros_like(lsp)
+    o_lfr = np.zeros_like(lfr)
+    lay = record_layout(wl.spec)
+    mism = 0
+    for it in range(nsteps):
+        conv = lo.convol(it)
+        s, fr, m = lo.nonlinear(conv, np.ascontiguousarray(U[it]), np.ascontiguousarray(Uc[it]), cap)
+        mism += m
+        o_lsp[it] = s
+        o_lfr[it] = fr
+        vo.step(s, noise=noise[it], ff=np.ascontiguousarray(ff[it]), near=np.ascontiguousarray(near[it]), cap=cap)
+        r = o_raw[it]
+        r[lay["sInfo"]:lay["sInfo"] + nV1] = vo.get("sInfo")
+        r[lay["dep"]:lay["dep"] + nV1] = vo.get("dep")
+        if "w" in lay:
+            r[lay["w"]:lay["w"] + nV1] = vo.get("w")
+        r[lay["v"]:lay["v"] + nV1] = vo.get("v")
+        for k in ("gFF", "hFF", "gE", "gI", "hE", "hI"):
+            if k in lay:
+                a = vo.get(k)
+                r[lay[k]:lay[k] + a.size] = a
+    o_final = {k: vo.get(k) for k in ("v", "gE", "gI", "gFF", "tBack")}
+    vo.close()
+    return dict(gpu=dict(raw=raw, lsp=lsp, lfr=lfr, tables=gpu_tables, S=gpu_S, final=final),
+                ora=dict(raw=o_raw, lsp=o_lsp, lfr=o_lfr, tables=ora_tables, S=ora_S, final=o_final),
+                draw_count_mismatch=mism, launches=launches)
+
+
+def first_divergence(a_sinfo, b_sinfo):
+    """First step at which the spike rasters (sInfo >= 1) differ, or None."""
+    sa = a_sinfo >= 1
+    sb = b_sinfo >= 1
+    diff = np.nonzero((sa != sb).any(axis=1))[0]
+    return int(diff[0]) if diff.size else None
+
+
+def knife_edge(spec, a_sinfo, b_sinfo, step, eps_mv=1e-3):
+    """True if every raster difference at `step` is a threshold crossing decided by float
+    rounding: on the side that did not spike the membrane sits within eps_mv of vThres."""
+    sa, sb = a_sinfo[step] >= 1, b_sinfo[step] >= 1
+    idx = np.nonzero(sa != sb)[0]
+    vthr = np.asarray(spec.vThres, dtype=np.float64)[spec.type_of(idx % spec.blockSize)]
+    v_other = np.where(sa[idx], b_sinfo[step][idx], a_sinfo[step][idx])
+    return bool(np.all(np.abs(v_other - vthr) < eps_mv))
+
+
+def first_spike_time_divergence(a_v1, b_v1, a_lgn, b_lgn, tol_tsp):
+    """First step at which a V1 or LGN spike present on both sides differs in its time by
+    more than tol_tsp (in units of dt), or the rasters differ; None if never."""
+    n = a_v1.shape[0]
+    for t in range(n):
+        for a, b in ((a_v1[t], b_v1[t]), (a_lgn[t], b_lgn[t])):
+            sa, sb = a >= 1, b >= 1
+            if (sa != sb).any():
+                return t
+            if sa.any() and np.max(np.abs(a[sa] - b[sa])) > tol_tsp:
+                return t
+    return None
+
+
+def compare(res, spec, tol_tsp=1e-3):
+    """Summary numbers of a parity run (all assertions are left to the caller).
+
+    Traces are compared up to the first spike-time divergence: the first step at which a
+    spike (V1 or LGN) present in both runs differs in time by more than tol_tsp of a step,
+    or a spike is present in only one run.
+
+    Membrane traces are compared relative to |v|; conductance traces relative to the
+    largest value of that conductance over the population at the same step (a conductance
+    that is decaying towards 0 has no meaningful relative error of its own)."""
+    g, o = res["gpu"], res["ora"]
+    G = split_record(spec, g["raw"])
+    O = split_record(spec, o["raw"])
+    nsteps = g["raw"].shape[0]
+    div = first_divergence(G["sInfo"], O["sInfo"])
+    tdiv = first_spike_time_divergence(G["sInfo"], O["sInfo"], g["lsp"], o["lsp"], tol_tsp)
+    upto = nsteps if tdiv is None else tdiv
+    out = {"first_raster_divergence": div, "first_spike_time_divergence": tdiv, "steps": nsteps,
+           "divergence_is_knife_edge": None if div is None else knife_edge(spec, G["sInfo"], O["sInfo"], div)}
+    full_v = np.abs(G["v"].astype(np.float64) - O["v"]) / np.maximum(np.abs(O["v"]), 1.0)
+    out["max_rel_v_to_raster_divergence"] = float(full_v[:nsteps if div is None else div].max()) if (div is None or div) else 0.0
+    for k in ("v", "gE", "gI", "gFF"):
+        a, b = G[k][:upto].astype(np.float64), O[k][:upto].astype(np.float64)
+        if not upto:
+            out[f"max_rel_{k}"] = 0.0
+            continue
+        if k == "v":
+            scale = np.maximum(np.abs(b), 1.0)
+        else:
+            scale = np.maximum(np.abs(b).max(axis=1, keepdims=True), 1e-12)
+        out[f"max_rel_{k}"] = float(np.max(np.abs(a - b) / scale))
+    both = (G["sInfo"][:upto] >= 1) & (O["sInfo"][:upto] >= 1)
+    out["v1_tsp_maxdiff"] = float(np.max(np.abs(G["sInfo"][:upto][both] - O["sInfo"][:upto][both]))) if both.any() else 0.0
+    lg = g["lsp"] >= 1
+    lo_ = o["lsp"] >= 1
+    out["lgn_spike_mismatch"] = int((lg != lo_).sum())
+    out["lgn_spikes"] = int(lg.sum())
+    out["v1_spikes_gpu"] = int((G["sInfo"] >= 1).sum())
+    out["v1_spikes_ora"] = int((O["sInfo"] >= 1).sum())
+    both = lg & lo_
+    out["lgn_tsp_maxdiff"] = float(np.max(np.abs(g["lsp"][both] - o["lsp"][both]))) if both.any() else 0.0
+    out["lgn_fr_maxrel"] = float(np.max(np.abs(g["lfr"] - o["lfr"]) / np.maximum(np.abs(o["lfr"]), 1e-3)))
+    return out

@@ -1,0 +1,768 @@
+/*
+ * pv1_oracle.c -- CPU restatement of the patchV1 simulation hot path.
+ *
+ * TEST INFRASTRUCTURE: this file is the checker for the GPU library.  Only the tests, the
+ * smoke check and the CPU-baseline leg of the benchmark load it; the product path never
+ * does.  It follows the reference's own structure (one pass per kernel, per-synapse delay
+ * rings for the far synapses, the sample-by-sample temporal convolution) rather than the GPU
+ * design, so that agreement between the two is evidence about the algorithm and not about a
+ * shared implementation.
+ *
+ * Reference files followed (paths relative to the reference project root):
+ *   ConductanceShape               src/condShape.h:13-41
+ *   AdEx / get_a / get_b           src/coredynamics.cuh:15-118
+ *   compute_V_..._fast             src/coredynamics.cu:1235-2059
+ *   recal_G_mat_nd_fast            src/coredynamics.cu:2609-2922
+ *   recal_G_vec + fill_fSpikeTrain src/coredynamics.cu:181-372, src/stats.cu:114-126
+ *   sum_G                          src/coredynamics.cu:2312-2349
+ *   store_PM (magno) / TW          src/discrete_input_convol.cu:230-305, 427-744
+ *   LGN_convol_magno               src/discrete_input_convol.cu:1342-1585
+ *   LGN_nonlinear / get_spike      src/discrete_input_convol.cu:1587-1821
+ *   transform / hStatic_nonlinear  src/LGN_props.cuh:94-100, src/LGN_props.h:143-170
+ *   texture sampling               src/patch.h:95-109 (bilinear, normalised, border)
+ *
+ * Random numbers: the reference draws from cuRAND on the device.  This file does not
+ * re-derive cuRAND; every draw it needs is passed in (recorded by the GPU run under test).
+ * Build with -ffp-contract=off so the float arithmetic is the same on every host.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/patchv1_gb300.h"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef struct {
+    float rise[PV1_MAX_NG], decay[PV1_MAX_NG], dod[PV1_MAX_NG];
+} ocond;
+
+static ocond ocond_make(const float *rt, const float *dc, int n) {
+    ocond c;
+    memset(&c, 0, sizeof(c));
+    for (int i = 0; i < n; i++) {
+        c.rise[i] = rt[i];
+        c.decay[i] = dc[i];
+        c.dod[i] = rt[i] / (dc[i] - rt[i]);
+    }
+    return c;
+}
+
+static inline void ocond_input(const ocond *c, float *g, float *h, float f, float dt, int ig) {
+    float etr = expf(-dt / c->rise[ig]);
+    *g += f * c->dod[ig] * (expf(-dt / c->decay[ig]) - etr);
+    *h += f * etr;
+}
+
+static inline void ocond_decay(const ocond *c, float *g, float *h, float dt, int ig) {
+    float etr = expf(-dt / c->rise[ig]);
+    float etd = expf(-dt / c->decay[ig]);
+    *g = *g * etd + *h * c->dod[ig] * (etd - etr);
+    *h *= etr;
+}
+
+int orc_version(void) { return 1; }
+
+/* ================================================================== LGN ============ */
+
+static float gauss2(float x, float y, float rx, float ry) {
+    return expf(-x * x / (rx * rx) - y * y / (ry * ry));
+}
+
+static float temporal_kernel(float tau, float tauR, float tauD, float nR, float nD, float ratio,
+                             float lfac1, float lfac2) {
+    float tau1 = tau / tauR, tau2 = tau / tauD;
+    float A1 = (nR - 1) * logf(tau1);
+    float A2 = (nD - 1) * logf(tau2);
+    float tpR = expf(A1 - tau1 - lfac1) / tauR;
+    float tpD = expf(A2 - tau2 - lfac2) / tauD;
+    return tpR - ratio * tpD;
+}
+
+/* store_PM for magno cells: TW [nMagno][nKS], SW [nMagno][nSample], SC [2][nMagno][nSample],
+ * maxConvol [nLGN], absk [nMagno]; logistic la/lb [nLGN]. */
+int orc_lgn_setup(const pv1_lgn_config *c, const pv1_lgn_params *p, float *TW, float *SW,
+                  float *SC, float *maxConvol, float *absk, float *la, float *lb) {
+    const int nLGN = (int)c->nLGN;
+    const int nMagno = (int)(c->nMagno_I + c->nMagno_C);
+    const int n1 = (int)c->mSample1D, nS = n1 * n1, nKS = (int)c->nKernelSample;
+    for (int i = 0; i < nLGN; i++) {
+        const float e_kc50 = expf(p->sharpness[i] * p->c50[i]);
+        const float e_kc50_k = expf(p->sharpness[i] * p->c50[i] - p->sharpness[i]);
+        la[i] = (1 - p->spont[i]) * (1 + e_kc50) * (1 + e_kc50_k) / (e_kc50 - e_kc50_k);
+        lb[i] = 1 - la[i] / (1 + e_kc50_k);
+    }
+    float *cw = (float *)malloc(sizeof(float) * nS), *sw = (float *)malloc(sizeof(float) * nS);
+    for (int m = 0; m < nMagno; m++) {
+        int id = (int)c->nParvo_I + m;
+        if (m >= (int)c->nMagno_I) id += (int)c->nParvo_C;
+        /* temporal weights, time reversed and L1 normalised */
+        const float lfac1 = lgammaf(p->nR[id]), lfac2 = lgammaf(p->nD[id]);
+        const float t0 = c->kernelSampleT0 - p->delay[id];
+        float tot = 0.f;
+        for (int j = 0; j < nKS; j++) {
+            int twid = nKS - 1 - j;
+            float t = twid * c->kernelSampleDt + t0;
+            float tw = t < 0 ? 0.0f
+                             : temporal_kernel(t, p->tauR[id], p->tauD[id], p->nR[id], p->nD[id],
+                                               p->ratio[id], lfac1, lfac2);
+            TW[(size_t)m * nKS + j] = tw;
+            tot += fabsf(tw);
+        }
+        for (int j = 0; j < nKS; j++) TW[(size_t)m * nKS + j] /= tot;
+        /* DoG weights */
+        const int sid = nLGN + id;
+        const float ox = p->ecc[sid] * cosf(p->polar[sid]) - p->ecc[id] * cosf(p->polar[id]);
+        const float oy = p->ecc[sid] * sinf(p->polar[sid]) - p->ecc[id] * sinf(p->polar[id]);
+        float d_orient = p->orient[id] - p->orient[sid];
+        if (fabsf(d_orient) > (float)(M_PI / 2)) d_orient -= copysignf((float)M_PI, d_orient);
+        const float rc = cosf(d_orient), rsn = sinf(d_orient);
+        const float rs = p->rw[sid] > p->rh[sid] ? p->rw[sid] : p->rh[sid];
+        const float span = c->nsig * rs + sqrtf(ox * ox + oy * oy);
+        const float ds = 2 * span / n1;
+        float csum = 0.f, ssum = 0.f;
+        for (int s = 0; s < nS; s++) {
+            const int tx = s % n1, ty = s / n1;
+            const float cx = (tx + 0.5f) * ds - span, cy = (ty + 0.5f) * ds - span;
+            const float ttx = cx - ox, tty = cy - oy;
+            const float sx = ttx * rc - tty * rsn, sy = ttx * rsn + tty * rc;
+            cw[s] = gauss2(cx, cy, p->rw[id], p->rh[id]);
+            sw[s] = gauss2(sx, sy, p->rw[sid], p->rh[sid]);
+            csum += cw[s];
+            ssum += sw[s];
+        }
+        const float k = p->k[id];
+        float wsum = 0.f;
+        for (int s = 0; s < nS; s++) {
+            float w = copysignf(cw[s] / csum, k) - copysignf(sw[s] / ssum, k);
+            SW[(size_t)m * nS + s] = w;
+            wsum += fabsf(w);
+        }
+        for (int s = 0; s < nS; s++) SW[(size_t)m * nS + s] /= wsum;
+        maxConvol[id] = fabsf(k) * wsum;
+        absk[m] = fabsf(k);
+        /* texture coordinates (flat retina) */
+        const int left = m < (int)c->nMagno_I;
+        const float x0 = left ? c->L_x0 : c->R_x0, y0 = left ? c->L_y0 : c->R_y0;
+        const float coso = cosf(p->orient[id]), sino = sinf(p->orient[id]);
+        for (int s = 0; s < nS; s++) {
+            const int tx = s % n1, ty = s / n1;
+            const float cx = (tx + 0.5f) * ds - span, cy = (ty + 0.5f) * ds - span;
+            SC[(size_t)m * nS + s] = x0 + (p->ecc[id] * cosf(p->polar[id]) + cx * coso - cy * sino) * c->normViewDistance;
+            SC[(size_t)nMagno * nS + (size_t)m * nS + s] =
+                y0 + (p->ecc[id] * sinf(p->polar[id]) + cx * sino + cy * coso) * c->normViewDistance;
+        }
+    }
+    free(cw);
+    free(sw);
+    return 0;
+}
+
+/* Bilinear texture fetch with normalised coordinates and border addressing: the filtering
+ * the CUDA programming guide documents for linear texture filtering, with the fractional
+ * weights held in 9-bit fixed point (8 fractional bits). */
+static float tex_fetch(const float *plane, int w, int h, float x, float y, int wbits) {
+    float xb = x * w - 0.5f, yb = y * h - 0.5f;
+    float fi = floorf(xb), fj = floorf(yb);
+    float a = xb - fi, b = yb - fj;
+    if (wbits > 0) {
+        const float q = (float)(1 << wbits);
+        a = rintf(a * q) / q;
+        b = rintf(b * q) / q;
+    }
+    int i = (int)fi, j = (int)fj;
+    float t00 = (i >= 0 && i < w && j >= 0 && j < h) ? plane[(size_t)j * w + i] : 0.f;
+    float t10 = (i + 1 >= 0 && i + 1 < w && j >= 0 && j < h) ? plane[(size_t)j * w + i + 1] : 0.f;
+    float t01 = (i >= 0 && i < w && j + 1 >= 0 && j + 1 < h) ? plane[(size_t)(j + 1) * w + i] : 0.f;
+    float t11 = (i + 1 >= 0 && i + 1 < w && j + 1 >= 0 && j + 1 < h) ? plane[(size_t)(j + 1) * w + i + 1] : 0.f;
+    return (1 - a) * (1 - b) * t00 + a * (1 - b) * t10 + (1 - a) * b * t01 + a * b * t11;
+}
+
+static float intensity(int cone, const float *L, const float *M, const float *S, int w, int h,
+                       float x, float y, int wbits) {
+    switch (cone) {
+        case 0: return tex_fetch(L, w, h, x, y, wbits);
+        case 1: return tex_fetch(M, w, h, x, y, wbits);
+        case 2: return tex_fetch(S, w, h, x, y, wbits);
+        case 3: return (tex_fetch(L, w, h, x, y, wbits) + tex_fetch(M, w, h, x, y, wbits)) / 2.0f;
+        case 4:
+            return tex_fetch(L, w, h, x, y, wbits) * 0.45436904f + tex_fetch(M, w, h, x, y, wbits) * 0.47353315f +
+                   tex_fetch(S, w, h, x, y, wbits) * 0.0720978f;
+        default: return 0.f;
+    }
+}
+
+/* Spatial contrast of every (frame, cell): layers [nLayer][3][h][w] (the last layer may be
+ * the initial luminance).  S [nLayer][nMagno]. */
+int orc_lgn_spatial(int nMagno, int nSample, const float *SW, const float *SC,
+                    const uint32_t *coneType, const float *layers, int nLayer, int h, int w,
+                    int wbits, float *S) {
+    const size_t npix = (size_t)w * h;
+#pragma omp parallel for schedule(static)
+    for (int f = 0; f < nLayer; f++) {
+        const float *L = layers + (size_t)f * 3 * npix, *M = L + npix, *Sp = M + npix;
+        for (int m = 0; m < nMagno; m++) {
+            const float *sx = SC + (size_t)m * nSample, *sy = SC + (size_t)nMagno * nSample + (size_t)m * nSample;
+            float sum = 0.f;
+            for (int s = 0; s < nSample; s++) sum += intensity(3, L, M, Sp, w, h, sx[s], sy[s], wbits);
+            const float mean = sum / nSample;
+            float acc = 0.f;
+            for (int s = 0; s < nSample; s++) {
+                float I = intensity((int)coneType[m], L, M, Sp, w, h, sx[s], sy[s], wbits);
+                float cc = mean > 0 ? I / mean - 1.0f : I;
+                if (fabsf(cc) > 1.0f) cc = copysignf(1.0f, cc);
+                acc += SW[(size_t)m * nSample + s] * cc;
+            }
+            S[(size_t)f * nMagno + m] = acc;
+        }
+    }
+    return 0;
+}
+
+/* Temporal convolution of step `it`, sample by sample as LGN_convol_magno walks it:
+ * sample j of the window reads the texture layer tail + ((T0 + j*interval)*denorm +
+ * phase)/ntPerFrame; the layer holds the newest frame with that residue mod maxFrame, or the
+ * initial luminance if no frame was loaded there yet.  convol_out[m] = convol * |k|. */
+int orc_lgn_convol(const pv1_lgn_config *c, int nMagno, int nFrame, long long it, const float *TW,
+                   const float *S, const float *absk, float *convol_out) {
+    const long long num = (it + 1) * (long long)c->denorm;
+    const int currentFrame = (int)((num + c->ntPerFrame - 1) / c->ntPerFrame);
+    const int oldFrameHead = (currentFrame - 1) % (int)c->maxFrame;
+    const int phase = (int)((c->magnoComp + (it + 1) * (long long)c->denorm) % c->ntPerFrame);
+    const int tail = oldFrameHead + (int)c->frameOffset + (phase <= (int)c->magnoComp ? 2 : 1);
+    const int nKS = (int)c->nKernelSample;
+    int *rowOf = (int *)malloc(sizeof(int) * nKS);
+    for (int j = 0; j < nKS; j++) {
+        long long o = (long long)(c->iKernelSampleT0 + (long long)j * c->kernelSampleInterval) * c->denorm + phase;
+        int layer = (int)((tail + o / c->ntPerFrame) % c->maxFrame);
+        /* newest frame F <= currentFrame-1 with F % maxFrame == layer */
+        int Fnew = currentFrame - 1;
+        int back = ((Fnew % (int)c->maxFrame) - layer + (int)c->maxFrame) % (int)c->maxFrame;
+        int F = Fnew - back;
+        rowOf[j] = F < 0 ? nFrame : F % nFrame;
+    }
+    for (int m = 0; m < nMagno; m++) {
+        float conv = 0.f;
+        for (int j = 0; j < nKS; j++) conv += S[(size_t)rowOf[j] * nMagno + m] * TW[(size_t)m * nKS + j];
+        convol_out[m] = conv * absk[m];
+    }
+    free(rowOf);
+    return 0;
+}
+
+/* LGN_nonlinear + get_spike for every magno cell of one step.  u: recorded uniforms
+ * [nLGN][cap] of this step, ucount [nLGN].  Returns the number of cells whose draw count
+ * disagrees with the record (0 when the CPU and GPU took the same branches). */
+int orc_lgn_nonlinear(const pv1_lgn_config *c, const float *convol, const float *maxConvol,
+                      const float *c50, const float *sharp, const float *la, const float *lb,
+                      float *ltr, float *lnl, const float *u, const int32_t *ucount, int cap,
+                      float *sInfo_out, float *fr_out) {
+    const int nMagno = (int)(c->nMagno_I + c->nMagno_C);
+    int mismatch = 0;
+    for (int m = 0; m < nMagno; m++) {
+        int id = (int)c->nParvo_I + m;
+        if (m >= (int)c->nMagno_I) id += (int)c->nParvo_C;
+        const float mx = maxConvol[id];
+        float current = convol[m] * c->convolRatio;
+        if (current < 0) current = 0;
+        float X = (float)(1.0 / (double)(1 + expf(sharp[id] * (c50[id] - current / mx))));
+        float fr = c->frRatio * mx * (la[id] * X + lb[id]);
+        const float dt = c->dt;
+        const float rate = fr / 1000.0f;
+        const float rT = dt * rate;
+        float next_rT = lnl[id] - ltr[id];
+        unsigned nsp = 0;
+        float tsp = 0.f;
+        if (next_rT > rT) {
+            ltr[id] += rT;
+        } else {
+            float old_rT = 0.f;
+            do {
+                float rnd = (int)nsp < cap ? u[(size_t)id * cap + nsp] : 0.5f;
+                lnl[id] = fmaxf(-logf(rnd), 0.0f * rate);
+                old_rT = next_rT;
+                next_rT += lnl[id];
+                nsp++;
+            } while (next_rT <= rT);
+            ltr[id] = rT - old_rT;
+            tsp = old_rT / (rate * nsp);
+        }
+        if (ucount && (int)nsp != ucount[id]) mismatch++;
+        sInfo_out[id] = nsp + tsp / dt;
+        if (fr_out) fr_out[id] = fr;
+    }
+    return mismatch;
+}
+
+/* ================================================================== V1 ============= */
+
+typedef struct orc_v1 {
+    pv1_v1_config c;
+    int nV1, nE, nI, bs, nblock;
+    ocond cFF, cE, cI;
+    float *v, *w, *tBack, *dep, *gFF, *hFF, *gE, *hE, *gI, *hI, *tonic, *lastNoise, *sInfo;
+    /* LGN synapses */
+    int maxLGN;
+    uint32_t *nLGN, *lgnId;
+    float *sLGN;
+    /* near */
+    int nnb;
+    uint32_t *nNearNB, *nbId;
+    const float *conMat; /* borrowed */
+    /* far: per-(post, j) spike rings (fSpikeTrain) */
+    size_t nFar;
+    uint32_t *nVec, *vecID;
+    size_t *vecOff;
+    float *conVec, *delayVec;
+    float *ring;
+    size_t *ringOff;
+    uint32_t *depth, *slot;
+    int anyFar;
+} orc_v1;
+
+static int otype(const orc_v1 *o, int local) {
+    for (uint32_t j = 0; j < o->c.nType; j++)
+        if ((uint32_t)local < o->c.typeAcc[j]) return (int)j;
+    return (int)o->c.nType - 1;
+}
+
+void orc_v1_destroy(orc_v1 *o);
+
+orc_v1 *orc_v1_create(const pv1_v1_config *cfg, uint32_t maxLGN, const uint32_t *nLGN,
+                      const uint32_t *lgnId, const float *sLGN, uint32_t nnb,
+                      const uint32_t *nNearNB, const uint32_t *nbId, const float *conMat,
+                      const uint32_t *nVec, const uint32_t *vecID, const float *conVec,
+                      const float *delayVec, const float *tonicDep) {
+    orc_v1 *o = (orc_v1 *)calloc(1, sizeof(orc_v1));
+    o->c = *cfg;
+    o->bs = (int)cfg->blockSize;
+    o->nblock = (int)cfg->nblock;
+    o->nV1 = o->bs * o->nblock;
+    o->nE = (int)cfg->typeAcc[cfg->nTypeE - 1];
+    o->nI = o->bs - o->nE;
+    o->cFF = ocond_make(cfg->riseFF, cfg->decayFF, (int)cfg->ngFF);
+    o->cE = ocond_make(cfg->riseE, cfg->decayE, (int)cfg->ngE);
+    o->cI = ocond_make(cfg->riseI, cfg->decayI, (int)cfg->ngI);
+    const size_t n = (size_t)o->nV1;
+#define OALLOC(f, cnt) o->f = (float *)calloc((cnt), sizeof(float))
+    OALLOC(v, n); OALLOC(w, n); OALLOC(tBack, n); OALLOC(dep, n);
+    OALLOC(gFF, cfg->ngFF * n); OALLOC(hFF, cfg->ngFF * n);
+    OALLOC(gE, cfg->ngE * n); OALLOC(hE, cfg->ngE * n);
+    OALLOC(gI, cfg->ngI * n); OALLOC(hI, cfg->ngI * n);
+    OALLOC(tonic, n); OALLOC(lastNoise, n); OALLOC(sInfo, n);
+#undef OALLOC
+    memcpy(o->tonic, tonicDep, n * sizeof(float));
+    o->maxLGN = (int)maxLGN;
+    o->nLGN = (uint32_t *)malloc(n * sizeof(uint32_t));
+    memcpy(o->nLGN, nLGN, n * sizeof(uint32_t));
+    o->lgnId = (uint32_t *)malloc((size_t)maxLGN * n * sizeof(uint32_t) + 4);
+    memcpy(o->lgnId, lgnId, (size_t)maxLGN * n * sizeof(uint32_t));
+    o->sLGN = (float *)malloc((size_t)maxLGN * n * sizeof(float) + 4);
+    memcpy(o->sLGN, sLGN, (size_t)maxLGN * n * sizeof(float));
+    o->nnb = (int)nnb;
+    o->nNearNB = (uint32_t *)malloc(o->nblock * sizeof(uint32_t));
+    memcpy(o->nNearNB, nNearNB, o->nblock * sizeof(uint32_t));
+    o->nbId = (uint32_t *)malloc((size_t)o->nblock * nnb * sizeof(uint32_t));
+    memcpy(o->nbId, nbId, (size_t)o->nblock * nnb * sizeof(uint32_t));
+    o->conMat = conMat;
+    /* far rings: depth = ceil(delay/speed/dt) + 1, initialised to -1 (src/patch.cu:3838-3864) */
+    o->nVec = (uint32_t *)malloc(n * sizeof(uint32_t));
+    memcpy(o->nVec, nVec, n * sizeof(uint32_t));
+    o->vecOff = (size_t *)malloc((n + 1) * sizeof(size_t));
+    o->vecOff[0] = 0;
+    for (size_t i = 0; i < n; i++) o->vecOff[i + 1] = o->vecOff[i] + nVec[i];
+    o->nFar = o->vecOff[n];
+    o->vecID = (uint32_t *)malloc(o->nFar * sizeof(uint32_t) + 4);
+    o->conVec = (float *)malloc(o->nFar * sizeof(float) + 4);
+    o->delayVec = (float *)malloc(o->nFar * sizeof(float) + 4);
+    if (o->nFar) {
+        memcpy(o->vecID, vecID, o->nFar * sizeof(uint32_t));
+        memcpy(o->conVec, conVec, o->nFar * sizeof(float));
+        memcpy(o->delayVec, delayVec, o->nFar * sizeof(float));
+    }
+    o->depth = (uint32_t *)malloc(o->nFar * sizeof(uint32_t) + 4);
+    o->slot = (uint32_t *)calloc(o->nFar + 1, sizeof(uint32_t));
+    o->ringOff = (size_t *)malloc((o->nFar + 1) * sizeof(size_t));
+    o->ringOff[0] = 0;
+    for (size_t e = 0; e < o->nFar; e++) {
+        o->depth[e] = (uint32_t)ceilf((o->delayVec[e] / cfg->speedOfThought) / cfg->dt) + 1;
+        o->ringOff[e + 1] = o->ringOff[e] + o->depth[e];
+    }
+    o->ring = (float *)malloc(o->ringOff[o->nFar] * sizeof(float) + 4);
+    for (size_t q = 0; q < o->ringOff[o->nFar]; q++) o->ring[q] = -1.0f;
+    o->anyFar = o->nFar > 0;
+    return o;
+}
+
+void orc_v1_destroy(orc_v1 *o) {
+    if (!o) return;
+    free(o->v); free(o->w); free(o->tBack); free(o->dep); free(o->gFF); free(o->hFF);
+    free(o->gE); free(o->hE); free(o->gI); free(o->hI); free(o->tonic); free(o->lastNoise);
+    free(o->sInfo); free(o->nLGN); free(o->lgnId); free(o->sLGN); free(o->nNearNB);
+    free(o->nbId); free(o->nVec); free(o->vecOff); free(o->vecID); free(o->conVec);
+    free(o->delayVec); free(o->ring); free(o->ringOff); free(o->depth); free(o->slot);
+    free(o);
+}
+
+/* which: same ids as PV1_ST_*. */
+static float *oarr(orc_v1 *o, int which, size_t *cnt) {
+    const size_t n = (size_t)o->nV1;
+    *cnt = n;
+    switch (which) {
+        case PV1_ST_V: return o->v;
+        case PV1_ST_W: return o->w;
+        case PV1_ST_TBACK: return o->tBack;
+        case PV1_ST_DEP: return o->dep;
+        case PV1_ST_GFF: *cnt = o->c.ngFF * n; return o->gFF;
+        case PV1_ST_HFF: *cnt = o->c.ngFF * n; return o->hFF;
+        case PV1_ST_GE: *cnt = o->c.ngE * n; return o->gE;
+        case PV1_ST_HE: *cnt = o->c.ngE * n; return o->hE;
+        case PV1_ST_GI: *cnt = o->c.ngI * n; return o->gI;
+        case PV1_ST_HI: *cnt = o->c.ngI * n; return o->hI;
+        case PV1_ST_SINFO: return o->sInfo;
+        default: return NULL;
+    }
+}
+
+int orc_v1_get(orc_v1 *o, int which, float *out) {
+    size_t cnt;
+    float *a = oarr(o, which, &cnt);
+    if (!a) return -1;
+    memcpy(out, a, cnt * sizeof(float));
+    return 0;
+}
+
+int orc_v1_put(orc_v1 *o, int which, const float *in) {
+    size_t cnt;
+    float *a = oarr(o, which, &cnt);
+    if (!a) return -1;
+    memcpy(a, in, cnt * sizeof(float));
+    return 0;
+}
+
+/* compute_V_collect_spike_learnFF_fast for every neuron (learning off, no gap junctions).
+ * noise: normals [nV1] of this step (NULL if no noise); ff: normals [nV1][cap] for the
+ * feed-forward failure draws.  Writes sInfo (the step's spike word). */
+int orc_v1_compute_v(orc_v1 *o, const float *lgnSInfo, const float *noise, const float *ff, int cap) {
+    const pv1_v1_config *c = &o->c;
+    const int nV1 = o->nV1;
+    const float dt = c->dt;
+    int nerr = 0;
+#pragma omp parallel for schedule(static) reduction(+ : nerr)
+    for (int i = 0; i < nV1; i++) {
+        const int local = i % o->bs;
+        const int it = otype(o, local);
+        const float vR = c->vR[it], vThres = c->vThres[it], gL = c->gL[it], Cm = c->C[it];
+        const float tRef = c->tRef[it], vT = c->vT[it], deltaT = c->deltaT[it];
+        const float tau_w = c->tau_w[it], aa = c->a[it], bb = c->b[it];
+        const float tonic = o->tonic[i];
+        float v0 = o->v[i];
+        float w0 = c->iModel == 1 ? o->w[i] : 0.0f;
+        float tBack = o->tBack[i];
+        float depC;
+        {
+            float targetV = c->vL + (vT - c->vL) * tonic;
+            if (targetV > vT) depC = (gL + aa) * (targetV - c->vL) - gL * deltaT;
+            else depC = (gL + aa) * (targetV - c->vL) - gL * deltaT * expf((targetV - vT) / deltaT);
+        }
+        float noise0 = c->tau_noise > 0 ? o->lastNoise[i] : 0.f;
+        float ge[PV1_MAX_NG], he[PV1_MAX_NG], gi[PV1_MAX_NG], hi[PV1_MAX_NG];
+        float gE_t1 = 0.0f, gI_t1 = 0.0f;
+        for (uint32_t ig = 0; ig < c->ngE; ig++) {
+            float g = o->gE[ig * nV1 + i], h = o->hE[ig * nV1 + i];
+            ge[ig] = g;
+            he[ig] = h;
+            ocond_decay(&o->cE, &g, &h, dt, (int)ig);
+            o->gE[ig * nV1 + i] = g;
+            o->hE[ig * nV1 + i] = h;
+            gE_t1 += g;
+        }
+        for (uint32_t ig = 0; ig < c->ngI; ig++) {
+            float g = o->gI[ig * nV1 + i], h = o->hI[ig * nV1 + i];
+            gi[ig] = g;
+            hi[ig] = h;
+            ocond_decay(&o->cI, &g, &h, dt, (int)ig);
+            o->gI[ig * nV1 + i] = g;
+            o->hI[ig * nV1 + i] = h;
+            gI_t1 += g;
+        }
+        float g0[PV1_MAX_NG], h0[PV1_MAX_NG], g1[PV1_MAX_NG], h1[PV1_MAX_NG];
+        for (uint32_t ig = 0; ig < c->ngFF; ig++) {
+            g1[ig] = o->gFF[ig * nV1 + i];
+            h1[ig] = o->hFF[ig * nV1 + i];
+            g0[ig] = g1[ig];
+            h0[ig] = h1[ig];
+            ocond_decay(&o->cFF, &g1[ig], &h1[ig], dt, (int)ig);
+        }
+        const float noiseRatio = c->noiseOnTonic ? tonic : 1.0f;
+        float noise1 = sqrtf(2 * c->noisyDep[it] * (vT - vR) * noiseRatio * dt);
+        const float pf = c->synFailFF[it], nSyn = c->synPerConFF[it];
+        if (noise1 > 0) {
+            noise1 *= noise ? noise[i] : 0.f;
+            if (c->tau_noise > 0) {
+                noise1 /= c->tau_noise;
+                float hk1 = -noise0 / c->tau_noise;
+                float hk2 = -(noise0 + dt * hk1 + noise1) / c->tau_noise;
+                noise1 += noise0 + dt * (hk1 + hk2) / 2;
+                o->lastNoise[i] = noise1;
+            }
+        }
+        const int backingUp = tBack < dt && tBack > 0;
+        o->dep[i] = depC + noise1;
+        if (backingUp)
+            for (uint32_t ig = 0; ig < c->ngFF; ig++) ocond_decay(&o->cFF, &g0[ig], &h0[ig], tBack, (int)ig);
+        int nff = 0;
+        for (uint32_t q = 0; q < o->nLGN[i]; q++) {
+            const size_t lid = (size_t)q * nV1 + i;
+            float f = o->sLGN[lid];
+            const float sFF = lgnSInfo[o->lgnId[lid]];
+            const unsigned nspFF = (unsigned)floorf(sFF);
+            if (nspFF > 0) {
+                const float tspFF = (sFF - nspFF) * dt;
+                if (pf > 0) {
+                    const float nstd = sqrtf(pf * (1 - pf) / nSyn);
+                    const float rnd = (ff && nff < cap) ? ff[(size_t)i * cap + nff] : 0.f;
+                    nff++;
+                    f *= 1 - pf + nstd * rnd;
+                }
+                if (f > 0) {
+                    float ddt = backingUp ? tBack - tspFF : 0.f;
+                    for (uint32_t ig = 0; ig < c->ngFF; ig++) {
+                        const float str = f * c->pFF[it * c->ngFF + ig];
+                        if (backingUp && ddt > 0) ocond_input(&o->cFF, &g0[ig], &h0[ig], str * nspFF, ddt, (int)ig);
+                        ocond_input(&o->cFF, &g1[ig], &h1[ig], str * nspFF, dt - tspFF, (int)ig);
+                    }
+                }
+            }
+        }
+        float gE_t0 = 0.0f;
+        for (uint32_t ig = 0; ig < c->ngFF; ig++) {
+            gE_t0 += g0[ig];
+            gE_t1 += g1[ig];
+            o->gFF[ig * nV1 + i] = g1[ig];
+            o->hFF[ig * nV1 + i] = h1[ig];
+        }
+        for (uint32_t ig = 0; ig < c->ngE; ig++) {
+            if (backingUp) ocond_decay(&o->cE, &ge[ig], &he[ig], tBack, (int)ig);
+            gE_t0 += ge[ig];
+        }
+        float gI_t0 = 0.0f;
+        for (uint32_t ig = 0; ig < c->ngI; ig++) {
+            if (backingUp) ocond_decay(&o->cI, &gi[ig], &hi[ig], tBack, (int)ig);
+            gI_t0 += gi[ig];
+        }
+        /* AdEx: set_p0/set_p1, rk2_vFixedBefore, rk2, compute_spike_time, reset, rk2_vFixedAfter */
+        float v = v0, w = w0, tsp = 0.f;
+        int spiked = 0;
+        if (tBack < dt) {
+            const float a0 = gE_t0 + gI_t0 + gL, b0 = gE_t0 * c->vE + gI_t0 * c->vI + gL * c->vL + depC;
+            const float a1 = gE_t1 + gI_t1 + gL, b1 = gE_t1 * c->vE + gI_t1 * c->vI + gL * c->vL + depC;
+            const float new_dt = dt - tBack;
+            if (backingUp) {
+                float A = aa * (v0 - c->vL);
+                w0 = (w0 - A) * expf(-tBack / tau_w) + A;
+            }
+            float n0, n1;
+            if (c->tau_noise > 0) { n0 = noise0; n1 = noise1; }
+            else { noise1 /= dt; n0 = noise1; n1 = noise1; }
+            const float dTgL = deltaT * gL;
+            const float fk1 = (-a0 * v0 + b0 + dTgL * expf((v0 - vT) / deltaT) - w0) / Cm + n0;
+            const float gk1 = (aa * (v0 - c->vL) - w0) / tau_w;
+            const float v1 = v0 + new_dt * fk1;
+            const float w1 = w0 + new_dt * gk1;
+            const float fk2 = (-a1 * v1 + b1 + dTgL * expf((v1 - vT) / deltaT) - w1) / Cm + n1;
+            const float gk2 = (aa * (v1 - c->vL) - w1) / tau_w;
+            w = w0 + new_dt * (gk1 + gk2) / 2;
+            v = v0 + new_dt * (fk1 + fk2) / 2;
+            if (v > vThres) {
+                const float ratio = (vThres - v0) / (v - v0);
+                tsp = tBack + ratio * new_dt;
+                w0 += ratio * (w - w0) + bb;
+                if (!(tsp >= 0)) nerr++;
+                spiked = 1;
+                tBack = tsp + tRef;
+                v = vR;
+            } else if (tBack > 0) {
+                tBack = 0;
+            }
+        }
+        if (tBack >= dt) {
+            v = vR;
+            const float A = aa * (v - c->vL);
+            w = (w0 - A) * expf(-(dt - tsp) / tau_w) + A;
+            tBack -= dt;
+        }
+        o->sInfo[i] = spiked ? 1.0f + tsp / dt : v;
+        o->v[i] = v;
+        if (c->iModel == 1) o->w[i] = w;
+        o->tBack[i] = tBack;
+    }
+    return nerr;
+}
+
+/* recal_G_mat_nd_fast: near-neighbour delivery of this step's spikes.  Spikers of a block
+ * are taken in ascending neuron order (E before I).  near: normals [nV1][cap] for the
+ * failure draws (consumed only when some failure rate > 0). */
+int orc_v1_deliver_near(orc_v1 *o, const float *near, int cap) {
+    const pv1_v1_config *c = &o->c;
+    const int nV1 = o->nV1, bs = o->bs;
+    const float dt = c->dt;
+    int condRng = 0;
+    for (uint32_t q = 0; q < c->nType * c->nType; q++) if (c->synFail[q] > 0) condRng = 1;
+    for (uint32_t q = 0; q < c->nType; q++) if (c->synFailFF[q] > 0) condRng = 1;
+    /* unit conductances of every spiker (output_g/h of compute_V) */
+    float *og = (float *)calloc((size_t)nV1 * PV1_MAX_NG, sizeof(float));
+    float *oh = (float *)calloc((size_t)nV1 * PV1_MAX_NG, sizeof(float));
+    for (int i = 0; i < nV1; i++) {
+        const float sI = o->sInfo[i];
+        if (sI >= 1) {
+            const float nsp = floorf(sI), tsp = (sI - nsp) * dt;
+            const int isE = (i % bs) < o->nE;
+            const int ng = isE ? (int)c->ngE : (int)c->ngI;
+            for (int ig = 0; ig < ng; ig++) {
+                float g = 0.f, h = 0.f;
+                ocond_input(isE ? &o->cE : &o->cI, &g, &h, nsp, dt - tsp, ig);
+                og[(size_t)i * PV1_MAX_NG + ig] = g;
+                oh[(size_t)i * PV1_MAX_NG + ig] = h;
+            }
+        }
+    }
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nV1; i++) {
+        const int b = i / bs, local = i % bs;
+        const int it = otype(o, local);
+        float lgE[PV1_MAX_NG] = {0, 0}, lhE[PV1_MAX_NG] = {0, 0}, lgI[PV1_MAX_NG] = {0, 0}, lhI[PV1_MAX_NG] = {0, 0};
+        int ndraw = 0;
+        for (uint32_t ib = 0; ib < o->nNearNB[b]; ib++) {
+            const int nb = (int)o->nbId[(size_t)b * o->nnb + ib];
+            const float *colbase = o->conMat + ((size_t)(b * o->nnb + ib) * bs) * bs + local;
+            for (int pass = 0; pass < 2; pass++) {
+                int rank = 0;
+                const int j0 = pass == 0 ? 0 : o->nE, j1 = pass == 0 ? o->nE : bs;
+                for (int j = j0; j < j1; j++) {
+                    const int pre = nb * bs + j;
+                    if (!(o->sInfo[pre] >= 1)) continue;
+                    float strength = colbase[(size_t)j * bs];
+                    if (strength > 0) {
+                        if (condRng) {
+                            int jtype = pass == 0 ? 0 : (int)c->nTypeE;
+                            const int ja = pass == 0 ? 0 : (int)c->nTypeE, jb = pass == 0 ? (int)c->nTypeE : (int)c->nType;
+                            for (int jj = ja; jj < jb; jj++)
+                                if ((uint32_t)rank < c->typeAcc[jj]) { jtype = jj; break; }
+                            const int idx = jtype * (int)c->nType + it;
+                            const float lp = c->synFail[idx];
+                            const float nstd = sqrtf(lp * (1 - lp) / c->synPerCon[idx]);
+                            const float rnd = (near && ndraw < cap) ? near[(size_t)i * cap + ndraw] : 0.f;
+                            ndraw++;
+                            strength *= 1 - lp + nstd * rnd;
+                        }
+                        if (strength > 0) {
+                            if (pass == 0) {
+                                for (uint32_t ig = 0; ig < c->ngE; ig++) {
+                                    const float str = strength * c->pE[it * c->ngE + ig];
+                                    lgE[ig] += str * og[(size_t)pre * PV1_MAX_NG + ig];
+                                    lhE[ig] += str * oh[(size_t)pre * PV1_MAX_NG + ig];
+                                }
+                            } else {
+                                for (uint32_t ig = 0; ig < c->ngI; ig++) {
+                                    const float str = strength * c->pI[it * c->ngI + ig];
+                                    lgI[ig] += str * og[(size_t)pre * PV1_MAX_NG + ig];
+                                    lhI[ig] += str * oh[(size_t)pre * PV1_MAX_NG + ig];
+                                }
+                            }
+                        }
+                    }
+                    rank++;
+                }
+            }
+        }
+        for (uint32_t ig = 0; ig < c->ngE; ig++) { o->gE[ig * nV1 + i] += lgE[ig]; o->hE[ig * nV1 + i] += lhE[ig]; }
+        for (uint32_t ig = 0; ig < c->ngI; ig++) { o->gI[ig * nV1 + i] += lgI[ig]; o->hI[ig * nV1 + i] += lhI[ig]; }
+    }
+    free(og);
+    free(oh);
+    return 0;
+}
+
+/* Far delivery: fill_fSpikeTrain, then recal_G_vec + sum_G when some far presynaptic neuron
+ * spiked (sInfo > 1) this step, else only the ring slots advance (src/patch.cu:6596-6648).
+ * noFarDelay = 1 reproduces the reference's empty loop (far input dropped). */
+int orc_v1_deliver_far(orc_v1 *o) {
+    if (!o->anyFar) return 0;
+    const pv1_v1_config *c = &o->c;
+    const int nV1 = o->nV1, bs = o->bs;
+    const float dt = c->dt;
+    int farSpiked = 0;
+    for (int i = 0; i < nV1; i++)
+        for (size_t e = o->vecOff[i]; e < o->vecOff[i + 1]; e++) {
+            const float sI = o->sInfo[o->vecID[e]];
+            if (sI > 1.0f) farSpiked = 1;
+            o->ring[o->ringOff[e] + o->slot[e]] = sI;
+        }
+    if (!farSpiked) {
+        for (size_t e = 0; e < o->nFar; e++) o->slot[e] = (o->slot[e] + 1) % o->depth[e];
+        return 0;
+    }
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nV1; i++) {
+        const int itype = otype(o, i % bs);
+        float lgE[PV1_MAX_NG] = {0, 0}, lhE[PV1_MAX_NG] = {0, 0}, lgI[PV1_MAX_NG] = {0, 0}, lhI[PV1_MAX_NG] = {0, 0};
+        for (size_t e = o->vecOff[i]; e < o->vecOff[i + 1]; e++) {
+            const uint32_t pre = o->vecID[e];
+            const int tid = (int)(pre % bs);
+            const float strength = o->conVec[e];
+            float time2post = o->delayVec[e] / c->speedOfThought;
+            const int preE = tid < o->nE;
+            const ocond *cd = preE ? &o->cE : &o->cI;
+            const int ng = preE ? (int)c->ngE : (int)c->ngI;
+            float *lg = preE ? lgE : lgI, *lh = preE ? lhE : lhI;
+            const unsigned it2post = (unsigned)ceilf(time2post / dt);
+            time2post = it2post * dt - time2post;
+            int k0 = (int)o->slot[e] - (int)it2post;
+            if (k0 < 0) k0 += (int)o->depth[e];
+            o->slot[e] = (o->slot[e] + 1) % o->depth[e];
+            if (c->noFarDelay) continue;
+            for (int k = 0; k < 2; k++) {
+                float dtsp = o->ring[o->ringOff[e] + (size_t)((k0 + k) % (int)o->depth[e])];
+                if (dtsp >= 1.0f) {
+                    const unsigned nsp = (unsigned)floorf(dtsp);
+                    dtsp = (dtsp - nsp + k) * dt - time2post;
+                    if (dtsp < dt && dtsp >= 0) {
+                        const float f = strength;
+                        if (f > 0) {
+                            dtsp = dt - dtsp;
+                            for (int ig = 0; ig < ng; ig++) {
+                                const float ip = preE ? c->pE[itype * c->ngE + ig] : c->pI[itype * c->ngI + ig];
+                                ocond_input(cd, &lg[ig], &lh[ig], nsp * f * ip, dtsp, ig);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        if (o->vecOff[i + 1] > o->vecOff[i] && !c->noFarDelay) {
+            for (uint32_t ig = 0; ig < c->ngE; ig++) { o->gE[ig * nV1 + i] += lgE[ig]; o->hE[ig * nV1 + i] += lhE[ig]; }
+            for (uint32_t ig = 0; ig < c->ngI; ig++) { o->gI[ig * nV1 + i] += lgI[ig]; o->hI[ig * nV1 + i] += lhI[ig]; }
+        }
+    }
+    return 0;
+}
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}

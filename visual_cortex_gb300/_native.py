@@ -1,0 +1,146 @@
+"""ctypes binding of the C ABI declared in include/patchv1_gb300.h.
+
+The native library is the product: there is no Python or CPU fallback for the hot path.  If
+the library is missing the import of this module raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from .build import library_path
+
+MAX_NTYPE = 2
+MAX_NG = 2
+
+PV1_OK = 0
+ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "call out of order", -4: "unsupported option",
+          -5: "device error word", -6: "out of device memory"}
+
+REC_RAW, REC_LGN_SP, REC_LGN_FR, REC_SPIKES = 1, 2, 4, 8
+ST = dict(v=0, w=1, tBack=2, dep=3, gFF=4, hFF=5, gE=6, hE=7, gI=8, hI=9, sInfo=10,
+          lgn_ltr=11, lgn_lnl=12, lgn_sInfo=13)
+
+_f2 = C.c_float * MAX_NG
+_t2 = C.c_float * MAX_NTYPE
+_t4 = C.c_float * (MAX_NTYPE * MAX_NG)
+_tt = C.c_float * (MAX_NTYPE * MAX_NTYPE)
+
+
+class V1Config(C.Structure):
+    _fields_ = [
+        ("nblock", C.c_uint32), ("blockSize", C.c_uint32), ("nType", C.c_uint32),
+        ("nTypeE", C.c_uint32), ("typeAcc", C.c_uint32 * MAX_NTYPE),
+        ("ngFF", C.c_uint32), ("ngE", C.c_uint32), ("ngI", C.c_uint32), ("dt", C.c_float),
+        ("riseFF", _f2), ("decayFF", _f2), ("riseE", _f2), ("decayE", _f2),
+        ("riseI", _f2), ("decayI", _f2),
+        ("vE", C.c_float), ("vI", C.c_float), ("vL", C.c_float),
+        ("vR", _t2), ("vThres", _t2), ("gL", _t2), ("C", _t2), ("tRef", _t2), ("vT", _t2),
+        ("deltaT", _t2), ("tau_w", _t2), ("a", _t2), ("b", _t2),
+        ("pFF", _t4), ("pE", _t4), ("pI", _t4), ("synFail", _tt), ("synPerCon", _tt),
+        ("synFailFF", _t2), ("synPerConFF", _t2), ("noisyDep", _t2),
+        ("tau_noise", C.c_float), ("noiseOnTonic", C.c_int32), ("iModel", C.c_int32),
+        ("noDelay", C.c_int32), ("noFarDelay", C.c_int32), ("speedOfThought", C.c_float),
+        ("hWrite", C.c_int32),
+    ]
+
+
+class LgnConfig(C.Structure):
+    _fields_ = [
+        ("nLGN", C.c_uint32), ("nParvo_I", C.c_uint32), ("nMagno_I", C.c_uint32),
+        ("nParvo_C", C.c_uint32), ("nMagno_C", C.c_uint32), ("mSample1D", C.c_uint32),
+        ("nKernelSample", C.c_uint32), ("kernelSampleInterval", C.c_uint32),
+        ("iKernelSampleT0", C.c_uint32), ("denorm", C.c_uint32), ("ntPerFrame", C.c_uint32),
+        ("maxFrame", C.c_uint32), ("magnoComp", C.c_uint32), ("frameOffset", C.c_uint32),
+        ("dt", C.c_float), ("kernelSampleDt", C.c_float), ("kernelSampleT0", C.c_float),
+        ("convolRatio", C.c_float), ("frRatio", C.c_float), ("normViewDistance", C.c_float),
+        ("L_x0", C.c_float), ("L_y0", C.c_float), ("R_x0", C.c_float), ("R_y0", C.c_float),
+        ("nsig", C.c_float), ("flat_retina", C.c_int32),
+    ]
+
+
+_FP = C.POINTER(C.c_float)
+_UP = C.POINTER(C.c_uint32)
+
+
+class LgnParams(C.Structure):
+    _fields_ = [(n, _FP) for n in ("polar", "ecc", "rw", "rh", "orient", "k", "ratio", "tauR",
+                                   "tauD", "nR", "nD", "delay", "spont", "c50", "sharpness")] + \
+               [("coneType", _UP)]
+
+
+def _load() -> C.CDLL:
+    from .build import build_native
+    try:
+        path = build_native()   # no-op when the library is newer than its sources
+    except RuntimeError as e:
+        path = library_path()
+        if not Path(path).exists():
+            raise ImportError(f"native library {path} is missing and cannot be built: {e}") from e
+    lib = C.CDLL(str(path))
+    P = C.c_void_p
+    sig = {
+        "pv1_abi_version": ([], C.c_int),
+        "pv1_set_device": ([C.c_int], C.c_int),
+        "pv1_plan_create": ([C.POINTER(V1Config), C.POINTER(P)], C.c_int),
+        "pv1_plan_destroy": ([P], None),
+        "pv1_last_error": ([P], C.c_char_p),
+        "pv1_lgn_setup": ([P, C.POINTER(LgnConfig), C.POINTER(LgnParams), C.c_uint64], C.c_int),
+        "pv1_lgn_get_tables": ([P, _FP, _FP, _FP, _FP], C.c_int),
+        "pv1_stimulus_load": ([P, C.c_uint32, C.c_uint32, C.c_uint32, _FP, _FP], C.c_int),
+        "pv1_lgn_get_spatial": ([P, _FP], C.c_int),
+        "pv1_v1_set_lgn_synapses": ([P, C.c_uint32, _UP, _UP, _FP], C.c_int),
+        "pv1_v1_set_near": ([P, C.c_uint32, _UP, _UP, _FP], C.c_int),
+        "pv1_v1_set_far": ([P, _UP, _UP, _FP, _FP], C.c_int),
+        "pv1_v1_set_state": ([P, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP], C.c_int),
+        "pv1_v1_init_rng": ([P, C.c_uint64, C.c_uint32], C.c_int),
+        "pv1_host_init_state": ([C.POINTER(V1Config), C.c_uint64, _FP, _UP, C.c_int, C.c_float,
+                                 _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP],
+                                C.c_int),
+        "pv1_set_record": ([P, C.c_int, C.c_uint32], C.c_int),
+        "pv1_raw_record_floats": ([P], C.c_int64),
+        "pv1_run": ([P, C.c_uint32, C.c_int], C.c_int),
+        "pv1_fetch_records": ([P, C.c_uint64, C.c_uint32, _FP, _FP, _FP], C.c_int),
+        "pv1_get_state": ([P, C.c_int, _FP], C.c_int),
+        "pv1_put_state": ([P, C.c_int, _FP], C.c_int),
+        "pv1_set_draw_record": ([P, C.c_uint32, C.c_uint32], C.c_int),
+        "pv1_fetch_draws": ([P, C.c_int, _FP, C.POINTER(C.c_int32)], C.c_int),
+        "pv1_last_launch_count": ([P], C.c_int64),
+        "pv1_fetch_spikes": ([P, C.c_uint64, C.c_uint32, _FP], C.c_int),
+        "pv1_run_timed": ([P, C.c_uint32, C.c_uint64, _FP], C.c_int),
+        "pv1_time_kernels": ([P, C.c_uint32, _FP, _FP, C.POINTER(C.c_int)], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    return lib
+
+
+lib = _load()
+
+
+class NativeError(RuntimeError):
+    pass
+
+
+def fptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_FP)
+
+
+def uptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.uint32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_UP)
+
+
+def check(plan, rc: int, what: str):
+    if rc != PV1_OK:
+        msg = lib.pv1_last_error(plan).decode() if plan else ""
+        raise NativeError(f"{what} failed ({ERRORS.get(rc, rc)}): {msg}")

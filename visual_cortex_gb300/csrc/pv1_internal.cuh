@@ -1,0 +1,189 @@
+// Internal definitions shared by the patchV1 GB300 kernels and the host runtime.
+//
+// Device state is structure-of-arrays in HBM: every per-neuron quantity is a contiguous
+// [nV1] float array (conductance species as [ng][nV1]), so a warp touches 128 contiguous
+// bytes per quantity.  All arithmetic is fp32 as in the reference (Float = float,
+// src/types.h:6) and uses the same CUDA math calls (expf, logf, lgammaf, sqrtf).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <curand_kernel.h>
+#include <stdint.h>
+#include "../../include/patchv1_gb300.h"
+
+namespace pv1 {
+
+constexpr int kMaxType = PV1_MAX_NTYPE;
+constexpr int kMaxNG = PV1_MAX_NG;
+constexpr int kMaxSeg = 255;   // frames one temporal window may span (segments per step)
+
+// Error word bits raised by kernels (never trap).
+constexpr int kErrRecordOverflow = 1;   // a draw record ran out of capacity
+constexpr int kErrNegTsp = 2;           // interpolated spike time < 0 or NaN
+constexpr int kErrFarOverflow = 4;      // far event beyond the delay ring
+constexpr int kErrBounds = 8;           // an index failed its bounds check
+
+// Two-state (g, h) conductance kernel with rise and decay times: the kinetics of the
+// reference's ConductanceShape (src/condShape.h:13-41).  dod = tr/(td - tr).
+struct Cond {
+    float rise[kMaxNG], decay[kMaxNG], dod[kMaxNG];
+};
+
+__host__ inline Cond make_cond(const float *rt, const float *dc, int n) {
+    Cond c{};
+    for (int i = 0; i < n; i++) {
+        c.rise[i] = rt[i];
+        c.decay[i] = dc[i];
+        c.dod[i] = rt[i] / (dc[i] - rt[i]);
+    }
+    return c;
+}
+
+// Unit input of strength f arriving `dt` before the end of the interval
+// (compute_single_input_conductance, src/condShape.h:27-32).
+__device__ __forceinline__ void cond_input(const Cond &c, float &g, float &h, float f, float dt,
+                                           int ig) {
+    float etr = expf(-dt / c.rise[ig]);
+    g += f * c.dod[ig] * (expf(-dt / c.decay[ig]) - etr);
+    h += f * etr;
+}
+
+// Exact exponential decay of (g, h) over dt (decay_conductance, src/condShape.h:34-40).
+__device__ __forceinline__ void cond_decay(const Cond &c, float &g, float &h, float dt, int ig) {
+    float etr = expf(-dt / c.rise[ig]);
+    float etd = expf(-dt / c.decay[ig]);
+    g = g * etd + h * c.dod[ig] * (etd - etr);
+    h *= etr;
+}
+
+// Frame bookkeeping of the magno temporal window, shared by host and device.
+struct FrameSched {
+    int denorm, ntPerFrame, maxFrame, magnoComp, frameOffset;
+    int nFrame;        // frames in the movie (loops)
+    int initRow;       // row of S holding the initial-luminance frame
+};
+
+// Segments of the temporal kernel per frame phase: for phase p (0 <= p < ntPerFrame),
+// segment s covers samples [j0, j1) that all read the frame `rel` layers after the tail.
+struct SegTable {
+    int nPhase, maxSeg;
+    const int *nseg;     // [nPhase]
+    const int *rel;      // [nPhase][maxSeg]
+    const int *j0;       // [nPhase][maxSeg+1] (j0[s+1] = end of segment s)
+};
+
+// Number of stimulus frames read once step `it` has started.
+__host__ __device__ __forceinline__ int frames_read_after_step(const FrameSched &fs, long long it) {
+    // frames are read while (it+1)*denorm > currentFrame*ntPerFrame (src/patch.cu:5969)
+    long long num = (it + 1) * (long long)fs.denorm;
+    return (int)((num + fs.ntPerFrame - 1) / fs.ntPerFrame);
+}
+
+struct LgnParams {
+    int nMagno, nLGN;
+    int nParvo_I, nMagno_I, nParvo_C;
+    int nKS;                 // temporal samples
+    float dt, convolRatio, frRatio;
+    FrameSched fs;
+    SegTable seg;
+    int iKernelSampleT0, interval;
+    const double *ctw;       // [nKS+1][nMagno] cumulative temporal weights
+    const float *S;          // [nFrame+1][nMagno] spatial stage per frame
+    const float *absk;       // [nMagno] |k| of the center
+    const float *maxConvol;  // [nLGN]
+    const float *c50, *sharp, *la, *lb;  // logistic per LGN id [nLGN]
+    float *leftTimeRate, *lastNegLogRand;  // [nLGN]
+    curandStateMRG32k3a *state;            // [nLGN]
+    float *rate;             // [K][nLGN] rates of the chunk being computed
+    float *outSInfo;         // [outSlots][nLGN] spike words, row = step % outSlots
+    float *outFr;            // [outSlots][nLGN] rates (may be null)
+    int outSlots;
+    float *recU; int *recUCount; int recCap; long long recStep0; int recSteps;
+    int *err;
+};
+
+struct V1Params {
+    int nV1, blockSize, nblock, nE, nI, nType, nTypeE;
+    int typeAcc[kMaxType];
+    int ngFF, ngE, ngI;
+    float dt;
+    Cond condFF, condE, condI;
+    float vE, vI, vL;
+    float vR[kMaxType], vThres[kMaxType], gL[kMaxType], C[kMaxType], tRef[kMaxType];
+    float vT[kMaxType], deltaT[kMaxType], tau_w[kMaxType], a[kMaxType], b[kMaxType];
+    float pFF[kMaxType * kMaxNG], pE[kMaxType * kMaxNG], pI[kMaxType * kMaxNG];
+    float synFail[kMaxType * kMaxType], synPerCon[kMaxType * kMaxType];
+    float synFailFF[kMaxType], synPerConFF[kMaxType], noisyDep[kMaxType];
+    float tau_noise;
+    int noiseOnTonic, iModel;
+    int condRng;        // rGenCond draws can change results (some failure rate > 0)
+    int noiseRng;       // some noisyDep > 0
+    // state [nV1] / [ng][nV1]
+    float *v, *w, *tBack, *dep, *gFF, *hFF, *gE, *hE, *gI, *hI, *tonicDep, *lastNoise;
+    curandStateMRG32k3a *rGenCond, *rNoisy;
+    float *sInfo;       // [2][nV1], slot = step & 1
+    // LGN -> V1
+    int maxLGN;
+    int lgnN;                  // row length of the LGN spike ring (nLGN)
+    const int *nLGNperV1;      // [nV1]
+    const int *lgnId;          // [maxLGN][nV1]
+    const float *sLGN;         // [maxLGN][nV1]
+    // near delivery
+    int nnbMax;
+    const int *nNearNB;        // [nblock]
+    const int *nbId;           // [nblock][nnbMax]
+    const float *conMat;       // [nblock][nnbMax][bs][bs]
+    // far delivery (outgoing lists by pre-neuron)
+    int farOn;                 // 0: no far input at all (noFarDelay=1 or no far synapses)
+    const int *farOff;         // [nV1+1]
+    const int *farPost;        // [nnz]
+    const float *farStr;       // [nnz]
+    const int *farSteps;       // [nnz] it2post
+    const float *farFrac;      // [nnz] it2post*dt - delay/speed
+    const unsigned char *farPre;  // [nV1] 1 if the neuron is a far presynaptic partner
+    unsigned long long *farAcc;   // [farDepth][ngE+ngI][2][nV1] fixed-point g,h
+    int farDepth;
+    int *farFlag;              // [3] any far-pre spike (sInfo > 1) in step t%3
+    // records
+    float *rec; long long recStride; int recSlots; int hWrite;
+    float *recSpk;             // [recSlots][nV1] spike words (PV1_REC_SPIKES)
+    float *recNoise; float *recFF; int *recFFCount; float *recNear; int *recNearCount;
+    int recCap; long long recStep0; int recSteps;
+    int *err;
+};
+
+// Arguments of the LGN setup kernel (one CTA per magno cell).
+struct SetupArgs {
+    int nMagno, nLGN, nParvo_I, nMagno_I, nParvo_C;
+    int nSample, nSample1D, nKS;
+    float kernelSampleDt, kernelSampleT0;
+    float normViewDistance, L_x0, L_y0, R_x0, R_y0, nsig;
+    int flat;
+    const float *polar, *ecc, *rw, *rh, *orient, *k;
+    const float *ratio, *tauR, *tauD, *nR, *nD, *delay;
+    float *TW, *SW, *SC, *maxConvol, *absk;
+    double *ctw;
+    int *err;
+};
+
+// Launchers (defined next to their kernels).
+cudaError_t launch_lgn_setup(const SetupArgs &a, int blockThreads, cudaStream_t st);
+cudaError_t launch_lgn_rng_init(curandStateMRG32k3a *state, float *lnl, float *ltr,
+                                unsigned long long seed, int n, cudaStream_t st);
+cudaError_t launch_lgn_spatial(cudaTextureObject_t L, cudaTextureObject_t M, cudaTextureObject_t S,
+                               const float *SW, const float *SC, const int *coneType, int nMagno,
+                               int nSample, int layer0, int nLayer, int row0, float *out,
+                               cudaStream_t st);
+cudaError_t launch_lgn_step(const LgnParams &p, const long long *stepBase, int K, cudaStream_t st);
+cudaError_t launch_v1_step(const V1Params &p, const long long *stepBase, int stepOffset,
+                           const float *lgnSInfo, int lgnSlots, int deliverPrev, int doStep,
+                           cudaStream_t st);
+cudaError_t launch_v1_rng_init(curandStateMRG32k3a *cond, curandStateMRG32k3a *noisy,
+                               unsigned long long seed, int nV1, int trainDepth, cudaStream_t st);
+cudaError_t launch_advance_step(long long *stepBase, int k, cudaStream_t st);
+
+// Fixed-point scale for far-delivery accumulation: integer adds are associative, so the
+// sum of events does not depend on their order and runs are reproducible.
+constexpr double kFarScale = 4294967296.0;  // 2^32
+
+}  // namespace pv1

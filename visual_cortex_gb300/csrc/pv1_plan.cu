@@ -1,0 +1,1178 @@
+// Host runtime of the patchV1 GB300 hot path: the plan object behind the C ABI of
+// include/patchv1_gb300.h.  It owns every device buffer and one CUDA stream, builds the
+// device-side tables (far-delivery event lists, temporal-kernel segment table), and issues
+// the step loop as CUDA graphs of (one LGN launch + K V1 launches + a step-counter bump).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "pv1_internal.cuh"
+
+using namespace pv1;
+
+struct pv1_plan {
+    pv1_v1_config cfg{};
+    std::string err;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int nV1 = 0, nE = 0, nI = 0;
+    V1Params vp{};
+    LgnParams lp{};
+    // device allocations (freed in destroy)
+    std::vector<void *> allocs;
+    int *d_err = nullptr;
+    long long *d_stepBase = nullptr;
+    bool haveLGNsyn = false, haveNear = false, haveState = false, haveRng = false;
+    bool lgnReady = false, stimReady = false;
+    pv1_lgn_config lcfg{};
+    int nMagno = 0, nLGN = 0, mSample = 0;
+    float *d_TW = nullptr, *d_SW = nullptr, *d_SC = nullptr, *d_maxConvol = nullptr;
+    float *d_S = nullptr;
+    int *d_coneType = nullptr;
+    int nFrame = 0;
+    // LGN spike ring
+    float *d_lgnRing = nullptr, *d_lgnFr = nullptr;
+    int lgnSlots = 0;
+    int K = 32;  // steps per LGN launch / per graph
+    // stepping
+    long long step = 0;
+    bool pending = false;
+    // records
+    int recFlags = 0;
+    int recSlots = 0;
+    float *d_rec = nullptr;
+    long long recStride = 0;
+    // graphs
+    cudaGraphExec_t graphExec = nullptr;
+    long long launches = 0;
+    long long nFarSyn = 0;
+    void *flushBuf = nullptr;
+    uint64_t flushSize = 0;
+};
+
+namespace {
+
+int fail(pv1_plan *p, int code, const std::string &msg) {
+    if (p) p->err = msg;
+    return code;
+}
+
+#define PV1_CUDA(p, call)                                                                      \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail((p), PV1_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+int dev_alloc(pv1_plan *p, T **ptr, size_t n) {
+    *ptr = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)ptr, n * sizeof(T));
+    if (e != cudaSuccess) return fail(p, PV1_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    p->allocs.push_back((void *)*ptr);
+    e = cudaMemsetAsync(*ptr, 0, n * sizeof(T), p->stream);
+    if (e != cudaSuccess) return fail(p, PV1_E_CUDA, cudaGetErrorString(e));
+    return PV1_OK;
+}
+
+template <class T>
+int dev_upload(pv1_plan *p, T **ptr, const T *host, size_t n) {
+    int r = dev_alloc(p, ptr, n);
+    if (r) return r;
+    if (host && n) PV1_CUDA(p, cudaMemcpyAsync(*ptr, host, n * sizeof(T), cudaMemcpyHostToDevice, p->stream));
+    return PV1_OK;
+}
+
+void free_one(pv1_plan *p, void *ptr) {
+    auto it = std::find(p->allocs.begin(), p->allocs.end(), ptr);
+    if (it != p->allocs.end()) {
+        cudaFree(ptr);
+        p->allocs.erase(it);
+    }
+}
+
+int check_device_error(pv1_plan *p) {
+    int h = 0;
+    PV1_CUDA(p, cudaMemcpyAsync(&h, p->d_err, sizeof(int), cudaMemcpyDeviceToHost, p->stream));
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    if (h) {
+        std::string m = "device error word 0x" + std::to_string(h) + ":";
+        if (h & kErrRecordOverflow) m += " draw-record overflow;";
+        if (h & kErrNegTsp) m += " negative or NaN spike time;";
+        if (h & kErrFarOverflow) m += " far event beyond delay ring;";
+        if (h & kErrBounds) m += " bounds check;";
+        return fail(p, PV1_E_DEVICE, m);
+    }
+    return PV1_OK;
+}
+
+void drop_graph(pv1_plan *p) {
+    if (p->graphExec) {
+        cudaGraphExecDestroy(p->graphExec);
+        p->graphExec = nullptr;
+    }
+}
+
+// Issues k steps (one LGN launch, k V1 launches, one counter bump) on the plan's stream.
+int issue_chunk(pv1_plan *p, int k, int deliverFirst) {
+    cudaError_t e = launch_lgn_step(p->lp, p->d_stepBase, k, p->stream);
+    if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("lgn_step: ") + cudaGetErrorString(e));
+    for (int s = 0; s < k; s++) {
+        int deliver = (s == 0) ? deliverFirst : 1;
+        e = launch_v1_step(p->vp, p->d_stepBase, s, p->d_lgnRing, p->lgnSlots, deliver, 1, p->stream);
+        if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("v1_step: ") + cudaGetErrorString(e));
+    }
+    e = launch_advance_step(p->d_stepBase, k, p->stream);
+    if (e != cudaSuccess) return fail(p, PV1_E_CUDA, cudaGetErrorString(e));
+    return PV1_OK;
+}
+
+// Builds the per-phase segment table of the temporal kernel: for phase p the sample j sits
+// (T0 + j*interval)*denorm + p units of dt/denorm after the window tail, i.e. in the frame
+// rel = that / ntPerFrame after the tail frame (src/discrete_input_convol.cu:1442-1540).
+void build_segments(const pv1_lgn_config &c, std::vector<int> &nseg, std::vector<int> &rel,
+                    std::vector<int> &j0, int &maxSeg) {
+    const int nPhase = (int)c.ntPerFrame;
+    const int nKS = (int)c.nKernelSample;
+    std::vector<std::vector<int>> relv(nPhase), j0v(nPhase);
+    maxSeg = 1;
+    for (int ph = 0; ph < nPhase; ph++) {
+        int last = -1;
+        for (int j = 0; j < nKS; j++) {
+            long long o = (long long)(c.iKernelSampleT0 + (long long)j * c.kernelSampleInterval) * c.denorm + ph;
+            int r = (int)(o / c.ntPerFrame);
+            if (r != last) {
+                relv[ph].push_back(r);
+                j0v[ph].push_back(j);
+                last = r;
+            }
+        }
+        j0v[ph].push_back(nKS);
+        maxSeg = std::max<int>(maxSeg, (int)relv[ph].size());
+    }
+    nseg.assign(nPhase, 0);
+    rel.assign((size_t)nPhase * maxSeg, 0);
+    j0.assign((size_t)nPhase * (maxSeg + 1), nKS);
+    for (int ph = 0; ph < nPhase; ph++) {
+        nseg[ph] = (int)relv[ph].size();
+        for (size_t s = 0; s < relv[ph].size(); s++) rel[(size_t)ph * maxSeg + s] = relv[ph][s];
+        for (size_t s = 0; s < j0v[ph].size(); s++) j0[(size_t)ph * (maxSeg + 1) + s] = j0v[ph][s];
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int pv1_abi_version(void) { return 1; }
+
+int pv1_set_device(int device) {
+    return cudaSetDevice(device) == cudaSuccess ? PV1_OK : PV1_E_CUDA;
+}
+
+const char *pv1_last_error(const pv1_plan *plan) { return plan ? plan->err.c_str() : "null plan"; }
+
+int pv1_plan_create(const pv1_v1_config *cfg, pv1_plan **out) {
+    if (!cfg || !out) return PV1_E_ARG;
+    *out = nullptr;
+    const pv1_v1_config &c = *cfg;
+    if (c.nType < 1 || c.nType > PV1_MAX_NTYPE || c.nTypeE < 1 || c.nTypeE >= c.nType + 1)
+        return PV1_E_ARG;
+    if (c.blockSize < 32 || c.blockSize > 1024 || c.nblock < 1) return PV1_E_ARG;
+    if (c.typeAcc[c.nType - 1] != c.blockSize) return PV1_E_ARG;
+    if (c.ngFF < 1 || c.ngFF > PV1_MAX_NG || c.ngE < 1 || c.ngE > PV1_MAX_NG || c.ngI < 1 ||
+        c.ngI > PV1_MAX_NG)
+        return PV1_E_ARG;
+    if (!(c.dt > 0)) return PV1_E_ARG;
+    pv1_plan *p = new pv1_plan();
+    p->cfg = c;
+    if (cudaGetDevice(&p->device) != cudaSuccess) {
+        delete p;
+        return PV1_E_CUDA;
+    }
+    if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete p;
+        return PV1_E_CUDA;
+    }
+    if (c.noDelay != 1) {
+        *out = p;
+        return fail(p, PV1_E_UNSUPPORTED, "noDelay=0 (distance-delayed near delivery) is not built");
+    }
+    p->nV1 = (int)(c.nblock * c.blockSize);
+    p->nE = (int)c.typeAcc[c.nTypeE - 1];
+    p->nI = (int)c.blockSize - p->nE;
+    const int nV1 = p->nV1;
+    V1Params &v = p->vp;
+    v.nV1 = nV1;
+    v.blockSize = (int)c.blockSize;
+    v.nblock = (int)c.nblock;
+    v.nE = p->nE;
+    v.nI = p->nI;
+    v.nType = (int)c.nType;
+    v.nTypeE = (int)c.nTypeE;
+    for (int j = 0; j < kMaxType; j++) v.typeAcc[j] = (int)c.typeAcc[j];
+    v.ngFF = (int)c.ngFF;
+    v.ngE = (int)c.ngE;
+    v.ngI = (int)c.ngI;
+    v.dt = c.dt;
+    v.condFF = make_cond(c.riseFF, c.decayFF, c.ngFF);
+    v.condE = make_cond(c.riseE, c.decayE, c.ngE);
+    v.condI = make_cond(c.riseI, c.decayI, c.ngI);
+    v.vE = c.vE;
+    v.vI = c.vI;
+    v.vL = c.vL;
+    bool condRng = false, noiseRng = false;
+    for (int j = 0; j < kMaxType; j++) {
+        v.vR[j] = c.vR[j];
+        v.vThres[j] = c.vThres[j];
+        v.gL[j] = c.gL[j];
+        v.C[j] = c.C[j];
+        v.tRef[j] = c.tRef[j];
+        v.vT[j] = c.vT[j];
+        v.deltaT[j] = c.deltaT[j];
+        v.tau_w[j] = c.tau_w[j];
+        v.a[j] = c.a[j];
+        v.b[j] = c.b[j];
+        v.synFailFF[j] = c.synFailFF[j];
+        v.synPerConFF[j] = c.synPerConFF[j];
+        v.noisyDep[j] = c.noisyDep[j];
+        if (j < (int)c.nType && c.synFailFF[j] > 0) condRng = true;
+        if (j < (int)c.nType && c.noisyDep[j] > 0) noiseRng = true;
+    }
+    for (int j = 0; j < kMaxType * kMaxNG; j++) {
+        v.pFF[j] = c.pFF[j];
+        v.pE[j] = c.pE[j];
+        v.pI[j] = c.pI[j];
+    }
+    for (int j = 0; j < kMaxType * kMaxType; j++) {
+        v.synFail[j] = c.synFail[j];
+        v.synPerCon[j] = c.synPerCon[j];
+        if (j < (int)(c.nType * c.nType) && c.synFail[j] > 0) condRng = true;
+    }
+    v.condRng = condRng;
+    v.noiseRng = noiseRng;
+    v.tau_noise = c.tau_noise;
+    v.noiseOnTonic = c.noiseOnTonic;
+    v.iModel = c.iModel;
+    v.hWrite = c.hWrite;
+    int r = 0;
+    r |= dev_alloc(p, &p->d_err, 1);
+    r |= dev_alloc(p, &p->d_stepBase, 1);
+    r |= dev_alloc(p, &v.v, nV1);
+    r |= dev_alloc(p, &v.w, nV1);
+    r |= dev_alloc(p, &v.tBack, nV1);
+    r |= dev_alloc(p, &v.dep, nV1);
+    r |= dev_alloc(p, &v.gFF, (size_t)c.ngFF * nV1);
+    r |= dev_alloc(p, &v.hFF, (size_t)c.ngFF * nV1);
+    r |= dev_alloc(p, &v.gE, (size_t)c.ngE * nV1);
+    r |= dev_alloc(p, &v.hE, (size_t)c.ngE * nV1);
+    r |= dev_alloc(p, &v.gI, (size_t)c.ngI * nV1);
+    r |= dev_alloc(p, &v.hI, (size_t)c.ngI * nV1);
+    r |= dev_alloc(p, &v.tonicDep, nV1);
+    r |= dev_alloc(p, &v.lastNoise, nV1);
+    r |= dev_alloc(p, &v.sInfo, (size_t)2 * nV1);
+    r |= dev_alloc(p, &v.rGenCond, nV1);
+    r |= dev_alloc(p, &v.rNoisy, nV1);
+    r |= dev_alloc(p, &v.farFlag, 3);
+    if (r) {
+        *out = p;
+        return PV1_E_NOMEM;
+    }
+    v.err = p->d_err;
+    v.recSlots = 1;
+    *out = p;
+    return PV1_OK;
+}
+
+void pv1_plan_destroy(pv1_plan *p) {
+    if (!p) return;
+    cudaStreamSynchronize(p->stream);
+    drop_graph(p);
+    for (void *ptr : p->allocs) cudaFree(ptr);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+int pv1_lgn_setup(pv1_plan *p, const pv1_lgn_config *lc, const pv1_lgn_params *prm, uint64_t seed) {
+    if (!p || !lc || !prm) return PV1_E_ARG;
+    const pv1_lgn_config &c = *lc;
+    const int nParvo = (int)(c.nParvo_I + c.nParvo_C);
+    const int nMagno = (int)(c.nMagno_I + c.nMagno_C);
+    if (nParvo > 0) return fail(p, PV1_E_UNSUPPORTED, "parvocellular LGN cells are not built");
+    if (!c.flat_retina) return fail(p, PV1_E_UNSUPPORTED, "curved-retina sample geometry is not built (flat_retina=1 only)");
+    if ((int)c.nLGN != nParvo + nMagno) return fail(p, PV1_E_ARG, "nLGN != nParvo + nMagno");
+    if (c.mSample1D < 1 || c.mSample1D > 32) return fail(p, PV1_E_ARG, "mSample1D must be in [1,32]");
+    if (c.nKernelSample < 1 || c.ntPerFrame < 1 || c.denorm < 1 || c.maxFrame < 1)
+        return fail(p, PV1_E_ARG, "bad kernel-sampling bookkeeping");
+    if (!(c.nsig > 0)) return fail(p, PV1_E_UNSUPPORTED, "nsig <= 0 (python sampler) is not built");
+    p->lcfg = c;
+    p->nMagno = nMagno;
+    p->nLGN = (int)c.nLGN;
+    p->mSample = (int)(c.mSample1D * c.mSample1D);
+    const int nLGN = p->nLGN;
+    const int nKS = (int)c.nKernelSample;
+    LgnParams &L = p->lp;
+    L.nMagno = nMagno;
+    L.nLGN = nLGN;
+    L.nParvo_I = (int)c.nParvo_I;
+    L.nMagno_I = (int)c.nMagno_I;
+    L.nParvo_C = (int)c.nParvo_C;
+    L.nKS = nKS;
+    L.dt = c.dt;
+    L.convolRatio = c.convolRatio;
+    L.frRatio = c.frRatio;
+    L.iKernelSampleT0 = (int)c.iKernelSampleT0;
+    L.interval = (int)c.kernelSampleInterval;
+    L.err = p->d_err;
+    // per-cell parameters (2*nLGN arrays)
+    float *d_par[12];
+    const float *hpar[12] = {prm->polar, prm->ecc, prm->rw, prm->rh, prm->orient, prm->k,
+                             prm->ratio, prm->tauR, prm->tauD, prm->nR, prm->nD, prm->delay};
+    for (int q = 0; q < 12; q++) {
+        if (!hpar[q]) return fail(p, PV1_E_ARG, "missing LGN parameter array");
+        int r = dev_upload(p, &d_par[q], hpar[q], (size_t)2 * nLGN);
+        if (r) return r;
+    }
+    // logistic a, b (hStatic_nonlinear, src/LGN_props.h:159-169), float arithmetic
+    std::vector<float> la(nLGN), lb(nLGN);
+    for (int i = 0; i < nLGN; i++) {
+        const float e_kc50 = std::exp(prm->sharpness[i] * prm->c50[i]);
+        const float e_kc50_k = std::exp(prm->sharpness[i] * prm->c50[i] - prm->sharpness[i]);
+        la[i] = (1 - prm->spont[i]) * (1 + e_kc50) * (1 + e_kc50_k) / (e_kc50 - e_kc50_k);
+        lb[i] = 1 - la[i] / (1 + e_kc50_k);
+    }
+    float *d_c50, *d_sharp, *d_la, *d_lb, *d_absk;
+    int r = 0;
+    r |= dev_upload(p, &d_c50, prm->c50, nLGN);
+    r |= dev_upload(p, &d_sharp, prm->sharpness, nLGN);
+    r |= dev_upload(p, &d_la, la.data(), nLGN);
+    r |= dev_upload(p, &d_lb, lb.data(), nLGN);
+    r |= dev_alloc(p, &p->d_TW, (size_t)nMagno * nKS);
+    r |= dev_alloc(p, &p->d_SW, (size_t)nMagno * p->mSample);
+    r |= dev_alloc(p, &p->d_SC, (size_t)2 * nMagno * p->mSample);
+    r |= dev_alloc(p, &p->d_maxConvol, nLGN);
+    r |= dev_alloc(p, &d_absk, nMagno);
+    double *d_ctw;
+    r |= dev_alloc(p, &d_ctw, (size_t)(nKS + 1) * nMagno);
+    float *d_ltr, *d_lnl;
+    curandStateMRG32k3a *d_state;
+    r |= dev_alloc(p, &d_ltr, nLGN);
+    r |= dev_alloc(p, &d_lnl, nLGN);
+    r |= dev_alloc(p, &d_state, nLGN);
+    if (r) return fail(p, PV1_E_NOMEM, "LGN allocation failed");
+    // cone type of each magno center
+    std::vector<int> cone(nMagno);
+    for (int m = 0; m < nMagno; m++) {
+        int id = (int)c.nParvo_I + m;
+        if (m >= (int)c.nMagno_I) id += (int)c.nParvo_C;
+        cone[m] = (int)prm->coneType[id];
+        if (cone[m] > 4) return fail(p, PV1_E_ARG, "cone type > 4");
+    }
+    r = dev_upload(p, &p->d_coneType, cone.data(), nMagno);
+    if (r) return r;
+    SetupArgs A{};
+    A.nMagno = nMagno;
+    A.nLGN = nLGN;
+    A.nParvo_I = (int)c.nParvo_I;
+    A.nMagno_I = (int)c.nMagno_I;
+    A.nParvo_C = (int)c.nParvo_C;
+    A.nSample = p->mSample;
+    A.nSample1D = (int)c.mSample1D;
+    A.nKS = nKS;
+    A.kernelSampleDt = c.kernelSampleDt;
+    A.kernelSampleT0 = c.kernelSampleT0;
+    A.normViewDistance = c.normViewDistance;
+    A.L_x0 = c.L_x0;
+    A.L_y0 = c.L_y0;
+    A.R_x0 = c.R_x0;
+    A.R_y0 = c.R_y0;
+    A.nsig = c.nsig;
+    A.flat = c.flat_retina;
+    A.polar = d_par[0];
+    A.ecc = d_par[1];
+    A.rw = d_par[2];
+    A.rh = d_par[3];
+    A.orient = d_par[4];
+    A.k = d_par[5];
+    A.ratio = d_par[6];
+    A.tauR = d_par[7];
+    A.tauD = d_par[8];
+    A.nR = d_par[9];
+    A.nD = d_par[10];
+    A.delay = d_par[11];
+    A.TW = p->d_TW;
+    A.SW = p->d_SW;
+    A.SC = p->d_SC;
+    A.maxConvol = p->d_maxConvol;
+    A.absk = d_absk;
+    A.ctw = d_ctw;
+    A.err = p->d_err;
+    int threads = ((p->mSample + 31) / 32) * 32;
+    if (nMagno > 0) PV1_CUDA(p, launch_lgn_setup(A, threads, p->stream));
+    PV1_CUDA(p, launch_lgn_rng_init(d_state, d_lnl, d_ltr, (unsigned long long)seed, nLGN, p->stream));
+    // segment table
+    std::vector<int> nseg, rel, j0;
+    int maxSeg = 1;
+    build_segments(c, nseg, rel, j0, maxSeg);
+    if (maxSeg > kMaxSeg) return fail(p, PV1_E_UNSUPPORTED, "temporal window spans more than 255 frames");
+    r = dev_alloc(p, &L.rate, (size_t)p->K * nLGN);
+    if (r) return r;
+    int *d_nseg, *d_rel, *d_j0;
+    r = 0;
+    r |= dev_upload(p, &d_nseg, nseg.data(), nseg.size());
+    r |= dev_upload(p, &d_rel, rel.data(), rel.size());
+    r |= dev_upload(p, &d_j0, j0.data(), j0.size());
+    if (r) return r;
+    L.seg.nPhase = (int)c.ntPerFrame;
+    L.seg.maxSeg = maxSeg;
+    L.seg.nseg = d_nseg;
+    L.seg.rel = d_rel;
+    L.seg.j0 = d_j0;
+    L.fs.denorm = (int)c.denorm;
+    L.fs.ntPerFrame = (int)c.ntPerFrame;
+    L.fs.maxFrame = (int)c.maxFrame;
+    L.fs.magnoComp = (int)c.magnoComp;
+    L.fs.frameOffset = (int)c.frameOffset;
+    L.ctw = d_ctw;
+    L.absk = d_absk;
+    L.maxConvol = p->d_maxConvol;
+    L.c50 = d_c50;
+    L.sharp = d_sharp;
+    L.la = d_la;
+    L.lb = d_lb;
+    L.leftTimeRate = d_ltr;
+    L.lastNegLogRand = d_lnl;
+    L.state = d_state;
+    // LGN spike ring (rows = step % lgnSlots)
+    p->lgnSlots = std::max(p->K, 2);
+    r = dev_alloc(p, &p->d_lgnRing, (size_t)p->lgnSlots * nLGN);
+    if (r) return r;
+    L.outSInfo = p->d_lgnRing;
+    L.outFr = nullptr;
+    L.outSlots = p->lgnSlots;
+    p->vp.lgnN = nLGN;
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    for (int q = 0; q < 12; q++) free_one(p, d_par[q]);
+    int e = check_device_error(p);
+    if (e) return e;
+    p->lgnReady = true;
+    drop_graph(p);
+    return PV1_OK;
+}
+
+int pv1_lgn_get_tables(pv1_plan *p, float *TW, float *SW, float *SC, float *maxConvol) {
+    if (!p) return PV1_E_ARG;
+    if (!p->lgnReady) return fail(p, PV1_E_STATE, "LGN not set up");
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    const size_t nm = p->nMagno;
+    if (TW) PV1_CUDA(p, cudaMemcpy(TW, p->d_TW, nm * p->lcfg.nKernelSample * sizeof(float), cudaMemcpyDeviceToHost));
+    if (SW) PV1_CUDA(p, cudaMemcpy(SW, p->d_SW, nm * p->mSample * sizeof(float), cudaMemcpyDeviceToHost));
+    if (SC) PV1_CUDA(p, cudaMemcpy(SC, p->d_SC, 2 * nm * p->mSample * sizeof(float), cudaMemcpyDeviceToHost));
+    if (maxConvol) PV1_CUDA(p, cudaMemcpy(maxConvol, p->d_maxConvol, p->nLGN * sizeof(float), cudaMemcpyDeviceToHost));
+    return PV1_OK;
+}
+
+int pv1_stimulus_load(pv1_plan *p, uint32_t nFrame, uint32_t height, uint32_t width,
+                      const float init_LMS[3], const float *frames) {
+    if (!p || !init_LMS || (nFrame && !frames)) return PV1_E_ARG;
+    if (!p->lgnReady) return fail(p, PV1_E_STATE, "call pv1_lgn_setup first");
+    if (nFrame < 1 || width < 1 || height < 1 || width > 16384 || height > 16384)
+        return fail(p, PV1_E_ARG, "bad stimulus size");
+    const int nMagno = p->nMagno;
+    if (p->d_S) free_one(p, p->d_S);
+    int r = dev_alloc(p, &p->d_S, (size_t)(nFrame + 1) * std::max(nMagno, 1));
+    if (r) return r;
+    const size_t npix = (size_t)width * height;
+    // process the movie in batches of <= 2047 layers plus the initial-luminance layer
+    const int maxLayers = 2048;
+    std::vector<float> plane(npix);
+    cudaChannelFormatDesc desc = cudaCreateChannelDesc(32, 0, 0, 0, cudaChannelFormatKindFloat);
+    for (uint32_t f0 = 0; f0 < nFrame + 1; f0 += maxLayers) {
+        const uint32_t nl = std::min<uint32_t>(maxLayers, nFrame + 1 - f0);
+        cudaArray_t arr[3] = {nullptr, nullptr, nullptr};
+        cudaTextureObject_t tex[3] = {0, 0, 0};
+        for (int ch = 0; ch < 3; ch++) {
+            PV1_CUDA(p, cudaMalloc3DArray(&arr[ch], &desc, make_cudaExtent(width, height, nl), cudaArrayLayered));
+            for (uint32_t l = 0; l < nl; l++) {
+                const uint32_t f = f0 + l;
+                const float *src;
+                if (f < nFrame) {
+                    src = frames + ((size_t)f * 3 + ch) * npix;
+                } else {
+                    std::fill(plane.begin(), plane.end(), init_LMS[ch]);
+                    src = plane.data();
+                }
+                cudaMemcpy3DParms cp{};
+                cp.srcPtr = make_cudaPitchedPtr((void *)src, width * sizeof(float), width, height);
+                cp.dstArray = arr[ch];
+                cp.dstPos = make_cudaPos(0, 0, l);
+                cp.extent = make_cudaExtent(width, height, 1);
+                cp.kind = cudaMemcpyHostToDevice;
+                PV1_CUDA(p, cudaMemcpy3DAsync(&cp, p->stream));
+                if (f >= nFrame) PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+            }
+            cudaResourceDesc rd{};
+            rd.resType = cudaResourceTypeArray;
+            rd.res.array.array = arr[ch];
+            cudaTextureDesc td{};
+            td.addressMode[0] = cudaAddressModeBorder;
+            td.addressMode[1] = cudaAddressModeBorder;
+            td.filterMode = cudaFilterModeLinear;
+            td.readMode = cudaReadModeElementType;
+            td.normalizedCoords = 1;
+            PV1_CUDA(p, cudaCreateTextureObject(&tex[ch], &rd, &td, nullptr));
+        }
+        if (nMagno > 0)
+            PV1_CUDA(p, launch_lgn_spatial(tex[0], tex[1], tex[2], p->d_SW, p->d_SC, p->d_coneType, nMagno,
+                                          p->mSample, 0, (int)nl, (int)f0, p->d_S, p->stream));
+        PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+        for (int ch = 0; ch < 3; ch++) {
+            cudaDestroyTextureObject(tex[ch]);
+            cudaFreeArray(arr[ch]);
+        }
+    }
+    p->nFrame = (int)nFrame;
+    p->lp.S = p->d_S;
+    p->lp.fs.nFrame = (int)nFrame;
+    p->lp.fs.initRow = (int)nFrame;
+    p->stimReady = true;
+    drop_graph(p);
+    return PV1_OK;
+}
+
+int pv1_lgn_get_spatial(pv1_plan *p, float *S) {
+    if (!p || !S) return PV1_E_ARG;
+    if (!p->stimReady) return fail(p, PV1_E_STATE, "no stimulus loaded");
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    PV1_CUDA(p, cudaMemcpy(S, p->d_S, (size_t)(p->nFrame + 1) * p->nMagno * sizeof(float), cudaMemcpyDeviceToHost));
+    return PV1_OK;
+}
+
+int pv1_v1_set_lgn_synapses(pv1_plan *p, uint32_t maxLGN, const uint32_t *nLGNperV1,
+                            const uint32_t *lgnId, const float *sLGN) {
+    if (!p || !nLGNperV1 || (maxLGN && (!lgnId || !sLGN))) return PV1_E_ARG;
+    const int nV1 = p->nV1;
+    for (int i = 0; i < nV1; i++)
+        if (nLGNperV1[i] > maxLGN) return fail(p, PV1_E_ARG, "nLGNperV1 > maxLGN");
+    if (p->lgnReady) {
+        for (size_t q = 0; q < (size_t)maxLGN * nV1; q++) {
+            const size_t i = q % nV1, j = q / nV1;
+            if (j < nLGNperV1[i] && lgnId[q] >= (uint32_t)p->nLGN) return fail(p, PV1_E_ARG, "LGN id out of range");
+        }
+    }
+    int *d_n, *d_id;
+    float *d_s;
+    int r = 0;
+    r |= dev_upload(p, &d_n, (const int *)nLGNperV1, nV1);
+    r |= dev_upload(p, &d_id, (const int *)lgnId, (size_t)maxLGN * nV1);
+    r |= dev_upload(p, &d_s, sLGN, (size_t)maxLGN * nV1);
+    if (r) return r;
+    p->vp.maxLGN = (int)maxLGN;
+    p->vp.nLGNperV1 = d_n;
+    p->vp.lgnId = d_id;
+    p->vp.sLGN = d_s;
+    p->haveLGNsyn = true;
+    drop_graph(p);
+    return PV1_OK;
+}
+
+int pv1_v1_set_near(pv1_plan *p, uint32_t nnb, const uint32_t *nNearNB, const uint32_t *nbId,
+                    const float *conMat) {
+    if (!p || !nNearNB || !nbId || !conMat || nnb < 1) return PV1_E_ARG;
+    const int nblock = (int)p->cfg.nblock;
+    for (int b = 0; b < nblock; b++) {
+        if (nNearNB[b] > nnb) return fail(p, PV1_E_ARG, "nNearNeighborBlock > nearNeighborBlock");
+        for (uint32_t q = 0; q < nNearNB[b]; q++)
+            if (nbId[(size_t)b * nnb + q] >= (uint32_t)nblock) return fail(p, PV1_E_ARG, "neighbour block id out of range");
+    }
+    const size_t bs = p->cfg.blockSize;
+    int *d_n, *d_id;
+    float *d_c;
+    int r = 0;
+    r |= dev_upload(p, &d_n, (const int *)nNearNB, nblock);
+    r |= dev_upload(p, &d_id, (const int *)nbId, (size_t)nblock * nnb);
+    r |= dev_upload(p, &d_c, conMat, (size_t)nblock * nnb * bs * bs);
+    if (r) return r;
+    p->vp.nnbMax = (int)nnb;
+    p->vp.nNearNB = d_n;
+    p->vp.nbId = d_id;
+    p->vp.conMat = d_c;
+    p->haveNear = true;
+    drop_graph(p);
+    return PV1_OK;
+}
+
+int pv1_v1_set_far(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, const float *conVec,
+                   const float *delayVec) {
+    if (!p || !nVec) return PV1_E_ARG;
+    const int nV1 = p->nV1;
+    const pv1_v1_config &c = p->cfg;
+    size_t nnz = 0;
+    for (int i = 0; i < nV1; i++) nnz += nVec[i];
+    if (nnz && (!vecID || !conVec || !delayVec)) return PV1_E_ARG;
+    p->nFarSyn = (long long)nnz;
+    if (nnz == 0 || c.noFarDelay) {
+        // no far synapses, or the reference's noFarDelay=1 path, which drops far input
+        p->vp.farOn = 0;
+        drop_graph(p);
+        return PV1_OK;
+    }
+    for (int q = 0; q < (int)(c.nType * c.nType); q++)
+        if (c.synFail[q] > 0)
+            return fail(p, PV1_E_UNSUPPORTED,
+                        "synaptic failure on delayed far synapses (host std::normal_distribution per post) is not built");
+    // outgoing lists by pre (stable counting sort keeps the post/j order within a pre)
+    std::vector<int> off(nV1 + 1, 0);
+    for (size_t e = 0; e < nnz; e++) {
+        if (vecID[e] >= (uint32_t)nV1) return fail(p, PV1_E_ARG, "far pre id out of range");
+        off[vecID[e] + 1]++;
+    }
+    for (int i = 0; i < nV1; i++) off[i + 1] += off[i];
+    std::vector<int> fill(off.begin(), off.end() - 1);
+    std::vector<int> post(nnz), steps(nnz);
+    std::vector<float> str(nnz), frac(nnz);
+    std::vector<unsigned char> isPre(nV1, 0);
+    int maxSteps = 0;
+    size_t e = 0;
+    for (int i = 0; i < nV1; i++) {
+        for (uint32_t j = 0; j < nVec[i]; j++, e++) {
+            const int pre = (int)vecID[e];
+            // delay arithmetic of recal_G_vec (src/coredynamics.cu:282-287), in float
+            float time2post = delayVec[e] / c.speedOfThought;
+            unsigned it2post = (unsigned)std::ceil(time2post / c.dt);
+            time2post = it2post * c.dt - time2post;
+            const int slot = fill[pre]++;
+            post[slot] = i;
+            str[slot] = conVec[e];
+            steps[slot] = (int)it2post;
+            frac[slot] = time2post;
+            isPre[pre] = 1;
+            maxSteps = std::max(maxSteps, (int)it2post);
+        }
+    }
+    int *d_off, *d_post, *d_steps;
+    float *d_str, *d_frac;
+    unsigned char *d_pre;
+    unsigned long long *d_acc;
+    const int depth = maxSteps + 2;
+    int r = 0;
+    r |= dev_upload(p, &d_off, off.data(), off.size());
+    r |= dev_upload(p, &d_post, post.data(), nnz);
+    r |= dev_upload(p, &d_steps, steps.data(), nnz);
+    r |= dev_upload(p, &d_str, str.data(), nnz);
+    r |= dev_upload(p, &d_frac, frac.data(), nnz);
+    r |= dev_upload(p, &d_pre, isPre.data(), nV1);
+    r |= dev_alloc(p, &d_acc, (size_t)depth * (c.ngE + c.ngI) * 2 * nV1);
+    if (r) return r;
+    V1Params &v = p->vp;
+    v.farOn = 1;
+    v.farOff = d_off;
+    v.farPost = d_post;
+    v.farSteps = d_steps;
+    v.farStr = d_str;
+    v.farFrac = d_frac;
+    v.farPre = d_pre;
+    v.farAcc = d_acc;
+    v.farDepth = depth;
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    drop_graph(p);
+    return PV1_OK;
+}
+
+int pv1_v1_set_state(pv1_plan *p, const float *v, const float *w, const float *gFF,
+                     const float *hFF, const float *gE, const float *hE, const float *gI,
+                     const float *hI, const float *tonicDep) {
+    if (!p || !v || !gFF || !hFF || !gE || !hE || !gI || !hI || !tonicDep) return PV1_E_ARG;
+    const size_t n = p->nV1;
+    const pv1_v1_config &c = p->cfg;
+    V1Params &vp = p->vp;
+    auto up = [&](float *dst, const float *src, size_t cnt) {
+        return cudaMemcpyAsync(dst, src, cnt * sizeof(float), cudaMemcpyHostToDevice, p->stream);
+    };
+    PV1_CUDA(p, up(vp.v, v, n));
+    if (w) PV1_CUDA(p, up(vp.w, w, n));
+    else PV1_CUDA(p, cudaMemsetAsync(vp.w, 0, n * sizeof(float), p->stream));
+    PV1_CUDA(p, up(vp.gFF, gFF, c.ngFF * n));
+    PV1_CUDA(p, up(vp.hFF, hFF, c.ngFF * n));
+    PV1_CUDA(p, up(vp.gE, gE, c.ngE * n));
+    PV1_CUDA(p, up(vp.hE, hE, c.ngE * n));
+    PV1_CUDA(p, up(vp.gI, gI, c.ngI * n));
+    PV1_CUDA(p, up(vp.hI, hI, c.ngI * n));
+    PV1_CUDA(p, up(vp.tonicDep, tonicDep, n));
+    PV1_CUDA(p, cudaMemsetAsync(vp.tBack, 0, n * sizeof(float), p->stream));
+    PV1_CUDA(p, cudaMemsetAsync(vp.lastNoise, 0, n * sizeof(float), p->stream));
+    PV1_CUDA(p, cudaMemsetAsync(vp.sInfo, 0, 2 * n * sizeof(float), p->stream));
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    p->haveState = true;
+    p->pending = false;
+    return PV1_OK;
+}
+
+int pv1_v1_init_rng(pv1_plan *p, uint64_t seed, uint32_t trainDepth) {
+    if (!p || trainDepth < 1) return PV1_E_ARG;
+    PV1_CUDA(p, launch_v1_rng_init(p->vp.rGenCond, p->vp.rNoisy, (unsigned long long)seed, p->nV1,
+                                   (int)trainDepth, p->stream));
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    p->haveRng = true;
+    return PV1_OK;
+}
+
+int pv1_set_record(pv1_plan *p, int flags, uint32_t slots) {
+    if (!p) return PV1_E_ARG;
+    if (!p->lgnReady) return fail(p, PV1_E_STATE, "call pv1_lgn_setup first");
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    if (flags && slots < 2) return fail(p, PV1_E_ARG, "record ring needs >= 2 slots");
+    const pv1_v1_config &c = p->cfg;
+    if (p->d_rec) { free_one(p, p->d_rec); p->d_rec = nullptr; }
+    if (p->d_lgnFr) { free_one(p, p->d_lgnFr); p->d_lgnFr = nullptr; }
+    const long long n = p->nV1;
+    p->recStride = pv1_raw_record_floats(p);
+    p->recFlags = flags;
+    p->recSlots = flags ? (int)slots : 0;
+    if (flags & PV1_REC_RAW) {
+        int r = dev_alloc(p, &p->d_rec, (size_t)slots * p->recStride);
+        if (r) return r;
+    }
+    if (p->vp.recSpk) { free_one(p, p->vp.recSpk); p->vp.recSpk = nullptr; }
+    if (flags & PV1_REC_SPIKES) {
+        int r = dev_alloc(p, &p->vp.recSpk, (size_t)slots * n);
+        if (r) return r;
+    }
+    // the LGN ring doubles as the LGN_sp record when it is at least `slots` rows long
+    int want = std::max(p->K, 2);
+    if (flags & (PV1_REC_LGN_SP | PV1_REC_LGN_FR)) want = std::max<int>(want, (int)slots);
+    if (want != p->lgnSlots) {
+        free_one(p, p->d_lgnRing);
+        p->lgnSlots = want;
+        int r = dev_alloc(p, &p->d_lgnRing, (size_t)want * p->nLGN);
+        if (r) return r;
+    }
+    if (flags & PV1_REC_LGN_FR) {
+        int r = dev_alloc(p, &p->d_lgnFr, (size_t)want * p->nLGN);
+        if (r) return r;
+    }
+    p->lp.outSInfo = p->d_lgnRing;
+    p->lp.outFr = p->d_lgnFr;
+    p->lp.outSlots = p->lgnSlots;
+    p->vp.rec = p->d_rec;
+    p->vp.recStride = p->recStride;
+    p->vp.recSlots = (flags & (PV1_REC_RAW | PV1_REC_SPIKES)) ? (int)slots : 1;
+    (void)n;
+    (void)c;
+    drop_graph(p);
+    return PV1_OK;
+}
+
+int64_t pv1_raw_record_floats(const pv1_plan *p) {
+    if (!p) return -1;
+    const pv1_v1_config &c = p->cfg;
+    const long long n = p->nV1;
+    const long long mI = (long long)p->nI * c.nblock;
+    long long fl = n * (1 + 2 + (c.iModel == 1) + (long long)c.ngFF * (1 + (c.hWrite != 0)) +
+                        (long long)(c.ngE + c.ngI) * (1 + (c.hWrite != 0)));
+    return fl + mI;
+}
+
+int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
+    if (!p) return PV1_E_ARG;
+    if (!p->lgnReady || !p->stimReady) return fail(p, PV1_E_STATE, "LGN/stimulus not loaded");
+    if (!p->haveLGNsyn || !p->haveNear || !p->haveState || !p->haveRng)
+        return fail(p, PV1_E_STATE, "V1 synapses/connectivity/state/rng not set");
+    if (p->recFlags && nsteps > (uint32_t)(p->recSlots - 1))
+        return fail(p, PV1_E_ARG, "run longer than the record ring; fetch records in between");
+    p->launches = 0;
+    PV1_CUDA(p, cudaMemcpyAsync(p->d_stepBase, &p->step, sizeof(long long), cudaMemcpyHostToDevice, p->stream));
+    uint32_t done = 0;
+    // the first chunk of a run without a pending delivery cannot come from the graph
+    if (!p->pending && nsteps > 0) {
+        int k = (int)std::min<uint32_t>(nsteps, (uint32_t)p->K);
+        int r = issue_chunk(p, k, 0);
+        if (r) return r;
+        p->launches += k + 3;
+        done += k;
+    }
+    const int K = p->K;
+    if (nsteps - done >= (uint32_t)K) {
+        if (!p->graphExec) {
+            cudaGraph_t g;
+            PV1_CUDA(p, cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+            int r = issue_chunk(p, K, 1);
+            cudaError_t e2 = cudaStreamEndCapture(p->stream, &g);
+            if (r) return r;
+            if (e2 != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("capture: ") + cudaGetErrorString(e2));
+            PV1_CUDA(p, cudaGraphInstantiate(&p->graphExec, g, 0));
+            cudaGraphDestroy(g);
+        }
+        while (nsteps - done >= (uint32_t)K) {
+            PV1_CUDA(p, cudaGraphLaunch(p->graphExec, p->stream));
+            p->launches += K + 3;
+            done += K;
+        }
+    }
+    if (done < nsteps) {
+        int k = (int)(nsteps - done);
+        int r = issue_chunk(p, k, 1);
+        if (r) return r;
+        p->launches += k + 3;
+        done += k;
+    }
+    p->step += nsteps;
+    if (nsteps > 0) p->pending = true;
+    if (sync) return check_device_error(p);
+    return PV1_OK;
+}
+
+int64_t pv1_last_launch_count(const pv1_plan *p) { return p ? p->launches : -1; }
+
+int pv1_fetch_spikes(pv1_plan *p, uint64_t step0, uint32_t n, float *out) {
+    if (!p || !out) return PV1_E_ARG;
+    if (!(p->recFlags & PV1_REC_SPIKES)) return fail(p, PV1_E_STATE, "spike recording is off");
+    if (step0 + n > (uint64_t)p->step) return fail(p, PV1_E_ARG, "records not produced yet");
+    if ((uint64_t)p->step - step0 > (uint64_t)p->recSlots) return fail(p, PV1_E_ARG, "records already overwritten");
+    const size_t nV1 = p->nV1;
+    // contiguous slot ranges, one or two copies
+    uint32_t done = 0;
+    while (done < n) {
+        const uint64_t t = step0 + done;
+        const uint32_t slot = (uint32_t)(t % p->recSlots);
+        const uint32_t cnt = std::min<uint32_t>(n - done, (uint32_t)p->recSlots - slot);
+        PV1_CUDA(p, cudaMemcpyAsync(out + (size_t)done * nV1, p->vp.recSpk + (size_t)slot * nV1,
+                                    (size_t)cnt * nV1 * sizeof(float), cudaMemcpyDeviceToHost, p->stream));
+        done += cnt;
+    }
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    return PV1_OK;
+}
+
+int pv1_run_timed(pv1_plan *p, uint32_t nsteps, uint64_t flush_bytes, float *ms) {
+    if (!p || !ms) return PV1_E_ARG;
+    if (flush_bytes > p->flushSize) {
+        if (p->flushBuf) free_one(p, p->flushBuf);
+        p->flushBuf = nullptr;
+        p->flushSize = 0;
+        unsigned char *buf = nullptr;
+        int r = dev_alloc(p, &buf, flush_bytes);
+        if (r) return r;
+        p->flushBuf = buf;
+        p->flushSize = flush_bytes;
+    }
+    cudaEvent_t e0, e1;
+    PV1_CUDA(p, cudaEventCreate(&e0));
+    PV1_CUDA(p, cudaEventCreate(&e1));
+    if (flush_bytes) PV1_CUDA(p, cudaMemsetAsync(p->flushBuf, (int)(p->step & 0xff), flush_bytes, p->stream));
+    PV1_CUDA(p, cudaEventRecord(e0, p->stream));
+    int r = pv1_run(p, nsteps, 0);
+    if (r) return r;
+    PV1_CUDA(p, cudaEventRecord(e1, p->stream));
+    PV1_CUDA(p, cudaEventSynchronize(e1));
+    PV1_CUDA(p, cudaEventElapsedTime(ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return check_device_error(p);
+}
+
+int pv1_time_kernels(pv1_plan *p, uint32_t nsteps, float *v1_ms, float *lgn_ms, int *chunk) {
+    if (!p || !v1_ms || !lgn_ms) return PV1_E_ARG;
+    if (!p->lgnReady || !p->stimReady || !p->haveState || !p->haveRng || !p->haveNear || !p->haveLGNsyn)
+        return fail(p, PV1_E_STATE, "plan not ready");
+    const int K = p->K;
+    nsteps = (nsteps / K) * K;
+    if (nsteps == 0) return fail(p, PV1_E_ARG, "nsteps < chunk");
+    std::vector<cudaEvent_t> ev(2 * (nsteps + nsteps / K));
+    for (auto &e : ev) PV1_CUDA(p, cudaEventCreate(&e));
+    PV1_CUDA(p, cudaMemcpyAsync(p->d_stepBase, &p->step, sizeof(long long), cudaMemcpyHostToDevice, p->stream));
+    size_t q = 0;
+    for (uint32_t c = 0; c < nsteps / K; c++) {
+        PV1_CUDA(p, cudaEventRecord(ev[q++], p->stream));
+        PV1_CUDA(p, launch_lgn_step(p->lp, p->d_stepBase, K, p->stream));
+        PV1_CUDA(p, cudaEventRecord(ev[q++], p->stream));
+        for (int s = 0; s < K; s++) {
+            const int deliver = (c == 0 && s == 0) ? (p->pending ? 1 : 0) : 1;
+            PV1_CUDA(p, cudaEventRecord(ev[q++], p->stream));
+            PV1_CUDA(p, launch_v1_step(p->vp, p->d_stepBase, s, p->d_lgnRing, p->lgnSlots, deliver, 1, p->stream));
+            PV1_CUDA(p, cudaEventRecord(ev[q++], p->stream));
+        }
+        PV1_CUDA(p, launch_advance_step(p->d_stepBase, K, p->stream));
+    }
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    double tl = 0, tv = 0;
+    q = 0;
+    for (uint32_t c = 0; c < nsteps / K; c++) {
+        float ms;
+        PV1_CUDA(p, cudaEventElapsedTime(&ms, ev[q], ev[q + 1]));
+        tl += ms;
+        q += 2;
+        for (int s = 0; s < K; s++) {
+            PV1_CUDA(p, cudaEventElapsedTime(&ms, ev[q], ev[q + 1]));
+            tv += ms;
+            q += 2;
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    p->step += nsteps;
+    p->pending = true;
+    *v1_ms = (float)(tv / nsteps);
+    *lgn_ms = (float)(tl / (nsteps / K));
+    if (chunk) *chunk = K;
+    return check_device_error(p);
+}
+
+// Applies the delivery of the last step's spikes (kept pending so that the next step can
+// fuse it), so that g/h and the last record are complete.
+static int flush_delivery(pv1_plan *p) {
+    if (!p->pending) return PV1_OK;
+    PV1_CUDA(p, cudaMemcpyAsync(p->d_stepBase, &p->step, sizeof(long long), cudaMemcpyHostToDevice, p->stream));
+    PV1_CUDA(p, launch_v1_step(p->vp, p->d_stepBase, 0, p->d_lgnRing, p->lgnSlots, 1, 0, p->stream));
+    p->pending = false;
+    return check_device_error(p);
+}
+
+int pv1_fetch_records(pv1_plan *p, uint64_t step0, uint32_t n, float *raw, float *lgn_sp, float *lgn_fr) {
+    if (!p) return PV1_E_ARG;
+    if (!p->recFlags) return fail(p, PV1_E_STATE, "recording is off");
+    if (step0 + n > (uint64_t)p->step) return fail(p, PV1_E_ARG, "records not produced yet");
+    if ((uint64_t)p->step - step0 > (uint64_t)p->recSlots) return fail(p, PV1_E_ARG, "records already overwritten");
+    if (step0 + n == (uint64_t)p->step) {
+        int r = flush_delivery(p);  // completes the g/h of the last record
+        if (r) return r;
+    }
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    for (uint32_t s = 0; s < n; s++) {
+        const uint64_t t = step0 + s;
+        if (raw && (p->recFlags & PV1_REC_RAW)) {
+            const size_t slot = t % p->recSlots;
+            PV1_CUDA(p, cudaMemcpy(raw + (size_t)s * p->recStride, p->d_rec + slot * p->recStride,
+                                   (p->recStride - (long long)p->nI * p->cfg.nblock) * sizeof(float),
+                                   cudaMemcpyDeviceToHost));
+            // gap junction values (InhGap is not built): zero
+            std::fill(raw + (size_t)s * p->recStride + (p->recStride - (long long)p->nI * p->cfg.nblock),
+                      raw + (size_t)(s + 1) * p->recStride, 0.0f);
+        }
+        const size_t lrow = t % p->lgnSlots;
+        if (lgn_sp && (p->recFlags & PV1_REC_LGN_SP))
+            PV1_CUDA(p, cudaMemcpy(lgn_sp + (size_t)s * p->nLGN, p->d_lgnRing + lrow * p->nLGN,
+                                   p->nLGN * sizeof(float), cudaMemcpyDeviceToHost));
+        if (lgn_fr && (p->recFlags & PV1_REC_LGN_FR))
+            PV1_CUDA(p, cudaMemcpy(lgn_fr + (size_t)s * p->nLGN, p->d_lgnFr + lrow * p->nLGN,
+                                   p->nLGN * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    return PV1_OK;
+}
+
+int pv1_get_state(pv1_plan *p, int which, float *out) {
+    if (!p || !out) return PV1_E_ARG;
+    int r = flush_delivery(p);
+    if (r) return r;
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    const size_t n = p->nV1;
+    const pv1_v1_config &c = p->cfg;
+    const V1Params &v = p->vp;
+    const void *src = nullptr;
+    size_t cnt = n;
+    switch (which) {
+        case PV1_ST_V: src = v.v; break;
+        case PV1_ST_W: src = v.w; break;
+        case PV1_ST_TBACK: src = v.tBack; break;
+        case PV1_ST_DEP: src = v.dep; break;
+        case PV1_ST_GFF: src = v.gFF; cnt = c.ngFF * n; break;
+        case PV1_ST_HFF: src = v.hFF; cnt = c.ngFF * n; break;
+        case PV1_ST_GE: src = v.gE; cnt = c.ngE * n; break;
+        case PV1_ST_HE: src = v.hE; cnt = c.ngE * n; break;
+        case PV1_ST_GI: src = v.gI; cnt = c.ngI * n; break;
+        case PV1_ST_HI: src = v.hI; cnt = c.ngI * n; break;
+        case PV1_ST_SINFO:
+            if (p->step == 0) return fail(p, PV1_E_STATE, "no step run yet");
+            src = v.sInfo + (size_t)((p->step - 1) & 1) * n;
+            break;
+        case PV1_ST_LGN_LTR: src = p->lp.leftTimeRate; cnt = p->nLGN; break;
+        case PV1_ST_LGN_LNL: src = p->lp.lastNegLogRand; cnt = p->nLGN; break;
+        case PV1_ST_LGN_SINFO:
+            if (p->step == 0) return fail(p, PV1_E_STATE, "no step run yet");
+            src = p->d_lgnRing + (size_t)((p->step - 1) % p->lgnSlots) * p->nLGN;
+            cnt = p->nLGN;
+            break;
+        default: return fail(p, PV1_E_ARG, "unknown state id");
+    }
+    if (!src) return fail(p, PV1_E_STATE, "state not allocated");
+    PV1_CUDA(p, cudaMemcpy(out, src, cnt * sizeof(float), cudaMemcpyDeviceToHost));
+    return PV1_OK;
+}
+
+int pv1_put_state(pv1_plan *p, int which, const float *in) {
+    if (!p || !in) return PV1_E_ARG;
+    int r = flush_delivery(p);
+    if (r) return r;
+    const size_t n = p->nV1;
+    const pv1_v1_config &c = p->cfg;
+    const V1Params &v = p->vp;
+    void *dst = nullptr;
+    size_t cnt = n;
+    switch (which) {
+        case PV1_ST_V: dst = v.v; break;
+        case PV1_ST_W: dst = v.w; break;
+        case PV1_ST_TBACK: dst = v.tBack; break;
+        case PV1_ST_GFF: dst = v.gFF; cnt = c.ngFF * n; break;
+        case PV1_ST_HFF: dst = v.hFF; cnt = c.ngFF * n; break;
+        case PV1_ST_GE: dst = v.gE; cnt = c.ngE * n; break;
+        case PV1_ST_HE: dst = v.hE; cnt = c.ngE * n; break;
+        case PV1_ST_GI: dst = v.gI; cnt = c.ngI * n; break;
+        case PV1_ST_HI: dst = v.hI; cnt = c.ngI * n; break;
+        case PV1_ST_LGN_LTR: dst = p->lp.leftTimeRate; cnt = p->nLGN; break;
+        case PV1_ST_LGN_LNL: dst = p->lp.lastNegLogRand; cnt = p->nLGN; break;
+        default: return fail(p, PV1_E_ARG, "state id cannot be written");
+    }
+    if (!dst) return fail(p, PV1_E_STATE, "state not allocated");
+    PV1_CUDA(p, cudaMemcpy(dst, in, cnt * sizeof(float), cudaMemcpyHostToDevice));
+    return PV1_OK;
+}
+
+int pv1_set_draw_record(pv1_plan *p, uint32_t steps, uint32_t cap) {
+    if (!p) return PV1_E_ARG;
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    V1Params &v = p->vp;
+    LgnParams &L = p->lp;
+    void *old[] = {L.recU, L.recUCount, v.recNoise, v.recFF, v.recFFCount, v.recNear, v.recNearCount};
+    for (void *o : old)
+        if (o) free_one(p, o);
+    L.recU = nullptr; L.recUCount = nullptr;
+    v.recNoise = v.recFF = v.recNear = nullptr;
+    v.recFFCount = v.recNearCount = nullptr;
+    if (steps == 0 || cap == 0) {
+        drop_graph(p);
+        return PV1_OK;
+    }
+    int r = 0;
+    const size_t nV1 = p->nV1, nLGN = std::max(p->nLGN, 1);
+    r |= dev_alloc(p, &L.recU, steps * nLGN * cap);
+    r |= dev_alloc(p, &L.recUCount, steps * nLGN);
+    r |= dev_alloc(p, &v.recNoise, steps * nV1);
+    r |= dev_alloc(p, &v.recFF, steps * nV1 * cap);
+    r |= dev_alloc(p, &v.recFFCount, steps * nV1);
+    r |= dev_alloc(p, &v.recNear, steps * nV1 * cap);
+    r |= dev_alloc(p, &v.recNearCount, steps * nV1);
+    if (r) return r;
+    L.recCap = v.recCap = (int)cap;
+    L.recSteps = v.recSteps = (int)steps;
+    L.recStep0 = v.recStep0 = p->step;
+    drop_graph(p);
+    return PV1_OK;
+}
+
+int pv1_fetch_draws(pv1_plan *p, int kind, float *draws, int32_t *counts) {
+    if (!p) return PV1_E_ARG;
+    int r = flush_delivery(p);
+    if (r) return r;
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    const V1Params &v = p->vp;
+    const LgnParams &L = p->lp;
+    if (!v.recNoise) return fail(p, PV1_E_STATE, "draw recording is off");
+    const size_t steps = v.recSteps, cap = v.recCap, nV1 = p->nV1, nLGN = std::max(p->nLGN, 1);
+    const void *src = nullptr, *csrc = nullptr;
+    size_t cnt = 0, ccnt = 0;
+    switch (kind) {
+        case 0: src = L.recU; cnt = steps * nLGN * cap; csrc = L.recUCount; ccnt = steps * nLGN; break;
+        case 1: src = v.recNoise; cnt = steps * nV1; break;
+        case 2: src = v.recFF; cnt = steps * nV1 * cap; csrc = v.recFFCount; ccnt = steps * nV1; break;
+        case 3: src = v.recNear; cnt = steps * nV1 * cap; csrc = v.recNearCount; ccnt = steps * nV1; break;
+        default: return fail(p, PV1_E_ARG, "unknown draw kind");
+    }
+    if (draws) PV1_CUDA(p, cudaMemcpy(draws, src, cnt * sizeof(float), cudaMemcpyDeviceToHost));
+    if (counts && csrc) PV1_CUDA(p, cudaMemcpy(counts, csrc, ccnt * sizeof(int), cudaMemcpyDeviceToHost));
+    return PV1_OK;
+}
+
+// ---- host initial state (src/patch.cu:4405-4560) -----------------------------------------
+int pv1_host_init_state(const pv1_v1_config *cfg, uint64_t seed, const float *tonicDep,
+                        const uint32_t *nLGNperV1, int use_v0, float tonicMax, const float *w0,
+                        const float *gFF0, const float *gE0, const float *gI0, float *v, float *w,
+                        float *gFF, float *hFF, float *gE, float *hE, float *gI, float *hI) {
+    if (!cfg || !tonicDep || !nLGNperV1 || !v || !gFF || !hFF || !gE || !hE || !gI || !hI || !gFF0 ||
+        !gE0 || !gI0)
+        return PV1_E_ARG;
+    const pv1_v1_config &c = *cfg;
+    const size_t bs = c.blockSize, nblock = c.nblock, nV1 = bs * nblock;
+    const int nType = (int)c.nType;
+    std::vector<size_t> acc(nType + 1, 0);
+    for (int j = 0; j < nType; j++) acc[j + 1] = c.typeAcc[j];
+    std::default_random_engine rGen((std::default_random_engine::result_type)seed);
+    // one normal distribution object shared by every draw, as the reference's function-local
+    // static inside its sampling lambda is (src/patch.cu:4417-4429)
+    std::normal_distribution<float> norm(0.0f, 1.0f);
+    auto sampler = [&](float mean, float std, bool nonNeg) {
+        return [&rGen, &norm, mean, std, nonNeg]() {
+            float r;
+            do {
+                r = norm(rGen) * std + mean;
+            } while (nonNeg && r < 0.0f);
+            return r;
+        };
+    };
+    for (int i = 0; i < nType; i++) {
+        if (c.iModel == 1) {
+            if (!w0 || !w) return PV1_E_ARG;
+            auto get = sampler(w0[i * 2 + 0], w0[i * 2 + 1], false);
+            for (size_t b = 0; b < nblock; b++)
+                std::generate(w + b * bs + acc[i], w + b * bs + acc[i + 1], get);
+        }
+        if (use_v0 || tonicMax > 1.0f) {
+            std::uniform_real_distribution<float> uni(c.vR[i], c.vT[i]);
+            for (size_t b = 0; b < nblock; b++)
+                std::generate(v + b * bs + acc[i], v + b * bs + acc[i + 1], [&]() { return uni(rGen); });
+        } else {
+            for (size_t b = 0; b < nblock; b++)
+                for (size_t j = acc[i]; j < acc[i + 1]; j++)
+                    v[b * bs + j] = c.vR[i] + (c.vT[i] - c.vR[i]) * tonicDep[b * bs + j];
+        }
+    }
+    if (c.iModel != 1 && w) std::fill(w, w + nV1, 0.0f);
+    const int ngFF = (int)c.ngFF, ngE = (int)c.ngE, ngI = (int)c.ngI;
+    for (int i = 0; i < nType; i++) {
+        for (int k = 0; k < ngFF; k++) {
+            const float *q = gFF0 + (size_t)i * ngFF * 4 + k * 4;
+            auto gg = sampler(q[0], q[0] * q[1], true);
+            auto gh = sampler(q[2], q[2] * q[3], true);
+            for (size_t b = 0; b < nblock; b++) {
+                size_t ind = k * nV1 + b * bs;
+                std::generate(gFF + ind + acc[i], gFF + ind + acc[i + 1], gg);
+                std::generate(hFF + ind + acc[i], hFF + ind + acc[i + 1], gh);
+                for (size_t j = acc[i]; j < acc[i + 1]; j++) {
+                    if (nLGNperV1[b * bs + j] == 0) {
+                        gFF[k * nV1 + b * bs + j] = 0;
+                        hFF[k * nV1 + b * bs + j] = 0;
+                    }
+                }
+            }
+        }
+    }
+    for (int i = 0; i < nType; i++) {
+        for (int k = 0; k < ngE; k++) {
+            const float *q = gE0 + (size_t)i * ngE * 4 + k * 4;
+            auto gg = sampler(q[0], q[0] * q[1], true);
+            auto gh = sampler(q[2], q[2] * q[3], true);
+            for (size_t b = 0; b < nblock; b++) {
+                size_t off = k * nV1 + b * bs;
+                std::generate(gE + off + acc[i], gE + off + acc[i + 1], gg);
+                std::generate(hE + off + acc[i], hE + off + acc[i + 1], gh);
+            }
+        }
+        for (int k = 0; k < ngI; k++) {
+            const float *q = gI0 + (size_t)i * ngI * 4 + k * 4;
+            auto gg = sampler(q[0], q[0] * q[1], true);
+            auto gh = sampler(q[2], q[2] * q[3], true);
+            for (size_t b = 0; b < nblock; b++) {
+                size_t off = k * nV1 + b * bs;
+                std::generate(gI + off + acc[i], gI + off + acc[i + 1], gg);
+                std::generate(hI + off + acc[i], hI + off + acc[i + 1], gh);
+            }
+        }
+    }
+    return PV1_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,296 @@
+"""Seeded synthetic workloads in the reference's input layouts.
+
+No dataset or connectome ships with the reference, so every workload is generated here from
+a seed: a V1 sheet of blocks, Gaussian distance-dependent recurrent connectivity (a dense
+conMat tile per block, a sparse far list with distance delays), ON/OFF magno LGN cells with
+DoG receptive fields, simple-cell-like LGN->V1 wiring, and a drifting-grating stimulus.
+The same objects are written to the reference's file formats by formats.py.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from .model import InitState, LgnSpec, Seeds, Stimulus, V1Network, V1Spec, host_init_state
+from .schedule import make_schedule
+
+f32 = np.float32
+u32 = np.uint32
+DEG = math.pi / 180.0
+
+
+@dataclass
+class Workload:
+    name: str
+    spec: V1Spec
+    net: V1Network
+    lgn: LgnSpec
+    stim: Stimulus
+    init: InitState
+    seeds: Seeds
+    nt: int
+    pos: np.ndarray          # V1 positions [nV1][2] (mm)
+    rf_center: np.ndarray    # V1 RF centers [nV1][2] (deg)
+    rf_orient: np.ndarray    # V1 preferred orientation [nV1] (rad)
+
+
+def make_spec(nblock: int, blockSize: int = 1024, nE: int = 768, dt: float = 0.125,
+              adex_inh: bool = False, vL: float = -65.0, noisyDep=(0.0, 0.0),
+              synFail=(0.0, 0.0, 0.0, 0.0), synFailFF=(0.0, 0.0), noFarDelay: int = 0) -> V1Spec:
+    """Neuron and synapse recipe of the benchmark configurations.
+
+    Conductance-based LIF (gL 0.05/ms, C 1, threshold -50 mV, reset -60 mV, refractory
+    2/1 ms) written as the reference's AdEx with a = b = 0 and vT = vThres; AMPA 1/5 ms,
+    NMDA 2/80 ms (feed-forward and cortical excitation) and GABA 1/7 ms.  With adex_inh the
+    inhibitory type is AdEx (a 0.02, b 0.4, tau_w 150 ms in the normalised units C = 1)."""
+    a_i, b_i = (0.02, 0.4) if adex_inh else (0.0, 0.0)
+    return V1Spec(
+        nblock=nblock, blockSize=blockSize, typeAcc=[nE, blockSize], nTypeE=1,
+        ngFF=2, ngE=2, ngI=1, dt=dt,
+        riseFF=[1.0, 2.0], decayFF=[5.0, 80.0], riseE=[1.0, 2.0], decayE=[5.0, 80.0],
+        riseI=[1.0], decayI=[7.0],
+        vR=[-60.0, -60.0], vThres=[-50.0, -50.0], gL=[0.05, 0.05], C=[1.0, 1.0],
+        tRef=[2.0, 1.0], vT=[-50.0, -50.0], deltaT=[1.0, 1.0], tau_w=[150.0, 150.0],
+        a=[0.0, a_i], b=[0.0, b_i],
+        pFF=[0.8, 0.2, 0.8, 0.2], pE=[0.8, 0.2, 0.8, 0.2], pI=[1.0, 1.0],
+        synFail=list(synFail), synPerCon=[10.0, 10.0, 10.0, 10.0],
+        synFailFF=list(synFailFF), synPerConFF=[10.0, 10.0], noisyDep=list(noisyDep),
+        tau_noise=0.0, noiseOnTonic=True, iModel=1, noDelay=1, noFarDelay=noFarDelay,
+        speedOfThought=1.0, hWrite=True, vE=0.0, vI=-75.0, vL=vL)
+
+
+def grating_frames(nFrame: int, width: int, height: int, extent_deg: float, cpd: float,
+                   tf_hz: float, contrast: float, orient: float, frame_rate: int,
+                   mean: float = 0.5) -> np.ndarray:
+    """Drifting sinusoidal grating, identical L, M, S planes, [nFrame][3][h][w] float32."""
+    xs = (np.arange(width) + 0.5) / width * extent_deg - extent_deg / 2
+    ys = (np.arange(height) + 0.5) / height * extent_deg - extent_deg / 2
+    X, Y = np.meshgrid(xs, ys)
+    proj = X * math.cos(orient) + Y * math.sin(orient)
+    out = np.empty((nFrame, 3, height, width), f32)
+    for f in range(nFrame):
+        t = f / frame_rate
+        img = mean * (1 + contrast * np.sin(2 * math.pi * (cpd * proj - tf_hz * t)))
+        out[f, :] = img.astype(f32)
+    return out
+
+
+def make_lgn(n_lgn: int, rng: np.random.Generator, patch_deg: float, dt: float,
+             frame_rate: int = 120, mSample1D: int = 16, mau: float = 250.0,
+             mKernelSample: int = 250, sigma_c: float = 0.03, sigma_s: float = 0.09,
+             stim_range_deg: float | None = None, buffer_deg: float = 0.2,
+             jitter: float = 0.0) -> tuple[LgnSpec, float]:
+    """ON/OFF magno cells with centers uniform in a patch_deg square around the fixation.
+
+    Returns the spec and the full stimulus extent (deg) the texture spans (flat retina)."""
+    nOn = n_lgn // 2
+    xy = rng.uniform(-patch_deg / 2, patch_deg / 2, size=(n_lgn, 2))
+    polar = np.arctan2(xy[:, 1], xy[:, 0])
+    ecc = np.hypot(xy[:, 0], xy[:, 1]) * DEG
+    max_ecc = float(np.max(np.hypot(xy[:, 0], xy[:, 1])))
+    if stim_range_deg is None:
+        stim_range_deg = max(max_ecc, patch_deg / 2) * 1.05
+    extent = 2 * (stim_range_deg + buffer_deg)
+    norm_ecc_max = max_ecc / extent
+    normViewDistance = norm_ecc_max / max_ecc / DEG
+    sc = sigma_c * (1 + jitter * rng.uniform(-1, 1, n_lgn))
+    ss = sigma_s * (1 + jitter * rng.uniform(-1, 1, n_lgn))
+    two = lambda c, s: np.concatenate([c, s]).astype(f32)
+    types = np.where(np.arange(n_lgn) < nOn, 4, 5)
+    k_center = np.where(types == 4, 60.0, -60.0)
+    sched = make_schedule(dt, frame_rate, mau, mau, mKernelSample, mKernelSample)
+    spec = LgnSpec(
+        nParvo_I=0, nMagno_I=n_lgn, nParvo_C=0, nMagno_C=0, mSample1D=mSample1D, sched=sched,
+        polar=two(polar, polar), ecc=two(ecc, ecc), rw=two(sc * DEG, ss * DEG),
+        rh=two(sc * DEG, ss * DEG), orient=two(np.zeros(n_lgn), np.zeros(n_lgn)),
+        k=two(k_center, -k_center), ratio=two(np.full(n_lgn, 1.0), np.full(n_lgn, 1.0)),
+        tauR=two(np.full(n_lgn, 1.5), np.full(n_lgn, 1.5)),
+        tauD=two(np.full(n_lgn, 4.5), np.full(n_lgn, 4.5)),
+        nR=two(np.full(n_lgn, 19.0), np.full(n_lgn, 19.0)),
+        nD=two(np.full(n_lgn, 9.5), np.full(n_lgn, 9.5)),
+        delay=two(np.full(n_lgn, 14.0), np.full(n_lgn, 14.0)),
+        spont=np.full(n_lgn, 0.1, f32), c50=np.full(n_lgn, 0.25, f32),
+        sharpness=np.full(n_lgn, 3.0, f32),
+        coneType=np.full(2 * n_lgn, 3, u32),
+        normViewDistance=normViewDistance, L_x0=0.5, L_y0=0.5, R_x0=1.0, R_y0=1.0,
+        nsig=3.0, convolRatio=1.0, frRatio=1.0, flat_retina=True)
+    spec.types = types
+    spec.xy = xy
+    return spec, extent
+
+
+def block_positions(nblock: int, blockSize: int, side_mm: float, rng: np.random.Generator,
+                    nbx: int | None = None):
+    """Jittered-grid positions, blocks tiled on a sheet; returns pos [nV1][2] in mm."""
+    g = int(math.ceil(math.sqrt(blockSize)))
+    if nbx is None:
+        nbx = int(math.ceil(math.sqrt(nblock)))
+    pos = np.empty((nblock * blockSize, 2))
+    for b in range(nblock):
+        bx, by = b % nbx, b // nbx
+        cells = rng.permutation(g * g)[:blockSize]
+        gx, gy = cells % g, cells // g
+        jit = rng.uniform(0, 1, size=(blockSize, 2))
+        pos[b * blockSize:(b + 1) * blockSize, 0] = (bx + (gx + jit[:, 0]) / g) * side_mm
+        pos[b * blockSize:(b + 1) * blockSize, 1] = (by + (gy + jit[:, 1]) / g) * side_mm
+    return pos, nbx
+
+
+def near_conmat(spec: V1Spec, pos: np.ndarray, rng: np.random.Generator, sigma: float,
+                nE_partners: float, nI_partners: float, wE: float, wI: float,
+                side_mm: float) -> np.ndarray:
+    """Dense-probabilistic within-block tiles conMat[b][0][pre][post] (self block only)."""
+    bs, nE = spec.blockSize, spec.nE
+    nI = bs - nE
+    area = side_mm * side_mm
+    p0E = min(1.0, nE_partners / ((nE / area) * 2 * math.pi * sigma * sigma))
+    p0I = min(1.0, nI_partners / ((nI / area) * 2 * math.pi * sigma * sigma))
+    out = np.zeros((spec.nblock, 1, bs, bs), f32)
+    for b in range(spec.nblock):
+        P = pos[b * bs:(b + 1) * bs]
+        d2 = ((P[:, None, :] - P[None, :, :]) ** 2).sum(-1)   # [pre][post]
+        p = np.exp(-d2 / (2 * sigma * sigma))
+        p[:nE] *= p0E
+        p[nE:] *= p0I
+        np.fill_diagonal(p, 0.0)
+        conn = rng.uniform(size=p.shape) < p
+        w = rng.lognormal(0.0, 0.5, size=p.shape)
+        w[:nE] *= wE
+        w[nE:] *= wI
+        out[b, 0] = np.where(conn, w, 0.0).astype(f32)
+    return out
+
+
+def far_vectors(spec: V1Spec, pos: np.ndarray, rng: np.random.Generator, n_partners: int,
+                sigma: float, wE: float, wI: float, side_mm: float, nbx: int):
+    """~n_partners Gaussian-distance partners per neuron from other blocks (V1_vec lists)."""
+    bs, nV1 = spec.blockSize, spec.nV1
+    nby = int(math.ceil(spec.nblock / nbx))
+    g = int(math.ceil(math.sqrt(bs)))
+    # lookup from (block, grid cell) to neuron id, built from the jittered grid positions
+    cell_of = np.full((spec.nblock, g * g), -1, np.int64)
+    bx = np.minimum((pos[:, 0] / side_mm).astype(int), nbx - 1)
+    by = np.minimum((pos[:, 1] / side_mm).astype(int), nby - 1)
+    gx = np.minimum(((pos[:, 0] / side_mm - bx) * g).astype(int), g - 1)
+    gy = np.minimum(((pos[:, 1] / side_mm - by) * g).astype(int), g - 1)
+    blk = np.arange(nV1) // bs
+    cell_of[blk, gy * g + gx] = np.arange(nV1)
+    ncand = n_partners * 3
+    nVec = np.zeros(nV1, u32)
+    ids, ws, ds = [], [], []
+    chunk = 4096
+    for s in range(0, nV1, chunk):
+        e = min(nV1, s + chunk)
+        P = pos[s:e]
+        loc = P[:, None, :] + rng.normal(0, sigma, size=(e - s, ncand, 2))
+        cbx = np.floor(loc[..., 0] / side_mm).astype(int)
+        cby = np.floor(loc[..., 1] / side_mm).astype(int)
+        ok = (cbx >= 0) & (cbx < nbx) & (cby >= 0) & (cby < nby)
+        cb = np.where(ok, cby * nbx + cbx, 0)
+        ok &= cb < spec.nblock
+        cgx = np.clip(((loc[..., 0] / side_mm - cbx) * g).astype(int), 0, g - 1)
+        cgy = np.clip(((loc[..., 1] / side_mm - cby) * g).astype(int), 0, g - 1)
+        cand = np.where(ok, cell_of[np.where(ok, cb, 0), cgy * g + cgx], -1)
+        own = (np.arange(s, e) // bs)[:, None]
+        cand = np.where((cand >= 0) & (cand // bs != own), cand, -1)
+        for r in range(e - s):
+            c = cand[r]
+            c = c[c >= 0]
+            _, first = np.unique(c, return_index=True)
+            c = c[np.sort(first)][:n_partners]
+            i = s + r
+            nVec[i] = len(c)
+            d = np.sqrt(((pos[c] - pos[i]) ** 2).sum(-1))
+            w = rng.lognormal(0.0, 0.5, size=len(c)) * np.where((c % bs) < spec.nE, wE, wI)
+            ids.append(c.astype(u32))
+            ws.append(w.astype(f32))
+            ds.append(d.astype(f32))
+    return (nVec, np.concatenate(ids) if ids else np.zeros(0, u32),
+            np.concatenate(ws) if ws else np.zeros(0, f32),
+            np.concatenate(ds) if ds else np.zeros(0, f32))
+
+
+def lgn_to_v1(spec: V1Spec, lgn: LgnSpec, rng: np.random.Generator, m: int, w: float,
+              patch_deg: float, sub_offset_deg: float = 0.05):
+    """Simple-cell wiring: half ON cells near c + d*u, half OFF near c - d*u."""
+    nV1 = spec.nV1
+    xy = lgn.xy
+    on = np.nonzero(lgn.types == 4)[0]
+    off = np.nonzero(lgn.types == 5)[0]
+    centers = rng.uniform(-patch_deg / 2 * 0.8, patch_deg / 2 * 0.8, size=(nV1, 2))
+    orient = rng.uniform(0, math.pi, nV1)
+    u = np.stack([np.cos(orient + math.pi / 2), np.sin(orient + math.pi / 2)], -1)
+    from scipy.spatial import cKDTree
+    mo = m // 2
+    _, kon = cKDTree(xy[on]).query(centers + sub_offset_deg * u, k=mo)
+    _, koff = cKDTree(xy[off]).query(centers - sub_offset_deg * u, k=m - mo)
+    kon = np.asarray(kon).reshape(nV1, mo)
+    koff = np.asarray(koff).reshape(nV1, m - mo)
+    ids = np.concatenate([on[kon], off[koff]], axis=1).T.astype(u32).copy()
+    s = (w * rng.uniform(0.5, 1.5, size=(m, nV1))).astype(f32)
+    return np.full(nV1, m, u32), ids, s, centers, orient
+
+
+def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int = 512,
+                  m: int = 20, width: int = 64, height: int = 64, nt: int = 8000,
+                  orient: float = 0.0, contrast: float = 0.5, far_partners: int = 0,
+                  adex_inh: bool = False, patch_deg: float = 2.0, nFrame: int = 120,
+                  wFF: float = 0.25, wE: float = 0.006, wI: float = 0.3, wFar: float = 0.002,
+                  noisyDep=(0.0, 0.0), synFail=(0.0, 0.0, 0.0, 0.0), synFailFF=(0.0, 0.0),
+                  mSample1D: int = 16, dt: float = 0.125) -> Workload:
+    """Builds one synthetic patch; C1 = 1x1024 V1 / 512 LGN; C2 = 32 blocks / 16384 LGN."""
+    rng = np.random.default_rng(seed)
+    spec = make_spec(nblock, adex_inh=adex_inh, noisyDep=noisyDep, synFail=synFail,
+                     synFailFF=synFailFF, dt=dt)
+    lgn, extent = make_lgn(n_lgn, rng, patch_deg, dt, mSample1D=mSample1D)
+    side = 0.5
+    pos, nbx = block_positions(nblock, spec.blockSize, side, rng)
+    conMat = near_conmat(spec, pos, rng, sigma=0.1, nE_partners=100, nI_partners=50,
+                         wE=wE, wI=wI, side_mm=side)
+    if far_partners > 0 and nblock > 1:
+        nVec, vecID, conVec, delayVec = far_vectors(spec, pos, rng, far_partners, 0.3,
+                                                    wE=wFar, wI=4 * wFar, side_mm=side, nbx=nbx)
+    else:
+        nVec = np.zeros(spec.nV1, u32)
+        vecID, conVec, delayVec = np.zeros(0, u32), np.zeros(0, f32), np.zeros(0, f32)
+    nLGNperV1, lgnId, sLGN, rfc, rfo = lgn_to_v1(spec, lgn, rng, m, wFF, patch_deg)
+    tonic = np.where(spec.type_of(np.arange(spec.nV1) % spec.blockSize) == 0,
+                     rng.uniform(0.3, 0.6, spec.nV1), rng.uniform(0.4, 0.7, spec.nV1)).astype(f32)
+    net = V1Network(nLGNperV1=nLGNperV1, lgnId=lgnId, sLGN=sLGN,
+                    nNearNB=np.ones(nblock, u32), nbId=np.arange(nblock, dtype=u32)[:, None].copy(),
+                    conMat=conMat, nVec=nVec, vecID=vecID, conVec=conVec, delayVec=delayVec,
+                    tonicDep=tonic)
+    frames = grating_frames(nFrame, width, height, extent, cpd=4.0, tf_hz=8.0,
+                            contrast=contrast, orient=orient, frame_rate=120)
+    stim = Stimulus(frames=frames, init_LMS=(0.5, 0.5, 0.5))
+    # seed sequence of src/patch.cu: logRand_init(seed), per-neuron host engines, init, spInit
+    s_lgn = seed
+    s_init = seed + 1 + spec.nV1
+    s_sp = s_init + 1
+    gFF0 = np.tile([0.01, 0.2, 0.0, 0.2], spec.nType * spec.ngFF).astype(f32)
+    gE0 = np.tile([0.005, 0.2, 0.0, 0.2], spec.nType * spec.ngE).astype(f32)
+    gI0 = np.tile([0.01, 0.2, 0.0, 0.2], spec.nType * spec.ngI).astype(f32)
+    w0 = np.tile([0.0, 0.0], spec.nType).astype(f32)
+    init = host_init_state(spec, s_init, tonic, nLGNperV1, None, w0, gFF0, gE0, gI0)
+    max_delay = float(delayVec.max()) if delayVec.size else 0.0
+    trainDepth = int(math.ceil(max(max_delay, 0.0) / spec.speedOfThought / spec.dt)) + 1
+    seeds = Seeds(lgn=s_lgn, cond=s_sp, trainDepth=max(trainDepth, 2))
+    return Workload(name=name, spec=spec, net=net, lgn=lgn, stim=stim, init=init, seeds=seeds,
+                    nt=nt, pos=pos, rf_center=rfc, rf_orient=rfo)
+
+
+def config1(seed: int = 0, **kw) -> Workload:
+    """1 block of 1024 V1 neurons (768 E / 256 I), 512 LGN, 64x64 frames, 1 s at 0.125 ms."""
+    return make_workload("C1: 1x1024 V1, 512 LGN, 64x64 grating", seed=seed, nblock=1,
+                         n_lgn=512, m=20, width=64, height=64, nt=8000, **kw)
+
+
+def config2(seed: int = 0, orient: float = 0.0, **kw) -> Workload:
+    """32 blocks x 1024 = 32768 V1 (80% LIF E / 20% AdEx I), 16384 LGN, 128x128 frames,
+    ~400 far partners per neuron, 2 s at 0.125 ms."""
+    return make_workload("C2: 32x1024 V1, 16384 LGN, 128x128 grating, 400 far partners",
+                         seed=seed, nblock=32, n_lgn=16384, m=20, width=128, height=128,
+                         nt=16000, orient=orient, far_partners=400, adex_inh=True,
+                         patch_deg=4.0, nFrame=240, **kw)

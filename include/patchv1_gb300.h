@@ -246,10 +246,16 @@ int64_t pv1_last_launch_count(const pv1_plan *plan);
  * events on the plan's stream; *ms receives the device time of the run alone. */
 int pv1_run_timed(pv1_plan *plan, uint32_t nsteps, uint64_t flush_bytes, float *ms);
 
-/* Runs nsteps with one direct launch per kernel, each bracketed by CUDA events on the plan's
- * stream; returns the mean device time per launch of the V1 step kernel and of the LGN
- * rate+spike pair (per chunk of `chunk` steps; one chunk per `chunk` steps). */
+/* Runs nsteps (rounded down to whole chunks of `chunk` steps) with direct launches, CUDA
+ * events on the plan's stream around the LGN rate+spike pair and around the V1 work of each
+ * chunk; returns the mean V1 device time per simulation step and the mean LGN time per
+ * chunk. */
 int pv1_time_kernels(pv1_plan *plan, uint32_t nsteps, float *v1_ms, float *lgn_ms, int *chunk);
+
+/* allow = 1/0 enables/disables the persistent cooperative V1 kernel (one launch per chunk of
+ * steps, state in registers, bounded grid barrier between steps); allow = -1 only queries.
+ * Returns 1 if the plan steps with the persistent kernel, 0 if with one launch per step. */
+int pv1_persistent_mode(pv1_plan *plan, int allow);
 
 #ifdef __cplusplus
 }

@@ -155,7 +155,7 @@ def first_spike_time_divergence(a_v1, b_v1, a_lgn, b_lgn, tol_tsp):
     return None
 
 
-def compare(res, spec, tol_tsp=1e-3):
+def compare(res, spec, tol_tsp=1e-5):
     """Summary numbers of a parity run (all assertions are left to the caller).
 
     Traces are compared up to the first spike-time divergence: the first step at which a

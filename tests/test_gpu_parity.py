@@ -4,10 +4,11 @@ Tolerances (written here, from the target of the port):
   * LGN setup tables (TW, SW, SC, max_convol): 1e-5 relative (fp32 reductions in a
     different order).
   * membrane and conductance traces: 1e-5 relative until the first spike-time divergence
-    (a spike present on both sides whose time differs by more than 1e-3 of a step, or a
+    (a spike present on both sides whose time differs by more than 1e-5 of a step, or a
     spike present on one side only); the LGN generator's carried rate integral is
     ill-conditioned (lastNegLogRand - leftTimeRate), so ulp-level rate differences move LGN
-    spike times by ~1e-4 of a step, which is why the criterion is on spike times;
+    spike times by up to ~1e-4 of a step, and the unit conductance of a spike late in a step
+    is as sensitive to its time, which is why the criterion is tied to spike times;
   * membrane traces: 1e-3 relative over the whole raster window;
   * spike rasters: identical over the first 50 ms (400 steps at dt = 0.125 ms).
 """
@@ -125,6 +126,28 @@ def test_far_delivery_parity(native):
     assert_raster_ok(cmp)
     for k in ("v", "gE", "gI"):
         assert cmp[f"max_rel_{k}"] < 1e-5, cmp
+
+
+def test_persistent_equals_per_step_launches(native):
+    """The cooperative persistent kernel (state in registers, grid barrier between steps)
+    and one launch per step produce bit-identical states, far delivery included."""
+    from visual_cortex_gb300 import synth
+    from visual_cortex_gb300.model import Simulation
+    wl = synth.make_workload("far4", seed=7, nblock=4, n_lgn=1024, m=20, width=64, height=64,
+                             nt=800, far_partners=100, adex_inh=True, patch_deg=2.0, nFrame=120,
+                             wFar=0.01, noisyDep=(0.1, 0.1), synFailFF=(0.05, 0.05))
+    a = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    b = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        assert a.persistent(1)
+        assert not b.persistent(0)
+        a.run(300)
+        b.run(300)
+        for k in ("v", "w", "gE", "hE", "gI", "hI", "gFF", "hFF", "tBack", "lgn_lnl"):
+            np.testing.assert_array_equal(a.state(k), b.state(k), err_msg=k)
+    finally:
+        a.close()
+        b.close()
 
 
 def test_chunked_runs_identical(c1_small):

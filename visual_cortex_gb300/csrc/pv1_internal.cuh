@@ -22,6 +22,7 @@ constexpr int kErrRecordOverflow = 1;   // a draw record ran out of capacity
 constexpr int kErrNegTsp = 2;           // interpolated spike time < 0 or NaN
 constexpr int kErrFarOverflow = 4;      // far event beyond the delay ring
 constexpr int kErrBounds = 8;           // an index failed its bounds check
+constexpr int kErrBarrier = 16;         // a grid barrier gave up waiting
 
 // Two-state (g, h) conductance kernel with rise and decay times: the kinetics of the
 // reference's ConductanceShape (src/condShape.h:13-41).  dod = tr/(td - tr).
@@ -180,6 +181,9 @@ cudaError_t launch_v1_step(const V1Params &p, const long long *stepBase, int ste
                            cudaStream_t st);
 cudaError_t launch_v1_rng_init(curandStateMRG32k3a *cond, curandStateMRG32k3a *noisy,
                                unsigned long long seed, int nV1, int trainDepth, cudaStream_t st);
+int v1_persistent_ctas(const V1Params &p, int device, bool *fits);
+cudaError_t launch_v1_persistent(const V1Params &p, const long long *stepBase, int K, const float *lgnRing,
+                                 int lgnSlots, int deliverFirst, unsigned *barrier, cudaStream_t st);
 cudaError_t launch_advance_step(long long *stepBase, int k, cudaStream_t st);
 
 // Fixed-point scale for far-delivery accumulation: integer adds are associative, so the

@@ -38,7 +38,12 @@ struct pv1_plan {
     // LGN spike ring
     float *d_lgnRing = nullptr, *d_lgnFr = nullptr;
     int lgnSlots = 0;
-    int K = 32;  // steps per LGN launch / per graph
+    int K = 64;  // steps per LGN launch / per persistent V1 launch / per graph
+    bool persistent = false;     // V1 steps run as one cooperative launch per chunk
+    bool allowPersistent = true;
+    unsigned *d_barrier = nullptr;
+    bool modeChosen = false;
+    long long graphLaunches = 0;
     // stepping
     long long step = 0;
     bool pending = false;
@@ -113,23 +118,36 @@ int check_device_error(pv1_plan *p) {
 }
 
 void drop_graph(pv1_plan *p) {
+    p->modeChosen = false;
     if (p->graphExec) {
         cudaGraphExecDestroy(p->graphExec);
         p->graphExec = nullptr;
     }
 }
 
-// Issues k steps (one LGN launch, k V1 launches, one counter bump) on the plan's stream.
-int issue_chunk(pv1_plan *p, int k, int deliverFirst) {
+// Issues k steps on the plan's stream: the LGN rate+spike pair for the k steps, then either
+// one persistent cooperative V1 launch for all k steps or k per-step V1 launches, then the
+// step-counter bump.  Returns the number of kernel launches through *launches.
+int issue_chunk(pv1_plan *p, int k, int deliverFirst, long long *launches) {
     cudaError_t e = launch_lgn_step(p->lp, p->d_stepBase, k, p->stream);
     if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("lgn_step: ") + cudaGetErrorString(e));
-    for (int s = 0; s < k; s++) {
-        int deliver = (s == 0) ? deliverFirst : 1;
-        e = launch_v1_step(p->vp, p->d_stepBase, s, p->d_lgnRing, p->lgnSlots, deliver, 1, p->stream);
-        if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("v1_step: ") + cudaGetErrorString(e));
+    long long n = 2;
+    if (p->persistent) {
+        e = launch_v1_persistent(p->vp, p->d_stepBase, k, p->d_lgnRing, p->lgnSlots, deliverFirst, p->d_barrier,
+                                 p->stream);
+        if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("v1_persistent: ") + cudaGetErrorString(e));
+        n += 1;
+    } else {
+        for (int s = 0; s < k; s++) {
+            int deliver = (s == 0) ? deliverFirst : 1;
+            e = launch_v1_step(p->vp, p->d_stepBase, s, p->d_lgnRing, p->lgnSlots, deliver, 1, p->stream);
+            if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("v1_step: ") + cudaGetErrorString(e));
+        }
+        n += k;
     }
     e = launch_advance_step(p->d_stepBase, k, p->stream);
     if (e != cudaSuccess) return fail(p, PV1_E_CUDA, cudaGetErrorString(e));
+    if (launches) *launches += n + 1;
     return PV1_OK;
 }
 
@@ -779,6 +797,22 @@ int64_t pv1_raw_record_floats(const pv1_plan *p) {
     return fl + mI;
 }
 
+// Chooses between the persistent cooperative V1 kernel and per-step launches (once the
+// connectivity is known): persistent when every CTA can be resident at once and the LGN
+// synapse lists fit in registers.
+static int choose_mode(pv1_plan *p) {
+    if (p->modeChosen) return PV1_OK;
+    bool fits = false;
+    v1_persistent_ctas(p->vp, p->device, &fits);
+    p->persistent = fits && p->allowPersistent;
+    if (p->persistent && !p->d_barrier) {
+        int r = dev_alloc(p, &p->d_barrier, 2);
+        if (r) return r;
+    }
+    p->modeChosen = true;
+    return PV1_OK;
+}
+
 int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
     if (!p) return PV1_E_ARG;
     if (!p->lgnReady || !p->stimReady) return fail(p, PV1_E_STATE, "LGN/stimulus not loaded");
@@ -786,40 +820,51 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
         return fail(p, PV1_E_STATE, "V1 synapses/connectivity/state/rng not set");
     if (p->recFlags && nsteps > (uint32_t)(p->recSlots - 1))
         return fail(p, PV1_E_ARG, "run longer than the record ring; fetch records in between");
+    int r = choose_mode(p);
+    if (r) return r;
     p->launches = 0;
     PV1_CUDA(p, cudaMemcpyAsync(p->d_stepBase, &p->step, sizeof(long long), cudaMemcpyHostToDevice, p->stream));
     uint32_t done = 0;
-    // the first chunk of a run without a pending delivery cannot come from the graph
+    const int K = p->K;
+    // the first chunk of a run without a pending delivery differs from the captured one
     if (!p->pending && nsteps > 0) {
-        int k = (int)std::min<uint32_t>(nsteps, (uint32_t)p->K);
-        int r = issue_chunk(p, k, 0);
+        int k = (int)std::min<uint32_t>(nsteps, (uint32_t)K);
+        r = issue_chunk(p, k, 0, &p->launches);
         if (r) return r;
-        p->launches += k + 3;
         done += k;
     }
-    const int K = p->K;
     if (nsteps - done >= (uint32_t)K) {
-        if (!p->graphExec) {
-            cudaGraph_t g;
-            PV1_CUDA(p, cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
-            int r = issue_chunk(p, K, 1);
-            cudaError_t e2 = cudaStreamEndCapture(p->stream, &g);
-            if (r) return r;
-            if (e2 != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("capture: ") + cudaGetErrorString(e2));
-            PV1_CUDA(p, cudaGraphInstantiate(&p->graphExec, g, 0));
-            cudaGraphDestroy(g);
-        }
-        while (nsteps - done >= (uint32_t)K) {
-            PV1_CUDA(p, cudaGraphLaunch(p->graphExec, p->stream));
-            p->launches += K + 3;
-            done += K;
+        if (p->persistent) {
+            // a cooperative launch per chunk: issued directly (4 launches per K steps)
+            while (nsteps - done >= (uint32_t)K) {
+                r = issue_chunk(p, K, 1, &p->launches);
+                if (r) return r;
+                done += K;
+            }
+        } else {
+            long long per = 0;
+            if (!p->graphExec) {
+                cudaGraph_t g;
+                PV1_CUDA(p, cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+                r = issue_chunk(p, K, 1, &per);
+                cudaError_t e2 = cudaStreamEndCapture(p->stream, &g);
+                if (r) return r;
+                if (e2 != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("capture: ") + cudaGetErrorString(e2));
+                PV1_CUDA(p, cudaGraphInstantiate(&p->graphExec, g, 0));
+                cudaGraphDestroy(g);
+                p->graphLaunches = per;
+            }
+            while (nsteps - done >= (uint32_t)K) {
+                PV1_CUDA(p, cudaGraphLaunch(p->graphExec, p->stream));
+                p->launches += p->graphLaunches;
+                done += K;
+            }
         }
     }
     if (done < nsteps) {
         int k = (int)(nsteps - done);
-        int r = issue_chunk(p, k, 1);
+        r = issue_chunk(p, k, 1, &p->launches);
         if (r) return r;
-        p->launches += k + 3;
         done += k;
     }
     p->step += nsteps;
@@ -881,46 +926,58 @@ int pv1_time_kernels(pv1_plan *p, uint32_t nsteps, float *v1_ms, float *lgn_ms, 
     if (!p || !v1_ms || !lgn_ms) return PV1_E_ARG;
     if (!p->lgnReady || !p->stimReady || !p->haveState || !p->haveRng || !p->haveNear || !p->haveLGNsyn)
         return fail(p, PV1_E_STATE, "plan not ready");
+    int r = choose_mode(p);
+    if (r) return r;
     const int K = p->K;
-    nsteps = (nsteps / K) * K;
-    if (nsteps == 0) return fail(p, PV1_E_ARG, "nsteps < chunk");
-    std::vector<cudaEvent_t> ev(2 * (nsteps + nsteps / K));
+    const uint32_t nchunk = nsteps / K;
+    if (nchunk == 0) return fail(p, PV1_E_ARG, "nsteps < chunk");
+    std::vector<cudaEvent_t> ev(3 * nchunk);
     for (auto &e : ev) PV1_CUDA(p, cudaEventCreate(&e));
     PV1_CUDA(p, cudaMemcpyAsync(p->d_stepBase, &p->step, sizeof(long long), cudaMemcpyHostToDevice, p->stream));
-    size_t q = 0;
-    for (uint32_t c = 0; c < nsteps / K; c++) {
-        PV1_CUDA(p, cudaEventRecord(ev[q++], p->stream));
+    for (uint32_t c = 0; c < nchunk; c++) {
+        const int deliverFirst = (c == 0) ? (p->pending ? 1 : 0) : 1;
+        PV1_CUDA(p, cudaEventRecord(ev[3 * c], p->stream));
         PV1_CUDA(p, launch_lgn_step(p->lp, p->d_stepBase, K, p->stream));
-        PV1_CUDA(p, cudaEventRecord(ev[q++], p->stream));
-        for (int s = 0; s < K; s++) {
-            const int deliver = (c == 0 && s == 0) ? (p->pending ? 1 : 0) : 1;
-            PV1_CUDA(p, cudaEventRecord(ev[q++], p->stream));
-            PV1_CUDA(p, launch_v1_step(p->vp, p->d_stepBase, s, p->d_lgnRing, p->lgnSlots, deliver, 1, p->stream));
-            PV1_CUDA(p, cudaEventRecord(ev[q++], p->stream));
+        PV1_CUDA(p, cudaEventRecord(ev[3 * c + 1], p->stream));
+        if (p->persistent) {
+            PV1_CUDA(p, launch_v1_persistent(p->vp, p->d_stepBase, K, p->d_lgnRing, p->lgnSlots, deliverFirst,
+                                             p->d_barrier, p->stream));
+        } else {
+            for (int s = 0; s < K; s++)
+                PV1_CUDA(p, launch_v1_step(p->vp, p->d_stepBase, s, p->d_lgnRing, p->lgnSlots,
+                                           s == 0 ? deliverFirst : 1, 1, p->stream));
         }
+        PV1_CUDA(p, cudaEventRecord(ev[3 * c + 2], p->stream));
         PV1_CUDA(p, launch_advance_step(p->d_stepBase, K, p->stream));
     }
     PV1_CUDA(p, cudaStreamSynchronize(p->stream));
     double tl = 0, tv = 0;
-    q = 0;
-    for (uint32_t c = 0; c < nsteps / K; c++) {
-        float ms;
-        PV1_CUDA(p, cudaEventElapsedTime(&ms, ev[q], ev[q + 1]));
-        tl += ms;
-        q += 2;
-        for (int s = 0; s < K; s++) {
-            PV1_CUDA(p, cudaEventElapsedTime(&ms, ev[q], ev[q + 1]));
-            tv += ms;
-            q += 2;
-        }
+    for (uint32_t c = 0; c < nchunk; c++) {
+        float a, b;
+        PV1_CUDA(p, cudaEventElapsedTime(&a, ev[3 * c], ev[3 * c + 1]));
+        PV1_CUDA(p, cudaEventElapsedTime(&b, ev[3 * c + 1], ev[3 * c + 2]));
+        tl += a;
+        tv += b;
     }
     for (auto &e : ev) cudaEventDestroy(e);
-    p->step += nsteps;
+    p->step += (long long)nchunk * K;
     p->pending = true;
-    *v1_ms = (float)(tv / nsteps);
-    *lgn_ms = (float)(tl / (nsteps / K));
+    *v1_ms = (float)(tv / ((double)nchunk * K));
+    *lgn_ms = (float)(tl / nchunk);
     if (chunk) *chunk = K;
     return check_device_error(p);
+}
+
+int pv1_persistent_mode(pv1_plan *p, int allow) {
+    if (!p) return PV1_E_ARG;
+    if (allow >= 0) {
+        p->allowPersistent = allow != 0;
+        p->modeChosen = false;
+        drop_graph(p);
+    }
+    int r = choose_mode(p);
+    if (r) return r;
+    return p->persistent ? 1 : 0;
 }
 
 // Applies the delivery of the last step's spikes (kept pending so that the next step can

@@ -1,26 +1,28 @@
-// V1 stage of the patchV1 hot path on GB300 (sm_103a): one kernel per simulation step.
+// V1 stage of the patchV1 hot path on GB300 (sm_103a).
 //
 // The reference runs, per step, compute_V_collect_spike_learnFF_fast (src/coredynamics.cu:
 // 1235-2059), then recal_G_mat_nd_fast for the near-neighbour blocks (:2609-2922), then a
 // single-threaded host loop for the far synapses (recal_G_vec :181-372, fill_fSpikeTrain
 // src/stats.cu:114-126) whose result is copied back and added by sum_G (:2312-2349).
 //
-// Here one launch per step does three phases:
+// Here every simulation step has three phases, one thread per neuron:
 //   A. deliver the previous step's spikes: every CTA compacts the spikers of its neighbour
 //      blocks with warp ballots (ascending neuron order, E before I), stages their unit
 //      conductance (og/oh) in shared memory and reads one coalesced conMat row per spiker;
 //      far events that arrive in the previous step come from a fixed-point ring filled by
 //      phase C.  The sum is added to g/h exactly where the reference's delivery adds it.
-//   B. the V1 membrane step of this step (conductance decay, LGN input, RK2 AdEx/LIF,
-//      spike-time interpolation, refractoriness), same float operation order as the
-//      reference's kernel.
+//   B. the V1 membrane step (conductance decay, LGN input, RK2 AdEx/LIF, spike-time
+//      interpolation, refractoriness), with the float operations of the reference's kernel.
 //   C. push this step's spikes into the far-delivery ring: one event per (spike, far
 //      synapse), with the reference's delay arithmetic deciding the arrival step.
 // Adding the previous step's delivery before this step's decay is the same sequence of
 // float operations as the reference's separate kernels.
 //
-// All per-species arrays are indexed with compile-time indices (loops over kMaxNG with a
-// runtime guard) so that they live in registers.
+// Two kernels run these phases: v1_step_kernel does one step per launch (state in HBM), and
+// v1_persistent_kernel runs K steps in one cooperative launch with the neuron state, the
+// LGN synapse list and the generators held in registers and a bounded grid barrier between
+// steps.  All per-species arrays are indexed with compile-time indices so that they stay in
+// registers.
 #include "pv1_internal.cuh"
 
 namespace pv1 {
@@ -29,6 +31,9 @@ constexpr int kCta = 256;
 constexpr int kWarps = kCta / 32;
 constexpr int kMaxBS = 1024;
 constexpr int kLgnBatch = 8;
+constexpr int kMaxLgnReg = 32;        // LGN synapses kept in registers by the persistent kernel
+constexpr int kConBatch = 8;          // conMat rows fetched together
+constexpr long long kBarrierSpins = 20000000;  // ~1 s of polling before a barrier gives up
 
 __device__ __forceinline__ int type_of(const V1Params &P, int local) {
     int t = P.nType - 1;
@@ -59,26 +64,70 @@ __device__ __forceinline__ RecOff rec_off(const V1Params &P) {
     return o;
 }
 
+// Per-neuron dynamic state (registers).
+struct NState {
+    float v, w, tBack, lastNoise;
+    float gE[kMaxNG], hE[kMaxNG], gI[kMaxNG], hI[kMaxNG], gFF[kMaxNG], hFF[kMaxNG];
+};
+
+struct Smem {
+    int pre[kMaxBS];
+    float val[kMaxBS];
+    float og[kMaxNG][kMaxBS];
+    float oh[kMaxNG][kMaxBS];
+    unsigned ball[kMaxBS / 32];
+};
+
+__device__ __forceinline__ void load_state(const V1Params &P, int i, NState &s) {
+    const int nV1 = P.nV1;
+    s.v = P.v[i];
+    s.w = P.iModel == 1 ? P.w[i] : 0.0f;
+    s.tBack = P.tBack[i];
+    s.lastNoise = P.tau_noise > 0 ? P.lastNoise[i] : 0.f;
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        s.gE[ig] = ig < P.ngE ? P.gE[ig * nV1 + i] : 0.f;
+        s.hE[ig] = ig < P.ngE ? P.hE[ig * nV1 + i] : 0.f;
+        s.gI[ig] = ig < P.ngI ? P.gI[ig * nV1 + i] : 0.f;
+        s.hI[ig] = ig < P.ngI ? P.hI[ig * nV1 + i] : 0.f;
+        s.gFF[ig] = ig < P.ngFF ? P.gFF[ig * nV1 + i] : 0.f;
+        s.hFF[ig] = ig < P.ngFF ? P.hFF[ig * nV1 + i] : 0.f;
+    }
+}
+
+__device__ __forceinline__ void store_state(const V1Params &P, int i, const NState &s) {
+    const int nV1 = P.nV1;
+    P.v[i] = s.v;
+    if (P.iModel == 1) P.w[i] = s.w;
+    P.tBack[i] = s.tBack;
+    if (P.tau_noise > 0) P.lastNoise[i] = s.lastNoise;
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        if (ig < P.ngE) { P.gE[ig * nV1 + i] = s.gE[ig]; P.hE[ig * nV1 + i] = s.hE[ig]; }
+        if (ig < P.ngI) { P.gI[ig * nV1 + i] = s.gI[ig]; P.hI[ig * nV1 + i] = s.hI[ig]; }
+        if (ig < P.ngFF) { P.gFF[ig * nV1 + i] = s.gFF[ig]; P.hFF[ig * nV1 + i] = s.hFF[ig]; }
+    }
+}
+
 // Compacts the spike words blk[0..n) that are >= 1 into list[] (ascending index) using one
 // ballot word per 32 entries.  Returns the count (all threads); *below receives the number
 // of listed entries with index < split.  vals[j] keeps the word of every listed j.
 __device__ __forceinline__ int compact_spikers(const float *__restrict__ blk, int n, int split,
-                                               int *list, float *vals, unsigned *s_ball,
-                                               int *below) {
+                                               Smem &sm, int *below) {
     const int lane = threadIdx.x & 31;
     const int nw = (n + 31) >> 5;
     for (int j0 = threadIdx.x & ~31; j0 < n; j0 += kCta) {
         const int j = j0 + lane;
-        const float v = j < n ? blk[j] : 0.f;
+        const float v = j < n ? __ldcg(blk + j) : 0.f;
         const bool f = j < n && v >= 1.0f;
         const unsigned bal = __ballot_sync(0xffffffffu, f);
-        if (lane == 0) s_ball[j0 >> 5] = bal;
-        if (f) vals[j] = v;
+        if (lane == 0) sm.ball[j0 >> 5] = bal;
+        if (f) sm.val[j] = v;
     }
     __syncthreads();
     int total = 0, nb = 0;
     for (int w = 0; w < nw; w++) {
-        const unsigned bal = s_ball[w];
+        const unsigned bal = sm.ball[w];
         const int c = __popc(bal);
         if ((w + 1) * 32 <= split) nb += c;
         else if (w * 32 < split) nb += __popc(bal & ((1u << (split - w * 32)) - 1u));
@@ -87,11 +136,11 @@ __device__ __forceinline__ int compact_spikers(const float *__restrict__ blk, in
     if (total > 0) {
         for (int j0 = threadIdx.x & ~31; j0 < n; j0 += kCta) {
             const int w = j0 >> 5;
-            const unsigned bal = s_ball[w];
+            const unsigned bal = sm.ball[w];
             if ((bal >> lane) & 1u) {
                 int pos = __popc(bal & ((1u << lane) - 1u));
-                for (int q = 0; q < w; q++) pos += __popc(s_ball[q]);
-                list[pos] = j0 + lane;
+                for (int q = 0; q < w; q++) pos += __popc(sm.ball[q]);
+                sm.pre[pos] = j0 + lane;
             }
         }
         __syncthreads();
@@ -100,32 +149,437 @@ __device__ __forceinline__ int compact_spikers(const float *__restrict__ blk, in
     return total;
 }
 
+// Phase A: delivery of step tp's spikes to this thread's neuron (all threads of the CTA
+// must call it; `active` masks the neuron work).
+__device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, int b, int local, int i,
+                                             bool active, int itype, NState &st,
+                                             curandStateMRG32k3a &condState, Smem &sm) {
+    const int bs = P.blockSize, nV1 = P.nV1;
+    const int ngE = P.ngE, ngI = P.ngI;
+    const float dt = P.dt;
+    const float *sPrev = P.sInfo + (size_t)(tp & 1) * nV1;
+    float lgE[kMaxNG], lhE[kMaxNG], lgI[kMaxNG], lhI[kMaxNG], ipE[kMaxNG], ipI[kMaxNG];
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        lgE[ig] = lhE[ig] = lgI[ig] = lhI[ig] = 0.f;
+        ipE[ig] = ig < ngE ? P.pE[itype * ngE + ig] : 0.f;
+        ipI[ig] = ig < ngI ? P.pI[itype * ngI + ig] : 0.f;
+    }
+    // far events arriving in step tp, fetched early so that the loads overlap the compaction
+    const int ns = ngE + ngI;
+    unsigned long long farG[2 * kMaxNG], farH[2 * kMaxNG];
+    unsigned long long *acc = nullptr;
+    bool farSpiked = false;
+    if (P.farOn && active) {
+        acc = P.farAcc + (size_t)(tp % P.farDepth) * ns * 2 * nV1;
+        farSpiked = __ldcg(P.farFlag + tp % 3) != 0;
+#pragma unroll
+        for (int q = 0; q < 2 * kMaxNG; q++) {
+            farG[q] = q < ns ? __ldcg(acc + (size_t)(2 * q) * nV1 + i) : 0ull;
+            farH[q] = q < ns ? __ldcg(acc + (size_t)(2 * q + 1) * nV1 + i) : 0ull;
+        }
+    }
+    const int nnb = P.nNearNB[b];
+    float *recNear = nullptr;
+    int nNearDraw = 0;
+    if (P.recNear && active) {
+        long long rs = tp - P.recStep0;
+        if (rs >= 0 && rs < P.recSteps) recNear = P.recNear + ((size_t)rs * nV1 + i) * P.recCap;
+    }
+    for (int ib = 0; ib < nnb; ib++) {
+        const int nb = P.nbId[b * P.nnbMax + ib];
+        int cntE;
+        const int cnt = compact_spikers(sPrev + (size_t)nb * bs, bs, P.nE, sm, &cntE);
+        if (cnt == 0) continue;
+        // unit conductance of each spiker (output_g/h of compute_V, :2008-2041)
+        for (int r = threadIdx.x; r < cnt; r += kCta) {
+            const float sI = sm.val[sm.pre[r]];
+            const float nsp = floorf(sI);
+            const float tsp = (sI - nsp) * dt;
+            const bool isE = r < cntE;
+#pragma unroll
+            for (int ig = 0; ig < kMaxNG; ig++) {
+                if (ig < (isE ? ngE : ngI)) {
+                    float g = 0.f, h = 0.f;
+                    cond_input(isE ? P.condE : P.condI, g, h, nsp, dt - tsp, ig);
+                    sm.og[ig][r] = g;
+                    sm.oh[ig][r] = h;
+                }
+            }
+        }
+        __syncthreads();
+        if (active) {
+            const float *col = P.conMat + ((size_t)(b * P.nnbMax + ib) * bs) * bs + local;
+            for (int r0 = 0; r0 < cnt; r0 += kConBatch) {
+                float sv[kConBatch];
+#pragma unroll
+                for (int k = 0; k < kConBatch; k++)
+                    sv[k] = r0 + k < cnt ? __ldg(col + (size_t)sm.pre[r0 + k] * bs) : 0.f;
+#pragma unroll
+                for (int k = 0; k < kConBatch; k++) {
+                    const int r = r0 + k;
+                    float strength = sv[k];
+                    if (r < cnt && strength > 0) {
+                        const bool isE = r < cntE;
+                        if (P.condRng) {
+                            // pre type from the spiker's rank, as the reference does
+                            // (src/coredynamics.cu:2760-2766, 2815-2821)
+                            const int rank = isE ? r : r - cntE;
+                            const int ja = isE ? 0 : P.nTypeE, jb = isE ? P.nTypeE : P.nType;
+                            int jtype = ja;
+                            for (int jj = ja; jj < jb; jj++) {
+                                if (rank < P.typeAcc[jj]) { jtype = jj; break; }
+                            }
+                            const int idx = jtype * P.nType + itype;
+                            const float lp = P.synFail[idx];
+                            const float normed_std = sqrtf(lp * (1 - lp) / P.synPerCon[idx]);
+                            const float rnd = curand_normal(&condState);
+                            if (recNear) {
+                                if (nNearDraw < P.recCap) recNear[nNearDraw] = rnd;
+                                else atomicOr(P.err, kErrRecordOverflow);
+                            }
+                            nNearDraw++;
+                            strength *= 1 - lp + normed_std * rnd;
+                        }
+                        if (strength > 0) {
+                            if (isE) {
+#pragma unroll
+                                for (int ig = 0; ig < kMaxNG; ig++) {
+                                    if (ig < ngE) {
+                                        const float str = strength * ipE[ig];
+                                        lgE[ig] += str * sm.og[ig][r];
+                                        lhE[ig] += str * sm.oh[ig][r];
+                                    }
+                                }
+                            } else {
+#pragma unroll
+                                for (int ig = 0; ig < kMaxNG; ig++) {
+                                    if (ig < ngI) {
+                                        const float str = strength * ipI[ig];
+                                        lgI[ig] += str * sm.og[ig][r];
+                                        lhI[ig] += str * sm.oh[ig][r];
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (recNear) P.recNearCount[(size_t)(tp - P.recStep0) * nV1 + i] = nNearDraw;
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        st.gE[ig] += lgE[ig]; st.hE[ig] += lhE[ig];
+        st.gI[ig] += lgI[ig]; st.hI[ig] += lhI[ig];
+    }
+    // far events (sum_G adds them after the near delivery); the ring slot is cleared
+    if (acc) {
+#pragma unroll
+        for (int q = 0; q < 2 * kMaxNG; q++) {
+            if (q < ns) {
+                if (farG[q] | farH[q]) {
+                    acc[(size_t)(2 * q) * nV1 + i] = 0ull;
+                    acc[(size_t)(2 * q + 1) * nV1 + i] = 0ull;
+                }
+                if (farSpiked) {
+                    const float fg = (float)((double)(long long)farG[q] / kFarScale);
+                    const float fh = (float)((double)(long long)farH[q] / kFarScale);
+#pragma unroll
+                    for (int ig = 0; ig < kMaxNG; ig++) {
+                        if (q < ngE && ig == q) { st.gE[ig] += fg; st.hE[ig] += fh; }
+                        if (q >= ngE && ig == q - ngE) { st.gI[ig] += fg; st.hI[ig] += fh; }
+                    }
+                }
+            }
+        }
+    }
+    if (P.rec && active) {
+        const long long slot = tp % P.recSlots;
+        float *r = P.rec + slot * P.recStride;
+        const RecOff o = rec_off(P);
+#pragma unroll
+        for (int ig = 0; ig < kMaxNG; ig++) {
+            if (ig < ngE) r[o.gE + ig * nV1 + i] = st.gE[ig];
+            if (ig < ngI) r[o.gI + ig * nV1 + i] = st.gI[ig];
+            if (P.hWrite) {
+                if (ig < ngE) r[o.hE + ig * nV1 + i] = st.hE[ig];
+                if (ig < ngI) r[o.hI + ig * nV1 + i] = st.hI[ig];
+            }
+        }
+    }
+}
+
+// The tonic drive of the AdEx constructor (src/coredynamics.cuh:41-49).
+__device__ __forceinline__ float tonic_current(const V1Params &P, int itype, float tonic) {
+    const float vT = P.vT[itype], gL = P.gL[itype], aa = P.a[itype], deltaT = P.deltaT[itype];
+    const float targetV = P.vL + (vT - P.vL) * tonic;
+    if (targetV > vT) return (gL + aa) * (targetV - P.vL) - gL * deltaT;
+    return (gL + aa) * (targetV - P.vL) - gL * deltaT * expf((targetV - vT) / deltaT);
+}
+
+// Phase B: one membrane step of neuron i.  lgnIds/lgnW hold the first min(m, kMaxLgnReg)
+// synapses when `regSyn` is set (persistent kernel); otherwise they are loaded here.
+// Returns the spike word.
+template <bool RegSyn>
+__device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int i, int itype,
+                                             float tonic, float depC, int m, const int *lgnIds,
+                                             const float *lgnW, const float *__restrict__ lgnSInfo,
+                                             NState &st, curandStateMRG32k3a &condState,
+                                             curandStateMRG32k3a &noisyState) {
+    const int nV1 = P.nV1;
+    const float dt = P.dt;
+    const int ngE = P.ngE, ngI = P.ngI, ngFF = P.ngFF;
+    const float vR = P.vR[itype], vThres = P.vThres[itype], gL = P.gL[itype];
+    const float Cm = P.C[itype], tRef = P.tRef[itype], vT = P.vT[itype];
+    const float deltaT = P.deltaT[itype], tau_w = P.tau_w[itype], aa = P.a[itype];
+    const float bb = P.b[itype];
+    const float v0 = st.v;
+    float w0 = st.w;
+    float tBack = st.tBack;
+    const float noise0 = st.lastNoise;
+
+    // cortical conductances: keep the start-of-step value, decay to the end
+    float ge[kMaxNG], he[kMaxNG], gi[kMaxNG], hi[kMaxNG];
+    float gE_t1 = 0.0f, gI_t1 = 0.0f;
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        ge[ig] = st.gE[ig]; he[ig] = st.hE[ig];
+        if (ig < ngE) {
+            cond_decay(P.condE, st.gE[ig], st.hE[ig], dt, ig);
+            gE_t1 += st.gE[ig];
+        }
+    }
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        gi[ig] = st.gI[ig]; hi[ig] = st.hI[ig];
+        if (ig < ngI) {
+            cond_decay(P.condI, st.gI[ig], st.hI[ig], dt, ig);
+            gI_t1 += st.gI[ig];
+        }
+    }
+    float g0[kMaxNG], h0[kMaxNG], g1[kMaxNG], h1[kMaxNG];
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        g1[ig] = st.gFF[ig];
+        h1[ig] = st.hFF[ig];
+        g0[ig] = g1[ig];
+        h0[ig] = h1[ig];
+        if (ig < ngFF) cond_decay(P.condFF, g1[ig], h1[ig], dt, ig);
+    }
+    // noise (src/coredynamics.cu:1422-1440)
+    const float noiseRatio = P.noiseOnTonic ? tonic : 1.0f;
+    float noise1 = sqrtf(2 * P.noisyDep[itype] * (vT - vR) * noiseRatio * dt);
+    const float pf = P.synFailFF[itype];
+    const float nSynFF = P.synPerConFF[itype];
+    if (noise1 > 0) {
+        const float rnd = curand_normal(&noisyState);
+        if (P.recNoise) {
+            long long rs = t - P.recStep0;
+            if (rs >= 0 && rs < P.recSteps) P.recNoise[(size_t)rs * nV1 + i] = rnd;
+        }
+        noise1 *= rnd;
+        if (P.tau_noise > 0) {
+            noise1 /= P.tau_noise;
+            const float hk1 = -noise0 / P.tau_noise;
+            const float hk2 = -(noise0 + dt * hk1 + noise1) / P.tau_noise;
+            noise1 += noise0 + dt * (hk1 + hk2) / 2;
+            st.lastNoise = noise1;
+        }
+    }
+    const bool backingUp = tBack < dt && tBack > 0;
+    const float depOut = depC + noise1;
+    P.dep[i] = depOut;
+    if (backingUp) {
+#pragma unroll
+        for (int ig = 0; ig < kMaxNG; ig++)
+            if (ig < ngFF) cond_decay(P.condFF, g0[ig], h0[ig], tBack, ig);
+    }
+    // LGN input (src/coredynamics.cu:1466-1502), synapse order kept; loads gathered in
+    // batches so that they overlap
+    float *recFF = nullptr;
+    int nFF = 0;
+    if (P.recFF) {
+        long long rs = t - P.recStep0;
+        if (rs >= 0 && rs < P.recSteps) recFF = P.recFF + ((size_t)rs * nV1 + i) * P.recCap;
+    }
+    // (RegSyn: the synapse list is register resident, so the loop is unrolled over its
+    // compile-time capacity; otherwise ids and weights are loaded batch by batch)
+#pragma unroll
+    for (int q0 = 0; q0 < (RegSyn ? kMaxLgnReg : 1 << 30); q0 += kLgnBatch) {
+        if (q0 >= m) break;
+        int ids[kLgnBatch];
+        float fs[kLgnBatch], sp[kLgnBatch];
+#pragma unroll
+        for (int k = 0; k < kLgnBatch; k++) {
+            const int q = q0 + k;
+            if constexpr (RegSyn) {
+                ids[k] = lgnIds[q];
+                fs[k] = lgnW[q];
+            } else {
+                const size_t lid = (size_t)q * nV1 + i;
+                ids[k] = q < m ? __ldg(P.lgnId + lid) : 0;
+                fs[k] = q < m ? __ldg(P.sLGN + lid) : 0.f;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kLgnBatch; k++) sp[k] = q0 + k < m ? __ldcg(lgnSInfo + ids[k]) : 0.f;
+#pragma unroll
+        for (int k = 0; k < kLgnBatch; k++) {
+            const float sFF = sp[k];
+            const unsigned nspFF = (unsigned)floorf(sFF);
+            if (q0 + k < m && nspFF > 0) {
+                float f = fs[k];
+                const float tspFF = (sFF - nspFF) * dt;
+                if (pf > 0) {
+                    const float normed_std = sqrtf(pf * (1 - pf) / nSynFF);
+                    const float rnd = curand_normal(&condState);
+                    if (recFF) {
+                        if (nFF < P.recCap) recFF[nFF] = rnd;
+                        else atomicOr(P.err, kErrRecordOverflow);
+                    }
+                    nFF++;
+                    f *= 1 - pf + normed_std * rnd;
+                }
+                if (f > 0) {
+                    const float ddt = backingUp ? tBack - tspFF : 0.f;
+#pragma unroll
+                    for (int ig = 0; ig < kMaxNG; ig++) {
+                        if (ig < ngFF) {
+                            const float str = f * P.pFF[itype * ngFF + ig];
+                            if (backingUp && ddt > 0) cond_input(P.condFF, g0[ig], h0[ig], str * nspFF, ddt, ig);
+                            cond_input(P.condFF, g1[ig], h1[ig], str * nspFF, dt - tspFF, ig);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (recFF) P.recFFCount[(size_t)(t - P.recStep0) * nV1 + i] = nFF;
+    float gE_t0 = 0.0f;
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        if (ig < ngFF) {
+            gE_t0 += g0[ig];
+            gE_t1 += g1[ig];
+        }
+        st.gFF[ig] = g1[ig];
+        st.hFF[ig] = h1[ig];
+    }
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        if (ig < ngE) {
+            if (backingUp) cond_decay(P.condE, ge[ig], he[ig], tBack, ig);
+            gE_t0 += ge[ig];
+        }
+    }
+    float gI_t0 = 0.0f;
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        if (ig < ngI) {
+            if (backingUp) cond_decay(P.condI, gi[ig], hi[ig], tBack, ig);
+            gI_t0 += gi[ig];
+        }
+    }
+    // stepping (src/coredynamics.cu:1546-1590; AdEx src/coredynamics.cuh:27-118)
+    float v = v0, w = w0, tsp = 0.f;
+    int spikeCount = 0;
+    if (tBack < dt) {
+        const float a0 = gE_t0 + gI_t0 + gL;
+        const float b0 = gE_t0 * P.vE + gI_t0 * P.vI + gL * P.vL + depC;
+        const float a1 = gE_t1 + gI_t1 + gL;
+        const float b1 = gE_t1 * P.vE + gI_t1 * P.vI + gL * P.vL + depC;
+        const float new_dt = dt - tBack;
+        if (backingUp) {
+            const float A = aa * (v0 - P.vL);
+            w0 = (w0 - A) * expf(-tBack / tau_w) + A;
+        }
+        float nz0, nz1;
+        if (P.tau_noise > 0) { nz0 = noise0; nz1 = noise1; }
+        else { noise1 /= dt; nz0 = noise1; nz1 = noise1; }
+        {
+            const float dTgL = deltaT * gL;
+            const float fk1 = (-a0 * v0 + b0 + dTgL * expf((v0 - vT) / deltaT) - w0) / Cm + nz0;
+            const float gk1 = (aa * (v0 - P.vL) - w0) / tau_w;
+            const float v1 = v0 + new_dt * fk1;
+            const float w1 = w0 + new_dt * gk1;
+            const float fk2 = (-a1 * v1 + b1 + dTgL * expf((v1 - vT) / deltaT) - w1) / Cm + nz1;
+            const float gk2 = (aa * (v1 - P.vL) - w1) / tau_w;
+            w = w0 + new_dt * (gk1 + gk2) / 2;
+            v = v0 + new_dt * (fk1 + fk2) / 2;
+        }
+        if (v > vThres) {
+            const float ratio = (vThres - v0) / (v - v0);
+            tsp = tBack + ratio * new_dt;
+            w0 += ratio * (w - w0) + bb;
+            if (!(tsp >= 0)) atomicOr(P.err, kErrNegTsp);
+            spikeCount = 1;
+            tBack = tsp + tRef;
+            v = vR;
+        } else {
+            if (tBack > 0) tBack = 0;
+        }
+    }
+    if (tBack >= dt) {
+        v = vR;
+        const float A = aa * (v - P.vL);
+        w = (w0 - A) * expf(-(dt - tsp) / tau_w) + A;
+        tBack -= dt;
+    }
+    const float sInfo = spikeCount > 0 ? 1.0f + tsp / dt : v;
+    st.v = v;
+    if (P.iModel == 1) st.w = w;
+    st.tBack = tBack;
+    __stcg(P.sInfo + (size_t)(t & 1) * nV1 + i, sInfo);
+    if (P.recSpk) P.recSpk[(size_t)(t % P.recSlots) * nV1 + i] = sInfo;
+    if (P.rec) {
+        const long long slot = t % P.recSlots;
+        float *r = P.rec + slot * P.recStride;
+        const RecOff o = rec_off(P);
+        r[o.sinfo + i] = sInfo;
+        r[o.dep + i] = depOut;
+        if (P.iModel == 1) r[o.w + i] = w;
+        r[o.v + i] = v;
+#pragma unroll
+        for (int ig = 0; ig < kMaxNG; ig++) {
+            if (ig < ngFF) r[o.gFF + ig * nV1 + i] = g1[ig];
+            if (P.hWrite && ig < ngFF) r[o.hFF + ig * nV1 + i] = h1[ig];
+        }
+    }
+    return sInfo;
+}
+
 // Phase C: one event per (spike, far synapse), arrival step and offset as recal_G_vec
-// computes them (src/coredynamics.cu:282-333).  The arithmetic deciding the arrival is done
-// with explicitly rounded operations, as on the reference's host.
-__device__ __forceinline__ void far_push(const V1Params &P, long long t, int i, bool push,
-                                         float sInfo, int *s_list, float *s_si, unsigned *s_ball) {
+// computes them (src/coredynamics.cu:282-333), with explicitly rounded operations as on the
+// reference's host.  All threads of the CTA call it.
+__device__ __forceinline__ void far_phase(const V1Params &P, long long t, int i, bool active,
+                                          float sInfo, Smem &sm) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.farFlag[(t + 1) % 3] = 0;
+    if (active && sInfo > 1.0f && P.farPre[i]) P.farFlag[t % 3] = 1;
+    const bool push = active && sInfo >= 1.0f && P.farOff[i + 1] > P.farOff[i];
+    if (__syncthreads_or(push) == 0) return;
     const int nV1 = P.nV1, bs = P.blockSize;
     const float dt = P.dt;
     const unsigned bal = __ballot_sync(0xffffffffu, push);
-    if ((threadIdx.x & 31) == 0) s_ball[threadIdx.x >> 5] = bal;
+    if ((threadIdx.x & 31) == 0) sm.ball[threadIdx.x >> 5] = bal;
     __syncthreads();
     int cnt = 0, pos = 0;
     for (int w = 0; w < kWarps; w++) {
-        const int c = __popc(s_ball[w]);
+        const int c = __popc(sm.ball[w]);
         if (w < (int)(threadIdx.x >> 5)) pos += c;
         cnt += c;
     }
     if (push) {
         pos += __popc(bal & ((1u << (threadIdx.x & 31)) - 1u));
-        s_list[pos] = i;
-        s_si[pos] = sInfo;
+        sm.pre[pos] = i;
+        sm.val[pos] = sInfo;
     }
     __syncthreads();
     const int ns = P.ngE + P.ngI;
     for (int r = 0; r < cnt; r++) {
-        const int pre = s_list[r];
-        const float sI = s_si[r];
+        const int pre = sm.pre[r];
+        const float sI = sm.val[r];
         const unsigned nsp = (unsigned)floorf(sI);
         const bool preE = (pre % bs) < P.nE;
         const int ng = preE ? P.ngE : P.ngI;
@@ -174,14 +628,8 @@ __global__ void __launch_bounds__(kCta) v1_step_kernel(V1Params P, const long lo
                                                        const float *__restrict__ lgnRing,
                                                        int lgnSlots, int deliverPrev,
                                                        int doStep) {
-    __shared__ int s_pre[kMaxBS];
-    __shared__ float s_val[kMaxBS];
-    __shared__ float s_og[kMaxNG][kMaxBS];
-    __shared__ float s_oh[kMaxNG][kMaxBS];
-    __shared__ unsigned s_ball[kMaxBS / 32];
-
+    __shared__ Smem sm;
     const long long t = *stepBase + stepOffset;
-    const float *__restrict__ lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
     const int bs = P.blockSize;
     const int nq = (bs + kCta - 1) / kCta;
     const int b = blockIdx.x / nq;
@@ -189,415 +637,118 @@ __global__ void __launch_bounds__(kCta) v1_step_kernel(V1Params P, const long lo
     const bool active = local < bs;
     const int i = b * bs + (active ? local : 0);
     const int itype = type_of(P, active ? local : 0);
-    const int nV1 = P.nV1;
-    const float dt = P.dt;
-    const int ngE = P.ngE, ngI = P.ngI, ngFF = P.ngFF;
 
-    // conductances after delivery of the previous step (registers)
-    float gE[kMaxNG], hE[kMaxNG], gI[kMaxNG], hI[kMaxNG];
-#pragma unroll
-    for (int ig = 0; ig < kMaxNG; ig++) {
-        gE[ig] = hE[ig] = gI[ig] = hI[ig] = 0.f;
-        if (ig < ngE) { gE[ig] = P.gE[ig * nV1 + i]; hE[ig] = P.hE[ig * nV1 + i]; }
-        if (ig < ngI) { gI[ig] = P.gI[ig * nV1 + i]; hI[ig] = P.hI[ig * nV1 + i]; }
-    }
-    curandStateMRG32k3a condState;
+    NState st;
+    load_state(P, i, st);
+    curandStateMRG32k3a condState, noisyState;
     if (P.condRng && active) condState = P.rGenCond[i];
+    if (P.noiseRng && active) noisyState = P.rNoisy[i];
 
-    // ------------------------------------------------------------------ phase A
-    if (deliverPrev) {
-        const long long tp = t - 1;
-        const float *sPrev = P.sInfo + (size_t)(tp & 1) * nV1;
-        float lgE[kMaxNG], lhE[kMaxNG], lgI[kMaxNG], lhI[kMaxNG], ipE[kMaxNG], ipI[kMaxNG];
-#pragma unroll
-        for (int ig = 0; ig < kMaxNG; ig++) {
-            lgE[ig] = lhE[ig] = lgI[ig] = lhI[ig] = 0.f;
-            ipE[ig] = ig < ngE ? P.pE[itype * ngE + ig] : 0.f;
-            ipI[ig] = ig < ngI ? P.pI[itype * ngI + ig] : 0.f;
-        }
-        const int nnb = P.nNearNB[b];
-        float *recNear = nullptr;
-        int nNearDraw = 0;
-        if (P.recNear && active) {
-            long long rs = tp - P.recStep0;
-            if (rs >= 0 && rs < P.recSteps) recNear = P.recNear + ((size_t)rs * nV1 + i) * P.recCap;
-        }
-        for (int ib = 0; ib < nnb; ib++) {
-            const int nb = P.nbId[b * P.nnbMax + ib];
-            int cntE;
-            const int cnt = compact_spikers(sPrev + (size_t)nb * bs, bs, P.nE, s_pre, s_val, s_ball, &cntE);
-            if (cnt == 0) continue;
-            // unit conductance of each spiker (output_g/h of compute_V, :2008-2041)
-            for (int r = threadIdx.x; r < cnt; r += kCta) {
-                const float sI = s_val[s_pre[r]];
-                const float nsp = floorf(sI);
-                const float tsp = (sI - nsp) * dt;
-                const bool isE = r < cntE;
-#pragma unroll
-                for (int ig = 0; ig < kMaxNG; ig++) {
-                    if (ig < (isE ? ngE : ngI)) {
-                        float g = 0.f, h = 0.f;
-                        cond_input(isE ? P.condE : P.condI, g, h, nsp, dt - tsp, ig);
-                        s_og[ig][r] = g;
-                        s_oh[ig][r] = h;
-                    }
-                }
-            }
-            __syncthreads();
-            if (active) {
-                const float *col = P.conMat + ((size_t)(b * P.nnbMax + ib) * bs) * bs + local;
-                for (int r = 0; r < cnt; r++) {
-                    float strength = col[(size_t)s_pre[r] * bs];
-                    if (strength > 0) {
-                        const bool isE = r < cntE;
-                        if (P.condRng) {
-                            // pre type from the spiker's rank, as the reference does
-                            // (src/coredynamics.cu:2760-2766, 2815-2821)
-                            const int rank = isE ? r : r - cntE;
-                            const int ja = isE ? 0 : P.nTypeE, jb = isE ? P.nTypeE : P.nType;
-                            int jtype = ja;
-                            for (int jj = ja; jj < jb; jj++) {
-                                if (rank < P.typeAcc[jj]) { jtype = jj; break; }
-                            }
-                            const int idx = jtype * P.nType + itype;
-                            const float lp = P.synFail[idx];
-                            const float normed_std = sqrtf(lp * (1 - lp) / P.synPerCon[idx]);
-                            const float rnd = curand_normal(&condState);
-                            if (recNear) {
-                                if (nNearDraw < P.recCap) recNear[nNearDraw] = rnd;
-                                else atomicOr(P.err, kErrRecordOverflow);
-                            }
-                            nNearDraw++;
-                            strength *= 1 - lp + normed_std * rnd;
-                        }
-                        if (strength > 0) {
-                            if (isE) {
-#pragma unroll
-                                for (int ig = 0; ig < kMaxNG; ig++) {
-                                    if (ig < ngE) {
-                                        const float str = strength * ipE[ig];
-                                        lgE[ig] += str * s_og[ig][r];
-                                        lhE[ig] += str * s_oh[ig][r];
-                                    }
-                                }
-                            } else {
-#pragma unroll
-                                for (int ig = 0; ig < kMaxNG; ig++) {
-                                    if (ig < ngI) {
-                                        const float str = strength * ipI[ig];
-                                        lgI[ig] += str * s_og[ig][r];
-                                        lhI[ig] += str * s_oh[ig][r];
-                                    }
-                                }
-                            }
-                        }
-                    }
-                }
-            }
-            __syncthreads();
-        }
-        if (recNear) P.recNearCount[(size_t)(tp - P.recStep0) * nV1 + i] = nNearDraw;
-#pragma unroll
-        for (int ig = 0; ig < kMaxNG; ig++) {
-            gE[ig] += lgE[ig]; hE[ig] += lhE[ig];
-            gI[ig] += lgI[ig]; hI[ig] += lhI[ig];
-        }
-        // far events arriving in step tp (sum_G adds them after the near delivery)
-        if (P.farOn && active) {
-            const int ns = ngE + ngI;
-            unsigned long long *acc = P.farAcc + (size_t)(tp % P.farDepth) * ns * 2 * nV1;
-            const bool farSpiked = P.farFlag[tp % 3] != 0;
-#pragma unroll
-            for (int q = 0; q < 2 * kMaxNG; q++) {
-                if (q < ns) {
-                    const unsigned long long ug = acc[(size_t)(2 * q) * nV1 + i];
-                    const unsigned long long uh = acc[(size_t)(2 * q + 1) * nV1 + i];
-                    if (ug | uh) {
-                        acc[(size_t)(2 * q) * nV1 + i] = 0ull;
-                        acc[(size_t)(2 * q + 1) * nV1 + i] = 0ull;
-                    }
-                    if (farSpiked) {
-                        const float fg = (float)((double)(long long)ug / kFarScale);
-                        const float fh = (float)((double)(long long)uh / kFarScale);
-#pragma unroll
-                        for (int ig = 0; ig < kMaxNG; ig++) {
-                            if (q < ngE && ig == q) { gE[ig] += fg; hE[ig] += fh; }
-                            if (q >= ngE && ig == q - ngE) { gI[ig] += fg; hI[ig] += fh; }
-                        }
-                    }
-                }
-            }
-        }
-        if (P.rec && active) {
-            const long long slot = tp % P.recSlots;
-            float *r = P.rec + slot * P.recStride;
-            const RecOff o = rec_off(P);
-#pragma unroll
-            for (int ig = 0; ig < kMaxNG; ig++) {
-                if (ig < ngE) r[o.gE + ig * nV1 + i] = gE[ig];
-                if (ig < ngI) r[o.gI + ig * nV1 + i] = gI[ig];
-                if (P.hWrite) {
-                    if (ig < ngE) r[o.hE + ig * nV1 + i] = hE[ig];
-                    if (ig < ngI) r[o.hI + ig * nV1 + i] = hI[ig];
-                }
-            }
-        }
-    }
-
+    if (deliverPrev) deliver_prev(P, t - 1, b, local, i, active, itype, st, condState, sm);
     if (!doStep) {
-        // delivery only (end of a run): store the delivered conductances
         if (active) {
-#pragma unroll
-            for (int ig = 0; ig < kMaxNG; ig++) {
-                if (ig < ngE) { P.gE[ig * nV1 + i] = gE[ig]; P.hE[ig * nV1 + i] = hE[ig]; }
-                if (ig < ngI) { P.gI[ig * nV1 + i] = gI[ig]; P.hI[ig * nV1 + i] = hI[ig]; }
-            }
+            store_state(P, i, st);
             if (P.condRng) P.rGenCond[i] = condState;
         }
         return;
     }
-
-    // ------------------------------------------------------------------ phase B
     float sInfo = 0.f;
     if (active) {
-        const float vR = P.vR[itype], vThres = P.vThres[itype], gL = P.gL[itype];
-        const float Cm = P.C[itype], tRef = P.tRef[itype], vT = P.vT[itype];
-        const float deltaT = P.deltaT[itype], tau_w = P.tau_w[itype], aa = P.a[itype];
-        const float bb = P.b[itype];
         const float tonic = P.tonicDep[i];
-        float v0 = P.v[i];
-        float w0 = P.iModel == 1 ? P.w[i] : 0.0f;
-        float tBack = P.tBack[i];
-        float g1[kMaxNG], h1[kMaxNG];
-#pragma unroll
-        for (int ig = 0; ig < kMaxNG; ig++) {
-            g1[ig] = ig < ngFF ? P.gFF[ig * nV1 + i] : 0.f;
-            h1[ig] = ig < ngFF ? P.hFF[ig * nV1 + i] : 0.f;
-        }
-        const int m = P.nLGNperV1[i];
-        // tonic drive (AdEx constructor, src/coredynamics.cuh:41-49)
-        float depC;
-        {
-            const float targetV = P.vL + (vT - P.vL) * tonic;
-            if (targetV > vT) depC = (gL + aa) * (targetV - P.vL) - gL * deltaT;
-            else depC = (gL + aa) * (targetV - P.vL) - gL * deltaT * expf((targetV - vT) / deltaT);
-        }
-        float noise0 = 0.f;
-        if (P.tau_noise > 0) noise0 = P.lastNoise[i];
-
-        // cortical conductances: keep the start-of-step value, decay to the end
-        float ge[kMaxNG], he[kMaxNG], gi[kMaxNG], hi[kMaxNG];
-        float gE_t1 = 0.0f, gI_t1 = 0.0f;
-#pragma unroll
-        for (int ig = 0; ig < kMaxNG; ig++) {
-            ge[ig] = gE[ig]; he[ig] = hE[ig];
-            if (ig < ngE) {
-                float g = gE[ig], h = hE[ig];
-                cond_decay(P.condE, g, h, dt, ig);
-                P.gE[ig * nV1 + i] = g;
-                P.hE[ig * nV1 + i] = h;
-                gE_t1 += g;
-            }
-        }
-#pragma unroll
-        for (int ig = 0; ig < kMaxNG; ig++) {
-            gi[ig] = gI[ig]; hi[ig] = hI[ig];
-            if (ig < ngI) {
-                float g = gI[ig], h = hI[ig];
-                cond_decay(P.condI, g, h, dt, ig);
-                P.gI[ig * nV1 + i] = g;
-                P.hI[ig * nV1 + i] = h;
-                gI_t1 += g;
-            }
-        }
-        float g0[kMaxNG], h0[kMaxNG];
-#pragma unroll
-        for (int ig = 0; ig < kMaxNG; ig++) {
-            g0[ig] = g1[ig];
-            h0[ig] = h1[ig];
-            if (ig < ngFF) cond_decay(P.condFF, g1[ig], h1[ig], dt, ig);
-        }
-        // noise (src/coredynamics.cu:1422-1440)
-        const float noiseRatio = P.noiseOnTonic ? tonic : 1.0f;
-        float noise1 = sqrtf(2 * P.noisyDep[itype] * (vT - vR) * noiseRatio * dt);
-        const float pf = P.synFailFF[itype];
-        const float nSynFF = P.synPerConFF[itype];
-        if (noise1 > 0) {
-            curandStateMRG32k3a ns = P.rNoisy[i];
-            const float rnd = curand_normal(&ns);
-            P.rNoisy[i] = ns;
-            if (P.recNoise) {
-                long long rs = t - P.recStep0;
-                if (rs >= 0 && rs < P.recSteps) P.recNoise[(size_t)rs * nV1 + i] = rnd;
-            }
-            noise1 *= rnd;
-            if (P.tau_noise > 0) {
-                noise1 /= P.tau_noise;
-                const float hk1 = -noise0 / P.tau_noise;
-                const float hk2 = -(noise0 + dt * hk1 + noise1) / P.tau_noise;
-                noise1 += noise0 + dt * (hk1 + hk2) / 2;
-                P.lastNoise[i] = noise1;
-            }
-        }
-        const bool backingUp = tBack < dt && tBack > 0;
-        const float depOut = depC + noise1;
-        P.dep[i] = depOut;
-        if (backingUp) {
-#pragma unroll
-            for (int ig = 0; ig < kMaxNG; ig++)
-                if (ig < ngFF) cond_decay(P.condFF, g0[ig], h0[ig], tBack, ig);
-        }
-        // LGN input (src/coredynamics.cu:1466-1502), synapse order kept; the ids and spike
-        // words are gathered in batches so that the loads overlap
-        float *recFF = nullptr;
-        int nFF = 0;
-        if (P.recFF) {
-            long long rs = t - P.recStep0;
-            if (rs >= 0 && rs < P.recSteps) recFF = P.recFF + ((size_t)rs * nV1 + i) * P.recCap;
-        }
-        for (int q0 = 0; q0 < m; q0 += kLgnBatch) {
-            int ids[kLgnBatch];
-            float fs[kLgnBatch], sp[kLgnBatch];
-#pragma unroll
-            for (int k = 0; k < kLgnBatch; k++) {
-                const size_t lid = (size_t)(q0 + k) * nV1 + i;
-                ids[k] = q0 + k < m ? __ldg(P.lgnId + lid) : 0;
-                fs[k] = q0 + k < m ? __ldg(P.sLGN + lid) : 0.f;
-            }
-#pragma unroll
-            for (int k = 0; k < kLgnBatch; k++) sp[k] = q0 + k < m ? lgnSInfo[ids[k]] : 0.f;
-#pragma unroll
-            for (int k = 0; k < kLgnBatch; k++) {
-                const float sFF = sp[k];
-                const unsigned nspFF = (unsigned)floorf(sFF);
-                if (q0 + k < m && nspFF > 0) {
-                    float f = fs[k];
-                    const float tspFF = (sFF - nspFF) * dt;
-                    if (pf > 0) {
-                        const float normed_std = sqrtf(pf * (1 - pf) / nSynFF);
-                        const float rnd = curand_normal(&condState);
-                        if (recFF) {
-                            if (nFF < P.recCap) recFF[nFF] = rnd;
-                            else atomicOr(P.err, kErrRecordOverflow);
-                        }
-                        nFF++;
-                        f *= 1 - pf + normed_std * rnd;
-                    }
-                    if (f > 0) {
-                        const float ddt = backingUp ? tBack - tspFF : 0.f;
-#pragma unroll
-                        for (int ig = 0; ig < kMaxNG; ig++) {
-                            if (ig < ngFF) {
-                                const float str = f * P.pFF[itype * ngFF + ig];
-                                if (backingUp && ddt > 0) cond_input(P.condFF, g0[ig], h0[ig], str * nspFF, ddt, ig);
-                                cond_input(P.condFF, g1[ig], h1[ig], str * nspFF, dt - tspFF, ig);
-                            }
-                        }
-                    }
-                }
-            }
-        }
-        if (recFF) P.recFFCount[(size_t)(t - P.recStep0) * nV1 + i] = nFF;
+        const float depC = tonic_current(P, itype, tonic);
+        const float *lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
+        sInfo = step_neuron<false>(P, t, i, itype, tonic, depC, P.nLGNperV1[i], nullptr, nullptr, lgnSInfo,
+                                   st, condState, noisyState);
+        store_state(P, i, st);
         if (P.condRng) P.rGenCond[i] = condState;
-        float gE_t0 = 0.0f;
-#pragma unroll
-        for (int ig = 0; ig < kMaxNG; ig++) {
-            if (ig < ngFF) {
-                gE_t0 += g0[ig];
-                gE_t1 += g1[ig];
-                P.gFF[ig * nV1 + i] = g1[ig];
-                P.hFF[ig * nV1 + i] = h1[ig];
-            }
-        }
-#pragma unroll
-        for (int ig = 0; ig < kMaxNG; ig++) {
-            if (ig < ngE) {
-                if (backingUp) cond_decay(P.condE, ge[ig], he[ig], tBack, ig);
-                gE_t0 += ge[ig];
-            }
-        }
-        float gI_t0 = 0.0f;
-#pragma unroll
-        for (int ig = 0; ig < kMaxNG; ig++) {
-            if (ig < ngI) {
-                if (backingUp) cond_decay(P.condI, gi[ig], hi[ig], tBack, ig);
-                gI_t0 += gi[ig];
-            }
-        }
-        // stepping (src/coredynamics.cu:1546-1590; AdEx src/coredynamics.cuh:27-118)
-        float v = v0, w = w0, tsp = 0.f;
-        int spikeCount = 0;
-        if (tBack < dt) {
-            const float a0 = gE_t0 + gI_t0 + gL;
-            const float b0 = gE_t0 * P.vE + gI_t0 * P.vI + gL * P.vL + depC;
-            const float a1 = gE_t1 + gI_t1 + gL;
-            const float b1 = gE_t1 * P.vE + gI_t1 * P.vI + gL * P.vL + depC;
-            const float new_dt = dt - tBack;
-            if (backingUp) {
-                const float A = aa * (v0 - P.vL);
-                w0 = (w0 - A) * expf(-tBack / tau_w) + A;
-            }
-            float nz0, nz1;
-            if (P.tau_noise > 0) { nz0 = noise0; nz1 = noise1; }
-            else { noise1 /= dt; nz0 = noise1; nz1 = noise1; }
-            {
-                const float dTgL = deltaT * gL;
-                const float fk1 = (-a0 * v0 + b0 + dTgL * expf((v0 - vT) / deltaT) - w0) / Cm + nz0;
-                const float gk1 = (aa * (v0 - P.vL) - w0) / tau_w;
-                const float v1 = v0 + new_dt * fk1;
-                const float w1 = w0 + new_dt * gk1;
-                const float fk2 = (-a1 * v1 + b1 + dTgL * expf((v1 - vT) / deltaT) - w1) / Cm + nz1;
-                const float gk2 = (aa * (v1 - P.vL) - w1) / tau_w;
-                w = w0 + new_dt * (gk1 + gk2) / 2;
-                v = v0 + new_dt * (fk1 + fk2) / 2;
-            }
-            if (v > vThres) {
-                const float ratio = (vThres - v0) / (v - v0);
-                tsp = tBack + ratio * new_dt;
-                w0 += ratio * (w - w0) + bb;
-                if (!(tsp >= 0)) atomicOr(P.err, kErrNegTsp);
-                spikeCount = 1;
-                tBack = tsp + tRef;
-                v = vR;
-            } else {
-                if (tBack > 0) tBack = 0;
-            }
-        }
-        if (tBack >= dt) {
-            v = vR;
-            const float A = aa * (v - P.vL);
-            w = (w0 - A) * expf(-(dt - tsp) / tau_w) + A;
-            tBack -= dt;
-        }
-        sInfo = spikeCount > 0 ? 1.0f + tsp / dt : v;
-        P.sInfo[(size_t)(t & 1) * nV1 + i] = sInfo;
-        if (P.recSpk) P.recSpk[(size_t)(t % P.recSlots) * nV1 + i] = sInfo;
-        P.v[i] = v;
-        if (P.iModel == 1) P.w[i] = w;
-        P.tBack[i] = tBack;
-        if (P.rec) {
-            const long long slot = t % P.recSlots;
-            float *r = P.rec + slot * P.recStride;
-            const RecOff o = rec_off(P);
-            r[o.sinfo + i] = sInfo;
-            r[o.dep + i] = depOut;
-            if (P.iModel == 1) r[o.w + i] = w;
-            r[o.v + i] = v;
-#pragma unroll
-            for (int ig = 0; ig < kMaxNG; ig++) {
-                if (ig < ngFF) r[o.gFF + ig * nV1 + i] = g1[ig];
-                if (P.hWrite && ig < ngFF) r[o.hFF + ig * nV1 + i] = h1[ig];
-            }
-        }
+        if (P.noiseRng) P.rNoisy[i] = noisyState;
     }
+    if (P.farOn) far_phase(P, t, i, active, sInfo, sm);
+}
 
-    // ------------------------------------------------------------------ phase C
-    if (!P.farOn) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) P.farFlag[(t + 1) % 3] = 0;
-    if (active && sInfo > 1.0f && P.farPre[i]) P.farFlag[t % 3] = 1;
-    const bool push = active && sInfo >= 1.0f && P.farOff[i + 1] > P.farOff[i];
-    if (__syncthreads_or(push) == 0) return;
-    far_push(P, t, i, push, sInfo, s_pre, s_val, s_ball);
+// Grid-wide barrier between the steps of the persistent kernel: arrive on a counter, the
+// last CTA bumps the generation; waiting CTAs poll with a bounded number of attempts and
+// raise kErrBarrier (instead of hanging) if the generation never moves.
+__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned *gen, unsigned nCTA, int *err) {
+    __syncthreads();
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        const unsigned g = *(volatile unsigned *)gen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(count, 1u);
+        int ok = 1;
+        if (arrived == nCTA - 1) {
+            *(volatile unsigned *)count = 0u;
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            long long spins = 0;
+            while (*(volatile unsigned *)gen == g) {
+                if (++spins > kBarrierSpins) {
+                    atomicOr(err, kErrBarrier);
+                    ok = 0;
+                    break;
+                }
+                if (spins > 64) __nanosleep(40);
+            }
+        }
+        __threadfence();
+        if (*(volatile int *)err & kErrBarrier) ok = 0;
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// K steps in one cooperative launch.  Neuron state, generators and up to kMaxLgnReg LGN
+// synapses stay in registers; one grid barrier separates consecutive steps.
+__global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, const long long *stepBase,
+                                                                 int K, const float *__restrict__ lgnRing,
+                                                                 int lgnSlots, int deliverFirst,
+                                                                 unsigned *barrier) {
+    __shared__ Smem sm;
+    const long long t0 = *stepBase;
+    const int bs = P.blockSize;
+    const int nq = (bs + kCta - 1) / kCta;
+    const int b = blockIdx.x / nq;
+    const int local = (blockIdx.x % nq) * kCta + threadIdx.x;
+    const bool active = local < bs;
+    const int i = b * bs + (active ? local : 0);
+    const int itype = type_of(P, active ? local : 0);
+
+    NState st;
+    load_state(P, i, st);
+    curandStateMRG32k3a condState, noisyState;
+    if (P.condRng && active) condState = P.rGenCond[i];
+    if (P.noiseRng && active) noisyState = P.rNoisy[i];
+    const float tonic = active ? P.tonicDep[i] : 0.f;
+    const float depC = tonic_current(P, itype, tonic);
+    const int m = active ? P.nLGNperV1[i] : 0;
+    int lgnIds[kMaxLgnReg];
+    float lgnW[kMaxLgnReg];
+#pragma unroll
+    for (int q = 0; q < kMaxLgnReg; q++) {
+        const size_t lid = (size_t)q * P.nV1 + i;
+        lgnIds[q] = q < m ? __ldg(P.lgnId + lid) : 0;
+        lgnW[q] = q < m ? __ldg(P.sLGN + lid) : 0.f;
+    }
+    for (int s = 0; s < K; s++) {
+        const long long t = t0 + s;
+        if (s > 0 || deliverFirst) deliver_prev(P, t - 1, b, local, i, active, itype, st, condState, sm);
+        float sInfo = 0.f;
+        if (active) {
+            const float *lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
+            sInfo = step_neuron<true>(P, t, i, itype, tonic, depC, m, lgnIds, lgnW, lgnSInfo, st, condState,
+                                      noisyState);
+        }
+        if (P.farOn) far_phase(P, t, i, active, sInfo, sm);
+        if (s + 1 < K && !grid_barrier(barrier, barrier + 1, gridDim.x, P.err)) break;
+    }
+    if (active) {
+        store_state(P, i, st);
+        if (P.condRng) P.rGenCond[i] = condState;
+        if (P.noiseRng) P.rNoisy[i] = noisyState;
+    }
 }
 
 // rand_spInit (src/coredynamics.cu:5-146) for a network without initial spikes: seeds the
@@ -625,6 +776,36 @@ cudaError_t launch_v1_step(const V1Params &p, const long long *stepBase, int ste
     v1_step_kernel<<<p.nblock * nq, kCta, 0, st>>>(p, stepBase, stepOffset, lgnSInfo, lgnSlots,
                                                    deliverPrev, doStep);
     return cudaGetLastError();
+}
+
+// Number of CTAs of the persistent kernel and whether they can all be resident at once.
+int v1_persistent_ctas(const V1Params &p, int device, bool *fits) {
+    const int nq = (p.blockSize + kCta - 1) / kCta;
+    const int n = p.nblock * nq;
+    int perSM = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_persistent_kernel, kCta, 0);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+    *fits = coop && perSM > 0 && n <= perSM * sms && p.maxLGN <= kMaxLgnReg;
+    return n;
+}
+
+cudaError_t launch_v1_persistent(const V1Params &p, const long long *stepBase, int K, const float *lgnRing,
+                                 int lgnSlots, int deliverFirst, unsigned *barrier, cudaStream_t st) {
+    const int nq = (p.blockSize + kCta - 1) / kCta;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(p.nblock * nq);
+    cfg.blockDim = dim3(kCta);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, v1_persistent_kernel, p, stepBase, K, lgnRing, lgnSlots, deliverFirst,
+                              barrier);
 }
 
 cudaError_t launch_v1_rng_init(curandStateMRG32k3a *cond, curandStateMRG32k3a *noisy,

@@ -322,6 +322,14 @@ class Simulation:
         self.step += (int(nsteps) // k.value) * k.value
         return float(v1.value), float(lgn.value), int(k.value)
 
+    def persistent(self, allow: int = -1) -> bool:
+        """Queries (allow=-1) or sets whether V1 steps run as one cooperative launch per
+        chunk of steps."""
+        rc = N.lib.pv1_persistent_mode(self.plan, int(allow))
+        if rc < 0:
+            N.check(self.plan, rc, "pv1_persistent_mode")
+        return rc == 1
+
     def fetch_spikes(self, step0: int, n: int) -> np.ndarray:
         out = np.empty((n, self.spec.nV1), f32)
         N.check(self.plan, N.lib.pv1_fetch_spikes(self.plan, int(step0), int(n), N.fptr(out)), "pv1_fetch_spikes")

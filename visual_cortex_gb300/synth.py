@@ -237,7 +237,7 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
                   m: int = 20, width: int = 64, height: int = 64, nt: int = 8000,
                   orient: float = 0.0, contrast: float = 0.5, far_partners: int = 0,
                   adex_inh: bool = False, patch_deg: float = 2.0, nFrame: int = 120,
-                  wFF: float = 0.25, wE: float = 0.006, wI: float = 0.3, wFar: float = 0.002,
+                  wFF: float = 0.2, wE: float = 0.004, wI: float = 0.6, wFar: float = 0.002,
                   noisyDep=(0.0, 0.0), synFail=(0.0, 0.0, 0.0, 0.0), synFailFF=(0.0, 0.0),
                   mSample1D: int = 16, dt: float = 0.125) -> Workload:
     """Builds one synthetic patch; C1 = 1x1024 V1 / 512 LGN; C2 = 32 blocks / 16384 LGN."""

@@ -252,6 +252,20 @@ int pv1_run_timed(pv1_plan *plan, uint32_t nsteps, uint64_t flush_bytes, float *
  * chunk. */
 int pv1_time_kernels(pv1_plan *plan, uint32_t nsteps, float *v1_ms, float *lgn_ms, int *chunk);
 
+/* Allocation-free LGN stepping (no counterpart in the reference).  For callers that cannot
+ * allocate device memory when they step the LGN stage (a host loop under a fixed device
+ * memory budget, or a framework that owns every allocation): runs the LGN rate and spike
+ * kernels for the plan's next nsteps steps and writes the spike words, and the rates if d_fr
+ * is not NULL, to the caller's device buffers [nsteps][nLGN] (magno cells; other entries are
+ * left untouched).  The only scratch, the rates passed between the two kernels, lives in a
+ * fixed 4 MiB device array of the library: nsteps * nLGN must not exceed 1048576, otherwise
+ * PV1_E_ARG.  It calls no cudaMalloc/cudaFree.  Work is queued on the plan's stream.  The
+ * first call on a device looks up the array's device address (cudaGetSymbolAddress): make
+ * that first call before any stream capture.  Calls share the array, so calls that overlap on
+ * the GPU race.  It advances the plan's LGN generators and step counter: a plan stepped this
+ * way is an LGN-only plan (do not mix with pv1_run). */
+int pv1_lgn_spikes_noalloc(pv1_plan *plan, uint32_t nsteps, float *d_sinfo, float *d_fr);
+
 /* allow = 1/0 enables/disables the persistent cooperative V1 kernel (one launch per chunk of
  * steps, state in registers, bounded grid barrier between steps); allow = -1 only queries.
  * Returns 1 if the plan steps with the persistent kernel, 0 if with one launch per step. */

@@ -112,6 +112,7 @@ def _load() -> C.CDLL:
         "pv1_run_timed": ([P, C.c_uint32, C.c_uint64, _FP], C.c_int),
         "pv1_time_kernels": ([P, C.c_uint32, _FP, _FP, C.POINTER(C.c_int)], C.c_int),
         "pv1_persistent_mode": ([P, C.c_int], C.c_int),
+        "pv1_lgn_spikes_noalloc": ([P, C.c_uint32, _FP, _FP], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

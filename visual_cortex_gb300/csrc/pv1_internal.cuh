@@ -176,6 +176,18 @@ cudaError_t launch_lgn_spatial(cudaTextureObject_t L, cudaTextureObject_t M, cud
                                int nSample, int layer0, int nLayer, int row0, float *out,
                                cudaStream_t st);
 cudaError_t launch_lgn_step(const LgnParams &p, const long long *stepBase, int K, cudaStream_t st);
+cudaError_t launch_lgn_rate_only(const LgnParams &p, const long long *stepBase, int K, cudaStream_t st);
+
+// What the allocation-free LGN entry point needs from a plan (defined in pv1_plan.cu).
+struct PlanLgnView {
+    LgnParams lp;
+    cudaStream_t stream;
+    long long step;
+    int device;
+};
+int plan_lgn_view(pv1_plan *p, PlanLgnView *out);
+void plan_advance_steps(pv1_plan *p, long long n);
+int plan_fail(pv1_plan *p, int code, const char *msg);
 cudaError_t launch_v1_step(const V1Params &p, const long long *stepBase, int stepOffset,
                            const float *lgnSInfo, int lgnSlots, int deliverPrev, int doStep,
                            cudaStream_t st);

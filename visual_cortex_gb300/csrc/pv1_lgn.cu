@@ -348,6 +348,13 @@ cudaError_t launch_lgn_spatial(cudaTextureObject_t L, cudaTextureObject_t M, cud
     return cudaGetLastError();
 }
 
+cudaError_t launch_lgn_rate_only(const LgnParams &p, const long long *stepBase, int K, cudaStream_t st) {
+    if (p.nMagno <= 0) return cudaSuccess;
+    dim3 grid((p.nMagno + 255) / 256, K);
+    lgn_rate_kernel<<<grid, 256, 0, st>>>(p, stepBase);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_lgn_step(const LgnParams &p, const long long *stepBase, int K, cudaStream_t st) {
     if (p.nMagno <= 0) return cudaSuccess;
     dim3 grid((p.nMagno + 255) / 256, K);

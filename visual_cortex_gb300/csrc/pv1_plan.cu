@@ -186,6 +186,24 @@ void build_segments(const pv1_lgn_config &c, std::vector<int> &nseg, std::vector
 
 }  // namespace
 
+namespace pv1 {
+
+int plan_lgn_view(pv1_plan *p, PlanLgnView *out) {
+    if (!p || !out) return PV1_E_ARG;
+    if (!p->lgnReady || !p->stimReady) return fail(p, PV1_E_STATE, "LGN/stimulus not loaded");
+    out->lp = p->lp;
+    out->stream = p->stream;
+    out->step = p->step;
+    out->device = p->device;
+    return PV1_OK;
+}
+
+void plan_advance_steps(pv1_plan *p, long long n) { p->step += n; }
+
+int plan_fail(pv1_plan *p, int code, const char *msg) { return fail(p, code, msg); }
+
+}  // namespace pv1
+
 extern "C" {
 
 int pv1_abi_version(void) { return 1; }

@@ -96,6 +96,20 @@ def test_c1_end_to_end_own_tables(c1_small):
     assert cmp["lgn_fr_maxrel"] < 1e-3, cmp
 
 
+def test_per_cell_temporal_kernels_parity(native):
+    """Cells with their own temporal kernels take the general (cell, step)-parallel rate
+    kernel; the single-class fused kernel is covered by the other parity tests."""
+    from visual_cortex_gb300 import synth
+    from oracle.parity import run_parity, compare
+    wl = synth.config1(seed=4, tjitter=0.2)
+    res = run_parity(wl, RASTER_STEPS, cap=8)
+    cmp = compare(res, wl.spec)
+    assert res["draw_count_mismatch"] == 0
+    assert cmp["lgn_spike_mismatch"] == 0, cmp
+    assert cmp["lgn_fr_maxrel"] < 1e-5, cmp
+    assert_raster_ok(cmp)
+
+
 def test_noise_and_failures_parity(native):
     """Noise (rNoisy normals) and synaptic failure (rGenCond normals, FF and near) consume
     the same draws in the same order as the reference's kernels."""

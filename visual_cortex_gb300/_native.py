@@ -72,9 +72,13 @@ class LgnParams(C.Structure):
 
 
 def _load() -> C.CDLL:
+    import os
     from .build import build_native
+    override = os.environ.get("PV1_LIBRARY")
     try:
-        path = build_native()   # no-op when the library is newer than its sources
+        # PV1_LIBRARY: an already built library with this ABI; otherwise the in-tree build
+        # (a no-op when the library is newer than its sources)
+        path = override if override else build_native()
     except RuntimeError as e:
         path = library_path()
         if not Path(path).exists():

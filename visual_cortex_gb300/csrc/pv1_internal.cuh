@@ -9,13 +9,17 @@
 #include <cuda_runtime.h>
 #include <curand_kernel.h>
 #include <stdint.h>
-#include "../../include/patchv1_gb300.h"
+#include "patchv1_gb300.h"   // include/ (on the include path)
 
 namespace pv1 {
 
 constexpr int kMaxType = PV1_MAX_NTYPE;
 constexpr int kMaxNG = PV1_MAX_NG;
 constexpr int kMaxSeg = 255;   // frames one temporal window may span (segments per step)
+// single-temporal-class LGN kernel limits: steps per chunk, segments per step, frames per chunk
+constexpr int kClassMaxK = 64;
+constexpr int kClassMaxSeg = 48;
+constexpr int kClassMaxSlots = 64;
 
 // Error word bits raised by kernels (never trap).
 constexpr int kErrRecordOverflow = 1;   // a draw record ran out of capacity
@@ -49,12 +53,33 @@ __device__ __forceinline__ void cond_input(const Cond &c, float &g, float &h, fl
     h += f * etr;
 }
 
+// The same input with the kernel's constants passed as values (lets a caller choose between
+// two kernels without taking the address of a kernel parameter).
+__device__ __forceinline__ void cond_input_v(float rise, float decay, float dod, float &g, float &h, float f,
+                                             float dt) {
+    float etr = expf(-dt / rise);
+    g += f * dod * (expf(-dt / decay) - etr);
+    h += f * etr;
+}
+
 // Exact exponential decay of (g, h) over dt (decay_conductance, src/condShape.h:34-40).
 __device__ __forceinline__ void cond_decay(const Cond &c, float &g, float &h, float dt, int ig) {
     float etr = expf(-dt / c.rise[ig]);
     float etd = expf(-dt / c.decay[ig]);
     g = g * etd + h * c.dod[ig] * (etd - etr);
     h *= etr;
+}
+
+// Decay factors over one full step, exp(-dt/decay) and exp(-dt/rise) per species: constant
+// for a run, computed once on the device with the same expression cond_decay evaluates, so
+// using them gives the same values as evaluating the exponentials every step.
+struct StepDecay {
+    float etd[kMaxNG], etr[kMaxNG];
+};
+
+__device__ __forceinline__ void cond_decay_step(const Cond &c, const StepDecay &e, float &g, float &h, int ig) {
+    g = g * e.etd[ig] + h * c.dod[ig] * (e.etd[ig] - e.etr[ig]);
+    h *= e.etr[ig];
 }
 
 // Frame bookkeeping of the magno temporal window, shared by host and device.
@@ -89,6 +114,7 @@ struct LgnParams {
     SegTable seg;
     int iKernelSampleT0, interval;
     const double *ctw;       // [nKS+1][nMagno] cumulative temporal weights
+    const double *classCtw;  // [nKS+1] when every magno cell has the same temporal weights, else null
     const float *S;          // [nFrame+1][nMagno] spatial stage per frame
     const float *absk;       // [nMagno] |k| of the center
     const float *maxConvol;  // [nLGN]
@@ -109,6 +135,7 @@ struct V1Params {
     int ngFF, ngE, ngI;
     float dt;
     Cond condFF, condE, condI;
+    StepDecay decFF, decE, decI;   // full-step decay factors (filled by launch_step_decay)
     float vE, vI, vL;
     float vR[kMaxType], vThres[kMaxType], gL[kMaxType], C[kMaxType], tRef[kMaxType];
     float vT[kMaxType], deltaT[kMaxType], tau_w[kMaxType], a[kMaxType], b[kMaxType];
@@ -145,6 +172,9 @@ struct V1Params {
     unsigned long long *farAcc;   // [farDepth][ngE+ngI][2][nV1] fixed-point g,h
     int farDepth;
     int *farFlag;              // [3] any far-pre spike (sInfo > 1) in step t%3
+    const int *farN1;          // [nV1] leading synapses of each list with whole-step delay <= 1
+    int4 *farList;             // [3][nV1] step t%3's far spikers: (pre, first synapse, count, sInfo bits)
+    int *farCount;             // [3] length of each list
     // records
     float *rec; long long recStride; int recSlots; int hWrite;
     float *recSpk;             // [recSlots][nV1] spike words (PV1_REC_SPIKES)
@@ -194,6 +224,9 @@ cudaError_t launch_v1_step(const V1Params &p, const long long *stepBase, int ste
 cudaError_t launch_v1_rng_init(curandStateMRG32k3a *cond, curandStateMRG32k3a *noisy,
                                unsigned long long seed, int nV1, int trainDepth, cudaStream_t st);
 int v1_persistent_ctas(const V1Params &p, int device, bool *fits);
+// Evaluates the full-step decay factors of the three conductance kernels on the device and
+// stores them into p (synchronous).
+cudaError_t compute_step_decay(V1Params &p, cudaStream_t st);
 cudaError_t launch_v1_persistent(const V1Params &p, const long long *stepBase, int K, const float *lgnRing,
                                  int lgnSlots, int deliverFirst, unsigned *barrier, cudaStream_t st);
 cudaError_t launch_advance_step(long long *stepBase, int k, cudaStream_t st);
@@ -201,5 +234,13 @@ cudaError_t launch_advance_step(long long *stepBase, int k, cudaStream_t st);
 // Fixed-point scale for far-delivery accumulation: integer adds are associative, so the
 // sum of events does not depend on their order and runs are reproducible.
 constexpr double kFarScale = 4294967296.0;  // 2^32
+
+// Float <-> fixed-point conversions of the far ring.  Scaling by 2^32 is exact in float (no
+// overflow or underflow in range), so these give the same integers and floats as the
+// corresponding double-precision expressions, without FP64 work (GB300's FP64 rate is low).
+__device__ __forceinline__ long long far_to_fixed(float x) { return __float2ll_rn(x * 4294967296.0f); }
+__device__ __forceinline__ float far_from_fixed(unsigned long long u) {
+    return __ll2float_rn((long long)u) * 2.3283064365386963e-10f;  // 2^-32
+}
 
 }  // namespace pv1

@@ -222,6 +222,130 @@ __device__ __forceinline__ int frame_row(const FrameSched &fs, int currentFrame,
     return F % fs.nFrame;
 }
 
+// Number of the stimulus frame held by that layer (negative: the initial luminance).
+__device__ __forceinline__ int frame_number(const FrameSched &fs, int currentFrame, int x) {
+    int back = (fs.maxFrame - (x % fs.maxFrame)) % fs.maxFrame;
+    return currentFrame - 1 - back;
+}
+
+constexpr int kClassCta = 128;
+
+// The whole LGN step for a chunk of K steps when every magno cell has the same temporal
+// weights (one temporal kernel class): the window segment weights W[s][q] (differences of the
+// shared cumulative weights) and the frame slot of every segment are computed once per CTA;
+// each thread (one cell) stages the S values of the chunk's frames in shared memory, then for
+// each step contracts them with W, applies the logistic rate and draws the Poisson spikes.
+// The arithmetic per (cell, step) is the one of lgn_rate_kernel + lgn_spike_kernel: same
+// segment weights, same summation order, same generator calls.
+__global__ void __launch_bounds__(kClassCta) lgn_class_kernel(LgnParams P, const long long *stepBase, int K) {
+    extern __shared__ float sS[];                       // [kClassMaxSlots][kClassCta]
+    __shared__ float sW[kClassMaxK][kClassMaxSeg];
+    __shared__ unsigned char sSlot[kClassMaxK][kClassMaxSeg];
+    __shared__ int sNseg[kClassMaxK];
+    __shared__ int sFlo, sNU;
+    const long long t0 = *stepBase;
+    const FrameSched fs = P.fs;
+    if (threadIdx.x == 0) {
+        const int cf0 = frames_read_after_step(fs, t0);
+        const int ph0 = (int)((fs.magnoComp + (t0 + 1) * (long long)fs.denorm) % fs.ntPerFrame);
+        const int te0 = fs.frameOffset + (ph0 <= fs.magnoComp ? 2 : 1);
+        sFlo = frame_number(fs, cf0, te0 + P.seg.rel[(size_t)ph0 * P.seg.maxSeg]);
+        const long long t1 = t0 + K - 1;
+        const int cf1 = frames_read_after_step(fs, t1);
+        const int ph1 = (int)((fs.magnoComp + (t1 + 1) * (long long)fs.denorm) % fs.ntPerFrame);
+        const int te1 = fs.frameOffset + (ph1 <= fs.magnoComp ? 2 : 1);
+        const int n1 = P.seg.nseg[ph1];
+        const int Fhi = frame_number(fs, cf1, te1 + P.seg.rel[(size_t)ph1 * P.seg.maxSeg + n1 - 1]);
+        sNU = Fhi - sFlo + 1;
+        if (sNU > kClassMaxSlots || sNU < 1) atomicOr(P.err, kErrBounds);
+    }
+    __syncthreads();
+    const int Flo = sFlo, nU = min(max(sNU, 1), kClassMaxSlots);
+    for (int s = threadIdx.x; s < K; s += blockDim.x) {
+        const long long it = t0 + s;
+        const int cf = frames_read_after_step(fs, it);
+        const int phase = (int)((fs.magnoComp + (it + 1) * (long long)fs.denorm) % fs.ntPerFrame);
+        const int te = fs.frameOffset + (phase <= fs.magnoComp ? 2 : 1);
+        const int nseg = P.seg.nseg[phase];
+        sNseg[s] = nseg;
+        const int *rel = P.seg.rel + (size_t)phase * P.seg.maxSeg;
+        const int *j0 = P.seg.j0 + (size_t)phase * (P.seg.maxSeg + 1);
+        double ca = P.classCtw[j0[0]];
+        for (int q = 0; q < nseg; q++) {
+            const double cb = P.classCtw[j0[q + 1]];
+            sW[s][q] = (float)(cb - ca);
+            ca = cb;
+            const int slot = frame_number(fs, cf, te + rel[q]) - Flo;
+            sSlot[s][q] = (unsigned char)min(max(slot, 0), kClassMaxSlots - 1);
+        }
+    }
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool on = cell < P.nMagno;
+    if (on) {
+        for (int u = 0; u < nU; u++) {
+            const int F = Flo + u;
+            const int row = F < 0 ? fs.initRow : F % fs.nFrame;
+            sS[u * kClassCta + threadIdx.x] = __ldg(P.S + (size_t)row * P.nMagno + cell);
+        }
+    }
+    __syncthreads();
+    if (!on) return;
+    int id = P.nParvo_I + cell;
+    if (cell >= P.nMagno_I) id += P.nParvo_C;
+    const float absk = P.absk[cell];
+    const float mx = P.maxConvol[id];
+    const float C50 = P.c50[id], Kc = P.sharp[id], LA = P.la[id], LB = P.lb[id];
+    float ltr = P.leftTimeRate[id];
+    float lnl = P.lastNegLogRand[id];
+    curandStateMRG32k3a st = P.state[id];
+    const float dt = P.dt;
+    for (int s = 0; s < K; s++) {
+        const long long it = t0 + s;
+        float convol = 0.f;
+        const int nseg = sNseg[s];
+        for (int q = 0; q < nseg; q++) convol += sS[sSlot[s][q] * kClassCta + threadIdx.x] * sW[s][q];
+        // LGN_nonlinear (src/discrete_input_convol.cu:1660-1730)
+        float current = (convol * absk) * P.convolRatio;
+        if (current < 0) current = 0;
+        const float X = (float)(1.0 / (double)(1 + expf(Kc * (C50 - current / mx))));
+        const float fr = P.frRatio * mx * (LA * X + LB);
+        if (P.outFr) P.outFr[(size_t)(it % P.outSlots) * P.nLGN + id] = fr;
+        // get_spike (src/discrete_input_convol.cu:1589-1619)
+        const float rate = fr / 1000.0f;
+        const float rT = dt * rate;
+        float next_rT = lnl - ltr;
+        unsigned nsp = 0;
+        float tsp = 0.f;
+        if (next_rT > rT) {
+            ltr += rT;
+        } else {
+            float old_rT;
+            do {
+                const float u = curand_uniform(&st);
+                if (P.recU) {
+                    const long long rs = it - P.recStep0;
+                    if (rs >= 0 && rs < P.recSteps) {
+                        const size_t base = (size_t)rs * P.nLGN + id;
+                        if ((int)nsp < P.recCap) P.recU[base * P.recCap + nsp] = u;
+                        else atomicOr(P.err, kErrRecordOverflow);
+                        P.recUCount[base] = nsp + 1;
+                    }
+                }
+                lnl = fmaxf(-logf(u), 0.0f * rate);
+                old_rT = next_rT;
+                next_rT += lnl;
+                nsp++;
+            } while (next_rT <= rT);
+            ltr = rT - old_rT;
+            tsp = old_rT / (rate * nsp);
+        }
+        P.outSInfo[(size_t)(it % P.outSlots) * P.nLGN + id] = nsp + tsp / dt;
+    }
+    P.leftTimeRate[id] = ltr;
+    P.lastNegLogRand[id] = lnl;
+    P.state[id] = st;
+}
+
 // Temporal contraction and logistic rate for (cell, step) pairs of a chunk of K steps: grid
 // (cells/256, K).  The frame rows and sample ranges of the step's window segments are
 // computed once per CTA into shared memory; each thread then sums, over ~33 segments,
@@ -357,6 +481,17 @@ cudaError_t launch_lgn_rate_only(const LgnParams &p, const long long *stepBase, 
 
 cudaError_t launch_lgn_step(const LgnParams &p, const long long *stepBase, int K, cudaStream_t st) {
     if (p.nMagno <= 0) return cudaSuccess;
+    if (p.classCtw && K <= kClassMaxK) {
+        const size_t smem = (size_t)kClassMaxSlots * kClassCta * sizeof(float);
+        static bool attrSet = false;
+        if (!attrSet) {
+            cudaError_t e = cudaFuncSetAttribute(lgn_class_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            attrSet = true;
+        }
+        lgn_class_kernel<<<(p.nMagno + kClassCta - 1) / kClassCta, kClassCta, smem, st>>>(p, stepBase, K);
+        return cudaGetLastError();
+    }
     dim3 grid((p.nMagno + 255) / 256, K);
     lgn_rate_kernel<<<grid, 256, 0, st>>>(p, stepBase);
     cudaError_t e = cudaGetLastError();

@@ -131,7 +131,7 @@ void drop_graph(pv1_plan *p) {
 int issue_chunk(pv1_plan *p, int k, int deliverFirst, long long *launches) {
     cudaError_t e = launch_lgn_step(p->lp, p->d_stepBase, k, p->stream);
     if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("lgn_step: ") + cudaGetErrorString(e));
-    long long n = 2;
+    long long n = (p->lp.classCtw && k <= kClassMaxK) ? 1 : 2;
     if (p->persistent) {
         e = launch_v1_persistent(p->vp, p->d_stepBase, k, p->d_lgnRing, p->lgnSlots, deliverFirst, p->d_barrier,
                                  p->stream);
@@ -323,6 +323,7 @@ int pv1_plan_create(const pv1_v1_config *cfg, pv1_plan **out) {
     v.err = p->d_err;
     v.recSlots = 1;
     *out = p;
+    PV1_CUDA(p, compute_step_decay(v, p->stream));
     return PV1_OK;
 }
 
@@ -495,6 +496,25 @@ int pv1_lgn_setup(pv1_plan *p, const pv1_lgn_config *lc, const pv1_lgn_params *p
     p->vp.lgnN = nLGN;
     PV1_CUDA(p, cudaStreamSynchronize(p->stream));
     for (int q = 0; q < 12; q++) free_one(p, d_par[q]);
+    // one temporal-kernel class (every magno cell has bit-identical temporal weights): the
+    // fused single-class LGN kernel applies
+    L.classCtw = nullptr;
+    if (nMagno > 0) {
+        std::vector<float> tw((size_t)nMagno * nKS);
+        PV1_CUDA(p, cudaMemcpy(tw.data(), p->d_TW, tw.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        bool same = true;
+        for (int m = 1; m < nMagno && same; m++)
+            same = std::memcmp(tw.data(), tw.data() + (size_t)m * nKS, nKS * sizeof(float)) == 0;
+        const int shift = (int)((p->K * (long long)c.denorm + c.ntPerFrame - 1) / c.ntPerFrame);
+        if (same && maxSeg <= kClassMaxSeg && maxSeg + shift + 1 <= kClassMaxSlots && p->K <= kClassMaxK) {
+            double *d_cls;
+            r = dev_alloc(p, &d_cls, (size_t)nKS + 1);
+            if (r) return r;
+            PV1_CUDA(p, cudaMemcpy2D(d_cls, sizeof(double), d_ctw, (size_t)nMagno * sizeof(double), sizeof(double),
+                                     (size_t)nKS + 1, cudaMemcpyDeviceToDevice));
+            L.classCtw = d_cls;
+        }
+    }
     int e = check_device_error(p);
     if (e) return e;
     p->lgnReady = true;
@@ -663,14 +683,25 @@ int pv1_v1_set_far(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, con
         if (c.synFail[q] > 0)
             return fail(p, PV1_E_UNSUPPORTED,
                         "synaptic failure on delayed far synapses (host std::normal_distribution per post) is not built");
-    // outgoing lists by pre (stable counting sort keeps the post/j order within a pre)
-    std::vector<int> off(nV1 + 1, 0);
+    // outgoing lists by pre (stable counting sort keeps the post/j order within a pre);
+    // within a list the synapses with a whole-step delay <= 1 come first, because their
+    // events can arrive within the spike's own step
+    std::vector<int> off(nV1 + 1, 0), n1(nV1, 0);
+    std::vector<unsigned> it2(nnz);
+    std::vector<float> t2p(nnz);
     for (size_t e = 0; e < nnz; e++) {
         if (vecID[e] >= (uint32_t)nV1) return fail(p, PV1_E_ARG, "far pre id out of range");
         off[vecID[e] + 1]++;
+        // delay arithmetic of recal_G_vec (src/coredynamics.cu:282-287), in float
+        float time2post = delayVec[e] / c.speedOfThought;
+        const unsigned it2post = (unsigned)std::ceil(time2post / c.dt);
+        it2[e] = it2post;
+        t2p[e] = it2post * c.dt - time2post;
+        if (it2post <= 1) n1[vecID[e]]++;
     }
     for (int i = 0; i < nV1; i++) off[i + 1] += off[i];
-    std::vector<int> fill(off.begin(), off.end() - 1);
+    std::vector<int> fillShort(off.begin(), off.end() - 1), fill(nV1);
+    for (int i = 0; i < nV1; i++) fill[i] = off[i] + n1[i];
     std::vector<int> post(nnz), steps(nnz);
     std::vector<float> str(nnz), frac(nnz);
     std::vector<unsigned char> isPre(nV1, 0);
@@ -679,26 +710,33 @@ int pv1_v1_set_far(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, con
     for (int i = 0; i < nV1; i++) {
         for (uint32_t j = 0; j < nVec[i]; j++, e++) {
             const int pre = (int)vecID[e];
-            // delay arithmetic of recal_G_vec (src/coredynamics.cu:282-287), in float
-            float time2post = delayVec[e] / c.speedOfThought;
-            unsigned it2post = (unsigned)std::ceil(time2post / c.dt);
-            time2post = it2post * c.dt - time2post;
-            const int slot = fill[pre]++;
+            const unsigned it2post = it2[e];
+            const float time2post = t2p[e];
+            const int slot = it2post <= 1 ? fillShort[pre]++ : fill[pre]++;
             post[slot] = i;
             str[slot] = conVec[e];
-            steps[slot] = (int)it2post;
+            if (it2post > 0xffff) return fail(p, PV1_E_UNSUPPORTED, "far delay longer than 65535 steps");
+            // whole-step delay in the low 16 bits, the post neuron's type above
+            int ptype = (int)c.nType - 1;
+            for (int jt = (int)c.nType - 1; jt >= 0; jt--)
+                if ((uint32_t)(i % (int)c.blockSize) < c.typeAcc[jt]) ptype = jt;
+            steps[slot] = (int)it2post | (ptype << 16);
             frac[slot] = time2post;
             isPre[pre] = 1;
             maxSteps = std::max(maxSteps, (int)it2post);
         }
     }
-    int *d_off, *d_post, *d_steps;
+    int *d_off, *d_post, *d_steps, *d_n1, *d_count;
     float *d_str, *d_frac;
     unsigned char *d_pre;
     unsigned long long *d_acc;
+    int4 *d_list;
     const int depth = maxSteps + 2;
     int r = 0;
     r |= dev_upload(p, &d_off, off.data(), off.size());
+    r |= dev_upload(p, &d_n1, n1.data(), n1.size());
+    r |= dev_alloc(p, &d_list, (size_t)3 * nV1);
+    r |= dev_alloc(p, &d_count, 3);
     r |= dev_upload(p, &d_post, post.data(), nnz);
     r |= dev_upload(p, &d_steps, steps.data(), nnz);
     r |= dev_upload(p, &d_str, str.data(), nnz);
@@ -716,6 +754,9 @@ int pv1_v1_set_far(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, con
     v.farPre = d_pre;
     v.farAcc = d_acc;
     v.farDepth = depth;
+    v.farN1 = d_n1;
+    v.farList = d_list;
+    v.farCount = d_count;
     PV1_CUDA(p, cudaStreamSynchronize(p->stream));
     drop_graph(p);
     return PV1_OK;

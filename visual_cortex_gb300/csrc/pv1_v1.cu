@@ -20,9 +20,10 @@
 //
 // Two kernels run these phases: v1_step_kernel does one step per launch (state in HBM), and
 // v1_persistent_kernel runs K steps in one cooperative launch with the neuron state, the
-// LGN synapse list and the generators held in registers and a bounded grid barrier between
-// steps.  All per-species arrays are indexed with compile-time indices so that they stay in
-// registers.
+// LGN synapse ids and the generators held in registers and a bounded grid barrier between
+// steps.  Both are instantiated with and without the random-number paths (noise, synaptic
+// failure); the host picks the variant.  Per-species arrays use compile-time indices so that
+// they stay in registers.
 #include "pv1_internal.cuh"
 
 namespace pv1 {
@@ -31,7 +32,7 @@ constexpr int kCta = 256;
 constexpr int kWarps = kCta / 32;
 constexpr int kMaxBS = 1024;
 constexpr int kLgnBatch = 8;
-constexpr int kMaxLgnReg = 32;        // LGN synapses kept in registers by the persistent kernel
+constexpr int kMaxLgnReg = 32;        // LGN synapse ids kept in registers by the persistent kernel
 constexpr int kConBatch = 8;          // conMat rows fetched together
 constexpr long long kBarrierSpins = 20000000;  // ~1 s of polling before a barrier gives up
 
@@ -76,6 +77,11 @@ struct Smem {
     float og[kMaxNG][kMaxBS];
     float oh[kMaxNG][kMaxBS];
     unsigned ball[kMaxBS / 32];
+    int pref[kMaxBS / 32];
+    int total, below;
+    unsigned fball[kWarps];
+    int fpre[kCta], fe0[kCta], fdeg[kCta], fpref[kCta + 1];
+    float fsi[kCta];
 };
 
 __device__ __forceinline__ void load_state(const V1Params &P, int i, NState &s) {
@@ -109,54 +115,88 @@ __device__ __forceinline__ void store_state(const V1Params &P, int i, const NSta
     }
 }
 
-// Compacts the spike words blk[0..n) that are >= 1 into list[] (ascending index) using one
-// ballot word per 32 entries.  Returns the count (all threads); *below receives the number
-// of listed entries with index < split.  vals[j] keeps the word of every listed j.
-__device__ __forceinline__ int compact_spikers(const float *__restrict__ blk, int n, int split,
-                                               Smem &sm, int *below) {
-    const int lane = threadIdx.x & 31;
-    const int nw = (n + 31) >> 5;
-    for (int j0 = threadIdx.x & ~31; j0 < n; j0 += kCta) {
-        const int j = j0 + lane;
-        const float v = j < n ? __ldcg(blk + j) : 0.f;
-        const bool f = j < n && v >= 1.0f;
+// Compacts the spike words blk[0..bs) that are >= 1 into sm.pre[] (ascending index) and
+// stages the unit conductance of each (output_g/h of compute_V, src/coredynamics.cu:
+// 2008-2041) in sm.og/sm.oh.  Returns the count; *cntE receives the number of excitatory
+// spikers (index < nE), which come first.  Three CTA barriers when there are spikers, two
+// otherwise.
+__device__ __forceinline__ int compact_spikers(const V1Params &P, const float *__restrict__ blk, Smem &sm,
+                                               int *cntE) {
+    const int bs = P.blockSize, nE = P.nE;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (bs + 31) >> 5;
+    const float dt = P.dt;
+    float vals[kMaxBS / kCta];
+#pragma unroll
+    for (int k = 0; k < kMaxBS / kCta; k++) {
+        const int j = k * kCta + threadIdx.x;
+        vals[k] = j < bs ? __ldcg(blk + j) : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxBS / kCta; k++) {
+        const int j = k * kCta + threadIdx.x;
+        const bool f = j < bs && vals[k] >= 1.0f;
         const unsigned bal = __ballot_sync(0xffffffffu, f);
-        if (lane == 0) sm.ball[j0 >> 5] = bal;
-        if (f) sm.val[j] = v;
+        if (k * kCta < bs && lane == 0) sm.ball[k * kWarps + warp] = bal;
     }
     __syncthreads();
-    int total = 0, nb = 0;
-    for (int w = 0; w < nw; w++) {
-        const unsigned bal = sm.ball[w];
+    if (warp == 0) {
+        const unsigned bal = lane < nw ? sm.ball[lane] : 0u;
         const int c = __popc(bal);
-        if ((w + 1) * 32 <= split) nb += c;
-        else if (w * 32 < split) nb += __popc(bal & ((1u << (split - w * 32)) - 1u));
-        total += c;
+        int below = 0;
+        if ((lane + 1) * 32 <= nE) below = c;
+        else if (lane * 32 < nE) below = __popc(bal & ((1u << (nE - lane * 32)) - 1u));
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) below += __shfl_xor_sync(0xffffffffu, below, o);
+        if (lane < nw) sm.pref[lane] = incl - c;
+        if (lane == 31) sm.total = incl;
+        if (lane == 0) sm.below = below;
     }
-    if (total > 0) {
-        for (int j0 = threadIdx.x & ~31; j0 < n; j0 += kCta) {
-            const int w = j0 >> 5;
-            const unsigned bal = sm.ball[w];
-            if ((bal >> lane) & 1u) {
-                int pos = __popc(bal & ((1u << lane) - 1u));
-                for (int q = 0; q < w; q++) pos += __popc(sm.ball[q]);
-                sm.pre[pos] = j0 + lane;
+    __syncthreads();
+    const int total = sm.total;
+    *cntE = sm.below;
+    if (total == 0) return 0;
+#pragma unroll
+    for (int k = 0; k < kMaxBS / kCta; k++) {
+        const int j = k * kCta + threadIdx.x;
+        if (j < bs && vals[k] >= 1.0f) {
+            const int w = j >> 5;
+            const int pos = sm.pref[w] + __popc(sm.ball[w] & ((1u << lane) - 1u));
+            sm.pre[pos] = j;
+            const float sI = vals[k];
+            const float nsp = floorf(sI);
+            const float tsp = (sI - nsp) * dt;
+            const bool isE = j < nE;
+#pragma unroll
+            for (int ig = 0; ig < kMaxNG; ig++) {
+                if (ig < (isE ? P.ngE : P.ngI)) {
+                    float g = 0.f, h = 0.f;
+                    cond_input_v(isE ? P.condE.rise[ig] : P.condI.rise[ig], isE ? P.condE.decay[ig] : P.condI.decay[ig],
+                                 isE ? P.condE.dod[ig] : P.condI.dod[ig], g, h, nsp, dt - tsp);
+                    sm.og[ig][pos] = g;
+                    sm.oh[ig][pos] = h;
+                }
             }
         }
-        __syncthreads();
     }
-    *below = nb;
+    __syncthreads();
     return total;
 }
 
 // Phase A: delivery of step tp's spikes to this thread's neuron (all threads of the CTA
 // must call it; `active` masks the neuron work).
+template <bool Rng>
 __device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, int b, int local, int i,
                                              bool active, int itype, NState &st,
                                              curandStateMRG32k3a &condState, Smem &sm) {
     const int bs = P.blockSize, nV1 = P.nV1;
     const int ngE = P.ngE, ngI = P.ngI;
-    const float dt = P.dt;
     const float *sPrev = P.sInfo + (size_t)(tp & 1) * nV1;
     float lgE[kMaxNG], lhE[kMaxNG], lgI[kMaxNG], lhI[kMaxNG], ipE[kMaxNG], ipI[kMaxNG];
 #pragma unroll
@@ -182,32 +222,15 @@ __device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, in
     const int nnb = P.nNearNB[b];
     float *recNear = nullptr;
     int nNearDraw = 0;
-    if (P.recNear && active) {
+    if (Rng && P.recNear && active) {
         long long rs = tp - P.recStep0;
         if (rs >= 0 && rs < P.recSteps) recNear = P.recNear + ((size_t)rs * nV1 + i) * P.recCap;
     }
     for (int ib = 0; ib < nnb; ib++) {
         const int nb = P.nbId[b * P.nnbMax + ib];
         int cntE;
-        const int cnt = compact_spikers(sPrev + (size_t)nb * bs, bs, P.nE, sm, &cntE);
+        const int cnt = compact_spikers(P, sPrev + (size_t)nb * bs, sm, &cntE);
         if (cnt == 0) continue;
-        // unit conductance of each spiker (output_g/h of compute_V, :2008-2041)
-        for (int r = threadIdx.x; r < cnt; r += kCta) {
-            const float sI = sm.val[sm.pre[r]];
-            const float nsp = floorf(sI);
-            const float tsp = (sI - nsp) * dt;
-            const bool isE = r < cntE;
-#pragma unroll
-            for (int ig = 0; ig < kMaxNG; ig++) {
-                if (ig < (isE ? ngE : ngI)) {
-                    float g = 0.f, h = 0.f;
-                    cond_input(isE ? P.condE : P.condI, g, h, nsp, dt - tsp, ig);
-                    sm.og[ig][r] = g;
-                    sm.oh[ig][r] = h;
-                }
-            }
-        }
-        __syncthreads();
         if (active) {
             const float *col = P.conMat + ((size_t)(b * P.nnbMax + ib) * bs) * bs + local;
             for (int r0 = 0; r0 < cnt; r0 += kConBatch) {
@@ -221,25 +244,27 @@ __device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, in
                     float strength = sv[k];
                     if (r < cnt && strength > 0) {
                         const bool isE = r < cntE;
-                        if (P.condRng) {
-                            // pre type from the spiker's rank, as the reference does
-                            // (src/coredynamics.cu:2760-2766, 2815-2821)
-                            const int rank = isE ? r : r - cntE;
-                            const int ja = isE ? 0 : P.nTypeE, jb = isE ? P.nTypeE : P.nType;
-                            int jtype = ja;
-                            for (int jj = ja; jj < jb; jj++) {
-                                if (rank < P.typeAcc[jj]) { jtype = jj; break; }
+                        if constexpr (Rng) {
+                            if (P.condRng) {
+                                // pre type from the spiker's rank, as the reference does
+                                // (src/coredynamics.cu:2760-2766, 2815-2821)
+                                const int rank = isE ? r : r - cntE;
+                                const int ja = isE ? 0 : P.nTypeE, jb = isE ? P.nTypeE : P.nType;
+                                int jtype = ja;
+                                for (int jj = ja; jj < jb; jj++) {
+                                    if (rank < P.typeAcc[jj]) { jtype = jj; break; }
+                                }
+                                const int idx = jtype * P.nType + itype;
+                                const float lp = P.synFail[idx];
+                                const float normed_std = sqrtf(lp * (1 - lp) / P.synPerCon[idx]);
+                                const float rnd = curand_normal(&condState);
+                                if (recNear) {
+                                    if (nNearDraw < P.recCap) recNear[nNearDraw] = rnd;
+                                    else atomicOr(P.err, kErrRecordOverflow);
+                                }
+                                nNearDraw++;
+                                strength *= 1 - lp + normed_std * rnd;
                             }
-                            const int idx = jtype * P.nType + itype;
-                            const float lp = P.synFail[idx];
-                            const float normed_std = sqrtf(lp * (1 - lp) / P.synPerCon[idx]);
-                            const float rnd = curand_normal(&condState);
-                            if (recNear) {
-                                if (nNearDraw < P.recCap) recNear[nNearDraw] = rnd;
-                                else atomicOr(P.err, kErrRecordOverflow);
-                            }
-                            nNearDraw++;
-                            strength *= 1 - lp + normed_std * rnd;
                         }
                         if (strength > 0) {
                             if (isE) {
@@ -284,8 +309,8 @@ __device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, in
                     acc[(size_t)(2 * q + 1) * nV1 + i] = 0ull;
                 }
                 if (farSpiked) {
-                    const float fg = (float)((double)(long long)farG[q] / kFarScale);
-                    const float fh = (float)((double)(long long)farH[q] / kFarScale);
+                    const float fg = far_from_fixed(farG[q]);
+                    const float fh = far_from_fixed(farH[q]);
 #pragma unroll
                     for (int ig = 0; ig < kMaxNG; ig++) {
                         if (q < ngE && ig == q) { st.gE[ig] += fg; st.hE[ig] += fh; }
@@ -319,18 +344,60 @@ __device__ __forceinline__ float tonic_current(const V1Params &P, int itype, flo
     return (gL + aa) * (targetV - P.vL) - gL * deltaT * expf((targetV - vT) / deltaT);
 }
 
-// Phase B: one membrane step of neuron i.  lgnIds/lgnW hold the first min(m, kMaxLgnReg)
-// synapses when `regSyn` is set (persistent kernel); otherwise they are loaded here.
-// Returns the spike word.
-template <bool RegSyn>
+// One LGN synapse with spike word sFF and weight f (src/coredynamics.cu:1476-1500).
+template <bool Rng>
+__device__ __forceinline__ void lgn_input(const V1Params &P, int itype, float sFF, float f, bool backingUp,
+                                          float tBack, float pf, float nSynFF, float *g0, float *h0,
+                                          float *g1, float *h1, curandStateMRG32k3a &condState,
+                                          float *recFF, int &nFF) {
+    const float dt = P.dt;
+    const unsigned nspFF = (unsigned)floorf(sFF);
+    if (nspFF == 0) return;
+    const float tspFF = (sFF - nspFF) * dt;
+    if constexpr (Rng) {
+        if (pf > 0) {
+            const float normed_std = sqrtf(pf * (1 - pf) / nSynFF);
+            const float rnd = curand_normal(&condState);
+            if (recFF) {
+                if (nFF < P.recCap) recFF[nFF] = rnd;
+                else atomicOr(P.err, kErrRecordOverflow);
+            }
+            nFF++;
+            f *= 1 - pf + normed_std * rnd;
+        }
+    }
+    if (f > 0) {
+        const float ddt = backingUp ? tBack - tspFF : 0.f;
+#pragma unroll
+        for (int ig = 0; ig < kMaxNG; ig++) {
+            if (ig < P.ngFF) {
+                const float str = f * P.pFF[itype * P.ngFF + ig];
+                if (backingUp && ddt > 0) cond_input(P.condFF, g0[ig], h0[ig], str * nspFF, ddt, ig);
+                cond_input(P.condFF, g1[ig], h1[ig], str * nspFF, dt - tspFF, ig);
+            }
+        }
+    }
+}
+
+// Phase B: one membrane step of neuron i.  With RegSyn the synapse ids are the register
+// array lgnIds (up to kMaxLgnReg of them) and the weights are read only for synapses that
+// received a spike; otherwise ids and weights are loaded batch by batch.  Returns the
+// spike word.
+template <bool Rng, bool RegSyn>
 __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int i, int itype,
                                              float tonic, float depC, int m, const int *lgnIds,
-                                             const float *lgnW, const float *__restrict__ lgnSInfo,
+                                             const float *__restrict__ lgnSInfo,
                                              NState &st, curandStateMRG32k3a &condState,
                                              curandStateMRG32k3a &noisyState) {
     const int nV1 = P.nV1;
     const float dt = P.dt;
     const int ngE = P.ngE, ngI = P.ngI, ngFF = P.ngFF;
+    // spike words of this neuron's LGN inputs, gathered first so that they overlap the decay
+    float spReg[RegSyn ? kMaxLgnReg : 1];
+    if constexpr (RegSyn) {
+#pragma unroll
+        for (int q = 0; q < kMaxLgnReg; q++) spReg[q] = q < m ? __ldcg(lgnSInfo + lgnIds[q]) : 0.f;
+    }
     const float vR = P.vR[itype], vThres = P.vThres[itype], gL = P.gL[itype];
     const float Cm = P.C[itype], tRef = P.tRef[itype], vT = P.vT[itype];
     const float deltaT = P.deltaT[itype], tau_w = P.tau_w[itype], aa = P.a[itype];
@@ -347,7 +414,7 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
     for (int ig = 0; ig < kMaxNG; ig++) {
         ge[ig] = st.gE[ig]; he[ig] = st.hE[ig];
         if (ig < ngE) {
-            cond_decay(P.condE, st.gE[ig], st.hE[ig], dt, ig);
+            cond_decay_step(P.condE, P.decE, st.gE[ig], st.hE[ig], ig);
             gE_t1 += st.gE[ig];
         }
     }
@@ -355,7 +422,7 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
     for (int ig = 0; ig < kMaxNG; ig++) {
         gi[ig] = st.gI[ig]; hi[ig] = st.hI[ig];
         if (ig < ngI) {
-            cond_decay(P.condI, st.gI[ig], st.hI[ig], dt, ig);
+            cond_decay_step(P.condI, P.decI, st.gI[ig], st.hI[ig], ig);
             gI_t1 += st.gI[ig];
         }
     }
@@ -366,28 +433,31 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
         h1[ig] = st.hFF[ig];
         g0[ig] = g1[ig];
         h0[ig] = h1[ig];
-        if (ig < ngFF) cond_decay(P.condFF, g1[ig], h1[ig], dt, ig);
+        if (ig < ngFF) cond_decay_step(P.condFF, P.decFF, g1[ig], h1[ig], ig);
     }
     // noise (src/coredynamics.cu:1422-1440)
-    const float noiseRatio = P.noiseOnTonic ? tonic : 1.0f;
-    float noise1 = sqrtf(2 * P.noisyDep[itype] * (vT - vR) * noiseRatio * dt);
-    const float pf = P.synFailFF[itype];
-    const float nSynFF = P.synPerConFF[itype];
-    if (noise1 > 0) {
-        const float rnd = curand_normal(&noisyState);
-        if (P.recNoise) {
-            long long rs = t - P.recStep0;
-            if (rs >= 0 && rs < P.recSteps) P.recNoise[(size_t)rs * nV1 + i] = rnd;
-        }
-        noise1 *= rnd;
-        if (P.tau_noise > 0) {
-            noise1 /= P.tau_noise;
-            const float hk1 = -noise0 / P.tau_noise;
-            const float hk2 = -(noise0 + dt * hk1 + noise1) / P.tau_noise;
-            noise1 += noise0 + dt * (hk1 + hk2) / 2;
-            st.lastNoise = noise1;
+    float noise1 = 0.f;
+    if constexpr (Rng) {
+        const float noiseRatio = P.noiseOnTonic ? tonic : 1.0f;
+        noise1 = sqrtf(2 * P.noisyDep[itype] * (vT - vR) * noiseRatio * dt);
+        if (noise1 > 0) {
+            const float rnd = curand_normal(&noisyState);
+            if (P.recNoise) {
+                long long rs = t - P.recStep0;
+                if (rs >= 0 && rs < P.recSteps) P.recNoise[(size_t)rs * nV1 + i] = rnd;
+            }
+            noise1 *= rnd;
+            if (P.tau_noise > 0) {
+                noise1 /= P.tau_noise;
+                const float hk1 = -noise0 / P.tau_noise;
+                const float hk2 = -(noise0 + dt * hk1 + noise1) / P.tau_noise;
+                noise1 += noise0 + dt * (hk1 + hk2) / 2;
+                st.lastNoise = noise1;
+            }
         }
     }
+    const float pf = Rng ? P.synFailFF[itype] : 0.f;
+    const float nSynFF = P.synPerConFF[itype];
     const bool backingUp = tBack < dt && tBack > 0;
     const float depOut = depC + noise1;
     P.dep[i] = depOut;
@@ -396,63 +466,44 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
         for (int ig = 0; ig < kMaxNG; ig++)
             if (ig < ngFF) cond_decay(P.condFF, g0[ig], h0[ig], tBack, ig);
     }
-    // LGN input (src/coredynamics.cu:1466-1502), synapse order kept; loads gathered in
-    // batches so that they overlap
+    // LGN input (src/coredynamics.cu:1466-1502), synapse order kept
     float *recFF = nullptr;
     int nFF = 0;
-    if (P.recFF) {
+    if (Rng && P.recFF) {
         long long rs = t - P.recStep0;
         if (rs >= 0 && rs < P.recSteps) recFF = P.recFF + ((size_t)rs * nV1 + i) * P.recCap;
     }
-    // (RegSyn: the synapse list is register resident, so the loop is unrolled over its
-    // compile-time capacity; otherwise ids and weights are loaded batch by batch)
+    if constexpr (RegSyn) {
+        // synapses that received a spike, as a bit mask; they are visited in synapse order
+        unsigned mask = 0u;
 #pragma unroll
-    for (int q0 = 0; q0 < (RegSyn ? kMaxLgnReg : 1 << 30); q0 += kLgnBatch) {
-        if (q0 >= m) break;
-        int ids[kLgnBatch];
-        float fs[kLgnBatch], sp[kLgnBatch];
-#pragma unroll
-        for (int k = 0; k < kLgnBatch; k++) {
-            const int q = q0 + k;
-            if constexpr (RegSyn) {
-                ids[k] = lgnIds[q];
-                fs[k] = lgnW[q];
-            } else {
-                const size_t lid = (size_t)q * nV1 + i;
-                ids[k] = q < m ? __ldg(P.lgnId + lid) : 0;
-                fs[k] = q < m ? __ldg(P.sLGN + lid) : 0.f;
-            }
+        for (int q = 0; q < kMaxLgnReg; q++) mask |= (spReg[q] >= 1.0f ? 1u : 0u) << q;
+        while (mask) {
+            const int q = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const size_t lid = (size_t)q * nV1 + i;
+            const float sFF = __ldcg(lgnSInfo + __ldg(P.lgnId + lid));
+            const float f = __ldg(P.sLGN + lid);
+            lgn_input<Rng>(P, itype, sFF, f, backingUp, tBack, pf, nSynFF, g0, h0, g1, h1, condState, recFF,
+                           nFF);
         }
+    } else {
+        for (int q0 = 0; q0 < m; q0 += kLgnBatch) {
+            int ids[kLgnBatch];
+            float fs[kLgnBatch], sp[kLgnBatch];
 #pragma unroll
-        for (int k = 0; k < kLgnBatch; k++) sp[k] = q0 + k < m ? __ldcg(lgnSInfo + ids[k]) : 0.f;
+            for (int k = 0; k < kLgnBatch; k++) {
+                const size_t lid = (size_t)(q0 + k) * nV1 + i;
+                ids[k] = q0 + k < m ? __ldg(P.lgnId + lid) : 0;
+                fs[k] = q0 + k < m ? __ldg(P.sLGN + lid) : 0.f;
+            }
 #pragma unroll
-        for (int k = 0; k < kLgnBatch; k++) {
-            const float sFF = sp[k];
-            const unsigned nspFF = (unsigned)floorf(sFF);
-            if (q0 + k < m && nspFF > 0) {
-                float f = fs[k];
-                const float tspFF = (sFF - nspFF) * dt;
-                if (pf > 0) {
-                    const float normed_std = sqrtf(pf * (1 - pf) / nSynFF);
-                    const float rnd = curand_normal(&condState);
-                    if (recFF) {
-                        if (nFF < P.recCap) recFF[nFF] = rnd;
-                        else atomicOr(P.err, kErrRecordOverflow);
-                    }
-                    nFF++;
-                    f *= 1 - pf + normed_std * rnd;
-                }
-                if (f > 0) {
-                    const float ddt = backingUp ? tBack - tspFF : 0.f;
+            for (int k = 0; k < kLgnBatch; k++) sp[k] = q0 + k < m ? __ldcg(lgnSInfo + ids[k]) : 0.f;
 #pragma unroll
-                    for (int ig = 0; ig < kMaxNG; ig++) {
-                        if (ig < ngFF) {
-                            const float str = f * P.pFF[itype * ngFF + ig];
-                            if (backingUp && ddt > 0) cond_input(P.condFF, g0[ig], h0[ig], str * nspFF, ddt, ig);
-                            cond_input(P.condFF, g1[ig], h1[ig], str * nspFF, dt - tspFF, ig);
-                        }
-                    }
-                }
+            for (int k = 0; k < kLgnBatch; k++) {
+                if (q0 + k < m)
+                    lgn_input<Rng>(P, itype, sp[k], fs[k], backingUp, tBack, pf, nSynFF, g0, h0, g1, h1, condState,
+                                   recFF, nFF);
             }
         }
     }
@@ -550,79 +601,185 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
     return sInfo;
 }
 
-// Phase C: one event per (spike, far synapse), arrival step and offset as recal_G_vec
-// computes them (src/coredynamics.cu:282-333), with explicitly rounded operations as on the
-// reference's host.  All threads of the CTA call it.
-__device__ __forceinline__ void far_phase(const V1Params &P, long long t, int i, bool active,
-                                          float sInfo, Smem &sm) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) P.farFlag[(t + 1) % 3] = 0;
-    if (active && sInfo > 1.0f && P.farPre[i]) P.farFlag[t % 3] = 1;
-    const bool push = active && sInfo >= 1.0f && P.farOff[i + 1] > P.farOff[i];
-    if (__syncthreads_or(push) == 0) return;
-    const int nV1 = P.nV1, bs = P.blockSize;
+// One far event: the spike of `pre` at step t (spike word sI) through far synapse e, in its
+// k-th arrival slot; arrival step and offset as recal_G_vec computes them
+// (src/coredynamics.cu:282-333), with explicitly rounded operations as on the reference's host.
+__device__ __forceinline__ void far_event(const V1Params &P, long long t, int pre, float sI, int post,
+                                          float f, int steps, int ptype, float frac, int kk) {
     const float dt = P.dt;
-    const unsigned bal = __ballot_sync(0xffffffffu, push);
-    if ((threadIdx.x & 31) == 0) sm.ball[threadIdx.x >> 5] = bal;
-    __syncthreads();
-    int cnt = 0, pos = 0;
-    for (int w = 0; w < kWarps; w++) {
-        const int c = __popc(sm.ball[w]);
-        if (w < (int)(threadIdx.x >> 5)) pos += c;
-        cnt += c;
+    const unsigned nsp = (unsigned)floorf(sI);
+    // dtsp = (sInfo - nsp + k)*dt - time2post, rounded step by step
+    const float x = __fadd_rn(__fsub_rn(sI, (float)nsp), (float)kk);
+    const float dtsp = __fsub_rn(__fmul_rn(x, dt), frac);
+    if (!(dtsp < dt && dtsp >= 0 && f > 0)) return;
+    const long long tArr = t + steps - kk;
+    if (tArr < t || tArr - t >= P.farDepth - 1) {
+        atomicOr(P.err, kErrFarOverflow);
+        return;
     }
-    if (push) {
-        pos += __popc(bal & ((1u << (threadIdx.x & 31)) - 1u));
-        sm.pre[pos] = i;
-        sm.val[pos] = sInfo;
-    }
-    __syncthreads();
+    const int nV1 = P.nV1;
     const int ns = P.ngE + P.ngI;
-    for (int r = 0; r < cnt; r++) {
-        const int pre = sm.pre[r];
-        const float sI = sm.val[r];
-        const unsigned nsp = (unsigned)floorf(sI);
-        const bool preE = (pre % bs) < P.nE;
-        const int ng = preE ? P.ngE : P.ngI;
-        const int qoff = preE ? 0 : P.ngE;
-        const int e1 = P.farOff[pre + 1];
-        for (int e = P.farOff[pre] + threadIdx.x; e < e1; e += kCta) {
-            const int post = P.farPost[e];
-            const float f = P.farStr[e];
-            const int steps = P.farSteps[e];
-            const float frac = P.farFrac[e];
-            const int ptype = type_of(P, post % bs);
+    const bool preE = (pre % P.blockSize) < P.nE;
+    const int ng = preE ? P.ngE : P.ngI;
+    const int qoff = preE ? 0 : P.ngE;
+    const float delta = __fsub_rn(dt, dtsp);
+    unsigned long long *acc = P.farAcc + (size_t)(tArr % P.farDepth) * ns * 2 * nV1;
 #pragma unroll
-            for (int kk = 0; kk < 2; kk++) {
-                // dtsp = (sInfo - nsp + k)*dt - time2post, rounded step by step
-                const float x = __fadd_rn(__fsub_rn(sI, (float)nsp), (float)kk);
-                const float dtsp = __fsub_rn(__fmul_rn(x, dt), frac);
-                if (dtsp < dt && dtsp >= 0 && f > 0) {
-                    const long long tArr = t + steps - kk;
-                    if (tArr < t || tArr - t >= P.farDepth - 1) {
-                        atomicOr(P.err, kErrFarOverflow);
-                        continue;
-                    }
-                    const float delta = __fsub_rn(dt, dtsp);
-                    unsigned long long *acc = P.farAcc + (size_t)(tArr % P.farDepth) * ns * 2 * nV1;
-#pragma unroll
-                    for (int ig = 0; ig < kMaxNG; ig++) {
-                        if (ig < ng) {
-                            const float ip = preE ? P.pE[ptype * P.ngE + ig] : P.pI[ptype * P.ngI + ig];
-                            const float fv = __fmul_rn(__fmul_rn((float)nsp, f), ip);
-                            float g = 0.f, h = 0.f;
-                            cond_input(preE ? P.condE : P.condI, g, h, fv, delta, ig);
-                            const long long qg = __double2ll_rn((double)g * kFarScale);
-                            const long long qh = __double2ll_rn((double)h * kFarScale);
-                            atomicAdd(&acc[(size_t)(2 * (qoff + ig)) * nV1 + post], (unsigned long long)qg);
-                            atomicAdd(&acc[(size_t)(2 * (qoff + ig) + 1) * nV1 + post], (unsigned long long)qh);
-                        }
-                    }
-                }
-            }
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        if (ig < ng) {
+            const float ip = preE ? P.pE[ptype * P.ngE + ig] : P.pI[ptype * P.ngI + ig];
+            const float fv = __fmul_rn(__fmul_rn((float)nsp, f), ip);
+            float g = 0.f, h = 0.f;
+            cond_input_v(preE ? P.condE.rise[ig] : P.condI.rise[ig], preE ? P.condE.decay[ig] : P.condI.decay[ig],
+                         preE ? P.condE.dod[ig] : P.condI.dod[ig], g, h, fv, delta);
+            atomicAdd(&acc[(size_t)(2 * (qoff + ig)) * nV1 + post], (unsigned long long)far_to_fixed(g));
+            atomicAdd(&acc[(size_t)(2 * (qoff + ig) + 1) * nV1 + post], (unsigned long long)far_to_fixed(h));
         }
     }
 }
 
+// Exclusive prefix of sm.fdeg[0..cnt) into sm.fpref (warp 0), total in sm.fpref[cnt].
+__device__ __forceinline__ void scan_degrees(Smem &sm, int cnt) {
+    const int lane = threadIdx.x & 31;
+    if ((threadIdx.x >> 5) == 0) {
+        int run = 0;
+        for (int base = 0; base < cnt; base += 32) {
+            const int r = base + lane;
+            const int d = r < cnt ? sm.fdeg[r] : 0;
+            int incl = d;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (r < cnt) sm.fpref[r] = run + incl - d;
+            run += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (lane == 0) sm.fpref[cnt] = run;
+    }
+}
+
+// Entry r of the chunk in shared memory that owns flattened work item w: the last r with
+// fpref[r] <= w.
+__device__ __forceinline__ int owner_of(const Smem &sm, int cnt, int w) {
+    int lo = 0, hi = cnt - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sm.fpref[mid] <= w) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Phase C, part 1 (runs in step tl + 1): the far events of step tl's spikes that arrive after
+// step tl, from the step's global spiker list.  The (spiker, synapse) work is flattened over
+// every thread of the grid, so one CTA's burst of spikers no longer serialises on that CTA;
+// the fixed-point ring makes the sums independent of the order of the atomic appends.
+__device__ __forceinline__ void far_push_list(const V1Params &P, long long tl, Smem &sm) {
+    const int slot = (int)((tl + 3) % 3);  // tl >= -1
+    const int n = __ldcg(P.farCount + slot);
+    if (n == 0) return;
+    const int4 *list = P.farList + (size_t)slot * P.nV1;
+    const int G = gridDim.x * kCta;
+    const int gt = blockIdx.x * kCta + threadIdx.x;
+    int W0 = 0;  // work of the earlier chunks, modulo G
+    for (int c0 = 0; c0 < n; c0 += kCta) {
+        const int cnt = min(kCta, n - c0);
+        __syncthreads();
+        if (threadIdx.x < cnt) {
+            const int4 e = __ldcg(list + c0 + threadIdx.x);
+            sm.fpre[threadIdx.x] = e.x;
+            sm.fe0[threadIdx.x] = e.y;
+            sm.fdeg[threadIdx.x] = e.z;
+            sm.fsi[threadIdx.x] = __int_as_float(e.w);
+        }
+        __syncthreads();
+        scan_degrees(sm, cnt);
+        __syncthreads();
+        const int work = sm.fpref[cnt];
+        // this thread takes the items whose global index is congruent to gt modulo G
+        int w = gt - W0;
+        if (w < 0) w += G;
+        for (; w < work; w += G) {
+            const int r = owner_of(sm, cnt, w);
+            const int e = sm.fe0[r] + (w - sm.fpref[r]);
+            const int post = __ldg(P.farPost + e);
+            const float f = __ldg(P.farStr + e);
+            const int sp = __ldg(P.farSteps + e);
+            const float frac = __ldg(P.farFrac + e);
+            const int steps = sp & 0xffff, ptype = (sp >> 16) & 0xff;
+            const int pre = sm.fpre[r];
+            const float sI = sm.fsi[r];
+            // the slot arriving in step tl itself (steps == k) was pushed in step tl
+            if (steps != 0) far_event(P, tl, pre, sI, post, f, steps, ptype, frac, 0);
+            if (steps != 1) far_event(P, tl, pre, sI, post, f, steps, ptype, frac, 1);
+        }
+        W0 = (int)(((long long)W0 + work) % G);
+    }
+}
+
+// Phase C, part 2 (runs in step t): appends this CTA's far presynaptic spikers to step t's
+// global list (one atomic per warp), and pushes the events that arrive within step t itself
+// (whole-step delay 0 or 1: the first n1 synapses of each list), which must be in the ring
+// before the next step delivers it.  All threads of the CTA call it.
+__device__ __forceinline__ void far_phase(const V1Params &P, long long t, int i, bool active, float sInfo,
+                                          bool isFarPre, int e0, int deg, int n1, Smem &sm) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        P.farFlag[(t + 1) % 3] = 0;
+        P.farCount[(t + 1) % 3] = 0;
+    }
+    if (active && sInfo > 1.0f && isFarPre) P.farFlag[t % 3] = 1;
+    const bool spk = active && sInfo >= 1.0f;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool app = spk && deg > 0;
+    const unsigned ab = __ballot_sync(0xffffffffu, app);
+    if (ab) {
+        const int leader = __ffs(ab) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(P.farCount + t % 3, __popc(ab));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (app)
+            P.farList[(size_t)(t % 3) * P.nV1 + base + __popc(ab & ((1u << lane) - 1u))] =
+                make_int4(i, e0, deg, __float_as_int(sInfo));
+    }
+    const bool push = spk && n1 > 0;
+    const unsigned bal = __ballot_sync(0xffffffffu, push);
+    if (lane == 0) sm.fball[warp] = bal;
+    __syncthreads();
+    // list of this CTA's neurons with same-step events (ascending) and their counts
+    int cnt = 0, pos = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; w++) {
+        const int c = __popc(sm.fball[w]);
+        if (w < warp) pos += c;
+        cnt += c;
+    }
+    if (cnt == 0) return;
+    if (push) {
+        pos += __popc(bal & ((1u << lane) - 1u));
+        sm.fpre[pos] = i;
+        sm.fsi[pos] = sInfo;
+        sm.fe0[pos] = e0;
+        sm.fdeg[pos] = n1;
+    }
+    __syncthreads();
+    scan_degrees(sm, cnt);
+    __syncthreads();
+    const int work = sm.fpref[cnt];
+    for (int w = threadIdx.x; w < work; w += kCta) {
+        const int r = owner_of(sm, cnt, w);
+        const int e = sm.fe0[r] + (w - sm.fpref[r]);
+        const int post = __ldg(P.farPost + e);
+        const float f = __ldg(P.farStr + e);
+        const int sp = __ldg(P.farSteps + e);
+        const float frac = __ldg(P.farFrac + e);
+        const int steps = sp & 0xffff;
+        // steps is 0 or 1 here: the slot with tArr == t
+        far_event(P, t, sm.fpre[r], sm.fsi[r], post, f, steps, (sp >> 16) & 0xff, frac, steps);
+    }
+}
+
+template <bool Rng>
 __global__ void __launch_bounds__(kCta) v1_step_kernel(V1Params P, const long long *stepBase,
                                                        int stepOffset,
                                                        const float *__restrict__ lgnRing,
@@ -641,14 +798,14 @@ __global__ void __launch_bounds__(kCta) v1_step_kernel(V1Params P, const long lo
     NState st;
     load_state(P, i, st);
     curandStateMRG32k3a condState, noisyState;
-    if (P.condRng && active) condState = P.rGenCond[i];
-    if (P.noiseRng && active) noisyState = P.rNoisy[i];
+    if (Rng && P.condRng && active) condState = P.rGenCond[i];
+    if (Rng && P.noiseRng && active) noisyState = P.rNoisy[i];
 
-    if (deliverPrev) deliver_prev(P, t - 1, b, local, i, active, itype, st, condState, sm);
+    if (deliverPrev) deliver_prev<Rng>(P, t - 1, b, local, i, active, itype, st, condState, sm);
     if (!doStep) {
         if (active) {
             store_state(P, i, st);
-            if (P.condRng) P.rGenCond[i] = condState;
+            if (Rng && P.condRng) P.rGenCond[i] = condState;
         }
         return;
     }
@@ -657,13 +814,20 @@ __global__ void __launch_bounds__(kCta) v1_step_kernel(V1Params P, const long lo
         const float tonic = P.tonicDep[i];
         const float depC = tonic_current(P, itype, tonic);
         const float *lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
-        sInfo = step_neuron<false>(P, t, i, itype, tonic, depC, P.nLGNperV1[i], nullptr, nullptr, lgnSInfo,
-                                   st, condState, noisyState);
+        sInfo = step_neuron<Rng, false>(P, t, i, itype, tonic, depC, P.nLGNperV1[i], nullptr, lgnSInfo, st,
+                                        condState, noisyState);
         store_state(P, i, st);
-        if (P.condRng) P.rGenCond[i] = condState;
-        if (P.noiseRng) P.rNoisy[i] = noisyState;
+        if (Rng && P.condRng) P.rGenCond[i] = condState;
+        if (Rng && P.noiseRng) P.rNoisy[i] = noisyState;
     }
-    if (P.farOn) far_phase(P, t, i, active, sInfo, sm);
+    if (P.farOn) {
+        const int e0 = active ? P.farOff[i] : 0;
+        const int deg = active ? P.farOff[i + 1] - e0 : 0;
+        const int n1 = active ? P.farN1[i] : 0;
+        const bool isFarPre = active && P.farPre[i];
+        far_push_list(P, t - 1, sm);
+        far_phase(P, t, i, active, sInfo, isFarPre, e0, deg, n1, sm);
+    }
 }
 
 // Grid-wide barrier between the steps of the persistent kernel: arrive on a counter, the
@@ -689,7 +853,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned *gen, uns
                     ok = 0;
                     break;
                 }
-                if (spins > 64) __nanosleep(40);
+                if (spins > 64) __nanosleep(32);
             }
         }
         __threadfence();
@@ -701,7 +865,8 @@ __device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned *gen, uns
 }
 
 // K steps in one cooperative launch.  Neuron state, generators and up to kMaxLgnReg LGN
-// synapses stay in registers; one grid barrier separates consecutive steps.
+// synapse ids stay in registers; one grid barrier separates consecutive steps.
+template <bool Rng>
 __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, const long long *stepBase,
                                                                  int K, const float *__restrict__ lgnRing,
                                                                  int lgnSlots, int deliverFirst,
@@ -719,35 +884,38 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
     NState st;
     load_state(P, i, st);
     curandStateMRG32k3a condState, noisyState;
-    if (P.condRng && active) condState = P.rGenCond[i];
-    if (P.noiseRng && active) noisyState = P.rNoisy[i];
+    if (Rng && P.condRng && active) condState = P.rGenCond[i];
+    if (Rng && P.noiseRng && active) noisyState = P.rNoisy[i];
     const float tonic = active ? P.tonicDep[i] : 0.f;
     const float depC = tonic_current(P, itype, tonic);
     const int m = active ? P.nLGNperV1[i] : 0;
     int lgnIds[kMaxLgnReg];
-    float lgnW[kMaxLgnReg];
 #pragma unroll
-    for (int q = 0; q < kMaxLgnReg; q++) {
-        const size_t lid = (size_t)q * P.nV1 + i;
-        lgnIds[q] = q < m ? __ldg(P.lgnId + lid) : 0;
-        lgnW[q] = q < m ? __ldg(P.sLGN + lid) : 0.f;
-    }
+    for (int q = 0; q < kMaxLgnReg; q++) lgnIds[q] = q < m ? __ldg(P.lgnId + (size_t)q * P.nV1 + i) : 0;
+    // this neuron's outgoing far list (static for the run)
+    const int farE0 = (P.farOn && active) ? P.farOff[i] : 0;
+    const int farDeg = (P.farOn && active) ? P.farOff[i + 1] - farE0 : 0;
+    const int farN1 = (P.farOn && active) ? P.farN1[i] : 0;
+    const bool isFarPre = P.farOn && active && P.farPre[i];
     for (int s = 0; s < K; s++) {
         const long long t = t0 + s;
-        if (s > 0 || deliverFirst) deliver_prev(P, t - 1, b, local, i, active, itype, st, condState, sm);
+        if (s > 0 || deliverFirst) deliver_prev<Rng>(P, t - 1, b, local, i, active, itype, st, condState, sm);
         float sInfo = 0.f;
         if (active) {
             const float *lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
-            sInfo = step_neuron<true>(P, t, i, itype, tonic, depC, m, lgnIds, lgnW, lgnSInfo, st, condState,
-                                      noisyState);
+            sInfo = step_neuron<Rng, true>(P, t, i, itype, tonic, depC, m, lgnIds, lgnSInfo, st, condState,
+                                           noisyState);
         }
-        if (P.farOn) far_phase(P, t, i, active, sInfo, sm);
+        if (P.farOn) {
+            far_push_list(P, t - 1, sm);
+            far_phase(P, t, i, active, sInfo, isFarPre, farE0, farDeg, farN1, sm);
+        }
         if (s + 1 < K && !grid_barrier(barrier, barrier + 1, gridDim.x, P.err)) break;
     }
     if (active) {
         store_state(P, i, st);
-        if (P.condRng) P.rGenCond[i] = condState;
-        if (P.noiseRng) P.rNoisy[i] = noisyState;
+        if (Rng && P.condRng) P.rGenCond[i] = condState;
+        if (Rng && P.noiseRng) P.rNoisy[i] = noisyState;
     }
 }
 
@@ -769,12 +937,49 @@ __global__ void v1_rng_init_kernel(curandStateMRG32k3a *cond, curandStateMRG32k3
 
 __global__ void advance_step_kernel(long long *stepBase, int k) { *stepBase += k; }
 
+// Full-step decay factors, evaluated with the same expressions as cond_decay (one thread).
+__global__ void step_decay_kernel(Cond cFF, Cond cE, Cond cI, float dt, StepDecay *out) {
+    if (threadIdx.x != 0) return;
+    const Cond *cs[3] = {&cFF, &cE, &cI};
+    for (int k = 0; k < 3; k++) {
+        for (int ig = 0; ig < kMaxNG; ig++) {
+            out[k].etr[ig] = expf(-dt / cs[k]->rise[ig]);
+            out[k].etd[ig] = expf(-dt / cs[k]->decay[ig]);
+        }
+    }
+}
+
+cudaError_t compute_step_decay(V1Params &p, cudaStream_t st) {
+    StepDecay *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, 3 * sizeof(StepDecay));
+    if (e != cudaSuccess) return e;
+    step_decay_kernel<<<1, 32, 0, st>>>(p.condFF, p.condE, p.condI, p.dt, d);
+    StepDecay h[3];
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d);
+    if (e != cudaSuccess) return e;
+    p.decFF = h[0];
+    p.decE = h[1];
+    p.decI = h[2];
+    return cudaSuccess;
+}
+
+// The random-number paths are needed when a draw can change a result (the draws are then
+// also recorded when recording is on).
+static bool needs_rng(const V1Params &p) { return p.condRng || p.noiseRng; }
+
 cudaError_t launch_v1_step(const V1Params &p, const long long *stepBase, int stepOffset,
                            const float *lgnSInfo, int lgnSlots, int deliverPrev, int doStep,
                            cudaStream_t st) {
     const int nq = (p.blockSize + kCta - 1) / kCta;
-    v1_step_kernel<<<p.nblock * nq, kCta, 0, st>>>(p, stepBase, stepOffset, lgnSInfo, lgnSlots,
-                                                   deliverPrev, doStep);
+    if (needs_rng(p))
+        v1_step_kernel<true><<<p.nblock * nq, kCta, 0, st>>>(p, stepBase, stepOffset, lgnSInfo, lgnSlots,
+                                                             deliverPrev, doStep);
+    else
+        v1_step_kernel<false><<<p.nblock * nq, kCta, 0, st>>>(p, stepBase, stepOffset, lgnSInfo, lgnSlots,
+                                                              deliverPrev, doStep);
     return cudaGetLastError();
 }
 
@@ -783,7 +988,10 @@ int v1_persistent_ctas(const V1Params &p, int device, bool *fits) {
     const int nq = (p.blockSize + kCta - 1) / kCta;
     const int n = p.nblock * nq;
     int perSM = 0, sms = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_persistent_kernel, kCta, 0);
+    if (needs_rng(p))
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_persistent_kernel<true>, kCta, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_persistent_kernel<false>, kCta, 0);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     int coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
@@ -804,8 +1012,11 @@ cudaError_t launch_v1_persistent(const V1Params &p, const long long *stepBase, i
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, v1_persistent_kernel, p, stepBase, K, lgnRing, lgnSlots, deliverFirst,
-                              barrier);
+    if (needs_rng(p))
+        return cudaLaunchKernelEx(&cfg, v1_persistent_kernel<true>, p, stepBase, K, lgnRing, lgnSlots,
+                                  deliverFirst, barrier);
+    return cudaLaunchKernelEx(&cfg, v1_persistent_kernel<false>, p, stepBase, K, lgnRing, lgnSlots,
+                              deliverFirst, barrier);
 }
 
 cudaError_t launch_v1_rng_init(curandStateMRG32k3a *cond, curandStateMRG32k3a *noisy,

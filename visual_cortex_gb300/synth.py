@@ -81,7 +81,7 @@ def make_lgn(n_lgn: int, rng: np.random.Generator, patch_deg: float, dt: float,
              frame_rate: int = 120, mSample1D: int = 16, mau: float = 250.0,
              mKernelSample: int = 250, sigma_c: float = 0.03, sigma_s: float = 0.09,
              stim_range_deg: float | None = None, buffer_deg: float = 0.2,
-             jitter: float = 0.0) -> tuple[LgnSpec, float]:
+             jitter: float = 0.0, tjitter: float = 0.0) -> tuple[LgnSpec, float]:
     """ON/OFF magno cells with centers uniform in a patch_deg square around the fixation.
 
     Returns the spec and the full stimulus extent (deg) the texture spans (flat retina)."""
@@ -106,8 +106,8 @@ def make_lgn(n_lgn: int, rng: np.random.Generator, patch_deg: float, dt: float,
         polar=two(polar, polar), ecc=two(ecc, ecc), rw=two(sc * DEG, ss * DEG),
         rh=two(sc * DEG, ss * DEG), orient=two(np.zeros(n_lgn), np.zeros(n_lgn)),
         k=two(k_center, -k_center), ratio=two(np.full(n_lgn, 1.0), np.full(n_lgn, 1.0)),
-        tauR=two(np.full(n_lgn, 1.5), np.full(n_lgn, 1.5)),
-        tauD=two(np.full(n_lgn, 4.5), np.full(n_lgn, 4.5)),
+        tauR=two(1.5 * (1 + tjitter * rng.uniform(-1, 1, n_lgn)), np.full(n_lgn, 1.5)),
+        tauD=two(4.5 * (1 + tjitter * rng.uniform(-1, 1, n_lgn)), np.full(n_lgn, 4.5)),
         nR=two(np.full(n_lgn, 19.0), np.full(n_lgn, 19.0)),
         nD=two(np.full(n_lgn, 9.5), np.full(n_lgn, 9.5)),
         delay=two(np.full(n_lgn, 14.0), np.full(n_lgn, 14.0)),
@@ -239,12 +239,12 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
                   adex_inh: bool = False, patch_deg: float = 2.0, nFrame: int = 120,
                   wFF: float = 0.2, wE: float = 0.004, wI: float = 0.6, wFar: float = 0.002,
                   noisyDep=(0.0, 0.0), synFail=(0.0, 0.0, 0.0, 0.0), synFailFF=(0.0, 0.0),
-                  mSample1D: int = 16, dt: float = 0.125) -> Workload:
+                  mSample1D: int = 16, dt: float = 0.125, tjitter: float = 0.0) -> Workload:
     """Builds one synthetic patch; C1 = 1x1024 V1 / 512 LGN; C2 = 32 blocks / 16384 LGN."""
     rng = np.random.default_rng(seed)
     spec = make_spec(nblock, adex_inh=adex_inh, noisyDep=noisyDep, synFail=synFail,
                      synFailFF=synFailFF, dt=dt)
-    lgn, extent = make_lgn(n_lgn, rng, patch_deg, dt, mSample1D=mSample1D)
+    lgn, extent = make_lgn(n_lgn, rng, patch_deg, dt, mSample1D=mSample1D, tjitter=tjitter)
     side = 0.5
     pos, nbx = block_positions(nblock, spec.blockSize, side, rng)
     conMat = near_conmat(spec, pos, rng, sigma=0.1, nE_partners=100, nI_partners=50,

@@ -1,0 +1,81 @@
+"""The cfg-driven run: reference-format inputs in, reference-format outputs out."""
+import tempfile
+
+import numpy as np
+import pytest
+
+from visual_cortex_gb300 import cfg, driver, formats as FM, synth
+
+
+@pytest.fixture(scope="module")
+def written():
+    wl = synth.make_workload("drv", seed=2, nblock=2, n_lgn=512, m=20, width=64, height=64,
+                             nt=96, far_partners=50, adex_inh=True, nFrame=60)
+    d = tempfile.mkdtemp()
+    fn = synth.write_reference_files(wl, d, seed=2, nt=96)
+    return wl, fn
+
+
+def test_build_reads_back_the_workload(written):
+    wl, fn = written
+    m = driver.build(cfg.load(["-c", fn]))
+    assert m.spec == wl.spec
+    for k in ("nLGNperV1", "lgnId", "sLGN", "nNearNB", "nbId", "conMat", "nVec", "vecID",
+              "conVec", "delayVec"):
+        assert np.array_equal(getattr(m.net, k), getattr(wl.net, k)), k
+    assert np.array_equal(m.stim.frames, wl.stim.frames)
+    assert m.lgn.sched == wl.lgn.sched
+    # CmoreDep tonic drive: tonicDep * (minTonicRatio + (1 - minTonicRatio) * scaled ratio)
+    t = m.spec.type_of(np.arange(m.spec.nV1) % m.spec.blockSize)
+    assert np.all(m.net.tonicDep[t == 0] <= np.float32(0.6) + 1e-6)
+    assert np.all(m.net.tonicDep[t == 0] >= np.float32(0.3) - 1e-6)
+    # trainDepth from the largest connected within-block distance
+    assert m.seeds.trainDepth >= 2
+
+
+def test_scaling_rules(written):
+    wl, fn = written
+    m = driver.build(cfg.load(["-c", fn, "--sRatioV1", "0.5,2,3,4", "--sRatioLGN", "2"]))
+    bs, nE = m.spec.blockSize, m.spec.nE
+    c = m.net.conMat[0, 0]
+    c0 = wl.net.conMat[0, 0]
+    np.testing.assert_array_equal(c[:nE, :nE], (c0[:nE, :nE] * np.float32(0.5)).astype(np.float32))
+    np.testing.assert_array_equal(c[:nE, nE:], (c0[:nE, nE:] * np.float32(2)).astype(np.float32))
+    np.testing.assert_array_equal(c[nE:, :nE], (c0[nE:, :nE] * np.float32(3)).astype(np.float32))
+    np.testing.assert_array_equal(m.net.sLGN, (wl.net.sLGN * np.float32(2)).astype(np.float32))
+
+
+def test_unsupported_keys_fail_loudly(written):
+    _, fn = written
+    with pytest.raises(cfg.ConfigError, match="learning"):
+        driver.build(cfg.load(["-c", fn, "--learning", "1"]))
+    with pytest.raises(cfg.ConfigError, match="noDelay"):
+        driver.build(cfg.load(["-c", fn, "--noDelay", "0", "--noFarDelay", "0"]))
+
+
+@pytest.mark.gpu
+def test_run_writes_reference_outputs(written, native):
+    from visual_cortex_gb300.model import Simulation
+    from visual_cortex_gb300 import _native as N
+    wl, fn = written
+    c = cfg.load(["-c", fn])
+    m = driver.run(c, chunk=40, log=lambda *_: None)
+    P = cfg.resolve_paths(c)
+    h, raw = FM.read_raw(P.raw)
+    assert h["nt"] == 96 and h["nV1"] == m.spec.nV1 and h["mI"] == m.spec.nI * m.spec.nblock
+    dt, sp = FM.read_lgn_sp(P.lgn_sp)
+    fr = FM.read_lgn_fr(P.lgn_fr)
+    sim = Simulation(m.spec, m.net, m.lgn, m.stim, m.init, m.seeds)
+    try:
+        sim.set_record(N.REC_RAW | N.REC_LGN_SP | N.REC_LGN_FR, 96)
+        sim.run(96)
+        r2, sp2, fr2 = sim.fetch_records(0, 96, raw=True, lgn_sp=True, lgn_fr=True)
+    finally:
+        sim.close()
+    np.testing.assert_array_equal(raw, r2)
+    np.testing.assert_array_equal(sp, sp2)
+    np.testing.assert_array_equal(fr, fr2)
+    assert (raw[:, :m.spec.nV1] >= 1).sum() > 0 or (sp >= 1).sum() > 0
+    b = open(P.patchV1_cfg, "rb").read()
+    assert np.frombuffer(b[:4], np.uint32)[0] == 4
+    assert np.frombuffer(b[4:16], np.float32).tolist() == [m.spec.vL, m.spec.vE, m.spec.vI]

@@ -1,0 +1,339 @@
+"""The `patch` run as a library call: config + binary inputs -> GPU simulation -> outputs.
+
+``python -m visual_cortex_gb300 -c patchV1.cfg [-s seed]`` reads the keys of cfg.py, the input
+files of formats.py, builds the model objects with the reference's scaling and expansion
+rules (src/patch.cu:612-1060 options, 3313-3700 connectivity, 4100-4220 tonic drive, 4278-4301
+LGN->V1 lists, 4405-4560 initial state), runs the steps on the GPU and writes rawData,
+LGN_fr, LGN_sp and patchV1_cfg with the reference's headers and record order.
+
+Supported: magno (ON/OFF) LGN read from the LGN parameter file (useNewLGN = false), flat
+retina, learning = 0, no gap junctions, no orientation boost (nOri = 0), no snapshot
+restore, minimal = false.  Anything else raises ConfigError naming the key.
+"""
+from __future__ import annotations
+
+import math
+import sys
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import formats as FM
+from .cfg import Config, ConfigError, load, resolve_paths
+from .model import InitState, LgnSpec, Seeds, Stimulus, V1Network, V1Spec, host_init_state
+from .schedule import make_schedule
+
+f32, u32 = np.float32, np.uint32
+DEG = math.pi / 180.0
+
+
+def _per_type(c: Config, key: str, n: int, required=True, default=None):
+    """Size-1 vectors are replicated to n; otherwise the size must be n (src/patch.cu:849-1035)."""
+    v = c.values.get(key)
+    if v is None:
+        if required:
+            raise ConfigError(f"option '{key}' is required")
+        return list(default) if default is not None else None
+    if len(v) == 1:
+        return [v[0]] * n
+    if len(v) != n:
+        raise ConfigError(f"size of {key} is {len(v)} != {n}")
+    return list(v)
+
+
+def _exact(c: Config, key: str, n: int):
+    v = c.values.get(key)
+    if v is None or len(v) != n:
+        raise ConfigError(f"the size of {key} is {0 if v is None else len(v)} != {n}")
+    return list(v)
+
+
+@dataclass
+class Model:
+    spec: V1Spec
+    net: V1Network
+    lgn: LgnSpec
+    stim: Stimulus
+    init: InitState
+    seeds: Seeds
+    nt: int
+    seed: int
+    extra: dict
+
+
+def _check_supported(c: Config):
+    bad = []
+    if c.learning != 0:
+        bad.append("learning (LGN->V1 / cortical plasticity)")
+    if c.InhGap:
+        bad.append("InhGap (gap junctions)")
+    if c.nOri > 0:
+        bad.append("nOri > 0 (orientation boost of the tonic drive)")
+    if c.useNewLGN:
+        bad.append("useNewLGN = true (LGN parameters drawn from distributions)")
+    if c.virtual_LGN or c.LGN_switch or c.reverseInput:
+        bad.append("virtual_LGN / LGN_switch / reverseInput")
+    if not c.flat_retina:
+        bad.append("flat_retina = false (binocular stimulus)")
+    if c.minimal:
+        bad.append("minimal = true (sampled output)")
+    if c.fSnapshot:
+        bad.append("fSnapshot (restore)")
+    if c.manual:
+        bad.append("manual connections")
+    if bad:
+        raise ConfigError("not supported by this build: " + "; ".join(bad))
+
+
+def _max_near_distance(conMat, delayMat, nblock, nChunk):
+    """maxDistance of src/patch.cu:3808-3812: findDisConMax over each chunk of blocks, always
+    over the first remainChunkSize blocks' worth of elements of the chunk (the loop keeps the
+    chunk length of the last chunk), a[0] counted unconditionally."""
+    nChunk = min(nChunk, nblock)
+    split = nblock % nChunk
+    remain = nblock // nChunk
+    big = remain + (1 if split > 0 else 0)
+    per_block = conMat[0].size
+    n = remain * per_block
+    a_all, b_all = delayMat.reshape(-1), conMat.reshape(-1)
+    best = f32(0.0)
+    start = 0
+    for i in range(nChunk):
+        a = a_all[start * per_block:start * per_block + n]
+        b = b_all[start * per_block:start * per_block + n]
+        m = a[0]
+        sel = a[1:][b[1:] > 0]
+        if sel.size:
+            m = max(m, sel.max())
+        best = max(best, f32(m))
+        start += big if i < split else remain
+    return float(best)
+
+
+def build(c: Config) -> Model:
+    _check_supported(c)
+    P = resolve_paths(c)
+    seed = int(c.values.get("seed", 0) or 0)
+    nType, nTypeI, typeAcc = FM.read_connectome_cfg(P.connectome_cfg)
+    nblock, blockSize, pos = FM.read_v1_allpos(P.v1_allpos)
+    nV1 = nblock * blockSize
+    nh = list(c.values.get("nTypeHierarchy") or [])
+    if len(nh) != 2 or nh[0] + nh[1] != nType or nh[1] != nTypeI:
+        raise ConfigError("nTypeHierarchy inconsistent with the connectome's nType/nTypeI")
+    nTypeE = nh[0]
+    nE = int(typeAcc[nTypeE - 1])
+    if int(typeAcc[-1]) != blockSize:
+        raise ConfigError("typeAccCount does not end at blockSize")
+    synPerCon = _exact(c, "synPerCon", nType * nType)
+    synPerConFF = _per_type(c, "synPerConFF", nType)
+    sRatioV1 = _per_type(c, "sRatioV1", nType * nType)
+    sRatioLGN = _per_type(c, "sRatioLGN", nType)
+    grFF, gdFF = list(c.riseTimeFF), list(c.decayTimeFF)
+    grE, gdE = list(c.riseTimeE), list(c.decayTimeE)
+    grI, gdI = list(c.riseTimeI), list(c.decayTimeI)
+    ngFF, ngE, ngI = len(grFF), len(grE), len(grI)
+    if len(gdFF) != ngFF or len(gdE) != ngE or len(gdI) != ngI:
+        raise ConfigError("rise and decay time lists differ in size")
+    pFF = _exact(c, "pFF", nType * ngFF)
+    pE = _exact(c, "pE", nType * ngE)
+    pI = _exact(c, "pI", nType * ngI)
+    gFF0 = _exact(c, "gFF0", nType * ngFF * 4)
+    gE0 = _exact(c, "gE0", nType * ngE * 4)
+    gI0 = _exact(c, "gI0", nType * ngI * 4)
+    if c.noFarDelay and not c.noDelay:
+        raise ConfigError("noFarDelay = 1 requires noDelay = 1")
+    if c.noDelay != 1:
+        raise ConfigError("not supported by this build: noDelay = 0 (delayed near delivery)")
+    tonicDep = _per_type(c, "tonicDep", nType)
+    noisyDep = _per_type(c, "noisyDep", nType)
+    minTonicRatio = _per_type(c, "minTonicRatio", nType, required=False, default=[0.0] * nType)
+    synFailFF = _per_type(c, "synFailFF", nType)
+    synFail = [max(0.0, x) for x in _exact(c, "synFail", nType * nType)]
+    vR = _per_type(c, "vR", nType)
+    vThres = _per_type(c, "vThres", nType)
+    vT = _per_type(c, "vT", nType) if c.iModel == 1 else list(vThres)
+    Cm = _per_type(c, "C", nType)
+    gL = _per_type(c, "gL", nType)
+    tRef = _per_type(c, "tRef", nType)
+    if c.iModel == 1:
+        deltaT, tau_w = _per_type(c, "deltaT", nType), _per_type(c, "tau_w", nType)
+        a, b = _per_type(c, "a", nType), _per_type(c, "b", nType)
+    else:
+        deltaT, tau_w, a, b = [1.0] * nType, [1.0] * nType, [0.0] * nType, [0.0] * nType
+    if min(tRef) < c.dt:
+        raise ConfigError("dt > min tRef selects the multi-spike step, not built")
+    spec = V1Spec(
+        nblock=nblock, blockSize=blockSize, typeAcc=[int(x) for x in typeAcc], nTypeE=nTypeE,
+        ngFF=ngFF, ngE=ngE, ngI=ngI, dt=c.dt, riseFF=grFF, decayFF=gdFF, riseE=grE, decayE=gdE,
+        riseI=grI, decayI=gdI, vR=vR, vThres=vThres, gL=gL, C=Cm, tRef=tRef, vT=vT,
+        deltaT=deltaT, tau_w=tau_w, a=a, b=b, pFF=pFF, pE=pE, pI=pI, synFail=synFail,
+        synPerCon=synPerCon, synFailFF=synFailFF, synPerConFF=synPerConFF, noisyDep=noisyDep,
+        tau_noise=c.tau_noise, noiseOnTonic=c.noiseOnTonic, iModel=c.iModel, noDelay=c.noDelay,
+        noFarDelay=c.noFarDelay, speedOfThought=c.speedOfThought, hWrite=c.hWrite)
+    ptype = spec.type_of(np.arange(blockSize))
+
+    # near connectivity, scaled by sRatioV1[pre type * 2 + post type] (src/patch.cu:3655-3680)
+    nnb, conMat = FM.read_mat(P.conMat, nblock, blockSize)
+    nnb2, delayMat = FM.read_mat(P.delayMat, nblock, blockSize)
+    if nnb2 != nnb:
+        raise ConfigError("conMat and delayMat does not match")
+    nNear, nbId = FM.read_neighbor_block(P.neighborBlock, nblock, nnb)
+    scale = np.array(sRatioV1, f32)[ptype[:, None] * 2 + ptype[None, :]].astype(f32)
+    for bb in range(nblock):
+        for k in range(int(nNear[bb])):
+            conMat[bb, k] = conMat[bb, k] * scale
+    maxDistance = _max_near_distance(conMat, delayMat, nblock, c.nChunk)
+    trainDepth = int(math.ceil(f32(f32(maxDistance) / f32(c.speedOfThought)) / f32(c.dt))) + 1
+
+    # far connectivity (src/patch.cu:3313-3352)
+    nVec, vecID, conVec, delayVec = FM.read_v1_vec(P.v1_vec, nV1)
+    post = np.repeat(np.arange(nV1), nVec.astype(np.int64))
+    jt = np.where(vecID % blockSize < nE, 0, 1)
+    it = np.where(post % blockSize < nE, 0, 1)
+    conVec = (conVec * np.array(sRatioV1, f32)[jt * 2 + it]).astype(f32)
+
+    # LGN -> V1 (src/patch.h:30-77, src/util/util.h:162-186)
+    ids = FM.read_list_of_lists(P.lgn_v1_id, u32)
+    sl, maxList = FM.read_list_of_lists(P.lgn_v1_s, np.float32, with_max=True)
+    if len(ids) != nV1 or len(sl) != nV1:
+        raise ConfigError("LGN_V1 lists do not hold nV1 lists")
+    nL = np.array([len(x) for x in ids], u32)
+    lgnId = np.zeros((maxList, nV1), u32)
+    sLGN = np.zeros((maxList, nV1), f32)
+    rtype = spec.type_of(np.arange(nV1) % int(typeAcc[-1]))
+    for i in range(nV1):
+        lgnId[:len(ids[i]), i] = ids[i]
+        sLGN[:len(sl[i]), i] = (sl[i] * f32(sRatioLGN[rtype[i]])).astype(f32)
+
+    # tonic drive (src/patch.cu:4119-4220): CmoreDep scales by the feed-forward ratio
+    ffRatio = FM.read_con_stats(P.conStats, nType, nV1)
+    acc0 = [0] + [int(x) for x in typeAcc]
+    mn = np.ones(nType, f32)
+    mx = np.zeros(nType, f32)
+    for bb in range(nblock):
+        for j in range(nType):
+            seg = ffRatio[bb * blockSize + acc0[j]:bb * blockSize + acc0[j + 1]]
+            if seg.size:
+                mx[j] = max(mx[j], seg.max())
+                mn[j] = min(mn[j], seg.min())
+    iTonic = np.zeros(nV1, f32)
+    for i in range(nV1):
+        t = int(ptype[i % blockSize])
+        td = f32(tonicDep[t])
+        if c.CmoreDep and mx[t] > mn[t]:
+            rel = f32(1) - ffRatio[i]
+            lo, hi = f32(1) - mx[t], f32(1) - mn[t]
+            mr = f32(minTonicRatio[t])
+            iTonic[i] = td * f32(mr + (f32(1) - mr) * ((rel - lo) / (hi - lo)))
+        else:
+            iTonic[i] = td
+    net = V1Network(nLGNperV1=nL, lgnId=lgnId, sLGN=sLGN, nNearNB=nNear.astype(u32),
+                    nbId=nbId, conMat=conMat, nVec=nVec, vecID=vecID, conVec=conVec,
+                    delayVec=delayVec, tonicDep=iTonic)
+
+    # LGN cells (src/patch.cu:1523-1640, 2505-2530) and the stimulus
+    stim_f = FM.read_stimulus(P.stimulus)
+    if stim_f.neye != 1:
+        raise ConfigError("flat retina needs a one-eye stimulus")
+    nI_, nC_, max_ecc, _, _, LGNtype = FM.read_lgn_vpos(P.lgn_vpos)
+    nLGN = nI_ + nC_
+    if max_ecc > stim_f.range:
+        raise ConfigError(f"max_ecc: {max_ecc} must not be larger than {stim_f.range}")
+    if np.any(LGNtype < 4):
+        raise ConfigError("not supported by this build: parvocellular LGN cells")
+    prm = FM.read_lgn_params(P.lgn, nLGN)
+    extent = f32(2) * (f32(stim_f.range) + f32(stim_f.buffer))
+    normEcc = f32(f32(max_ecc) / extent)
+    nvd = float(f32(f32(normEcc / f32(max_ecc)) / f32(DEG)))
+    sched = make_schedule(c.dt, c.frameRate, c.tau, c.mau, c.nKernelSample, c.mKernelSample)
+    lgn = LgnSpec(nParvo_I=0, nMagno_I=nI_, nParvo_C=0, nMagno_C=nC_,
+                  mSample1D=c.mSpatialSample1D, sched=sched,
+                  **{k: prm[k] for k in FM.LGN_FIELDS2 + FM.LGN_FIELDS1 + ("coneType",)},
+                  normViewDistance=nvd, L_x0=0.5, L_y0=0.5, R_x0=1.0, R_y0=1.0, nsig=c.nsig,
+                  convolRatio=c.convolRatio, frRatio=c.frRatioLGN, flat_retina=True)
+    stim = Stimulus(frames=stim_f.frames, init_LMS=stim_f.init_LMS)
+
+    # initial state and the seed sequence of src/patch.cu (logRand_init, host engines, init)
+    s_lgn = seed
+    s_init = seed + 1 + nV1
+    s_sp = s_init + 1
+    w0 = _exact(c, "w0", nType * 2) if c.iModel == 1 else [0.0] * (2 * nType)
+    v0 = _exact(c, "v0", nType * 2) if c.use_v0 else None
+    init = host_init_state(spec, s_init, iTonic, nL, v0, w0, gFF0, gE0, gI0, use_v0=c.use_v0,
+                           tonicMax=float(iTonic.max()))
+    seeds = Seeds(lgn=s_lgn, cond=s_sp, trainDepth=max(trainDepth, 1))
+    extra = dict(nType=nType, nTypeE=nTypeE, nTypeI=nTypeI, typeAcc=typeAcc, nLGN=nLGN,
+                 normViewDistance=nvd, stimulus_filename=P.stimulus, sRatioV1=sRatioV1,
+                 sRatioLGN=sRatioLGN, tonicDep=tonicDep, noisyDep=noisyDep, vR=vR,
+                 vThres=vThres, gL=gL, vT=vT, C=Cm, tRef=tRef, a=a, b=b, tau_w=tau_w,
+                 deltaT=deltaT, synFail=synFail, synFailFF=synFailFF, paths=P)
+    return Model(spec, net, lgn, stim, init, seeds, int(c.nt), seed, extra)
+
+
+def run(c: Config, chunk: int = 512, log=print) -> Model:
+    """Runs the configured number of steps and writes the outputs the options ask for."""
+    from . import _native as N
+    from .model import Simulation
+    m = build(c)
+    P = m.extra["paths"]
+    spec = m.spec
+    sim = Simulation(m.spec, m.net, m.lgn, m.stim, m.init, m.seeds)
+    try:
+        flags = (N.REC_RAW if c.rawData else 0) | (N.REC_LGN_SP if c.getLGN_sp else 0) | \
+                (N.REC_LGN_FR if c.saveLGN_fr else 0)
+        raw = lsp = lfr = None
+        nLGN = m.extra["nLGN"]
+        if c.saveLGN_fr:
+            lfr = FM.LgnFrWriter(P.lgn_fr, m.nt, nLGN)
+        if c.rawData:
+            raw = FM.RawDataWriter(P.raw, spec.dt, m.nt, spec.nV1, spec.iModel,
+                                   spec.nI * spec.nblock, spec.hWrite, spec.ngFF, spec.ngE, spec.ngI)
+        if c.getLGN_sp:
+            lsp = FM.LgnSpWriter(P.lgn_sp, spec.dt, m.nt, nLGN)
+        if flags:
+            sim.set_record(flags, chunk)
+        done = 0
+        while done < m.nt:
+            k = min(chunk, m.nt - done)
+            sim.run(k)
+            if flags:
+                r, sp, fr = sim.fetch_records(done, k, raw=raw is not None, lgn_sp=lsp is not None,
+                                              lgn_fr=lfr is not None)
+                if raw is not None:
+                    raw.write(r)
+                if lsp is not None:
+                    lsp.write(sp)
+                if lfr is not None:
+                    lfr.write(fr)
+            done += k
+        for w in (raw, lsp, lfr):
+            if w is not None:
+                w.close()
+    finally:
+        sim.close()
+    e = m.extra
+    with open(P.patchV1_cfg, "wb") as f:
+        vals = dict(c.values)
+        vals.update(vR=e["vR"], vThres=e["vThres"], gL=e["gL"], vT=e["vT"], C=e["C"],
+                    tRef=e["tRef"], a=e["a"], b=e["b"], tau_w=e["tau_w"], deltaT=e["deltaT"],
+                    sRatioLGN=e["sRatioLGN"], sRatioV1=e["sRatioV1"], tonicDep=e["tonicDep"],
+                    noisyDep=e["noisyDep"], synFail=e["synFail"], synFailFF=e["synFailFF"])
+        for k in ("spE0", "spI0", "v0", "w0", "gFF0", "gE0", "gI0", "riseTimeFF",
+                  "decayTimeFF", "riseTimeE", "decayTimeE", "riseTimeI", "decayTimeI", "pFF",
+                  "pE", "pI"):
+            vals.setdefault(k, None)
+        f.write(FM.patchv1_cfg_bytes(
+            vals, vL=spec.vL, vE=spec.vE, vI=spec.vI, nType=e["nType"], nTypeE=e["nTypeE"],
+            nTypeI=e["nTypeI"], typeAcc=e["typeAcc"], stimulus_filename=e["stimulus_filename"],
+            nLGN=e["nLGN"], nV1=spec.nV1, normViewDistance=e["normViewDistance"], L_x0=0.5,
+            L_y0=0.5, R_x0=1.0, R_y0=1.0, ngFF=spec.ngFF, ngE=spec.ngE, ngI=spec.ngI,
+            seed=m.seed))
+    log(f"simulation for {c.output_suffix} done: {m.nt} steps of {spec.nV1} V1 neurons")
+    return m
+
+
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    c = load(argv)
+    run(c)
+    return 0

@@ -1,0 +1,414 @@
+"""Binary files of the patchV1 path: little-endian, ``Size`` = uint32, ``Float`` = float32.
+
+Inputs (read by the driver, written by the synthetic generator):
+  connectome_cfg   src/patch.cu:636-645     nType, nTypeI, typeAccCount[nType]
+  V1_allpos        src/patch.cu:2754-2776   nblock, blockSize, posDim, f64 x0, xspan, y0,
+                                            yspan, f64 pos[2][nV1]
+  V1_conMat        src/patch.cu:3442-3680   nearNeighborBlock, f32 [nblock][nnb][pre][post]
+  V1_delayMat      src/patch.cu:3450-3460   same layout (distances in mm)
+  neighborBlock    src/patch.cu:3481-3497   nNearNeighborBlock[nblock], nNeighborBlock[nblock],
+                                            then per block its neighbour ids
+  conStats         src/patch.cu:4119-4133   nType, nV1, f32 ffRatio[nV1] (rest unread)
+  V1_vec           src/patch.cu:3313-3352   i32 connectLongRange, nVec[nV1] (a second nVec if
+                                            connectLongRange == 1), then per post with
+                                            nVec > 0: ids, f32 strengths, f32 distances
+  LGN_V1_idList    src/util/util.h:162-186  nList, then per list: n, u32 ids[n]
+  LGN_V1_sList     src/patch.h:30-77        nList, maxList, then per list: n, f32 s[n]
+  stimulus         src/patch.cu:1393-1471   i32 inputType, nFrame, height, width, f32 init_L,
+                                            init_M, init_S, f32 domain[2], u32 neye, then per
+                                            frame L, M, S planes [height][width]
+  LGN_vpos         src/patch.cu:1523-1700   nLGN_I, nLGN_C, f32 max_ecc, f32 x0, xspan, y0,
+                                            yspan, f32 x[nLGN], y[nLGN], u32 LGNtype[nLGN]
+  LGN              src/patch.cu:2505-2530   nLGN, u32 LGNtype[nLGN], f32 polar, ecc, rw, rh,
+                                            orient, k, ratio, tauR, tauD, nR, nD, delay
+                                            [2][nLGN], f32 spont, c50, sharpness [nLGN],
+                                            u32 coneType[2][nLGN], f32 covariant[nLGN]
+Outputs:
+  rawData          src/patch.cu:4704-4713 header, one record per step (6140-6163, 6258,
+                   6916-6925): sInfo, dep, [w], v, gFF, [hFF], gE, gI, [hE, hI], gap[mI]
+  LGN_sp           src/patch.cu:4835-4837 {dt, nt, nLGN}, then sInfo[nLGN] per step (6423)
+  LGN_fr           src/patch.cu:4682-4683 {nt, nLGN}, then fr[nLGN] per step (6346)
+  patchV1_cfg      src/patch.cu:6954-7030
+"""
+from __future__ import annotations
+
+import io
+from dataclasses import dataclass
+
+import numpy as np
+
+f32, u32, i32, f64 = np.float32, np.uint32, np.int32, np.float64
+
+
+def _w(f, arr, dtype):
+    f.write(np.ascontiguousarray(arr, dtype=dtype).tobytes())
+
+
+def _r(f, dtype, n=1):
+    n = int(n)
+    b = f.read(np.dtype(dtype).itemsize * n)
+    if len(b) != np.dtype(dtype).itemsize * n:
+        raise EOFError(f"file ends early ({len(b)} of {np.dtype(dtype).itemsize * n} bytes)")
+    return np.frombuffer(b, dtype=dtype).copy()
+
+
+def _r1(f, dtype):
+    return _r(f, dtype, 1)[0].item()
+
+
+# ------------------------------------------------------------------ inputs
+
+def write_connectome_cfg(fn, nType, nTypeI, typeAcc):
+    with open(fn, "wb") as f:
+        _w(f, [nType, nTypeI], u32)
+        _w(f, typeAcc, u32)
+
+
+def read_connectome_cfg(fn):
+    with open(fn, "rb") as f:
+        nType = _r1(f, u32)
+        nTypeI = _r1(f, u32)
+        acc = _r(f, u32, nType)
+    return nType, nTypeI, acc
+
+
+def write_v1_allpos(fn, nblock, blockSize, pos):
+    """pos: [nV1][2] in mm."""
+    pos = np.asarray(pos, dtype=f64)
+    with open(fn, "wb") as f:
+        _w(f, [nblock, blockSize, 2], u32)
+        x0, y0 = pos[:, 0].min(), pos[:, 1].min()
+        _w(f, [x0, pos[:, 0].max() - x0, y0, pos[:, 1].max() - y0], f64)
+        _w(f, pos[:, 0], f64)
+        _w(f, pos[:, 1], f64)
+
+
+def read_v1_allpos(fn):
+    with open(fn, "rb") as f:
+        nblock, blockSize, posDim = (_r1(f, u32) for _ in range(3))
+        if posDim > 2:
+            raise ValueError("3-D positions are not implemented")
+        _r(f, f64, 4)
+        n = nblock * blockSize
+        x = _r(f, f64, n)
+        y = _r(f, f64, n)
+    return nblock, blockSize, np.stack([x, y], 1)
+
+
+def write_mat(fn, nnb, mat):
+    """conMat / delayMat: mat [nblock][nnb][bs][bs]."""
+    with open(fn, "wb") as f:
+        _w(f, [nnb], u32)
+        _w(f, mat, f32)
+
+
+def read_mat(fn, nblock, blockSize):
+    with open(fn, "rb") as f:
+        nnb = _r1(f, u32)
+        m = _r(f, f32, nblock * nnb * blockSize * blockSize)
+    return nnb, m.reshape(nblock, nnb, blockSize, blockSize)
+
+
+def write_neighbor_block(fn, nNear, neighbors):
+    """nNear[nblock]; neighbors: per block the list of all neighbour ids (near ones first)."""
+    with open(fn, "wb") as f:
+        _w(f, nNear, u32)
+        _w(f, [len(x) for x in neighbors], u32)
+        for x in neighbors:
+            _w(f, x, u32)
+
+
+def read_neighbor_block(fn, nblock, nnb):
+    with open(fn, "rb") as f:
+        nNear = _r(f, u32, nblock)
+        nAll = _r(f, u32, nblock)
+        if nNear.max(initial=0) > nnb:
+            raise ValueError("conMat nearNeighborBlock not compatible with nNearNeighborBlock")
+        ids = np.zeros((nblock, nnb), u32)
+        for b in range(nblock):
+            if nAll[b] > 0:
+                t = _r(f, u32, nAll[b])
+                if t.max() >= nblock:
+                    raise ValueError("conMat neighbor blockID exceeds nblock")
+                ids[b, :nNear[b]] = t[:nNear[b]]
+    return nNear, ids
+
+
+def write_con_stats(fn, nType, ffRatio):
+    with open(fn, "wb") as f:
+        _w(f, [nType, len(ffRatio)], u32)
+        _w(f, ffRatio, f32)
+
+
+def read_con_stats(fn, nType, nV1):
+    with open(fn, "rb") as f:
+        t = _r1(f, u32)
+        n = _r1(f, u32)
+        if t != nType or n != nV1:
+            raise ValueError(f"conStats holds nType={t}, nV1={n}; expected {nType}, {nV1}")
+        return _r(f, f32, nV1)
+
+
+def write_v1_vec(fn, nVec, vecID, conVec, delayVec):
+    nVec = np.asarray(nVec, u32)
+    with open(fn, "wb") as f:
+        _w(f, [0], i32)
+        _w(f, nVec, u32)
+        off = 0
+        for n in nVec:
+            if n > 0:
+                _w(f, vecID[off:off + n], u32)
+                _w(f, conVec[off:off + n], f32)
+                _w(f, delayVec[off:off + n], f32)
+            off += int(n)
+
+
+def read_v1_vec(fn, nV1):
+    """nVec, vecID, conVec (unscaled), delayVec, flattened in post order."""
+    with open(fn, "rb") as f:
+        longRange = _r1(f, i32)
+        nVec = _r(f, u32, nV1)
+        if longRange == 1:
+            _r(f, u32, nV1)
+        ids, s, d = [], [], []
+        for n in nVec:
+            if n > 0:
+                ids.append(_r(f, u32, n))
+                s.append(_r(f, f32, n))
+                d.append(_r(f, f32, n))
+    cat = lambda xs, t: np.concatenate(xs).astype(t) if xs else np.zeros(0, t)
+    return nVec, cat(ids, u32), cat(s, f32), cat(d, f32)
+
+
+def write_list_of_lists(fn, lists, dtype, with_max=False):
+    with open(fn, "wb") as f:
+        _w(f, [len(lists)], u32)
+        if with_max:
+            _w(f, [max((len(x) for x in lists), default=0)], u32)
+        for x in lists:
+            _w(f, [len(x)], u32)
+            _w(f, x, dtype)
+
+
+def read_list_of_lists(fn, dtype, with_max=False):
+    with open(fn, "rb") as f:
+        n = _r1(f, u32)
+        mx = _r1(f, u32) if with_max else None
+        out = [_r(f, dtype, _r1(f, u32)) for _ in range(n)]
+    return (out, mx) if with_max else out
+
+
+def write_stimulus(fn, frames, init_LMS, domain=(0.0, 1.0), neye=1):
+    """frames: [nFrame][3][h][w] f32 (L, M, S planes)."""
+    frames = np.asarray(frames, f32)
+    nFrame, _, h, w = frames.shape
+    with open(fn, "wb") as f:
+        _w(f, [-1], i32)
+        _w(f, [nFrame, h, w], u32)
+        _w(f, init_LMS, f32)
+        _w(f, domain, f32)
+        _w(f, [neye], u32)
+        _w(f, frames, f32)
+
+
+@dataclass
+class StimulusFile:
+    inputType: int
+    frames: np.ndarray
+    init_LMS: tuple
+    buffer: float
+    range: float
+    neye: int
+
+
+def read_stimulus(fn):
+    with open(fn, "rb") as f:
+        inputType = _r1(f, i32)
+        nFrame, h, w = (_r1(f, u32) for _ in range(3))
+        if inputType != -1:
+            raise ValueError(f"inputType {inputType} does not match with normal external stimulus")
+        init = tuple(float(x) for x in _r(f, f32, 3))
+        dom = _r(f, f32, 2)
+        neye = _r1(f, u32)
+        frames = _r(f, f32, nFrame * 3 * h * w).reshape(nFrame, 3, h, w)
+    return StimulusFile(inputType, frames, init, float(dom[0]), float(dom[1]), neye)
+
+
+def write_lgn_vpos(fn, nLGN_I, nLGN_C, max_ecc, x, y, LGNtype):
+    with open(fn, "wb") as f:
+        _w(f, [nLGN_I, nLGN_C], u32)
+        _w(f, [max_ecc], f32)
+        _w(f, [x.min(), x.max() - x.min(), y.min(), y.max() - y.min()], f32)
+        _w(f, x, f32)
+        _w(f, y, f32)
+        _w(f, LGNtype, u32)
+
+
+def read_lgn_vpos(fn):
+    with open(fn, "rb") as f:
+        nI = _r1(f, u32)
+        nC = _r1(f, u32)
+        max_ecc = float(_r1(f, f32))
+        _r(f, f32, 4)
+        n = nI + nC
+        x = _r(f, f32, n)
+        y = _r(f, f32, n)
+        t = _r(f, u32, n)
+    return nI, nC, max_ecc, x, y, t
+
+
+LGN_FIELDS2 = ("polar", "ecc", "rw", "rh", "orient", "k", "ratio", "tauR", "tauD", "nR", "nD",
+               "delay")
+LGN_FIELDS1 = ("spont", "c50", "sharpness")
+
+
+def write_lgn_params(fn, LGNtype, p: dict):
+    n = len(LGNtype)
+    with open(fn, "wb") as f:
+        _w(f, [n], u32)
+        _w(f, LGNtype, u32)
+        for k in LGN_FIELDS2:
+            _w(f, p[k], f32)
+        for k in LGN_FIELDS1:
+            _w(f, p[k], f32)
+        _w(f, p["coneType"], u32)
+        _w(f, p.get("covariant", np.zeros(n, f32)), f32)
+
+
+def read_lgn_params(fn, nLGN):
+    with open(fn, "rb") as f:
+        _r1(f, u32)
+        out = {"LGNtype": _r(f, u32, nLGN)}
+        for k in LGN_FIELDS2:
+            out[k] = _r(f, f32, 2 * nLGN)
+        for k in LGN_FIELDS1:
+            out[k] = _r(f, f32, nLGN)
+        out["coneType"] = _r(f, u32, 2 * nLGN)
+        out["covariant"] = _r(f, f32, nLGN)
+    return out
+
+
+# ------------------------------------------------------------------ outputs
+
+class RawDataWriter:
+    """rawData: header, then one record per step in the order the step loop writes them."""
+
+    def __init__(self, fn, dt, nt, nV1, iModel, mI, hWrite, ngFF, ngE, ngI):
+        self.f = open(fn, "wb")
+        _w(self.f, [dt], f32)
+        _w(self.f, [nt, nV1], u32)
+        _w(self.f, [iModel], i32)
+        _w(self.f, [mI, int(bool(hWrite)), ngFF, ngE, ngI], u32)
+        self.rec = nV1 * (3 + (iModel == 1) + (ngFF + ngE + ngI) * (1 + int(bool(hWrite)))) + mI
+
+    def write(self, records: np.ndarray):
+        records = np.ascontiguousarray(records, f32)
+        assert records.size % self.rec == 0
+        self.f.write(records.tobytes())
+
+    def close(self):
+        self.f.close()
+
+
+def read_raw_header(f):
+    dt = float(_r1(f, f32))
+    nt, nV1 = (_r1(f, u32) for _ in range(2))
+    iModel = _r1(f, i32)
+    mI, hWrite, ngFF, ngE, ngI = (_r1(f, u32) for _ in range(5))
+    return dict(dt=dt, nt=nt, nV1=nV1, iModel=iModel, mI=mI, hWrite=hWrite, ngFF=ngFF, ngE=ngE,
+                ngI=ngI)
+
+
+def read_raw(fn):
+    """Header dict and the records [nt][floats per record], as src/readPatchOutput.py:291-354
+    walks them."""
+    with open(fn, "rb") as f:
+        h = read_raw_header(f)
+        rec = h["nV1"] * (3 + (h["iModel"] == 1) + (h["ngFF"] + h["ngE"] + h["ngI"]) *
+                          (1 + h["hWrite"])) + h["mI"]
+        data = np.frombuffer(f.read(), dtype=f32)
+    assert data.size == h["nt"] * rec, (data.size, h["nt"], rec)
+    return h, data.reshape(h["nt"], rec)
+
+
+class LgnSpWriter:
+    def __init__(self, fn, dt, nt, nLGN):
+        self.f = open(fn, "wb")
+        _w(self.f, [dt], f32)
+        _w(self.f, [nt, nLGN], u32)
+
+    def write(self, rows):
+        self.f.write(np.ascontiguousarray(rows, f32).tobytes())
+
+    def close(self):
+        self.f.close()
+
+
+class LgnFrWriter(LgnSpWriter):
+    def __init__(self, fn, nt, nLGN):
+        self.f = open(fn, "wb")
+        _w(self.f, [nt, nLGN], u32)
+
+
+def read_lgn_sp(fn):
+    with open(fn, "rb") as f:
+        dt = float(_r1(f, f32))
+        nt, n = (_r1(f, u32) for _ in range(2))
+        d = _r(f, f32, nt * n).reshape(nt, n)
+    return dt, d
+
+
+def read_lgn_fr(fn):
+    with open(fn, "rb") as f:
+        nt, n = (_r1(f, u32) for _ in range(2))
+        d = _r(f, f32, nt * n).reshape(nt, n)
+    return d
+
+
+def _pad(v, n):
+    v = list(v or [])
+    return (v + [0.0] * n)[:n]
+
+
+def patchv1_cfg_bytes(c, *, vL, vE, vI, nType, nTypeE, nTypeI, typeAcc, stimulus_filename, nLGN,
+                      nV1, normViewDistance, L_x0, L_y0, R_x0, R_y0, ngFF, ngE, ngI,
+                      seed) -> bytes:
+    """patchV1_cfg as src/patch.cu:6954-7030 writes it; ``c`` is the parsed option set with
+    the per-type vectors already expanded to nType as the reference does."""
+    b = io.BytesIO()
+    _w(b, [4], u32)
+    _w(b, [vL, vE, vI], f32)
+    _w(b, [nType, nTypeE, nTypeI], u32)
+    for k in ("vR", "vThres", "gL", "vT"):
+        _w(b, _pad(c[k], nType), f32)
+    _w(b, _pad(c["nTypeHierarchy"], 2), u32)
+    _w(b, typeAcc, u32)
+    _w(b, _pad(c["sRatioLGN"], nType), f32)
+    _w(b, _pad(c["sRatioV1"], nType * nType), f32)
+    _w(b, [c["frRatioLGN"], c["convolRatio"]], f32)
+    _w(b, [c["frameRate"]], u32)
+    name = stimulus_filename.encode()
+    _w(b, [len(name)], u32)
+    b.write(name)
+    _w(b, [nLGN, nV1, c["nt"]], u32)
+    _w(b, [c["dt"], normViewDistance, L_x0, L_y0, R_x0, R_y0], f32)
+    _w(b, _pad(c["tonicDep"], nType), f32)
+    _w(b, _pad(c["noisyDep"], nType), f32)
+    _w(b, [int(c["virtual_LGN"])], i32)
+    _w(b, [seed], np.uint64)
+    _w(b, [c["iModel"], c["learning"]], i32)
+    _w(b, [ngFF, ngE, ngI], u32)
+    for k, n in (("riseTimeFF", ngFF), ("decayTimeFF", ngFF), ("riseTimeE", ngE),
+                 ("decayTimeE", ngE), ("riseTimeI", ngI), ("decayTimeI", ngI),
+                 ("pFF", ngFF * nType), ("pE", ngE * nType), ("pI", ngI * nType),
+                 ("C", nType), ("tRef", nType), ("a", nType), ("b", nType), ("tau_w", nType),
+                 ("deltaT", nType)):
+        _w(b, _pad(c[k], n), f32)
+    nh = _pad(c["nTypeHierarchy"], 2)
+    _w(b, _pad(c["spE0"], int(nh[0]) * 2), f32)
+    _w(b, _pad(c["spI0"], int(nh[1]) * 2), f32)
+    for k in ("v0", "w0", "gFF0", "gE0", "gI0"):
+        _w(b, _pad(c[k], nType * 2), f32)
+    _w(b, _pad(c["synFail"], nType * nType), f32)
+    _w(b, _pad(c["synFailFF"], nType), f32)
+    return b.getvalue()

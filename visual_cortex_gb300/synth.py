@@ -294,3 +294,76 @@ def config2(seed: int = 0, orient: float = 0.0, **kw) -> Workload:
                          seed=seed, nblock=32, n_lgn=16384, m=20, width=128, height=128,
                          nt=16000, orient=orient, far_partners=400, adex_inh=True,
                          patch_deg=4.0, nFrame=240, **kw)
+
+
+def write_reference_files(wl: Workload, folder: str, seed: int = 0, nt: int | None = None,
+                          extra: dict | None = None) -> str:
+    """Writes a workload as the reference's input files plus a patchV1 cfg; returns the cfg
+    path.  The within-block distances of the near tiles go to V1_delayMat, a per-neuron
+    feed-forward ratio to conStats (the tonic drive is then derived from it by the reader,
+    CmoreDep = true), and the LGN cells to LGN_vpos + LGN (useNewLGN = false)."""
+    import os
+    from . import formats as FM
+    from .cfg import write_cfg
+    os.makedirs(folder, exist_ok=True)
+    spec, net, lgn = wl.spec, wl.net, wl.lgn
+    d = folder.rstrip("/") + "/"
+    bs, nb = spec.blockSize, spec.nblock
+    FM.write_connectome_cfg(d + "connectome_cfg.bin", spec.nType, spec.nType - spec.nTypeE,
+                            spec.typeAcc)
+    FM.write_v1_allpos(d + "V1_allpos.bin", nb, bs, wl.pos)
+    FM.write_mat(d + "V1_conMat.bin", net.nnb, net.conMat)
+    delay = np.zeros_like(net.conMat)
+    for b in range(nb):
+        for k in range(int(net.nNearNB[b])):
+            P = wl.pos[b * bs:(b + 1) * bs]
+            Q = wl.pos[int(net.nbId[b, k]) * bs:(int(net.nbId[b, k]) + 1) * bs]
+            delay[b, k] = np.sqrt(((P[:, None, :] - Q[None, :, :]) ** 2).sum(-1)).astype(f32)
+    FM.write_mat(d + "V1_delayMat.bin", net.nnb, delay)
+    FM.write_neighbor_block(d + "neighborBlock.bin", net.nNearNB,
+                            [net.nbId[b, :int(net.nNearNB[b])] for b in range(nb)])
+    rng = np.random.default_rng(seed + 12345)
+    FM.write_con_stats(d + "conStats.bin", spec.nType, rng.uniform(0.2, 0.9, spec.nV1).astype(f32))
+    FM.write_v1_vec(d + "V1_vec.bin", net.nVec, net.vecID, net.conVec, net.delayVec)
+    ids = [net.lgnId[:int(net.nLGNperV1[i]), i] for i in range(spec.nV1)]
+    ss = [net.sLGN[:int(net.nLGNperV1[i]), i] for i in range(spec.nV1)]
+    FM.write_list_of_lists(d + "LGN_V1_idList.bin", ids, u32)
+    FM.write_list_of_lists(d + "LGN_V1_sList.bin", ss, f32, with_max=True)
+    buffer_deg = 0.2
+    max_ecc = float(np.max(np.hypot(lgn.xy[:, 0], lgn.xy[:, 1])))
+    patch = float(np.max(np.abs(lgn.xy))) * 2
+    stim_range = max(max_ecc, patch / 2) * 1.05
+    FM.write_stimulus(d + "stimulus.bin", wl.stim.frames, wl.stim.init_LMS,
+                      domain=(buffer_deg, stim_range), neye=1)
+    FM.write_lgn_vpos(d + "LGN_vpos.bin", lgn.nMagno_I, lgn.nMagno_C, max_ecc,
+                      lgn.xy[:, 0].astype(f32), lgn.xy[:, 1].astype(f32), lgn.types)
+    FM.write_lgn_params(d + "LGN", lgn.types, {k: getattr(lgn, k) for k in
+                                               FM.LGN_FIELDS2 + FM.LGN_FIELDS1 + ("coneType",)})
+    s = lgn.sched
+    keys = dict(
+        inputFolder=d, resourceFolder=d, outputFolder=d, seed=seed, dt=spec.dt,
+        nt=wl.nt if nt is None else nt, frameRate=s.frameRate, tau=s.nRetrace * spec.dt,
+        mau=s.mRetrace * spec.dt, nKernelSample=s.nKernelSample, mKernelSample=s.mKernelSample,
+        mSpatialSample1D=lgn.mSample1D, nsig=lgn.nsig, convolRatio=lgn.convolRatio,
+        frRatioLGN=lgn.frRatio, flat_retina=True, useNewLGN=False, learning=0,
+        nTypeHierarchy=[spec.nTypeE, spec.nType - spec.nTypeE], sRatioLGN=[1.0],
+        sRatioV1=[1.0], synPerCon=spec.synPerCon, synPerConFF=spec.synPerConFF,
+        riseTimeFF=spec.riseFF, decayTimeFF=spec.decayFF, riseTimeE=spec.riseE,
+        decayTimeE=spec.decayE, riseTimeI=spec.riseI, decayTimeI=spec.decayI,
+        pFF=spec.pFF, pE=spec.pE, pI=spec.pI,
+        gFF0=[0.01, 0.2, 0.0, 0.2] * (spec.nType * spec.ngFF),
+        gE0=[0.005, 0.2, 0.0, 0.2] * (spec.nType * spec.ngE),
+        gI0=[0.01, 0.2, 0.0, 0.2] * (spec.nType * spec.ngI),
+        w0=[0.0, 0.0] * spec.nType, v0=[-60.0, 1.0] * spec.nType,
+        iModel=spec.iModel, noDelay=spec.noDelay, noFarDelay=spec.noFarDelay,
+        speedOfThought=spec.speedOfThought, tonicDep=[0.6, 0.7], minTonicRatio=[0.5, 0.5],
+        CmoreDep=True, noisyDep=spec.noisyDep, tau_noise=spec.tau_noise,
+        noiseOnTonic=spec.noiseOnTonic, synFail=spec.synFail, synFailFF=spec.synFailFF,
+        vR=spec.vR, vThres=spec.vThres, gL=spec.gL, C=spec.C, tRef=spec.tRef, vT=spec.vT,
+        deltaT=spec.deltaT, tau_w=spec.tau_w, a=spec.a, b=spec.b, hWrite=spec.hWrite,
+        spE0=[0.0, 0.0], spI0=[0.0, 0.0], getLGN_sp=True, saveLGN_fr=True, rawData=True)
+    keys.update(extra or {})
+    fn = d + "patchV1.cfg"
+    with open(fn, "w") as f:
+        f.write("# synthetic patch written by visual_cortex_gb300.synth\n" + write_cfg(keys))
+    return fn

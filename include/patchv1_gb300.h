@@ -271,6 +271,39 @@ int pv1_lgn_spikes_noalloc(pv1_plan *plan, uint32_t nsteps, float *d_sinfo, floa
  * Returns 1 if the plan steps with the persistent kernel, 0 if with one launch per step. */
 int pv1_persistent_mode(pv1_plan *plan, int allow);
 
+/* ---- Batched trials ------------------------------------------------------------------
+ * Replaces the reference's one-process-per-trial sweep (src/ori.sh runs `patch -c cfg` once
+ * per orientation/seed): many fully set-up plans (each a trial with its own stimulus, seeds,
+ * state and connectivity) are stepped together, every step of every trial in the same
+ * launches: one batched LGN launch and K batched V1 launches per chunk of K steps, captured
+ * once as a CUDA graph.  Trials may differ in duration (trialSteps) and size (nblock).  Each
+ * trial computes exactly what pv1_run would compute for it alone.  The plans must live on
+ * the current device and stay alive until pv1_batch_destroy. */
+typedef struct pv1_batch pv1_batch;
+
+int pv1_batch_create(pv1_plan *const *plans, uint32_t nTrials, const uint64_t *trialSteps,
+                     pv1_batch **out);
+void pv1_batch_destroy(pv1_batch *batch);
+const char *pv1_batch_last_error(const pv1_batch *batch);
+/* Runs every trial until its end (trialSteps after create), or at most maxSteps more steps
+ * (0 = no limit).  Returns the number of steps of the longest trial still to run (0: all
+ * done), or a negative error code.  *ms (may be null) receives the device time of the call
+ * (CUDA events on the batch stream). */
+int64_t pv1_batch_run(pv1_batch *batch, uint64_t maxSteps, float *ms);
+/* Autotuner: tries each chunk length in {16, 32, 64} with each V1 kernel variant (1, 2 or 3
+ * resident CTAs per SM) for one chunk of the real run and keeps the fastest; the tuning
+ * chunks are ordinary steps of the simulation.  enable = 0 fixes K = 64, 1 CTA per SM. */
+int pv1_batch_autotune(pv1_batch *batch, int enable);
+/* Chosen chunk length, V1 variant and the measured ms per chunk of every candidate tried
+ * (times[i] for candidate i = kIndex*3 + (minB-1); 9 entries, -1 where not tried). */
+int pv1_batch_tuning(const pv1_batch *batch, int *K, int *minB, float *times);
+/* FP64 statistics of one trial: simulated time (ms), per-neuron firing rates (Hz, may be
+ * null) and their mean, from spike counters kept by the V1 kernel since pv1_batch_create. */
+int pv1_batch_stats(pv1_batch *batch, uint32_t trial, double *simTimeMs, double *rates,
+                    double *meanRate);
+/* Kernel launches issued by the last pv1_batch_run. */
+int64_t pv1_batch_launch_count(const pv1_batch *batch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,89 @@
+"""Batched trials: every trial of a batch ends bit-identical to the same trial run alone."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+STATE = ("v", "w", "tBack", "gE", "hE", "gI", "hI", "gFF", "hFF", "lgn_lnl", "lgn_ltr")
+
+
+def _trials(**kw):
+    from visual_cortex_gb300 import synth
+    args = dict(n_trials=4, nblock=2, n_lgn=512, width=64, height=64, nFrame=60, far_partners=50,
+                dur_ms=(8.0, 25.0))
+    args.update(kw)
+    return synth.batch_trials(**args)
+
+
+def _sim(wl):
+    from visual_cortex_gb300.model import Simulation
+    return Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+
+
+@pytest.mark.parametrize("autotune", [False, True])
+def test_batch_equals_trials_alone(native, autotune):
+    from visual_cortex_gb300.batch import Batch
+    trials = _trials()
+    alone, batched = [], []
+    try:
+        for tr in trials:
+            s = _sim(tr.wl)
+            s.persistent(0)
+            s.run(tr.steps)
+            alone.append(s)
+        batched = [_sim(tr.wl) for tr in trials]
+        b = Batch(batched, [tr.steps for tr in trials], autotune=autotune)
+        try:
+            left, ms = b.run()
+            assert left == 0 and ms > 0
+            for q, tr in enumerate(trials):
+                assert batched[q].step == tr.steps
+                for k in STATE:
+                    np.testing.assert_array_equal(batched[q].state(k), alone[q].state(k),
+                                                  err_msg=f"trial {q} {k}")
+                t, mean, rates = b.stats(q, rates=True)
+                assert t == pytest.approx(tr.steps * tr.wl.spec.dt, rel=1e-12)
+                assert mean == pytest.approx(rates.mean(), rel=1e-12)
+        finally:
+            b.close()
+    finally:
+        for s in alone + batched:
+            s.close()
+
+
+def test_batch_in_pieces_with_noise(native):
+    """maxSteps slices, a trial continuing after the batch, noise and failure draws."""
+    from visual_cortex_gb300.batch import Batch
+    from visual_cortex_gb300 import synth
+    base = synth.make_workload("nz", seed=9, nblock=2, n_lgn=512, width=64, height=64, nt=0,
+                               far_partners=50, adex_inh=True, nFrame=60, noisyDep=(0.2, 0.2),
+                               synFailFF=(0.1, 0.1), synFail=(0.1, 0.1, 0.1, 0.1))
+    # far synapses cannot fail in this build: drop them for the failure case
+    import dataclasses
+    net = dataclasses.replace(base.net, nVec=np.zeros_like(base.net.nVec),
+                              vecID=np.zeros(0, np.uint32), conVec=np.zeros(0, np.float32),
+                              delayVec=np.zeros(0, np.float32))
+    base = dataclasses.replace(base, net=net)
+    trials = _trials(n_trials=3, base=base, dur_ms=(10.0, 20.0))
+    alone, batched = [], []
+    try:
+        for tr in trials:
+            s = _sim(tr.wl)
+            s.persistent(0)
+            s.run(tr.steps + 30)
+            alone.append(s)
+        batched = [_sim(tr.wl) for tr in trials]
+        b = Batch(batched, [tr.steps for tr in trials], autotune=False)
+        try:
+            while b.run(max_steps=37)[0] > 0:
+                pass
+        finally:
+            b.close()
+        for q, tr in enumerate(trials):
+            batched[q].run(30)      # the plan continues on its own after the batch
+            for k in STATE:
+                np.testing.assert_array_equal(batched[q].state(k), alone[q].state(k),
+                                              err_msg=f"trial {q} {k}")
+    finally:
+        for s in alone + batched:
+            s.close()

@@ -67,7 +67,7 @@ def test_run_writes_reference_outputs(written, native):
     fr = FM.read_lgn_fr(P.lgn_fr)
     sim = Simulation(m.spec, m.net, m.lgn, m.stim, m.init, m.seeds)
     try:
-        sim.set_record(N.REC_RAW | N.REC_LGN_SP | N.REC_LGN_FR, 96)
+        sim.set_record(N.REC_RAW | N.REC_LGN_SP | N.REC_LGN_FR, 97)
         sim.run(96)
         r2, sp2, fr2 = sim.fetch_records(0, 96, raw=True, lgn_sp=True, lgn_fr=True)
     finally:

@@ -117,6 +117,15 @@ def _load() -> C.CDLL:
         "pv1_time_kernels": ([P, C.c_uint32, _FP, _FP, C.POINTER(C.c_int)], C.c_int),
         "pv1_persistent_mode": ([P, C.c_int], C.c_int),
         "pv1_lgn_spikes_noalloc": ([P, C.c_uint32, _FP, _FP], C.c_int),
+        "pv1_batch_create": ([C.POINTER(P), C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(P)], C.c_int),
+        "pv1_batch_destroy": ([P], None),
+        "pv1_batch_last_error": ([P], C.c_char_p),
+        "pv1_batch_run": ([P, C.c_uint64, _FP], C.c_int64),
+        "pv1_batch_autotune": ([P, C.c_int], C.c_int),
+        "pv1_batch_tuning": ([P, C.POINTER(C.c_int), C.POINTER(C.c_int), _FP], C.c_int),
+        "pv1_batch_stats": ([P, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                             C.POINTER(C.c_double)], C.c_int),
+        "pv1_batch_launch_count": ([P], C.c_int64),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

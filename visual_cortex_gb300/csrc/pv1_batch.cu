@@ -1,0 +1,371 @@
+// Batched trials behind the C ABI (pv1_batch_*): many independent patches stepped by the
+// same launches, replacing the reference's one-process-per-trial sweeps (src/ori.sh).
+//
+// Per chunk of K steps: one batched LGN launch (grid = cell CTAs x trials), K batched V1
+// launches (grid = the active (trial, CTA) tiles of all trials) and one advance launch, captured
+// once per (K, V1 variant) as a CUDA graph.  Every trial keeps its own device step counter;
+// chunks run as a graph only while every active trial has K or more steps left, otherwise as
+// direct launches of the smallest remainder, so no kernel steps a trial past its end and each
+// trial computes exactly what pv1_run computes for it alone.  The tile list is rebuilt on the
+// host when a trial ends (the V1 grid is sized for all tiles; CTAs past the list return).
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "pv1_internal.cuh"
+
+using namespace pv1;
+
+struct pv1_batch {
+    std::string err;
+    int n = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<pv1_plan *> plans;
+    std::vector<PlanBatchView> views;
+    std::vector<BatchTrial> hT;
+    std::vector<BatchLgn> hL;
+    BatchTrial *dT = nullptr;
+    BatchLgn *dL = nullptr;
+    int2 *dTiles = nullptr;
+    int *dNTiles = nullptr;
+    int totalTiles = 0;
+    int maxCellCtas = 0;
+    bool allClass = true;
+    bool rng = false;
+    unsigned *dCounts = nullptr;
+    long long *dCountOff = nullptr;
+    std::vector<long long> countOff;
+    double *dSimTime = nullptr;
+    double *dMean = nullptr;
+    std::vector<long long> step, end;
+    std::vector<char> activeSet;
+    std::vector<int2> hTiles;
+    int hNTiles = 0;
+    int K = 64, minB = 1;
+    bool tune = false;
+    int nextCandidate = 0;
+    float times[9];
+    std::map<int, cudaGraphExec_t> graphs;   // key K*4 + minB
+    long long launches = 0;
+    std::vector<void *> allocs;
+};
+
+namespace {
+
+const int kCandK[3] = {16, 32, 64};
+
+int bfail(pv1_batch *b, int code, const std::string &m) {
+    if (b) b->err = m;
+    return code;
+}
+
+#define PV1_BCUDA(b, call)                                                                      \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return bfail((b), PV1_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));  \
+    } while (0)
+
+template <class T>
+int balloc(pv1_batch *b, T **p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) return bfail(b, PV1_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    b->allocs.push_back(*p);
+    e = cudaMemsetAsync(*p, 0, n * sizeof(T), b->stream);
+    if (e != cudaSuccess) return bfail(b, PV1_E_CUDA, cudaGetErrorString(e));
+    return PV1_OK;
+}
+
+// Rebuilds the (trial, CTA) tile list of the trials that still have steps to run.
+int refresh_tiles(pv1_batch *b) {
+    std::vector<char> act(b->n);
+    for (int q = 0; q < b->n; q++) act[q] = b->step[q] < b->end[q];
+    if (act == b->activeSet) return PV1_OK;
+    b->activeSet = act;
+    b->hTiles.clear();
+    for (int q = 0; q < b->n; q++)
+        if (act[q])
+            for (int c = 0; c < b->hT[q].nCta; c++) b->hTiles.push_back(make_int2(q, c));
+    b->hNTiles = (int)b->hTiles.size();
+    if (b->hNTiles)
+        PV1_BCUDA(b, cudaMemcpyAsync(b->dTiles, b->hTiles.data(), b->hTiles.size() * sizeof(int2),
+                                     cudaMemcpyHostToDevice, b->stream));
+    PV1_BCUDA(b, cudaMemcpyAsync(b->dNTiles, &b->hNTiles, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    // the host vectors are reused by the next refresh: wait for the copies
+    PV1_BCUDA(b, cudaStreamSynchronize(b->stream));
+    return PV1_OK;
+}
+
+// One chunk of k steps for every active trial, on the batch stream (direct or under capture).
+int issue(pv1_batch *b, int k, int minB, long long *launches) {
+    long long n = 0;
+    cudaError_t e;
+    if (b->allClass) {
+        e = launch_lgn_class_batch(b->dL, b->n, b->maxCellCtas, k, b->stream);
+        if (e != cudaSuccess) return bfail(b, PV1_E_CUDA, std::string("lgn batch: ") + cudaGetErrorString(e));
+        n += 1;
+    } else {
+        for (int q = 0; q < b->n; q++) {
+            if (!b->activeSet[q]) continue;
+            e = launch_lgn_step(b->views[q].lp, b->views[q].d_stepBase, k, b->stream);
+            if (e != cudaSuccess) return bfail(b, PV1_E_CUDA, std::string("lgn step: ") + cudaGetErrorString(e));
+            n += (b->views[q].lp.classCtw && k <= kClassMaxK) ? 1 : 2;
+        }
+    }
+    for (int s = 0; s < k; s++) {
+        e = launch_v1_batch_step(b->dT, b->dTiles, b->dNTiles, b->totalTiles, s, b->rng, minB, b->stream);
+        if (e != cudaSuccess) return bfail(b, PV1_E_CUDA, std::string("v1 batch: ") + cudaGetErrorString(e));
+    }
+    n += k;
+    e = launch_batch_advance(b->dT, b->n, k, b->dSimTime, b->stream);
+    if (e != cudaSuccess) return bfail(b, PV1_E_CUDA, cudaGetErrorString(e));
+    n += 1;
+    if (launches) *launches += n;
+    return PV1_OK;
+}
+
+int graph_for(pv1_batch *b, int K, int minB, cudaGraphExec_t *out) {
+    const int key = K * 4 + minB;
+    auto it = b->graphs.find(key);
+    if (it != b->graphs.end()) {
+        *out = it->second;
+        return PV1_OK;
+    }
+    cudaGraph_t g;
+    PV1_BCUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    int r = issue(b, K, minB, nullptr);
+    cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+    if (r) return r;
+    if (e2 != cudaSuccess) return bfail(b, PV1_E_CUDA, std::string("capture: ") + cudaGetErrorString(e2));
+    cudaGraphExec_t ex;
+    cudaError_t e3 = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) return bfail(b, PV1_E_CUDA, std::string("instantiate: ") + cudaGetErrorString(e3));
+    b->graphs[key] = ex;
+    *out = ex;
+    return PV1_OK;
+}
+
+int check_errors(pv1_batch *b) {
+    for (int q = 0; q < b->n; q++) {
+        int h = 0;
+        PV1_BCUDA(b, cudaMemcpy(&h, b->hT[q].v.err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (h) return bfail(b, PV1_E_DEVICE, "device error word 0x" + std::to_string(h) + " in trial " +
+                                                 std::to_string(q));
+    }
+    return PV1_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pv1_batch_create(pv1_plan *const *plans, uint32_t nTrials, const uint64_t *trialSteps, pv1_batch **out) {
+    if (!plans || !trialSteps || !out || nTrials == 0) return PV1_E_ARG;
+    *out = nullptr;
+    pv1_batch *b = new pv1_batch();
+    *out = b;
+    b->n = (int)nTrials;
+    for (float &t : b->times) t = -1.f;
+    if (cudaGetDevice(&b->device) != cudaSuccess) return bfail(b, PV1_E_CUDA, "cudaGetDevice");
+    PV1_BCUDA(b, cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    PV1_BCUDA(b, cudaEventCreate(&b->ev0));
+    PV1_BCUDA(b, cudaEventCreate(&b->ev1));
+    b->plans.assign(plans, plans + nTrials);
+    b->views.resize(nTrials);
+    b->hT.resize(nTrials);
+    b->hL.resize(nTrials);
+    b->step.resize(nTrials);
+    b->end.resize(nTrials);
+    b->countOff.resize(nTrials + 1, 0);
+    for (int q = 0; q < b->n; q++) {
+        if (!plans[q]) return bfail(b, PV1_E_ARG, "null plan");
+        for (int r = 0; r < q; r++)
+            if (plans[r] == plans[q]) return bfail(b, PV1_E_ARG, "a plan appears twice in the batch");
+        int r = plan_batch_view(plans[q], &b->views[q]);
+        if (r) return bfail(b, r, "trial " + std::to_string(q) + ": " + pv1_last_error(plans[q]));
+        if (b->views[q].device != b->device) return bfail(b, PV1_E_ARG, "plans on different devices");
+        PV1_BCUDA(b, cudaStreamSynchronize(b->views[q].stream));
+        b->countOff[q + 1] = b->countOff[q] + b->views[q].vp.nV1;
+    }
+    int r = 0;
+    r |= balloc(b, &b->dT, nTrials);
+    r |= balloc(b, &b->dL, nTrials);
+    r |= balloc(b, &b->dCounts, (size_t)b->countOff[nTrials]);
+    r |= balloc(b, &b->dCountOff, nTrials + 1);
+    r |= balloc(b, &b->dSimTime, nTrials);
+    r |= balloc(b, &b->dMean, 1);
+    if (r) return r;
+    b->totalTiles = 0;
+    for (int q = 0; q < b->n; q++) {
+        const PlanBatchView &v = b->views[q];
+        BatchTrial &T = b->hT[q];
+        T.v = v.vp;
+        T.v.spikeCount = b->dCounts + b->countOff[q];
+        T.lgnRing = v.lgnRing;
+        T.lgnSlots = v.lgnSlots;
+        T.nCta = v.vp.nblock * ((v.vp.blockSize + 255) / 256);
+        T.step = v.d_stepBase;
+        T.tEnd = v.step + (long long)trialSteps[q];
+        T.tDeliverFrom = v.pending ? v.step : v.step + 1;
+        T.dt = (double)v.vp.dt;
+        BatchLgn &L = b->hL[q];
+        L.p = v.lp;
+        L.step = v.d_stepBase;
+        L.tEnd = T.tEnd;
+        b->step[q] = v.step;
+        b->end[q] = T.tEnd;
+        b->totalTiles += T.nCta;
+        b->maxCellCtas = std::max(b->maxCellCtas, (v.lp.nMagno + 127) / 128);
+        if (!v.lp.classCtw) b->allClass = false;
+        if (v.vp.condRng || v.vp.noiseRng) b->rng = true;
+        if (v.lgnSlots < 64) b->allClass = false;
+        PV1_BCUDA(b, cudaMemcpyAsync(v.d_stepBase, &b->step[q], sizeof(long long), cudaMemcpyHostToDevice,
+                                     b->stream));
+    }
+    PV1_BCUDA(b, cudaMemcpyAsync(b->dT, b->hT.data(), nTrials * sizeof(BatchTrial), cudaMemcpyHostToDevice,
+                                 b->stream));
+    PV1_BCUDA(b, cudaMemcpyAsync(b->dL, b->hL.data(), nTrials * sizeof(BatchLgn), cudaMemcpyHostToDevice,
+                                 b->stream));
+    PV1_BCUDA(b, cudaMemcpyAsync(b->dCountOff, b->countOff.data(), (nTrials + 1) * sizeof(long long),
+                                 cudaMemcpyHostToDevice, b->stream));
+    r = balloc(b, &b->dTiles, (size_t)b->totalTiles);
+    r |= balloc(b, &b->dNTiles, 1);
+    if (r) return r;
+    PV1_BCUDA(b, cudaStreamSynchronize(b->stream));
+    return refresh_tiles(b);
+}
+
+void pv1_batch_destroy(pv1_batch *b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    for (void *p : b->allocs) cudaFree(p);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+const char *pv1_batch_last_error(const pv1_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+int pv1_batch_autotune(pv1_batch *b, int enable) {
+    if (!b) return PV1_E_ARG;
+    b->tune = enable != 0;
+    b->nextCandidate = 0;
+    if (!b->tune) {
+        b->K = 64;
+        b->minB = 1;
+    }
+    return PV1_OK;
+}
+
+int pv1_batch_tuning(const pv1_batch *b, int *K, int *minB, float *times) {
+    if (!b) return PV1_E_ARG;
+    if (K) *K = b->K;
+    if (minB) *minB = b->minB;
+    if (times) std::memcpy(times, b->times, sizeof(b->times));
+    return PV1_OK;
+}
+
+int64_t pv1_batch_run(pv1_batch *b, uint64_t maxSteps, float *ms) {
+    if (!b) return PV1_E_ARG;
+    b->launches = 0;
+    uint64_t done = 0;
+    PV1_BCUDA(b, cudaEventRecord(b->ev0, b->stream));
+    while (true) {
+        long long left = 0, minLeft = -1;
+        for (int q = 0; q < b->n; q++) {
+            const long long l = b->end[q] - b->step[q];
+            if (l <= 0) continue;
+            left = std::max(left, l);
+            minLeft = minLeft < 0 ? l : std::min(minLeft, l);
+        }
+        if (left == 0 || (maxSteps && done >= maxSteps)) break;
+        int r = refresh_tiles(b);
+        if (r) return r;
+        const bool tuning = b->tune && b->nextCandidate < 9;
+        const int K = tuning ? kCandK[b->nextCandidate / 3] : b->K;
+        const int minB = tuning ? b->nextCandidate % 3 + 1 : b->minB;
+        long long k = std::min<long long>(K, minLeft);
+        if (maxSteps) k = std::min<long long>(k, (long long)(maxSteps - done));
+        if (b->allClass && k == K) {
+            cudaGraphExec_t g;
+            r = graph_for(b, K, minB, &g);
+            if (r) return r;
+            if (tuning) {
+                cudaEvent_t t0, t1;
+                PV1_BCUDA(b, cudaEventCreate(&t0));
+                PV1_BCUDA(b, cudaEventCreate(&t1));
+                PV1_BCUDA(b, cudaEventRecord(t0, b->stream));
+                PV1_BCUDA(b, cudaGraphLaunch(g, b->stream));
+                PV1_BCUDA(b, cudaEventRecord(t1, b->stream));
+                PV1_BCUDA(b, cudaEventSynchronize(t1));
+                float t = 0.f;
+                PV1_BCUDA(b, cudaEventElapsedTime(&t, t0, t1));
+                cudaEventDestroy(t0);
+                cudaEventDestroy(t1);
+                b->times[b->nextCandidate] = t;
+                b->nextCandidate++;
+                if (b->nextCandidate == 9) {
+                    // fastest per step
+                    int best = -1;
+                    for (int c = 0; c < 9; c++)
+                        if (b->times[c] > 0 && (best < 0 || b->times[c] / kCandK[c / 3] <
+                                                                b->times[best] / kCandK[best / 3]))
+                            best = c;
+                    if (best >= 0) {
+                        b->K = kCandK[best / 3];
+                        b->minB = best % 3 + 1;
+                    }
+                }
+            } else {
+                PV1_BCUDA(b, cudaGraphLaunch(g, b->stream));
+            }
+            b->launches += K + 2;
+        } else {
+            r = issue(b, (int)k, minB, &b->launches);
+            if (r) return r;
+        }
+        for (int q = 0; q < b->n; q++)
+            if (b->step[q] < b->end[q]) b->step[q] = std::min(b->end[q], b->step[q] + k);
+        done += (uint64_t)k;
+    }
+    PV1_BCUDA(b, cudaEventRecord(b->ev1, b->stream));
+    PV1_BCUDA(b, cudaEventSynchronize(b->ev1));
+    if (ms) PV1_BCUDA(b, cudaEventElapsedTime(ms, b->ev0, b->ev1));
+    int r = check_errors(b);
+    if (r) return r;
+    for (int q = 0; q < b->n; q++) plan_batch_finish(b->plans[q], b->step[q]);
+    long long left = 0;
+    for (int q = 0; q < b->n; q++) left = std::max(left, b->end[q] - b->step[q]);
+    return left;
+}
+
+int pv1_batch_stats(pv1_batch *b, uint32_t trial, double *simTimeMs, double *rates, double *meanRate) {
+    if (!b || trial >= (uint32_t)b->n) return PV1_E_ARG;
+    const int nV1 = b->hT[trial].v.nV1;
+    double *dRates = nullptr;
+    if (rates) PV1_BCUDA(b, cudaMalloc((void **)&dRates, nV1 * sizeof(double)));
+    cudaError_t e = launch_batch_rates(b->dT, b->dCounts, b->countOff.data(), b->dSimTime, (int)trial, nV1, dRates,
+                                       b->dMean, b->stream);
+    if (e == cudaSuccess && rates)
+        e = cudaMemcpyAsync(rates, dRates, nV1 * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess && meanRate)
+        e = cudaMemcpyAsync(meanRate, b->dMean, sizeof(double), cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess && simTimeMs)
+        e = cudaMemcpyAsync(simTimeMs, b->dSimTime + trial, sizeof(double), cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (dRates) cudaFree(dRates);
+    if (e != cudaSuccess) return bfail(b, PV1_E_CUDA, cudaGetErrorString(e));
+    return PV1_OK;
+}
+
+int64_t pv1_batch_launch_count(const pv1_batch *b) { return b ? b->launches : -1; }
+
+}  // extern "C"

@@ -175,6 +175,7 @@ struct V1Params {
     const int *farN1;          // [nV1] leading synapses of each list with whole-step delay <= 1
     int4 *farList;             // [3][nV1] step t%3's far spikers: (pre, first synapse, count, sInfo bits)
     int *farCount;             // [3] length of each list
+    unsigned *spikeCount;      // [nV1] spikes per neuron since the counters were cleared (may be null)
     // records
     float *rec; long long recStride; int recSlots; int hWrite;
     float *recSpk;             // [recSlots][nV1] spike words (PV1_REC_SPIKES)
@@ -230,6 +231,50 @@ cudaError_t compute_step_decay(V1Params &p, cudaStream_t st);
 cudaError_t launch_v1_persistent(const V1Params &p, const long long *stepBase, int K, const float *lgnRing,
                                  int lgnSlots, int deliverFirst, unsigned *barrier, cudaStream_t st);
 cudaError_t launch_advance_step(long long *stepBase, int k, cudaStream_t st);
+
+// ---- batched trials: many independent patches stepped by the same launches ----
+// One trial of a batch as the V1 kernel sees it (copied to shared memory by each CTA).
+struct BatchTrial {
+    V1Params v;
+    const float *lgnRing;
+    int lgnSlots;
+    int nCta;                  // CTAs of this patch (nblock * ceil(blockSize / 256))
+    long long *step;           // the trial's device step counter (its plan's)
+    long long tEnd;            // first step the trial does not run
+    long long tDeliverFrom;    // steps t >= this deliver the spikes of step t-1 first
+    double dt;
+};
+// One trial as the LGN kernel sees it.
+struct BatchLgn {
+    LgnParams p;
+    long long *step;
+    long long tEnd;
+};
+// What the batch needs from a plan (defined in pv1_plan.cu).
+struct PlanBatchView {
+    V1Params vp;
+    LgnParams lp;
+    const float *lgnRing;
+    int lgnSlots;
+    long long *d_stepBase;
+    long long step;
+    bool pending;
+    int device;
+    cudaStream_t stream;
+};
+int plan_batch_view(pv1_plan *p, PlanBatchView *out);
+void plan_batch_finish(pv1_plan *p, long long step);
+// minB selects the __launch_bounds__ variant (1, 2 or 3 resident CTAs per SM).
+cudaError_t launch_v1_batch_step(const BatchTrial *trials, const int2 *tiles, const int *nTiles,
+                                 int gridTiles, int stepOffset, bool rng, int minB, cudaStream_t st);
+cudaError_t launch_lgn_class_batch(const BatchLgn *trials, int nTrials, int maxCellCtas, int K,
+                                   cudaStream_t st);
+cudaError_t launch_batch_advance(BatchTrial *trials, int nTrials, int K, double *simTime,
+                                 cudaStream_t st);
+cudaError_t launch_batch_rates(const BatchTrial *trials, const unsigned *counts, const long long *countOff,
+                               const double *simTime, int trial, int nV1, double *rates,
+                               double *meanRate, cudaStream_t st);
+int v1_batch_regs(int minB, bool rng);
 
 // Fixed-point scale for far-delivery accumulation: integer adds are associative, so the
 // sum of events does not depend on their order and runs are reproducible.

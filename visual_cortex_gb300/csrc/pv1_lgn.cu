@@ -237,13 +237,12 @@ constexpr int kClassCta = 128;
 // each step contracts them with W, applies the logistic rate and draws the Poisson spikes.
 // The arithmetic per (cell, step) is the one of lgn_rate_kernel + lgn_spike_kernel: same
 // segment weights, same summation order, same generator calls.
-__global__ void __launch_bounds__(kClassCta) lgn_class_kernel(LgnParams P, const long long *stepBase, int K) {
+__device__ __forceinline__ void lgn_class_body(const LgnParams &P, long long t0, int K, int cellBase) {
     extern __shared__ float sS[];                       // [kClassMaxSlots][kClassCta]
     __shared__ float sW[kClassMaxK][kClassMaxSeg];
     __shared__ unsigned char sSlot[kClassMaxK][kClassMaxSeg];
     __shared__ int sNseg[kClassMaxK];
     __shared__ int sFlo, sNU;
-    const long long t0 = *stepBase;
     const FrameSched fs = P.fs;
     if (threadIdx.x == 0) {
         const int cf0 = frames_read_after_step(fs, t0);
@@ -279,7 +278,7 @@ __global__ void __launch_bounds__(kClassCta) lgn_class_kernel(LgnParams P, const
             sSlot[s][q] = (unsigned char)min(max(slot, 0), kClassMaxSlots - 1);
         }
     }
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    const int cell = cellBase + threadIdx.x;
     const bool on = cell < P.nMagno;
     if (on) {
         for (int u = 0; u < nU; u++) {
@@ -344,6 +343,26 @@ __global__ void __launch_bounds__(kClassCta) lgn_class_kernel(LgnParams P, const
     P.leftTimeRate[id] = ltr;
     P.lastNegLogRand[id] = lnl;
     P.state[id] = st;
+}
+
+__global__ void __launch_bounds__(kClassCta) lgn_class_kernel(LgnParams P, const long long *stepBase, int K) {
+    lgn_class_body(P, *stepBase, K, blockIdx.x * kClassCta);
+}
+
+// The single-class LGN chunk for every trial of a batch: grid (cell CTAs, trials); each CTA
+// copies its trial's parameters to shared memory and runs the same body for the steps the
+// trial still has in this chunk.
+__global__ void __launch_bounds__(kClassCta) lgn_class_batch_kernel(const BatchLgn *__restrict__ trials, int K) {
+    __shared__ __align__(16) BatchLgn sT;
+    const int *src = reinterpret_cast<const int *>(trials + blockIdx.y);
+    int *dst = reinterpret_cast<int *>(&sT);
+    for (int w = threadIdx.x; w < (int)(sizeof(BatchLgn) / sizeof(int)); w += kClassCta) dst[w] = src[w];
+    __syncthreads();
+    const long long t0 = *sT.step;
+    const long long left = sT.tEnd - t0;
+    const int k = left < K ? (int)left : K;
+    if (k <= 0 || (int)blockIdx.x * kClassCta >= sT.p.nMagno) return;
+    lgn_class_body(sT.p, t0, k, blockIdx.x * kClassCta);
 }
 
 // Temporal contraction and logistic rate for (cell, step) pairs of a chunk of K steps: grid
@@ -497,6 +516,21 @@ cudaError_t launch_lgn_step(const LgnParams &p, const long long *stepBase, int K
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     lgn_spike_kernel<<<(p.nMagno + 255) / 256, 256, 0, st>>>(p, stepBase, K);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lgn_class_batch(const BatchLgn *trials, int nTrials, int maxCellCtas, int K, cudaStream_t st) {
+    if (nTrials <= 0 || maxCellCtas <= 0) return cudaSuccess;
+    if (K > kClassMaxK) return cudaErrorInvalidValue;
+    const size_t smem = (size_t)kClassMaxSlots * kClassCta * sizeof(float);
+    static bool attrSet = false;
+    if (!attrSet) {
+        cudaError_t e = cudaFuncSetAttribute(lgn_class_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        attrSet = true;
+    }
+    lgn_class_batch_kernel<<<dim3(maxCellCtas, nTrials), kClassCta, smem, st>>>(trials, K);
     return cudaGetLastError();
 }
 

@@ -200,6 +200,30 @@ int plan_lgn_view(pv1_plan *p, PlanLgnView *out) {
 
 void plan_advance_steps(pv1_plan *p, long long n) { p->step += n; }
 
+int plan_batch_view(pv1_plan *p, PlanBatchView *out) {
+    if (!p || !out) return PV1_E_ARG;
+    if (!p->lgnReady || !p->stimReady) return fail(p, PV1_E_STATE, "LGN/stimulus not loaded");
+    if (!p->haveLGNsyn || !p->haveNear || !p->haveState || !p->haveRng)
+        return fail(p, PV1_E_STATE, "V1 synapses/connectivity/state/rng not set");
+    out->vp = p->vp;
+    out->lp = p->lp;
+    out->lgnRing = p->d_lgnRing;
+    out->lgnSlots = p->lgnSlots;
+    out->d_stepBase = p->d_stepBase;
+    out->step = p->step;
+    out->pending = p->pending;
+    out->device = p->device;
+    out->stream = p->stream;
+    return PV1_OK;
+}
+
+void plan_batch_finish(pv1_plan *p, long long step) {
+    if (step > p->step) {
+        p->step = step;
+        p->pending = true;
+    }
+}
+
 int plan_fail(pv1_plan *p, int code, const char *msg) { return fail(p, code, msg); }
 
 }  // namespace pv1

@@ -487,6 +487,30 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
             lgn_input<Rng>(P, itype, sFF, f, backingUp, tBack, pf, nSynFF, g0, h0, g1, h1, condState, recFF,
                            nFF);
         }
+    } else if (m <= kMaxLgnReg) {
+        // ids and spike words in chunks of 16 (all loads of a chunk in flight together); the
+        // weight is read only for synapses that received a spike, in synapse order
+        unsigned mask = 0u;
+#pragma unroll
+        for (int c = 0; c < kMaxLgnReg; c += 16) {
+            if (c < m) {
+                int ids[16];
+#pragma unroll
+                for (int k = 0; k < 16; k++) ids[k] = c + k < m ? __ldg(P.lgnId + (size_t)(c + k) * nV1 + i) : 0;
+#pragma unroll
+                for (int k = 0; k < 16; k++)
+                    mask |= ((c + k < m && __ldcg(lgnSInfo + ids[k]) >= 1.0f) ? 1u : 0u) << (c + k);
+            }
+        }
+        while (mask) {
+            const int q = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const size_t lid = (size_t)q * nV1 + i;
+            const float sFF = __ldcg(lgnSInfo + __ldg(P.lgnId + lid));
+            const float f = __ldg(P.sLGN + lid);
+            lgn_input<Rng>(P, itype, sFF, f, backingUp, tBack, pf, nSynFF, g0, h0, g1, h1, condState, recFF,
+                           nFF);
+        }
     } else {
         for (int q0 = 0; q0 < m; q0 += kLgnBatch) {
             int ids[kLgnBatch];
@@ -675,13 +699,13 @@ __device__ __forceinline__ int owner_of(const Smem &sm, int cnt, int w) {
 // step tl, from the step's global spiker list.  The (spiker, synapse) work is flattened over
 // every thread of the grid, so one CTA's burst of spikers no longer serialises on that CTA;
 // the fixed-point ring makes the sums independent of the order of the atomic appends.
-__device__ __forceinline__ void far_push_list(const V1Params &P, long long tl, Smem &sm) {
+__device__ __forceinline__ void far_push_list(const V1Params &P, long long tl, Smem &sm, int cta, int nCta) {
     const int slot = (int)((tl + 3) % 3);  // tl >= -1
     const int n = __ldcg(P.farCount + slot);
     if (n == 0) return;
     const int4 *list = P.farList + (size_t)slot * P.nV1;
-    const int G = gridDim.x * kCta;
-    const int gt = blockIdx.x * kCta + threadIdx.x;
+    const int G = nCta * kCta;
+    const int gt = cta * kCta + threadIdx.x;
     int W0 = 0;  // work of the earlier chunks, modulo G
     for (int c0 = 0; c0 < n; c0 += kCta) {
         const int cnt = min(kCta, n - c0);
@@ -723,8 +747,8 @@ __device__ __forceinline__ void far_push_list(const V1Params &P, long long tl, S
 // (whole-step delay 0 or 1: the first n1 synapses of each list), which must be in the ring
 // before the next step delivers it.  All threads of the CTA call it.
 __device__ __forceinline__ void far_phase(const V1Params &P, long long t, int i, bool active, float sInfo,
-                                          bool isFarPre, int e0, int deg, int n1, Smem &sm) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+                                          bool isFarPre, int e0, int deg, int n1, Smem &sm, int cta) {
+    if (cta == 0 && threadIdx.x == 0) {
         P.farFlag[(t + 1) % 3] = 0;
         P.farCount[(t + 1) % 3] = 0;
     }
@@ -779,18 +803,16 @@ __device__ __forceinline__ void far_phase(const V1Params &P, long long t, int i,
     }
 }
 
+// One V1 step (with the delivery of the previous step first) for CTA `cta` of the nCta CTAs
+// that hold one patch: the per-step kernel and the batched kernel run this body.
 template <bool Rng>
-__global__ void __launch_bounds__(kCta) v1_step_kernel(V1Params P, const long long *stepBase,
-                                                       int stepOffset,
-                                                       const float *__restrict__ lgnRing,
-                                                       int lgnSlots, int deliverPrev,
-                                                       int doStep) {
-    __shared__ Smem sm;
-    const long long t = *stepBase + stepOffset;
+__device__ __forceinline__ void v1_step_body(const V1Params &P, long long t, int cta, int nCta,
+                                             const float *__restrict__ lgnRing, int lgnSlots,
+                                             int deliverPrev, int doStep, Smem &sm) {
     const int bs = P.blockSize;
     const int nq = (bs + kCta - 1) / kCta;
-    const int b = blockIdx.x / nq;
-    const int local = (blockIdx.x % nq) * kCta + threadIdx.x;
+    const int b = cta / nq;
+    const int local = (cta % nq) * kCta + threadIdx.x;
     const bool active = local < bs;
     const int i = b * bs + (active ? local : 0);
     const int itype = type_of(P, active ? local : 0);
@@ -819,15 +841,27 @@ __global__ void __launch_bounds__(kCta) v1_step_kernel(V1Params P, const long lo
         store_state(P, i, st);
         if (Rng && P.condRng) P.rGenCond[i] = condState;
         if (Rng && P.noiseRng) P.rNoisy[i] = noisyState;
+        if (P.spikeCount && sInfo >= 1.0f) P.spikeCount[i] += (unsigned)floorf(sInfo);
     }
     if (P.farOn) {
         const int e0 = active ? P.farOff[i] : 0;
         const int deg = active ? P.farOff[i + 1] - e0 : 0;
         const int n1 = active ? P.farN1[i] : 0;
         const bool isFarPre = active && P.farPre[i];
-        far_push_list(P, t - 1, sm);
-        far_phase(P, t, i, active, sInfo, isFarPre, e0, deg, n1, sm);
+        far_push_list(P, t - 1, sm, cta, nCta);
+        far_phase(P, t, i, active, sInfo, isFarPre, e0, deg, n1, sm, cta);
     }
+}
+
+template <bool Rng>
+__global__ void __launch_bounds__(kCta) v1_step_kernel(V1Params P, const long long *stepBase,
+                                                       int stepOffset,
+                                                       const float *__restrict__ lgnRing,
+                                                       int lgnSlots, int deliverPrev,
+                                                       int doStep) {
+    __shared__ Smem sm;
+    const long long t = *stepBase + stepOffset;
+    v1_step_body<Rng>(P, t, blockIdx.x, gridDim.x, lgnRing, lgnSlots, deliverPrev, doStep, sm);
 }
 
 // Grid-wide barrier between the steps of the persistent kernel: arrive on a counter, the
@@ -905,10 +939,11 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
             const float *lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
             sInfo = step_neuron<Rng, true>(P, t, i, itype, tonic, depC, m, lgnIds, lgnSInfo, st, condState,
                                            noisyState);
+            if (P.spikeCount && sInfo >= 1.0f) P.spikeCount[i] += (unsigned)floorf(sInfo);
         }
         if (P.farOn) {
-            far_push_list(P, t - 1, sm);
-            far_phase(P, t, i, active, sInfo, isFarPre, farE0, farDeg, farN1, sm);
+            far_push_list(P, t - 1, sm, blockIdx.x, gridDim.x);
+            far_phase(P, t, i, active, sInfo, isFarPre, farE0, farDeg, farN1, sm, blockIdx.x);
         }
         if (s + 1 < K && !grid_barrier(barrier, barrier + 1, gridDim.x, P.err)) break;
     }
@@ -1027,6 +1062,110 @@ cudaError_t launch_v1_rng_init(curandStateMRG32k3a *cond, curandStateMRG32k3a *n
 
 cudaError_t launch_advance_step(long long *stepBase, int k, cudaStream_t st) {
     advance_step_kernel<<<1, 1, 0, st>>>(stepBase, k);
+    return cudaGetLastError();
+}
+
+// ---- batched trials ----
+// One step of every active (trial, CTA) tile of a batch.  Each CTA copies its trial's
+// parameter block to shared memory and runs the same step body as the per-step kernel with
+// the trial's own CTA index and count, so each trial computes exactly what it would alone.
+// Finished trials have no tiles in the list (the host rebuilds it between chunks); a tile
+// whose trial ends inside the chunk returns at its last step.
+template <bool Rng, int MinB>
+__global__ void __launch_bounds__(kCta, MinB) v1_batch_step_kernel(const BatchTrial *__restrict__ trials,
+                                                                   const int2 *__restrict__ tiles,
+                                                                   const int *__restrict__ nTiles,
+                                                                   int stepOffset) {
+    __shared__ Smem sm;
+    __shared__ __align__(16) BatchTrial sT;
+    if ((int)blockIdx.x >= *nTiles) return;
+    const int2 tile = tiles[blockIdx.x];
+    const int *src = reinterpret_cast<const int *>(trials + tile.x);
+    int *dst = reinterpret_cast<int *>(&sT);
+    for (int w = threadIdx.x; w < (int)(sizeof(BatchTrial) / sizeof(int)); w += kCta) dst[w] = src[w];
+    __syncthreads();
+    const long long t = *sT.step + stepOffset;
+    if (t >= sT.tEnd) return;
+    v1_step_body<Rng>(sT.v, t, tile.y, sT.nCta, sT.lgnRing, sT.lgnSlots, t >= sT.tDeliverFrom ? 1 : 0, 1, sm);
+}
+
+template <bool Rng>
+static cudaError_t launch_batch_variant(int minB, const BatchTrial *trials, const int2 *tiles,
+                                        const int *nTiles, int grid, int stepOffset, cudaStream_t st) {
+    switch (minB) {
+    case 1: v1_batch_step_kernel<Rng, 1><<<grid, kCta, 0, st>>>(trials, tiles, nTiles, stepOffset); break;
+    case 2: v1_batch_step_kernel<Rng, 2><<<grid, kCta, 0, st>>>(trials, tiles, nTiles, stepOffset); break;
+    case 3: v1_batch_step_kernel<Rng, 3><<<grid, kCta, 0, st>>>(trials, tiles, nTiles, stepOffset); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_v1_batch_step(const BatchTrial *trials, const int2 *tiles, const int *nTiles,
+                                 int gridTiles, int stepOffset, bool rng, int minB, cudaStream_t st) {
+    if (gridTiles <= 0) return cudaSuccess;
+    return rng ? launch_batch_variant<true>(minB, trials, tiles, nTiles, gridTiles, stepOffset, st)
+               : launch_batch_variant<false>(minB, trials, tiles, nTiles, gridTiles, stepOffset, st);
+}
+
+int v1_batch_regs(int minB, bool rng) {
+    cudaFuncAttributes a{};
+    cudaError_t e = cudaErrorInvalidValue;
+    if (rng) {
+        if (minB == 1) e = cudaFuncGetAttributes(&a, v1_batch_step_kernel<true, 1>);
+        if (minB == 2) e = cudaFuncGetAttributes(&a, v1_batch_step_kernel<true, 2>);
+        if (minB == 3) e = cudaFuncGetAttributes(&a, v1_batch_step_kernel<true, 3>);
+    } else {
+        if (minB == 1) e = cudaFuncGetAttributes(&a, v1_batch_step_kernel<false, 1>);
+        if (minB == 2) e = cudaFuncGetAttributes(&a, v1_batch_step_kernel<false, 2>);
+        if (minB == 3) e = cudaFuncGetAttributes(&a, v1_batch_step_kernel<false, 3>);
+    }
+    return e == cudaSuccess ? a.numRegs : -1;
+}
+
+// Per trial: step += the steps it ran in the chunk (K, or fewer at its end), and its FP64
+// simulated-time accumulator += those steps * dt.
+__global__ void batch_advance_kernel(BatchTrial *trials, int nTrials, int K, double *simTime) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nTrials) return;
+    const long long s = *trials[q].step;
+    long long k = trials[q].tEnd - s;
+    k = k < 0 ? 0 : (k > K ? K : k);
+    *trials[q].step = s + k;
+    simTime[q] += (double)k * trials[q].dt;
+}
+
+cudaError_t launch_batch_advance(BatchTrial *trials, int nTrials, int K, double *simTime, cudaStream_t st) {
+    batch_advance_kernel<<<(nTrials + 127) / 128, 128, 0, st>>>(trials, nTrials, K, simTime);
+    return cudaGetLastError();
+}
+
+// FP64 firing rates of one trial: rate[i] = count[i] / simulated seconds, and the mean over
+// its neurons (one CTA, double-precision tree reduction).
+__global__ void __launch_bounds__(1024) batch_rates_kernel(const unsigned *counts, int nV1, const double *simTime,
+                                                           double *rates, double *meanRate) {
+    __shared__ double red[32];
+    const double sec = *simTime * 1e-3;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < nV1; i += blockDim.x) {
+        const double r = sec > 0 ? (double)counts[i] / sec : 0.0;
+        if (rates) rates[i] = r;
+        acc += r;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        acc = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (threadIdx.x == 0) *meanRate = acc / (double)nV1;
+    }
+}
+
+cudaError_t launch_batch_rates(const BatchTrial *, const unsigned *counts, const long long *countOff,
+                               const double *simTime, int trial, int nV1, double *rates, double *meanRate,
+                               cudaStream_t st) {
+    batch_rates_kernel<<<1, 1024, 0, st>>>(counts + countOff[trial], nV1, simTime + trial, rates, meanRate);
     return cudaGetLastError();
 }
 

@@ -291,7 +291,7 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
         if c.getLGN_sp:
             lsp = FM.LgnSpWriter(P.lgn_sp, spec.dt, m.nt, nLGN)
         if flags:
-            sim.set_record(flags, chunk)
+            sim.set_record(flags, chunk + 1)
         done = 0
         while done < m.nt:
             k = min(chunk, m.nt - done)

@@ -367,3 +367,50 @@ def write_reference_files(wl: Workload, folder: str, seed: int = 0, nt: int | No
     with open(fn, "w") as f:
         f.write("# synthetic patch written by visual_cortex_gb300.synth\n" + write_cfg(keys))
     return fn
+
+
+@dataclass
+class Trial:
+    wl: Workload          # the trial's full workload (network shared with the other trials)
+    steps: int
+    orient: float
+    contrast: float
+
+
+def batch_trials(n_trials: int = 64, seed: int = 0, nblock: int = 8, n_lgn: int = 4096,
+                 width: int = 128, height: int = 128, nFrame: int = 120, n_ori: int = 12,
+                 dur_ms=(250.0, 2000.0), contrast=(0.1, 1.0), far_partners: int = 400,
+                 patch_deg: float = 2.0, base: Workload | None = None) -> list[Trial]:
+    """Batched sweep: n_trials instances of one nblock x 1024 patch (the recipe of the 32-block
+    patch), orientation (i mod n_ori) * pi / n_ori, contrast and duration uniform in the given
+    ranges, each trial with its own seeds for the LGN generators, the V1 generators and the
+    initial state."""
+    rng = np.random.default_rng(seed + 777)
+    if base is None:
+        base = make_workload("batch base", seed=seed, nblock=nblock, n_lgn=n_lgn, m=20,
+                             width=width, height=height, nt=0, far_partners=far_partners,
+                             adex_inh=True, patch_deg=patch_deg, nFrame=nFrame)
+    spec, net, lgn = base.spec, base.net, base.lgn
+    extent = 2 * (max(float(np.max(np.hypot(lgn.xy[:, 0], lgn.xy[:, 1]))),
+                      float(np.max(np.abs(lgn.xy)))) * 1.05 + 0.2)
+    out = []
+    for q in range(n_trials):
+        ori = (q % n_ori) * math.pi / n_ori
+        c = float(rng.uniform(*contrast))
+        steps = int(round(float(rng.uniform(*dur_ms)) / spec.dt))
+        frames = grating_frames(base.stim.frames.shape[0], base.stim.frames.shape[3],
+                                base.stim.frames.shape[2], extent, cpd=4.0, tf_hz=8.0,
+                                contrast=c, orient=ori, frame_rate=120)
+        s = seed + 1000 * (q + 1)
+        s_init = s + 1 + spec.nV1
+        gFF0 = np.tile([0.01, 0.2, 0.0, 0.2], spec.nType * spec.ngFF).astype(f32)
+        gE0 = np.tile([0.005, 0.2, 0.0, 0.2], spec.nType * spec.ngE).astype(f32)
+        gI0 = np.tile([0.01, 0.2, 0.0, 0.2], spec.nType * spec.ngI).astype(f32)
+        w0 = np.zeros(2 * spec.nType, f32)
+        init = host_init_state(spec, s_init, net.tonicDep, net.nLGNperV1, None, w0, gFF0, gE0, gI0)
+        wl = Workload(name=f"trial {q}", spec=spec, net=net, lgn=lgn,
+                      stim=Stimulus(frames=frames, init_LMS=(0.5, 0.5, 0.5)), init=init,
+                      seeds=Seeds(lgn=s, cond=s_init + 1, trainDepth=base.seeds.trainDepth),
+                      nt=steps, pos=base.pos, rf_center=base.rf_center, rf_orient=base.rf_orient)
+        out.append(Trial(wl=wl, steps=steps, orient=ori, contrast=c))
+    return out

@@ -222,10 +222,44 @@ def run_gb300(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(wl, args.cpu_sample_steps)
+    if rank == 0 and not args.no_forms:
+        del wl, sim
+        forms = {"batched": bench_batched(args.batch_trials)}
+        forms["batched"]["vs_plain"] = forms["batched"]["value"] / value
+        out["forms"] = forms
     if dist:
         dist.barrier()
         dist.destroy_process_group()
     return out if rank == 0 else None
+
+
+def bench_batched(n_trials: int):
+    """The batched sweep: n_trials instances of an 8 x 1024 patch, 12 orientations, contrast
+    U[0.1, 1], durations U[250, 2000] ms, all run to their ends by one Batch (autotuned).
+    Value = sum over trials of neurons x steps / device time of the whole sweep."""
+    from visual_cortex_gb300 import synth
+    from visual_cortex_gb300.batch import Batch
+    from visual_cortex_gb300.model import Simulation
+    trials = synth.batch_trials(n_trials=n_trials, seed=0)
+    t0 = time.perf_counter()
+    sims = [Simulation(t.wl.spec, t.wl.net, t.wl.lgn, t.wl.stim, t.wl.init, t.wl.seeds) for t in trials]
+    b = Batch(sims, [t.steps for t in trials], autotune=True)
+    _, ms = b.run()
+    rates = [b.stats(q)[1] for q in range(len(trials))]
+    e2e_s = time.perf_counter() - t0
+    launches = b.launches()
+    tuning = b.tuning()
+    b.close()
+    for s in sims:
+        s.close()
+    work = sum(t.steps * t.wl.spec.nV1 for t in trials)
+    return {"value": work / (ms * 1e-3), "unit": UNIT, "device_ms": ms,
+            "e2e": {"value": work / e2e_s, "unit": UNIT,
+                    "note": "plan creation with all host->device uploads, the sweep and the FP64 rate read-back"},
+            "workload": f"{n_trials} trials x 8x1024 V1 / 4096 LGN, 128x128 gratings at 12 orientations, "
+                        "contrast U[0.1,1], durations U[250,2000] ms, dt 0.125 ms",
+            "neuron_steps": work, "trial_steps": [t.steps for t in trials], "gpu_launches": launches,
+            "tuning": tuning, "mean_rate_hz": float(np.mean(rates))}
 
 
 def cpu_baseline(wl, nsteps: int):
@@ -280,6 +314,8 @@ def main():
     ap.add_argument("--sim-steps", type=int, default=800)
     ap.add_argument("--cpu-sample-steps", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched / adjoint / BF16 lines")
+    ap.add_argument("--batch-trials", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

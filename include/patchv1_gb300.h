@@ -304,6 +304,45 @@ int pv1_batch_stats(pv1_batch *batch, uint32_t trial, double *simTimeMs, double 
 /* Kernel launches issued by the last pv1_batch_run. */
 int64_t pv1_batch_launch_count(const pv1_batch *batch);
 
+/* ---- Surrogate-gradient adjoint ----------------------------------------------------------
+ * No counterpart in the reference (it has no gradient code).  The differentiable form of the
+ * V1 step: conductance-based LIF, RK2 membrane step, two-state AMPA (from the LGN) and GABA
+ * (from the block's I neurons) kernels with the conductance-shape constants of
+ * src/condShape.h:13-51 passed in as (Ed, Er, dod) = (e^{-dt/td}, e^{-dt/tr}, tr/(td-tr)),
+ * spikes with a fast-sigmoid surrogate derivative, step-granular delivery, B independent
+ * trials.  All pointers are device pointers owned by the caller (torch tensors); work goes on
+ * `stream` (a cudaStream_t, 0 = legacy default).  Sizes: N = nblock*blockSize, nI = blockSize-nE,
+ * nWin = T/win, nSeg = ceil(T/seg). */
+typedef struct {
+    uint32_t B, nblock, blockSize, nE, nLGN, K, T, seg, win;
+    float dt, vL, vE, vI, vR, vThres, gL, slope;  /* slope of the surrogate, 1/mV */
+    uint32_t tRefE, tRefI;                          /* refractory steps */
+    float EdE, ErE, dodE, EdI, ErI, dodI;           /* AMPA and GABA kernel constants */
+} pv1_adj_problem;
+
+typedef struct {
+    const int32_t *ids;   /* [K][N] LGN id of synapse k of neuron n */
+    const float *W;       /* [K][N] LGN->V1 weights */
+    const uint8_t *X;     /* [B][T][nLGN] LGN spike counts per step */
+    const float *Crec;    /* [nblock][nI][blockSize] I -> block GABA weights (pre row, post column) */
+    const float *I0;      /* [N] constant drive */
+    const float *v0;      /* [B][N] initial v (conductances start at 0) */
+    float *rates;         /* out [B][nWin][N] spike rate per window (Hz) */
+    float *vbar;          /* out [B][nWin][N] mean v per window (mV) */
+    float *ck;            /* [nSeg][6][B][N] checkpoints, written by forward, read by backward */
+    const float *gR;      /* [B][nWin][N] dL/drates (may be null) */
+    const float *gV;      /* [B][nWin][N] dL/dvbar (may be null) */
+    float *gW;            /* out [K][N] dL/dW, accumulated (zero it first) */
+    double *gC;           /* out [6] dL/d(EdE, ErE, dodE, EdI, ErI, dodI), accumulated */
+    float *scratch;       /* [B*nblock][seg][6][blockSize] recompute buffer */
+} pv1_adj_buffers;
+
+uint64_t pv1_adj_checkpoint_floats(const pv1_adj_problem *p);
+uint64_t pv1_adj_scratch_floats(const pv1_adj_problem *p);
+int pv1_adj_forward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *stream);
+int pv1_adj_backward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *stream);
+const char *pv1_adj_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,361 @@
+// Surrogate-gradient adjoint of a conductance-based LIF patch (the differentiable form).
+//
+// The reference has no gradient code; this is the differentiable counterpart of its V1 step
+// (src/coredynamics.cu:1235-2059 with the two-state conductance kernel of
+// src/condShape.h:13-51), on batches of trials:
+//   conductances  g' = g*Ed + h*dod*(Ed - Er),  h' = h*Er   (Ed = e^{-dt/td}, Er = e^{-dt/tr},
+//                 dod = tr/(td - tr)), AMPA from the LGN, GABA from the block's I neurons;
+//   membrane      RK2 (Heun) of dv/dt = -gL(v-vL) - gE(v-vE) - gI(v-vI) + I0 with the
+//                 conductances of the start and of the end of the step, as the reference;
+//   spikes        s = H(vn - vThres) forward, ds/dvn = 1/(1 + slope|vn - vThres|)^2 (fast
+//                 sigmoid) backward; reset to vR with the reset gate held constant; refractory
+//                 steps hold v at vR;
+//   inputs        end of step t: hE += sum_k W[k][n] X[t][id[k][n]] (k ascending),
+//                 hI += sum of C[p][n] over the I neurons p of the block that spiked (ascending);
+//   outputs       per window of `win` steps: spike rate (Hz) and mean membrane potential.
+// Spikes are delivered at step granularity (no sub-step spike-time offsets).
+//
+// One CTA holds one (trial, block) pair, one thread per neuron; blocks do not interact.  The
+// forward stores a checkpoint of (v, gE, hE, gI, hI, refractory count) every `seg` steps; the
+// backward walks the segments from the last one, recomputes each forward from its checkpoint
+// into a per-CTA scratch, then runs the adjoint backwards through it.  The recurrent term of
+// the adjoint (sum over posts of C[p][n] * lambda_hI[n] for every I neuron p) is a
+// warp-cooperative mat-vec over the block's C rows per step.  Gradients: dL/dW by atomic adds
+// at the (sparse) LGN events, dL/d(EdE, ErE, dodE, EdI, ErI, dodI) reduced in FP64.
+#include <cmath>
+#include <cstdint>
+#include <string>
+
+#include "pv1_internal.cuh"
+
+namespace {
+
+thread_local std::string g_adjErr;
+
+struct AdjArgs {
+    pv1_adj_problem p;
+    pv1_adj_buffers b;
+    int N, nI, nWin, nSeg;
+};
+
+constexpr int kAdjMaxK = 32;
+
+struct AState {
+    float v, gE, hE, gI, hI;
+    int ref;
+};
+
+__device__ __forceinline__ float adj_f(float v, float gE, float gI, float gL, float vL, float vE, float vI,
+                                       float I0) {
+    return -gL * (v - vL) - gE * (v - vE) - gI * (v - vI) + I0;
+}
+
+// Forward step of one neuron up to the spike decision; returns v_next, sets spk, refr and the
+// decayed conductances.  Shared by the forward and the recompute of the backward.
+__device__ __forceinline__ float adj_neuron_step(const pv1_adj_problem &P, AState &s, float I0, bool isE,
+                                                 bool &spk, bool &refr, float &gE1, float &hE1, float &gI1,
+                                                 float &hI1) {
+    gE1 = s.gE * P.EdE + s.hE * P.dodE * (P.EdE - P.ErE);
+    hE1 = s.hE * P.ErE;
+    gI1 = s.gI * P.EdI + s.hI * P.dodI * (P.EdI - P.ErI);
+    hI1 = s.hI * P.ErI;
+    refr = s.ref > 0;
+    spk = false;
+    if (refr) {
+        s.ref -= 1;
+        return P.vR;
+    }
+    const float k1 = adj_f(s.v, s.gE, s.gI, P.gL, P.vL, P.vE, P.vI, I0);
+    const float v1 = s.v + P.dt * k1;
+    const float k2 = adj_f(v1, gE1, gI1, P.gL, P.vL, P.vE, P.vI, I0);
+    const float vn = s.v + (P.dt * 0.5f) * (k1 + k2);
+    spk = vn > P.vThres;
+    if (spk) {
+        s.ref = (int)(isE ? P.tRefE : P.tRefI);
+        return P.vR;
+    }
+    return vn;
+}
+
+// The end-of-step inputs: LGN events into hE (synapse order), spiking I neurons of the block
+// into hI (ascending).  ball[] holds this step's spike ballots of the CTA's warps.
+__device__ __forceinline__ void adj_inputs(const AdjArgs &A, int b, int t, int n, int local, float &hE,
+                                           float &hI, const unsigned *ball) {
+    const pv1_adj_problem &P = A.p;
+    const uint8_t *x = A.b.X + ((size_t)b * P.T + t) * P.nLGN;
+    for (int k = 0; k < (int)P.K; k++) {
+        const int id = __ldg(A.b.ids + (size_t)k * A.N + n);
+        const uint8_t c = __ldg(x + id);
+        if (c) hE = hE + __ldg(A.b.W + (size_t)k * A.N + n) * (float)c;
+    }
+    const int blk = n / (int)P.blockSize;
+    const float *C = A.b.Crec + (size_t)blk * A.nI * P.blockSize;
+    const int nWarp = ((int)P.blockSize + 31) / 32;
+    for (int w = (int)P.nE / 32; w < nWarp; w++) {
+        unsigned bits = ball[w];
+        while (bits) {
+            const int lane = __ffs(bits) - 1;
+            bits &= bits - 1;
+            const int pl = w * 32 + lane;
+            if (pl < (int)P.nE) continue;
+            hI = hI + __ldg(C + (size_t)(pl - (int)P.nE) * P.blockSize + local);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(1024) adj_forward_kernel(AdjArgs A) {
+    __shared__ unsigned ball[32];
+    const pv1_adj_problem &P = A.p;
+    const int blk = blockIdx.x, b = blockIdx.y;
+    const int local = threadIdx.x;
+    const bool on = local < (int)P.blockSize;
+    const int n = blk * (int)P.blockSize + (on ? local : 0);
+    const size_t bn = (size_t)b * A.N + n;
+    const bool isE = local < (int)P.nE;
+    const float I0 = on ? A.b.I0[n] : 0.f;
+    AState s{on ? A.b.v0[bn] : P.vR, 0.f, 0.f, 0.f, 0.f, 0};
+    float cnt = 0.f, vsum = 0.f;
+    const size_t BN = (size_t)P.B * A.N;
+    for (int t = 0; t < (int)P.T; t++) {
+        if (t % (int)P.seg == 0 && on) {
+            float *ck = A.b.ck + (size_t)(t / P.seg) * 6 * BN + bn;
+            ck[0] = s.v; ck[BN] = s.gE; ck[2 * BN] = s.hE; ck[3 * BN] = s.gI; ck[4 * BN] = s.hI;
+            ck[5 * BN] = (float)s.ref;
+        }
+        bool spk = false, refr = false;
+        float gE1 = 0.f, hE1 = 0.f, gI1 = 0.f, hI1 = 0.f, vnext = 0.f;
+        if (on) vnext = adj_neuron_step(P, s, I0, isE, spk, refr, gE1, hE1, gI1, hI1);
+        const unsigned bal = __ballot_sync(0xffffffffu, on && spk);
+        __syncthreads();   // the previous step's readers of ball[] are done
+        if ((local & 31) == 0) ball[local >> 5] = bal;
+        __syncthreads();
+        if (on) {
+            adj_inputs(A, b, t, n, local, hE1, hI1, ball);
+            s.v = vnext;
+            s.gE = gE1; s.hE = hE1; s.gI = gI1; s.hI = hI1;
+            cnt += spk ? 1.f : 0.f;
+            vsum += vnext;
+            if ((t + 1) % (int)P.win == 0) {
+                const size_t o = ((size_t)b * A.nWin + t / P.win) * A.N + n;
+                A.b.rates[o] = cnt / ((float)P.win * P.dt * 1e-3f);
+                A.b.vbar[o] = vsum / (float)P.win;
+                cnt = 0.f;
+                vsum = 0.f;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void block_add_double(double v, double *out, double *red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = threadIdx.x < (blockDim.x + 31) / 32 ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) atomicAdd(out, v);
+    }
+}
+
+__global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A) {
+    __shared__ unsigned ball[32];
+    __shared__ float lam[1024];
+    __shared__ float dS[1024];
+    __shared__ double red[32];
+    const pv1_adj_problem &P = A.p;
+    const int blk = blockIdx.x, b = blockIdx.y;
+    const int local = threadIdx.x;
+    const int bs = (int)P.blockSize;
+    const bool on = local < bs;
+    const int n = blk * bs + (on ? local : 0);
+    const size_t bn = (size_t)b * A.N + n;
+    const bool isE = local < (int)P.nE;
+    const float I0 = on ? A.b.I0[n] : 0.f;
+    const size_t BN = (size_t)P.B * A.N;
+    float *scr = A.b.scratch + (size_t)(b * gridDim.x + blk) * P.seg * 6 * bs;
+    const float *C = A.b.Crec + (size_t)blk * A.nI * bs;
+    const float rateScale = 1.f / ((float)P.win * P.dt * 1e-3f);
+    const float invWin = 1.f / (float)P.win;
+    const int warp = local >> 5, lane = local & 31, nWarp = (bs + 31) / 32;
+    // adjoints of the state after the current step
+    float lv = 0.f, lgE = 0.f, lhE = 0.f, lgI = 0.f, lhI = 0.f;
+    float dEdE = 0.f, dErE = 0.f, ddodE = 0.f, dEdI = 0.f, dErI = 0.f, ddodI = 0.f;
+    for (int sg = A.nSeg - 1; sg >= 0; sg--) {
+        const int t0 = sg * (int)P.seg;
+        const int t1 = min((int)P.T, t0 + (int)P.seg);
+        // recompute the segment forward from its checkpoint
+        AState s{};
+        if (on) {
+            const float *ck = A.b.ck + (size_t)sg * 6 * BN + bn;
+            s = AState{ck[0], ck[BN], ck[2 * BN], ck[3 * BN], ck[4 * BN], (int)ck[5 * BN]};
+        }
+        for (int t = t0; t < t1; t++) {
+            bool spk = false, refr = false;
+            float gE1 = 0.f, hE1 = 0.f, gI1 = 0.f, hI1 = 0.f, vnext = 0.f;
+            if (on) {
+                float *o = scr + (size_t)(t - t0) * 6 * bs + local;
+                o[0] = s.v; o[bs] = s.gE; o[2 * bs] = s.hE; o[3 * bs] = s.gI; o[4 * bs] = s.hI;
+                vnext = adj_neuron_step(P, s, I0, isE, spk, refr, gE1, hE1, gI1, hI1);
+                o[5 * bs] = (float)((refr ? 1 : 0) | (spk ? 2 : 0));
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, on && spk);
+            __syncthreads();
+            if (lane == 0) ball[warp] = bal;
+            __syncthreads();
+            if (on) {
+                adj_inputs(A, b, t, n, local, hE1, hI1, ball);
+                s.v = vnext;
+                s.gE = gE1; s.hE = hE1; s.gI = gI1; s.hI = hI1;
+            }
+        }
+        // adjoint backwards through the segment
+        for (int t = t1 - 1; t >= t0; t--) {
+            // recurrent term: dS[p] = sum_n C[p][n] * lambda_hI(t+1)[n] for the I neurons p
+            __syncthreads();
+            lam[local] = on ? lhI : 0.f;
+            __syncthreads();
+            for (int p = warp; p < A.nI; p += nWarp) {
+                const float *row = C + (size_t)p * bs;
+                float acc = 0.f;
+                for (int j = lane; j < bs; j += 32) acc += __ldg(row + j) * lam[j];
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+                if (lane == 0) dS[p] = acc;
+            }
+            __syncthreads();
+            if (!on) continue;
+            const int win = t / (int)P.win;
+            const size_t oo = ((size_t)b * A.nWin + win) * A.N + n;
+            float dLds = A.b.gR ? A.b.gR[oo] * rateScale : 0.f;
+            if (!isE) dLds += dS[local - (int)P.nE];
+            float lvn_next = lv + (A.b.gV ? A.b.gV[oo] * invWin : 0.f);   // adjoint of v(t+1)
+            // LGN weight gradients at this step's events
+            const uint8_t *x = A.b.X + ((size_t)b * P.T + t) * P.nLGN;
+            for (int k = 0; k < (int)P.K; k++) {
+                const int id = __ldg(A.b.ids + (size_t)k * A.N + n);
+                const uint8_t c = __ldg(x + id);
+                if (c) atomicAdd(A.b.gW + (size_t)k * A.N + n, lhE * (float)c);
+            }
+            const float *o = scr + (size_t)(t - t0) * 6 * bs + local;
+            const float v = o[0], gE = o[bs], hE = o[2 * bs], gI = o[3 * bs], hI = o[4 * bs];
+            const int fl = (int)o[5 * bs];
+            const bool refr = fl & 1, spk = fl & 2;
+            const float gE1 = gE * P.EdE + hE * P.dodE * (P.EdE - P.ErE);
+            const float gI1 = gI * P.EdI + hI * P.dodI * (P.EdI - P.ErI);
+            float lgE1 = lgE, lgI1 = lgI;
+            const float lhE1 = lhE, lhI1 = lhI;
+            float lvt = 0.f, lgE0 = 0.f, lgI0 = 0.f;
+            if (!refr) {
+                const float k1 = adj_f(v, gE, gI, P.gL, P.vL, P.vE, P.vI, I0);
+                const float v1 = v + P.dt * k1;
+                const float k2 = adj_f(v1, gE1, gI1, P.gL, P.vL, P.vE, P.vI, I0);
+                const float vn = v + (P.dt * 0.5f) * (k1 + k2);
+                const float xs = vn - P.vThres;
+                const float den = 1.f + P.slope * fabsf(xs);
+                const float lvn = (spk ? 0.f : lvn_next) + dLds / (den * den);
+                const float lk2 = lvn * (P.dt * 0.5f);
+                const float a1 = -P.gL - gE1 - gI1;
+                const float lv1 = lk2 * a1;
+                const float lk1 = lvn * (P.dt * 0.5f) + lv1 * P.dt;
+                const float a0 = -P.gL - gE - gI;
+                lvt = lvn + lk1 * a0 + lv1;
+                lgE0 = -lk1 * (v - P.vE);
+                lgI0 = -lk1 * (v - P.vI);
+                lgE1 += -lk2 * (v1 - P.vE);
+                lgI1 += -lk2 * (v1 - P.vI);
+            }
+            dEdE += lgE1 * (gE + hE * P.dodE);
+            ddodE += lgE1 * hE * (P.EdE - P.ErE);
+            dErE += lhE1 * hE - lgE1 * hE * P.dodE;
+            dEdI += lgI1 * (gI + hI * P.dodI);
+            ddodI += lgI1 * hI * (P.EdI - P.ErI);
+            dErI += lhI1 * hI - lgI1 * hI * P.dodI;
+            lgE = lgE1 * P.EdE + lgE0;
+            lhE = lgE1 * P.dodE * (P.EdE - P.ErE) + lhE1 * P.ErE;
+            lgI = lgI1 * P.EdI + lgI0;
+            lhI = lgI1 * P.dodI * (P.EdI - P.ErI) + lhI1 * P.ErI;
+            lv = lvt;
+        }
+    }
+    if (!on) dEdE = dErE = ddodE = dEdI = dErI = ddodI = 0.f;
+    block_add_double(dEdE, A.b.gC + 0, red);
+    block_add_double(dErE, A.b.gC + 1, red);
+    block_add_double(ddodE, A.b.gC + 2, red);
+    block_add_double(dEdI, A.b.gC + 3, red);
+    block_add_double(dErI, A.b.gC + 4, red);
+    block_add_double(ddodI, A.b.gC + 5, red);
+}
+
+int adj_check(const pv1_adj_problem *p, const pv1_adj_buffers *b, AdjArgs *A, bool backward) {
+    if (!p || !b) return PV1_E_ARG;
+    if (p->blockSize < 32 || p->blockSize > 1024 || p->blockSize % 32 || p->nE % 32 || p->nE >= p->blockSize ||
+        p->B < 1 || p->nblock < 1 || p->K < 1 || p->K > kAdjMaxK || p->T < 1 || p->seg < 1 || p->win < 1 ||
+        p->T % p->win || p->nLGN < 1 || !(p->dt > 0)) {
+        g_adjErr = "bad problem sizes (blockSize multiple of 32 up to 1024, nE multiple of 32, K <= 32, "
+                   "T a multiple of win)";
+        return PV1_E_ARG;
+    }
+    if (!b->ids || !b->W || !b->X || !b->Crec || !b->I0 || !b->v0 || !b->ck) {
+        g_adjErr = "missing input buffer";
+        return PV1_E_ARG;
+    }
+    if (!backward && (!b->rates || !b->vbar)) {
+        g_adjErr = "missing output buffer";
+        return PV1_E_ARG;
+    }
+    if (backward && (!b->gW || !b->gC || !b->scratch)) {
+        g_adjErr = "missing gradient or scratch buffer";
+        return PV1_E_ARG;
+    }
+    A->p = *p;
+    A->b = *b;
+    A->N = (int)(p->nblock * p->blockSize);
+    A->nI = (int)(p->blockSize - p->nE);
+    A->nWin = (int)(p->T / p->win);
+    A->nSeg = (int)((p->T + p->seg - 1) / p->seg);
+    return PV1_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *pv1_adj_last_error(void) { return g_adjErr.c_str(); }
+
+uint64_t pv1_adj_checkpoint_floats(const pv1_adj_problem *p) {
+    if (!p) return 0;
+    return (uint64_t)((p->T + p->seg - 1) / p->seg) * 6 * p->B * p->nblock * p->blockSize;
+}
+
+uint64_t pv1_adj_scratch_floats(const pv1_adj_problem *p) {
+    if (!p) return 0;
+    return (uint64_t)p->B * p->nblock * p->seg * 6 * p->blockSize;
+}
+
+int pv1_adj_forward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *stream) {
+    AdjArgs A;
+    int r = adj_check(p, b, &A, false);
+    if (r) return r;
+    adj_forward_kernel<<<dim3(p->nblock, p->B), p->blockSize, 0, (cudaStream_t)stream>>>(A);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        g_adjErr = cudaGetErrorString(e);
+        return PV1_E_CUDA;
+    }
+    return PV1_OK;
+}
+
+int pv1_adj_backward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *stream) {
+    AdjArgs A;
+    int r = adj_check(p, b, &A, true);
+    if (r) return r;
+    adj_backward_kernel<<<dim3(p->nblock, p->B), p->blockSize, 0, (cudaStream_t)stream>>>(A);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        g_adjErr = cudaGetErrorString(e);
+        return PV1_E_CUDA;
+    }
+    return PV1_OK;
+}
+
+}  // extern "C"

@@ -226,6 +226,7 @@ def run_gb300(args):
         del wl, sim
         forms = {"batched": bench_batched(args.batch_trials)}
         forms["batched"]["vs_plain"] = forms["batched"]["value"] / value
+        forms["adjoint"] = bench_adjoint()
         out["forms"] = forms
     if dist:
         dist.barrier()
@@ -260,6 +261,59 @@ def bench_batched(n_trials: int):
                         "contrast U[0.1,1], durations U[250,2000] ms, dt 0.125 ms",
             "neuron_steps": work, "trial_steps": [t.steps for t in trials], "gpu_launches": launches,
             "tuning": tuning, "mean_rate_hz": float(np.mean(rates))}
+
+
+def bench_adjoint(reps: int = 3):
+    """The differentiable form: 4096 neurons x batch 16 x 4000 steps (0.125 ms), 30 LGN weights
+    per neuron, fast-sigmoid surrogate (slope 5/mV), loss = MSE of 20 ms-window rates against a
+    teacher with perturbed weights.  Forward alone vs forward + adjoint (checkpoints every 64
+    steps), device time with CUDA events on torch's stream."""
+    import torch
+    from visual_cortex_gb300.adjoint import make_patch, rate_loss
+    patch, W0 = make_patch(B=16, nblock=4, T=4000, K=30, seed=0)
+    c = patch.cfg
+    rng = np.random.default_rng(1)
+    W = torch.tensor(W0, device="cuda")
+    WT = torch.tensor(np.maximum(W0 * (1 + 0.2 * rng.standard_normal(W0.shape)), 0).astype(np.float32),
+                      device="cuda")
+    tE = torch.tensor(5.0, dtype=torch.float64, device="cuda", requires_grad=True)
+    tI = torch.tensor(7.0, dtype=torch.float64, device="cuda", requires_grad=True)
+    with torch.no_grad():
+        target, _ = patch.forward(WT, tE.detach(), tI.detach())
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+
+    def fwd():
+        with torch.no_grad():
+            return patch.forward(W, tE.detach(), tI.detach())
+
+    def fwd_bwd():
+        Wg = W.clone().requires_grad_(True)
+        r, _ = patch.forward(Wg, tE, tI)
+        loss = rate_loss(r, target)
+        loss.backward()
+        return loss, Wg.grad
+
+    fwd(); fwd_bwd()
+    torch.cuda.synchronize()
+    ev[0].record()
+    for _ in range(reps):
+        rates, _ = fwd()
+    ev[1].record()
+    ev[2].record()
+    for _ in range(reps):
+        loss, g = fwd_bwd()
+    ev[3].record()
+    torch.cuda.synchronize()
+    f_ms = ev[0].elapsed_time(ev[1]) / reps
+    fb_ms = ev[2].elapsed_time(ev[3]) / reps
+    work = c.B * c.N * c.T
+    return {"fwd": {"value": work / (f_ms * 1e-3), "unit": UNIT, "ms": f_ms},
+            "fwd_adjoint": {"value": work / (fb_ms * 1e-3), "unit": UNIT, "ms": fb_ms},
+            "fwd_adjoint_over_fwd_time": fb_ms / f_ms,
+            "workload": "4096 neurons (4x1024) x batch 16 x 4000 steps, 30 LGN weights/neuron, "
+                        "checkpoint every 64 steps, grads wrt W and AMPA/GABA decay",
+            "mean_rate_hz": float(rates.mean()), "loss": float(loss.detach()),
+            "grad_norm_W": float(g.norm()), "grad_tauE": float(tE.grad), "grad_tauI": float(tI.grad)}
 
 
 def cpu_baseline(wl, nsteps: int):

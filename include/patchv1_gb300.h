@@ -318,6 +318,9 @@ typedef struct {
     float dt, vL, vE, vI, vR, vThres, gL, slope;  /* slope of the surrogate, 1/mV */
     uint32_t tRefE, tRefI;                          /* refractory steps */
     float EdE, ErE, dodE, EdI, ErI, dodI;           /* AMPA and GABA kernel constants */
+    uint32_t recGrad;   /* 1: the gradient flows through the recurrent I spikes too; 0: the
+                         * recurrent spike input is held constant in the backward (stop-gradient),
+                         * the usual cure for the exploding recurrent surrogate gradient */
 } pv1_adj_problem;
 
 typedef struct {

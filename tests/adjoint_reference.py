@@ -67,7 +67,7 @@ def unrolled(patch, W, consts):
         x = X[:, t, :].to(f)                               # [B][nLGN]
         for k in range(c.K):
             hE1 = hE1 + W[k] * x[:, ids[k]]
-        sI = s.view(B, c.nblock, bs)[:, :, nE:]              # [B][nblock][nI]
+        sI = (s if c.rec_grad else sd).view(B, c.nblock, bs)[:, :, nE:]   # [B][nblock][nI]
         hI1v = hI1.view(B, c.nblock, bs)
         for p in range(nI):
             hI1v = hI1v + sI[:, :, p:p + 1] * Crec[None, :, p, :]

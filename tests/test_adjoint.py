@@ -12,12 +12,12 @@ pytestmark = pytest.mark.gpu
 
 
 def _patch(B=2, nblock=2, bs=128, nE=96, K=8, nLGN=96, T=320, seed=0, vThres=-50.0, w=0.6,
-           rate=0.01):
+           rate=0.01, rec_grad=True):
     import torch
     from visual_cortex_gb300.adjoint import AdjointConfig, AdjointPatch
     rng = np.random.default_rng(seed)
     cfg = AdjointConfig(B=B, nblock=nblock, blockSize=bs, nE=nE, nLGN=nLGN, K=K, T=T, seg=64, win=160,
-                        vThres=vThres)
+                        vThres=vThres, rec_grad=rec_grad)
     N = cfg.N
     ids = rng.integers(0, nLGN, size=(K, N)).astype(np.int32)
     X = (rng.random((B, T, nLGN)) < rate).astype(np.uint8)
@@ -49,10 +49,11 @@ def test_forward_matches_unrolled_reference(native):
     assert torch.equal(vb, vb2)
 
 
-def test_gradients_match_unrolled_autograd(native):
+@pytest.mark.parametrize("rec_grad", [True, False])
+def test_gradients_match_unrolled_autograd(native, rec_grad):
     import torch
     from adjoint_reference import unrolled
-    patch, W = _patch(seed=1)
+    patch, W = _patch(seed=1, rec_grad=rec_grad)
     target = torch.rand(patch.cfg.B, patch.cfg.T // patch.cfg.win, patch.cfg.N, device="cuda") * 40
     vt = torch.full_like(target, -55.0)
 

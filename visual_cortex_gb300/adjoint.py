@@ -26,7 +26,8 @@ class AdjProblem(C.Structure):
     _fields_ = [(n, _PU) for n in ("B", "nblock", "blockSize", "nE", "nLGN", "K", "T", "seg", "win")] + \
                [(n, _PF) for n in ("dt", "vL", "vE", "vI", "vR", "vThres", "gL", "slope")] + \
                [("tRefE", _PU), ("tRefI", _PU)] + \
-               [(n, _PF) for n in ("EdE", "ErE", "dodE", "EdI", "ErI", "dodI")]
+               [(n, _PF) for n in ("EdE", "ErE", "dodE", "EdI", "ErI", "dodI")] + \
+               [("recGrad", _PU)]
 
 
 class AdjBuffers(C.Structure):
@@ -79,6 +80,10 @@ class AdjointConfig:
     vThres: float = -50.0
     gL: float = 0.05
     slope: float = 5.0
+    # gradient through the recurrent I spikes: exact for the surrogate, but it grows without
+    # bound over long windows in a strongly inhibitory network; False holds the recurrent
+    # spike input constant in the backward (stop-gradient)
+    rec_grad: bool = False
     tRefE: int = 16                # 2 ms
     tRefI: int = 8                 # 1 ms
     tauRE: float = 1.0             # AMPA rise
@@ -157,7 +162,7 @@ class AdjointPatch:
         return AdjProblem(B=c.B, nblock=c.nblock, blockSize=c.blockSize, nE=c.nE, nLGN=c.nLGN, K=c.K, T=c.T,
                           seg=c.seg, win=c.win, dt=c.dt, vL=c.vL, vE=c.vE, vI=c.vI, vR=c.vR, vThres=c.vThres,
                           gL=c.gL, slope=c.slope, tRefE=c.tRefE, tRefI=c.tRefI, EdE=v[0], ErE=v[1],
-                          dodE=v[2], EdI=v[3], ErI=v[4], dodI=v[5])
+                          dodE=v[2], EdI=v[3], ErI=v[4], dodI=v[5], recGrad=int(bool(c.rec_grad)))
 
     def forward(self, W: torch.Tensor, tauE: torch.Tensor, tauI: torch.Tensor):
         """(rates [B][nWin][N] in Hz, vbar [B][nWin][N] in mV), differentiable in W, tauE, tauI."""

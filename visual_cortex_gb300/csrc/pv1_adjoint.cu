@@ -78,33 +78,142 @@ __device__ __forceinline__ float adj_neuron_step(const pv1_adj_problem &P, AStat
 }
 
 // The end-of-step inputs: LGN events into hE (synapse order), spiking I neurons of the block
-// into hI (ascending).  ball[] holds this step's spike ballots of the CTA's warps.
-__device__ __forceinline__ void adj_inputs(const AdjArgs &A, int b, int t, int n, int local, float &hE,
-                                           float &hI, const unsigned *ball) {
+// into hI (ascending).  ball[] holds this step's spike ballots of the CTA's warps; x is the
+// step's row of LGN counts (shared-memory stage or global).  Returns the mask of the synapses
+// that carried an event.
+__device__ __forceinline__ unsigned adj_inputs(const AdjArgs &A, const uint8_t *x, int n, int local,
+                                               float &hE, float &hI, const unsigned *ball) {
     const pv1_adj_problem &P = A.p;
-    const uint8_t *x = A.b.X + ((size_t)b * P.T + t) * P.nLGN;
-    for (int k = 0; k < (int)P.K; k++) {
-        const int id = __ldg(A.b.ids + (size_t)k * A.N + n);
-        const uint8_t c = __ldg(x + id);
-        if (c) hE = hE + __ldg(A.b.W + (size_t)k * A.N + n) * (float)c;
+    unsigned mask = 0u;
+    // LGN synapses in chunks of 8: the id and count loads of a chunk are in flight together;
+    // the additions stay in synapse order
+    for (int k0 = 0; k0 < (int)P.K; k0 += 8) {
+        int id[8];
+        unsigned c[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) id[j] = k0 + j < (int)P.K ? __ldg(A.b.ids + (size_t)(k0 + j) * A.N + n) : 0;
+#pragma unroll
+        // x may be the shared-memory stage: a generic load, not the global-only __ldg
+        for (int j = 0; j < 8; j++) c[j] = k0 + j < (int)P.K ? x[id[j]] : 0u;
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            if (c[j]) {
+                hE = hE + __ldg(A.b.W + (size_t)(k0 + j) * A.N + n) * (float)c[j];
+                mask |= 1u << (k0 + j);
+            }
     }
+    // spiking I neurons of the block, ascending, up to 8 weight loads in flight
     const int blk = n / (int)P.blockSize;
     const float *C = A.b.Crec + (size_t)blk * A.nI * P.blockSize;
     const int nWarp = ((int)P.blockSize + 31) / 32;
-    for (int w = (int)P.nE / 32; w < nWarp; w++) {
-        unsigned bits = ball[w];
-        while (bits) {
-            const int lane = __ffs(bits) - 1;
-            bits &= bits - 1;
-            const int pl = w * 32 + lane;
-            if (pl < (int)P.nE) continue;
-            hI = hI + __ldg(C + (size_t)(pl - (int)P.nE) * P.blockSize + local);
+    int w = (int)P.nE / 32;
+    unsigned bits = w < nWarp ? ball[w] : 0u;
+    while (true) {
+        int pre[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            while (!bits && w < nWarp) {
+                if (++w < nWarp) bits = ball[w];
+            }
+            pre[j] = -1;
+            if (w < nWarp) {
+                const int lane = __ffs(bits) - 1;
+                bits &= bits - 1;
+                pre[j] = w * 32 + lane - (int)P.nE;
+            }
         }
+        if (pre[0] < 0) break;
+        float cv[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) cv[j] = pre[j] >= 0 ? __ldg(C + (size_t)pre[j] * P.blockSize + local) : 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+            if (pre[j] >= 0) hI = hI + cv[j];
+        if (pre[7] < 0) break;
+    }
+    return mask;
+}
+
+// ---- LGN count rows staged into shared memory by the bulk-copy (TMA) engine ----
+// Two buffers of one row (nLGN bytes) each with an mbarrier; the copy of the next row in
+// program order is issued by thread 0 while the CTA works on the current one.  A wait gives
+// up after a bounded number of polls and the step reads the row from global memory instead
+// (same bytes), so a copy that never lands can slow a step but never hang it.
+struct XStage {
+    uint8_t *buf0, *buf1;
+    uint64_t *bar;       // [2]
+    unsigned uses0, uses1;  // copies issued into each buffer (uniform across the CTA)
+    int row0, row1;      // step held by each buffer (-1: none)
+    bool on;
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void xs_init(XStage &s, uint8_t *buf, uint64_t *bar, int nLGN, bool on) {
+    s.buf0 = buf;
+    s.buf1 = buf + nLGN;
+    s.bar = bar;
+    s.uses0 = s.uses1 = 0;
+    s.row0 = s.row1 = -1;
+    s.on = on;
+    if (on && threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar + 1)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+}
+
+// Issue the copy of row t into buffer t & 1.  Call from all threads at a point where every
+// thread is done with the buffer's previous row (after a __syncthreads).
+__device__ __forceinline__ void xs_issue(XStage &s, const uint8_t *row, int t, int nLGN) {
+    if (!s.on) return;
+    const int k = t & 1;
+    if (threadIdx.x == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(s.bar + k)),
+                     "r"(nLGN)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_u32(k ? s.buf1 : s.buf0)),
+            "l"(row), "r"(nLGN), "r"(smem_u32(s.bar + k))
+            : "memory");
+    }
+    if (k) {
+        s.uses1++;
+        s.row1 = t;
+    } else {
+        s.uses0++;
+        s.row0 = t;
     }
 }
 
-__global__ void __launch_bounds__(1024) adj_forward_kernel(AdjArgs A) {
+// Row t: the staged copy once its mbarrier phase completed, else the global row.
+__device__ __forceinline__ const uint8_t *xs_get(XStage &s, const uint8_t *row, int t) {
+    if (!s.on) return row;
+    const int k = t & 1;
+    if ((k ? s.row1 : s.row0) != t) return row;
+    const unsigned parity = ((k ? s.uses1 : s.uses0) - 1) & 1;
+    for (int i = 0; i < (1 << 20); i++) {
+        unsigned ok;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(ok)
+            : "r"(smem_u32(s.bar + k)), "r"(parity)
+            : "memory");
+        if (ok) return k ? s.buf1 : s.buf0;
+        if (i > 32) __nanosleep(64);
+    }
+    return row;
+}
+
+__global__ void __launch_bounds__(1024) adj_forward_kernel(AdjArgs A, int stage) {
     __shared__ unsigned ball[32];
+    __shared__ __align__(8) uint64_t xbar[2];
+    extern __shared__ __align__(16) uint8_t xbuf[];
     const pv1_adj_problem &P = A.p;
     const int blk = blockIdx.x, b = blockIdx.y;
     const int local = threadIdx.x;
@@ -116,6 +225,10 @@ __global__ void __launch_bounds__(1024) adj_forward_kernel(AdjArgs A) {
     AState s{on ? A.b.v0[bn] : P.vR, 0.f, 0.f, 0.f, 0.f, 0};
     float cnt = 0.f, vsum = 0.f;
     const size_t BN = (size_t)P.B * A.N;
+    const uint8_t *Xb = A.b.X + (size_t)b * P.T * P.nLGN;
+    XStage xs;
+    xs_init(xs, xbuf, xbar, (int)P.nLGN, stage != 0);
+    xs_issue(xs, Xb, 0, (int)P.nLGN);
     for (int t = 0; t < (int)P.T; t++) {
         if (t % (int)P.seg == 0 && on) {
             float *ck = A.b.ck + (size_t)(t / P.seg) * 6 * BN + bn;
@@ -126,11 +239,13 @@ __global__ void __launch_bounds__(1024) adj_forward_kernel(AdjArgs A) {
         float gE1 = 0.f, hE1 = 0.f, gI1 = 0.f, hI1 = 0.f, vnext = 0.f;
         if (on) vnext = adj_neuron_step(P, s, I0, isE, spk, refr, gE1, hE1, gI1, hI1);
         const unsigned bal = __ballot_sync(0xffffffffu, on && spk);
-        __syncthreads();   // the previous step's readers of ball[] are done
+        __syncthreads();   // the previous step's readers of ball[] and of its count row are done
         if ((local & 31) == 0) ball[local >> 5] = bal;
         __syncthreads();
+        if (t + 1 < (int)P.T) xs_issue(xs, Xb + (size_t)(t + 1) * P.nLGN, t + 1, (int)P.nLGN);
+        const uint8_t *x = xs_get(xs, Xb + (size_t)t * P.nLGN, t);
         if (on) {
-            adj_inputs(A, b, t, n, local, hE1, hI1, ball);
+            adj_inputs(A, x, n, local, hE1, hI1, ball);
             s.v = vnext;
             s.gE = gE1; s.hE = hE1; s.gI = gI1; s.hI = hI1;
             cnt += spk ? 1.f : 0.f;
@@ -158,11 +273,15 @@ __device__ __forceinline__ void block_add_double(double v, double *out, double *
     }
 }
 
-__global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A) {
+constexpr int kScrWords = 7;   // v, gE, hE, gI, hI, flags, LGN event mask per neuron and step
+
+__global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A, int stage) {
     __shared__ unsigned ball[32];
     __shared__ float lam[1024];
     __shared__ float dS[1024];
     __shared__ double red[32];
+    __shared__ __align__(8) uint64_t xbar[2];
+    extern __shared__ __align__(16) uint8_t xbuf[];
     const pv1_adj_problem &P = A.p;
     const int blk = blockIdx.x, b = blockIdx.y;
     const int local = threadIdx.x;
@@ -173,11 +292,14 @@ __global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A) {
     const bool isE = local < (int)P.nE;
     const float I0 = on ? A.b.I0[n] : 0.f;
     const size_t BN = (size_t)P.B * A.N;
-    float *scr = A.b.scratch + (size_t)(b * gridDim.x + blk) * P.seg * 6 * bs;
+    float *scr = A.b.scratch + (size_t)(b * gridDim.x + blk) * P.seg * kScrWords * bs;
     const float *C = A.b.Crec + (size_t)blk * A.nI * bs;
     const float rateScale = 1.f / ((float)P.win * P.dt * 1e-3f);
     const float invWin = 1.f / (float)P.win;
     const int warp = local >> 5, lane = local & 31, nWarp = (bs + 31) / 32;
+    const uint8_t *Xb = A.b.X + (size_t)b * P.T * P.nLGN;
+    XStage xs;
+    xs_init(xs, xbuf, xbar, (int)P.nLGN, stage != 0);
     // adjoints of the state after the current step
     float lv = 0.f, lgE = 0.f, lhE = 0.f, lgI = 0.f, lhI = 0.f;
     float dEdE = 0.f, dErE = 0.f, ddodE = 0.f, dEdI = 0.f, dErI = 0.f, ddodI = 0.f;
@@ -190,11 +312,13 @@ __global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A) {
             const float *ck = A.b.ck + (size_t)sg * 6 * BN + bn;
             s = AState{ck[0], ck[BN], ck[2 * BN], ck[3 * BN], ck[4 * BN], (int)ck[5 * BN]};
         }
+        __syncthreads();
+        xs_issue(xs, Xb + (size_t)t0 * P.nLGN, t0, (int)P.nLGN);
         for (int t = t0; t < t1; t++) {
             bool spk = false, refr = false;
             float gE1 = 0.f, hE1 = 0.f, gI1 = 0.f, hI1 = 0.f, vnext = 0.f;
+            float *o = scr + (size_t)(t - t0) * kScrWords * bs + local;
             if (on) {
-                float *o = scr + (size_t)(t - t0) * 6 * bs + local;
                 o[0] = s.v; o[bs] = s.gE; o[2 * bs] = s.hE; o[3 * bs] = s.gI; o[4 * bs] = s.hI;
                 vnext = adj_neuron_step(P, s, I0, isE, spk, refr, gE1, hE1, gI1, hI1);
                 o[5 * bs] = (float)((refr ? 1 : 0) | (spk ? 2 : 0));
@@ -203,8 +327,11 @@ __global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A) {
             __syncthreads();
             if (lane == 0) ball[warp] = bal;
             __syncthreads();
+            if (t + 1 < t1) xs_issue(xs, Xb + (size_t)(t + 1) * P.nLGN, t + 1, (int)P.nLGN);
+            const uint8_t *x = xs_get(xs, Xb + (size_t)t * P.nLGN, t);
             if (on) {
-                adj_inputs(A, b, t, n, local, hE1, hI1, ball);
+                const unsigned mask = adj_inputs(A, x, n, local, hE1, hI1, ball);
+                o[6 * bs] = __uint_as_float(mask);
                 s.v = vnext;
                 s.gE = gE1; s.hE = hE1; s.gI = gI1; s.hI = hI1;
             }
@@ -212,33 +339,37 @@ __global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A) {
         // adjoint backwards through the segment
         for (int t = t1 - 1; t >= t0; t--) {
             // recurrent term: dS[p] = sum_n C[p][n] * lambda_hI(t+1)[n] for the I neurons p
-            __syncthreads();
-            lam[local] = on ? lhI : 0.f;
-            __syncthreads();
-            for (int p = warp; p < A.nI; p += nWarp) {
-                const float *row = C + (size_t)p * bs;
-                float acc = 0.f;
-                for (int j = lane; j < bs; j += 32) acc += __ldg(row + j) * lam[j];
-                for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-                if (lane == 0) dS[p] = acc;
+            if (P.recGrad) {
+                __syncthreads();
+                lam[local] = on ? lhI : 0.f;
+                __syncthreads();
+                for (int p = warp; p < A.nI; p += nWarp) {
+                    const float *row = C + (size_t)p * bs;
+                    float acc = 0.f;
+                    for (int j = lane; j < bs; j += 32) acc += __ldg(row + j) * lam[j];
+                    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+                    if (lane == 0) dS[p] = acc;
+                }
+                __syncthreads();
             }
-            __syncthreads();
             if (!on) continue;
+            const float *o = scr + (size_t)(t - t0) * kScrWords * bs + local;
+            const float v = o[0], gE = o[bs], hE = o[2 * bs], gI = o[3 * bs], hI = o[4 * bs];
+            const int fl = (int)o[5 * bs];
+            unsigned mask = __float_as_uint(o[6 * bs]);
             const int win = t / (int)P.win;
             const size_t oo = ((size_t)b * A.nWin + win) * A.N + n;
             float dLds = A.b.gR ? A.b.gR[oo] * rateScale : 0.f;
-            if (!isE) dLds += dS[local - (int)P.nE];
+            if (!isE && P.recGrad) dLds += dS[local - (int)P.nE];
             float lvn_next = lv + (A.b.gV ? A.b.gV[oo] * invWin : 0.f);   // adjoint of v(t+1)
-            // LGN weight gradients at this step's events
-            const uint8_t *x = A.b.X + ((size_t)b * P.T + t) * P.nLGN;
-            for (int k = 0; k < (int)P.K; k++) {
+            // LGN weight gradients at this step's events (the recompute recorded which synapses)
+            while (mask) {
+                const int k = __ffs(mask) - 1;
+                mask &= mask - 1;
                 const int id = __ldg(A.b.ids + (size_t)k * A.N + n);
-                const uint8_t c = __ldg(x + id);
-                if (c) atomicAdd(A.b.gW + (size_t)k * A.N + n, lhE * (float)c);
+                const float c = (float)__ldg(Xb + (size_t)t * P.nLGN + id);
+                atomicAdd(A.b.gW + (size_t)k * A.N + n, lhE * c);
             }
-            const float *o = scr + (size_t)(t - t0) * 6 * bs + local;
-            const float v = o[0], gE = o[bs], hE = o[2 * bs], gI = o[3 * bs], hI = o[4 * bs];
-            const int fl = (int)o[5 * bs];
             const bool refr = fl & 1, spk = fl & 2;
             const float gE1 = gE * P.EdE + hE * P.dodE * (P.EdE - P.ErE);
             const float gI1 = gI * P.EdI + hI * P.dodI * (P.EdI - P.ErI);
@@ -250,8 +381,8 @@ __global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A) {
                 const float v1 = v + P.dt * k1;
                 const float k2 = adj_f(v1, gE1, gI1, P.gL, P.vL, P.vE, P.vI, I0);
                 const float vn = v + (P.dt * 0.5f) * (k1 + k2);
-                const float xs = vn - P.vThres;
-                const float den = 1.f + P.slope * fabsf(xs);
+                const float xsv = vn - P.vThres;
+                const float den = 1.f + P.slope * fabsf(xsv);
                 const float lvn = (spk ? 0.f : lvn_next) + dLds / (den * den);
                 const float lk2 = lvn * (P.dt * 0.5f);
                 const float a1 = -P.gL - gE1 - gI1;
@@ -316,6 +447,10 @@ int adj_check(const pv1_adj_problem *p, const pv1_adj_buffers *b, AdjArgs *A, bo
     return PV1_OK;
 }
 
+// Count rows go through the bulk-copy stage when their size and offsets are multiples of 16
+// bytes and two of them fit the default dynamic shared memory.
+int adj_stage(const pv1_adj_problem *p) { return (p->nLGN % 16 == 0 && 2 * p->nLGN <= 32768) ? 1 : 0; }
+
 }  // namespace
 
 extern "C" {
@@ -329,14 +464,16 @@ uint64_t pv1_adj_checkpoint_floats(const pv1_adj_problem *p) {
 
 uint64_t pv1_adj_scratch_floats(const pv1_adj_problem *p) {
     if (!p) return 0;
-    return (uint64_t)p->B * p->nblock * p->seg * 6 * p->blockSize;
+    return (uint64_t)p->B * p->nblock * p->seg * kScrWords * p->blockSize;
 }
 
 int pv1_adj_forward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *stream) {
     AdjArgs A;
     int r = adj_check(p, b, &A, false);
     if (r) return r;
-    adj_forward_kernel<<<dim3(p->nblock, p->B), p->blockSize, 0, (cudaStream_t)stream>>>(A);
+    const int stage = adj_stage(p);
+    adj_forward_kernel<<<dim3(p->nblock, p->B), p->blockSize, stage ? 2 * p->nLGN : 0, (cudaStream_t)stream>>>(
+        A, stage);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         g_adjErr = cudaGetErrorString(e);
@@ -349,7 +486,9 @@ int pv1_adj_backward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *s
     AdjArgs A;
     int r = adj_check(p, b, &A, true);
     if (r) return r;
-    adj_backward_kernel<<<dim3(p->nblock, p->B), p->blockSize, 0, (cudaStream_t)stream>>>(A);
+    const int stage = adj_stage(p);
+    adj_backward_kernel<<<dim3(p->nblock, p->B), p->blockSize, stage ? 2 * p->nLGN : 0, (cudaStream_t)stream>>>(
+        A, stage);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         g_adjErr = cudaGetErrorString(e);

@@ -88,3 +88,29 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def main(argv=None):
+    """``python -m visual_cortex_gb300.batch``: one batched sweep of the synthetic trials,
+    printing the device time and throughput (used for profiling the batched kernels)."""
+    import argparse
+    from . import synth
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--trials", type=int, default=64)
+    ap.add_argument("--dur-ms", type=float, nargs=2, default=(250.0, 2000.0))
+    ap.add_argument("--no-autotune", action="store_true")
+    a = ap.parse_args(argv)
+    trials = synth.batch_trials(n_trials=a.trials, seed=0, dur_ms=tuple(a.dur_ms))
+    sims = [Simulation(t.wl.spec, t.wl.net, t.wl.lgn, t.wl.stim, t.wl.init, t.wl.seeds) for t in trials]
+    b = Batch(sims, [t.steps for t in trials], autotune=not a.no_autotune)
+    _, ms = b.run()
+    work = sum(t.steps * t.wl.spec.nV1 for t in trials)
+    print(f"{a.trials} trials, {work} neuron-steps in {ms:.2f} ms: {work / (ms * 1e-3):.4g} neuron-steps/s; "
+          f"tuning {b.tuning()}")
+    b.close()
+    for s in sims:
+        s.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -227,6 +227,7 @@ def run_gb300(args):
         forms = {"batched": bench_batched(args.batch_trials)}
         forms["batched"]["vs_plain"] = forms["batched"]["value"] / value
         forms["adjoint"] = bench_adjoint()
+        forms["lgn_bf16"] = bench_lgn_bf16()
         out["forms"] = forms
     if dist:
         dist.barrier()
@@ -314,6 +315,48 @@ def bench_adjoint(reps: int = 3):
                         "checkpoint every 64 steps, grads wrt W and AMPA/GABA decay",
             "mean_rate_hz": float(rates.mean()), "loss": float(loss.detach()),
             "grad_norm_W": float(g.norm()), "grad_tauE": float(tE.grad), "grad_tauI": float(tI.grad)}
+
+
+def bench_lgn_bf16():
+    """LGN convolution at scale: 16384 ON/OFF cells, 31x31-pixel DoG footprints (sigma +-20%),
+    250-tap temporal kernel, 256x256 1/f^2 noise frames at 120 Hz for 2 s (16000 steps).  The
+    temporal contraction as tcgen05 BF16 MMAs (FP32 accumulate) vs the same tiles in FP32 on CUDA
+    cores, each followed by the logistic rate and Poisson spikes; rates against an FP64 oracle
+    on 1024 cells x 250 steps."""
+    from visual_cortex_gb300 import lgn_bf16 as L
+    wl = L.make_workload(seed=0)
+    tc = L.LgnTensorCore(wl, fr_every=64)
+    try:
+        tc.run(tensor_cores=True)
+        tc.run(tensor_cores=False)
+        ms16 = float(np.median([tc.run(tensor_cores=True) for _ in range(3)]))
+        _, _, fr16 = tc.fetch()
+        ms32 = float(np.median([tc.run(tensor_cores=False) for _ in range(3)]))
+        _, _, fr32 = tc.fetch()
+    finally:
+        tc.close()
+    rng = np.random.default_rng(0)
+    cells = np.sort(rng.choice(wl.nCells, 1024, replace=False))
+    steps = np.arange(0, wl.T, 64)
+    ref = L.oracle_rates(wl, cells, steps)
+    work = wl.nCells * wl.T
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    flops = 2.0 * L.TILE_K * wl.T * wl.nCells          # MMA work as issued (K = 64 window)
+    kf = 2.0 * 32 * wl.T * wl.nCells                    # algorithmic: ~32 frames per window
+    out_bytes = 4.0 * wl.T * wl.nCells + 4.0 * len(range(0, wl.T, 64)) * wl.nCells
+    return {"bf16_tensor": {"value": work / (ms16 * 1e-3), "unit": "LGN cell-steps/s", "ms": ms16,
+                            "err_vs_fp64": L.rate_errors(fr16[:, cells], ref),
+                            "tensor_tflops": kf / (ms16 * 1e-3) / 1e12,
+                            "tensor_frac_of_measured_bf16": kf / (ms16 * 1e-3) / 1e12 / bf16_peak,
+                            "mma_tflops_issued": flops / (ms16 * 1e-3) / 1e12,
+                            "hbm_gbs_outputs": out_bytes / (ms16 * 1e-3) / 1e9},
+            "fp32_cuda_cores": {"value": work / (ms32 * 1e-3), "unit": "LGN cell-steps/s", "ms": ms32,
+                                "err_vs_fp64": L.rate_errors(fr32[:, cells], ref)},
+            "speedup_bf16_over_fp32": ms32 / ms16,
+            "workload": "16384 ON/OFF cells, 31x31 px DoG (sigma +-20%), 250 taps, 256x256 1/f^2 noise, "
+                        "120 Hz, 2 s (16000 steps at 0.125 ms)"}
 
 
 def cpu_baseline(wl, nsteps: int):

@@ -346,6 +346,36 @@ int pv1_adj_forward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *st
 int pv1_adj_backward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *stream);
 const char *pv1_adj_last_error(void);
 
+/* ---- LGN stage at scale on BF16 tensor cores -------------------------------------------
+ * Replaces LGN_convol_magno + LGN_nonlinear (src/discrete_input_convol.cu:1342-1730) for cells
+ * that share one temporal kernel, over a whole movie at once: convol[cell][t] =
+ * sum_f S[cell][f] W[t][f] as tcgen05 BF16 MMAs with FP32 accumulation in tensor memory (or the
+ * same tiles on CUDA cores in FP32), followed per step by the logistic rate and the
+ * exact-time Poisson generator.  The spatial stage is computed on the device from the movie:
+ * S[cell][pad + f] = sum over a side x side pixel footprint of SW * clamp(L/meanLum - 1, -1, 1).
+ * W comes as tiles: Wtiles[i][s][k] = weight of frame column f0[i] + k for step 128*i + s
+ * (f0[i] a multiple of 8; columns count frames from -pad). */
+typedef struct {
+    uint32_t nCells, nFrame, height, width, side, nFext, pad, T, frEvery, recordRates;
+    float dt, convolRatio, frRatio, meanLum;
+} pv1_lgn_tc_config;
+typedef struct pv1_lgn_tc pv1_lgn_tc;
+
+int pv1_lgn_tc_create(const pv1_lgn_tc_config *cfg, const float *frames /* [nFrame][height][width] */,
+                      const float *SW /* [nCells][side*side] */, const int32_t *cx, const int32_t *cy,
+                      const float *Wtiles /* [ceil(T/128)][128][64] */, const int32_t *f0,
+                      const float *absk, const float *maxConvol, const float *c50, const float *sharp,
+                      const float *la, const float *lb, pv1_lgn_tc **out);
+/* Runs all T steps from a fresh generator state (curand_init(seed, cell, 0), one uniform
+ * discarded as logRand_init does); tensorCores = 1: BF16 tcgen05 kernel, 0: FP32 CUDA cores.
+ * *ms: device time of the stepping kernel (CUDA events). */
+int pv1_lgn_tc_run(pv1_lgn_tc *p, int tensorCores, uint64_t seed, float *ms);
+/* S [nCells][nFext] (FP32 spatial stage), spike words [T][nCells], rates
+ * [ceil(T/frEvery)][nCells]; any may be null. */
+int pv1_lgn_tc_fetch(pv1_lgn_tc *p, float *S, float *sInfo, float *fr);
+void pv1_lgn_tc_destroy(pv1_lgn_tc *p);
+const char *pv1_lgn_tc_last_error(const pv1_lgn_tc *p);
+
 #ifdef __cplusplus
 }
 #endif

@@ -215,3 +215,29 @@ def make_patch(B: int = 16, nblock: int = 4, T: int = 4000, K: int = 30, seed: i
 def rate_loss(rates: torch.Tensor, target: torch.Tensor) -> torch.Tensor:
     """MSE between the 20 ms-window firing rates and a teacher's."""
     return torch.mean((rates - target) ** 2)
+
+
+def main(argv=None):
+    """``python -m visual_cortex_gb300.adjoint [--batch B] [--steps T]``: forward + adjoint of the
+    synthetic patch, printing device times (used for profiling)."""
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--steps", type=int, default=4000)
+    a = ap.parse_args(argv)
+    patch, W0 = make_patch(B=a.batch, T=a.steps)
+    W = torch.tensor(W0, device="cuda", requires_grad=True)
+    tE = torch.tensor(5.0, dtype=torch.float64, device="cuda", requires_grad=True)
+    tI = torch.tensor(7.0, dtype=torch.float64, device="cuda", requires_grad=True)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record()
+    r, _ = patch.forward(W, tE, tI)
+    ev[1].record()
+    rate_loss(r, torch.zeros_like(r)).backward()
+    ev[2].record()
+    torch.cuda.synchronize()
+    print(f"forward {ev[0].elapsed_time(ev[1]):.2f} ms, backward {ev[1].elapsed_time(ev[2]):.2f} ms")
+
+
+if __name__ == "__main__":
+    main()

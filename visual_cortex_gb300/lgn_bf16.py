@@ -274,3 +274,25 @@ def rate_errors(fr: np.ndarray, ref: np.ndarray) -> dict:
     rel = np.abs(fr.astype(np.float64) - ref) / np.abs(ref)
     return {"max_rel": float(rel.max()), "rms_rel": float(np.sqrt(np.mean(rel ** 2))),
             "mean_rate_hz": float(ref.mean())}
+
+
+def main(argv=None):
+    """``python -m visual_cortex_gb300.lgn_bf16 [--cells N] [--steps T] [--fp32]``: one run of the
+    stage on a synthetic movie, printing the device time (used for profiling)."""
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--cells", type=int, default=16384)
+    ap.add_argument("--steps", type=int, default=16000)
+    ap.add_argument("--fp32", action="store_true")
+    a = ap.parse_args(argv)
+    wl = make_workload(nCells=a.cells, T=a.steps)
+    tc = LgnTensorCore(wl, fr_every=64)
+    try:
+        ms = tc.run(tensor_cores=not a.fp32)
+    finally:
+        tc.close()
+    print(f"{a.cells} cells x {a.steps} steps: {ms:.3f} ms ({'FP32 CUDA cores' if a.fp32 else 'BF16 tcgen05'})")
+
+
+if __name__ == "__main__":
+    main()

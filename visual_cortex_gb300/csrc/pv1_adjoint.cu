@@ -135,17 +135,20 @@ __device__ __forceinline__ unsigned adj_inputs(const AdjArgs &A, const uint8_t *
 }
 
 // ---- LGN count rows staged into shared memory by the bulk-copy (TMA) engine ----
-// Two buffers of one row (nLGN bytes) each with an mbarrier; the copy of the next row in
-// program order is issued by thread 0 while the CTA works on the current one.  A wait gives
+// Three buffers of one row (nLGN bytes) each with an mbarrier; the copy of the row two steps
+// ahead is issued by thread 0 while the CTA works on the current one.  A wait gives
 // up after a bounded number of polls and the step reads the row from global memory instead
 // (same bytes), so a copy that never lands can slow a step but never hang it.
 struct XStage {
-    uint8_t *buf0, *buf1;
-    uint64_t *bar;       // [2]
-    unsigned uses0, uses1;  // copies issued into each buffer (uniform across the CTA)
-    int row0, row1;      // step held by each buffer (-1: none)
+    uint8_t *buf0, *buf1, *buf2;
+    uint64_t *bar;                 // [3]
+    unsigned uses0, uses1, uses2;  // copies issued into each buffer (uniform across the CTA)
+    int row0, row1, row2;          // step held by each buffer (-1: none)
     bool on;
 };
+
+template <class T>
+__device__ __forceinline__ T sel3(int k, T a, T b, T c) { return k == 0 ? a : (k == 1 ? b : c); }
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
     return (unsigned)__cvta_generic_to_shared(p);
@@ -154,23 +157,24 @@ __device__ __forceinline__ unsigned smem_u32(const void *p) {
 __device__ __forceinline__ void xs_init(XStage &s, uint8_t *buf, uint64_t *bar, int nLGN, bool on) {
     s.buf0 = buf;
     s.buf1 = buf + nLGN;
+    s.buf2 = buf + 2 * nLGN;
     s.bar = bar;
-    s.uses0 = s.uses1 = 0;
-    s.row0 = s.row1 = -1;
+    s.uses0 = s.uses1 = s.uses2 = 0;
+    s.row0 = s.row1 = s.row2 = -1;
     s.on = on;
     if (on && threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar + 1)));
+        for (int k = 0; k < 3; k++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar + k)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 }
 
-// Issue the copy of row t into buffer t & 1.  Call from all threads at a point where every
-// thread is done with the buffer's previous row (after a __syncthreads).
+// Issue the copy of row t into buffer t % 3 (two rows ahead of use, so the copy has a whole
+// step to land).  Call from all threads at a point where every thread is done with the
+// buffer's previous row (after a __syncthreads of a later step).
 __device__ __forceinline__ void xs_issue(XStage &s, const uint8_t *row, int t, int nLGN) {
     if (!s.on) return;
-    const int k = t & 1;
+    const int k = t % 3;
     if (threadIdx.x == 0) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(s.bar + k)),
@@ -178,25 +182,28 @@ __device__ __forceinline__ void xs_issue(XStage &s, const uint8_t *row, int t, i
                      : "memory");
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                smem_u32(k ? s.buf1 : s.buf0)),
+                smem_u32(sel3(k, s.buf0, s.buf1, s.buf2))),
             "l"(row), "r"(nLGN), "r"(smem_u32(s.bar + k))
             : "memory");
     }
-    if (k) {
+    if (k == 0) {
+        s.uses0++;
+        s.row0 = t;
+    } else if (k == 1) {
         s.uses1++;
         s.row1 = t;
     } else {
-        s.uses0++;
-        s.row0 = t;
+        s.uses2++;
+        s.row2 = t;
     }
 }
 
 // Row t: the staged copy once its mbarrier phase completed, else the global row.
 __device__ __forceinline__ const uint8_t *xs_get(XStage &s, const uint8_t *row, int t) {
     if (!s.on) return row;
-    const int k = t & 1;
-    if ((k ? s.row1 : s.row0) != t) return row;
-    const unsigned parity = ((k ? s.uses1 : s.uses0) - 1) & 1;
+    const int k = t % 3;
+    if (sel3(k, s.row0, s.row1, s.row2) != t) return row;
+    const unsigned parity = (sel3(k, s.uses0, s.uses1, s.uses2) - 1) & 1;
     for (int i = 0; i < (1 << 20); i++) {
         unsigned ok;
         asm volatile(
@@ -204,15 +211,15 @@ __device__ __forceinline__ const uint8_t *xs_get(XStage &s, const uint8_t *row, 
             : "=r"(ok)
             : "r"(smem_u32(s.bar + k)), "r"(parity)
             : "memory");
-        if (ok) return k ? s.buf1 : s.buf0;
-        if (i > 32) __nanosleep(64);
+        if (ok) return sel3(k, s.buf0, s.buf1, s.buf2);
+        if (i > 8) __nanosleep(256);
     }
     return row;
 }
 
 __global__ void __launch_bounds__(1024) adj_forward_kernel(AdjArgs A, int stage) {
     __shared__ unsigned ball[32];
-    __shared__ __align__(8) uint64_t xbar[2];
+    __shared__ __align__(8) uint64_t xbar[3];
     extern __shared__ __align__(16) uint8_t xbuf[];
     const pv1_adj_problem &P = A.p;
     const int blk = blockIdx.x, b = blockIdx.y;
@@ -229,6 +236,7 @@ __global__ void __launch_bounds__(1024) adj_forward_kernel(AdjArgs A, int stage)
     XStage xs;
     xs_init(xs, xbuf, xbar, (int)P.nLGN, stage != 0);
     xs_issue(xs, Xb, 0, (int)P.nLGN);
+    if (P.T > 1) xs_issue(xs, Xb + P.nLGN, 1, (int)P.nLGN);
     for (int t = 0; t < (int)P.T; t++) {
         if (t % (int)P.seg == 0 && on) {
             float *ck = A.b.ck + (size_t)(t / P.seg) * 6 * BN + bn;
@@ -242,7 +250,7 @@ __global__ void __launch_bounds__(1024) adj_forward_kernel(AdjArgs A, int stage)
         __syncthreads();   // the previous step's readers of ball[] and of its count row are done
         if ((local & 31) == 0) ball[local >> 5] = bal;
         __syncthreads();
-        if (t + 1 < (int)P.T) xs_issue(xs, Xb + (size_t)(t + 1) * P.nLGN, t + 1, (int)P.nLGN);
+        if (t + 2 < (int)P.T) xs_issue(xs, Xb + (size_t)(t + 2) * P.nLGN, t + 2, (int)P.nLGN);
         const uint8_t *x = xs_get(xs, Xb + (size_t)t * P.nLGN, t);
         if (on) {
             adj_inputs(A, x, n, local, hE1, hI1, ball);
@@ -280,7 +288,7 @@ __global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A, int stage
     __shared__ float lam[1024];
     __shared__ float dS[1024];
     __shared__ double red[32];
-    __shared__ __align__(8) uint64_t xbar[2];
+    __shared__ __align__(8) uint64_t xbar[3];
     extern __shared__ __align__(16) uint8_t xbuf[];
     const pv1_adj_problem &P = A.p;
     const int blk = blockIdx.x, b = blockIdx.y;
@@ -314,6 +322,7 @@ __global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A, int stage
         }
         __syncthreads();
         xs_issue(xs, Xb + (size_t)t0 * P.nLGN, t0, (int)P.nLGN);
+        if (t0 + 1 < t1) xs_issue(xs, Xb + (size_t)(t0 + 1) * P.nLGN, t0 + 1, (int)P.nLGN);
         for (int t = t0; t < t1; t++) {
             bool spk = false, refr = false;
             float gE1 = 0.f, hE1 = 0.f, gI1 = 0.f, hI1 = 0.f, vnext = 0.f;
@@ -327,7 +336,7 @@ __global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A, int stage
             __syncthreads();
             if (lane == 0) ball[warp] = bal;
             __syncthreads();
-            if (t + 1 < t1) xs_issue(xs, Xb + (size_t)(t + 1) * P.nLGN, t + 1, (int)P.nLGN);
+            if (t + 2 < t1) xs_issue(xs, Xb + (size_t)(t + 2) * P.nLGN, t + 2, (int)P.nLGN);
             const uint8_t *x = xs_get(xs, Xb + (size_t)t * P.nLGN, t);
             if (on) {
                 const unsigned mask = adj_inputs(A, x, n, local, hE1, hI1, ball);
@@ -449,7 +458,7 @@ int adj_check(const pv1_adj_problem *p, const pv1_adj_buffers *b, AdjArgs *A, bo
 
 // Count rows go through the bulk-copy stage when their size and offsets are multiples of 16
 // bytes and two of them fit the default dynamic shared memory.
-int adj_stage(const pv1_adj_problem *p) { return (p->nLGN % 16 == 0 && 2 * p->nLGN <= 32768) ? 1 : 0; }
+int adj_stage(const pv1_adj_problem *p) { return (p->nLGN % 16 == 0 && 3 * p->nLGN <= 32768) ? 1 : 0; }
 
 }  // namespace
 
@@ -472,7 +481,7 @@ int pv1_adj_forward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *st
     int r = adj_check(p, b, &A, false);
     if (r) return r;
     const int stage = adj_stage(p);
-    adj_forward_kernel<<<dim3(p->nblock, p->B), p->blockSize, stage ? 2 * p->nLGN : 0, (cudaStream_t)stream>>>(
+    adj_forward_kernel<<<dim3(p->nblock, p->B), p->blockSize, stage ? 3 * p->nLGN : 0, (cudaStream_t)stream>>>(
         A, stage);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -487,7 +496,7 @@ int pv1_adj_backward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *s
     int r = adj_check(p, b, &A, true);
     if (r) return r;
     const int stage = adj_stage(p);
-    adj_backward_kernel<<<dim3(p->nblock, p->B), p->blockSize, stage ? 2 * p->nLGN : 0, (cudaStream_t)stream>>>(
+    adj_backward_kernel<<<dim3(p->nblock, p->B), p->blockSize, stage ? 3 * p->nLGN : 0, (cudaStream_t)stream>>>(
         A, stage);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

@@ -162,6 +162,14 @@ int pv1_v1_set_near(pv1_plan *plan, uint32_t nearNeighborBlock, const uint32_t *
 int pv1_v1_set_far(pv1_plan *plan, const uint32_t *nVec, const uint32_t *vecID,
                    const float *conVec, const float *delayVec);
 
+/* Near-neighbour connectivity with distance delays, for plans with noDelay = 0: conMat as for
+ * pv1_v1_set_near and delayMat of the same layout (distances in mm, src/patch.cu:3450-3460,
+ * 3685).  Replaces recal_G_mat (src/coredynamics.cu:2063-2309): every non-zero entry becomes a
+ * delayed event of the same device event lists as the far synapses.  Synaptic failure is not
+ * supported with delays (PV1_E_UNSUPPORTED). */
+int pv1_v1_set_near_delayed(pv1_plan *plan, uint32_t nearNeighborBlock, const uint32_t *nNearNB,
+                            const uint32_t *neighborBlockId, const float *conMat, const float *delayMat);
+
 /* Initial state (host-generated as in src/patch.cu:4405-4560).  Layouts: [nV1] or
  * [ng][nV1]; w may be NULL for iModel 0. */
 int pv1_v1_set_state(pv1_plan *plan, const float *v, const float *w, const float *gFF,

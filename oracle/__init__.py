@@ -62,6 +62,8 @@ def lib():
         L.orc_v1_compute_v.argtypes = [P, FP, FP, FP, C.c_int]
         L.orc_v1_deliver_near.argtypes = [P, FP, C.c_int]
         L.orc_v1_deliver_far.argtypes = [P]
+        L.orc_v1_set_delays.argtypes = [P, FP, C.c_int]
+        L.orc_v1_deliver_near_delayed.argtypes = [P]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_num_threads.restype = C.c_int
         _lib = L
@@ -167,6 +169,16 @@ class V1Oracle:
         self.h = lib().orc_v1_create(C.byref(self.cfg), net.maxLGN, up(k[0]), up(k[1]), fp(k[2]), net.nnb,
                                      up(k[3]), up(k[4]), fp(k[5]), up(k[6]), up(k[7]), fp(k[8]), fp(k[9]),
                                      fp(k[10]))
+        self.delayed = not spec.noDelay
+        if self.delayed:
+            # ring depth of src/patch.cu:3808-3813: the largest connected near distance
+            dm = c(net.delayMat, f32)
+            self._keep.append(dm)
+            conn = np.asarray(net.conMat) != 0
+            maxd = float(dm[conn].max()) if conn.any() else 0.0
+            depth = int(np.ceil(np.float32(np.float32(maxd) / np.float32(spec.speedOfThought)) /
+                                np.float32(spec.dt))) + 1
+            lib().orc_v1_set_delays(self.h, fp(dm), max(depth, 2))
 
     def put(self, name, arr):
         lib().orc_v1_put(self.h, ST[name], fp(np.ascontiguousarray(arr, f32)))
@@ -191,7 +203,10 @@ class V1Oracle:
         nerr = L.orc_v1_compute_v(self.h, fp(np.ascontiguousarray(lgn_sInfo, f32)),
                                   fp(None if noise is None else np.ascontiguousarray(noise, f32)),
                                   fp(None if ff is None else np.ascontiguousarray(ff, f32)), int(cap))
-        L.orc_v1_deliver_near(self.h, fp(None if near is None else np.ascontiguousarray(near, f32)), int(cap))
+        if self.delayed:
+            L.orc_v1_deliver_near_delayed(self.h)
+        else:
+            L.orc_v1_deliver_near(self.h, fp(None if near is None else np.ascontiguousarray(near, f32)), int(cap))
         L.orc_v1_deliver_far(self.h)
         return nerr
 

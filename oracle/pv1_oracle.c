@@ -321,6 +321,10 @@ typedef struct orc_v1 {
     size_t *ringOff;
     uint32_t *depth, *slot;
     int anyFar;
+    /* delayed near delivery (noDelay = 0): the spike-word ring spikeTrain[trainDepth][nV1] */
+    const float *delayMat; /* borrowed, conMat layout */
+    float *spikeRing;
+    int trainDepth, curSlot;
 } orc_v1;
 
 static int otype(const orc_v1 *o, int local) {
@@ -404,6 +408,7 @@ void orc_v1_destroy(orc_v1 *o) {
     free(o->sInfo); free(o->nLGN); free(o->lgnId); free(o->sLGN); free(o->nNearNB);
     free(o->nbId); free(o->nVec); free(o->vecOff); free(o->vecID); free(o->conVec);
     free(o->delayVec); free(o->ring); free(o->ringOff); free(o->depth); free(o->slot);
+    free(o->spikeRing);
     free(o);
 }
 
@@ -684,6 +689,72 @@ int orc_v1_deliver_near(orc_v1 *o, const float *near, int cap) {
     }
     free(og);
     free(oh);
+    return 0;
+}
+
+/* Delayed near delivery (noDelay = 0): the spike-word ring of depth trainDepth
+ * (src/patch.cu:3813) and recal_G_mat (src/coredynamics.cu:2063-2309), without learning, gap
+ * junctions or synaptic failure. */
+int orc_v1_set_delays(orc_v1 *o, const float *delayMat, int trainDepth) {
+    o->delayMat = delayMat;
+    o->trainDepth = trainDepth;
+    o->curSlot = 0;
+    free(o->spikeRing);
+    o->spikeRing = (float *)calloc((size_t)trainDepth * o->nV1, sizeof(float));
+    return 0;
+}
+
+int orc_v1_deliver_near_delayed(orc_v1 *o) {
+    const pv1_v1_config *c = &o->c;
+    const int nV1 = o->nV1, bs = o->bs, depth = o->trainDepth;
+    const float dt = c->dt;
+    /* this step's spike words into the current slot */
+    memcpy(o->spikeRing + (size_t)o->curSlot * nV1, o->sInfo, (size_t)nV1 * sizeof(float));
+#pragma omp parallel for schedule(static)
+    for (int ipost = 0; ipost < nV1; ipost++) {
+        const int b = ipost / bs, local = ipost % bs;
+        const int it = otype(o, local);
+        float lgE[PV1_MAX_NG] = {0, 0}, lhE[PV1_MAX_NG] = {0, 0}, lgI[PV1_MAX_NG] = {0, 0}, lhI[PV1_MAX_NG] = {0, 0};
+        for (uint32_t ib = 0; ib < o->nNearNB[b]; ib++) {
+            const size_t local_bid = (size_t)b * o->nnb + ib;
+            const int bid = (int)o->nbId[local_bid];
+            for (int i = 0; i < bs; i++) {
+                const int ipre = bid * bs + i;
+                const size_t mid = (local_bid * bs + i) * bs + local;
+                const float strength = o->conMat[mid];
+                if (strength == 0) continue;
+                float time2post = o->delayMat[mid] / c->speedOfThought;
+                const unsigned it2post = (unsigned)ceilf(time2post / dt);
+                time2post = it2post * dt - time2post;
+                int j0 = o->curSlot - (int)it2post;
+                if (j0 < 0) j0 += depth;
+                const int isE = i < o->nE;
+                for (int j = 0; j < 2; j++) {
+                    float dtsp = o->spikeRing[(size_t)((j0 + j) % depth) * nV1 + ipre];
+                    if (dtsp >= 1.0f) {
+                        const float nsp = floorf(dtsp);
+                        dtsp = (dtsp - nsp + j) * dt - time2post;
+                        if (dtsp < dt && dtsp >= 0) {
+                            const float f = strength;
+                            if (f > 0) {
+                                dtsp = dt - dtsp;
+                                if (isE) {
+                                    for (uint32_t ig = 0; ig < c->ngE; ig++)
+                                        ocond_input(&o->cE, &lgE[ig], &lhE[ig], nsp * f * c->pE[it * c->ngE + ig], dtsp, (int)ig);
+                                } else {
+                                    for (uint32_t ig = 0; ig < c->ngI; ig++)
+                                        ocond_input(&o->cI, &lgI[ig], &lhI[ig], nsp * f * c->pI[it * c->ngI + ig], dtsp, (int)ig);
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        for (uint32_t ig = 0; ig < c->ngE; ig++) { o->gE[ig * nV1 + ipost] += lgE[ig]; o->hE[ig * nV1 + ipost] += lhE[ig]; }
+        for (uint32_t ig = 0; ig < c->ngI; ig++) { o->gI[ig * nV1 + ipost] += lgI[ig]; o->hI[ig * nV1 + ipost] += lhI[ig]; }
+    }
+    o->curSlot = (o->curSlot + 1) % depth;
     return 0;
 }
 

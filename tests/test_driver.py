@@ -49,8 +49,10 @@ def test_unsupported_keys_fail_loudly(written):
     _, fn = written
     with pytest.raises(cfg.ConfigError, match="learning"):
         driver.build(cfg.load(["-c", fn, "--learning", "1"]))
-    with pytest.raises(cfg.ConfigError, match="noDelay"):
-        driver.build(cfg.load(["-c", fn, "--noDelay", "0", "--noFarDelay", "0"]))
+    with pytest.raises(cfg.ConfigError, match="noFarDelay"):
+        driver.build(cfg.load(["-c", fn, "--noDelay", "0", "--noFarDelay", "1"]))
+    m = driver.build(cfg.load(["-c", fn, "--noDelay", "0", "--noFarDelay", "0"]))
+    assert m.spec.noDelay == 0 and m.net.delayMat is not None
 
 
 @pytest.mark.gpu

@@ -142,6 +142,41 @@ def test_far_delivery_parity(native):
         assert cmp[f"max_rel_{k}"] < 1e-5, cmp
 
 
+def test_delayed_near_delivery_parity(native):
+    """noDelay = 0: recal_G_mat's distance-delayed near delivery (spike-word ring, two slots
+    per synapse) vs the GPU's delayed-event ring, with far delivery alongside."""
+    from visual_cortex_gb300 import synth
+    from oracle.parity import run_parity, compare
+    wl = synth.make_workload("delayed", seed=6, nblock=2, n_lgn=512, m=20, width=64, height=64,
+                             nt=800, far_partners=50, adex_inh=True, nFrame=60, noDelay=0)
+    assert wl.spec.noDelay == 0 and wl.net.delayMat is not None
+    res = run_parity(wl, RASTER_STEPS, cap=8)
+    cmp = compare(res, wl.spec)
+    assert cmp["v1_spikes_gpu"] > 0, cmp
+    assert_raster_ok(cmp)
+    for k in ("v", "gE", "gI"):
+        assert cmp[f"max_rel_{k}"] < 1e-5, cmp
+
+
+def test_delayed_persistent_equals_per_step(native):
+    from visual_cortex_gb300 import synth
+    from visual_cortex_gb300.model import Simulation
+    wl = synth.make_workload("delayed", seed=8, nblock=2, n_lgn=512, m=20, width=64, height=64,
+                             nt=800, far_partners=50, adex_inh=True, nFrame=60, noDelay=0)
+    a = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    b = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        assert a.persistent(1)
+        assert not b.persistent(0)
+        a.run(300)
+        b.run(300)
+        for k in ("v", "w", "gE", "hE", "gI", "hI", "gFF", "tBack"):
+            np.testing.assert_array_equal(a.state(k), b.state(k), err_msg=k)
+    finally:
+        a.close()
+        b.close()
+
+
 def test_persistent_equals_per_step_launches(native):
     """The cooperative persistent kernel (state in registers, grid barrier between steps)
     and one launch per step produce bit-identical states, far delivery included."""

@@ -98,6 +98,7 @@ def _load() -> C.CDLL:
         "pv1_v1_set_lgn_synapses": ([P, C.c_uint32, _UP, _UP, _FP], C.c_int),
         "pv1_v1_set_near": ([P, C.c_uint32, _UP, _UP, _FP], C.c_int),
         "pv1_v1_set_far": ([P, _UP, _UP, _FP, _FP], C.c_int),
+        "pv1_v1_set_near_delayed": ([P, C.c_uint32, _UP, _UP, _FP, _FP], C.c_int),
         "pv1_v1_set_state": ([P, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP], C.c_int),
         "pv1_v1_init_rng": ([P, C.c_uint64, C.c_uint32], C.c_int),
         "pv1_host_init_state": ([C.POINTER(V1Config), C.c_uint64, _FP, _UP, C.c_int, C.c_float,

@@ -176,6 +176,10 @@ struct V1Params {
     int4 *farList;             // [3][nV1] step t%3's far spikers: (pre, first synapse, count, sInfo bits)
     int *farCount;             // [3] length of each list
     unsigned *spikeCount;      // [nV1] spikes per neuron since the counters were cleared (may be null)
+    int noDelay;               // 1: near delivery from this step's spikes (conMat); 0: delayed events
+    int nearOn;                // near-class (delayed) events exist: nearAcc is used
+    int farClass;              // far-class events exist: farAcc is used
+    unsigned long long *nearAcc;  // [farDepth][ngE+ngI][2][nV1] fixed-point g,h of near-class events
     // records
     float *rec; long long recStride; int recSlots; int hWrite;
     float *recSpk;             // [recSlots][nV1] spike words (PV1_REC_SPIKES)

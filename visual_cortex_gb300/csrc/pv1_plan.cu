@@ -15,6 +15,13 @@
 
 using namespace pv1;
 
+// One delayed synapse: pre, post, strength, distance (mm), class (1: near block, 0: far).
+struct EvSyn {
+    int pre, post;
+    float str, dist;
+    unsigned char near;
+};
+
 struct pv1_plan {
     pv1_v1_config cfg{};
     std::string err;
@@ -58,6 +65,8 @@ struct pv1_plan {
     long long nFarSyn = 0;
     void *flushBuf = nullptr;
     uint64_t flushSize = 0;
+    // delayed synapses (host copies, kept while the near and far lists are merged)
+    std::vector<EvSyn> farSyn, nearSyn;
 };
 
 namespace {
@@ -260,9 +269,13 @@ int pv1_plan_create(const pv1_v1_config *cfg, pv1_plan **out) {
         delete p;
         return PV1_E_CUDA;
     }
-    if (c.noDelay != 1) {
+    if (c.noDelay != 0 && c.noDelay != 1) {
         *out = p;
-        return fail(p, PV1_E_UNSUPPORTED, "noDelay=0 (distance-delayed near delivery) is not built");
+        return fail(p, PV1_E_ARG, "noDelay must be 0 or 1");
+    }
+    if (c.noDelay == 0 && c.noFarDelay) {
+        *out = p;
+        return fail(p, PV1_E_ARG, "noFarDelay = 1 requires noDelay = 1");
     }
     p->nV1 = (int)(c.nblock * c.blockSize);
     p->nE = (int)c.typeAcc[c.nTypeE - 1];
@@ -320,6 +333,7 @@ int pv1_plan_create(const pv1_v1_config *cfg, pv1_plan **out) {
     v.tau_noise = c.tau_noise;
     v.noiseOnTonic = c.noiseOnTonic;
     v.iModel = c.iModel;
+    v.noDelay = c.noDelay;
     v.hWrite = c.hWrite;
     int r = 0;
     r |= dev_alloc(p, &p->d_err, 1);
@@ -688,40 +702,38 @@ int pv1_v1_set_near(pv1_plan *p, uint32_t nnb, const uint32_t *nNearNB, const ui
     return PV1_OK;
 }
 
-int pv1_v1_set_far(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, const float *conVec,
-                   const float *delayVec) {
-    if (!p || !nVec) return PV1_E_ARG;
+}  // extern "C"
+
+namespace {
+
+// Builds the outgoing event lists by pre-neuron from delayed synapses (far ones, and the
+// near ones when noDelay = 0) and uploads them: post id, strength, whole-step delay, sub-step
+// offset, post type and class (near/far) per synapse.  Within a list the synapses with a
+// whole-step delay <= 1 come first, because their events can arrive within the spike's own
+// step.  The delay arithmetic is recal_G_vec's / recal_G_mat's (src/coredynamics.cu:282-287,
+// 2163-2166), in float.
+int build_event_lists(pv1_plan *p, const std::vector<EvSyn> &syn) {
     const int nV1 = p->nV1;
     const pv1_v1_config &c = p->cfg;
-    size_t nnz = 0;
-    for (int i = 0; i < nV1; i++) nnz += nVec[i];
-    if (nnz && (!vecID || !conVec || !delayVec)) return PV1_E_ARG;
-    p->nFarSyn = (long long)nnz;
-    if (nnz == 0 || c.noFarDelay) {
-        // no far synapses, or the reference's noFarDelay=1 path, which drops far input
-        p->vp.farOn = 0;
+    const size_t nnz = syn.size();
+    V1Params &v = p->vp;
+    if (nnz == 0) {
+        v.farOn = 0;
+        v.nearOn = 0;
+        v.farClass = 0;
         drop_graph(p);
         return PV1_OK;
     }
-    for (int q = 0; q < (int)(c.nType * c.nType); q++)
-        if (c.synFail[q] > 0)
-            return fail(p, PV1_E_UNSUPPORTED,
-                        "synaptic failure on delayed far synapses (host std::normal_distribution per post) is not built");
-    // outgoing lists by pre (stable counting sort keeps the post/j order within a pre);
-    // within a list the synapses with a whole-step delay <= 1 come first, because their
-    // events can arrive within the spike's own step
     std::vector<int> off(nV1 + 1, 0), n1(nV1, 0);
     std::vector<unsigned> it2(nnz);
     std::vector<float> t2p(nnz);
     for (size_t e = 0; e < nnz; e++) {
-        if (vecID[e] >= (uint32_t)nV1) return fail(p, PV1_E_ARG, "far pre id out of range");
-        off[vecID[e] + 1]++;
-        // delay arithmetic of recal_G_vec (src/coredynamics.cu:282-287), in float
-        float time2post = delayVec[e] / c.speedOfThought;
+        off[syn[e].pre + 1]++;
+        float time2post = syn[e].dist / c.speedOfThought;
         const unsigned it2post = (unsigned)std::ceil(time2post / c.dt);
         it2[e] = it2post;
         t2p[e] = it2post * c.dt - time2post;
-        if (it2post <= 1) n1[vecID[e]]++;
+        if (it2post <= 1) n1[syn[e].pre]++;
     }
     for (int i = 0; i < nV1; i++) off[i + 1] += off[i];
     std::vector<int> fillShort(off.begin(), off.end() - 1), fill(nV1);
@@ -730,32 +742,32 @@ int pv1_v1_set_far(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, con
     std::vector<float> str(nnz), frac(nnz);
     std::vector<unsigned char> isPre(nV1, 0);
     int maxSteps = 0;
-    size_t e = 0;
-    for (int i = 0; i < nV1; i++) {
-        for (uint32_t j = 0; j < nVec[i]; j++, e++) {
-            const int pre = (int)vecID[e];
-            const unsigned it2post = it2[e];
-            const float time2post = t2p[e];
-            const int slot = it2post <= 1 ? fillShort[pre]++ : fill[pre]++;
-            post[slot] = i;
-            str[slot] = conVec[e];
-            if (it2post > 0xffff) return fail(p, PV1_E_UNSUPPORTED, "far delay longer than 65535 steps");
-            // whole-step delay in the low 16 bits, the post neuron's type above
-            int ptype = (int)c.nType - 1;
-            for (int jt = (int)c.nType - 1; jt >= 0; jt--)
-                if ((uint32_t)(i % (int)c.blockSize) < c.typeAcc[jt]) ptype = jt;
-            steps[slot] = (int)it2post | (ptype << 16);
-            frac[slot] = time2post;
-            isPre[pre] = 1;
-            maxSteps = std::max(maxSteps, (int)it2post);
-        }
+    bool anyFar = false, anyNear = false;
+    for (size_t e = 0; e < nnz; e++) {
+        const int pre = syn[e].pre, i = syn[e].post;
+        const unsigned it2post = it2[e];
+        const int slot = it2post <= 1 ? fillShort[pre]++ : fill[pre]++;
+        post[slot] = i;
+        str[slot] = syn[e].str;
+        if (it2post > 0xffff) return fail(p, PV1_E_UNSUPPORTED, "synaptic delay longer than 65535 steps");
+        // whole-step delay in the low 16 bits, the post neuron's type above, the class at bit 24
+        int ptype = (int)c.nType - 1;
+        for (int jt = (int)c.nType - 1; jt >= 0; jt--)
+            if ((uint32_t)(i % (int)c.blockSize) < c.typeAcc[jt]) ptype = jt;
+        steps[slot] = (int)it2post | (ptype << 16) | (syn[e].near ? (1 << 24) : 0);
+        frac[slot] = t2p[e];
+        if (!syn[e].near) isPre[pre] = 1;
+        anyFar |= !syn[e].near;
+        anyNear |= syn[e].near != 0;
+        maxSteps = std::max(maxSteps, (int)it2post);
     }
     int *d_off, *d_post, *d_steps, *d_n1, *d_count;
     float *d_str, *d_frac;
     unsigned char *d_pre;
-    unsigned long long *d_acc;
+    unsigned long long *d_acc, *d_nacc = nullptr;
     int4 *d_list;
     const int depth = maxSteps + 2;
+    const size_t ringLen = (size_t)depth * (c.ngE + c.ngI) * 2 * nV1;
     int r = 0;
     r |= dev_upload(p, &d_off, off.data(), off.size());
     r |= dev_upload(p, &d_n1, n1.data(), n1.size());
@@ -766,10 +778,12 @@ int pv1_v1_set_far(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, con
     r |= dev_upload(p, &d_str, str.data(), nnz);
     r |= dev_upload(p, &d_frac, frac.data(), nnz);
     r |= dev_upload(p, &d_pre, isPre.data(), nV1);
-    r |= dev_alloc(p, &d_acc, (size_t)depth * (c.ngE + c.ngI) * 2 * nV1);
+    r |= dev_alloc(p, &d_acc, ringLen);
+    if (anyNear) r |= dev_alloc(p, &d_nacc, ringLen);
     if (r) return r;
-    V1Params &v = p->vp;
     v.farOn = 1;
+    v.farClass = anyFar ? 1 : 0;
+    v.nearOn = anyNear ? 1 : 0;
     v.farOff = d_off;
     v.farPost = d_post;
     v.farSteps = d_steps;
@@ -777,6 +791,7 @@ int pv1_v1_set_far(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, con
     v.farFrac = d_frac;
     v.farPre = d_pre;
     v.farAcc = d_acc;
+    v.nearAcc = d_nacc;
     v.farDepth = depth;
     v.farN1 = d_n1;
     v.farList = d_list;
@@ -784,6 +799,81 @@ int pv1_v1_set_far(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, con
     PV1_CUDA(p, cudaStreamSynchronize(p->stream));
     drop_graph(p);
     return PV1_OK;
+}
+
+int rebuild_events(pv1_plan *p) {
+    std::vector<EvSyn> all;
+    all.reserve(p->farSyn.size() + p->nearSyn.size());
+    all.insert(all.end(), p->farSyn.begin(), p->farSyn.end());
+    all.insert(all.end(), p->nearSyn.begin(), p->nearSyn.end());
+    return build_event_lists(p, all);
+}
+
+}  // namespace
+
+extern "C" {
+
+int pv1_v1_set_far(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, const float *conVec,
+                   const float *delayVec) {
+    if (!p || !nVec) return PV1_E_ARG;
+    const int nV1 = p->nV1;
+    const pv1_v1_config &c = p->cfg;
+    size_t nnz = 0;
+    for (int i = 0; i < nV1; i++) nnz += nVec[i];
+    if (nnz && (!vecID || !conVec || !delayVec)) return PV1_E_ARG;
+    p->nFarSyn = (long long)nnz;
+    p->farSyn.clear();
+    if (nnz && !c.noFarDelay) {
+        // (noFarDelay = 1 is the reference's path that drops far input)
+        for (int q = 0; q < (int)(c.nType * c.nType); q++)
+            if (c.synFail[q] > 0)
+                return fail(p, PV1_E_UNSUPPORTED,
+                            "synaptic failure on delayed synapses (host std::normal_distribution per post) is not built");
+        p->farSyn.resize(nnz);
+        size_t e = 0;
+        for (int i = 0; i < nV1; i++)
+            for (uint32_t j = 0; j < nVec[i]; j++, e++) {
+                if (vecID[e] >= (uint32_t)nV1) return fail(p, PV1_E_ARG, "far pre id out of range");
+                p->farSyn[e] = EvSyn{(int)vecID[e], i, conVec[e], delayVec[e], 0};
+            }
+    }
+    int r = rebuild_events(p);
+    if (c.noDelay) p->farSyn.clear();   // kept only while near lists may still be merged in
+    return r;
+}
+
+// Near connectivity with distance delays (noDelay = 0): recal_G_mat
+// (src/coredynamics.cu:2063-2309) delivers every non-zero conMat entry of the near blocks at
+// the arrival step of its delayMat distance.  Here those entries become delayed events of the
+// same event lists as the far synapses (class "near": no far-spike gate on delivery).
+int pv1_v1_set_near_delayed(pv1_plan *p, uint32_t nnb, const uint32_t *nNearNB, const uint32_t *nbId,
+                            const float *conMat, const float *delayMat) {
+    if (!p || !nNearNB || !nbId || !conMat || !delayMat || nnb < 1) return PV1_E_ARG;
+    const pv1_v1_config &c = p->cfg;
+    if (c.noDelay) return fail(p, PV1_E_STATE, "pv1_v1_set_near_delayed is for noDelay = 0 plans");
+    for (int q = 0; q < (int)(c.nType * c.nType); q++)
+        if (c.synFail[q] > 0)
+            return fail(p, PV1_E_UNSUPPORTED,
+                        "synaptic failure with distance-delayed near delivery is not built");
+    const int nblock = (int)c.nblock;
+    const size_t bs = c.blockSize;
+    p->nearSyn.clear();
+    for (int b = 0; b < nblock; b++) {
+        if (nNearNB[b] > nnb) return fail(p, PV1_E_ARG, "nNearNeighborBlock > nearNeighborBlock");
+        for (uint32_t k = 0; k < nNearNB[b]; k++) {
+            const uint32_t nb = nbId[(size_t)b * nnb + k];
+            if (nb >= (uint32_t)nblock) return fail(p, PV1_E_ARG, "neighbour block id out of range");
+            const size_t base = ((size_t)b * nnb + k) * bs * bs;
+            for (size_t i = 0; i < bs; i++)
+                for (size_t j = 0; j < bs; j++) {
+                    const float s = conMat[base + i * bs + j];
+                    if (s != 0)
+                        p->nearSyn.push_back(EvSyn{(int)(nb * bs + i), (int)(b * bs + j), s, delayMat[base + i * bs + j], 1});
+                }
+        }
+    }
+    p->haveNear = true;
+    return rebuild_events(p);
 }
 
 int pv1_v1_set_state(pv1_plan *p, const float *v, const float *w, const float *gFF,

@@ -210,7 +210,7 @@ __device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, in
     unsigned long long farG[2 * kMaxNG], farH[2 * kMaxNG];
     unsigned long long *acc = nullptr;
     bool farSpiked = false;
-    if (P.farOn && active) {
+    if (P.farClass && active) {
         acc = P.farAcc + (size_t)(tp % P.farDepth) * ns * 2 * nV1;
         farSpiked = __ldcg(P.farFlag + tp % 3) != 0;
 #pragma unroll
@@ -219,7 +219,32 @@ __device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, in
             farH[q] = q < ns ? __ldcg(acc + (size_t)(2 * q + 1) * nV1 + i) : 0ull;
         }
     }
-    const int nnb = P.nNearNB[b];
+    // delayed near events (noDelay = 0): recal_G_mat sums them into the same step's
+    // conductance update; here they were pushed into their own ring
+    if (!P.noDelay) {
+        if (P.nearOn && active) {
+            unsigned long long *nacc = P.nearAcc + (size_t)(tp % P.farDepth) * ns * 2 * nV1;
+#pragma unroll
+            for (int q = 0; q < 2 * kMaxNG; q++) {
+                if (q < ns) {
+                    unsigned long long *pg = nacc + (size_t)(2 * q) * nV1 + i;
+                    unsigned long long *ph = nacc + (size_t)(2 * q + 1) * nV1 + i;
+                    const unsigned long long ug = __ldcg(pg), uh = __ldcg(ph);
+                    if (ug | uh) {
+                        *pg = 0ull;
+                        *ph = 0ull;
+                        const float fg = far_from_fixed(ug), fh = far_from_fixed(uh);
+#pragma unroll
+                        for (int ig = 0; ig < kMaxNG; ig++) {
+                            if (q < ngE && ig == q) { lgE[ig] = fg; lhE[ig] = fh; }
+                            if (q >= ngE && ig == q - ngE) { lgI[ig] = fg; lhI[ig] = fh; }
+                        }
+                    }
+                }
+            }
+        }
+    }
+    const int nnb = P.noDelay ? P.nNearNB[b] : 0;
     float *recNear = nullptr;
     int nNearDraw = 0;
     if (Rng && P.recNear && active) {
@@ -625,11 +650,15 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
     return sInfo;
 }
 
-// One far event: the spike of `pre` at step t (spike word sI) through far synapse e, in its
-// k-th arrival slot; arrival step and offset as recal_G_vec computes them
-// (src/coredynamics.cu:282-333), with explicitly rounded operations as on the reference's host.
+// One delayed event: the spike of `pre` at step t (spike word sI) through delayed synapse e,
+// in its k-th arrival slot; arrival step and offset as recal_G_vec (src/coredynamics.cu:282-333)
+// and recal_G_mat (2163-2200) compute them, with explicitly rounded operations.  `code` is the
+// synapse's packed word: post type in bits 16-23, class in bit 24 (1: near block, delivered
+// through nearAcc; 0: far, through farAcc).
 __device__ __forceinline__ void far_event(const V1Params &P, long long t, int pre, float sI, int post,
-                                          float f, int steps, int ptype, float frac, int kk) {
+                                          float f, int steps, int code, float frac, int kk) {
+    const int ptype = (code >> 16) & 0xff;
+    const bool nearClass = (code >> 24) & 1;
     const float dt = P.dt;
     const unsigned nsp = (unsigned)floorf(sI);
     // dtsp = (sInfo - nsp + k)*dt - time2post, rounded step by step
@@ -647,7 +676,7 @@ __device__ __forceinline__ void far_event(const V1Params &P, long long t, int pr
     const int ng = preE ? P.ngE : P.ngI;
     const int qoff = preE ? 0 : P.ngE;
     const float delta = __fsub_rn(dt, dtsp);
-    unsigned long long *acc = P.farAcc + (size_t)(tArr % P.farDepth) * ns * 2 * nV1;
+    unsigned long long *acc = (nearClass ? P.nearAcc : P.farAcc) + (size_t)(tArr % P.farDepth) * ns * 2 * nV1;
 #pragma unroll
     for (int ig = 0; ig < kMaxNG; ig++) {
         if (ig < ng) {
@@ -731,12 +760,12 @@ __device__ __forceinline__ void far_push_list(const V1Params &P, long long tl, S
             const float f = __ldg(P.farStr + e);
             const int sp = __ldg(P.farSteps + e);
             const float frac = __ldg(P.farFrac + e);
-            const int steps = sp & 0xffff, ptype = (sp >> 16) & 0xff;
+            const int steps = sp & 0xffff;
             const int pre = sm.fpre[r];
             const float sI = sm.fsi[r];
             // the slot arriving in step tl itself (steps == k) was pushed in step tl
-            if (steps != 0) far_event(P, tl, pre, sI, post, f, steps, ptype, frac, 0);
-            if (steps != 1) far_event(P, tl, pre, sI, post, f, steps, ptype, frac, 1);
+            if (steps != 0) far_event(P, tl, pre, sI, post, f, steps, sp, frac, 0);
+            if (steps != 1) far_event(P, tl, pre, sI, post, f, steps, sp, frac, 1);
         }
         W0 = (int)(((long long)W0 + work) % G);
     }
@@ -799,7 +828,7 @@ __device__ __forceinline__ void far_phase(const V1Params &P, long long t, int i,
         const float frac = __ldg(P.farFrac + e);
         const int steps = sp & 0xffff;
         // steps is 0 or 1 here: the slot with tArr == t
-        far_event(P, t, sm.fpre[r], sm.fsi[r], post, f, steps, (sp >> 16) & 0xff, frac, steps);
+        far_event(P, t, sm.fpre[r], sm.fsi[r], post, f, steps, sp, frac, steps);
     }
 }
 

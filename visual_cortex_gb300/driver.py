@@ -142,8 +142,6 @@ def build(c: Config) -> Model:
     gI0 = _exact(c, "gI0", nType * ngI * 4)
     if c.noFarDelay and not c.noDelay:
         raise ConfigError("noFarDelay = 1 requires noDelay = 1")
-    if c.noDelay != 1:
-        raise ConfigError("not supported by this build: noDelay = 0 (delayed near delivery)")
     tonicDep = _per_type(c, "tonicDep", nType)
     noisyDep = _per_type(c, "noisyDep", nType)
     minTonicRatio = _per_type(c, "minTonicRatio", nType, required=False, default=[0.0] * nType)
@@ -229,7 +227,7 @@ def build(c: Config) -> Model:
             iTonic[i] = td
     net = V1Network(nLGNperV1=nL, lgnId=lgnId, sLGN=sLGN, nNearNB=nNear.astype(u32),
                     nbId=nbId, conMat=conMat, nVec=nVec, vecID=vecID, conVec=conVec,
-                    delayVec=delayVec, tonicDep=iTonic)
+                    delayVec=delayVec, tonicDep=iTonic, delayMat=None if c.noDelay else delayMat)
 
     # LGN cells (src/patch.cu:1523-1640, 2505-2530) and the stimulus
     stim_f = FM.read_stimulus(P.stimulus)

@@ -129,6 +129,7 @@ class V1Network:
     conVec: np.ndarray        # f32 [sum nVec] (sRatioV1 applied)
     delayVec: np.ndarray      # f32 [sum nVec] (mm)
     tonicDep: np.ndarray      # f32 [nV1]
+    delayMat: np.ndarray | None = None   # f32 like conMat: distances (mm), used when noDelay = 0
 
     @property
     def maxLGN(self) -> int:
@@ -285,8 +286,15 @@ class Simulation:
         N.check(self.plan, N.lib.pv1_v1_set_lgn_synapses(self.plan, net.maxLGN, N.uptr(n), N.uptr(ids), N.fptr(s)),
                 "pv1_v1_set_lgn_synapses")
         nn, nb, cm = c(net.nNearNB, u32), c(net.nbId, u32), c(net.conMat, f32)
-        N.check(self.plan, N.lib.pv1_v1_set_near(self.plan, net.nnb, N.uptr(nn), N.uptr(nb), N.fptr(cm)),
-                "pv1_v1_set_near")
+        if self.spec.noDelay:
+            N.check(self.plan, N.lib.pv1_v1_set_near(self.plan, net.nnb, N.uptr(nn), N.uptr(nb), N.fptr(cm)),
+                    "pv1_v1_set_near")
+        else:
+            if net.delayMat is None:
+                raise ValueError("noDelay = 0 needs the network's delayMat")
+            dm = c(net.delayMat, f32)
+            N.check(self.plan, N.lib.pv1_v1_set_near_delayed(self.plan, net.nnb, N.uptr(nn), N.uptr(nb),
+                                                             N.fptr(cm), N.fptr(dm)), "pv1_v1_set_near_delayed")
         nv, vid, cv, dv = c(net.nVec, u32), c(net.vecID, u32), c(net.conVec, f32), c(net.delayVec, f32)
         N.check(self.plan, N.lib.pv1_v1_set_far(self.plan, N.uptr(nv), N.uptr(vid), N.fptr(cv), N.fptr(dv)),
                 "pv1_v1_set_far")

@@ -121,6 +121,20 @@ def make_lgn(n_lgn: int, rng: np.random.Generator, patch_deg: float, dt: float,
     return spec, extent
 
 
+def near_distances(spec: V1Spec, pos: np.ndarray, nNearNB, nbId) -> np.ndarray:
+    """delayMat [nblock][nnb][pre][post]: cortical distance (mm) from each neuron of neighbour
+    block k (pre) to each neuron of block b (post), the layout of conMat."""
+    bs, nb = spec.blockSize, spec.nblock
+    out = np.zeros((nb, nbId.shape[1], bs, bs), f32)
+    for b in range(nb):
+        post = pos[b * bs:(b + 1) * bs]
+        for k in range(int(nNearNB[b])):
+            q = int(nbId[b, k])
+            pre = pos[q * bs:(q + 1) * bs]
+            out[b, k] = np.sqrt(((pre[:, None, :] - post[None, :, :]) ** 2).sum(-1)).astype(f32)
+    return out
+
+
 def block_positions(nblock: int, blockSize: int, side_mm: float, rng: np.random.Generator,
                     nbx: int | None = None):
     """Jittered-grid positions, blocks tiled on a sheet; returns pos [nV1][2] in mm."""
@@ -239,8 +253,11 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
                   adex_inh: bool = False, patch_deg: float = 2.0, nFrame: int = 120,
                   wFF: float = 0.2, wE: float = 0.004, wI: float = 0.6, wFar: float = 0.002,
                   noisyDep=(0.0, 0.0), synFail=(0.0, 0.0, 0.0, 0.0), synFailFF=(0.0, 0.0),
-                  mSample1D: int = 16, dt: float = 0.125, tjitter: float = 0.0) -> Workload:
-    """Builds one synthetic patch; C1 = 1x1024 V1 / 512 LGN; C2 = 32 blocks / 16384 LGN."""
+                  mSample1D: int = 16, dt: float = 0.125, tjitter: float = 0.0,
+                  noDelay: int = 1) -> Workload:
+    """Builds one synthetic patch; C1 = 1x1024 V1 / 512 LGN; C2 = 32 blocks / 16384 LGN.
+    noDelay = 0: near synapses are delivered after their distance delay (delayMat from the
+    neuron positions, mm, at speedOfThought 1 mm/ms)."""
     rng = np.random.default_rng(seed)
     spec = make_spec(nblock, adex_inh=adex_inh, noisyDep=noisyDep, synFail=synFail,
                      synFailFF=synFailFF, dt=dt)
@@ -258,10 +275,14 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
     nLGNperV1, lgnId, sLGN, rfc, rfo = lgn_to_v1(spec, lgn, rng, m, wFF, patch_deg)
     tonic = np.where(spec.type_of(np.arange(spec.nV1) % spec.blockSize) == 0,
                      rng.uniform(0.3, 0.6, spec.nV1), rng.uniform(0.4, 0.7, spec.nV1)).astype(f32)
+    nbId = np.arange(nblock, dtype=u32)[:, None].copy()
+    delayMat = near_distances(spec, pos, np.ones(nblock, u32), nbId) if not noDelay else None
+    if not noDelay:
+        spec.noDelay = 0
     net = V1Network(nLGNperV1=nLGNperV1, lgnId=lgnId, sLGN=sLGN,
-                    nNearNB=np.ones(nblock, u32), nbId=np.arange(nblock, dtype=u32)[:, None].copy(),
+                    nNearNB=np.ones(nblock, u32), nbId=nbId,
                     conMat=conMat, nVec=nVec, vecID=vecID, conVec=conVec, delayVec=delayVec,
-                    tonicDep=tonic)
+                    tonicDep=tonic, delayMat=delayMat)
     frames = grating_frames(nFrame, width, height, extent, cpd=4.0, tf_hz=8.0,
                             contrast=contrast, orient=orient, frame_rate=120)
     stim = Stimulus(frames=frames, init_LMS=(0.5, 0.5, 0.5))
@@ -313,12 +334,7 @@ def write_reference_files(wl: Workload, folder: str, seed: int = 0, nt: int | No
                             spec.typeAcc)
     FM.write_v1_allpos(d + "V1_allpos.bin", nb, bs, wl.pos)
     FM.write_mat(d + "V1_conMat.bin", net.nnb, net.conMat)
-    delay = np.zeros_like(net.conMat)
-    for b in range(nb):
-        for k in range(int(net.nNearNB[b])):
-            P = wl.pos[b * bs:(b + 1) * bs]
-            Q = wl.pos[int(net.nbId[b, k]) * bs:(int(net.nbId[b, k]) + 1) * bs]
-            delay[b, k] = np.sqrt(((P[:, None, :] - Q[None, :, :]) ** 2).sum(-1)).astype(f32)
+    delay = net.delayMat if net.delayMat is not None else near_distances(spec, wl.pos, net.nNearNB, net.nbId)
     FM.write_mat(d + "V1_delayMat.bin", net.nnb, delay)
     FM.write_neighbor_block(d + "neighborBlock.bin", net.nNearNB,
                             [net.nbId[b, :int(net.nNearNB[b])] for b in range(nb)])

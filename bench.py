@@ -176,6 +176,7 @@ def run_gb300(args):
 
     # per-kernel device time (direct launches, events around each launch)
     v1_ms, lgn_ms, chunk = sim.time_kernels(320)
+    persistent = sim.persistent()
 
     # end to end through the public API from host buffers
     sim.set_record(N.REC_SPIKES, S + 1)
@@ -195,9 +196,13 @@ def run_gb300(args):
 
     peak, peak_kind = load_peaks()
     bpn = algorithmic_bytes_per_neuron_step(wl, rate_hz)
-    bytes_per_launch = bpn * wl.spec.nV1
-    achieved = bytes_per_launch / (v1_ms * 1e-3) / 1e9
-    traffic = load_traffic("v1_step_kernel")
+    # the dominant kernel: one cooperative launch per chunk of steps, or one launch per step
+    kernel = "v1_persistent_kernel" if persistent else "v1_step_kernel"
+    steps_per_launch = chunk if persistent else 1
+    bytes_per_launch = bpn * wl.spec.nV1 * steps_per_launch
+    launch_ms = v1_ms * steps_per_launch
+    achieved = bytes_per_launch / (launch_ms * 1e-3) / 1e9
+    traffic = load_traffic(kernel)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -215,9 +220,10 @@ def run_gb300(args):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "v1_step_kernel", "peak_source": f"{peak_kind} hbm_gbs",
-                     "algorithmic_bytes_per_launch": bytes_per_launch,
-                     "launch_ms": v1_ms, "lgn_chunk_ms": lgn_ms, "lgn_chunk_steps": chunk},
+                     "kernel": kernel, "peak_source": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes_per_launch": bytes_per_launch, "steps_per_launch": steps_per_launch,
+                     "algorithmic_bytes_per_neuron_step": bpn,
+                     "launch_ms": launch_ms, "lgn_chunk_ms": lgn_ms, "lgn_chunk_steps": chunk},
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

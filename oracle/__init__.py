@@ -63,6 +63,13 @@ def lib():
         L.orc_v1_deliver_near.argtypes = [P, FP, C.c_int]
         L.orc_v1_deliver_far.argtypes = [P]
         L.orc_v1_set_delays.argtypes = [P, FP, C.c_int]
+        F = C.c_float
+        L.orc_cond_eval.argtypes = [F, F, F, F, F, F, FP]
+        L.orc_adex_depc.argtypes = [F] * 6
+        L.orc_adex_depc.restype = F
+        L.orc_adex_rk2.argtypes = [F] * 19 + [FP, FP]
+        L.orc_adex_spike.argtypes = [F] * 5 + [FP, FP]
+        L.orc_logistic_ab.argtypes = [FP, FP, FP, C.c_int, FP, FP]
         L.orc_v1_deliver_near_delayed.argtypes = [P]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_num_threads.restype = C.c_int

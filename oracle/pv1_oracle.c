@@ -82,6 +82,16 @@ static float temporal_kernel(float tau, float tauR, float tauD, float nR, float 
     return tpR - ratio * tpD;
 }
 
+/* hStatic_nonlinear's logistic a and b (src/LGN_props.h:159-169), in float. */
+void orc_logistic_ab(const float *spont, const float *c50, const float *sharp, int n, float *a, float *b) {
+    for (int i = 0; i < n; i++) {
+        const float e_kc50 = expf(sharp[i] * c50[i]);
+        const float e_kc50_k = expf(sharp[i] * c50[i] - sharp[i]);
+        a[i] = (1 - spont[i]) * (1 + e_kc50) * (1 + e_kc50_k) / (e_kc50 - e_kc50_k);
+        b[i] = 1 - a[i] / (1 + e_kc50_k);
+    }
+}
+
 /* store_PM for magno cells: TW [nMagno][nKS], SW [nMagno][nSample], SC [2][nMagno][nSample],
  * maxConvol [nLGN], absk [nMagno]; logistic la/lb [nLGN]. */
 int orc_lgn_setup(const pv1_lgn_config *c, const pv1_lgn_params *p, float *TW, float *SW,
@@ -89,12 +99,7 @@ int orc_lgn_setup(const pv1_lgn_config *c, const pv1_lgn_params *p, float *TW, f
     const int nLGN = (int)c->nLGN;
     const int nMagno = (int)(c->nMagno_I + c->nMagno_C);
     const int n1 = (int)c->mSample1D, nS = n1 * n1, nKS = (int)c->nKernelSample;
-    for (int i = 0; i < nLGN; i++) {
-        const float e_kc50 = expf(p->sharpness[i] * p->c50[i]);
-        const float e_kc50_k = expf(p->sharpness[i] * p->c50[i] - p->sharpness[i]);
-        la[i] = (1 - p->spont[i]) * (1 + e_kc50) * (1 + e_kc50_k) / (e_kc50 - e_kc50_k);
-        lb[i] = 1 - la[i] / (1 + e_kc50_k);
-    }
+    orc_logistic_ab(p->spont, p->c50, p->sharpness, nLGN, la, lb);
     float *cw = (float *)malloc(sizeof(float) * nS), *sw = (float *)malloc(sizeof(float) * nS);
     for (int m = 0; m < nMagno; m++) {
         int id = (int)c->nParvo_I + m;
@@ -448,6 +453,47 @@ int orc_v1_put(orc_v1 *o, int which, const float *in) {
     return 0;
 }
 
+/* The AdEx pieces of src/coredynamics.cuh:27-118, as compute_v uses them (exported so that
+ * they can be checked against the reference's own struct compiled on the host). */
+float orc_adex_depc(float vL, float vT, float gL, float a, float deltaT, float dep) {
+    const float targetV = vL + (vT - vL) * dep;
+    if (targetV > vT) return (gL + a) * (targetV - vL) - gL * deltaT;
+    return (gL + a) * (targetV - vL) - gL * deltaT * expf((targetV - vT) / deltaT);
+}
+
+/* set_p0 / set_p1 (get_a, get_b, depC, no gap junction) then rk2 over dt */
+void orc_adex_rk2(float vE, float vI, float vL, float gE0, float gI0, float gE1, float gI1, float depC,
+                  float gL, float vT, float deltaT, float Cm, float a, float tau_w, float v0, float w0, float dt,
+                  float n0, float n1, float *v, float *w) {
+    const float a0 = gE0 + gI0 + gL, b0 = gE0 * vE + gI0 * vI + gL * vL + depC;
+    const float a1 = gE1 + gI1 + gL, b1 = gE1 * vE + gI1 * vI + gL * vL + depC;
+    const float dTgL = deltaT * gL;
+    const float fk1 = (-a0 * v0 + b0 + dTgL * expf((v0 - vT) / deltaT) - w0) / Cm + n0;
+    const float gk1 = (a * (v0 - vL) - w0) / tau_w;
+    const float v1 = v0 + dt * fk1;
+    const float w1 = w0 + dt * gk1;
+    const float fk2 = (-a1 * v1 + b1 + dTgL * expf((v1 - vT) / deltaT) - w1) / Cm + n1;
+    const float gk2 = (a * (v1 - vL) - w1) / tau_w;
+    *w = w0 + dt * (gk1 + gk2) / 2;
+    *v = v0 + dt * (fk1 + fk2) / 2;
+}
+
+/* compute_spike_time: the threshold-crossing fraction of the step and w0's jump */
+void orc_adex_spike(float vThres, float v0, float v, float w, float b, float *ratio, float *w0) {
+    *ratio = (vThres - v0) / (v - v0);
+    *w0 += *ratio * (w - *w0) + b;
+}
+
+/* ConductanceShape (src/condShape.h:13-41) for one species: out = {g, h after
+ * decay_conductance(dt), g, h after compute_single_input_conductance(f, dt)} from (g, h). */
+void orc_cond_eval(float rise, float decay, float g, float h, float f, float dt, float *out) {
+    ocond c = ocond_make(&rise, &decay, 1);
+    float g1 = g, h1 = h, g2 = g, h2 = h;
+    ocond_decay(&c, &g1, &h1, dt, 0);
+    ocond_input(&c, &g2, &h2, f, dt, 0);
+    out[0] = g1; out[1] = h1; out[2] = g2; out[3] = h2;
+}
+
 /* compute_V_collect_spike_learnFF_fast for every neuron (learning off, no gap junctions).
  * noise: normals [nV1] of this step (NULL if no noise); ff: normals [nV1][cap] for the
  * feed-forward failure draws.  Writes sInfo (the step's spike word). */
@@ -467,12 +513,7 @@ int orc_v1_compute_v(orc_v1 *o, const float *lgnSInfo, const float *noise, const
         float v0 = o->v[i];
         float w0 = c->iModel == 1 ? o->w[i] : 0.0f;
         float tBack = o->tBack[i];
-        float depC;
-        {
-            float targetV = c->vL + (vT - c->vL) * tonic;
-            if (targetV > vT) depC = (gL + aa) * (targetV - c->vL) - gL * deltaT;
-            else depC = (gL + aa) * (targetV - c->vL) - gL * deltaT * expf((targetV - vT) / deltaT);
-        }
+        const float depC = orc_adex_depc(c->vL, vT, gL, aa, deltaT, tonic);
         float noise0 = c->tau_noise > 0 ? o->lastNoise[i] : 0.f;
         float ge[PV1_MAX_NG], he[PV1_MAX_NG], gi[PV1_MAX_NG], hi[PV1_MAX_NG];
         float gE_t1 = 0.0f, gI_t1 = 0.0f;
@@ -563,8 +604,6 @@ int orc_v1_compute_v(orc_v1 *o, const float *lgnSInfo, const float *noise, const
         float v = v0, w = w0, tsp = 0.f;
         int spiked = 0;
         if (tBack < dt) {
-            const float a0 = gE_t0 + gI_t0 + gL, b0 = gE_t0 * c->vE + gI_t0 * c->vI + gL * c->vL + depC;
-            const float a1 = gE_t1 + gI_t1 + gL, b1 = gE_t1 * c->vE + gI_t1 * c->vI + gL * c->vL + depC;
             const float new_dt = dt - tBack;
             if (backingUp) {
                 float A = aa * (v0 - c->vL);
@@ -573,19 +612,12 @@ int orc_v1_compute_v(orc_v1 *o, const float *lgnSInfo, const float *noise, const
             float n0, n1;
             if (c->tau_noise > 0) { n0 = noise0; n1 = noise1; }
             else { noise1 /= dt; n0 = noise1; n1 = noise1; }
-            const float dTgL = deltaT * gL;
-            const float fk1 = (-a0 * v0 + b0 + dTgL * expf((v0 - vT) / deltaT) - w0) / Cm + n0;
-            const float gk1 = (aa * (v0 - c->vL) - w0) / tau_w;
-            const float v1 = v0 + new_dt * fk1;
-            const float w1 = w0 + new_dt * gk1;
-            const float fk2 = (-a1 * v1 + b1 + dTgL * expf((v1 - vT) / deltaT) - w1) / Cm + n1;
-            const float gk2 = (aa * (v1 - c->vL) - w1) / tau_w;
-            w = w0 + new_dt * (gk1 + gk2) / 2;
-            v = v0 + new_dt * (fk1 + fk2) / 2;
+            orc_adex_rk2(c->vE, c->vI, c->vL, gE_t0, gI_t0, gE_t1, gI_t1, depC, gL, vT, deltaT, Cm, aa, tau_w,
+                         v0, w0, new_dt, n0, n1, &v, &w);
             if (v > vThres) {
-                const float ratio = (vThres - v0) / (v - v0);
+                float ratio;
+                orc_adex_spike(vThres, v0, v, w, bb, &ratio, &w0);
                 tsp = tBack + ratio * new_dt;
-                w0 += ratio * (w - w0) + bb;
                 if (!(tsp >= 0)) nerr++;
                 spiked = 1;
                 tBack = tsp + tRef;

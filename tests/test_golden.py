@@ -1,0 +1,111 @@
+"""The oracle against golden vectors computed by the reference's own code.
+
+tests/golden/ref_golden.npz holds inputs and the outputs of the reference's ConductanceShape,
+AdEx struct, hStatic_nonlinear, find_denorm and fill_fSpikeTrain + recal_G_vec, compiled on
+the host from its sources (oracle/ref/build_ref.sh, tests/golden/make_golden.py).  The
+oracle's restatements must reproduce them bit for bit (same float operations, same order).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "ref_golden.npz")
+f32 = np.float32
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD)
+
+
+@pytest.fixture(scope="module")
+def L():
+    import oracle
+    return oracle.lib()
+
+
+def fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def test_conductance_shape(gold, L):
+    x, y = gold["cond_in"], gold["cond_out"]
+    out = np.empty(4, f32)
+    got = np.empty_like(y)
+    for q in range(x.shape[0]):
+        L.orc_cond_eval(*[float(v) for v in x[q]], fp(out))
+        got[q] = out
+    np.testing.assert_array_equal(got, y)
+
+
+def test_adex_step(gold, L):
+    """Tonic drive (constructor), set_p0/set_p1 + rk2 and compute_spike_time."""
+    x, y = gold["adex_in"], gold["adex_out"]
+    vE, vI, vL = 0.0, -75.0, -65.0        # the reference's compile-time reversal potentials
+    v, w = C.c_float(), C.c_float()
+    ratio, w0 = C.c_float(), C.c_float()
+    for q in range(x.shape[0]):
+        (w_0, tau_w, a, b, v0, vR, vThres, gL, Cm, tRef, vT, deltaT, dep, gE0, gI0, gE1, gI1, dt) = \
+            [float(t) for t in x[q]]
+        depC = L.orc_adex_depc(vL, vT, gL, a, deltaT, dep)
+        assert np.float32(depC) == y[q, 0], q
+        L.orc_adex_rk2(vE, vI, vL, gE0, gI0, gE1, gI1, depC, gL, vT, deltaT, Cm, a, tau_w, v0, w_0, dt,
+                       0.0, 0.0, C.byref(v), C.byref(w))
+        assert (np.float32(v.value), np.float32(w.value)) == (y[q, 1], y[q, 2]), q
+        w0.value = w_0
+        L.orc_adex_spike(vThres, v0, v.value, w.value, b, C.byref(ratio), C.byref(w0))
+        # compute_spike_time with t0 = 0: tsp = ratio * dt
+        assert np.float32(np.float32(ratio.value) * np.float32(dt)) == y[q, 3], q
+        assert np.float32(w0.value) == y[q, 4], q
+
+
+def test_logistic_parameters(gold, L):
+    spont, c50, sharp = [np.ascontiguousarray(r, f32) for r in gold["logistic_in"]]
+    n = spont.size
+    a, b = np.empty(n, f32), np.empty(n, f32)
+    L.orc_logistic_ab(fp(spont), fp(c50), fp(sharp), n, fp(a), fp(b))
+    np.testing.assert_array_equal(a, gold["logistic_out"][0])
+    np.testing.assert_array_equal(b, gold["logistic_out"][1])
+
+
+def test_find_denorm(gold):
+    from visual_cortex_gb300.schedule import find_denorm
+    for (u1, u2, morn), (d, nrm) in zip(gold["denorm_in"], gold["denorm_out"]):
+        assert find_denorm(int(u1), int(u2), bool(morn)) == (int(d), int(nrm))
+
+
+def test_far_delivery_matches_recal_G_vec(gold):
+    """fill_fSpikeTrain + recal_G_vec over a 120-step spike sequence: the oracle's
+    restatement gives the same far conductances, bit for bit, every step."""
+    import oracle
+    from visual_cortex_gb300.model import V1Network, V1Spec
+    nV1, bs, nE, ngE, ngI, T = [int(v) for v in gold["far_hdr"][:6]]
+    prm = gold["far_prm"]
+    spec = V1Spec(nblock=nV1 // bs, blockSize=bs, typeAcc=[nE, bs], nTypeE=1, ngFF=1, ngE=ngE, ngI=ngI,
+                  dt=float(prm[0]), riseFF=[1.0], decayFF=[5.0], riseE=[float(prm[2]), float(prm[3])],
+                  decayE=[float(prm[4]), float(prm[5])], riseI=[float(prm[6])], decayI=[float(prm[8])],
+                  vR=[-60.0] * 2, vThres=[-50.0] * 2, gL=[0.05] * 2, C=[1.0] * 2, tRef=[2.0] * 2,
+                  vT=[-50.0] * 2, deltaT=[1.0] * 2, tau_w=[150.0] * 2, a=[0.0] * 2, b=[0.0] * 2,
+                  pFF=[1.0, 1.0], pE=[float(v) for v in prm[10:14]], pI=[float(prm[14]), float(prm[15])],
+                  synFail=[0.0] * 4, synPerCon=[1.0] * 4, synFailFF=[0.0] * 2, synPerConFF=[1.0] * 2,
+                  noisyDep=[0.0] * 2, noFarDelay=0, speedOfThought=float(prm[1]))
+    u32 = np.uint32
+    net = V1Network(nLGNperV1=np.zeros(nV1, u32), lgnId=np.zeros((1, nV1), u32), sLGN=np.zeros((1, nV1), f32),
+                    nNearNB=np.zeros(spec.nblock, u32), nbId=np.zeros((spec.nblock, 1), u32),
+                    conMat=np.zeros((spec.nblock, 1, bs, bs), f32), nVec=gold["far_nVec"],
+                    vecID=gold["far_vecID"], conVec=gold["far_conVec"], delayVec=gold["far_delayVec"],
+                    tonicDep=np.zeros(nV1, f32))
+    vo = oracle.V1Oracle(spec, net)
+    L = oracle.lib()
+    zE, zI = np.zeros(ngE * nV1, f32), np.zeros(ngI * nV1, f32)
+    for t in range(T):
+        for name, z in (("gE", zE), ("hE", zE), ("gI", zI), ("hI", zI)):
+            vo.put(name, z)
+        vo.put("sInfo", gold["far_sInfo"][t])
+        L.orc_v1_deliver_far(vo.h)
+        got = np.concatenate([vo.get("gE").reshape(ngE, nV1), vo.get("hE").reshape(ngE, nV1),
+                              vo.get("gI").reshape(ngI, nV1), vo.get("hI").reshape(ngI, nV1)])
+        np.testing.assert_array_equal(got, gold["far_out"][t], err_msg=f"step {t}")
+    assert np.abs(gold["far_out"]).sum() > 0

@@ -140,6 +140,36 @@ int pv1_stimulus_load(pv1_plan *plan, uint32_t nFrame, uint32_t height, uint32_t
 /* Reads the spatial-stage table S [nFrame+1][nMagno] (row nFrame: the initial luminance). */
 int pv1_lgn_get_spatial(pv1_plan *plan, float *S);
 
+/* Parvocellular cells: centre and surround are separate Gaussians of their own cone types
+ * (L/M opponent or L+M), each with its own temporal kernel, sampled on their own kernel
+ * grid (nKernelSample over tau) and their own frame-phase tail (parvoComp). */
+typedef struct pv1_lgn_parvo_config {
+    uint32_t nSample1D;          /* nSpatialSample1D (<= 32)                                  */
+    uint32_t nKernelSample;      /* nKernelSample                                             */
+    uint32_t kernelSampleInterval, iKernelSampleT0;   /* in steps                             */
+    uint32_t parvoComp, frameOffset;  /* frameOffset = (1-pLongerThanM)*dFrame               */
+    float kernelSampleDt, kernelSampleT0;             /* ms                                   */
+} pv1_lgn_parvo_config;
+
+/* pv1_lgn_setup for an LGN with parvocellular cells (nParvo_I + nParvo_C > 0): the magno part
+ * as pv1_lgn_setup, plus store_PM(PM=0) (src/discrete_input_convol.cu:427-520 with
+ * store_temporalWeight :230-305 and store_spatialWeight :309-425, flat retina) and
+ * parvo_maxConvol (:748-883) with the sample-grid size rule of src/patch.cu:5266-5312.
+ * covariant [nLGN] as stored in the `LGN` file.  pv1_lgn_setup is this call with pcfg = NULL
+ * and rejects parvo cells. */
+int pv1_lgn_setup_parvo(pv1_plan *plan, const pv1_lgn_config *lcfg, const pv1_lgn_parvo_config *pcfg,
+                        const pv1_lgn_params *p, const float *covariant, uint64_t seed);
+
+/* Parvo setup tables: TW [nParvo][2][nKernelSample] (centre, surround; time reversed, L1
+ * normalised), SW [nSample] (the normalised Gaussian every parvo cell shares), SC
+ * [2][nParvo][2][nSample] (x then y texture coordinates per cell and component).  Parvo cell
+ * c is LGN id c (c < nParvo_I) or c + nMagno_I.  Any pointer may be NULL. */
+int pv1_lgn_get_parvo_tables(pv1_plan *plan, float *TW, float *SW, float *SC);
+
+/* Parvo spatial stage PS [nFrame+1][2][nParvo]: per frame the centre and surround contrast
+ * sums of LGN_convol_parvo (src/discrete_input_convol.cu:1032-1062, 1151-1218). */
+int pv1_lgn_get_parvo_spatial(pv1_plan *plan, float *PS);
+
 /* ---- V1 --------------------------------------------------------------------------- */
 
 /* LGN->V1 feed-forward synapses, transposed [maxLGN][nV1] as the reference keeps them in

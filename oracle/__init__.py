@@ -54,6 +54,11 @@ def lib():
         L.orc_lgn_spatial.argtypes = [C.c_int, C.c_int, FP, FP, UP, FP, C.c_int, C.c_int, C.c_int, C.c_int, FP]
         L.orc_lgn_convol.argtypes = [P, C.c_int, C.c_int, C.c_longlong, FP, FP, FP, FP]
         L.orc_lgn_nonlinear.argtypes = [P, FP, FP, FP, FP, FP, FP, FP, FP, FP, IP, C.c_int, FP, FP]
+        L.orc_parvo_max_sample1d.argtypes = [P, P, C.c_int]
+        L.orc_lgn_parvo_setup.argtypes = [P, P, P, FP, FP, FP, FP, FP]
+        L.orc_lgn_parvo_spatial.argtypes = [C.c_int, C.c_int, FP, FP, UP, FP, C.c_int, C.c_int, C.c_int,
+                                            C.c_int, FP]
+        L.orc_lgn_parvo_convol.argtypes = [P, P, P, C.c_int, C.c_longlong, FP, FP, FP]
         L.orc_v1_create.argtypes = [P, C.c_uint32, UP, UP, FP, C.c_uint32, UP, UP, FP, UP, UP, FP, FP, FP]
         L.orc_v1_create.restype = P
         L.orc_v1_destroy.argtypes = [P]
@@ -102,7 +107,8 @@ ST = dict(v=0, w=1, tBack=2, dep=3, gFF=4, hFF=5, gE=6, hE=7, gI=8, hI=9, sInfo=
 
 
 class LgnOracle:
-    """store_PM + per-frame spatial stage + per-step convolution and spikes for magno cells."""
+    """store_PM + per-frame spatial stage + per-step convolution and spikes for the magno
+    and (when present) the parvo cells."""
 
     def __init__(self, lgn, stim, wbits: int = 8):
         self.lgn = lgn
@@ -127,6 +133,21 @@ class LgnOracle:
         self.sharp = np.ascontiguousarray(lgn.sharpness, f32)
         self.ltr = np.zeros(lgn.nLGN, f32)
         self.lnl = np.zeros(lgn.nLGN, f32)
+        self.nParvo = lgn.nParvo
+        self.PS = None
+        if self.nParvo:
+            self.pcfg = lgn.to_parvo_struct()
+            npv, ns, pks = self.nParvo, lgn.nSample1D ** 2, lgn.sched.nKernelSample
+            self.pTW = np.empty((npv, 2, pks), f32)
+            self.pSW = np.empty(ns, f32)
+            self.pSC = np.empty((2, npv, 2, ns), f32)
+            self._cov = np.ascontiguousarray(lgn.covariant, f32)
+            L.orc_lgn_parvo_setup(C.byref(self.cfg), C.byref(self.pcfg), C.byref(self.params), fp(self._cov),
+                                  fp(self.pTW), fp(self.pSW), fp(self.pSC), fp(self.maxConvol))
+            self.max_sample1d = L.orc_parvo_max_sample1d(C.byref(self.cfg), C.byref(self.params), lgn.nSample1D)
+            ct = np.asarray(lgn.coneType, np.uint32)
+            pid = lgn.parvo_ids()
+            self.pcone = np.ascontiguousarray(np.concatenate([ct[pid], ct[lgn.nLGN + pid]]), np.uint32)
 
     def spatial(self, SW=None, SC=None):
         """S [nFrame+1][nMagno]; by default from this oracle's own SW/SC tables."""
@@ -144,14 +165,44 @@ class LgnOracle:
         lib().orc_lgn_spatial(lgn.nMagno, lgn.mSample1D ** 2, fp(SW), fp(SC), up(cone), fp(layers), nF + 1,
                               h, w, self.wbits, fp(S))
         self.S = S
+        if self.nParvo:
+            self._layers = layers
+            self.parvo_spatial()
         return S
 
+    def parvo_spatial(self, SW=None, SC=None):
+        """PS [nFrame+1][2][nParvo]; by default from this oracle's own parvo tables."""
+        fr = self.stim.frames
+        nF, _, h, w = fr.shape
+        layers = getattr(self, "_layers", None)
+        if layers is None:
+            layers = np.empty((nF + 1, 3, h, w), f32)
+            layers[:nF] = fr
+            for ch in range(3):
+                layers[nF, ch] = self.stim.init_LMS[ch]
+            self._layers = layers
+        SW = self.pSW if SW is None else np.ascontiguousarray(SW, f32)
+        SC = self.pSC if SC is None else np.ascontiguousarray(SC, f32)
+        PS = np.empty((nF + 1, 2, self.nParvo), f32)
+        lib().orc_lgn_parvo_spatial(self.nParvo, self.lgn.nSample1D ** 2, fp(SW), fp(SC), up(self.pcone),
+                                    fp(layers), nF + 1, h, w, self.wbits, fp(PS))
+        self.PS = PS
+        return PS
+
     def convol(self, it: int, S=None, TW=None):
+        """Convolution of step it for every LGN cell, by LGN id (magno: times |k|)."""
         S = self.S if S is None else S
         TW = self.TW if TW is None else TW
-        out = np.empty(self.lgn.nMagno, f32)
+        mag = np.empty(self.lgn.nMagno, f32)
         lib().orc_lgn_convol(C.byref(self.cfg), self.lgn.nMagno, self.nFrame, int(it), fp(TW), fp(S),
-                             fp(self.absk), fp(out))
+                             fp(self.absk), fp(mag))
+        out = np.zeros(self.lgn.nLGN, f32)
+        out[self.lgn.magno_ids()] = mag
+        if self.nParvo:
+            par = np.empty(self.nParvo, f32)
+            lib().orc_lgn_parvo_convol(C.byref(self.cfg), C.byref(self.pcfg), C.byref(self.params), self.nFrame,
+                                       int(it), fp(self.pTW), fp(self.PS), fp(par))
+            out[self.lgn.parvo_ids()] = par
         return out
 
     def nonlinear(self, convol, u, ucount, cap):

@@ -65,6 +65,7 @@ def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None
     try:
         gpu_tables = sim.lgn_tables()
         gpu_S = sim.lgn_spatial()
+        gpu_parvo = (sim.lgn_parvo_tables(), sim.lgn_parvo_spatial()) if wl.lgn.nParvo else None
         lnl0 = sim.state("lgn_lnl")
         ltr0 = sim.state("lgn_ltr")
         sim.set_record(N.REC_RAW | N.REC_LGN_SP | N.REC_LGN_FR, nsteps + 1)
@@ -89,6 +90,10 @@ def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None
         lo.TW[:] = TW
         lo.maxConvol[:] = mc
         lo.S = np.ascontiguousarray(gpu_S)
+        if gpu_parvo is not None:
+            (pTW, _, _), PS = gpu_parvo
+            lo.pTW[:] = pTW
+            lo.PS = np.ascontiguousarray(PS)
     lo.lnl[:] = lnl0
     lo.ltr[:] = ltr0
     vo = V1Oracle(wl.spec, wl.net)

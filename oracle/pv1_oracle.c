@@ -17,6 +17,9 @@
  *   sum_G                          src/coredynamics.cu:2312-2349
  *   store_PM (magno) / TW          src/discrete_input_convol.cu:230-305, 427-744
  *   LGN_convol_magno               src/discrete_input_convol.cu:1342-1585
+ *   store_PM (parvo), parvo_maxConvol, LGN_convol_parvo
+ *                                  src/discrete_input_convol.cu:309-520, 748-883, 886-1340;
+ *                                  sample-grid rule src/patch.cu:5266-5312
  *   LGN_nonlinear / get_spike      src/discrete_input_convol.cu:1587-1821
  *   transform / hStatic_nonlinear  src/LGN_props.cuh:94-100, src/LGN_props.h:143-170
  *   texture sampling               src/patch.h:95-109 (bilinear, normalised, border)
@@ -71,6 +74,12 @@ int orc_version(void) { return 1; }
 static float gauss2(float x, float y, float rx, float ry) {
     return expf(-x * x / (rx * rx) - y * y / (ry * ry));
 }
+
+/* nsig * r / SQRT2: the float product divided in double (SQRT2, src/CONST.h:30). */
+static float parvo_span(float nsig, float r) { return (float)((double)(nsig * r) / 1.4142135623730951); }
+/* Sample coordinate (i + 0.5) * d - span in double, rounded once to float, as the
+ * reference's `(threadIdx.x + 0.5)*ds - span` evaluates. */
+static float grid_at(int i, float d, float span) { return (float)(((double)i + 0.5) * (double)d - (double)span); }
 
 static float temporal_kernel(float tau, float tauR, float tauD, float nR, float nD, float ratio,
                              float lfac1, float lfac2) {
@@ -131,7 +140,7 @@ int orc_lgn_setup(const pv1_lgn_config *c, const pv1_lgn_params *p, float *TW, f
         float csum = 0.f, ssum = 0.f;
         for (int s = 0; s < nS; s++) {
             const int tx = s % n1, ty = s / n1;
-            const float cx = (tx + 0.5f) * ds - span, cy = (ty + 0.5f) * ds - span;
+            const float cx = grid_at(tx, ds, span), cy = grid_at(ty, ds, span);
             const float ttx = cx - ox, tty = cy - oy;
             const float sx = ttx * rc - tty * rsn, sy = ttx * rsn + tty * rc;
             cw[s] = gauss2(cx, cy, p->rw[id], p->rh[id]);
@@ -155,7 +164,7 @@ int orc_lgn_setup(const pv1_lgn_config *c, const pv1_lgn_params *p, float *TW, f
         const float coso = cosf(p->orient[id]), sino = sinf(p->orient[id]);
         for (int s = 0; s < nS; s++) {
             const int tx = s % n1, ty = s / n1;
-            const float cx = (tx + 0.5f) * ds - span, cy = (ty + 0.5f) * ds - span;
+            const float cx = grid_at(tx, ds, span), cy = grid_at(ty, ds, span);
             SC[(size_t)m * nS + s] = x0 + (p->ecc[id] * cosf(p->polar[id]) + cx * coso - cy * sino) * c->normViewDistance;
             SC[(size_t)nMagno * nS + (size_t)m * nS + s] =
                 y0 + (p->ecc[id] * sinf(p->polar[id]) + cx * sino + cy * coso) * c->normViewDistance;
@@ -231,24 +240,36 @@ int orc_lgn_spatial(int nMagno, int nSample, const float *SW, const float *SC,
  * sample j of the window reads the texture layer tail + ((T0 + j*interval)*denorm +
  * phase)/ntPerFrame; the layer holds the newest frame with that residue mod maxFrame, or the
  * initial luminance if no frame was loaded there yet.  convol_out[m] = convol * |k|. */
-int orc_lgn_convol(const pv1_lgn_config *c, int nMagno, int nFrame, long long it, const float *TW,
-                   const float *S, const float *absk, float *convol_out) {
+/* Row of the spatial table read by sample j of step it's window: sample j sits
+ * (T0 + j*interval)*denorm + phase units after the window tail layer
+ * (oldFrameHead + frameOffset + (phase <= comp ? 2 : 1), getTail of src/patch.cu:5413-5422);
+ * the layer holds the newest loaded frame with that residue mod maxFrame, or the initial
+ * luminance (row nFrame) if no frame was loaded there yet. */
+static void window_rows(const pv1_lgn_config *c, int nKS, int T0, int interval, int comp, int frameOffset,
+                        int nFrame, long long it, int *rowOf) {
     const long long num = (it + 1) * (long long)c->denorm;
     const int currentFrame = (int)((num + c->ntPerFrame - 1) / c->ntPerFrame);
     const int oldFrameHead = (currentFrame - 1) % (int)c->maxFrame;
-    const int phase = (int)((c->magnoComp + (it + 1) * (long long)c->denorm) % c->ntPerFrame);
-    const int tail = oldFrameHead + (int)c->frameOffset + (phase <= (int)c->magnoComp ? 2 : 1);
-    const int nKS = (int)c->nKernelSample;
-    int *rowOf = (int *)malloc(sizeof(int) * nKS);
+    const int phase = (int)((comp + (it + 1) * (long long)c->denorm) % c->ntPerFrame);
+    const int tail = oldFrameHead + frameOffset + (phase <= comp ? 2 : 1);
     for (int j = 0; j < nKS; j++) {
-        long long o = (long long)(c->iKernelSampleT0 + (long long)j * c->kernelSampleInterval) * c->denorm + phase;
+        long long o = (long long)(T0 + (long long)j * interval) * c->denorm + phase;
         int layer = (int)((tail + o / c->ntPerFrame) % c->maxFrame);
-        /* newest frame F <= currentFrame-1 with F % maxFrame == layer */
         int Fnew = currentFrame - 1;
         int back = ((Fnew % (int)c->maxFrame) - layer + (int)c->maxFrame) % (int)c->maxFrame;
         int F = Fnew - back;
         rowOf[j] = F < 0 ? nFrame : F % nFrame;
     }
+}
+
+/* Temporal convolution of step `it` for the magno cells, sample by sample as
+ * LGN_convol_magno walks it.  convol_out[m] = convol * |k|. */
+int orc_lgn_convol(const pv1_lgn_config *c, int nMagno, int nFrame, long long it, const float *TW,
+                   const float *S, const float *absk, float *convol_out) {
+    const int nKS = (int)c->nKernelSample;
+    int *rowOf = (int *)malloc(sizeof(int) * nKS);
+    window_rows(c, nKS, (int)c->iKernelSampleT0, (int)c->kernelSampleInterval, (int)c->magnoComp,
+                (int)c->frameOffset, nFrame, it, rowOf);
     for (int m = 0; m < nMagno; m++) {
         float conv = 0.f;
         for (int j = 0; j < nKS; j++) conv += S[(size_t)rowOf[j] * nMagno + m] * TW[(size_t)m * nKS + j];
@@ -258,20 +279,211 @@ int orc_lgn_convol(const pv1_lgn_config *c, int nMagno, int nFrame, long long it
     return 0;
 }
 
-/* LGN_nonlinear + get_spike for every magno cell of one step.  u: recorded uniforms
- * [nLGN][cap] of this step, ucount [nLGN].  Returns the number of cells whose draw count
- * disagrees with the record (0 when the CPU and GPU took the same branches). */
+/* ---- parvocellular cells (store_PM with PM = 0, parvo_maxConvol, LGN_convol_parvo) ---- */
+
+/* Side of parvo_maxConvol's sample grid, src/patch.cu:5266-5312: round(mean over cone
+ * type < 4 cells of sqrt(R^2 / (wSpan hSpan)), divided by nParvo) * nSpatialSample1D, at least
+ * 32, and at most what 48 KB - 128 B of shared memory holds for two float arrays. */
+int orc_parvo_max_sample1d(const pv1_lgn_config *c, const pv1_lgn_params *p, int n1) {
+    const int nLGN = (int)c->nLGN, nParvo = (int)(c->nParvo_I + c->nParvo_C);
+    const float nsig = fabsf(c->nsig);
+    float meanRatio = 0.f;
+    for (int i = 0; i < nLGN; i++) {
+        if (p->coneType[i] >= 4) continue;
+        float dx = p->ecc[i] * cosf(p->polar[i]) - p->ecc[nLGN + i] * cosf(p->polar[nLGN + i]);
+        float dy = p->ecc[i] * sinf(p->polar[i]) - p->ecc[nLGN + i] * sinf(p->polar[nLGN + i]);
+        float r = sqrtf(dx * dx + dy * dy);
+        float wSpan = parvo_span(nsig, p->rw[nLGN + i]), hSpan = parvo_span(nsig, p->rh[nLGN + i]);
+        float R = wSpan > hSpan ? wSpan : hSpan;
+        wSpan = parvo_span(nsig, p->rw[i]);
+        hSpan = parvo_span(nsig, p->rh[i]);
+        r += wSpan > hSpan ? wSpan : hSpan;
+        R = r > R ? r : R;
+        meanRatio += sqrtf(R * R / wSpan / hSpan);
+    }
+    meanRatio /= nParvo;
+    long long m1 = (long long)roundf(meanRatio) * n1;
+    if (m1 * m1 < 1024) return 32;
+    const size_t avail = 48 * 1024 - 32 * sizeof(float);
+    if ((size_t)(m1 * m1) * 2 * sizeof(float) > avail)
+        m1 = (long long)floor(sqrt((double)(avail / sizeof(float) / 2 / (size_t)(n1 * n1)))) * n1;
+    return (int)m1;
+}
+
+/* TW [nParvo][2][nKS], SW [nSample], SC [2][nParvo][2][nSample], maxConvol at parvo ids. */
+int orc_lgn_parvo_setup(const pv1_lgn_config *c, const pv1_lgn_parvo_config *q, const pv1_lgn_params *p,
+                        const float *covariant, float *TW, float *SW, float *SC, float *maxConvol) {
+    const int nLGN = (int)c->nLGN, nParvo = (int)(c->nParvo_I + c->nParvo_C);
+    const int n1 = (int)q->nSample1D, nS = n1 * n1, nKS = (int)q->nKernelSample;
+    for (int cell = 0; cell < nParvo; cell++) {
+        const int id = cell < (int)c->nParvo_I ? cell : cell + (int)c->nMagno_I;
+        for (int type = 0; type < 2; type++) {
+            const int lid = type * nLGN + id;
+            /* store_temporalWeight (src/discrete_input_convol.cu:230-305) */
+            const float lfac1 = lgammaf(p->nR[lid]), lfac2 = lgammaf(p->nD[lid]);
+            const float t0 = q->kernelSampleT0 - p->delay[lid];
+            float *tw = TW + ((size_t)cell * 2 + type) * nKS;
+            float tot = 0.f;
+            for (int j = 0; j < nKS; j++) {
+                float t = (nKS - 1 - j) * q->kernelSampleDt + t0;
+                tw[j] = t < 0 ? 0.0f
+                              : temporal_kernel(t, p->tauR[lid], p->tauD[lid], p->nR[lid], p->nD[lid],
+                                                p->ratio[lid], lfac1, lfac2);
+                tot += fabsf(tw[j]);
+            }
+            for (int j = 0; j < nKS; j++) tw[j] /= tot;
+            /* store_spatialWeight (:309-425), flat retina */
+            const float rx = p->rw[lid], ry = p->rh[lid];
+            const float wSpan = parvo_span(c->nsig, rx), hSpan = parvo_span(c->nsig, ry);
+            const float dw = 2 * wSpan / n1, dh = 2 * hSpan / n1;
+            if (cell == 0 && type == 0) {
+                float sum = 0.f;
+                for (int s = 0; s < nS; s++) {
+                    SW[s] = gauss2(grid_at(s % n1, dw, wSpan), grid_at(s / n1, dh, hSpan), rx, ry);
+                    sum += SW[s];
+                }
+                for (int s = 0; s < nS; s++) SW[s] /= sum;
+            }
+            const int left = cell < (int)c->nParvo_I;
+            const float x0 = left ? c->L_x0 : c->R_x0, y0 = left ? c->L_y0 : c->R_y0;
+            const float coso = cosf(p->orient[lid]), sino = sinf(p->orient[lid]);
+            const float ce = p->ecc[lid], cp = p->polar[lid];
+            for (int s = 0; s < nS; s++) {
+                const float w = grid_at(s % n1, dw, wSpan), h = grid_at(s / n1, dh, hSpan);
+                const size_t sid = ((size_t)cell * 2 + type) * nS + s;
+                SC[sid] = x0 + (ce * cosf(cp) + w * coso - h * sino) * c->normViewDistance;
+                SC[(size_t)nParvo * 2 * nS + sid] = y0 + (ce * sinf(cp) + w * sino + h * coso) * c->normViewDistance;
+            }
+        }
+    }
+    /* parvo_maxConvol (:748-883) */
+    const int m1 = orc_parvo_max_sample1d(c, p, n1);
+    const int nUse = (m1 * m1 / 1024) * 1024;
+    float *swC = (float *)malloc(sizeof(float) * (size_t)(nUse > 0 ? nUse : 1));
+    float *swS = (float *)malloc(sizeof(float) * (size_t)(nUse > 0 ? nUse : 1));
+    for (int cell = 0; cell < nParvo; cell++) {
+        const int id = cell < (int)c->nParvo_I ? cell : cell + (int)c->nMagno_I;
+        const int sid = nLGN + id;
+        float wSpan = parvo_span(c->nsig, p->rw[sid]), hSpan = parvo_span(c->nsig, p->rh[sid]);
+        float R = wSpan > hSpan ? wSpan : hSpan;
+        wSpan = parvo_span(c->nsig, p->rw[id]);
+        hSpan = parvo_span(c->nsig, p->rh[id]);
+        const float dx = p->ecc[id] * cosf(p->polar[id]) - p->ecc[sid] * cosf(p->polar[sid]);
+        const float dy = p->ecc[id] * sinf(p->polar[id]) - p->ecc[sid] * sinf(p->polar[sid]);
+        float r = sqrtf(dx * dx + dy * dy);
+        r += wSpan > hSpan ? wSpan : hSpan;
+        R = r > R ? r : R;
+        const float coss = cosf(p->orient[sid]), sins = sinf(p->orient[sid]);
+        const float cosc = cosf(p->orient[id]), sinc = sinf(p->orient[id]);
+        const float ds = 2 * R / m1;
+        float sumC = 0.f, sumS = 0.f;
+        for (int s = 0; s < nUse; s++) {
+            const float lx = grid_at(s % m1, ds, R), ly = grid_at(s / m1, ds, R);
+            float x = cosc * (lx - dx) + sinc * (ly - dy), y = -sinc * (lx - dx) + cosc * (ly - dy);
+            swC[s] = gauss2(x, y, p->rw[id], p->rh[id]);
+            x = coss * lx + sins * ly;
+            y = -sins * lx + coss * ly;
+            swS[s] = gauss2(x, y, p->rw[sid], p->rh[sid]);
+            sumC += swC[s];
+            sumS += swS[s];
+        }
+        for (int s = 0; s < nUse; s++) {
+            swC[s] /= sumC;
+            swS[s] /= sumS;
+        }
+        const float *twC = TW + (size_t)cell * 2 * nKS, *twS = twC + nKS;
+        const float kc = p->k[id], ks = p->k[sid], cov = covariant[id];
+        double conv = 0.0;
+        for (int it = 0; it < nKS; it++) {
+            for (int s = 0; s < nUse; s++) {
+                const float lc = swC[s] * twC[it] * kc, ls = swS[s] * twS[it] * ks;
+                float decide;
+                if (fabsf(lc) > fabsf(ls)) decide = fabsf(lc) + ls * copysignf(cov, lc);
+                else decide = fabsf(ls) + lc * copysignf(cov, ls);
+                conv += decide;
+            }
+        }
+        maxConvol[id] = (float)conv;
+    }
+    free(swC);
+    free(swS);
+    return 0;
+}
+
+/* Per-frame centre and surround contrast sums of the parvo cells: layers [nLayer][3][h][w];
+ * cone [2][nParvo]; PS [nLayer][2][nParvo].  Both means are taken at the surround's
+ * coordinates, as src/discrete_input_convol.cu:1034-1035 samples them. */
+int orc_lgn_parvo_spatial(int nParvo, int nSample, const float *SW, const float *SC, const uint32_t *cone,
+                          const float *layers, int nLayer, int h, int w, int wbits, float *PS) {
+    const size_t npix = (size_t)w * h;
+    const size_t yOff = (size_t)nParvo * 2 * nSample;
+#pragma omp parallel for schedule(static)
+    for (int f = 0; f < nLayer; f++) {
+        const float *L = layers + (size_t)f * 3 * npix, *M = L + npix, *Sp = M + npix;
+        for (int cell = 0; cell < nParvo; cell++) {
+            const float *xC = SC + (size_t)cell * 2 * nSample, *yC = xC + yOff;
+            const float *xS = xC + nSample, *yS = xS + yOff;
+            const int tC = (int)cone[cell], tS = (int)cone[nParvo + cell];
+            float sumC = 0.f, sumS = 0.f;
+            for (int s = 0; s < nSample; s++) {
+                sumC += intensity(tC, L, M, Sp, w, h, xS[s], yS[s], wbits);
+                sumS += intensity(tS, L, M, Sp, w, h, xS[s], yS[s], wbits);
+            }
+            const float meanC = sumC / nSample, meanS = sumS / nSample;
+            float accC = 0.f, accS = 0.f;
+            for (int s = 0; s < nSample; s++) {
+                float I = intensity(tC, L, M, Sp, w, h, xC[s], yC[s], wbits);
+                float cc = meanC > 0 ? I / meanC - 1.0f : I;
+                if (fabsf(cc) > 1.0f) cc = copysignf(1.0f, cc);
+                accC += SW[s] * cc;
+                I = intensity(tS, L, M, Sp, w, h, xS[s], yS[s], wbits);
+                cc = meanS > 0 ? I / meanS - 1.0f : I;
+                if (fabsf(cc) > 1.0f) cc = copysignf(1.0f, cc);
+                accS += SW[s] * cc;
+            }
+            PS[((size_t)f * 2 + 0) * nParvo + cell] = accC;
+            PS[((size_t)f * 2 + 1) * nParvo + cell] = accS;
+        }
+    }
+    return 0;
+}
+
+/* LGN_convol_parvo for step it: sum over samples of (centre contrast x centre weight) and
+ * (surround contrast x surround weight), each times its k.  out [nParvo]. */
+int orc_lgn_parvo_convol(const pv1_lgn_config *c, const pv1_lgn_parvo_config *q, const pv1_lgn_params *p,
+                         int nFrame, long long it, const float *TW, const float *PS, float *out) {
+    const int nLGN = (int)c->nLGN, nParvo = (int)(c->nParvo_I + c->nParvo_C);
+    const int nKS = (int)q->nKernelSample;
+    int *rowOf = (int *)malloc(sizeof(int) * nKS);
+    window_rows(c, nKS, (int)q->iKernelSampleT0, (int)q->kernelSampleInterval, (int)q->parvoComp,
+                (int)q->frameOffset, nFrame, it, rowOf);
+    for (int cell = 0; cell < nParvo; cell++) {
+        const int id = cell < (int)c->nParvo_I ? cell : cell + (int)c->nMagno_I;
+        const float *twC = TW + (size_t)cell * 2 * nKS, *twS = twC + nKS;
+        float convC = 0.f, convS = 0.f;
+        for (int j = 0; j < nKS; j++) {
+            const size_t row = (size_t)rowOf[j] * 2 * nParvo;
+            convC += PS[row + cell] * twC[j];
+            convS += PS[row + nParvo + cell] * twS[j];
+        }
+        out[cell] = convC * p->k[id] + convS * p->k[nLGN + id];
+    }
+    free(rowOf);
+    return 0;
+}
+
+/* LGN_nonlinear + get_spike for every LGN cell of one step; convol [nLGN] by LGN id (magno
+ * entries already times |k|).  u: recorded uniforms [nLGN][cap] of this step, ucount [nLGN].
+ * Returns the number of cells whose draw count disagrees with the record (0 when the CPU and
+ * GPU took the same branches). */
 int orc_lgn_nonlinear(const pv1_lgn_config *c, const float *convol, const float *maxConvol,
                       const float *c50, const float *sharp, const float *la, const float *lb,
                       float *ltr, float *lnl, const float *u, const int32_t *ucount, int cap,
                       float *sInfo_out, float *fr_out) {
-    const int nMagno = (int)(c->nMagno_I + c->nMagno_C);
     int mismatch = 0;
-    for (int m = 0; m < nMagno; m++) {
-        int id = (int)c->nParvo_I + m;
-        if (m >= (int)c->nMagno_I) id += (int)c->nParvo_C;
+    for (int id = 0; id < (int)c->nLGN; id++) {
         const float mx = maxConvol[id];
-        float current = convol[m] * c->convolRatio;
+        float current = convol[id] * c->convolRatio;
         if (current < 0) current = 0;
         float X = (float)(1.0 / (double)(1 + expf(sharp[id] * (c50[id] - current / mx))));
         float fr = c->frRatio * mx * (la[id] * X + lb[id]);

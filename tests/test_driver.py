@@ -81,3 +81,20 @@ def test_run_writes_reference_outputs(written, native):
     b = open(P.patchV1_cfg, "rb").read()
     assert np.frombuffer(b[:4], np.uint32)[0] == 4
     assert np.frombuffer(b[4:16], np.float32).tolist() == [m.spec.vL, m.spec.vE, m.spec.vI]
+
+
+def test_parvo_cells_read_back():
+    """Parvo cells (LGN types 0-3 before the magno cells) go through the reference's files:
+    counts, component parameters, cone types, covariant and the parvo kernel grid."""
+    wl = synth.make_workload("parvo", seed=9, nblock=1, n_lgn=256, m=20, width=64, height=64, nt=48,
+                             nFrame=40, n_parvo=64, tau=300.0, nKernelSample=150)
+    d = tempfile.mkdtemp()
+    fn = synth.write_reference_files(wl, d, seed=3, nt=48)
+    m = driver.build(cfg.load(["-c", fn]))
+    L, L0 = m.lgn, wl.lgn
+    assert (L.nParvo_I, L.nMagno_I, L.nParvo_C, L.nMagno_C) == (64, 256, 0, 0)
+    assert L.nSample1D == L0.nSample1D and L.sched == L0.sched
+    assert L.sched.kernelSampleInterval == 16 and L.sched.pLongerThanM
+    for k in ("polar", "ecc", "rw", "rh", "orient", "k", "tauR", "tauD", "delay", "coneType", "covariant",
+              "c50", "sharpness"):
+        assert np.array_equal(getattr(L, k), getattr(L0, k)), k

@@ -215,3 +215,70 @@ def test_chunked_runs_identical(c1_small):
     finally:
         a.close()
         b.close()
+
+
+@pytest.fixture(scope="module")
+def parvo_wl(native):
+    """128 parvo (L/M opponent, centre and surround with their own kernels) + 512 magno cells;
+    parvo window 300 ms in 150 taps (interval 16 steps), magno 250 ms in 250 taps, so the two
+    windows have different frame tails (pLongerThanM, dFrame > 0)."""
+    from visual_cortex_gb300 import synth
+    return synth.make_workload("parvo", seed=9, nblock=1, n_lgn=512, m=20, width=64, height=64, nt=800,
+                               nFrame=120, n_parvo=128, tau=300.0, nKernelSample=150)
+
+
+def test_parvo_setup_tables(parvo_wl):
+    """store_PM(PM=0) and parvo_maxConvol on the GPU vs the oracle's restatement (including the
+    sample-grid rule and its partial last patch)."""
+    import oracle
+    from visual_cortex_gb300.model import Simulation
+    wl = parvo_wl
+    sim = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        TW, SW, SC = sim.lgn_parvo_tables()
+        _, _, _, mc = sim.lgn_tables()
+    finally:
+        sim.close()
+    lo = oracle.LgnOracle(wl.lgn, wl.stim)
+    assert lo.max_sample1d * lo.max_sample1d % 1024 != 0    # the partial-grid case is exercised
+    scale = np.abs(lo.pTW).max(axis=2, keepdims=True)
+    assert np.max(np.abs(TW - lo.pTW) / scale) < 1e-5
+    np.testing.assert_allclose(SW, lo.pSW, rtol=1e-5, atol=1e-8)
+    np.testing.assert_allclose(SC, lo.pSC, rtol=1e-6, atol=1e-6)
+    pid = wl.lgn.parvo_ids()
+    np.testing.assert_allclose(mc[pid], lo.maxConvol[pid], rtol=1e-5)
+    np.testing.assert_allclose(mc, lo.maxConvol, rtol=1e-5)
+
+
+def test_parvo_spatial_stage(parvo_wl):
+    import oracle
+    from visual_cortex_gb300.model import Simulation
+    wl = parvo_wl
+    sim = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        PS = sim.lgn_parvo_spatial()
+        _, SW, SC = sim.lgn_parvo_tables()
+    finally:
+        sim.close()
+    lo = oracle.LgnOracle(wl.lgn, wl.stim)
+    ref = lo.parvo_spatial(SW=SW, SC=SC)
+    assert np.abs(PS - ref).max() < 2e-4
+    assert np.abs(PS[-1]).max() < 1e-5
+    assert np.abs(PS[:-1]).max() > 1e-2
+
+
+def test_parvo_dynamics_parity(parvo_wl):
+    """LGN_convol_parvo + LGN_nonlinear + the V1 step with parvo inputs: LGN spikes identical,
+    rates within 1e-5, V1 rasters and traces as for the magno-only patch."""
+    from oracle.parity import run_parity, compare
+    wl = parvo_wl
+    res = run_parity(wl, RASTER_STEPS + 400, cap=8)
+    cmp = compare(res, wl.spec)
+    assert res["draw_count_mismatch"] == 0
+    assert cmp["lgn_spike_mismatch"] == 0, cmp
+    assert cmp["lgn_fr_maxrel"] < 1e-5, cmp
+    pid = wl.lgn.parvo_ids()
+    assert (res["gpu"]["lsp"][:, pid] >= 1).sum() > 0
+    assert_raster_ok(cmp)
+    for k in ("v", "gE", "gI", "gFF"):
+        assert cmp[f"max_rel_{k}"] < 1e-5, cmp

@@ -61,6 +61,12 @@ class LgnConfig(C.Structure):
     ]
 
 
+class LgnParvoConfig(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("nSample1D", "nKernelSample", "kernelSampleInterval",
+                                          "iKernelSampleT0", "parvoComp", "frameOffset")] + \
+               [("kernelSampleDt", C.c_float), ("kernelSampleT0", C.c_float)]
+
+
 _FP = C.POINTER(C.c_float)
 _UP = C.POINTER(C.c_uint32)
 
@@ -95,6 +101,10 @@ def _load() -> C.CDLL:
         "pv1_lgn_get_tables": ([P, _FP, _FP, _FP, _FP], C.c_int),
         "pv1_stimulus_load": ([P, C.c_uint32, C.c_uint32, C.c_uint32, _FP, _FP], C.c_int),
         "pv1_lgn_get_spatial": ([P, _FP], C.c_int),
+        "pv1_lgn_setup_parvo": ([P, C.POINTER(LgnConfig), C.POINTER(LgnParvoConfig), C.POINTER(LgnParams), _FP,
+                                 C.c_uint64], C.c_int),
+        "pv1_lgn_get_parvo_tables": ([P, _FP, _FP, _FP], C.c_int),
+        "pv1_lgn_get_parvo_spatial": ([P, _FP], C.c_int),
         "pv1_v1_set_lgn_synapses": ([P, C.c_uint32, _UP, _UP, _FP], C.c_int),
         "pv1_v1_set_near": ([P, C.c_uint32, _UP, _UP, _FP], C.c_int),
         "pv1_v1_set_far": ([P, _UP, _UP, _FP, _FP], C.c_int),

@@ -114,7 +114,7 @@ int issue(pv1_batch *b, int k, int minB, long long *launches) {
             if (!b->activeSet[q]) continue;
             e = launch_lgn_step(b->views[q].lp, b->views[q].d_stepBase, k, b->stream);
             if (e != cudaSuccess) return bfail(b, PV1_E_CUDA, std::string("lgn step: ") + cudaGetErrorString(e));
-            n += (b->views[q].lp.classCtw && k <= kClassMaxK) ? 1 : 2;
+            n += lgn_step_launches(b->views[q].lp, k);
         }
     }
     for (int s = 0; s < k; s++) {

@@ -127,6 +127,14 @@ struct LgnParams {
     int outSlots;
     float *recU; int *recUCount; int recCap; long long recStep0; int recSteps;
     int *err;
+    // parvocellular cells (nParvo = 0: none); parvo cell c is LGN id c or c + nMagno_I
+    int nParvo;
+    int pKS, pT0, pInterval;   // their kernel sampling
+    int parvoComp, pFrameOffset;
+    SegTable pseg;
+    const double *pctw;        // [2][pKS+1][nParvo] cumulative temporal weights (centre, surround)
+    const float *pS;           // [nFrame+1][2][nParvo] spatial stage per frame
+    const float *pk;           // [2][nParvo] amplitude k of centre and surround
 };
 
 struct V1Params {
@@ -202,8 +210,33 @@ struct SetupArgs {
     int *err;
 };
 
+// Parvo store_PM + parvo_maxConvol arguments.
+struct ParvoSetupArgs {
+    int nParvo, nLGN, nParvo_I, nMagno_I;
+    int nSample, nSample1D, nKS;
+    float kernelSampleDt, kernelSampleT0;
+    float normViewDistance, L_x0, L_y0, R_x0, R_y0, nsig;
+    const float *polar, *ecc, *rw, *rh, *orient, *k;
+    const float *ratio, *tauR, *tauD, *nR, *nD, *delay;
+    const float *covariant;
+    int maxSample1D;           // parvo_maxConvol sample grid (src/patch.cu:5299-5312)
+    float *TW;                 // [nParvo][2][nKS]
+    float *SW;                 // [nSample]
+    float *SC;                 // [2][nParvo][2][nSample]
+    float *maxConvol;          // [nLGN]
+    float *pk;                 // [2][nParvo]
+    double *pctw;              // [2][nKS+1][nParvo]
+    int *err;
+};
+
 // Launchers (defined next to their kernels).
 cudaError_t launch_lgn_setup(const SetupArgs &a, int blockThreads, cudaStream_t st);
+cudaError_t launch_parvo_setup(const ParvoSetupArgs &a, cudaStream_t st);
+cudaError_t launch_parvo_spatial(cudaTextureObject_t L, cudaTextureObject_t M, cudaTextureObject_t S,
+                                 const float *SW, const float *SC, const int *coneType, int nParvo,
+                                 int nSample, int nLayer, int row0, float *out, cudaStream_t st);
+// Kernel launches one launch_lgn_step of K steps issues.
+int lgn_step_launches(const LgnParams &p, int K);
 cudaError_t launch_lgn_rng_init(curandStateMRG32k3a *state, float *lnl, float *ltr,
                                 unsigned long long seed, int n, cudaStream_t st);
 cudaError_t launch_lgn_spatial(cudaTextureObject_t L, cudaTextureObject_t M, cudaTextureObject_t S,

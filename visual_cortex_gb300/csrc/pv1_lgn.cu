@@ -49,6 +49,21 @@ __device__ float block_sum(float v, float *scratch) {
 }
 
 
+constexpr double kSqrt2 = 1.4142135623730951;   // SQRT2 of src/CONST.h:30
+
+// Span of a Gaussian's sample grid: nsig * r / SQRT2 with the float product promoted to double
+// for the division, as the reference's expression evaluates.
+__device__ __forceinline__ float sample_span(float nsig, float r) {
+    return (float)((double)(nsig * r) / kSqrt2);
+}
+
+// Sample coordinate (i + 0.5) * d - span, evaluated in double as the reference's
+// `(threadIdx.x + 0.5)*dw - wSpan` is, then rounded once.
+__device__ __forceinline__ float grid_coord(int i, float d, float span) {
+    return (float)(((double)i + 0.5) * (double)d - (double)span);
+}
+
+
 
 // One CTA per magno cell, one thread per spatial sample (store_PM with PM=1,
 // src/discrete_input_convol.cu:427-744, store_temporalWeight :230-305).
@@ -111,8 +126,8 @@ __global__ void __launch_bounds__(1024) lgn_setup_kernel(SetupArgs A) {
     const float ds = 2 * span / A.nSample1D;
     const int tx = tid % A.nSample1D, ty = tid / A.nSample1D;
     const bool active = tid < nSample;
-    float cx = (tx + 0.5f) * ds - span;
-    float cy = (ty + 0.5f) * ds - span;
+    float cx = grid_coord(tx, ds, span);
+    float cy = grid_coord(ty, ds, span);
     float ttx = cx - ox, tty = cy - oy;
     float sx = ttx * rcos - tty * rsin;
     float sy = ttx * rsin + tty * rcos;
@@ -143,6 +158,154 @@ __global__ void __launch_bounds__(1024) lgn_setup_kernel(SetupArgs A) {
         }
     } else if (tid == 0) {
         atomicOr(A.err, kErrBounds);  // curved-retina geometry is not built (host rejects it)
+    }
+}
+
+// ---- parvocellular cells ---------------------------------------------------------------
+
+// One CTA per (parvo cell, component), one thread per spatial sample: store_PM with PM = 0
+// (src/discrete_input_convol.cu:427-520) -- the component's temporal weights
+// (store_temporalWeight :230-305, time reversed, L1 normalised), its texture coordinates on a
+// (2 nsig r/sqrt2)^2 grid around its own centre (store_spatialWeight :309-425, flat retina)
+// and, from the first cell's centre only, the normalised Gaussian SW every parvo cell shares.
+__global__ void __launch_bounds__(1024) lgn_parvo_setup_kernel(ParvoSetupArgs A) {
+    __shared__ float scratch[33];
+    const int cell = blockIdx.x, type = blockIdx.y;
+    const int tid = threadIdx.x;
+    const int nSample = A.nSample, n1 = A.nSample1D, nKS = A.nKS;
+    const int id = cell < A.nParvo_I ? cell : cell + A.nMagno_I;
+    const int lid = type * A.nLGN + id;
+    {
+        const float tauR = A.tauR[lid], tauD = A.tauD[lid], nR = A.nR[lid], nD = A.nD[lid];
+        const float ratio = A.ratio[lid];
+        const float lfac1 = lgammaf(nR), lfac2 = lgammaf(nD);
+        const float t0 = A.kernelSampleT0 - A.delay[lid];
+        float *tw_row = A.TW + ((size_t)cell * 2 + type) * nKS;
+        float local = 0.f;
+        for (int j = tid; j < nKS; j += blockDim.x) {
+            const int twid = nKS - 1 - j;
+            const float t = twid * A.kernelSampleDt + t0;
+            const float tw = t < 0 ? 0.0f : temporal_kernel(t, tauR, tauD, nR, nD, ratio, lfac1, lfac2);
+            tw_row[j] = tw;
+            local += fabsf(tw);
+        }
+        const float total = block_sum(local, scratch);
+        for (int j = tid; j < nKS; j += blockDim.x) tw_row[j] /= total;
+        __syncthreads();
+        if (tid == 0) {
+            double *c = A.pctw + (size_t)type * (nKS + 1) * A.nParvo + cell;
+            double acc = 0.0;
+            c[0] = 0.0;
+            for (int j = 0; j < nKS; j++) {
+                acc += (double)tw_row[j];
+                c[(size_t)(j + 1) * A.nParvo] = acc;
+            }
+            A.pk[type * A.nParvo + cell] = A.k[lid];
+        }
+    }
+    const float polar = A.polar[lid], ecc = A.ecc[lid];
+    const float rx = A.rw[lid], ry = A.rh[lid];
+    const float wSpan = sample_span(A.nsig, rx), hSpan = sample_span(A.nsig, ry);
+    const float dw = 2 * wSpan / n1, dh = 2 * hSpan / n1;
+    const bool active = tid < nSample;
+    const int tx = tid % n1, ty = tid / n1;
+    const float w = grid_coord(tx, dw, wSpan), h = grid_coord(ty, dh, hSpan);
+    if (cell == 0 && type == 0) {
+        const float sw = active ? gauss2(w, h, rx, ry) : 0.f;
+        const float sum = block_sum(sw, scratch);
+        if (active) A.SW[tid] = sw / sum;
+    }
+    const float coso = cosf(A.orient[lid]), sino = sinf(A.orient[lid]);
+    const bool left = cell < A.nParvo_I;
+    const float x0 = left ? A.L_x0 : A.R_x0, y0 = left ? A.L_y0 : A.R_y0;
+    if (active) {
+        const float x = x0 + (ecc * cosf(polar) + w * coso - h * sino) * A.normViewDistance;
+        const float y = y0 + (ecc * sinf(polar) + w * sino + h * coso) * A.normViewDistance;
+        const size_t sid = ((size_t)cell * 2 + type) * nSample + tid;
+        A.SC[sid] = x;
+        A.SC[(size_t)A.nParvo * 2 * nSample + sid] = y;
+    }
+}
+
+// max_convol of a parvo cell (parvo_maxConvol, src/discrete_input_convol.cu:748-883): centre
+// and surround Gaussians sampled on one maxSample1D^2 grid around the surround, each
+// normalised to unit sum, and the largest response a stimulus can drive through them, summed
+// over the temporal samples: at every (sample, tap) the dominant component at full contrast
+// plus the other one at the covariant fraction of it.  One CTA of 1024 threads per cell;
+// (maxSample1D^2 / 1024) * 1024 samples take part, as in the reference.  The sum is kept in
+// double per thread over the taps and reduced once (the reference reduces per tap in float).
+__global__ void __launch_bounds__(1024) lgn_parvo_maxconvol_kernel(ParvoSetupArgs A) {
+    extern __shared__ float swC[];
+    __shared__ double dscratch[33];
+    __shared__ float scratch[33];
+    const int cell = blockIdx.x;
+    const int id = cell < A.nParvo_I ? cell : cell + A.nMagno_I;
+    const int sid = A.nLGN + id;
+    const int n1 = A.maxSample1D;
+    const int nPatch = (n1 * n1) / (int)blockDim.x;
+    float *swS = swC + nPatch * blockDim.x;
+    const float rxs = A.rw[sid], rys = A.rh[sid], xs = A.polar[sid], ys = A.ecc[sid];
+    float wSpan = sample_span(A.nsig, rxs), hSpan = sample_span(A.nsig, rys);
+    const float rxc = A.rw[id], ryc = A.rh[id];
+    float R = wSpan > hSpan ? wSpan : hSpan;
+    const float xc = A.polar[id], yc = A.ecc[id];
+    wSpan = sample_span(A.nsig, rxc);
+    hSpan = sample_span(A.nsig, ryc);
+    const float dx = yc * cosf(xc) - ys * cosf(xs);
+    const float dy = yc * sinf(xc) - ys * sinf(xs);
+    float r = sqrtf(dx * dx + dy * dy);
+    const float cov = A.covariant[id];
+    r += wSpan > hSpan ? wSpan : hSpan;
+    R = r > R ? r : R;
+    const float coss = cosf(A.orient[sid]), sins = sinf(A.orient[sid]);
+    const float cosc = cosf(A.orient[id]), sinc = sinf(A.orient[id]);
+    const float ks = A.k[sid], kc = A.k[id];
+    const float ds = 2 * R / n1;
+    float sumC = 0.f, sumS = 0.f;
+    for (int ip = 0; ip < nPatch; ip++) {
+        const int pid = ip * blockDim.x + threadIdx.x;
+        const float lx = grid_coord(pid % n1, ds, R), ly = grid_coord(pid / n1, ds, R);
+        float x = cosc * (lx - dx) + sinc * (ly - dy);
+        float y = -sinc * (lx - dx) + cosc * (ly - dy);
+        const float c = gauss2(x, y, rxc, ryc);
+        swC[pid] = c;
+        sumC += block_sum(c, scratch);
+        x = coss * lx + sins * ly;
+        y = -sins * lx + coss * ly;
+        const float s = gauss2(x, y, rxs, rys);
+        swS[pid] = s;
+        sumS += block_sum(s, scratch);
+    }
+    __syncthreads();
+    for (int ip = 0; ip < nPatch; ip++) {
+        const int pid = ip * blockDim.x + threadIdx.x;
+        swC[pid] /= sumC;
+        swS[pid] /= sumS;
+    }
+    __syncthreads();
+    const float *twC = A.TW + (size_t)cell * 2 * A.nKS, *twS = twC + A.nKS;
+    double acc = 0.0;
+    for (int it = 0; it < A.nKS; it++) {
+        const float tc = twC[it], ts = twS[it];
+        for (int ip = 0; ip < nPatch; ip++) {
+            const int pid = ip * blockDim.x + threadIdx.x;
+            const float lc = swC[pid] * tc * kc;
+            const float ls = swS[pid] * ts * ks;
+            float decide;
+            if (fabsf(lc) > fabsf(ls)) decide = fabsf(lc) + ls * copysignf(cov, lc);
+            else decide = fabsf(ls) + lc * copysignf(cov, ls);
+            acc += (double)decide;
+        }
+    }
+    // block sum in double
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) dscratch[warp] = acc;
+    __syncthreads();
+    if (warp == 0) {
+        double t = lane < (int)(blockDim.x >> 5) ? dscratch[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) A.maxConvol[id] = (float)t;
     }
 }
 
@@ -209,6 +372,55 @@ __global__ void __launch_bounds__(256) lgn_spatial_kernel(
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) S[(size_t)(row0 + li) * nMagno + cell] = acc;
+}
+
+// Parvo spatial stage, once per (frame, cell): the mean luminances of the centre and the
+// surround cone types -- both sampled at the surround's coordinates, as
+// src/discrete_input_convol.cu:1034-1035 reads them -- then the clipped local contrast of
+// each component at its own coordinates, weighted by the shared Gaussian SW and summed
+// (:1151-1209).  One warp per (cell, frame).  PS [row][2][nParvo].
+__global__ void __launch_bounds__(256) lgn_parvo_spatial_kernel(
+    cudaTextureObject_t texL, cudaTextureObject_t texM, cudaTextureObject_t texS,
+    const float *__restrict__ SW, const float *__restrict__ SC, const int *__restrict__ coneType,
+    int nParvo, int nSample, int nLayer, int row0, float *__restrict__ PS) {
+    const int lane = threadIdx.x & 31;
+    const int cell = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int li = blockIdx.y;
+    if (cell >= nParvo || li >= nLayer) return;
+    const size_t yOff = (size_t)nParvo * 2 * nSample;
+    const float *xC = SC + (size_t)cell * 2 * nSample, *yC = xC + yOff;
+    const float *xS = xC + nSample, *yS = xS + yOff;
+    const int typeC = coneType[cell], typeS = coneType[nParvo + cell];
+    float sumC = 0.f, sumS = 0.f;
+    for (int s = lane; s < nSample; s += 32) {
+        sumC += intensity(typeC, xS[s], yS[s], li, texL, texM, texS);
+        sumS += intensity(typeS, xS[s], yS[s], li, texL, texM, texS);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sumC += __shfl_xor_sync(0xffffffffu, sumC, o);
+        sumS += __shfl_xor_sync(0xffffffffu, sumS, o);
+    }
+    const float meanC = sumC / nSample, meanS = sumS / nSample;
+    float accC = 0.f, accS = 0.f;
+    for (int s = lane; s < nSample; s += 32) {
+        const float sw = SW[s];
+        float I = intensity(typeC, xC[s], yC[s], li, texL, texM, texS);
+        float c = meanC > 0 ? I / meanC - 1.0f : I;
+        if (fabsf(c) > 1.0f) c = copysignf(1.0f, c);
+        accC += sw * c;
+        I = intensity(typeS, xS[s], yS[s], li, texL, texM, texS);
+        c = meanS > 0 ? I / meanS - 1.0f : I;
+        if (fabsf(c) > 1.0f) c = copysignf(1.0f, c);
+        accS += sw * c;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        accC += __shfl_xor_sync(0xffffffffu, accC, o);
+        accS += __shfl_xor_sync(0xffffffffu, accS, o);
+    }
+    if (lane == 0) {
+        PS[((size_t)(row0 + li) * 2 + 0) * nParvo + cell] = accC;
+        PS[((size_t)(row0 + li) * 2 + 1) * nParvo + cell] = accS;
+    }
 }
 
 // Row of S held by the texture layer `x` positions after the newest frame's layer at step it.
@@ -412,14 +624,70 @@ __global__ void __launch_bounds__(256) lgn_rate_kernel(LgnParams P, const long l
     if (P.outFr) P.outFr[(size_t)(it % P.outSlots) * P.nLGN + id] = fr;
 }
 
-// Exact-time Poisson spikes for K consecutive steps; one thread per magno cell carries the
-// rate integral and its generator across the steps in registers (get_spike,
-// src/discrete_input_convol.cu:1589-1619, and the write-back of :1750-1771).
+// Parvo temporal contraction and logistic rate for (cell, step) pairs of a chunk of K steps:
+// LGN_convol_parvo's sum over the window's samples of (centre contrast x centre weight) and
+// (surround contrast x surround weight), times k of each (src/discrete_input_convol.cu:
+// 1143-1327), on the parvo kernel grid (nKernelSample, interval, T0) and the parvo frame tail
+// (getTail with parvoComp and (1-pLongerThanM)*dFrame, src/patch.cu:5399-5422, 6068), then
+// LGN_nonlinear's rate.  Same segment form as lgn_rate_kernel.
+__global__ void __launch_bounds__(256) lgn_parvo_rate_kernel(LgnParams P, const long long *stepBase) {
+    __shared__ int s_row[kMaxSeg];
+    __shared__ int s_j[kMaxSeg + 1];
+    const int s = blockIdx.y;
+    const long long it = *stepBase + s;
+    const FrameSched fs = P.fs;
+    const int currentFrame = frames_read_after_step(fs, it);
+    const int phase = (int)((P.parvoComp + (it + 1) * (long long)fs.denorm) % fs.ntPerFrame);
+    const int tailExtra = P.pFrameOffset + (phase <= P.parvoComp ? 2 : 1);
+    const int nseg = P.pseg.nseg[phase];
+    if (threadIdx.x < nseg)
+        s_row[threadIdx.x] = frame_row(fs, currentFrame, tailExtra + P.pseg.rel[(size_t)phase * P.pseg.maxSeg + threadIdx.x]);
+    if (threadIdx.x <= nseg) s_j[threadIdx.x] = P.pseg.j0[(size_t)phase * (P.pseg.maxSeg + 1) + threadIdx.x];
+    __syncthreads();
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.nParvo) return;
+    const int id = cell < P.nParvo_I ? cell : cell + P.nMagno_I;
+    const size_t np = P.nParvo;
+    const double *__restrict__ ctwC = P.pctw + cell;
+    const double *__restrict__ ctwS = ctwC + (size_t)(P.pKS + 1) * np;
+    const float *__restrict__ S = P.pS + cell;
+    float convolC = 0.f, convolS = 0.f;
+    double caC = ctwC[(size_t)s_j[0] * np], caS = ctwS[(size_t)s_j[0] * np];
+#pragma unroll 2
+    for (int q = 0; q < nseg; q++) {
+        const double cbC = ctwC[(size_t)s_j[q + 1] * np], cbS = ctwS[(size_t)s_j[q + 1] * np];
+        const size_t row = (size_t)s_row[q] * 2 * np;
+        convolC += S[row] * (float)(cbC - caC);
+        convolS += S[row + np] * (float)(cbS - caS);
+        caC = cbC;
+        caS = cbS;
+    }
+    const float convol = convolC * P.pk[cell] + convolS * P.pk[np + cell];
+    // LGN_nonlinear (src/discrete_input_convol.cu:1660-1730)
+    const float mx = P.maxConvol[id];
+    float current = convol * P.convolRatio;
+    if (current < 0) current = 0;
+    const float X = (float)(1.0 / (double)(1 + expf(P.sharp[id] * (P.c50[id] - current / mx))));
+    const float fr = P.frRatio * mx * (P.la[id] * X + P.lb[id]);
+    P.rate[(size_t)s * P.nLGN + id] = fr;
+    if (P.outFr) P.outFr[(size_t)(it % P.outSlots) * P.nLGN + id] = fr;
+}
+
+// Exact-time Poisson spikes for K consecutive steps; one thread per cell carries the rate
+// integral and its generator across the steps in registers (get_spike,
+// src/discrete_input_convol.cu:1589-1619, and the write-back of :1750-1771).  blockIdx.y = 0:
+// magno cells, 1: parvo cells.
 __global__ void __launch_bounds__(256) lgn_spike_kernel(LgnParams P, const long long *stepBase, int K) {
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= P.nMagno) return;
-    int id = P.nParvo_I + cell;
-    if (cell >= P.nMagno_I) id += P.nParvo_C;
+    int id;
+    if (blockIdx.y == 0) {
+        if (cell >= P.nMagno) return;
+        id = P.nParvo_I + cell;
+        if (cell >= P.nMagno_I) id += P.nParvo_C;
+    } else {
+        if (cell >= P.nParvo) return;
+        id = cell < P.nParvo_I ? cell : cell + P.nMagno_I;
+    }
     float ltr = P.leftTimeRate[id];
     float lnl = P.lastNegLogRand[id];
     curandStateMRG32k3a st = P.state[id];
@@ -498,7 +766,55 @@ cudaError_t launch_lgn_rate_only(const LgnParams &p, const long long *stepBase, 
     return cudaGetLastError();
 }
 
+cudaError_t launch_parvo_setup(const ParvoSetupArgs &a, cudaStream_t st) {
+    if (a.nParvo <= 0) return cudaSuccess;
+    const int threads = ((a.nSample + 31) / 32) * 32;
+    lgn_parvo_setup_kernel<<<dim3(a.nParvo, 2), threads, 0, st>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int nPatch = a.maxSample1D * a.maxSample1D / 1024;
+    const size_t smem = (size_t)2 * nPatch * 1024 * sizeof(float);
+    if (smem > 48 * 1024) {
+        e = cudaFuncSetAttribute(lgn_parvo_maxconvol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    lgn_parvo_maxconvol_kernel<<<a.nParvo, 1024, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_parvo_spatial(cudaTextureObject_t L, cudaTextureObject_t M, cudaTextureObject_t S,
+                                 const float *SW, const float *SC, const int *coneType, int nParvo,
+                                 int nSample, int nLayer, int row0, float *out, cudaStream_t st) {
+    if (nParvo <= 0) return cudaSuccess;
+    dim3 grid((nParvo + 7) / 8, nLayer);
+    lgn_parvo_spatial_kernel<<<grid, 256, 0, st>>>(L, M, S, SW, SC, coneType, nParvo, nSample, nLayer, row0, out);
+    return cudaGetLastError();
+}
+
+int lgn_step_launches(const LgnParams &p, int K) {
+    if (p.nParvo == 0) {
+        if (p.nMagno <= 0) return 0;
+        if (p.classCtw && K <= kClassMaxK) return 1;
+        return 2;
+    }
+    return (p.nMagno > 0) + 2;
+}
+
 cudaError_t launch_lgn_step(const LgnParams &p, const long long *stepBase, int K, cudaStream_t st) {
+    if (p.nParvo > 0) {
+        cudaError_t e;
+        if (p.nMagno > 0) {
+            lgn_rate_kernel<<<dim3((p.nMagno + 255) / 256, K), 256, 0, st>>>(p, stepBase);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+        lgn_parvo_rate_kernel<<<dim3((p.nParvo + 255) / 256, K), 256, 0, st>>>(p, stepBase);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        const int n = std::max(p.nMagno, p.nParvo);
+        lgn_spike_kernel<<<dim3((n + 255) / 256, 2), 256, 0, st>>>(p, stepBase, K);
+        return cudaGetLastError();
+    }
     if (p.nMagno <= 0) return cudaSuccess;
     if (p.classCtw && K <= kClassMaxK) {
         const size_t smem = (size_t)kClassMaxSlots * kClassCta * sizeof(float);

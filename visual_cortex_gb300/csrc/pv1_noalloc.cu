@@ -109,6 +109,8 @@ extern "C" int pv1_lgn_spikes_noalloc(pv1_plan *plan, uint32_t nsteps, float *d_
     PlanLgnView view;
     int r = plan_lgn_view(plan, &view);
     if (r) return r;
+    if (view.lp.nParvo > 0)
+        return plan_fail(plan, PV1_E_UNSUPPORTED, "pv1_lgn_spikes_noalloc: plans with parvo cells are not supported");
     const size_t need = (size_t)nsteps * (size_t)view.lp.nLGN;
     if (need > kNoAllocRateFloats)
         return plan_fail(plan, PV1_E_ARG,

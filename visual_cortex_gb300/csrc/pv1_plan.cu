@@ -41,6 +41,11 @@ struct pv1_plan {
     float *d_TW = nullptr, *d_SW = nullptr, *d_SC = nullptr, *d_maxConvol = nullptr;
     float *d_S = nullptr;
     int *d_coneType = nullptr;
+    // parvocellular cells
+    pv1_lgn_parvo_config pcfg{};
+    int nParvo = 0, pSample = 0;
+    float *d_pTW = nullptr, *d_pSW = nullptr, *d_pSC = nullptr, *d_pS = nullptr;
+    int *d_pCone = nullptr;
     int nFrame = 0;
     // LGN spike ring
     float *d_lgnRing = nullptr, *d_lgnFr = nullptr;
@@ -140,7 +145,7 @@ void drop_graph(pv1_plan *p) {
 int issue_chunk(pv1_plan *p, int k, int deliverFirst, long long *launches) {
     cudaError_t e = launch_lgn_step(p->lp, p->d_stepBase, k, p->stream);
     if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("lgn_step: ") + cudaGetErrorString(e));
-    long long n = (p->lp.classCtw && k <= kClassMaxK) ? 1 : 2;
+    long long n = lgn_step_launches(p->lp, k);
     if (p->persistent) {
         e = launch_v1_persistent(p->vp, p->d_stepBase, k, p->d_lgnRing, p->lgnSlots, deliverFirst, p->d_barrier,
                                  p->stream);
@@ -163,17 +168,16 @@ int issue_chunk(pv1_plan *p, int k, int deliverFirst, long long *launches) {
 // Builds the per-phase segment table of the temporal kernel: for phase p the sample j sits
 // (T0 + j*interval)*denorm + p units of dt/denorm after the window tail, i.e. in the frame
 // rel = that / ntPerFrame after the tail frame (src/discrete_input_convol.cu:1442-1540).
-void build_segments(const pv1_lgn_config &c, std::vector<int> &nseg, std::vector<int> &rel,
-                    std::vector<int> &j0, int &maxSeg) {
-    const int nPhase = (int)c.ntPerFrame;
-    const int nKS = (int)c.nKernelSample;
+void build_segments(int nKS, int T0, int interval, int denorm, int ntPerFrame, std::vector<int> &nseg,
+                    std::vector<int> &rel, std::vector<int> &j0, int &maxSeg) {
+    const int nPhase = ntPerFrame;
     std::vector<std::vector<int>> relv(nPhase), j0v(nPhase);
     maxSeg = 1;
     for (int ph = 0; ph < nPhase; ph++) {
         int last = -1;
         for (int j = 0; j < nKS; j++) {
-            long long o = (long long)(c.iKernelSampleT0 + (long long)j * c.kernelSampleInterval) * c.denorm + ph;
-            int r = (int)(o / c.ntPerFrame);
+            long long o = (long long)(T0 + (long long)j * interval) * denorm + ph;
+            int r = (int)(o / ntPerFrame);
             if (r != last) {
                 relv[ph].push_back(r);
                 j0v[ph].push_back(j);
@@ -374,12 +378,49 @@ void pv1_plan_destroy(pv1_plan *p) {
     delete p;
 }
 
-int pv1_lgn_setup(pv1_plan *p, const pv1_lgn_config *lc, const pv1_lgn_params *prm, uint64_t seed) {
+namespace {
+
+// Sample grid of parvo_maxConvol (src/patch.cu:5266-5312): round(mean size ratio of the
+// surround-enclosing square to the centre's) * nSpatialSample1D per side, at least 32, at
+// most what 48 KB of shared memory holds.  The mean runs over the cells of cone type < 4 --
+// the reference's loop also counts L+M magno cells -- and is divided by nParvo.
+int parvo_max_sample1d(const pv1_lgn_config &c, const pv1_lgn_params &prm, int nParvo, int n1) {
+    const int nLGN = (int)c.nLGN;
+    const float nsig = std::fabs(c.nsig);
+    auto span = [&](float r) { return (float)((double)(nsig * r) / 1.4142135623730951); };
+    float meanRatio = 0.f;
+    for (int i = 0; i < nLGN; i++) {
+        if (prm.coneType[i] >= 4) continue;
+        const float dx = prm.ecc[i] * std::cos(prm.polar[i]) - prm.ecc[nLGN + i] * std::cos(prm.polar[nLGN + i]);
+        const float dy = prm.ecc[i] * std::sin(prm.polar[i]) - prm.ecc[nLGN + i] * std::sin(prm.polar[nLGN + i]);
+        float r = std::sqrt(dx * dx + dy * dy);
+        float wSpan = span(prm.rw[nLGN + i]), hSpan = span(prm.rh[nLGN + i]);
+        float R = wSpan > hSpan ? wSpan : hSpan;
+        wSpan = span(prm.rw[i]);
+        hSpan = span(prm.rh[i]);
+        r += wSpan > hSpan ? wSpan : hSpan;
+        R = r > R ? r : R;
+        meanRatio += std::sqrt(R * R / wSpan / hSpan);
+    }
+    meanRatio /= nParvo;
+    long long m1 = (long long)std::round(meanRatio) * n1;
+    if (m1 * m1 < 1024) return 32;
+    const size_t avail = 48 * 1024 - 32 * sizeof(float);
+    if ((size_t)(m1 * m1) * 2 * sizeof(float) > avail)
+        m1 = (long long)std::floor(std::sqrt((double)(avail / sizeof(float) / 2 / (size_t)(n1 * n1)))) * n1;
+    return (int)m1;
+}
+
+int lgn_setup_impl(pv1_plan *p, const pv1_lgn_config *lc, const pv1_lgn_parvo_config *pc,
+                   const pv1_lgn_params *prm, const float *covariant, uint64_t seed) {
     if (!p || !lc || !prm) return PV1_E_ARG;
     const pv1_lgn_config &c = *lc;
     const int nParvo = (int)(c.nParvo_I + c.nParvo_C);
     const int nMagno = (int)(c.nMagno_I + c.nMagno_C);
-    if (nParvo > 0) return fail(p, PV1_E_UNSUPPORTED, "parvocellular LGN cells are not built");
+    if (nParvo > 0 && !pc) return fail(p, PV1_E_UNSUPPORTED, "parvocellular LGN cells need pv1_lgn_setup_parvo");
+    if (nParvo > 0 && !covariant) return fail(p, PV1_E_ARG, "parvo cells need the covariant array");
+    if (nParvo > 0 && (pc->nSample1D < 1 || pc->nSample1D > 32 || pc->nKernelSample < 1))
+        return fail(p, PV1_E_ARG, "parvo nSample1D must be in [1,32] and nKernelSample >= 1");
     if (!c.flat_retina) return fail(p, PV1_E_UNSUPPORTED, "curved-retina sample geometry is not built (flat_retina=1 only)");
     if ((int)c.nLGN != nParvo + nMagno) return fail(p, PV1_E_ARG, "nLGN != nParvo + nMagno");
     if (c.mSample1D < 1 || c.mSample1D > 32) return fail(p, PV1_E_ARG, "mSample1D must be in [1,32]");
@@ -494,7 +535,8 @@ int pv1_lgn_setup(pv1_plan *p, const pv1_lgn_config *lc, const pv1_lgn_params *p
     // segment table
     std::vector<int> nseg, rel, j0;
     int maxSeg = 1;
-    build_segments(c, nseg, rel, j0, maxSeg);
+    build_segments(nKS, (int)c.iKernelSampleT0, (int)c.kernelSampleInterval, (int)c.denorm, (int)c.ntPerFrame,
+                   nseg, rel, j0, maxSeg);
     if (maxSeg > kMaxSeg) return fail(p, PV1_E_UNSUPPORTED, "temporal window spans more than 255 frames");
     r = dev_alloc(p, &L.rate, (size_t)p->K * nLGN);
     if (r) return r;
@@ -532,12 +574,102 @@ int pv1_lgn_setup(pv1_plan *p, const pv1_lgn_config *lc, const pv1_lgn_params *p
     L.outFr = nullptr;
     L.outSlots = p->lgnSlots;
     p->vp.lgnN = nLGN;
+    // parvocellular cells: store_PM(PM=0) and parvo_maxConvol, their own segment table
+    p->nParvo = nParvo;
+    L.nParvo = nParvo;
+    float *d_cov = nullptr;
+    if (nParvo > 0) {
+        const pv1_lgn_parvo_config &q = *pc;
+        p->pcfg = q;
+        const int n1 = (int)q.nSample1D, pKS = (int)q.nKernelSample;
+        p->pSample = n1 * n1;
+        std::vector<int> pcone(2 * (size_t)nParvo);
+        for (int cc = 0; cc < nParvo; cc++) {
+            const int id = cc < (int)c.nParvo_I ? cc : cc + (int)c.nMagno_I;
+            pcone[cc] = (int)prm->coneType[id];
+            pcone[nParvo + cc] = (int)prm->coneType[nLGN + id];
+            if (pcone[cc] > 4 || pcone[nParvo + cc] > 4) return fail(p, PV1_E_ARG, "cone type > 4");
+        }
+        float *d_pk;
+        double *d_pctw;
+        r = 0;
+        r |= dev_upload(p, &p->d_pCone, pcone.data(), pcone.size());
+        r |= dev_upload(p, &d_cov, covariant, nLGN);
+        r |= dev_alloc(p, &p->d_pTW, (size_t)nParvo * 2 * pKS);
+        r |= dev_alloc(p, &p->d_pSW, (size_t)p->pSample);
+        r |= dev_alloc(p, &p->d_pSC, (size_t)2 * nParvo * 2 * p->pSample);
+        r |= dev_alloc(p, &d_pk, (size_t)2 * nParvo);
+        r |= dev_alloc(p, &d_pctw, (size_t)2 * (pKS + 1) * nParvo);
+        if (r) return fail(p, PV1_E_NOMEM, "parvo LGN allocation failed");
+        ParvoSetupArgs PA{};
+        PA.nParvo = nParvo;
+        PA.nLGN = nLGN;
+        PA.nParvo_I = (int)c.nParvo_I;
+        PA.nMagno_I = (int)c.nMagno_I;
+        PA.nSample = p->pSample;
+        PA.nSample1D = n1;
+        PA.nKS = pKS;
+        PA.kernelSampleDt = q.kernelSampleDt;
+        PA.kernelSampleT0 = q.kernelSampleT0;
+        PA.normViewDistance = c.normViewDistance;
+        PA.L_x0 = c.L_x0;
+        PA.L_y0 = c.L_y0;
+        PA.R_x0 = c.R_x0;
+        PA.R_y0 = c.R_y0;
+        PA.nsig = c.nsig;
+        PA.polar = d_par[0];
+        PA.ecc = d_par[1];
+        PA.rw = d_par[2];
+        PA.rh = d_par[3];
+        PA.orient = d_par[4];
+        PA.k = d_par[5];
+        PA.ratio = d_par[6];
+        PA.tauR = d_par[7];
+        PA.tauD = d_par[8];
+        PA.nR = d_par[9];
+        PA.nD = d_par[10];
+        PA.delay = d_par[11];
+        PA.covariant = d_cov;
+        PA.maxSample1D = parvo_max_sample1d(c, *prm, nParvo, n1);
+        PA.TW = p->d_pTW;
+        PA.SW = p->d_pSW;
+        PA.SC = p->d_pSC;
+        PA.maxConvol = p->d_maxConvol;
+        PA.pk = d_pk;
+        PA.pctw = d_pctw;
+        PA.err = p->d_err;
+        PV1_CUDA(p, launch_parvo_setup(PA, p->stream));
+        std::vector<int> pnseg, prel, pj0;
+        int pMaxSeg = 1;
+        build_segments(pKS, (int)q.iKernelSampleT0, (int)q.kernelSampleInterval, (int)c.denorm, (int)c.ntPerFrame,
+                       pnseg, prel, pj0, pMaxSeg);
+        if (pMaxSeg > kMaxSeg) return fail(p, PV1_E_UNSUPPORTED, "parvo temporal window spans more than 255 frames");
+        int *d_pnseg, *d_prel, *d_pj0;
+        r = 0;
+        r |= dev_upload(p, &d_pnseg, pnseg.data(), pnseg.size());
+        r |= dev_upload(p, &d_prel, prel.data(), prel.size());
+        r |= dev_upload(p, &d_pj0, pj0.data(), pj0.size());
+        if (r) return r;
+        L.pseg.nPhase = (int)c.ntPerFrame;
+        L.pseg.maxSeg = pMaxSeg;
+        L.pseg.nseg = d_pnseg;
+        L.pseg.rel = d_prel;
+        L.pseg.j0 = d_pj0;
+        L.pKS = pKS;
+        L.pT0 = (int)q.iKernelSampleT0;
+        L.pInterval = (int)q.kernelSampleInterval;
+        L.parvoComp = (int)q.parvoComp;
+        L.pFrameOffset = (int)q.frameOffset;
+        L.pctw = d_pctw;
+        L.pk = d_pk;
+    }
     PV1_CUDA(p, cudaStreamSynchronize(p->stream));
     for (int q = 0; q < 12; q++) free_one(p, d_par[q]);
+    if (d_cov) free_one(p, d_cov);
     // one temporal-kernel class (every magno cell has bit-identical temporal weights): the
     // fused single-class LGN kernel applies
     L.classCtw = nullptr;
-    if (nMagno > 0) {
+    if (nMagno > 0 && nParvo == 0) {
         std::vector<float> tw((size_t)nMagno * nKS);
         PV1_CUDA(p, cudaMemcpy(tw.data(), p->d_TW, tw.size() * sizeof(float), cudaMemcpyDeviceToHost));
         bool same = true;
@@ -557,6 +689,39 @@ int pv1_lgn_setup(pv1_plan *p, const pv1_lgn_config *lc, const pv1_lgn_params *p
     if (e) return e;
     p->lgnReady = true;
     drop_graph(p);
+    return PV1_OK;
+}
+
+}  // namespace
+
+int pv1_lgn_setup(pv1_plan *p, const pv1_lgn_config *lc, const pv1_lgn_params *prm, uint64_t seed) {
+    return lgn_setup_impl(p, lc, nullptr, prm, nullptr, seed);
+}
+
+int pv1_lgn_setup_parvo(pv1_plan *p, const pv1_lgn_config *lc, const pv1_lgn_parvo_config *pc,
+                        const pv1_lgn_params *prm, const float *covariant, uint64_t seed) {
+    if (!pc || !covariant) return p ? fail(p, PV1_E_ARG, "missing parvo config or covariant") : PV1_E_ARG;
+    return lgn_setup_impl(p, lc, pc, prm, covariant, seed);
+}
+
+int pv1_lgn_get_parvo_tables(pv1_plan *p, float *TW, float *SW, float *SC) {
+    if (!p) return PV1_E_ARG;
+    if (!p->lgnReady) return fail(p, PV1_E_STATE, "LGN not set up");
+    if (p->nParvo == 0) return fail(p, PV1_E_STATE, "no parvo cells");
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    const size_t np = p->nParvo, ns = p->pSample;
+    if (TW) PV1_CUDA(p, cudaMemcpy(TW, p->d_pTW, np * 2 * p->pcfg.nKernelSample * sizeof(float), cudaMemcpyDeviceToHost));
+    if (SW) PV1_CUDA(p, cudaMemcpy(SW, p->d_pSW, ns * sizeof(float), cudaMemcpyDeviceToHost));
+    if (SC) PV1_CUDA(p, cudaMemcpy(SC, p->d_pSC, 4 * np * ns * sizeof(float), cudaMemcpyDeviceToHost));
+    return PV1_OK;
+}
+
+int pv1_lgn_get_parvo_spatial(pv1_plan *p, float *PS) {
+    if (!p || !PS) return PV1_E_ARG;
+    if (!p->stimReady) return fail(p, PV1_E_STATE, "no stimulus loaded");
+    if (p->nParvo == 0) return fail(p, PV1_E_STATE, "no parvo cells");
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    PV1_CUDA(p, cudaMemcpy(PS, p->d_pS, (size_t)(p->nFrame + 1) * 2 * p->nParvo * sizeof(float), cudaMemcpyDeviceToHost));
     return PV1_OK;
 }
 
@@ -582,6 +747,11 @@ int pv1_stimulus_load(pv1_plan *p, uint32_t nFrame, uint32_t height, uint32_t wi
     if (p->d_S) free_one(p, p->d_S);
     int r = dev_alloc(p, &p->d_S, (size_t)(nFrame + 1) * std::max(nMagno, 1));
     if (r) return r;
+    if (p->nParvo > 0) {
+        if (p->d_pS) free_one(p, p->d_pS);
+        r = dev_alloc(p, &p->d_pS, (size_t)(nFrame + 1) * 2 * p->nParvo);
+        if (r) return r;
+    }
     const size_t npix = (size_t)width * height;
     // process the movie in batches of <= 2047 layers plus the initial-luminance layer
     const int maxLayers = 2048;
@@ -625,6 +795,9 @@ int pv1_stimulus_load(pv1_plan *p, uint32_t nFrame, uint32_t height, uint32_t wi
         if (nMagno > 0)
             PV1_CUDA(p, launch_lgn_spatial(tex[0], tex[1], tex[2], p->d_SW, p->d_SC, p->d_coneType, nMagno,
                                           p->mSample, 0, (int)nl, (int)f0, p->d_S, p->stream));
+        if (p->nParvo > 0)
+            PV1_CUDA(p, launch_parvo_spatial(tex[0], tex[1], tex[2], p->d_pSW, p->d_pSC, p->d_pCone, p->nParvo,
+                                            p->pSample, (int)nl, (int)f0, p->d_pS, p->stream));
         PV1_CUDA(p, cudaStreamSynchronize(p->stream));
         for (int ch = 0; ch < 3; ch++) {
             cudaDestroyTextureObject(tex[ch]);
@@ -633,6 +806,7 @@ int pv1_stimulus_load(pv1_plan *p, uint32_t nFrame, uint32_t height, uint32_t wi
     }
     p->nFrame = (int)nFrame;
     p->lp.S = p->d_S;
+    p->lp.pS = p->d_pS;
     p->lp.fs.nFrame = (int)nFrame;
     p->lp.fs.initRow = (int)nFrame;
     p->stimReady = true;

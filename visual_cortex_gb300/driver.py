@@ -237,18 +237,24 @@ def build(c: Config) -> Model:
     nLGN = nI_ + nC_
     if max_ecc > stim_f.range:
         raise ConfigError(f"max_ecc: {max_ecc} must not be larger than {stim_f.range}")
-    if np.any(LGNtype < 4):
-        raise ConfigError("not supported by this build: parvocellular LGN cells")
+    # cell order parvo_I, magno_I, parvo_C, magno_C (src/patch.cu:1723-1750)
+    parvo = np.asarray(LGNtype) < 4
+    nParvo_I, nParvo_C = int(parvo[:nI_].sum()), int(parvo[nI_:].sum())
+    if not (np.all(parvo[:nParvo_I]) and np.all(parvo[nI_:nI_ + nParvo_C])):
+        raise ConfigError("LGN_vpos: parvo cells must come before the magno cells of each eye")
+    if nC_ and nParvo_I + nParvo_C:
+        raise ConfigError("not supported by this build: parvo cells with a second eye")
     prm = FM.read_lgn_params(P.lgn, nLGN)
     extent = f32(2) * (f32(stim_f.range) + f32(stim_f.buffer))
     normEcc = f32(f32(max_ecc) / extent)
     nvd = float(f32(f32(normEcc / f32(max_ecc)) / f32(DEG)))
     sched = make_schedule(c.dt, c.frameRate, c.tau, c.mau, c.nKernelSample, c.mKernelSample)
-    lgn = LgnSpec(nParvo_I=0, nMagno_I=nI_, nParvo_C=0, nMagno_C=nC_,
+    lgn = LgnSpec(nParvo_I=nParvo_I, nMagno_I=nI_ - nParvo_I, nParvo_C=nParvo_C, nMagno_C=nC_ - nParvo_C,
                   mSample1D=c.mSpatialSample1D, sched=sched,
                   **{k: prm[k] for k in FM.LGN_FIELDS2 + FM.LGN_FIELDS1 + ("coneType",)},
                   normViewDistance=nvd, L_x0=0.5, L_y0=0.5, R_x0=1.0, R_y0=1.0, nsig=c.nsig,
-                  convolRatio=c.convolRatio, frRatio=c.frRatioLGN, flat_retina=True)
+                  convolRatio=c.convolRatio, frRatio=c.frRatioLGN, flat_retina=True,
+                  nSample1D=c.nSpatialSample1D, covariant=prm["covariant"])
     stim = Stimulus(frames=stim_f.frames, init_LMS=stim_f.init_LMS)
 
     # initial state and the seed sequence of src/patch.cu (logRand_init, host engines, init)

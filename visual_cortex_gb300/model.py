@@ -174,6 +174,8 @@ class LgnSpec:
     convolRatio: float = 1.0
     frRatio: float = 1.0
     flat_retina: bool = True
+    nSample1D: int = 0                 # parvo nSpatialSample1D
+    covariant: np.ndarray | None = None  # f32 [nLGN] (parvo_maxConvol)
 
     @property
     def nLGN(self) -> int:
@@ -182,6 +184,27 @@ class LgnSpec:
     @property
     def nMagno(self) -> int:
         return self.nMagno_I + self.nMagno_C
+
+    @property
+    def nParvo(self) -> int:
+        return self.nParvo_I + self.nParvo_C
+
+    def parvo_ids(self) -> np.ndarray:
+        c = np.arange(self.nParvo)
+        return np.where(c < self.nParvo_I, c, c + self.nMagno_I)
+
+    def to_parvo_struct(self) -> N.LgnParvoConfig:
+        s = self.sched
+        q = N.LgnParvoConfig()
+        q.nSample1D = self.nSample1D
+        q.nKernelSample = s.nKernelSample
+        q.kernelSampleInterval = s.kernelSampleInterval
+        q.iKernelSampleT0 = s.iKernelSampleT0
+        q.parvoComp = s.parvoComp
+        q.frameOffset = 0 if s.pLongerThanM else s.dFrame
+        q.kernelSampleDt = s.kernelSampleDt
+        q.kernelSampleT0 = s.kernelSampleT0f
+        return q
 
     def magno_ids(self) -> np.ndarray:
         m = np.arange(self.nMagno)
@@ -268,7 +291,13 @@ class Simulation:
         N.check(plan, rc, "pv1_plan_create")
         lc = lgn.to_struct()
         lp, keep = lgn.params_struct()
-        N.check(plan, N.lib.pv1_lgn_setup(plan, C.byref(lc), C.byref(lp), int(seeds.lgn)), "pv1_lgn_setup")
+        if lgn.nParvo > 0:
+            pc = lgn.to_parvo_struct()
+            cov = np.ascontiguousarray(lgn.covariant, dtype=f32)
+            N.check(plan, N.lib.pv1_lgn_setup_parvo(plan, C.byref(lc), C.byref(pc), C.byref(lp), N.fptr(cov),
+                                                    int(seeds.lgn)), "pv1_lgn_setup_parvo")
+        else:
+            N.check(plan, N.lib.pv1_lgn_setup(plan, C.byref(lc), C.byref(lp), int(seeds.lgn)), "pv1_lgn_setup")
         del keep
         fr = np.ascontiguousarray(stim.frames, dtype=f32)
         nF, _, h, w = fr.shape
@@ -388,6 +417,20 @@ class Simulation:
         N.check(self.plan, N.lib.pv1_lgn_get_tables(self.plan, N.fptr(TW), N.fptr(SW), N.fptr(SC), N.fptr(mc)),
                 "pv1_lgn_get_tables")
         return TW, SW, SC, mc
+
+    def lgn_parvo_tables(self):
+        np_, ns, nks = self.lgn.nParvo, self.lgn.nSample1D ** 2, self.lgn.sched.nKernelSample
+        TW = np.empty((np_, 2, nks), f32)
+        SW = np.empty(ns, f32)
+        SC = np.empty((2, np_, 2, ns), f32)
+        N.check(self.plan, N.lib.pv1_lgn_get_parvo_tables(self.plan, N.fptr(TW), N.fptr(SW), N.fptr(SC)),
+                "pv1_lgn_get_parvo_tables")
+        return TW, SW, SC
+
+    def lgn_parvo_spatial(self):
+        PS = np.empty((self.stim.frames.shape[0] + 1, 2, self.lgn.nParvo), f32)
+        N.check(self.plan, N.lib.pv1_lgn_get_parvo_spatial(self.plan, N.fptr(PS)), "pv1_lgn_get_parvo_spatial")
+        return PS
 
     def lgn_spatial(self):
         S = np.empty((self.stim.frames.shape[0] + 1, self.lgn.nMagno), f32)

@@ -55,6 +55,17 @@ class FrameSchedule:
     magnoComp: int
 
     @property
+    def kernelSampleDt(self) -> float:
+        """Parvo kernel sample spacing (src/patch.cu:4962)."""
+        import numpy as np
+        return float(np.float32(self.kernelSampleInterval) * np.float32(self.dt))
+
+    @property
+    def kernelSampleT0f(self) -> float:
+        import numpy as np
+        return float(np.float32(self.iKernelSampleT0) * np.float32(self.dt))
+
+    @property
     def mKernelSampleDt(self) -> float:
         import numpy as np
         return float(np.float32(self.mKernelSampleInterval) * np.float32(self.dt))

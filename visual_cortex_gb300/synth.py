@@ -81,8 +81,14 @@ def make_lgn(n_lgn: int, rng: np.random.Generator, patch_deg: float, dt: float,
              frame_rate: int = 120, mSample1D: int = 16, mau: float = 250.0,
              mKernelSample: int = 250, sigma_c: float = 0.03, sigma_s: float = 0.09,
              stim_range_deg: float | None = None, buffer_deg: float = 0.2,
-             jitter: float = 0.0, tjitter: float = 0.0) -> tuple[LgnSpec, float]:
-    """ON/OFF magno cells with centers uniform in a patch_deg square around the fixation.
+             jitter: float = 0.0, tjitter: float = 0.0, n_parvo: int = 0,
+             tau: float | None = None, nKernelSample: int | None = None,
+             nSample1D: int = 8) -> tuple[LgnSpec, float]:
+    """ON/OFF magno cells with centers uniform in a patch_deg square around the fixation;
+    with n_parvo > 0 also parvocellular L/M-opponent cells (LGN ids 0..n_parvo-1, before the
+    magno cells as the reference orders them), centre and surround at slightly different
+    positions and orientations, each with its own temporal kernel, sampled over `tau` ms with
+    nKernelSample taps.
 
     Returns the spec and the full stimulus extent (deg) the texture spans (flat retina)."""
     nOn = n_lgn // 2
@@ -100,7 +106,11 @@ def make_lgn(n_lgn: int, rng: np.random.Generator, patch_deg: float, dt: float,
     two = lambda c, s: np.concatenate([c, s]).astype(f32)
     types = np.where(np.arange(n_lgn) < nOn, 4, 5)
     k_center = np.where(types == 4, 60.0, -60.0)
-    sched = make_schedule(dt, frame_rate, mau, mau, mKernelSample, mKernelSample)
+    sched = make_schedule(dt, frame_rate, mau if tau is None else tau, mau, mKernelSample if nKernelSample is None
+                          else nKernelSample, mKernelSample)
+    if n_parvo > 0:
+        return _with_parvo(n_lgn, n_parvo, rng, patch_deg, sched, mSample1D, nSample1D, sigma_c, sigma_s,
+                           stim_range_deg, buffer_deg, jitter)
     spec = LgnSpec(
         nParvo_I=0, nMagno_I=n_lgn, nParvo_C=0, nMagno_C=0, mSample1D=mSample1D, sched=sched,
         polar=two(polar, polar), ecc=two(ecc, ecc), rw=two(sc * DEG, ss * DEG),
@@ -116,6 +126,72 @@ def make_lgn(n_lgn: int, rng: np.random.Generator, patch_deg: float, dt: float,
         coneType=np.full(2 * n_lgn, 3, u32),
         normViewDistance=normViewDistance, L_x0=0.5, L_y0=0.5, R_x0=1.0, R_y0=1.0,
         nsig=3.0, convolRatio=1.0, frRatio=1.0, flat_retina=True)
+    spec.types = types
+    spec.xy = xy
+    return spec, extent
+
+
+def _with_parvo(n_magno, n_parvo, rng, patch_deg, sched, mSample1D, nSample1D, sigma_c, sigma_s,
+                stim_range_deg, buffer_deg, jitter):
+    """LGN of n_parvo parvo cells (ids first) and n_magno ON/OFF magno cells, one eye."""
+    n = n_parvo + n_magno
+    xy = rng.uniform(-patch_deg / 2, patch_deg / 2, size=(n, 2))
+    # surround centres of the parvo cells sit a little off their centres
+    sxy = xy.copy()
+    sxy[:n_parvo] += rng.normal(0.0, 0.01, size=(n_parvo, 2))
+    polar = np.arctan2(xy[:, 1], xy[:, 0])
+    ecc = np.hypot(xy[:, 0], xy[:, 1]) * DEG
+    spolar = np.arctan2(sxy[:, 1], sxy[:, 0])
+    secc = np.hypot(sxy[:, 0], sxy[:, 1]) * DEG
+    max_ecc = float(max(np.max(np.hypot(xy[:, 0], xy[:, 1])), np.max(np.hypot(sxy[:, 0], sxy[:, 1]))))
+    if stim_range_deg is None:
+        stim_range_deg = max(max_ecc, patch_deg / 2) * 1.05
+    extent = 2 * (stim_range_deg + buffer_deg)
+    normViewDistance = (max_ecc / extent) / max_ecc / DEG
+    types = np.empty(n, np.int64)
+    types[:n_parvo] = np.arange(n_parvo) % 4          # LonMoff, LoffMon, MonLoff, MoffLon
+    types[n_parvo:] = np.where(np.arange(n_magno) < n_magno // 2, 4, 5)
+    sc = sigma_c * (1 + jitter * rng.uniform(-1, 1, n))
+    ss = sigma_s * (1 + jitter * rng.uniform(-1, 1, n))
+    on_center = (types == 0) | (types == 2) | (types == 4)
+    kc = np.where(on_center, 60.0, -60.0)
+    ks = -kc
+    ks[:n_parvo] *= 0.8
+    orient_c = np.zeros(n)
+    orient_s = np.zeros(n)
+    orient_c[:n_parvo] = rng.uniform(0, math.pi, n_parvo)
+    orient_s[:n_parvo] = orient_c[:n_parvo] + rng.uniform(-0.3, 0.3, n_parvo)
+    rw_c = sc * DEG
+    rh_c = sc * DEG
+    rh_c[:n_parvo] *= 1.2                               # elongated parvo components
+    rw_s = ss * DEG
+    rh_s = ss * DEG * np.where(np.arange(n) < n_parvo, 0.9, 1.0)
+    cone_c = np.full(n, 3, np.int64)
+    cone_s = np.full(n, 3, np.int64)
+    cone_c[:n_parvo] = np.where(types[:n_parvo] < 2, 0, 1)
+    cone_s[:n_parvo] = 1 - cone_c[:n_parvo]
+    tauR_c = np.full(n, 1.5)
+    tauD_c = np.full(n, 4.5)
+    tauR_s = np.full(n, 1.5)
+    tauD_s = np.full(n, 4.5)
+    tauR_s[:n_parvo] = 1.9
+    tauD_s[:n_parvo] = 5.5
+    delay_c = np.full(n, 14.0)
+    delay_s = np.full(n, 14.0)
+    delay_s[:n_parvo] = 17.0
+    two = lambda c, s_: np.concatenate([c, s_]).astype(f32)
+    spec = LgnSpec(
+        nParvo_I=n_parvo, nMagno_I=n_magno, nParvo_C=0, nMagno_C=0, mSample1D=mSample1D, sched=sched,
+        polar=two(polar, spolar), ecc=two(ecc, secc), rw=two(rw_c, rw_s), rh=two(rh_c, rh_s),
+        orient=two(orient_c, orient_s), k=two(kc, ks), ratio=two(np.full(n, 1.0), np.full(n, 1.0)),
+        tauR=two(tauR_c, tauR_s), tauD=two(tauD_c, tauD_s), nR=two(np.full(n, 19.0), np.full(n, 19.0)),
+        nD=two(np.full(n, 9.5), np.full(n, 9.5)), delay=two(delay_c, delay_s),
+        spont=np.full(n, 0.1, f32), c50=np.where(types < 4, 0.3, 0.25).astype(f32),
+        sharpness=np.where(types < 4, 2.5, 3.0).astype(f32),
+        coneType=np.concatenate([cone_c, cone_s]).astype(u32),
+        normViewDistance=normViewDistance, L_x0=0.5, L_y0=0.5, R_x0=1.0, R_y0=1.0,
+        nsig=3.0, convolRatio=1.0, frRatio=1.0, flat_retina=True, nSample1D=nSample1D,
+        covariant=np.where(types < 4, 0.53753461391295254, 1.0).astype(f32))
     spec.types = types
     spec.xy = xy
     return spec, extent
@@ -233,16 +309,23 @@ def lgn_to_v1(spec: V1Spec, lgn: LgnSpec, rng: np.random.Generator, m: int, w: f
     xy = lgn.xy
     on = np.nonzero(lgn.types == 4)[0]
     off = np.nonzero(lgn.types == 5)[0]
+    parvo = np.nonzero(lgn.types < 4)[0]
     centers = rng.uniform(-patch_deg / 2 * 0.8, patch_deg / 2 * 0.8, size=(nV1, 2))
     orient = rng.uniform(0, math.pi, nV1)
     u = np.stack([np.cos(orient + math.pi / 2), np.sin(orient + math.pi / 2)], -1)
     from scipy.spatial import cKDTree
-    mo = m // 2
+    mp = m // 4 if parvo.size else 0      # parvo inputs: the cells nearest the RF centre
+    mm = m - mp
+    mo = mm // 2
     _, kon = cKDTree(xy[on]).query(centers + sub_offset_deg * u, k=mo)
-    _, koff = cKDTree(xy[off]).query(centers - sub_offset_deg * u, k=m - mo)
+    _, koff = cKDTree(xy[off]).query(centers - sub_offset_deg * u, k=mm - mo)
     kon = np.asarray(kon).reshape(nV1, mo)
-    koff = np.asarray(koff).reshape(nV1, m - mo)
-    ids = np.concatenate([on[kon], off[koff]], axis=1).T.astype(u32).copy()
+    koff = np.asarray(koff).reshape(nV1, mm - mo)
+    parts = [on[kon], off[koff]]
+    if mp:
+        _, kp = cKDTree(xy[parvo]).query(centers, k=mp)
+        parts.append(parvo[np.asarray(kp).reshape(nV1, mp)])
+    ids = np.concatenate(parts, axis=1).T.astype(u32).copy()
     s = (w * rng.uniform(0.5, 1.5, size=(m, nV1))).astype(f32)
     return np.full(nV1, m, u32), ids, s, centers, orient
 
@@ -254,14 +337,16 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
                   wFF: float = 0.2, wE: float = 0.004, wI: float = 0.6, wFar: float = 0.002,
                   noisyDep=(0.0, 0.0), synFail=(0.0, 0.0, 0.0, 0.0), synFailFF=(0.0, 0.0),
                   mSample1D: int = 16, dt: float = 0.125, tjitter: float = 0.0,
-                  noDelay: int = 1) -> Workload:
+                  noDelay: int = 1, n_parvo: int = 0, tau: float | None = None,
+                  nKernelSample: int | None = None) -> Workload:
     """Builds one synthetic patch; C1 = 1x1024 V1 / 512 LGN; C2 = 32 blocks / 16384 LGN.
     noDelay = 0: near synapses are delivered after their distance delay (delayMat from the
     neuron positions, mm, at speedOfThought 1 mm/ms)."""
     rng = np.random.default_rng(seed)
     spec = make_spec(nblock, adex_inh=adex_inh, noisyDep=noisyDep, synFail=synFail,
                      synFailFF=synFailFF, dt=dt)
-    lgn, extent = make_lgn(n_lgn, rng, patch_deg, dt, mSample1D=mSample1D, tjitter=tjitter)
+    lgn, extent = make_lgn(n_lgn, rng, patch_deg, dt, mSample1D=mSample1D, tjitter=tjitter,
+                           n_parvo=n_parvo, tau=tau, nKernelSample=nKernelSample)
     side = 0.5
     pos, nbx = block_positions(nblock, spec.blockSize, side, rng)
     conMat = near_conmat(spec, pos, rng, sigma=0.1, nE_partners=100, nI_partners=50,
@@ -351,16 +436,19 @@ def write_reference_files(wl: Workload, folder: str, seed: int = 0, nt: int | No
     stim_range = max(max_ecc, patch / 2) * 1.05
     FM.write_stimulus(d + "stimulus.bin", wl.stim.frames, wl.stim.init_LMS,
                       domain=(buffer_deg, stim_range), neye=1)
-    FM.write_lgn_vpos(d + "LGN_vpos.bin", lgn.nMagno_I, lgn.nMagno_C, max_ecc,
+    FM.write_lgn_vpos(d + "LGN_vpos.bin", lgn.nParvo_I + lgn.nMagno_I, lgn.nParvo_C + lgn.nMagno_C, max_ecc,
                       lgn.xy[:, 0].astype(f32), lgn.xy[:, 1].astype(f32), lgn.types)
-    FM.write_lgn_params(d + "LGN", lgn.types, {k: getattr(lgn, k) for k in
-                                               FM.LGN_FIELDS2 + FM.LGN_FIELDS1 + ("coneType",)})
+    lp = {k: getattr(lgn, k) for k in FM.LGN_FIELDS2 + FM.LGN_FIELDS1 + ("coneType",)}
+    if lgn.covariant is not None:
+        lp["covariant"] = lgn.covariant
+    FM.write_lgn_params(d + "LGN", lgn.types, lp)
     s = lgn.sched
     keys = dict(
         inputFolder=d, resourceFolder=d, outputFolder=d, seed=seed, dt=spec.dt,
         nt=wl.nt if nt is None else nt, frameRate=s.frameRate, tau=s.nRetrace * spec.dt,
         mau=s.mRetrace * spec.dt, nKernelSample=s.nKernelSample, mKernelSample=s.mKernelSample,
-        mSpatialSample1D=lgn.mSample1D, nsig=lgn.nsig, convolRatio=lgn.convolRatio,
+        mSpatialSample1D=lgn.mSample1D, nSpatialSample1D=lgn.nSample1D or 32, nsig=lgn.nsig,
+        convolRatio=lgn.convolRatio,
         frRatioLGN=lgn.frRatio, flat_retina=True, useNewLGN=False, learning=0,
         nTypeHierarchy=[spec.nTypeE, spec.nType - spec.nTypeE], sRatioLGN=[1.0],
         sRatioV1=[1.0], synPerCon=spec.synPerCon, synPerConFF=spec.synPerConFF,

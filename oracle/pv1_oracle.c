@@ -709,11 +709,187 @@ void orc_cond_eval(float rise, float decay, float g, float h, float f, float dt,
 /* compute_V_collect_spike_learnFF_fast for every neuron (learning off, no gap junctions).
  * noise: normals [nV1] of this step (NULL if no noise); ff: normals [nV1][cap] for the
  * feed-forward failure draws.  Writes sInfo (the step's spike word). */
+/* compute_V_collect_spike_learnFF (src/coredynamics.cu:427-845, learning off): the step taken
+ * when dt exceeds the shortest refractory period, several spikes per step.  Pass after pass:
+ * conductances at tBack from the previous interval start (new_t0), inputs after new_t0 and
+ * before tBack into g0, end-of-step inputs into g1 on the first pass only, RK2 over dt - tBack,
+ * spike -> tBack = tsp + tRef and another pass while tBack < dt.  With tau_noise = 0 the noise
+ * is divided by dt on every pass, as the reference does. */
+static int compute_v_multi(orc_v1 *o, const float *lgnSInfo, const float *noise, const float *ff, int cap) {
+    const pv1_v1_config *c = &o->c;
+    const int nV1 = o->nV1;
+    const float dt = c->dt;
+    int nerr = 0;
+#pragma omp parallel for schedule(static) reduction(+ : nerr)
+    for (int i = 0; i < nV1; i++) {
+        const int it = otype(o, i % o->bs);
+        const float vR = c->vR[it], vThres = c->vThres[it], gL = c->gL[it], Cm = c->C[it];
+        const float tRef = c->tRef[it], vT = c->vT[it], deltaT = c->deltaT[it];
+        const float tau_w = c->tau_w[it], aa = c->a[it], bb = c->b[it];
+        const float tonic = o->tonic[i];
+        float v0 = o->v[i];
+        float w0 = c->iModel == 1 ? o->w[i] : 0.0f;
+        float tBack = o->tBack[i];
+        const float depC = orc_adex_depc(c->vL, vT, gL, aa, deltaT, tonic);
+        const float noise0 = c->tau_noise > 0 ? o->lastNoise[i] : 0.f;
+        float ge[PV1_MAX_NG], he[PV1_MAX_NG], gi[PV1_MAX_NG], hi[PV1_MAX_NG];
+        float gE_t1 = 0.0f, gI_t1 = 0.0f;
+        for (uint32_t ig = 0; ig < c->ngE; ig++) {
+            float g = o->gE[ig * nV1 + i], h = o->hE[ig * nV1 + i];
+            ge[ig] = g;
+            he[ig] = h;
+            ocond_decay(&o->cE, &g, &h, dt, (int)ig);
+            o->gE[ig * nV1 + i] = g;
+            o->hE[ig * nV1 + i] = h;
+            gE_t1 += g;
+        }
+        for (uint32_t ig = 0; ig < c->ngI; ig++) {
+            float g = o->gI[ig * nV1 + i], h = o->hI[ig * nV1 + i];
+            gi[ig] = g;
+            hi[ig] = h;
+            ocond_decay(&o->cI, &g, &h, dt, (int)ig);
+            o->gI[ig * nV1 + i] = g;
+            o->hI[ig * nV1 + i] = h;
+            gI_t1 += g;
+        }
+        float g0[PV1_MAX_NG], h0[PV1_MAX_NG], g1[PV1_MAX_NG], h1[PV1_MAX_NG];
+        for (uint32_t ig = 0; ig < c->ngFF; ig++) {
+            g1[ig] = o->gFF[ig * nV1 + i];
+            h1[ig] = o->hFF[ig * nV1 + i];
+            g0[ig] = g1[ig];
+            h0[ig] = h1[ig];
+            ocond_decay(&o->cFF, &g1[ig], &h1[ig], dt, (int)ig);
+        }
+        const float noiseRatio = c->noiseOnTonic ? tonic : 1.0f;
+        float noise1 = sqrtf(2 * c->noisyDep[it] * (vT - vR) * noiseRatio * dt);
+        const float pf = c->synFailFF[it], nSyn = c->synPerConFF[it];
+        if (noise1 > 0) {
+            noise1 *= noise ? noise[i] : 0.f;
+            if (c->tau_noise > 0) {
+                noise1 /= c->tau_noise;
+                float hk1 = -noise0 / c->tau_noise;
+                float hk2 = -(noise0 + dt * hk1 + noise1) / c->tau_noise;
+                noise1 += noise0 + dt * (hk1 + hk2) / 2;
+                o->lastNoise[i] = noise1;
+            }
+        }
+        int backingUp = tBack < dt && tBack > 0;
+        float new_t0 = 0.f, sInfo = 0.f, v = v0, w = w0, tsp = 0.f;
+        unsigned spikeCount = 0;
+        const uint32_t m = o->nLGN[i];
+        float *f = (float *)malloc(sizeof(float) * (m ? m : 1));
+        int nff = 0, pass = 0;
+        o->dep[i] = depC + noise1;
+        do {
+            const float dtBack = backingUp ? tBack - new_t0 : 0.f;
+            if (backingUp)
+                for (uint32_t ig = 0; ig < c->ngFF; ig++) ocond_decay(&o->cFF, &g0[ig], &h0[ig], dtBack, (int)ig);
+            for (uint32_t q = 0; q < m; q++) {
+                const size_t lid = (size_t)q * nV1 + i;
+                if (spikeCount == 0) f[q] = o->sLGN[lid];
+                const float sFF = lgnSInfo[o->lgnId[lid]];
+                const unsigned nspFF = (unsigned)floorf(sFF);
+                const float tspFF = (sFF - nspFF) * dt;
+                if (nspFF > 0 && tspFF >= new_t0) {
+                    if (spikeCount == 0 && pf > 0) {
+                        const float nstd = sqrtf(pf * (1 - pf) / nSyn);
+                        const float rnd = (ff && nff < cap) ? ff[(size_t)i * cap + nff] : 0.f;
+                        nff++;
+                        f[q] *= 1 - pf + nstd * rnd;
+                    }
+                    if (f[q] > 0) {
+                        const float ddt = backingUp ? tBack - tspFF : 0.f;
+                        for (uint32_t ig = 0; ig < c->ngFF; ig++) {
+                            const float str = f[q] * c->pFF[it * c->ngFF + ig];
+                            if (backingUp && ddt > 0) ocond_input(&o->cFF, &g0[ig], &h0[ig], str * nspFF, ddt, (int)ig);
+                            if (spikeCount == 0) ocond_input(&o->cFF, &g1[ig], &h1[ig], str * nspFF, dt - tspFF, (int)ig);
+                        }
+                    }
+                }
+            }
+            float gE_t0 = 0.0f;
+            for (uint32_t ig = 0; ig < c->ngFF; ig++) {
+                gE_t0 += g0[ig];
+                if (spikeCount == 0) {
+                    gE_t1 += g1[ig];
+                    o->gFF[ig * nV1 + i] = g1[ig];
+                    o->hFF[ig * nV1 + i] = h1[ig];
+                }
+            }
+            for (uint32_t ig = 0; ig < c->ngE; ig++) {
+                if (backingUp) ocond_decay(&o->cE, &ge[ig], &he[ig], dtBack, (int)ig);
+                gE_t0 += ge[ig];
+            }
+            float gI_t0 = 0.0f;
+            for (uint32_t ig = 0; ig < c->ngI; ig++) {
+                if (backingUp) ocond_decay(&o->cI, &gi[ig], &hi[ig], dtBack, (int)ig);
+                gI_t0 += gi[ig];
+            }
+            tsp = 0.f;
+            if (tBack < dt) {
+                const float new_dt = dt - tBack;
+                if (backingUp) { /* rk2_vFixedBefore */
+                    const float A = aa * (v0 - c->vL);
+                    w0 = (w0 - A) * expf(-dtBack / tau_w) + A;
+                }
+                float n0, n1;
+                if (c->tau_noise > 0) { n0 = noise0; n1 = noise1; }
+                else { noise1 /= dt; n0 = noise1; n1 = noise1; }
+                orc_adex_rk2(c->vE, c->vI, c->vL, gE_t0, gI_t0, gE_t1, gI_t1, depC, gL, vT, deltaT, Cm, aa, tau_w,
+                             v0, w0, new_dt, n0, n1, &v, &w);
+                if (v > vThres) {
+                    new_t0 = tBack;
+                    float ratio;
+                    orc_adex_spike(vThres, v0, v, w, bb, &ratio, &w0);
+                    tsp = new_t0 + ratio * new_dt;
+                    if (!(tsp >= 0)) nerr++;
+                    sInfo += tsp;
+                    spikeCount++;
+                    tBack = tsp + tRef;
+                    backingUp = tBack < dt;
+                    if (backingUp) v0 = vR; /* reset */
+                    else v = vR;
+                } else {
+                    if (tBack > 0) tBack = 0;
+                    backingUp = 0;
+                }
+            }
+            if (tBack >= dt) { /* rk2_vFixedAfter */
+                v = vR;
+                const float A = aa * (v - c->vL);
+                w = (w0 - A) * expf(-(dt - tsp) / tau_w) + A;
+                tBack -= dt;
+            }
+            if (++pass >= 64 && backingUp) {
+                nerr++;
+                break;
+            }
+        } while (backingUp);
+        free(f);
+        if (spikeCount > 0) {
+            sInfo /= spikeCount * dt;
+            sInfo += spikeCount;
+        } else {
+            sInfo = v;
+        }
+        o->sInfo[i] = sInfo;
+        o->v[i] = v;
+        if (c->iModel == 1) o->w[i] = w;
+        o->tBack[i] = tBack;
+    }
+    return nerr;
+}
+
 int orc_v1_compute_v(orc_v1 *o, const float *lgnSInfo, const float *noise, const float *ff, int cap) {
     const pv1_v1_config *c = &o->c;
     const int nV1 = o->nV1;
     const float dt = c->dt;
     int nerr = 0;
+    {
+        float minTRef = c->tRef[0];
+        for (uint32_t j = 1; j < c->nType; j++) minTRef = c->tRef[j] < minTRef ? c->tRef[j] : minTRef;
+        if (dt > minTRef) return compute_v_multi(o, lgnSInfo, noise, ff, cap);
+    }
 #pragma omp parallel for schedule(static) reduction(+ : nerr)
     for (int i = 0; i < nV1; i++) {
         const int local = i % o->bs;

@@ -22,6 +22,8 @@ constexpr int kClassMaxSeg = 48;
 constexpr int kClassMaxSlots = 64;
 
 // Error word bits raised by kernels (never trap).
+constexpr int kMaxLgnMulti = 64;       // LGN synapses per neuron in the multi-spike step
+constexpr int kMaxSpikePasses = 64;    // integration passes per step in the multi-spike step
 constexpr int kErrRecordOverflow = 1;   // a draw record ran out of capacity
 constexpr int kErrNegTsp = 2;           // interpolated spike time < 0 or NaN
 constexpr int kErrFarOverflow = 4;      // far event beyond the delay ring
@@ -152,6 +154,7 @@ struct V1Params {
     float synFailFF[kMaxType], synPerConFF[kMaxType], noisyDep[kMaxType];
     float tau_noise;
     int noiseOnTonic, iModel;
+    int multiSpike;     // dt > min tRef: several spikes per step (compute_V_collect_spike_learnFF)
     int condRng;        // rGenCond draws can change results (some failure rate > 0)
     int noiseRng;       // some noisyDep > 0
     // state [nV1] / [ng][nV1]

@@ -338,6 +338,12 @@ int pv1_plan_create(const pv1_v1_config *cfg, pv1_plan **out) {
     v.noiseOnTonic = c.noiseOnTonic;
     v.iModel = c.iModel;
     v.noDelay = c.noDelay;
+    // dt > the shortest refractory period selects the multi-spike step (src/patch.cu:990-995, 6297)
+    {
+        float minTRef = c.tRef[0];
+        for (int j = 1; j < (int)c.nType; j++) minTRef = std::min(minTRef, c.tRef[j]);
+        v.multiSpike = c.dt > minTRef ? 1 : 0;
+    }
     v.hWrite = c.hWrite;
     int r = 0;
     r |= dev_alloc(p, &p->d_err, 1);
@@ -834,6 +840,8 @@ int pv1_v1_set_lgn_synapses(pv1_plan *p, uint32_t maxLGN, const uint32_t *nLGNpe
             if (j < nLGNperV1[i] && lgnId[q] >= (uint32_t)p->nLGN) return fail(p, PV1_E_ARG, "LGN id out of range");
         }
     }
+    if (p->vp.multiSpike && maxLGN > (uint32_t)kMaxLgnMulti)
+        return fail(p, PV1_E_UNSUPPORTED, "the multi-spike step (dt > min tRef) takes at most 64 LGN synapses per neuron");
     int *d_n, *d_id;
     float *d_s;
     int r = 0;
@@ -1151,7 +1159,7 @@ static int choose_mode(pv1_plan *p) {
     if (p->modeChosen) return PV1_OK;
     bool fits = false;
     v1_persistent_ctas(p->vp, p->device, &fits);
-    p->persistent = fits && p->allowPersistent;
+    p->persistent = fits && p->allowPersistent && !p->vp.multiSpike;
     if (p->persistent && !p->d_barrier) {
         int r = dev_alloc(p, &p->d_barrier, 2);
         if (r) return r;

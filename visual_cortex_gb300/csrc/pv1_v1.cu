@@ -650,6 +650,238 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
     return sInfo;
 }
 
+// Phase B when dt exceeds the shortest refractory period: a neuron may fire several times in
+// one step (compute_V_collect_spike_learnFF, src/coredynamics.cu:427-845, without learning).
+// After each spike whose refractory period ends inside the step the membrane is integrated
+// again from the end of that period (tBack): the feed-forward and cortical conductances at
+// tBack are advanced from the previous interval start, inputs arriving after the interval
+// start and before tBack are added, w is carried with v held at vR, and RK2 runs over the rest
+// of the step.  The end-of-step conductances (g1) and the failure draws come from the first
+// pass only.  Kept from the reference: with tau_noise = 0 the noise term is divided by dt once
+// more on every pass (src/coredynamics.cu:758-759).  The spike word is
+// nsp + mean(tsp)/dt.  m <= kMaxLgnMulti (checked by the host).
+template <bool Rng>
+__device__ __noinline__ float step_neuron_multi(const V1Params &P, long long t, int i, int itype, float tonic, float depC,
+                                   int m, const float *__restrict__ lgnSInfo, NState &st,
+                                   curandStateMRG32k3a &condState, curandStateMRG32k3a &noisyState) {
+    const int nV1 = P.nV1;
+    const float dt = P.dt;
+    const int ngE = P.ngE, ngI = P.ngI, ngFF = P.ngFF;
+    const float vR = P.vR[itype], vThres = P.vThres[itype], gL = P.gL[itype];
+    const float Cm = P.C[itype], tRef = P.tRef[itype], vT = P.vT[itype];
+    const float deltaT = P.deltaT[itype], tau_w = P.tau_w[itype], aa = P.a[itype];
+    const float bb = P.b[itype];
+    float v0 = st.v;
+    float w0 = st.w;
+    float tBack = st.tBack;
+    const float noise0 = st.lastNoise;
+    float ge[kMaxNG], he[kMaxNG], gi[kMaxNG], hi[kMaxNG];
+    float gE_t1 = 0.0f, gI_t1 = 0.0f;
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        ge[ig] = st.gE[ig]; he[ig] = st.hE[ig];
+        if (ig < ngE) {
+            cond_decay_step(P.condE, P.decE, st.gE[ig], st.hE[ig], ig);
+            gE_t1 += st.gE[ig];
+        }
+    }
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        gi[ig] = st.gI[ig]; hi[ig] = st.hI[ig];
+        if (ig < ngI) {
+            cond_decay_step(P.condI, P.decI, st.gI[ig], st.hI[ig], ig);
+            gI_t1 += st.gI[ig];
+        }
+    }
+    float g0[kMaxNG], h0[kMaxNG], g1[kMaxNG], h1[kMaxNG];
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        g1[ig] = st.gFF[ig];
+        h1[ig] = st.hFF[ig];
+        g0[ig] = g1[ig];
+        h0[ig] = h1[ig];
+        if (ig < ngFF) cond_decay_step(P.condFF, P.decFF, g1[ig], h1[ig], ig);
+    }
+    float noise1 = 0.f;
+    if constexpr (Rng) {
+        const float noiseRatio = P.noiseOnTonic ? tonic : 1.0f;
+        noise1 = sqrtf(2 * P.noisyDep[itype] * (vT - vR) * noiseRatio * dt);
+        if (noise1 > 0) {
+            const float rnd = curand_normal(&noisyState);
+            if (P.recNoise) {
+                long long rs = t - P.recStep0;
+                if (rs >= 0 && rs < P.recSteps) P.recNoise[(size_t)rs * nV1 + i] = rnd;
+            }
+            noise1 *= rnd;
+            if (P.tau_noise > 0) {
+                noise1 /= P.tau_noise;
+                const float hk1 = -noise0 / P.tau_noise;
+                const float hk2 = -(noise0 + dt * hk1 + noise1) / P.tau_noise;
+                noise1 += noise0 + dt * (hk1 + hk2) / 2;
+                st.lastNoise = noise1;
+            }
+        }
+    }
+    const float pf = Rng ? P.synFailFF[itype] : 0.f;
+    const float nSynFF = P.synPerConFF[itype];
+    const float depOut = depC + noise1;
+    P.dep[i] = depOut;
+    float *recFF = nullptr;
+    int nFF = 0;
+    if (Rng && P.recFF) {
+        long long rs = t - P.recStep0;
+        if (rs >= 0 && rs < P.recSteps) recFF = P.recFF + ((size_t)rs * nV1 + i) * P.recCap;
+    }
+    float fmod[kMaxLgnMulti];
+    const int mm = m < kMaxLgnMulti ? m : kMaxLgnMulti;
+    bool backingUp = tBack < dt && tBack > 0;
+    float new_t0 = 0.f, tspSum = 0.f, v = v0, w = w0, tsp = 0.f;
+    float a1 = 0.f, b1 = 0.f;
+    int spikeCount = 0, pass = 0;
+    do {
+        const float dtBack = backingUp ? tBack - new_t0 : 0.f;
+        if (backingUp) {
+#pragma unroll
+            for (int ig = 0; ig < kMaxNG; ig++)
+                if (ig < ngFF) cond_decay(P.condFF, g0[ig], h0[ig], dtBack, ig);
+        }
+        for (int q = 0; q < mm; q++) {
+            const size_t lid = (size_t)q * nV1 + i;
+            if (spikeCount == 0) fmod[q] = __ldg(P.sLGN + lid);
+            const float sFF = __ldcg(lgnSInfo + __ldg(P.lgnId + lid));
+            const unsigned nspFF = (unsigned)floorf(sFF);
+            const float tspFF = (sFF - nspFF) * dt;
+            if (nspFF > 0 && tspFF >= new_t0) {
+                if constexpr (Rng) {
+                    if (spikeCount == 0 && pf > 0) {
+                        const float normed_std = sqrtf(pf * (1 - pf) / nSynFF);
+                        const float rnd = curand_normal(&condState);
+                        if (recFF) {
+                            if (nFF < P.recCap) recFF[nFF] = rnd;
+                            else atomicOr(P.err, kErrRecordOverflow);
+                        }
+                        nFF++;
+                        fmod[q] *= 1 - pf + normed_std * rnd;
+                    }
+                }
+                if (fmod[q] > 0) {
+                    const float ddt = backingUp ? tBack - tspFF : 0.f;
+#pragma unroll
+                    for (int ig = 0; ig < kMaxNG; ig++) {
+                        if (ig < ngFF) {
+                            const float str = fmod[q] * P.pFF[itype * ngFF + ig];
+                            if (backingUp && ddt > 0) cond_input(P.condFF, g0[ig], h0[ig], str * nspFF, ddt, ig);
+                            if (spikeCount == 0) cond_input(P.condFF, g1[ig], h1[ig], str * nspFF, dt - tspFF, ig);
+                        }
+                    }
+                }
+            }
+        }
+        float gE_t0 = 0.0f;
+#pragma unroll
+        for (int ig = 0; ig < kMaxNG; ig++) {
+            if (ig < ngFF) {
+                gE_t0 += g0[ig];
+                if (spikeCount == 0) gE_t1 += g1[ig];
+            }
+        }
+#pragma unroll
+        for (int ig = 0; ig < kMaxNG; ig++) {
+            if (ig < ngE) {
+                if (backingUp) cond_decay(P.condE, ge[ig], he[ig], dtBack, ig);
+                gE_t0 += ge[ig];
+            }
+        }
+        float gI_t0 = 0.0f;
+#pragma unroll
+        for (int ig = 0; ig < kMaxNG; ig++) {
+            if (ig < ngI) {
+                if (backingUp) cond_decay(P.condI, gi[ig], hi[ig], dtBack, ig);
+                gI_t0 += gi[ig];
+            }
+        }
+        tsp = 0.f;
+        if (tBack < dt) {
+            const float a0 = gE_t0 + gI_t0 + gL;
+            const float b0 = gE_t0 * P.vE + gI_t0 * P.vI + gL * P.vL + depC;
+            if (spikeCount == 0) {
+                a1 = gE_t1 + gI_t1 + gL;
+                b1 = gE_t1 * P.vE + gI_t1 * P.vI + gL * P.vL + depC;
+            }
+            const float new_dt = dt - tBack;
+            if (backingUp) {
+                const float A = aa * (v0 - P.vL);
+                w0 = (w0 - A) * expf(-dtBack / tau_w) + A;
+            }
+            float nz0, nz1;
+            if (P.tau_noise > 0) { nz0 = noise0; nz1 = noise1; }
+            else { noise1 /= dt; nz0 = noise1; nz1 = noise1; }
+            const float dTgL = deltaT * gL;
+            const float fk1 = (-a0 * v0 + b0 + dTgL * expf((v0 - vT) / deltaT) - w0) / Cm + nz0;
+            const float gk1 = (aa * (v0 - P.vL) - w0) / tau_w;
+            const float v1 = v0 + new_dt * fk1;
+            const float w1 = w0 + new_dt * gk1;
+            const float fk2 = (-a1 * v1 + b1 + dTgL * expf((v1 - vT) / deltaT) - w1) / Cm + nz1;
+            const float gk2 = (aa * (v1 - P.vL) - w1) / tau_w;
+            w = w0 + new_dt * (gk1 + gk2) / 2;
+            v = v0 + new_dt * (fk1 + fk2) / 2;
+            if (v > vThres) {
+                new_t0 = tBack;
+                const float ratio = (vThres - v0) / (v - v0);
+                tsp = new_t0 + ratio * new_dt;
+                w0 += ratio * (w - w0) + bb;
+                if (!(tsp >= 0)) atomicOr(P.err, kErrNegTsp);
+                tspSum += tsp;
+                spikeCount++;
+                tBack = tsp + tRef;
+                backingUp = tBack < dt;
+                if (backingUp) v0 = vR;
+                else v = vR;
+            } else {
+                if (tBack > 0) tBack = 0;
+                backingUp = false;
+            }
+        }
+        if (tBack >= dt) {
+            v = vR;
+            const float A = aa * (v - P.vL);
+            w = (w0 - A) * expf(-(dt - tsp) / tau_w) + A;
+            tBack -= dt;
+        }
+        if (++pass >= kMaxSpikePasses && backingUp) {
+            atomicOr(P.err, kErrBounds);   // more passes than the refractory periods allow
+            break;
+        }
+    } while (backingUp);
+    if (recFF) P.recFFCount[(size_t)(t - P.recStep0) * nV1 + i] = nFF;
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        st.gFF[ig] = g1[ig];
+        st.hFF[ig] = h1[ig];
+    }
+    const float sInfo = spikeCount > 0 ? tspSum / (spikeCount * dt) + spikeCount : v;
+    st.v = v;
+    if (P.iModel == 1) st.w = w;
+    st.tBack = tBack;
+    __stcg(P.sInfo + (size_t)(t & 1) * nV1 + i, sInfo);
+    if (P.recSpk) P.recSpk[(size_t)(t % P.recSlots) * nV1 + i] = sInfo;
+    if (P.rec) {
+        const long long slot = t % P.recSlots;
+        float *r = P.rec + slot * P.recStride;
+        const RecOff o = rec_off(P);
+        r[o.sinfo + i] = sInfo;
+        r[o.dep + i] = depOut;
+        if (P.iModel == 1) r[o.w + i] = w;
+        r[o.v + i] = v;
+#pragma unroll
+        for (int ig = 0; ig < kMaxNG; ig++) {
+            if (ig < ngFF) r[o.gFF + ig * nV1 + i] = g1[ig];
+            if (P.hWrite && ig < ngFF) r[o.hFF + ig * nV1 + i] = h1[ig];
+        }
+    }
+    return sInfo;
+}
+
 // One delayed event: the spike of `pre` at step t (spike word sI) through delayed synapse e,
 // in its k-th arrival slot; arrival step and offset as recal_G_vec (src/coredynamics.cu:282-333)
 // and recal_G_mat (2163-2200) compute them, with explicitly rounded operations.  `code` is the
@@ -865,7 +1097,11 @@ __device__ __forceinline__ void v1_step_body(const V1Params &P, long long t, int
         const float tonic = P.tonicDep[i];
         const float depC = tonic_current(P, itype, tonic);
         const float *lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
-        sInfo = step_neuron<Rng, false>(P, t, i, itype, tonic, depC, P.nLGNperV1[i], nullptr, lgnSInfo, st,
+        if (P.multiSpike)
+            sInfo = step_neuron_multi<Rng>(P, t, i, itype, tonic, depC, P.nLGNperV1[i], lgnSInfo, st, condState,
+                                           noisyState);
+        else
+            sInfo = step_neuron<Rng, false>(P, t, i, itype, tonic, depC, P.nLGNperV1[i], nullptr, lgnSInfo, st,
                                         condState, noisyState);
         store_state(P, i, st);
         if (Rng && P.condRng) P.rGenCond[i] = condState;

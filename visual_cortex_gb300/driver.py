@@ -158,8 +158,6 @@ def build(c: Config) -> Model:
         a, b = _per_type(c, "a", nType), _per_type(c, "b", nType)
     else:
         deltaT, tau_w, a, b = [1.0] * nType, [1.0] * nType, [0.0] * nType, [0.0] * nType
-    if min(tRef) < c.dt:
-        raise ConfigError("dt > min tRef selects the multi-spike step, not built")
     spec = V1Spec(
         nblock=nblock, blockSize=blockSize, typeAcc=[int(x) for x in typeAcc], nTypeE=nTypeE,
         ngFF=ngFF, ngE=ngE, ngI=ngI, dt=c.dt, riseFF=grFF, decayFF=gdFF, riseE=grE, decayE=gdE,

@@ -413,15 +413,19 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
                                              float tonic, float depC, int m, const int *lgnIds,
                                              const float *__restrict__ lgnSInfo,
                                              NState &st, curandStateMRG32k3a &condState,
-                                             curandStateMRG32k3a &noisyState) {
+                                             curandStateMRG32k3a &noisyState,
+                                             const unsigned *preMask = nullptr) {
     const int nV1 = P.nV1;
     const float dt = P.dt;
     const int ngE = P.ngE, ngI = P.ngI, ngFF = P.ngFF;
     // spike words of this neuron's LGN inputs, gathered first so that they overlap the decay
+    // (unless the caller fetched them already: preMask = synapses that received spikes)
     float spReg[RegSyn ? kMaxLgnReg : 1];
     if constexpr (RegSyn) {
+        if (!preMask) {
 #pragma unroll
-        for (int q = 0; q < kMaxLgnReg; q++) spReg[q] = q < m ? __ldcg(lgnSInfo + lgnIds[q]) : 0.f;
+            for (int q = 0; q < kMaxLgnReg; q++) spReg[q] = q < m ? __ldcg(lgnSInfo + lgnIds[q]) : 0.f;
+        }
     }
     const float vR = P.vR[itype], vThres = P.vThres[itype], gL = P.gL[itype];
     const float Cm = P.C[itype], tRef = P.tRef[itype], vT = P.vT[itype];
@@ -501,8 +505,12 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
     if constexpr (RegSyn) {
         // synapses that received a spike, as a bit mask; they are visited in synapse order
         unsigned mask = 0u;
+        if (preMask) {
+            mask = *preMask;
+        } else {
 #pragma unroll
-        for (int q = 0; q < kMaxLgnReg; q++) mask |= (spReg[q] >= 1.0f ? 1u : 0u) << q;
+            for (int q = 0; q < kMaxLgnReg; q++) mask |= (spReg[q] >= 1.0f ? 1u : 0u) << q;
+        }
         while (mask) {
             const int q = __ffs(mask) - 1;
             mask &= mask - 1;
@@ -962,9 +970,12 @@ __device__ __forceinline__ int owner_of(const Smem &sm, int cnt, int w) {
 // the fixed-point ring makes the sums independent of the order of the atomic appends.
 __device__ __forceinline__ void far_push_list(const V1Params &P, long long tl, Smem &sm, int cta, int nCta) {
     const int slot = (int)((tl + 3) % 3);  // tl >= -1
+    const int4 *list = P.farList + (size_t)slot * P.nV1;
+    // the first chunk's entries are fetched together with the count (entries past the count
+    // are stale and not used)
+    const int4 first = (int)threadIdx.x < P.nV1 ? __ldcg(list + threadIdx.x) : make_int4(0, 0, 0, 0);
     const int n = __ldcg(P.farCount + slot);
     if (n == 0) return;
-    const int4 *list = P.farList + (size_t)slot * P.nV1;
     const int G = nCta * kCta;
     const int gt = cta * kCta + threadIdx.x;
     int W0 = 0;  // work of the earlier chunks, modulo G
@@ -972,7 +983,7 @@ __device__ __forceinline__ void far_push_list(const V1Params &P, long long tl, S
         const int cnt = min(kCta, n - c0);
         __syncthreads();
         if (threadIdx.x < cnt) {
-            const int4 e = __ldcg(list + c0 + threadIdx.x);
+            const int4 e = c0 == 0 ? first : __ldcg(list + c0 + threadIdx.x);
             sm.fpre[threadIdx.x] = e.x;
             sm.fe0[threadIdx.x] = e.y;
             sm.fdeg[threadIdx.x] = e.z;
@@ -1129,42 +1140,50 @@ __global__ void __launch_bounds__(kCta) v1_step_kernel(V1Params P, const long lo
     v1_step_body<Rng>(P, t, blockIdx.x, gridDim.x, lgnRing, lgnSlots, deliverPrev, doStep, sm);
 }
 
-// Grid-wide barrier between the steps of the persistent kernel: arrive on a counter, the
-// last CTA bumps the generation; waiting CTAs poll with a bounded number of attempts and
-// raise kErrBarrier (instead of hanging) if the generation never moves.
-__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned *gen, unsigned nCTA, int *err) {
+// Split grid barrier of the persistent kernel on a monotonic arrival counter (zeroed before
+// each launch): the barrier after step s completes when the counter reaches nCTA * (s + 1).
+// arrive() publishes this CTA's writes and counts it in; wait() polls the counter with a
+// bounded number of attempts.  A CTA that gives up sets kErrBarrier and the abort bit of the
+// counter, which releases and fails every other waiter.  Work placed between the two calls
+// must not read what other CTAs write in the step (the next step's LGN spike words are
+// written before the launch).
+constexpr unsigned kBarrierAbort = 0x80000000u;
+
+__device__ __forceinline__ void barrier_arrive(unsigned *count, unsigned *s_arrived) {
     __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        *s_arrived = atomicAdd(count, 1u) + 1u;
+    }
+}
+
+__device__ __forceinline__ bool barrier_wait(unsigned *count, unsigned target, const unsigned *s_arrived,
+                                             int *err) {
     __shared__ int s_ok;
     if (threadIdx.x == 0) {
-        const unsigned g = *(volatile unsigned *)gen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(count, 1u);
-        int ok = 1;
-        if (arrived == nCTA - 1) {
-            *(volatile unsigned *)count = 0u;
-            __threadfence();
-            atomicAdd(gen, 1u);
-        } else {
-            long long spins = 0;
-            while (*(volatile unsigned *)gen == g) {
-                if (++spins > kBarrierSpins) {
-                    atomicOr(err, kErrBarrier);
-                    ok = 0;
-                    break;
-                }
-                if (spins > 64) __nanosleep(32);
+        unsigned c = *s_arrived;
+        long long spins = 0;
+        while ((c & ~kBarrierAbort) < target && !(c & kBarrierAbort)) {
+            if (++spins > kBarrierSpins) {
+                atomicOr(err, kErrBarrier);
+                atomicOr(count, kBarrierAbort);
+                c = kBarrierAbort;
+                break;
             }
+            if (spins > 64) __nanosleep(32);
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(count) : "memory");
         }
         __threadfence();
-        if (*(volatile int *)err & kErrBarrier) ok = 0;
-        s_ok = ok;
+        s_ok = (c & kBarrierAbort) ? 0 : 1;
     }
     __syncthreads();
     return s_ok != 0;
 }
 
 // K steps in one cooperative launch.  Neuron state, generators and up to kMaxLgnReg LGN
-// synapse ids stay in registers; one grid barrier separates consecutive steps.
+// synapse ids stay in registers; one grid barrier separates consecutive steps, and while a CTA
+// waits at it the spike words of its neurons' LGN synapses for the next step are already
+// fetched (as a bit mask of the synapses that received spikes).
 template <bool Rng>
 __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, const long long *stepBase,
                                                                  int K, const float *__restrict__ lgnRing,
@@ -1196,6 +1215,9 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
     const int farDeg = (P.farOn && active) ? P.farOff[i + 1] - farE0 : 0;
     const int farN1 = (P.farOn && active) ? P.farN1[i] : 0;
     const bool isFarPre = P.farOn && active && P.farPre[i];
+    __shared__ unsigned s_arrived;
+    unsigned lgnMask = 0u;
+    bool haveMask = false;
     for (int s = 0; s < K; s++) {
         const long long t = t0 + s;
         if (s > 0 || deliverFirst) deliver_prev<Rng>(P, t - 1, b, local, i, active, itype, st, condState, sm);
@@ -1203,14 +1225,25 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
         if (active) {
             const float *lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
             sInfo = step_neuron<Rng, true>(P, t, i, itype, tonic, depC, m, lgnIds, lgnSInfo, st, condState,
-                                           noisyState);
+                                           noisyState, haveMask ? &lgnMask : nullptr);
             if (P.spikeCount && sInfo >= 1.0f) P.spikeCount[i] += (unsigned)floorf(sInfo);
         }
         if (P.farOn) {
             far_push_list(P, t - 1, sm, blockIdx.x, gridDim.x);
             far_phase(P, t, i, active, sInfo, isFarPre, farE0, farDeg, farN1, sm, blockIdx.x);
         }
-        if (s + 1 < K && !grid_barrier(barrier, barrier + 1, gridDim.x, P.err)) break;
+        if (s + 1 < K) {
+            barrier_arrive(barrier, &s_arrived);
+            lgnMask = 0u;
+            if (active) {
+                const float *next = lgnRing + (size_t)((t + 1) % lgnSlots) * P.lgnN;
+#pragma unroll
+                for (int q = 0; q < kMaxLgnReg; q++)
+                    lgnMask |= ((q < m && __ldcg(next + lgnIds[q]) >= 1.0f) ? 1u : 0u) << q;
+            }
+            haveMask = true;
+            if (!barrier_wait(barrier, (unsigned)gridDim.x * (unsigned)(s + 1), &s_arrived, P.err)) break;
+        }
     }
     if (active) {
         store_state(P, i, st);
@@ -1312,6 +1345,8 @@ cudaError_t launch_v1_persistent(const V1Params &p, const long long *stepBase, i
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    cudaError_t e = cudaMemsetAsync(barrier, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
     if (needs_rng(p))
         return cudaLaunchKernelEx(&cfg, v1_persistent_kernel<true>, p, stepBase, K, lgnRing, lgnSlots,
                                   deliverFirst, barrier);

@@ -141,7 +141,7 @@ def run_gb300(args):
     from visual_cortex_gb300.build import build_native
     build_native()
     from visual_cortex_gb300 import _native as N
-    from visual_cortex_gb300.model import Simulation
+    from visual_cortex_gb300.model import Simulation, Stimulus
 
     N.check(None, N.lib.pv1_set_device(local), "pv1_set_device")
     dist = None
@@ -178,15 +178,20 @@ def run_gb300(args):
     v1_ms, lgn_ms, chunk = sim.time_kernels(320)
     persistent = sim.persistent()
 
-    # end to end through the public API from host buffers
+    # end to end through the public API from page-locked host buffers: the stimulus movie in
+    # (and its per-frame spatial stage), the spike raster of every step out
     sim.set_record(N.REC_SPIKES, S + 1)
+    frames = N.pinned_empty(wl.stim.frames.shape, np.float32)
+    frames[...] = wl.stim.frames
+    stim = Stimulus(frames=frames, init_LMS=wl.stim.init_LMS)
+    raster = N.pinned_empty((S, wl.spec.nV1), np.float32)
     e2e_times, spikes = [], 0
     for q in range(max(1, args.steps)):
         t0 = time.perf_counter()
-        sim.load_stimulus(wl.stim)
+        sim.load_stimulus(stim)
         step0 = sim.step
         sim.run(S, sync=False)
-        sp = sim.fetch_spikes(step0, S)
+        sp = sim.fetch_spikes(step0, S, out=raster)
         e2e_times.append(time.perf_counter() - t0)
         spikes += int((sp >= 1).sum())
     e2e_s = float(np.sum(e2e_times))

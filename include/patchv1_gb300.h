@@ -67,7 +67,8 @@ typedef struct pv1_v1_config {
     float tau_noise;
     int32_t noiseOnTonic;
     int32_t iModel;                         /* 0: LIF (w held at 0), 1: AdEx              */
-    int32_t noDelay;                        /* 1 only (distance-free near delivery)       */
+    int32_t noDelay;                        /* 1: near delivery without distance delay;
+                                               0: delayed (pv1_v1_set_near_delayed)       */
     int32_t noFarDelay;                     /* 0: delayed far delivery; 1: reference drops
                                                far input (src/coredynamics.cu:218-220)    */
     float speedOfThought;                   /* mm/ms                                      */
@@ -102,6 +103,12 @@ typedef struct pv1_lgn_params {
 } pv1_lgn_params;
 
 /* ---- plan lifetime ------------------------------------------------------------------ */
+
+/* Page-locked host memory for the buffers a caller streams through the library (stimulus
+ * frames in, records out): copies from and to it run at the full host-link bandwidth and
+ * asynchronously.  Free with pv1_host_free. */
+int pv1_host_alloc(uint64_t bytes, void **out);
+void pv1_host_free(void *ptr);
 
 /* Makes `device` the current CUDA device of the calling thread for this library (the
  * reference picks the device with the most free memory, src/patch.cu:9-24; here the caller
@@ -328,12 +335,16 @@ const char *pv1_batch_last_error(const pv1_batch *batch);
  * done), or a negative error code.  *ms (may be null) receives the device time of the call
  * (CUDA events on the batch stream). */
 int64_t pv1_batch_run(pv1_batch *batch, uint64_t maxSteps, float *ms);
-/* Autotuner: tries each chunk length in {16, 32, 64} with each V1 kernel variant (1, 2 or 3
- * resident CTAs per SM) for one chunk of the real run and keeps the fastest; the tuning
- * chunks are ordinary steps of the simulation.  enable = 0 fixes K = 64, 1 CTA per SM. */
+/* V1 variants: 0 = one cooperative launch per chunk that runs every trial's K steps with its
+ * state in registers (slots of CTAs take the trials in turn; a barrier among a trial's own
+ * CTAs between steps), available when the largest trial fits the co-resident grid;
+ * 1, 2, 3 = one launch per step with 1, 2 or 3 resident CTAs per SM.
+ * Autotuner: tries each chunk length in {16, 32, 64} with each variant for one chunk of the
+ * real run and keeps the fastest per step; the tuning chunks are ordinary steps of the
+ * simulation.  enable = 0 fixes K = 64 and variant 0 (1 where 0 is not available). */
 int pv1_batch_autotune(pv1_batch *batch, int enable);
-/* Chosen chunk length, V1 variant and the measured ms per chunk of every candidate tried
- * (times[i] for candidate i = kIndex*3 + (minB-1); 9 entries, -1 where not tried). */
+/* Chosen chunk length, V1 variant (minB) and the measured ms per chunk of every candidate
+ * tried (times[i] for candidate i = kIndex*4 + variant; 12 entries, -1 where not tried). */
 int pv1_batch_tuning(const pv1_batch *batch, int *K, int *minB, float *times);
 /* FP64 statistics of one trial: simulated time (ms), per-neuron firing rates (Hz, may be
  * null) and their mean, from spike counters kept by the V1 kernel since pv1_batch_create. */

@@ -87,3 +87,33 @@ def test_batch_in_pieces_with_noise(native):
     finally:
         for s in alone + batched:
             s.close()
+
+
+def test_batch_uneven_sizes_persistent(native):
+    """Trials of 2 and 1 blocks in one batch: the persistent variant's slots are sized for the
+    larger trial, the smaller one leaves CTAs idle; every trial still ends as it does alone."""
+    from visual_cortex_gb300.batch import Batch
+    big = _trials(n_trials=2, dur_ms=(10.0, 16.0))
+    small = _trials(n_trials=2, nblock=1, far_partners=0, dur_ms=(12.0, 18.0), seed=5)
+    trials = [big[0], small[0], big[1], small[1]]
+    alone, batched = [], []
+    try:
+        for tr in trials:
+            s = _sim(tr.wl)
+            s.persistent(0)
+            s.run(tr.steps)
+            alone.append(s)
+        batched = [_sim(tr.wl) for tr in trials]
+        b = Batch(batched, [tr.steps for tr in trials], autotune=False)
+        try:
+            assert b.tuning()["variant"] == "persistent"
+            assert b.run()[0] == 0
+            for q in range(len(trials)):
+                for k in STATE:
+                    np.testing.assert_array_equal(batched[q].state(k), alone[q].state(k),
+                                                  err_msg=f"trial {q} {k}")
+        finally:
+            b.close()
+    finally:
+        for s in alone + batched:
+            s.close()

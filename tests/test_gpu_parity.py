@@ -329,3 +329,31 @@ def test_multi_spike_several_per_step(native):
     np.testing.assert_array_equal(np.floor(g[sg]), np.floor(o[so]))
     assert np.abs(g[sg] - o[so]).max() < 1e-3
     assert (np.abs(G["v"] - O["v"]) / np.maximum(np.abs(O["v"]), 1.0)).max() < 1e-5
+
+
+def test_stimulus_reload_same_size(c1_small):
+    """A second movie of the same size reuses the texture arrays and the captured step graph:
+    its spatial stage equals a fresh plan's, and a run after the reload equals one whose
+    tables and graph were rebuilt (a movie of another size loaded in between)."""
+    from visual_cortex_gb300.model import Simulation, Stimulus
+    wl = c1_small
+    stim2 = Stimulus(frames=np.ascontiguousarray(wl.stim.frames[::-1]), init_LMS=wl.stim.init_LMS)
+    short = Stimulus(frames=np.ascontiguousarray(wl.stim.frames[:-1]), init_LMS=wl.stim.init_LMS)
+    a = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    b = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    c = Simulation(wl.spec, wl.net, wl.lgn, stim2, wl.init, wl.seeds)
+    try:
+        a.run(128)
+        b.run(128)
+        a.load_stimulus(stim2)
+        b.load_stimulus(short)
+        b.load_stimulus(stim2)
+        np.testing.assert_array_equal(a.lgn_spatial(), c.lgn_spatial())
+        a.run(128)
+        b.run(128)
+        for k in ("v", "gE", "gI", "gFF", "lgn_lnl"):
+            np.testing.assert_array_equal(a.state(k), b.state(k), err_msg=k)
+    finally:
+        a.close()
+        b.close()
+        c.close()

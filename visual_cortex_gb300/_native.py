@@ -94,6 +94,8 @@ def _load() -> C.CDLL:
     sig = {
         "pv1_abi_version": ([], C.c_int),
         "pv1_set_device": ([C.c_int], C.c_int),
+        "pv1_host_alloc": ([C.c_uint64, C.POINTER(C.c_void_p)], C.c_int),
+        "pv1_host_free": ([C.c_void_p], None),
         "pv1_plan_create": ([C.POINTER(V1Config), C.POINTER(P)], C.c_int),
         "pv1_plan_destroy": ([P], None),
         "pv1_last_error": ([P], C.c_char_p),
@@ -170,3 +172,31 @@ def check(plan, rc: int, what: str):
     if rc != PV1_OK:
         msg = lib.pv1_last_error(plan).decode() if plan else ""
         raise NativeError(f"{what} failed ({ERRORS.get(rc, rc)}): {msg}")
+
+
+class _PinnedBlock:
+    """Owner of one page-locked host allocation (freed when the last array view goes)."""
+
+    def __init__(self, nbytes: int):
+        ptr = C.c_void_p()
+        rc = lib.pv1_host_alloc(nbytes, C.byref(ptr))
+        if rc != 0 or not ptr.value:
+            raise MemoryError(f"pv1_host_alloc({nbytes}) failed: {rc}")
+        self.ptr = ptr.value
+        self.nbytes = nbytes
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            lib.pv1_host_free(C.c_void_p(self.ptr))
+            self.ptr = None
+
+
+def pinned_empty(shape, dtype=np.float32) -> np.ndarray:
+    """A numpy array in page-locked host memory: the library's copies to and from it (stimulus
+    frames in, records out) run asynchronously at the full host-link bandwidth."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape))
+    block = _PinnedBlock(max(n * dtype.itemsize, 1))
+    buf = (C.c_char * block.nbytes).from_address(block.ptr)
+    buf.owner = block        # the allocation lives as long as any view of the array
+    return np.frombuffer(buf, dtype=dtype, count=n).reshape(shape)

@@ -59,11 +59,12 @@ class Batch:
 
     def tuning(self):
         K, mb = C.c_int(), C.c_int()
-        t = np.empty(9, np.float32)
+        t = np.empty(12, np.float32)
         self._check(N.lib.pv1_batch_tuning(self.h, C.byref(K), C.byref(mb), N.fptr(t)), "pv1_batch_tuning")
-        cand = {f"K{k}_minB{b}": float(t[i * 3 + b - 1]) for i, k in enumerate((16, 32, 64))
-                for b in (1, 2, 3)}
-        return {"K": K.value, "minB": mb.value, "ms_per_chunk": cand}
+        name = lambda b: "persistent" if b == 0 else f"minB{b}"
+        cand = {f"K{k}_{name(b)}": float(t[i * 4 + b]) for i, k in enumerate((16, 32, 64))
+                for b in (0, 1, 2, 3)}
+        return {"K": K.value, "variant": name(mb.value), "ms_per_chunk": cand}
 
     def stats(self, trial: int, rates: bool = False):
         """FP64 simulated time (ms), mean rate (Hz) and optionally per-neuron rates."""

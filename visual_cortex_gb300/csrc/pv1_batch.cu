@@ -1,9 +1,11 @@
 // Batched trials behind the C ABI (pv1_batch_*): many independent patches stepped by the
 // same launches, replacing the reference's one-process-per-trial sweeps (src/ori.sh).
 //
-// Per chunk of K steps: one batched LGN launch (grid = cell CTAs x trials), K batched V1
-// launches (grid = the active (trial, CTA) tiles of all trials) and one advance launch, captured
-// once per (K, V1 variant) as a CUDA graph.  Every trial keeps its own device step counter;
+// Per chunk of K steps: one batched LGN launch (grid = cell CTAs x trials), then either one
+// cooperative V1 launch that runs the K steps of every active trial with the trials' state in
+// registers (slots of CTAs taking the trials in turn, a barrier per trial between steps) or K
+// batched per-step V1 launches (grid = the active (trial, CTA) tiles of all trials), and one
+// advance launch, captured once per (K, V1 variant) as a CUDA graph.  Every trial keeps its own device step counter;
 // chunks run as a graph only while every active trial has K or more steps left, otherwise as
 // direct launches of the smallest remainder, so no kernel steps a trial past its end and each
 // trial computes exactly what pv1_run computes for it alone.  The tile list is rebuilt on the
@@ -17,6 +19,8 @@
 #include "pv1_internal.cuh"
 
 using namespace pv1;
+
+constexpr int kCandidates = 12;
 
 struct pv1_batch {
     std::string err;
@@ -32,6 +36,9 @@ struct pv1_batch {
     BatchLgn *dL = nullptr;
     int2 *dTiles = nullptr;
     int *dNTiles = nullptr;
+    int *dActive = nullptr, *dNActive = nullptr;   // active trial list (persistent variant)
+    unsigned *dBar = nullptr;                      // per-trial barrier counters
+    int slotCtas = 0, nSlots = 0;                  // persistent variant: CTAs per slot, slots
     int totalTiles = 0;
     int maxCellCtas = 0;
     bool allClass = true;
@@ -45,10 +52,12 @@ struct pv1_batch {
     std::vector<char> activeSet;
     std::vector<int2> hTiles;
     int hNTiles = 0;
-    int K = 64, minB = 1;
+    std::vector<int> hActive;
+    int hNActive = 0;
+    int K = 64, minB = 1;                    // minB 0: persistent variant, 1-3: per-step kernels
     bool tune = false;
     int nextCandidate = 0;
-    float times[9];
+    float times[kCandidates];
     std::map<int, cudaGraphExec_t> graphs;   // key K*4 + minB
     long long launches = 0;
     std::vector<void *> allocs;
@@ -57,6 +66,7 @@ struct pv1_batch {
 namespace {
 
 const int kCandK[3] = {16, 32, 64};
+// candidate c: chunk length kCandK[c / 4], V1 variant c % 4 (0: persistent, 1-3: minB)
 
 int bfail(pv1_batch *b, int code, const std::string &m) {
     if (b) b->err = m;
@@ -96,6 +106,14 @@ int refresh_tiles(pv1_batch *b) {
         PV1_BCUDA(b, cudaMemcpyAsync(b->dTiles, b->hTiles.data(), b->hTiles.size() * sizeof(int2),
                                      cudaMemcpyHostToDevice, b->stream));
     PV1_BCUDA(b, cudaMemcpyAsync(b->dNTiles, &b->hNTiles, sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    b->hActive.clear();
+    for (int q = 0; q < b->n; q++)
+        if (act[q]) b->hActive.push_back(q);
+    b->hNActive = (int)b->hActive.size();
+    if (b->hNActive)
+        PV1_BCUDA(b, cudaMemcpyAsync(b->dActive, b->hActive.data(), b->hActive.size() * sizeof(int),
+                                     cudaMemcpyHostToDevice, b->stream));
+    PV1_BCUDA(b, cudaMemcpyAsync(b->dNActive, &b->hNActive, sizeof(int), cudaMemcpyHostToDevice, b->stream));
     // the host vectors are reused by the next refresh: wait for the copies
     PV1_BCUDA(b, cudaStreamSynchronize(b->stream));
     return PV1_OK;
@@ -117,11 +135,18 @@ int issue(pv1_batch *b, int k, int minB, long long *launches) {
             n += lgn_step_launches(b->views[q].lp, k);
         }
     }
-    for (int s = 0; s < k; s++) {
-        e = launch_v1_batch_step(b->dT, b->dTiles, b->dNTiles, b->totalTiles, s, b->rng, minB, b->stream);
-        if (e != cudaSuccess) return bfail(b, PV1_E_CUDA, std::string("v1 batch: ") + cudaGetErrorString(e));
+    if (minB == 0) {
+        e = launch_v1_batch_persistent(b->dT, b->dActive, b->dNActive, b->slotCtas, b->nSlots, k, b->dBar, b->n,
+                                       b->rng, b->stream);
+        if (e != cudaSuccess) return bfail(b, PV1_E_CUDA, std::string("v1 batch persistent: ") + cudaGetErrorString(e));
+        n += 1;
+    } else {
+        for (int s = 0; s < k; s++) {
+            e = launch_v1_batch_step(b->dT, b->dTiles, b->dNTiles, b->totalTiles, s, b->rng, minB, b->stream);
+            if (e != cudaSuccess) return bfail(b, PV1_E_CUDA, std::string("v1 batch: ") + cudaGetErrorString(e));
+        }
+        n += k;
     }
-    n += k;
     e = launch_batch_advance(b->dT, b->n, k, b->dSimTime, b->stream);
     if (e != cudaSuccess) return bfail(b, PV1_E_CUDA, cudaGetErrorString(e));
     n += 1;
@@ -236,7 +261,15 @@ int pv1_batch_create(pv1_plan *const *plans, uint32_t nTrials, const uint64_t *t
                                  cudaMemcpyHostToDevice, b->stream));
     r = balloc(b, &b->dTiles, (size_t)b->totalTiles);
     r |= balloc(b, &b->dNTiles, 1);
+    r |= balloc(b, &b->dActive, nTrials);
+    r |= balloc(b, &b->dNActive, 1);
+    r |= balloc(b, &b->dBar, nTrials);
     if (r) return r;
+    // persistent variant: slots as large as the largest trial, as many as stay co-resident
+    for (int q = 0; q < b->n; q++) b->slotCtas = std::max(b->slotCtas, b->hT[q].nCta);
+    const int cap = v1_batch_persistent_capacity(b->rng, b->device);
+    b->nSlots = b->slotCtas > 0 ? std::min(cap / b->slotCtas, b->n) : 0;
+    if (b->nSlots > 0) b->minB = 0;
     PV1_BCUDA(b, cudaStreamSynchronize(b->stream));
     return refresh_tiles(b);
 }
@@ -260,7 +293,7 @@ int pv1_batch_autotune(pv1_batch *b, int enable) {
     b->nextCandidate = 0;
     if (!b->tune) {
         b->K = 64;
-        b->minB = 1;
+        b->minB = b->nSlots > 0 ? 0 : 1;
     }
     return PV1_OK;
 }
@@ -289,9 +322,11 @@ int64_t pv1_batch_run(pv1_batch *b, uint64_t maxSteps, float *ms) {
         if (left == 0 || (maxSteps && done >= maxSteps)) break;
         int r = refresh_tiles(b);
         if (r) return r;
-        const bool tuning = b->tune && b->nextCandidate < 9;
-        const int K = tuning ? kCandK[b->nextCandidate / 3] : b->K;
-        const int minB = tuning ? b->nextCandidate % 3 + 1 : b->minB;
+        if (b->tune && b->nextCandidate < kCandidates && b->nextCandidate % 4 == 0 && b->nSlots == 0)
+            b->nextCandidate++;   // no persistent variant on this device / for these trial sizes
+        const bool tuning = b->tune && b->nextCandidate < kCandidates;
+        const int K = tuning ? kCandK[b->nextCandidate / 4] : b->K;
+        const int minB = tuning ? b->nextCandidate % 4 : b->minB;
         long long k = std::min<long long>(K, minLeft);
         if (maxSteps) k = std::min<long long>(k, (long long)(maxSteps - done));
         if (b->allClass && k == K) {
@@ -312,22 +347,23 @@ int64_t pv1_batch_run(pv1_batch *b, uint64_t maxSteps, float *ms) {
                 cudaEventDestroy(t1);
                 b->times[b->nextCandidate] = t;
                 b->nextCandidate++;
-                if (b->nextCandidate == 9) {
+                if (b->nextCandidate < kCandidates && b->nextCandidate % 4 == 0 && b->nSlots == 0) b->nextCandidate++;
+                if (b->nextCandidate >= kCandidates) {
                     // fastest per step
                     int best = -1;
-                    for (int c = 0; c < 9; c++)
-                        if (b->times[c] > 0 && (best < 0 || b->times[c] / kCandK[c / 3] <
-                                                                b->times[best] / kCandK[best / 3]))
+                    for (int c = 0; c < kCandidates; c++)
+                        if (b->times[c] > 0 && (best < 0 || b->times[c] / kCandK[c / 4] <
+                                                                b->times[best] / kCandK[best / 4]))
                             best = c;
                     if (best >= 0) {
-                        b->K = kCandK[best / 3];
-                        b->minB = best % 3 + 1;
+                        b->K = kCandK[best / 4];
+                        b->minB = best % 4;
                     }
                 }
             } else {
                 PV1_BCUDA(b, cudaGraphLaunch(g, b->stream));
             }
-            b->launches += K + 2;
+            b->launches += (minB == 0 ? 1 : K) + 2;
         } else {
             r = issue(b, (int)k, minB, &b->launches);
             if (r) return r;

@@ -315,6 +315,11 @@ cudaError_t launch_batch_rates(const BatchTrial *trials, const unsigned *counts,
                                const double *simTime, int trial, int nV1, double *rates,
                                double *meanRate, cudaStream_t st);
 int v1_batch_regs(int minB, bool rng);
+// Batched trials in one cooperative launch per chunk (slots of slotCtas CTAs, per-trial barriers).
+int v1_batch_persistent_capacity(bool rng, int device);
+cudaError_t launch_v1_batch_persistent(const BatchTrial *trials, const int *activeList, const int *nActive,
+                                       int slotCtas, int nSlots, int K, unsigned *barriers, int nTrials, bool rng,
+                                       cudaStream_t st);
 
 // Fixed-point scale for far-delivery accumulation: integer adds are associative, so the
 // sum of events does not depend on their order and runs are reproducible.

@@ -340,6 +340,8 @@ __device__ __forceinline__ float intensity(int coneType, float x, float y, int l
     }
 }
 
+constexpr int kSpatialReg = 8;   // samples per lane held in registers by the spatial stage
+
 // Spatial stage, once per (frame, cell): mean luminance of the cell's samples (cone type 3),
 // local contrast clip(I/mean - 1, +-1) and its DoG-weighted sum
 // (src/discrete_input_convol.cu:1474-1532).  One warp per (cell, frame); the layered
@@ -356,19 +358,52 @@ __global__ void __launch_bounds__(256) lgn_spatial_kernel(
     const int layer = layer0 + li;
     const float *sc_x = SC + (size_t)cell * nSample;
     const float *sc_y = SC + (size_t)nMagno * nSample + (size_t)cell * nSample;
-    float sum = 0.f;
-    for (int s = lane; s < nSample; s += 32) sum += intensity(3, sc_x[s], sc_y[s], layer, texL, texM, texS);
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    const float mean = sum / nSample;
     const int type = coneType[cell];
-    float acc = 0.f;
-    for (int s = lane; s < nSample; s += 32) {
-        float I = intensity(type, sc_x[s], sc_y[s], layer, texL, texM, texS);
-        float c;
-        if (mean > 0) c = I / mean - 1.0f;
-        else c = I;
-        if (fabsf(c) > 1.0f) c = copysignf(1.0f, c);
-        acc += SW[(size_t)cell * nSample + s] * c;
+    float sum = 0.f, acc = 0.f;
+    if (nSample <= 32 * kSpatialReg) {
+        // each texel is fetched once: the cell's intensities stay in registers between the mean
+        // and the contrast pass (same values as fetching them twice)
+        float Iv[kSpatialReg];
+#pragma unroll
+        for (int k = 0; k < kSpatialReg; k++) {
+            const int s = lane + 32 * k;
+            Iv[k] = 0.f;
+            if (s < nSample) {
+                const float x = sc_x[s], y = sc_y[s];
+                const float L = tex2DLayered<float>(texL, x, y, layer), M = tex2DLayered<float>(texM, x, y, layer);
+                sum += (L + M) / 2.0f;
+                if (type == 3) Iv[k] = (L + M) / 2.0f;
+                else if (type == 0) Iv[k] = L;
+                else if (type == 1) Iv[k] = M;
+                else if (type == 2) Iv[k] = tex2DLayered<float>(texS, x, y, layer);
+                else if (type == 4) Iv[k] = L * 0.45436904f + M * 0.47353315f + tex2DLayered<float>(texS, x, y, layer) * 0.0720978f;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        const float mean = sum / nSample;
+#pragma unroll
+        for (int k = 0; k < kSpatialReg; k++) {
+            const int s = lane + 32 * k;
+            if (s < nSample) {
+                float c;
+                if (mean > 0) c = Iv[k] / mean - 1.0f;
+                else c = Iv[k];
+                if (fabsf(c) > 1.0f) c = copysignf(1.0f, c);
+                acc += SW[(size_t)cell * nSample + s] * c;
+            }
+        }
+    } else {
+        for (int s = lane; s < nSample; s += 32) sum += intensity(3, sc_x[s], sc_y[s], layer, texL, texM, texS);
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        const float mean = sum / nSample;
+        for (int s = lane; s < nSample; s += 32) {
+            float I = intensity(type, sc_x[s], sc_y[s], layer, texL, texM, texS);
+            float c;
+            if (mean > 0) c = I / mean - 1.0f;
+            else c = I;
+            if (fabsf(c) > 1.0f) c = copysignf(1.0f, c);
+            acc += SW[(size_t)cell * nSample + s] * c;
+        }
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) S[(size_t)(row0 + li) * nMagno + cell] = acc;

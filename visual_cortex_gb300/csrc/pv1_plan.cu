@@ -46,6 +46,10 @@ struct pv1_plan {
     int nParvo = 0, pSample = 0;
     float *d_pTW = nullptr, *d_pSW = nullptr, *d_pSC = nullptr, *d_pS = nullptr;
     int *d_pCone = nullptr;
+    // stimulus texture arrays kept between loads of movies of the same size (one layer batch)
+    cudaArray_t stimArr[3] = {nullptr, nullptr, nullptr};
+    cudaTextureObject_t stimTex[3] = {0, 0, 0};
+    uint32_t stimW = 0, stimH = 0, stimL = 0;
     int nFrame = 0;
     // LGN spike ring
     float *d_lgnRing = nullptr, *d_lgnFr = nullptr;
@@ -375,10 +379,13 @@ int pv1_plan_create(const pv1_v1_config *cfg, pv1_plan **out) {
     return PV1_OK;
 }
 
+static void release_stimulus_textures(pv1_plan *p);
+
 void pv1_plan_destroy(pv1_plan *p) {
     if (!p) return;
     cudaStreamSynchronize(p->stream);
     drop_graph(p);
+    release_stimulus_textures(p);
     for (void *ptr : p->allocs) cudaFree(ptr);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
@@ -743,6 +750,16 @@ int pv1_lgn_get_tables(pv1_plan *p, float *TW, float *SW, float *SC, float *maxC
     return PV1_OK;
 }
 
+static void release_stimulus_textures(pv1_plan *p) {
+    for (int ch = 0; ch < 3; ch++) {
+        if (p->stimTex[ch]) cudaDestroyTextureObject(p->stimTex[ch]);
+        if (p->stimArr[ch]) cudaFreeArray(p->stimArr[ch]);
+        p->stimTex[ch] = 0;
+        p->stimArr[ch] = nullptr;
+    }
+    p->stimW = p->stimH = p->stimL = 0;
+}
+
 int pv1_stimulus_load(pv1_plan *p, uint32_t nFrame, uint32_t height, uint32_t width,
                       const float init_LMS[3], const float *frames) {
     if (!p || !init_LMS || (nFrame && !frames)) return PV1_E_ARG;
@@ -750,42 +767,61 @@ int pv1_stimulus_load(pv1_plan *p, uint32_t nFrame, uint32_t height, uint32_t wi
     if (nFrame < 1 || width < 1 || height < 1 || width > 16384 || height > 16384)
         return fail(p, PV1_E_ARG, "bad stimulus size");
     const int nMagno = p->nMagno;
-    if (p->d_S) free_one(p, p->d_S);
-    int r = dev_alloc(p, &p->d_S, (size_t)(nFrame + 1) * std::max(nMagno, 1));
-    if (r) return r;
-    if (p->nParvo > 0) {
-        if (p->d_pS) free_one(p, p->d_pS);
-        r = dev_alloc(p, &p->d_pS, (size_t)(nFrame + 1) * 2 * p->nParvo);
+    const bool sameSize = p->stimReady && (int)nFrame == p->nFrame;
+    int r = 0;
+    if (!sameSize) {  // the spatial-stage tables of a movie of another length
+        if (p->d_S) free_one(p, p->d_S);
+        r = dev_alloc(p, &p->d_S, (size_t)(nFrame + 1) * std::max(nMagno, 1));
         if (r) return r;
+        if (p->nParvo > 0) {
+            if (p->d_pS) free_one(p, p->d_pS);
+            r = dev_alloc(p, &p->d_pS, (size_t)(nFrame + 1) * 2 * p->nParvo);
+            if (r) return r;
+        }
     }
     const size_t npix = (size_t)width * height;
     // process the movie in batches of <= 2047 layers plus the initial-luminance layer
     const int maxLayers = 2048;
-    std::vector<float> plane(npix);
     cudaChannelFormatDesc desc = cudaCreateChannelDesc(32, 0, 0, 0, cudaChannelFormatKindFloat);
+    std::vector<float> initPlanes(3 * npix);
+    for (int ch = 0; ch < 3; ch++) std::fill(initPlanes.begin() + ch * npix, initPlanes.begin() + (ch + 1) * npix, init_LMS[ch]);
     for (uint32_t f0 = 0; f0 < nFrame + 1; f0 += maxLayers) {
         const uint32_t nl = std::min<uint32_t>(maxLayers, nFrame + 1 - f0);
+        const uint32_t nMovie = f0 < nFrame ? std::min<uint32_t>(nl, nFrame - f0) : 0;
         cudaArray_t arr[3] = {nullptr, nullptr, nullptr};
         cudaTextureObject_t tex[3] = {0, 0, 0};
+        // a movie held in one batch keeps its arrays and texture objects for the next load
+        const bool single = f0 == 0 && nl == nFrame + 1;
+        const bool reuse = single && p->stimArr[0] && p->stimW == width && p->stimH == height && p->stimL == nl;
+        if (single && !reuse) release_stimulus_textures(p);
         for (int ch = 0; ch < 3; ch++) {
-            PV1_CUDA(p, cudaMalloc3DArray(&arr[ch], &desc, make_cudaExtent(width, height, nl), cudaArrayLayered));
-            for (uint32_t l = 0; l < nl; l++) {
-                const uint32_t f = f0 + l;
-                const float *src;
-                if (f < nFrame) {
-                    src = frames + ((size_t)f * 3 + ch) * npix;
-                } else {
-                    std::fill(plane.begin(), plane.end(), init_LMS[ch]);
-                    src = plane.data();
-                }
+            if (reuse) arr[ch] = p->stimArr[ch];
+            else PV1_CUDA(p, cudaMalloc3DArray(&arr[ch], &desc, make_cudaExtent(width, height, nl), cudaArrayLayered));
+            // every movie layer of this channel in one copy: the source slices are the channel's
+            // planes, 3 planes apart ([frame][channel][h][w])
+            if (nMovie) {
                 cudaMemcpy3DParms cp{};
-                cp.srcPtr = make_cudaPitchedPtr((void *)src, width * sizeof(float), width, height);
+                cp.srcPtr = make_cudaPitchedPtr((void *)(frames + ((size_t)f0 * 3 + ch) * npix), width * sizeof(float),
+                                                width, 3 * (size_t)height);
                 cp.dstArray = arr[ch];
-                cp.dstPos = make_cudaPos(0, 0, l);
+                cp.dstPos = make_cudaPos(0, 0, 0);
+                cp.extent = make_cudaExtent(width, height, nMovie);
+                cp.kind = cudaMemcpyHostToDevice;
+                PV1_CUDA(p, cudaMemcpy3DAsync(&cp, p->stream));
+            }
+            if (nMovie < nl) {  // the initial-luminance layer closes the last batch
+                cudaMemcpy3DParms cp{};
+                cp.srcPtr = make_cudaPitchedPtr((void *)(initPlanes.data() + ch * npix), width * sizeof(float), width,
+                                                height);
+                cp.dstArray = arr[ch];
+                cp.dstPos = make_cudaPos(0, 0, nMovie);
                 cp.extent = make_cudaExtent(width, height, 1);
                 cp.kind = cudaMemcpyHostToDevice;
                 PV1_CUDA(p, cudaMemcpy3DAsync(&cp, p->stream));
-                if (f >= nFrame) PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+            }
+            if (reuse) {
+                tex[ch] = p->stimTex[ch];
+                continue;
             }
             cudaResourceDesc rd{};
             rd.resType = cudaResourceTypeArray;
@@ -798,6 +834,15 @@ int pv1_stimulus_load(pv1_plan *p, uint32_t nFrame, uint32_t height, uint32_t wi
             td.normalizedCoords = 1;
             PV1_CUDA(p, cudaCreateTextureObject(&tex[ch], &rd, &td, nullptr));
         }
+        if (single && !reuse) {
+            for (int ch = 0; ch < 3; ch++) {
+                p->stimArr[ch] = arr[ch];
+                p->stimTex[ch] = tex[ch];
+            }
+            p->stimW = width;
+            p->stimH = height;
+            p->stimL = nl;
+        }
         if (nMagno > 0)
             PV1_CUDA(p, launch_lgn_spatial(tex[0], tex[1], tex[2], p->d_SW, p->d_SC, p->d_coneType, nMagno,
                                           p->mSample, 0, (int)nl, (int)f0, p->d_S, p->stream));
@@ -805,9 +850,11 @@ int pv1_stimulus_load(pv1_plan *p, uint32_t nFrame, uint32_t height, uint32_t wi
             PV1_CUDA(p, launch_parvo_spatial(tex[0], tex[1], tex[2], p->d_pSW, p->d_pSC, p->d_pCone, p->nParvo,
                                             p->pSample, (int)nl, (int)f0, p->d_pS, p->stream));
         PV1_CUDA(p, cudaStreamSynchronize(p->stream));
-        for (int ch = 0; ch < 3; ch++) {
-            cudaDestroyTextureObject(tex[ch]);
-            cudaFreeArray(arr[ch]);
+        if (!single) {
+            for (int ch = 0; ch < 3; ch++) {
+                cudaDestroyTextureObject(tex[ch]);
+                cudaFreeArray(arr[ch]);
+            }
         }
     }
     p->nFrame = (int)nFrame;
@@ -816,8 +863,20 @@ int pv1_stimulus_load(pv1_plan *p, uint32_t nFrame, uint32_t height, uint32_t wi
     p->lp.fs.nFrame = (int)nFrame;
     p->lp.fs.initRow = (int)nFrame;
     p->stimReady = true;
-    drop_graph(p);
+    // the captured step graph stays valid when the tables kept their place and size
+    if (!sameSize) drop_graph(p);
     return PV1_OK;
+}
+
+int pv1_host_alloc(uint64_t bytes, void **out) {
+    if (!out) return PV1_E_ARG;
+    *out = nullptr;
+    if (bytes == 0) return PV1_E_ARG;
+    return cudaHostAlloc(out, (size_t)bytes, cudaHostAllocDefault) == cudaSuccess ? PV1_OK : PV1_E_NOMEM;
+}
+
+void pv1_host_free(void *ptr) {
+    if (ptr) cudaFreeHost(ptr);
 }
 
 int pv1_lgn_get_spatial(pv1_plan *p, float *S) {

@@ -66,6 +66,13 @@ __device__ __forceinline__ RecOff rec_off(const V1Params &P) {
 }
 
 // Per-neuron dynamic state (registers).
+// LGN input of the next step fetched ahead by the persistent kernel: the synapses that
+// received spikes (bit mask, synapse order) and the spike word and weight of the first one.
+struct LgnPre {
+    unsigned mask;
+    float s0, f0;
+};
+
 struct NState {
     float v, w, tBack, lastNoise;
     float gE[kMaxNG], hE[kMaxNG], gI[kMaxNG], hI[kMaxNG], gFF[kMaxNG], hFF[kMaxNG];
@@ -414,15 +421,15 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
                                              const float *__restrict__ lgnSInfo,
                                              NState &st, curandStateMRG32k3a &condState,
                                              curandStateMRG32k3a &noisyState,
-                                             const unsigned *preMask = nullptr) {
+                                             const LgnPre *pre = nullptr) {
     const int nV1 = P.nV1;
     const float dt = P.dt;
     const int ngE = P.ngE, ngI = P.ngI, ngFF = P.ngFF;
     // spike words of this neuron's LGN inputs, gathered first so that they overlap the decay
-    // (unless the caller fetched them already: preMask = synapses that received spikes)
+    // (unless the caller fetched them already: pre)
     float spReg[RegSyn ? kMaxLgnReg : 1];
     if constexpr (RegSyn) {
-        if (!preMask) {
+        if (!pre) {
 #pragma unroll
             for (int q = 0; q < kMaxLgnReg; q++) spReg[q] = q < m ? __ldcg(lgnSInfo + lgnIds[q]) : 0.f;
         }
@@ -505,8 +512,13 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
     if constexpr (RegSyn) {
         // synapses that received a spike, as a bit mask; they are visited in synapse order
         unsigned mask = 0u;
-        if (preMask) {
-            mask = *preMask;
+        if (pre) {
+            mask = pre->mask;
+            if (mask) {  // the first spiking synapse comes with its spike word and weight
+                lgn_input<Rng>(P, itype, pre->s0, pre->f0, backingUp, tBack, pf, nSynFF, g0, h0, g1, h1, condState,
+                               recFF, nFF);
+                mask &= mask - 1;
+            }
         } else {
 #pragma unroll
             for (int q = 0; q < kMaxLgnReg; q++) mask |= (spReg[q] >= 1.0f ? 1u : 0u) << q;
@@ -1216,7 +1228,7 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
     const int farN1 = (P.farOn && active) ? P.farN1[i] : 0;
     const bool isFarPre = P.farOn && active && P.farPre[i];
     __shared__ unsigned s_arrived;
-    unsigned lgnMask = 0u;
+    LgnPre lgnPre{0u, 0.f, 0.f};
     bool haveMask = false;
     for (int s = 0; s < K; s++) {
         const long long t = t0 + s;
@@ -1225,7 +1237,7 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
         if (active) {
             const float *lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
             sInfo = step_neuron<Rng, true>(P, t, i, itype, tonic, depC, m, lgnIds, lgnSInfo, st, condState,
-                                           noisyState, haveMask ? &lgnMask : nullptr);
+                                           noisyState, haveMask ? &lgnPre : nullptr);
             if (P.spikeCount && sInfo >= 1.0f) P.spikeCount[i] += (unsigned)floorf(sInfo);
         }
         if (P.farOn) {
@@ -1234,12 +1246,21 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
         }
         if (s + 1 < K) {
             barrier_arrive(barrier, &s_arrived);
-            lgnMask = 0u;
+            lgnPre.mask = 0u;
             if (active) {
                 const float *next = lgnRing + (size_t)((t + 1) % lgnSlots) * P.lgnN;
+                float sp[kMaxLgnReg];
 #pragma unroll
-                for (int q = 0; q < kMaxLgnReg; q++)
-                    lgnMask |= ((q < m && __ldcg(next + lgnIds[q]) >= 1.0f) ? 1u : 0u) << q;
+                for (int q = 0; q < kMaxLgnReg; q++) sp[q] = q < m ? __ldcg(next + lgnIds[q]) : 0.f;
+                float s0 = 0.f;
+#pragma unroll
+                for (int q = kMaxLgnReg - 1; q >= 0; q--) {
+                    const bool hit = sp[q] >= 1.0f;
+                    lgnPre.mask |= (hit ? 1u : 0u) << q;
+                    if (hit) s0 = sp[q];
+                }
+                lgnPre.s0 = s0;
+                if (lgnPre.mask) lgnPre.f0 = __ldg(P.sLGN + (size_t)(__ffs(lgnPre.mask) - 1) * P.nV1 + i);
             }
             haveMask = true;
             if (!barrier_wait(barrier, (unsigned)gridDim.x * (unsigned)(s + 1), &s_arrived, P.err)) break;
@@ -1387,6 +1408,122 @@ __global__ void __launch_bounds__(kCta, MinB) v1_batch_step_kernel(const BatchTr
     const long long t = *sT.step + stepOffset;
     if (t >= sT.tEnd) return;
     v1_step_body<Rng>(sT.v, t, tile.y, sT.nCta, sT.lgnRing, sT.lgnSlots, t >= sT.tDeliverFrom ? 1 : 0, 1, sm);
+}
+
+// Batched trials in one cooperative launch per chunk: the grid is split into slots of
+// slotCtas CTAs (the largest trial's CTA count); slot s runs active trials s, s + nSlots, ...
+// one after the other, each for its steps of the chunk, with the trial's state in registers
+// and a barrier among the trial's own CTAs between steps (no grid-wide barrier: trials are
+// independent).  The step is the per-step kernels' (same delivery order, same arithmetic), so
+// every trial computes what the per-step batch and pv1_run compute for it.
+template <bool Rng>
+__device__ __forceinline__ void batch_trial_steps(const V1Params &P, long long t0, int steps, int cta, int nCta,
+                                                  const float *__restrict__ lgnRing, int lgnSlots, bool deliverFirst,
+                                                  unsigned *barrier, Smem &sm, unsigned *s_arrived) {
+    const int bs = P.blockSize;
+    const int nq = (bs + kCta - 1) / kCta;
+    const int b = cta / nq;
+    const int local = (cta % nq) * kCta + threadIdx.x;
+    const bool active = local < bs;
+    const int i = b * bs + (active ? local : 0);
+    const int itype = type_of(P, active ? local : 0);
+    NState st;
+    load_state(P, i, st);
+    curandStateMRG32k3a condState, noisyState;
+    if (Rng && P.condRng && active) condState = P.rGenCond[i];
+    if (Rng && P.noiseRng && active) noisyState = P.rNoisy[i];
+    const float tonic = active ? P.tonicDep[i] : 0.f;
+    const float depC = tonic_current(P, itype, tonic);
+    const int m = active ? P.nLGNperV1[i] : 0;
+    const int farE0 = (P.farOn && active) ? P.farOff[i] : 0;
+    const int farDeg = (P.farOn && active) ? P.farOff[i + 1] - farE0 : 0;
+    const int farN1 = (P.farOn && active) ? P.farN1[i] : 0;
+    const bool isFarPre = P.farOn && active && P.farPre[i];
+    for (int s = 0; s < steps; s++) {
+        const long long t = t0 + s;
+        if (s > 0 || deliverFirst) deliver_prev<Rng>(P, t - 1, b, local, i, active, itype, st, condState, sm);
+        float sInfo = 0.f;
+        if (active) {
+            const float *lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
+            if (P.multiSpike)
+                sInfo = step_neuron_multi<Rng>(P, t, i, itype, tonic, depC, m, lgnSInfo, st, condState, noisyState);
+            else
+                sInfo = step_neuron<Rng, false>(P, t, i, itype, tonic, depC, m, nullptr, lgnSInfo, st, condState,
+                                                noisyState);
+            if (P.spikeCount && sInfo >= 1.0f) P.spikeCount[i] += (unsigned)floorf(sInfo);
+        }
+        if (P.farOn) {
+            far_push_list(P, t - 1, sm, cta, nCta);
+            far_phase(P, t, i, active, sInfo, isFarPre, farE0, farDeg, farN1, sm, cta);
+        }
+        if (s + 1 < steps) {
+            barrier_arrive(barrier, s_arrived);
+            if (!barrier_wait(barrier, (unsigned)nCta * (unsigned)(s + 1), s_arrived, P.err)) break;
+        }
+    }
+    if (active) {
+        store_state(P, i, st);
+        if (Rng && P.condRng) P.rGenCond[i] = condState;
+        if (Rng && P.noiseRng) P.rNoisy[i] = noisyState;
+    }
+}
+
+template <bool Rng>
+__global__ void __launch_bounds__(kCta, 2) v1_batch_persistent_kernel(const BatchTrial *__restrict__ trials,
+                                                                     const int *__restrict__ activeList,
+                                                                     const int *__restrict__ nActive, int slotCtas,
+                                                                     int nSlots, int K, unsigned *barriers) {
+    __shared__ Smem sm;
+    __shared__ __align__(16) BatchTrial sT;
+    __shared__ unsigned s_arrived;
+    const int slot = blockIdx.x / slotCtas, c = blockIdx.x % slotCtas;
+    const int na = *nActive;
+    for (int j = slot; j < na; j += nSlots) {
+        const int q = activeList[j];
+        __syncthreads();
+        const int *src = reinterpret_cast<const int *>(trials + q);
+        int *dst = reinterpret_cast<int *>(&sT);
+        for (int w = threadIdx.x; w < (int)(sizeof(BatchTrial) / sizeof(int)); w += kCta) dst[w] = src[w];
+        __syncthreads();
+        if (c >= sT.nCta) continue;
+        const long long t0 = *sT.step;
+        const long long left = sT.tEnd - t0;
+        const int steps = left < K ? (int)left : K;
+        if (steps <= 0) continue;
+        batch_trial_steps<Rng>(sT.v, t0, steps, c, sT.nCta, sT.lgnRing, sT.lgnSlots, t0 >= sT.tDeliverFrom,
+                               barriers + q, sm, &s_arrived);
+    }
+}
+
+int v1_batch_persistent_capacity(bool rng, int device) {
+    int perSM = 0, sms = 0;
+    cudaError_t e = rng ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_batch_persistent_kernel<true>, kCta, 0)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_batch_persistent_kernel<false>, kCta, 0);
+    if (e != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+    return perSM * sms;
+}
+
+cudaError_t launch_v1_batch_persistent(const BatchTrial *trials, const int *activeList, const int *nActive,
+                                       int slotCtas, int nSlots, int K, unsigned *barriers, int nTrials, bool rng,
+                                       cudaStream_t st) {
+    if (nSlots <= 0 || slotCtas <= 0) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(barriers, 0, (size_t)nTrials * sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nSlots * slotCtas);
+    cfg.blockDim = dim3(kCta);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (rng)
+        return cudaLaunchKernelEx(&cfg, v1_batch_persistent_kernel<true>, trials, activeList, nActive, slotCtas,
+                                  nSlots, K, barriers);
+    return cudaLaunchKernelEx(&cfg, v1_batch_persistent_kernel<false>, trials, activeList, nActive, slotCtas, nSlots,
+                              K, barriers);
 }
 
 template <bool Rng>

@@ -367,8 +367,13 @@ class Simulation:
             N.check(self.plan, rc, "pv1_persistent_mode")
         return rc == 1
 
-    def fetch_spikes(self, step0: int, n: int) -> np.ndarray:
-        out = np.empty((n, self.spec.nV1), f32)
+    def fetch_spikes(self, step0: int, n: int, out: np.ndarray | None = None) -> np.ndarray:
+        """Spike words [n][nV1] of steps step0..step0+n-1; `out` may be a caller-owned
+        (e.g. N.pinned_empty) float32 array of that shape."""
+        if out is None:
+            out = np.empty((n, self.spec.nV1), f32)
+        elif out.shape != (n, self.spec.nV1) or out.dtype != f32 or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous float32 array [n][nV1]")
         N.check(self.plan, N.lib.pv1_fetch_spikes(self.plan, int(step0), int(n), N.fptr(out)), "pv1_fetch_spikes")
         return out
 

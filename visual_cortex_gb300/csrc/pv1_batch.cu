@@ -349,12 +349,18 @@ int64_t pv1_batch_run(pv1_batch *b, uint64_t maxSteps, float *ms) {
                 b->nextCandidate++;
                 if (b->nextCandidate < kCandidates && b->nextCandidate % 4 == 0 && b->nSlots == 0) b->nextCandidate++;
                 if (b->nextCandidate >= kCandidates) {
-                    // fastest per step
+                    // fastest per step; a longer chunk is kept unless a shorter one is more than
+                    // 10% faster (one tuning chunk underestimates the per-chunk costs -- LGN
+                    // launch, host loop, partial chunks at trial ends -- that longer chunks
+                    // amortise over the whole sweep)
                     int best = -1;
-                    for (int c = 0; c < kCandidates; c++)
-                        if (b->times[c] > 0 && (best < 0 || b->times[c] / kCandK[c / 4] <
-                                                                b->times[best] / kCandK[best / 4]))
-                            best = c;
+                    for (int c = kCandidates - 1; c >= 0; c--) {
+                        if (b->times[c] <= 0) continue;
+                        const float per = b->times[c] / kCandK[c / 4];
+                        const float bestPer = best < 0 ? 0.f : b->times[best] / kCandK[best / 4];
+                        const bool shorter = best >= 0 && kCandK[c / 4] < kCandK[best / 4];
+                        if (best < 0 || (shorter ? per < 0.9f * bestPer : per < bestPer)) best = c;
+                    }
                     if (best >= 0) {
                         b->K = kCandK[best / 4];
                         b->minB = best % 4;

@@ -73,6 +73,25 @@ struct LgnPre {
     float s0, f0;
 };
 
+// Fetches the spike words of a neuron's (at most kMaxLgnReg) LGN synapses for one step: ids
+// at ids[q * Stride] (registers: Stride 1; shared memory: Stride kCta).
+template <int Stride>
+__device__ __forceinline__ LgnPre lgn_prefetch(const V1Params &P, const float *__restrict__ ring, const int *ids,
+                                               int m, int i) {
+    LgnPre pre{0u, 0.f, 0.f};
+    float sp[kMaxLgnReg];
+#pragma unroll
+    for (int q = 0; q < kMaxLgnReg; q++) sp[q] = q < m ? __ldcg(ring + ids[q * Stride]) : 0.f;
+#pragma unroll
+    for (int q = kMaxLgnReg - 1; q >= 0; q--) {
+        const bool hit = sp[q] >= 1.0f;
+        pre.mask |= (hit ? 1u : 0u) << q;
+        if (hit) pre.s0 = sp[q];
+    }
+    if (pre.mask) pre.f0 = __ldg(P.sLGN + (size_t)(__ffs(pre.mask) - 1) * P.nV1 + i);
+    return pre;
+}
+
 struct NState {
     float v, w, tBack, lastNoise;
     float gE[kMaxNG], hE[kMaxNG], gI[kMaxNG], hI[kMaxNG], gFF[kMaxNG], hFF[kMaxNG];
@@ -1247,21 +1266,7 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
         if (s + 1 < K) {
             barrier_arrive(barrier, &s_arrived);
             lgnPre.mask = 0u;
-            if (active) {
-                const float *next = lgnRing + (size_t)((t + 1) % lgnSlots) * P.lgnN;
-                float sp[kMaxLgnReg];
-#pragma unroll
-                for (int q = 0; q < kMaxLgnReg; q++) sp[q] = q < m ? __ldcg(next + lgnIds[q]) : 0.f;
-                float s0 = 0.f;
-#pragma unroll
-                for (int q = kMaxLgnReg - 1; q >= 0; q--) {
-                    const bool hit = sp[q] >= 1.0f;
-                    lgnPre.mask |= (hit ? 1u : 0u) << q;
-                    if (hit) s0 = sp[q];
-                }
-                lgnPre.s0 = s0;
-                if (lgnPre.mask) lgnPre.f0 = __ldg(P.sLGN + (size_t)(__ffs(lgnPre.mask) - 1) * P.nV1 + i);
-            }
+            if (active) lgnPre = lgn_prefetch<1>(P, lgnRing + (size_t)((t + 1) % lgnSlots) * P.lgnN, lgnIds, m, i);
             haveMask = true;
             if (!barrier_wait(barrier, (unsigned)gridDim.x * (unsigned)(s + 1), &s_arrived, P.err)) break;
         }
@@ -1419,7 +1424,8 @@ __global__ void __launch_bounds__(kCta, MinB) v1_batch_step_kernel(const BatchTr
 template <bool Rng>
 __device__ __forceinline__ void batch_trial_steps(const V1Params &P, long long t0, int steps, int cta, int nCta,
                                                   const float *__restrict__ lgnRing, int lgnSlots, bool deliverFirst,
-                                                  unsigned *barrier, Smem &sm, unsigned *s_arrived) {
+                                                  unsigned *barrier, Smem &sm, unsigned *s_arrived,
+                                                  int *sIds) {
     const int bs = P.blockSize;
     const int nq = (bs + kCta - 1) / kCta;
     const int b = cta / nq;
@@ -1439,17 +1445,32 @@ __device__ __forceinline__ void batch_trial_steps(const V1Params &P, long long t
     const int farDeg = (P.farOn && active) ? P.farOff[i + 1] - farE0 : 0;
     const int farN1 = (P.farOn && active) ? P.farN1[i] : 0;
     const bool isFarPre = P.farOn && active && P.farPre[i];
+    // short LGN lists: ids in shared memory (column per thread) for the trial's steps, and each
+    // step's spike words fetched while the trial's CTAs meet at the barrier
+    const bool smemIds = sIds && P.maxLGN <= kMaxLgnReg && !P.multiSpike;
+    if (smemIds) {
+#pragma unroll
+        for (int q = 0; q < kMaxLgnReg; q++)
+            sIds[q * kCta + threadIdx.x] = (active && q < m) ? __ldg(P.lgnId + (size_t)q * P.nV1 + i) : 0;
+    }
+    LgnPre pre{0u, 0.f, 0.f};
+    bool havePre = false;
     for (int s = 0; s < steps; s++) {
         const long long t = t0 + s;
         if (s > 0 || deliverFirst) deliver_prev<Rng>(P, t - 1, b, local, i, active, itype, st, condState, sm);
         float sInfo = 0.f;
         if (active) {
             const float *lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
-            if (P.multiSpike)
+            if (P.multiSpike) {
                 sInfo = step_neuron_multi<Rng>(P, t, i, itype, tonic, depC, m, lgnSInfo, st, condState, noisyState);
-            else
+            } else if (smemIds) {
+                if (!havePre) pre = lgn_prefetch<kCta>(P, lgnSInfo, sIds + threadIdx.x, m, i);
+                sInfo = step_neuron<Rng, true>(P, t, i, itype, tonic, depC, m, nullptr, lgnSInfo, st, condState,
+                                               noisyState, &pre);
+            } else {
                 sInfo = step_neuron<Rng, false>(P, t, i, itype, tonic, depC, m, nullptr, lgnSInfo, st, condState,
                                                 noisyState);
+            }
             if (P.spikeCount && sInfo >= 1.0f) P.spikeCount[i] += (unsigned)floorf(sInfo);
         }
         if (P.farOn) {
@@ -1458,6 +1479,9 @@ __device__ __forceinline__ void batch_trial_steps(const V1Params &P, long long t
         }
         if (s + 1 < steps) {
             barrier_arrive(barrier, s_arrived);
+            if (smemIds && active)
+                pre = lgn_prefetch<kCta>(P, lgnRing + (size_t)((t + 1) % lgnSlots) * P.lgnN, sIds + threadIdx.x, m, i);
+            havePre = smemIds;
             if (!barrier_wait(barrier, (unsigned)nCta * (unsigned)(s + 1), s_arrived, P.err)) break;
         }
     }
@@ -1476,6 +1500,7 @@ __global__ void __launch_bounds__(kCta, 2) v1_batch_persistent_kernel(const Batc
     __shared__ Smem sm;
     __shared__ __align__(16) BatchTrial sT;
     __shared__ unsigned s_arrived;
+    extern __shared__ int sIds[];   // [kMaxLgnReg][kCta] LGN synapse ids (dynamic)
     const int slot = blockIdx.x / slotCtas, c = blockIdx.x % slotCtas;
     const int na = *nActive;
     for (int j = slot; j < na; j += nSlots) {
@@ -1491,14 +1516,30 @@ __global__ void __launch_bounds__(kCta, 2) v1_batch_persistent_kernel(const Batc
         const int steps = left < K ? (int)left : K;
         if (steps <= 0) continue;
         batch_trial_steps<Rng>(sT.v, t0, steps, c, sT.nCta, sT.lgnRing, sT.lgnSlots, t0 >= sT.tDeliverFrom,
-                               barriers + q, sm, &s_arrived);
+                               barriers + q, sm, &s_arrived, sIds);
     }
+}
+
+// The kernel's shared memory (Smem, the trial block and 32 KB of ids) passes the 48 KB a
+// block gets without opting in.
+static cudaError_t batch_persistent_smem_optin() {
+    static cudaError_t done = cudaErrorNotReady;
+    if (done == cudaErrorNotReady) {
+        const int dyn = kMaxLgnReg * kCta * (int)sizeof(int);
+        done = cudaFuncSetAttribute(v1_batch_persistent_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+        if (done == cudaSuccess)
+            done = cudaFuncSetAttribute(v1_batch_persistent_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        dyn);
+    }
+    return done;
 }
 
 int v1_batch_persistent_capacity(bool rng, int device) {
     int perSM = 0, sms = 0;
-    cudaError_t e = rng ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_batch_persistent_kernel<true>, kCta, 0)
-                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_batch_persistent_kernel<false>, kCta, 0);
+    if (batch_persistent_smem_optin() != cudaSuccess) return 0;
+    const size_t dyn = (size_t)kMaxLgnReg * kCta * sizeof(int);
+    cudaError_t e = rng ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_batch_persistent_kernel<true>, kCta, dyn)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_batch_persistent_kernel<false>, kCta, dyn);
     if (e != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
     return perSM * sms;
@@ -1508,11 +1549,14 @@ cudaError_t launch_v1_batch_persistent(const BatchTrial *trials, const int *acti
                                        int slotCtas, int nSlots, int K, unsigned *barriers, int nTrials, bool rng,
                                        cudaStream_t st) {
     if (nSlots <= 0 || slotCtas <= 0) return cudaErrorInvalidValue;
-    cudaError_t e = cudaMemsetAsync(barriers, 0, (size_t)nTrials * sizeof(unsigned), st);
+    cudaError_t e = batch_persistent_smem_optin();
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(barriers, 0, (size_t)nTrials * sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nSlots * slotCtas);
     cfg.blockDim = dim3(kCta);
+    cfg.dynamicSmemBytes = (size_t)kMaxLgnReg * kCta * sizeof(int);
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;

@@ -340,7 +340,8 @@ int64_t pv1_batch_run(pv1_batch *batch, uint64_t maxSteps, float *ms);
  * CTAs between steps), available when the largest trial fits the co-resident grid;
  * 1, 2, 3 = one launch per step with 1, 2 or 3 resident CTAs per SM.
  * Autotuner: tries each chunk length in {16, 32, 64} with each variant for one chunk of the
- * real run and keeps the fastest per step; the tuning chunks are ordinary steps of the
+ * real run, in forward then in backward order, and keeps the fastest average per step (a
+ * shorter chunk only if more than 10% faster); the tuning chunks are ordinary steps of the
  * simulation.  enable = 0 fixes K = 64 and variant 0 (1 where 0 is not available). */
 int pv1_batch_autotune(pv1_batch *batch, int enable);
 /* Chosen chunk length, V1 variant (minB) and the measured ms per chunk of every candidate

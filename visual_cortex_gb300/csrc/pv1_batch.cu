@@ -322,11 +322,16 @@ int64_t pv1_batch_run(pv1_batch *b, uint64_t maxSteps, float *ms) {
         if (left == 0 || (maxSteps && done >= maxSteps)) break;
         int r = refresh_tiles(b);
         if (r) return r;
-        if (b->tune && b->nextCandidate < kCandidates && b->nextCandidate % 4 == 0 && b->nSlots == 0)
+        // tuning visits the candidates forward then backward (2 * kCandidates chunks) and
+        // averages the two per-step times of each, so that the drift of the activity over the
+        // first chunks (onset transient) does not favour the candidates tried first
+        auto cand_of = [](int idx) { return idx < kCandidates ? idx : 2 * kCandidates - 1 - idx; };
+        while (b->tune && b->nextCandidate < 2 * kCandidates && cand_of(b->nextCandidate) % 4 == 0 && b->nSlots == 0)
             b->nextCandidate++;   // no persistent variant on this device / for these trial sizes
-        const bool tuning = b->tune && b->nextCandidate < kCandidates;
-        const int K = tuning ? kCandK[b->nextCandidate / 4] : b->K;
-        const int minB = tuning ? b->nextCandidate % 4 : b->minB;
+        const bool tuning = b->tune && b->nextCandidate < 2 * kCandidates;
+        const int cand = tuning ? cand_of(b->nextCandidate) : 0;
+        const int K = tuning ? kCandK[cand / 4] : b->K;
+        const int minB = tuning ? cand % 4 : b->minB;
         long long k = std::min<long long>(K, minLeft);
         if (maxSteps) k = std::min<long long>(k, (long long)(maxSteps - done));
         if (b->allClass && k == K) {
@@ -345,10 +350,11 @@ int64_t pv1_batch_run(pv1_batch *b, uint64_t maxSteps, float *ms) {
                 PV1_BCUDA(b, cudaEventElapsedTime(&t, t0, t1));
                 cudaEventDestroy(t0);
                 cudaEventDestroy(t1);
-                b->times[b->nextCandidate] = t;
+                b->times[cand] = b->nextCandidate < kCandidates ? t : 0.5f * (b->times[cand] + t);
                 b->nextCandidate++;
-                if (b->nextCandidate < kCandidates && b->nextCandidate % 4 == 0 && b->nSlots == 0) b->nextCandidate++;
-                if (b->nextCandidate >= kCandidates) {
+                while (b->nextCandidate < 2 * kCandidates && cand_of(b->nextCandidate) % 4 == 0 && b->nSlots == 0)
+                    b->nextCandidate++;
+                if (b->nextCandidate >= 2 * kCandidates) {
                     // fastest per step; a longer chunk is kept unless a shorter one is more than
                     // 10% faster (one tuning chunk underestimates the per-chunk costs -- LGN
                     // launch, host loop, partial chunks at trial ends -- that longer chunks

@@ -237,6 +237,9 @@ def run_gb300(args):
         del wl, sim
         forms = {"batched": bench_batched(args.batch_trials)}
         forms["batched"]["vs_plain"] = forms["batched"]["value"] / value
+        bound = out.get("cpu_baseline", {}).get("reference_plain_gpu_bound")
+        if bound:
+            forms["batched"]["vs_reference_plain_gpu_bound"] = forms["batched"]["value"] / bound["value"]
         forms["adjoint"] = bench_adjoint()
         forms["lgn_bf16"] = bench_lgn_bf16()
         out["forms"] = forms
@@ -377,10 +380,37 @@ def cpu_baseline(wl, nsteps: int):
     cp = CpuPatch(wl)
     cp.step(2)
     dt = cp.time_steps(nsteps)
-    return {"value": wl.spec.nV1 * nsteps / dt, "unit": UNIT, "cores": cp.threads, "kind": "port",
-            "sample": f"{nsteps} steps of the same workload ({wl.spec.nV1} neurons), "
-                      f"CPU restatement with OpenMP on {cp.threads} threads ({cpu_model()})",
-            "seconds": dt}
+    out = {"value": wl.spec.nV1 * nsteps / dt, "unit": UNIT, "cores": cp.threads, "kind": "port",
+           "sample": f"{nsteps} steps of the same workload ({wl.spec.nV1} neurons), "
+                     f"CPU restatement with OpenMP on {cp.threads} threads ({cpu_model()})",
+           "seconds": dt}
+    out["reference_plain_gpu_bound"] = reference_plain_bound(cp, wl)
+    return out
+
+
+def reference_plain_bound(cp, wl, nsteps: int = 12):
+    """An upper bound on the reference's own plain-GPU rate for this workload: its step loop
+    runs the far delivery (fill_fSpikeTrain + recal_G_vec, src/patch.cu:6597-6620) on one host
+    thread every step, over every far synapse, whatever the GPU does meanwhile.  Timed here
+    with the oracle's C restatement of that loop on one thread (contiguous arrays, so no
+    slower than the reference's nested vectors), on the spike words of the CPU run above."""
+    import time
+    import oracle
+    L = oracle.lib()
+    L.orc_set_threads(1)
+    vo = cp.vo
+    sI = vo.get("sInfo")
+    L.orc_v1_deliver_far(vo.h)
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        vo.put("sInfo", sI)
+        L.orc_v1_deliver_far(vo.h)
+    per = (time.perf_counter() - t0) / nsteps
+    L.orc_set_threads(cp.threads)
+    return {"value": wl.spec.nV1 / per, "unit": UNIT, "host_far_ms_per_step": per * 1e3,
+            "far_synapses": int(np.sum(wl.net.nVec)),
+            "how": "neurons / (time of the reference's per-step host far delivery, restated in C, one thread); "
+                   "the reference's GPU work and its per-step host<->device copies only add to its step time"}
 
 
 def run_reference(args):

@@ -371,6 +371,10 @@ typedef struct {
     uint32_t recGrad;   /* 1: the gradient flows through the recurrent I spikes too; 0: the
                          * recurrent spike input is held constant in the backward (stop-gradient),
                          * the usual cure for the exploding recurrent surrogate gradient */
+    uint32_t ctaSplit;  /* CTAs per (trial, block), joined in a thread-block cluster: 1 or 2;
+                         * 0 = 2 when blockSize is a multiple of 64 and B * nblock * 2 CTAs fit
+                         * the SMs, else 1.  Results do not depend on it (up to the order of the
+                         * FP64 atomic sums of dL/d(kernel constants)). */
 } pv1_adj_problem;
 
 typedef struct {

@@ -12,12 +12,12 @@ pytestmark = pytest.mark.gpu
 
 
 def _patch(B=2, nblock=2, bs=128, nE=96, K=8, nLGN=96, T=320, seed=0, vThres=-50.0, w=0.6,
-           rate=0.01, rec_grad=True):
+           rate=0.01, rec_grad=True, cta_split=0):
     import torch
     from visual_cortex_gb300.adjoint import AdjointConfig, AdjointPatch
     rng = np.random.default_rng(seed)
     cfg = AdjointConfig(B=B, nblock=nblock, blockSize=bs, nE=nE, nLGN=nLGN, K=K, T=T, seg=64, win=160,
-                        vThres=vThres, rec_grad=rec_grad)
+                        vThres=vThres, rec_grad=rec_grad, cta_split=cta_split)
     N = cfg.N
     ids = rng.integers(0, nLGN, size=(K, N)).astype(np.int32)
     X = (rng.random((B, T, nLGN)) < rate).astype(np.uint8)
@@ -111,3 +111,27 @@ def test_finite_differences_subthreshold(native):
             fd = (float(loss(W, *tp)) - float(loss(W, *tm))) / (2 * h)
             g = float((tE, tI)[which].grad)
             assert abs(fd - g) <= 3e-2 * abs(g) + 1e-6, (which, fd, g)
+
+
+@pytest.mark.parametrize("rec_grad", [True, False])
+def test_cluster_split_matches_single_cta(native, rec_grad):
+    """A block held by a 2-CTA cluster (ballots, lambda_hI and the recurrent adjoint exchanged
+    through distributed shared memory) computes what one CTA computes: identical forward
+    outputs; gradients up to the order of their atomic sums (dL/dW sums the trials of the batch
+    with float atomics, dL/d(kernel constants) the CTAs with FP64 atomics)."""
+    import torch
+    out = []
+    for split in (1, 2):
+        patch, W = _patch(seed=2, rec_grad=rec_grad, cta_split=split)
+        target = torch.rand(patch.cfg.B, patch.cfg.T // patch.cfg.win, patch.cfg.N, device="cuda",
+                            generator=torch.Generator(device="cuda").manual_seed(5)) * 40
+        W1 = W.clone().requires_grad_(True)
+        tE, tI = _taus()
+        r, vb = patch.forward(W1, tE, tI)
+        (torch.mean((r - target) ** 2) + 0.1 * torch.mean((vb + 55.0) ** 2)).backward()
+        out.append((r.detach(), vb.detach(), W1.grad, float(tE.grad), float(tI.grad)))
+    (r1, v1, g1, e1, i1), (r2, v2, g2, e2, i2) = out
+    assert float(r1.sum()) > 0
+    assert torch.equal(r1, r2) and torch.equal(v1, v2)
+    assert float((g1 - g2).abs().max() / g1.abs().max()) < 1e-5
+    assert e1 == pytest.approx(e2, rel=1e-6, abs=1e-9) and i1 == pytest.approx(i2, rel=1e-6, abs=1e-9)

@@ -27,7 +27,7 @@ class AdjProblem(C.Structure):
                [(n, _PF) for n in ("dt", "vL", "vE", "vI", "vR", "vThres", "gL", "slope")] + \
                [("tRefE", _PU), ("tRefI", _PU)] + \
                [(n, _PF) for n in ("EdE", "ErE", "dodE", "EdI", "ErI", "dodI")] + \
-               [("recGrad", _PU)]
+               [("recGrad", _PU), ("ctaSplit", _PU)]
 
 
 class AdjBuffers(C.Structure):
@@ -84,6 +84,7 @@ class AdjointConfig:
     # bound over long windows in a strongly inhibitory network; False holds the recurrent
     # spike input constant in the backward (stop-gradient)
     rec_grad: bool = False
+    cta_split: int = 0             # CTAs per (trial, block) in a cluster: 0 automatic, 1 or 2
     tRefE: int = 16                # 2 ms
     tRefI: int = 8                 # 1 ms
     tauRE: float = 1.0             # AMPA rise
@@ -162,7 +163,8 @@ class AdjointPatch:
         return AdjProblem(B=c.B, nblock=c.nblock, blockSize=c.blockSize, nE=c.nE, nLGN=c.nLGN, K=c.K, T=c.T,
                           seg=c.seg, win=c.win, dt=c.dt, vL=c.vL, vE=c.vE, vI=c.vI, vR=c.vR, vThres=c.vThres,
                           gL=c.gL, slope=c.slope, tRefE=c.tRefE, tRefI=c.tRefI, EdE=v[0], ErE=v[1],
-                          dodE=v[2], EdI=v[3], ErI=v[4], dodI=v[5], recGrad=int(bool(c.rec_grad)))
+                          dodE=v[2], EdI=v[3], ErI=v[4], dodI=v[5], recGrad=int(bool(c.rec_grad)),
+                          ctaSplit=int(c.cta_split))
 
     def forward(self, W: torch.Tensor, tauE: torch.Tensor, tauI: torch.Tensor):
         """(rates [B][nWin][N] in Hz, vbar [B][nWin][N] in mV), differentiable in W, tauE, tauI."""

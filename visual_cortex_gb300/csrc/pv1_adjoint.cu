@@ -15,7 +15,9 @@
 //   outputs       per window of `win` steps: spike rate (Hz) and mean membrane potential.
 // Spikes are delivered at step granularity (no sub-step spike-time offsets).
 //
-// One CTA holds one (trial, block) pair, one thread per neuron; blocks do not interact.  The
+// One CTA (or a cluster of ctaSplit CTAs sharing the block's spike ballots and adjoints through
+// distributed shared memory) holds one (trial, block) pair, one thread per neuron; blocks do
+// not interact.  The
 // forward stores a checkpoint of (v, gE, hE, gI, hI, refractory count) every `seg` steps; the
 // backward walks the segments from the last one, recomputes each forward from its checkpoint
 // into a per-CTA scratch, then runs the adjoint backwards through it.  The recurrent term of
@@ -26,7 +28,11 @@
 #include <cstdint>
 #include <string>
 
+#include <cooperative_groups.h>
+
 #include "pv1_internal.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -36,7 +42,42 @@ struct AdjArgs {
     pv1_adj_problem p;
     pv1_adj_buffers b;
     int N, nI, nWin, nSeg;
+    int split;   // CTAs per (trial, block)
 };
+
+// Block-wide exchange between the CTAs of a (trial, block): stores go to every CTA of the
+// cluster (split > 1) or to this CTA's shared memory only.
+__device__ __forceinline__ void share_word(unsigned *addr, unsigned v, int split) {
+    if (split == 1) {
+        *addr = v;
+        return;
+    }
+    cg::cluster_group cl = cg::this_cluster();
+    for (int r = 0; r < split; r++) *cl.map_shared_rank(addr, r) = v;
+}
+
+__device__ __forceinline__ void share_float(float *addr, float v, int split) {
+    if (split == 1) {
+        *addr = v;
+        return;
+    }
+    cg::cluster_group cl = cg::this_cluster();
+    for (int r = 0; r < split; r++) *cl.map_shared_rank(addr, r) = v;
+}
+
+__device__ __forceinline__ void store_at_rank(float *addr, float v, int rank, int split) {
+    if (split == 1) {
+        *addr = v;
+        return;
+    }
+    *cg::this_cluster().map_shared_rank(addr, rank) = v;
+}
+
+// Barrier over the (trial, block)'s CTAs (with the memory ordering of their shared writes).
+__device__ __forceinline__ void block_sync(int split) {
+    if (split == 1) __syncthreads();
+    else cg::this_cluster().sync();
+}
 
 constexpr int kAdjMaxK = 32;
 
@@ -217,13 +258,15 @@ __device__ __forceinline__ const uint8_t *xs_get(XStage &s, const uint8_t *row, 
     return row;
 }
 
-__global__ void __launch_bounds__(1024) adj_forward_kernel(AdjArgs A, int stage) {
-    __shared__ unsigned ball[32];
+template <int MaxThreads>
+__global__ void __launch_bounds__(MaxThreads) adj_forward_kernel(AdjArgs A, int stage) {
+    __shared__ unsigned ball[2][32];   // double buffered: step t uses ball[t & 1]
     __shared__ __align__(8) uint64_t xbar[3];
     extern __shared__ __align__(16) uint8_t xbuf[];
     const pv1_adj_problem &P = A.p;
-    const int blk = blockIdx.x, b = blockIdx.y;
-    const int local = threadIdx.x;
+    const int split = A.split;
+    const int blk = blockIdx.x / split, b = blockIdx.y;
+    const int local = (blockIdx.x % split) * blockDim.x + threadIdx.x;
     const bool on = local < (int)P.blockSize;
     const int n = blk * (int)P.blockSize + (on ? local : 0);
     const size_t bn = (size_t)b * A.N + n;
@@ -235,6 +278,7 @@ __global__ void __launch_bounds__(1024) adj_forward_kernel(AdjArgs A, int stage)
     const uint8_t *Xb = A.b.X + (size_t)b * P.T * P.nLGN;
     XStage xs;
     xs_init(xs, xbuf, xbar, (int)P.nLGN, stage != 0);
+    if (split > 1) cg::this_cluster().sync();   // every CTA of the cluster runs before remote stores
     xs_issue(xs, Xb, 0, (int)P.nLGN);
     if (P.T > 1) xs_issue(xs, Xb + P.nLGN, 1, (int)P.nLGN);
     for (int t = 0; t < (int)P.T; t++) {
@@ -247,13 +291,14 @@ __global__ void __launch_bounds__(1024) adj_forward_kernel(AdjArgs A, int stage)
         float gE1 = 0.f, hE1 = 0.f, gI1 = 0.f, hI1 = 0.f, vnext = 0.f;
         if (on) vnext = adj_neuron_step(P, s, I0, isE, spk, refr, gE1, hE1, gI1, hI1);
         const unsigned bal = __ballot_sync(0xffffffffu, on && spk);
-        __syncthreads();   // the previous step's readers of ball[] and of its count row are done
-        if ((local & 31) == 0) ball[local >> 5] = bal;
-        __syncthreads();
+        // the readers of ball[t & 1] (step t - 2) and of the count row t - 1 finished before the
+        // previous step's barrier
+        if ((local & 31) == 0) share_word(&ball[t & 1][local >> 5], bal, split);
+        block_sync(split);
         if (t + 2 < (int)P.T) xs_issue(xs, Xb + (size_t)(t + 2) * P.nLGN, t + 2, (int)P.nLGN);
         const uint8_t *x = xs_get(xs, Xb + (size_t)t * P.nLGN, t);
         if (on) {
-            adj_inputs(A, x, n, local, hE1, hI1, ball);
+            adj_inputs(A, x, n, local, hE1, hI1, ball[t & 1]);
             s.v = vnext;
             s.gE = gE1; s.hE = hE1; s.gI = gI1; s.hI = hI1;
             cnt += spk ? 1.f : 0.f;
@@ -283,16 +328,19 @@ __device__ __forceinline__ void block_add_double(double v, double *out, double *
 
 constexpr int kScrWords = 7;   // v, gE, hE, gI, hI, flags, LGN event mask per neuron and step
 
-__global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A, int stage) {
-    __shared__ unsigned ball[32];
+template <int MaxThreads>
+__global__ void __launch_bounds__(MaxThreads) adj_backward_kernel(AdjArgs A, int stage) {
+    __shared__ unsigned ball[2][32];
     __shared__ float lam[1024];
     __shared__ float dS[1024];
     __shared__ double red[32];
     __shared__ __align__(8) uint64_t xbar[3];
     extern __shared__ __align__(16) uint8_t xbuf[];
     const pv1_adj_problem &P = A.p;
-    const int blk = blockIdx.x, b = blockIdx.y;
-    const int local = threadIdx.x;
+    const int split = A.split;
+    const int ctaN = (int)blockDim.x;
+    const int blk = blockIdx.x / split, b = blockIdx.y;
+    const int local = (blockIdx.x % split) * ctaN + threadIdx.x;
     const int bs = (int)P.blockSize;
     const bool on = local < bs;
     const int n = blk * bs + (on ? local : 0);
@@ -300,7 +348,7 @@ __global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A, int stage
     const bool isE = local < (int)P.nE;
     const float I0 = on ? A.b.I0[n] : 0.f;
     const size_t BN = (size_t)P.B * A.N;
-    float *scr = A.b.scratch + (size_t)(b * gridDim.x + blk) * P.seg * kScrWords * bs;
+    float *scr = A.b.scratch + (size_t)(b * (int)P.nblock + blk) * P.seg * kScrWords * bs;
     const float *C = A.b.Crec + (size_t)blk * A.nI * bs;
     const float rateScale = 1.f / ((float)P.win * P.dt * 1e-3f);
     const float invWin = 1.f / (float)P.win;
@@ -308,6 +356,7 @@ __global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A, int stage
     const uint8_t *Xb = A.b.X + (size_t)b * P.T * P.nLGN;
     XStage xs;
     xs_init(xs, xbuf, xbar, (int)P.nLGN, stage != 0);
+    if (split > 1) cg::this_cluster().sync();   // every CTA of the cluster runs before remote stores
     // adjoints of the state after the current step
     float lv = 0.f, lgE = 0.f, lhE = 0.f, lgI = 0.f, lhI = 0.f;
     float dEdE = 0.f, dErE = 0.f, ddodE = 0.f, dEdI = 0.f, dErI = 0.f, ddodI = 0.f;
@@ -333,13 +382,12 @@ __global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A, int stage
                 o[5 * bs] = (float)((refr ? 1 : 0) | (spk ? 2 : 0));
             }
             const unsigned bal = __ballot_sync(0xffffffffu, on && spk);
-            __syncthreads();
-            if (lane == 0) ball[warp] = bal;
-            __syncthreads();
+            if (lane == 0) share_word(&ball[t & 1][warp], bal, split);
+            block_sync(split);
             if (t + 2 < t1) xs_issue(xs, Xb + (size_t)(t + 2) * P.nLGN, t + 2, (int)P.nLGN);
             const uint8_t *x = xs_get(xs, Xb + (size_t)t * P.nLGN, t);
             if (on) {
-                const unsigned mask = adj_inputs(A, x, n, local, hE1, hI1, ball);
+                const unsigned mask = adj_inputs(A, x, n, local, hE1, hI1, ball[t & 1]);
                 o[6 * bs] = __uint_as_float(mask);
                 s.v = vnext;
                 s.gE = gE1; s.hE = hE1; s.gI = gI1; s.hI = hI1;
@@ -349,17 +397,18 @@ __global__ void __launch_bounds__(1024) adj_backward_kernel(AdjArgs A, int stage
         for (int t = t1 - 1; t >= t0; t--) {
             // recurrent term: dS[p] = sum_n C[p][n] * lambda_hI(t+1)[n] for the I neurons p
             if (P.recGrad) {
-                __syncthreads();
-                lam[local] = on ? lhI : 0.f;
-                __syncthreads();
+                block_sync(split);   // the readers of lam[] and dS[] of the previous step are done
+                share_float(&lam[local], on ? lhI : 0.f, split);
+                block_sync(split);
                 for (int p = warp; p < A.nI; p += nWarp) {
                     const float *row = C + (size_t)p * bs;
                     float acc = 0.f;
                     for (int j = lane; j < bs; j += 32) acc += __ldg(row + j) * lam[j];
                     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-                    if (lane == 0) dS[p] = acc;
+                    // into the CTA that holds I neuron p
+                    if (lane == 0) store_at_rank(&dS[p], acc, ((int)P.nE + p) / ctaN, split);
                 }
-                __syncthreads();
+                block_sync(split);
             }
             if (!on) continue;
             const float *o = scr + (size_t)(t - t0) * kScrWords * bs + local;
@@ -453,7 +502,36 @@ int adj_check(const pv1_adj_problem *p, const pv1_adj_buffers *b, AdjArgs *A, bo
     A->nI = (int)(p->blockSize - p->nE);
     A->nWin = (int)(p->T / p->win);
     A->nSeg = (int)((p->T + p->seg - 1) / p->seg);
+    int split = (int)p->ctaSplit;
+    if (split == 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        split = (p->blockSize % 64 == 0 && (long long)p->B * p->nblock * 2 <= sms) ? 2 : 1;
+    }
+    if (split != 1 && (split != 2 || p->blockSize % 64)) {
+        g_adjErr = "ctaSplit must be 0, 1 or 2 (2 needs blockSize a multiple of 64)";
+        return PV1_E_ARG;
+    }
+    A->split = split;
     return PV1_OK;
+}
+
+template <class Kern>
+cudaError_t adj_launch(Kern kern, const AdjArgs &A, int stage, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(A.p.nblock * A.split, A.p.B);
+    cfg.blockDim = dim3(A.p.blockSize / A.split);
+    cfg.dynamicSmemBytes = stage ? 3 * A.p.nLGN : 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = A.split;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = A.split > 1 ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, A, stage);
 }
 
 // Count rows go through the bulk-copy stage when their size and offsets are multiples of 16
@@ -481,9 +559,8 @@ int pv1_adj_forward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *st
     int r = adj_check(p, b, &A, false);
     if (r) return r;
     const int stage = adj_stage(p);
-    adj_forward_kernel<<<dim3(p->nblock, p->B), p->blockSize, stage ? 3 * p->nLGN : 0, (cudaStream_t)stream>>>(
-        A, stage);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = A.p.blockSize / A.split <= 512 ? adj_launch(adj_forward_kernel<512>, A, stage, (cudaStream_t)stream)
+                                                   : adj_launch(adj_forward_kernel<1024>, A, stage, (cudaStream_t)stream);
     if (e != cudaSuccess) {
         g_adjErr = cudaGetErrorString(e);
         return PV1_E_CUDA;
@@ -496,9 +573,9 @@ int pv1_adj_backward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *s
     int r = adj_check(p, b, &A, true);
     if (r) return r;
     const int stage = adj_stage(p);
-    adj_backward_kernel<<<dim3(p->nblock, p->B), p->blockSize, stage ? 3 * p->nLGN : 0, (cudaStream_t)stream>>>(
-        A, stage);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = A.p.blockSize / A.split <= 512
+                        ? adj_launch(adj_backward_kernel<512>, A, stage, (cudaStream_t)stream)
+                        : adj_launch(adj_backward_kernel<1024>, A, stage, (cudaStream_t)stream);
     if (e != cudaSuccess) {
         g_adjErr = cudaGetErrorString(e);
         return PV1_E_CUDA;

@@ -43,6 +43,8 @@ struct AdjArgs {
     pv1_adj_buffers b;
     int N, nI, nWin, nSeg;
     int split;   // CTAs per (trial, block)
+    int xBytes;  // dynamic shared memory of the LGN count stage (16-byte multiple)
+    int synSmem; // 1: the synapse ids and weights are copied to dynamic shared memory after it
 };
 
 // Block-wide exchange between the CTAs of a (trial, block): stores go to every CTA of the
@@ -122,8 +124,16 @@ __device__ __forceinline__ float adj_neuron_step(const pv1_adj_problem &P, AStat
 // into hI (ascending).  ball[] holds this step's spike ballots of the CTA's warps; x is the
 // step's row of LGN counts (shared-memory stage or global).  Returns the mask of the synapses
 // that carried an event.
+// The neuron's LGN synapse ids and weights: synapse k at ids[k * stride], W[k * stride] (the
+// global [K][N] arrays with stride N, or the CTA's shared-memory copy with stride blockDim.x).
+struct SynView {
+    const int32_t *ids;
+    const float *W;
+    int stride;
+};
+
 __device__ __forceinline__ unsigned adj_inputs(const AdjArgs &A, const uint8_t *x, int n, int local,
-                                               float &hE, float &hI, const unsigned *ball) {
+                                               float &hE, float &hI, const unsigned *ball, SynView sv) {
     const pv1_adj_problem &P = A.p;
     unsigned mask = 0u;
     // LGN synapses in chunks of 8: the id and count loads of a chunk are in flight together;
@@ -132,14 +142,14 @@ __device__ __forceinline__ unsigned adj_inputs(const AdjArgs &A, const uint8_t *
         int id[8];
         unsigned c[8];
 #pragma unroll
-        for (int j = 0; j < 8; j++) id[j] = k0 + j < (int)P.K ? __ldg(A.b.ids + (size_t)(k0 + j) * A.N + n) : 0;
+        for (int j = 0; j < 8; j++) id[j] = k0 + j < (int)P.K ? sv.ids[(k0 + j) * sv.stride] : 0;
 #pragma unroll
         // x may be the shared-memory stage: a generic load, not the global-only __ldg
         for (int j = 0; j < 8; j++) c[j] = k0 + j < (int)P.K ? x[id[j]] : 0u;
 #pragma unroll
         for (int j = 0; j < 8; j++)
             if (c[j]) {
-                hE = hE + __ldg(A.b.W + (size_t)(k0 + j) * A.N + n) * (float)c[j];
+                hE = hE + sv.W[(k0 + j) * sv.stride] * (float)c[j];
                 mask |= 1u << (k0 + j);
             }
     }
@@ -173,6 +183,19 @@ __device__ __forceinline__ unsigned adj_inputs(const AdjArgs &A, const uint8_t *
         if (pre[7] < 0) break;
     }
     return mask;
+}
+
+// Copies the neuron's synapse ids and weights into the CTA's shared memory (column per
+// thread) when the caller gave room for them, else views the global arrays.
+__device__ __forceinline__ SynView stage_synapses(const AdjArgs &A, uint8_t *room, int n, bool on) {
+    if (!room) return SynView{A.b.ids + n, A.b.W + n, A.N};
+    int32_t *sIds = reinterpret_cast<int32_t *>(room);
+    float *sW = reinterpret_cast<float *>(room + (size_t)A.p.K * blockDim.x * sizeof(int32_t));
+    for (int k = 0; k < (int)A.p.K; k++) {
+        sIds[k * blockDim.x + threadIdx.x] = on ? __ldg(A.b.ids + (size_t)k * A.N + n) : 0;
+        sW[k * blockDim.x + threadIdx.x] = on ? __ldg(A.b.W + (size_t)k * A.N + n) : 0.f;
+    }
+    return SynView{sIds + threadIdx.x, sW + threadIdx.x, (int)blockDim.x};
 }
 
 // ---- LGN count rows staged into shared memory by the bulk-copy (TMA) engine ----
@@ -278,6 +301,7 @@ __global__ void __launch_bounds__(MaxThreads) adj_forward_kernel(AdjArgs A, int 
     const uint8_t *Xb = A.b.X + (size_t)b * P.T * P.nLGN;
     XStage xs;
     xs_init(xs, xbuf, xbar, (int)P.nLGN, stage != 0);
+    const SynView sv = stage_synapses(A, A.synSmem ? xbuf + A.xBytes : nullptr, n, on);
     if (split > 1) cg::this_cluster().sync();   // every CTA of the cluster runs before remote stores
     xs_issue(xs, Xb, 0, (int)P.nLGN);
     if (P.T > 1) xs_issue(xs, Xb + P.nLGN, 1, (int)P.nLGN);
@@ -298,7 +322,7 @@ __global__ void __launch_bounds__(MaxThreads) adj_forward_kernel(AdjArgs A, int 
         if (t + 2 < (int)P.T) xs_issue(xs, Xb + (size_t)(t + 2) * P.nLGN, t + 2, (int)P.nLGN);
         const uint8_t *x = xs_get(xs, Xb + (size_t)t * P.nLGN, t);
         if (on) {
-            adj_inputs(A, x, n, local, hE1, hI1, ball[t & 1]);
+            adj_inputs(A, x, n, local, hE1, hI1, ball[t & 1], sv);
             s.v = vnext;
             s.gE = gE1; s.hE = hE1; s.gI = gI1; s.hI = hI1;
             cnt += spk ? 1.f : 0.f;
@@ -356,6 +380,7 @@ __global__ void __launch_bounds__(MaxThreads) adj_backward_kernel(AdjArgs A, int
     const uint8_t *Xb = A.b.X + (size_t)b * P.T * P.nLGN;
     XStage xs;
     xs_init(xs, xbuf, xbar, (int)P.nLGN, stage != 0);
+    const SynView sv = stage_synapses(A, A.synSmem ? xbuf + A.xBytes : nullptr, n, on);
     if (split > 1) cg::this_cluster().sync();   // every CTA of the cluster runs before remote stores
     // adjoints of the state after the current step
     float lv = 0.f, lgE = 0.f, lhE = 0.f, lgI = 0.f, lhI = 0.f;
@@ -387,7 +412,7 @@ __global__ void __launch_bounds__(MaxThreads) adj_backward_kernel(AdjArgs A, int
             if (t + 2 < t1) xs_issue(xs, Xb + (size_t)(t + 2) * P.nLGN, t + 2, (int)P.nLGN);
             const uint8_t *x = xs_get(xs, Xb + (size_t)t * P.nLGN, t);
             if (on) {
-                const unsigned mask = adj_inputs(A, x, n, local, hE1, hI1, ball[t & 1]);
+                const unsigned mask = adj_inputs(A, x, n, local, hE1, hI1, ball[t & 1], sv);
                 o[6 * bs] = __uint_as_float(mask);
                 s.v = vnext;
                 s.gE = gE1; s.hE = hE1; s.gI = gI1; s.hI = hI1;
@@ -424,7 +449,7 @@ __global__ void __launch_bounds__(MaxThreads) adj_backward_kernel(AdjArgs A, int
             while (mask) {
                 const int k = __ffs(mask) - 1;
                 mask &= mask - 1;
-                const int id = __ldg(A.b.ids + (size_t)k * A.N + n);
+                const int id = sv.ids[k * sv.stride];
                 const float c = (float)__ldg(Xb + (size_t)t * P.nLGN + id);
                 atomicAdd(A.b.gW + (size_t)k * A.N + n, lhE * c);
             }
@@ -517,12 +542,26 @@ int adj_check(const pv1_adj_problem *p, const pv1_adj_buffers *b, AdjArgs *A, bo
     return PV1_OK;
 }
 
+// Dynamic shared memory: the LGN count stage (3 rows) and, when it fits, the CTA's synapse
+// ids and weights (K x threads each).
+void adj_smem_plan(AdjArgs &A, int stage) {
+    const int threads = (int)(A.p.blockSize / A.split);
+    A.xBytes = stage ? (int)((3 * A.p.nLGN + 15) / 16 * 16) : 0;
+    const size_t syn = (size_t)A.p.K * threads * 8;
+    A.synSmem = A.xBytes + syn <= 160 * 1024 ? 1 : 0;
+}
+
 template <class Kern>
 cudaError_t adj_launch(Kern kern, const AdjArgs &A, int stage, cudaStream_t st) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(A.p.nblock * A.split, A.p.B);
     cfg.blockDim = dim3(A.p.blockSize / A.split);
-    cfg.dynamicSmemBytes = stage ? 3 * A.p.nLGN : 0;
+    cfg.dynamicSmemBytes = (size_t)A.xBytes + (A.synSmem ? (size_t)A.p.K * cfg.blockDim.x * 8 : 0);
+    if (cfg.dynamicSmemBytes > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)cfg.dynamicSmemBytes);
+        if (e != cudaSuccess) return e;
+    }
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -559,6 +598,7 @@ int pv1_adj_forward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *st
     int r = adj_check(p, b, &A, false);
     if (r) return r;
     const int stage = adj_stage(p);
+    adj_smem_plan(A, stage);
     cudaError_t e = A.p.blockSize / A.split <= 512 ? adj_launch(adj_forward_kernel<512>, A, stage, (cudaStream_t)stream)
                                                    : adj_launch(adj_forward_kernel<1024>, A, stage, (cudaStream_t)stream);
     if (e != cudaSuccess) {
@@ -573,6 +613,7 @@ int pv1_adj_backward(const pv1_adj_problem *p, const pv1_adj_buffers *b, void *s
     int r = adj_check(p, b, &A, true);
     if (r) return r;
     const int stage = adj_stage(p);
+    adj_smem_plan(A, stage);
     cudaError_t e = A.p.blockSize / A.split <= 512
                         ? adj_launch(adj_backward_kernel<512>, A, stage, (cudaStream_t)stream)
                         : adj_launch(adj_backward_kernel<1024>, A, stage, (cudaStream_t)stream);

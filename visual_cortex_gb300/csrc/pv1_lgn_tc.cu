@@ -9,11 +9,12 @@
 // MMA's M); time advances in tiles of 128 steps (N); the frames a tile's steps read lie in a
 // 64-frame window (K).  Per tile: TMA loads the S window (128 cells x 64 frames, bf16, 128B
 // swizzle) and the tile's W (128 steps x 64 frames), one thread issues four
-// tcgen05.mma.kind::f16 (K = 16 each) into an FP32 accumulator in tensor memory, and the four
-// warps read their 32 lanes (cells) back with tcgen05.ld, 32 steps at a time, and run the
-// logistic rate and the exact-time Poisson generator of LGN_nonlinear / get_spike
-// (src/discrete_input_convol.cu:1587-1730) step by step, carrying each cell's generator state
-// across tiles.  Every wait on an mbarrier is bounded; a timeout sets the error word and the
+// tcgen05.mma.kind::f16 (K = 16 each) into an FP32 accumulator in tensor memory; two
+// warpgroups read the lanes (cells) back with tcgen05.ld, 32 steps at a time, and evaluate the
+// logistic rate of LGN_nonlinear (src/discrete_input_convol.cu:1637-1730) for half the steps
+// each; the first group then runs the exact-time Poisson generator of get_spike (:1587-1635)
+// step by step, carrying each cell's generator state across tiles, while the next tile is
+// loaded and multiplied.  Every wait on an mbarrier is bounded; a timeout sets the error word and the
 // CTA stops issuing work, frees its tensor memory and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -174,8 +175,16 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, float *v) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-__global__ void __launch_bounds__(128, 1) lgn_tc_kernel(TcArgs A, const __grid_constant__ CUtensorMap mapS,
-                                                        const __grid_constant__ CUtensorMap mapW) {
+// Two warpgroups.  Per tile: the MMA result is read back by both (warp w reads the lanes of
+// quadrant w % 4; the first group columns 0-63, the second 64-127), each thread turning its 64
+// sums into rates (the independent part) stored to shared memory R [step][cell]; then the first
+// group runs the generator of its cell through the 128 steps from R while one thread of the
+// second group already loads and multiplies the next tile into the (now free) tensor memory.
+constexpr int kTcThreads = 256;
+constexpr unsigned kTcSmem = 1024 + 2 * kTileBytes + kTcN * kTcM * 4;   // alignment, tiles, R
+
+__global__ void __launch_bounds__(kTcThreads, 1) lgn_tc_kernel(TcArgs A, const __grid_constant__ CUtensorMap mapS,
+                                                               const __grid_constant__ CUtensorMap mapW) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t barFull, barMma;
     __shared__ unsigned tmemSlot;
@@ -183,8 +192,12 @@ __global__ void __launch_bounds__(128, 1) lgn_tc_kernel(TcArgs A, const __grid_c
     uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *tileS = base;
     uint8_t *tileW = base + kTileBytes;
+    float *R = reinterpret_cast<float *>(base + 2 * kTileBytes);   // [kTcN][kTcM]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int quad = warp & 3, half = warp >> 2;
     const int cell0 = blockIdx.x * kTcM;
+    const int cl = quad * 32 + lane;   // this thread's lane of the accumulator = its cell
+    const int issuer = 4 * 32;         // first thread of the second group issues the copies and MMAs
     if (threadIdx.x == 0) {
         mbar_init(&barFull, 1);
         mbar_init(&barMma, 1);
@@ -200,55 +213,80 @@ __global__ void __launch_bounds__(128, 1) lgn_tc_kernel(TcArgs A, const __grid_c
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned tmem = tmemSlot;
-    // this thread's cell and its carried state
-    const int cell = cell0 + threadIdx.x;
+    const int cell = cell0 + cl;
     const bool on = cell < A.nCells;
     float absk = 0.f, mx = 1.f, C50 = 0.f, Kc = 0.f, LA = 0.f, LB = 0.f, ltr = 0.f, lnl = 0.f;
     curandStateMRG32k3a st;
     if (on) {
         absk = A.absk[cell]; mx = A.maxConvol[cell]; C50 = A.c50[cell]; Kc = A.sharp[cell];
-        LA = A.la[cell]; LB = A.lb[cell]; ltr = A.ltr[cell]; lnl = A.lnl[cell]; st = A.state[cell];
+        LA = A.la[cell]; LB = A.lb[cell];
+        if (half == 0) {
+            ltr = A.ltr[cell];
+            lnl = A.lnl[cell];
+            st = A.state[cell];
+        }
     }
     const float rmx = 1.0f / mx;
-    for (int i = 0; i < A.nTiles; i++) {
+    const float scale = A.dt * 1e-3f;   // rate in spikes/ms times dt
+    // tile i: TMA of its S window and W, four MMAs into tensor memory, bounded waits
+    auto load_and_multiply = [&](int i) {
         const unsigned parity = (unsigned)(i & 1);
-        if (threadIdx.x == 0) {
-            mbar_expect_tx(&barFull, 2 * kTileBytes);
-            tma_load_2d(tileS, &mapS, A.f0[i], cell0, &barFull);
-            tma_load_2d(tileW, &mapW, 0, i * kTcN, &barFull);
-            if (!mbar_wait(&barFull, parity)) {
-                atomicOr(A.err, kErrBarrier);
-                abortFlag = 1;
-                mbar_wait(&barFull, parity);   // once more, bounded: let the copies in flight land
-            } else {
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint64_t da = umma_desc_sw128(smem_u32(tileS));
-                const uint64_t db = umma_desc_sw128(smem_u32(tileW));
+        mbar_expect_tx(&barFull, 2 * kTileBytes);
+        tma_load_2d(tileS, &mapS, A.f0[i], cell0, &barFull);
+        tma_load_2d(tileW, &mapW, 0, i * kTcN, &barFull);
+        if (!mbar_wait(&barFull, parity)) {
+            atomicOr(A.err, kErrBarrier);
+            abortFlag = 1;
+            mbar_wait(&barFull, parity);   // once more, bounded: let the copies in flight land
+            return;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint64_t da = umma_desc_sw128(smem_u32(tileS));
+        const uint64_t db = umma_desc_sw128(smem_u32(tileW));
 #pragma unroll
-                for (int k = 0; k < kTcK / 16; k++)   // K = 16 per MMA: +32 bytes inside the swizzle atom
-                    umma_bf16(tmem, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k), k > 0);
-                umma_commit(&barMma);
-                if (!mbar_wait(&barMma, parity)) {
-                    atomicOr(A.err, kErrBarrier);
-                    abortFlag = 1;
-                    mbar_wait(&barMma, parity);    // once more, bounded, before the memory is freed
+        for (int k = 0; k < kTcK / 16; k++)   // K = 16 per MMA: +32 bytes inside the swizzle atom
+            umma_bf16(tmem, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k), k > 0);
+        umma_commit(&barMma);
+        if (!mbar_wait(&barMma, parity)) {
+            atomicOr(A.err, kErrBarrier);
+            abortFlag = 1;
+            mbar_wait(&barMma, parity);    // once more, bounded, before the memory is freed
+        }
+    };
+    if (threadIdx.x == issuer && A.nTiles > 0) load_and_multiply(0);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    for (int i = 0; i < A.nTiles; i++) {
+        if (abortFlag) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // rates of this thread's cell at its group's 64 steps of the tile
+        for (int c0 = half * (kTcN / 2); c0 < (half + 1) * (kTcN / 2); c0 += 32) {
+            float v[32];
+            tmem_ld32(tmem + ((unsigned)(quad * 32) << 16) + (unsigned)c0, v);
+            if (on) {
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const float fr = lgn_rate(A, v[j], absk, mx, rmx, C50, Kc, LA, LB);
+                    const int t = i * kTcN + c0 + j;
+                    if (A.fr && t < A.T && t % A.frEvery == 0) A.fr[(size_t)(t / A.frEvery) * A.nCells + cell] = fr;
+                    R[(c0 + j) * kTcM + cl] = fr * scale;
                 }
             }
         }
-        __syncthreads();
-        if (abortFlag) break;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // epilogue: this warp's 32 lanes = 32 cells, 32 steps per tensor-memory load
-        for (int c0 = 0; c0 < kTcN; c0 += 32) {
-            float v[32];
-            tmem_ld32(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0, v);
-            if (on) lgn_epilogue32(A, cell, i * kTcN + c0, v, absk, mx, rmx, C50, Kc, LA, LB, ltr, lnl, st);
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();   // R holds the tile; tensor memory and both tiles are free
+        if (threadIdx.x == issuer && i + 1 < A.nTiles) load_and_multiply(i + 1);
+        if (half == 0 && on) {
+            for (int c = 0; c < kTcN; c++) {
+                const int t = i * kTcN + c;
+                if (t < A.T) A.sInfo[(size_t)t * A.nCells + cell] = lgn_poisson(R[c * kTcM + cl], ltr, lnl, st);
+            }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();   // tensor memory and both tiles are free for the next tile
+        __syncthreads();   // R is read; the next tile is in tensor memory
     }
     (void)lane;
-    if (on) {
+    if (on && half == 0) {
         A.ltr[cell] = ltr;
         A.lnl[cell] = lnl;
         A.state[cell] = st;
@@ -506,9 +544,9 @@ int pv1_lgn_tc_run(pv1_lgn_tc *p, int tensorCores, uint64_t seed, float *ms) {
     if (tensorCores) {
         // 60 KB per CTA keeps at most 3 CTAs on an SM: 3 x 128 tensor-memory columns <= 512,
         // so no CTA ever waits in tcgen05.alloc
-        const int smem = 60 * 1024;
+        const int smem = (int)kTcSmem;
         PV1_TCUDA(p, cudaFuncSetAttribute(lgn_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        lgn_tc_kernel<<<grid, 128, smem, p->stream>>>(a, p->mapS, p->mapW);
+        lgn_tc_kernel<<<grid, kTcThreads, smem, p->stream>>>(a, p->mapS, p->mapW);
     } else {
         lgn_f32_kernel<<<grid, 128, 0, p->stream>>>(a);
     }

@@ -117,3 +117,38 @@ def test_batch_uneven_sizes_persistent(native):
     finally:
         for s in alone + batched:
             s.close()
+
+
+def test_batch_parvo_and_multi_spike_trials(native):
+    """Trials whose LGN has parvo cells (per-trial LGN launches instead of the batched class
+    kernel) and trials in the multi-spike regime (dt > min tRef) batch like any other."""
+    from visual_cortex_gb300.batch import Batch
+    from visual_cortex_gb300 import synth
+    parvo = synth.make_workload("parvo", seed=9, nblock=1, n_lgn=256, m=20, width=64, height=64, nt=0,
+                                nFrame=40, n_parvo=64, tau=300.0, nKernelSample=150)
+    multi = synth.make_workload("multi", seed=11, nblock=1, n_lgn=256, m=20, width=64, height=64, nt=0,
+                                nFrame=40)
+    multi.spec.tRef = [0.1, 0.05]
+    trials = [synth.Trial(wl=parvo, steps=120, orient=0.0, contrast=0.5),
+              synth.Trial(wl=multi, steps=100, orient=0.0, contrast=0.5),
+              synth.Trial(wl=parvo, steps=90, orient=0.0, contrast=0.5)]
+    alone, batched = [], []
+    try:
+        for tr in trials:
+            s = _sim(tr.wl)
+            s.persistent(0)
+            s.run(tr.steps)
+            alone.append(s)
+        batched = [_sim(tr.wl) for tr in trials]
+        b = Batch(batched, [tr.steps for tr in trials], autotune=True)
+        try:
+            assert b.run()[0] == 0
+            for q in range(len(trials)):
+                for k in STATE:
+                    np.testing.assert_array_equal(batched[q].state(k), alone[q].state(k),
+                                                  err_msg=f"trial {q} {k}")
+        finally:
+            b.close()
+    finally:
+        for s in alone + batched:
+            s.close()

@@ -357,3 +357,20 @@ def test_stimulus_reload_same_size(c1_small):
         a.close()
         b.close()
         c.close()
+
+
+def test_parvo_persistent_equals_per_step(parvo_wl):
+    from visual_cortex_gb300.model import Simulation
+    wl = parvo_wl
+    a = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    b = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        assert a.persistent(1)
+        assert not b.persistent(0)
+        a.run(300)
+        b.run(300)
+        for k in ("v", "w", "gE", "hE", "gI", "hI", "gFF", "tBack", "lgn_lnl"):
+            np.testing.assert_array_equal(a.state(k), b.state(k), err_msg=k)
+    finally:
+        a.close()
+        b.close()

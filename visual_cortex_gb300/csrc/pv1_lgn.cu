@@ -426,10 +426,22 @@ __global__ void __launch_bounds__(256) lgn_parvo_spatial_kernel(
     const float *xC = SC + (size_t)cell * 2 * nSample, *yC = xC + yOff;
     const float *xS = xC + nSample, *yS = xS + yOff;
     const int typeC = coneType[cell], typeS = coneType[nParvo + cell];
+    // the surround's intensities at its own coordinates serve its mean and its contrast: kept
+    // in registers between the two passes when the sample grid is small enough
+    const bool keep = nSample <= 32 * kSpatialReg;
+    float IS[kSpatialReg];
     float sumC = 0.f, sumS = 0.f;
-    for (int s = lane; s < nSample; s += 32) {
+#pragma unroll
+    for (int k = 0; k < kSpatialReg; k++) IS[k] = 0.f;
+    for (int s = lane, k = 0; s < nSample; s += 32, k++) {
         sumC += intensity(typeC, xS[s], yS[s], li, texL, texM, texS);
-        sumS += intensity(typeS, xS[s], yS[s], li, texL, texM, texS);
+        const float I = intensity(typeS, xS[s], yS[s], li, texL, texM, texS);
+        sumS += I;
+        if (keep) {
+#pragma unroll
+            for (int q = 0; q < kSpatialReg; q++)
+                if (q == k) IS[q] = I;
+        }
     }
     for (int o = 16; o > 0; o >>= 1) {
         sumC += __shfl_xor_sync(0xffffffffu, sumC, o);
@@ -437,13 +449,20 @@ __global__ void __launch_bounds__(256) lgn_parvo_spatial_kernel(
     }
     const float meanC = sumC / nSample, meanS = sumS / nSample;
     float accC = 0.f, accS = 0.f;
-    for (int s = lane; s < nSample; s += 32) {
+    for (int s = lane, k = 0; s < nSample; s += 32, k++) {
         const float sw = SW[s];
         float I = intensity(typeC, xC[s], yC[s], li, texL, texM, texS);
         float c = meanC > 0 ? I / meanC - 1.0f : I;
         if (fabsf(c) > 1.0f) c = copysignf(1.0f, c);
         accC += sw * c;
-        I = intensity(typeS, xS[s], yS[s], li, texL, texM, texS);
+        if (keep) {
+            I = 0.f;
+#pragma unroll
+            for (int q = 0; q < kSpatialReg; q++)
+                if (q == k) I = IS[q];
+        } else {
+            I = intensity(typeS, xS[s], yS[s], li, texL, texM, texS);
+        }
         c = meanS > 0 ? I / meanS - 1.0f : I;
         if (fabsf(c) > 1.0f) c = copysignf(1.0f, c);
         accS += sw * c;

@@ -56,6 +56,10 @@ struct pv1_plan {
     int lgnSlots = 0;
     int K = 64;  // steps per LGN launch / per persistent V1 launch / per graph
     bool persistent = false;     // V1 steps run as one cooperative launch per chunk
+    // the LGN of chunk c+1 runs on its own stream while the persistent V1 kernel runs chunk c
+    cudaStream_t lgnStream = nullptr;
+    cudaEvent_t evLgn = nullptr, evFree = nullptr;
+    long long *d_lgnStep = nullptr;
     bool allowPersistent = true;
     unsigned *d_barrier = nullptr;
     bool modeChosen = false;
@@ -384,8 +388,12 @@ static void release_stimulus_textures(pv1_plan *p);
 void pv1_plan_destroy(pv1_plan *p) {
     if (!p) return;
     cudaStreamSynchronize(p->stream);
+    if (p->lgnStream) cudaStreamSynchronize(p->lgnStream);
     drop_graph(p);
     release_stimulus_textures(p);
+    if (p->evLgn) cudaEventDestroy(p->evLgn);
+    if (p->evFree) cudaEventDestroy(p->evFree);
+    if (p->lgnStream) cudaStreamDestroy(p->lgnStream);
     for (void *ptr : p->allocs) cudaFree(ptr);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
@@ -580,7 +588,7 @@ int lgn_setup_impl(pv1_plan *p, const pv1_lgn_config *lc, const pv1_lgn_parvo_co
     L.lastNegLogRand = d_lnl;
     L.state = d_state;
     // LGN spike ring (rows = step % lgnSlots)
-    p->lgnSlots = std::max(p->K, 2);
+    p->lgnSlots = std::max(2 * p->K, 2);   // two chunks: the one V1 reads, the one the LGN writes
     r = dev_alloc(p, &p->d_lgnRing, (size_t)p->lgnSlots * nLGN);
     if (r) return r;
     L.outSInfo = p->d_lgnRing;
@@ -1177,7 +1185,7 @@ int pv1_set_record(pv1_plan *p, int flags, uint32_t slots) {
         if (r) return r;
     }
     // the LGN ring doubles as the LGN_sp record when it is at least `slots` rows long
-    int want = std::max(p->K, 2);
+    int want = std::max(2 * p->K, 2);
     if (flags & (PV1_REC_LGN_SP | PV1_REC_LGN_FR)) want = std::max<int>(want, (int)slots);
     if (want != p->lgnSlots) {
         free_one(p, p->d_lgnRing);
@@ -1248,7 +1256,43 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
         done += k;
     }
     if (nsteps - done >= (uint32_t)K) {
-        if (p->persistent) {
+        if (p->persistent && p->lgnSlots >= 2 * K) {
+            // one cooperative V1 launch per chunk on the plan's stream; the LGN of the next chunk
+            // of this run (never beyond it) on the LGN stream meanwhile, into the other half of
+            // the ring, after the V1 launch that read that half has finished
+            if (!p->lgnStream) {
+                PV1_CUDA(p, cudaStreamCreateWithFlags(&p->lgnStream, cudaStreamNonBlocking));
+                PV1_CUDA(p, cudaEventCreateWithFlags(&p->evLgn, cudaEventDisableTiming));
+                PV1_CUDA(p, cudaEventCreateWithFlags(&p->evFree, cudaEventDisableTiming));
+                r = dev_alloc(p, &p->d_lgnStep, 1);
+                if (r) return r;
+            }
+            const int nFull = (int)((nsteps - done) / (uint32_t)K);
+            const long long t0 = p->step + (long long)done;
+            PV1_CUDA(p, cudaMemcpyAsync(p->d_lgnStep, &t0, sizeof(long long), cudaMemcpyHostToDevice, p->stream));
+            cudaError_t e = launch_lgn_step(p->lp, p->d_lgnStep, K, p->stream);
+            if (e == cudaSuccess) e = launch_advance_step(p->d_lgnStep, K, p->stream);
+            if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("lgn_step: ") + cudaGetErrorString(e));
+            p->launches += lgn_step_launches(p->lp, K) + 1;
+            for (int c = 0; c < nFull; c++) {
+                if (c > 0) PV1_CUDA(p, cudaStreamWaitEvent(p->stream, p->evLgn, 0));
+                PV1_CUDA(p, cudaEventRecord(p->evFree, p->stream));   // chunk c-1's V1 is done
+                e = launch_v1_persistent(p->vp, p->d_stepBase, K, p->d_lgnRing, p->lgnSlots, 1, p->d_barrier,
+                                         p->stream);
+                if (e == cudaSuccess) e = launch_advance_step(p->d_stepBase, K, p->stream);
+                if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("v1_persistent: ") + cudaGetErrorString(e));
+                p->launches += 2;
+                if (c + 1 < nFull) {
+                    PV1_CUDA(p, cudaStreamWaitEvent(p->lgnStream, p->evFree, 0));
+                    e = launch_lgn_step(p->lp, p->d_lgnStep, K, p->lgnStream);
+                    if (e == cudaSuccess) e = launch_advance_step(p->d_lgnStep, K, p->lgnStream);
+                    if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("lgn_step: ") + cudaGetErrorString(e));
+                    PV1_CUDA(p, cudaEventRecord(p->evLgn, p->lgnStream));
+                    p->launches += lgn_step_launches(p->lp, K) + 1;
+                }
+                done += K;
+            }
+        } else if (p->persistent) {
             // a cooperative launch per chunk: issued directly (4 launches per K steps)
             while (nsteps - done >= (uint32_t)K) {
                 r = issue_chunk(p, K, 1, &p->launches);

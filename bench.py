@@ -189,9 +189,7 @@ def run_gb300(args):
     for q in range(max(1, args.steps)):
         t0 = time.perf_counter()
         sim.load_stimulus(stim)
-        step0 = sim.step
-        sim.run(S, sync=False)
-        sp = sim.fetch_spikes(step0, S, out=raster)
+        sp = sim.run_spikes_to_host(S, raster)
         e2e_times.append(time.perf_counter() - t0)
         spikes += int((sp >= 1).sum())
     e2e_s = float(np.sum(e2e_times))

@@ -282,6 +282,13 @@ int pv1_fetch_draws(pv1_plan *plan, int kind, float *draws, int32_t *counts);
 /* Spike words of steps [step0, step0+n) into out [n][nV1] (PV1_REC_SPIKES ring). */
 int pv1_fetch_spikes(pv1_plan *plan, uint64_t step0, uint32_t n, float *out);
 
+/* pv1_run(plan, nsteps, 1) that also writes the spike words of those steps into out
+ * [nsteps][nV1]: each chunk's rows are copied on a copy stream while the next chunks run (the
+ * reference overlaps its device-to-host copies of V1 data with the LGN convolution,
+ * src/patch.cu:6120-6160).  out should be page-locked (pv1_host_alloc) for the copies to
+ * overlap; PV1_REC_SPIKES must be on with a ring of at least nsteps + 1 rows. */
+int pv1_run_spikes_to_host(pv1_plan *plan, uint32_t nsteps, float *out);
+
 /* Number of kernel launches issued by the last pv1_run (for launch accounting). */
 int64_t pv1_last_launch_count(const pv1_plan *plan);
 

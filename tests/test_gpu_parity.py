@@ -374,3 +374,30 @@ def test_parvo_persistent_equals_per_step(parvo_wl):
     finally:
         a.close()
         b.close()
+
+
+def test_spikes_streamed_to_host_equal_fetched(c1_small):
+    """pv1_run_spikes_to_host (rows copied chunk by chunk during the run) returns the same spike
+    words as a run followed by pv1_fetch_spikes, and leaves the same state."""
+    from visual_cortex_gb300 import _native as N
+    from visual_cortex_gb300.model import Simulation
+    wl = c1_small
+    a = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    b = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        for s in (a, b):
+            s.set_record(N.REC_SPIKES, 401)
+        out = N.pinned_empty((300, wl.spec.nV1), np.float32)
+        a.run_spikes_to_host(300, out)
+        b.run(300)
+        ref = b.fetch_spikes(0, 300)
+        np.testing.assert_array_equal(out, ref)
+        assert (ref >= 1).sum() > 0
+        out2 = np.empty((100, wl.spec.nV1), np.float32)   # pageable memory works too
+        a.run_spikes_to_host(100, out2)
+        b.run(100)
+        np.testing.assert_array_equal(out2, b.fetch_spikes(300, 100))
+        np.testing.assert_array_equal(a.state("v"), b.state("v"))
+    finally:
+        a.close()
+        b.close()

@@ -95,6 +95,7 @@ def _load() -> C.CDLL:
         "pv1_abi_version": ([], C.c_int),
         "pv1_set_device": ([C.c_int], C.c_int),
         "pv1_host_alloc": ([C.c_uint64, C.POINTER(C.c_void_p)], C.c_int),
+        "pv1_run_spikes_to_host": ([P, C.c_uint32, _FP], C.c_int),
         "pv1_host_free": ([C.c_void_p], None),
         "pv1_plan_create": ([C.POINTER(V1Config), C.POINTER(P)], C.c_int),
         "pv1_plan_destroy": ([P], None),

@@ -237,7 +237,7 @@ cudaError_t launch_lgn_setup(const SetupArgs &a, int blockThreads, cudaStream_t 
 cudaError_t launch_parvo_setup(const ParvoSetupArgs &a, cudaStream_t st);
 cudaError_t launch_parvo_spatial(cudaTextureObject_t L, cudaTextureObject_t M, cudaTextureObject_t S,
                                  const float *SW, const float *SC, const int *coneType, int nParvo,
-                                 int nSample, int nLayer, int row0, float *out, cudaStream_t st);
+                                 int nSample, int layer0, int nLayer, int row0, float *out, cudaStream_t st);
 // Kernel launches one launch_lgn_step of K steps issues.
 int lgn_step_launches(const LgnParams &p, int K);
 cudaError_t launch_lgn_rng_init(curandStateMRG32k3a *state, float *lnl, float *ltr,

@@ -417,11 +417,12 @@ __global__ void __launch_bounds__(256) lgn_spatial_kernel(
 __global__ void __launch_bounds__(256) lgn_parvo_spatial_kernel(
     cudaTextureObject_t texL, cudaTextureObject_t texM, cudaTextureObject_t texS,
     const float *__restrict__ SW, const float *__restrict__ SC, const int *__restrict__ coneType,
-    int nParvo, int nSample, int nLayer, int row0, float *__restrict__ PS) {
+    int nParvo, int nSample, int layer0, int nLayer, int row0, float *__restrict__ PS) {
     const int lane = threadIdx.x & 31;
     const int cell = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int li = blockIdx.y;
     if (cell >= nParvo || li >= nLayer) return;
+    const int layer = layer0 + li;
     const size_t yOff = (size_t)nParvo * 2 * nSample;
     const float *xC = SC + (size_t)cell * 2 * nSample, *yC = xC + yOff;
     const float *xS = xC + nSample, *yS = xS + yOff;
@@ -434,8 +435,8 @@ __global__ void __launch_bounds__(256) lgn_parvo_spatial_kernel(
 #pragma unroll
     for (int k = 0; k < kSpatialReg; k++) IS[k] = 0.f;
     for (int s = lane, k = 0; s < nSample; s += 32, k++) {
-        sumC += intensity(typeC, xS[s], yS[s], li, texL, texM, texS);
-        const float I = intensity(typeS, xS[s], yS[s], li, texL, texM, texS);
+        sumC += intensity(typeC, xS[s], yS[s], layer, texL, texM, texS);
+        const float I = intensity(typeS, xS[s], yS[s], layer, texL, texM, texS);
         sumS += I;
         if (keep) {
 #pragma unroll
@@ -451,7 +452,7 @@ __global__ void __launch_bounds__(256) lgn_parvo_spatial_kernel(
     float accC = 0.f, accS = 0.f;
     for (int s = lane, k = 0; s < nSample; s += 32, k++) {
         const float sw = SW[s];
-        float I = intensity(typeC, xC[s], yC[s], li, texL, texM, texS);
+        float I = intensity(typeC, xC[s], yC[s], layer, texL, texM, texS);
         float c = meanC > 0 ? I / meanC - 1.0f : I;
         if (fabsf(c) > 1.0f) c = copysignf(1.0f, c);
         accC += sw * c;
@@ -461,7 +462,7 @@ __global__ void __launch_bounds__(256) lgn_parvo_spatial_kernel(
             for (int q = 0; q < kSpatialReg; q++)
                 if (q == k) I = IS[q];
         } else {
-            I = intensity(typeS, xS[s], yS[s], li, texL, texM, texS);
+            I = intensity(typeS, xS[s], yS[s], layer, texL, texM, texS);
         }
         c = meanS > 0 ? I / meanS - 1.0f : I;
         if (fabsf(c) > 1.0f) c = copysignf(1.0f, c);
@@ -838,10 +839,11 @@ cudaError_t launch_parvo_setup(const ParvoSetupArgs &a, cudaStream_t st) {
 
 cudaError_t launch_parvo_spatial(cudaTextureObject_t L, cudaTextureObject_t M, cudaTextureObject_t S,
                                  const float *SW, const float *SC, const int *coneType, int nParvo,
-                                 int nSample, int nLayer, int row0, float *out, cudaStream_t st) {
-    if (nParvo <= 0) return cudaSuccess;
+                                 int nSample, int layer0, int nLayer, int row0, float *out, cudaStream_t st) {
+    if (nParvo <= 0 || nLayer <= 0) return cudaSuccess;
     dim3 grid((nParvo + 7) / 8, nLayer);
-    lgn_parvo_spatial_kernel<<<grid, 256, 0, st>>>(L, M, S, SW, SC, coneType, nParvo, nSample, nLayer, row0, out);
+    lgn_parvo_spatial_kernel<<<grid, 256, 0, st>>>(L, M, S, SW, SC, coneType, nParvo, nSample, layer0, nLayer, row0,
+                                                   out);
     return cudaGetLastError();
 }
 

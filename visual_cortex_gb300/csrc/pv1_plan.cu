@@ -50,6 +50,10 @@ struct pv1_plan {
     cudaArray_t stimArr[3] = {nullptr, nullptr, nullptr};
     cudaTextureObject_t stimTex[3] = {0, 0, 0};
     uint32_t stimW = 0, stimH = 0, stimL = 0;
+    // spatial stage of a movie held in one texture batch is computed on demand: frames
+    // [0, framesDone) are in the tables (the initial-luminance row from the load on)
+    bool lazyFrames = false;
+    int framesDone = 0;
     int nFrame = 0;
     // LGN spike ring
     float *d_lgnRing = nullptr, *d_lgnFr = nullptr;
@@ -60,6 +64,11 @@ struct pv1_plan {
     cudaStream_t lgnStream = nullptr;
     cudaEvent_t evLgn = nullptr, evFree = nullptr;
     long long *d_lgnStep = nullptr;
+    // spike rows copied to a host buffer while the run goes on (pv1_run_spikes_to_host)
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t evChunk = nullptr, evCopied = nullptr;
+    float *sinkHost = nullptr;        // row 0 = step sinkStep0
+    long long sinkStep0 = 0;
     bool allowPersistent = true;
     unsigned *d_barrier = nullptr;
     bool modeChosen = false;
@@ -81,6 +90,11 @@ struct pv1_plan {
     // delayed synapses (host copies, kept while the near and far lists are merged)
     std::vector<EvSyn> farSyn, nearSyn;
 };
+
+static void release_stimulus_textures(pv1_plan *p);
+static int ensure_frames(pv1_plan *p, long long lastStep);
+// every frame of the loaded movie in the spatial-stage tables
+static int ensure_all_frames(pv1_plan *p) { return ensure_frames(p, (long long)1 << 40); }
 
 namespace {
 
@@ -145,6 +159,25 @@ void drop_graph(pv1_plan *p) {
         cudaGraphExecDestroy(p->graphExec);
         p->graphExec = nullptr;
     }
+}
+
+// With a spike sink set: copies the spike rows of steps [a, a + n) (already issued on the
+// plan's stream) to the sink on the copy stream, behind an event on the plan's stream.
+int sink_rows(pv1_plan *p, long long a, long long n) {
+    if (!p->sinkHost || n <= 0) return PV1_OK;
+    PV1_CUDA(p, cudaEventRecord(p->evChunk, p->stream));
+    PV1_CUDA(p, cudaStreamWaitEvent(p->copyStream, p->evChunk, 0));
+    const size_t nV1 = p->nV1;
+    long long done = 0;
+    while (done < n) {
+        const long long t = a + done;
+        const long long slot = t % p->recSlots;
+        const long long cnt = std::min<long long>(n - done, p->recSlots - slot);
+        PV1_CUDA(p, cudaMemcpyAsync(p->sinkHost + (size_t)(t - p->sinkStep0) * nV1, p->vp.recSpk + (size_t)slot * nV1,
+                                    (size_t)cnt * nV1 * sizeof(float), cudaMemcpyDeviceToHost, p->copyStream));
+        done += cnt;
+    }
+    return PV1_OK;
 }
 
 // Issues k steps on the plan's stream: the LGN rate+spike pair for the k steps, then either
@@ -212,6 +245,8 @@ namespace pv1 {
 int plan_lgn_view(pv1_plan *p, PlanLgnView *out) {
     if (!p || !out) return PV1_E_ARG;
     if (!p->lgnReady || !p->stimReady) return fail(p, PV1_E_STATE, "LGN/stimulus not loaded");
+    int r = ensure_all_frames(p);
+    if (r) return r;
     out->lp = p->lp;
     out->stream = p->stream;
     out->step = p->step;
@@ -224,6 +259,8 @@ void plan_advance_steps(pv1_plan *p, long long n) { p->step += n; }
 int plan_batch_view(pv1_plan *p, PlanBatchView *out) {
     if (!p || !out) return PV1_E_ARG;
     if (!p->lgnReady || !p->stimReady) return fail(p, PV1_E_STATE, "LGN/stimulus not loaded");
+    int er = ensure_all_frames(p);
+    if (er) return er;
     if (!p->haveLGNsyn || !p->haveNear || !p->haveState || !p->haveRng)
         return fail(p, PV1_E_STATE, "V1 synapses/connectivity/state/rng not set");
     out->vp = p->vp;
@@ -383,17 +420,19 @@ int pv1_plan_create(const pv1_v1_config *cfg, pv1_plan **out) {
     return PV1_OK;
 }
 
-static void release_stimulus_textures(pv1_plan *p);
-
 void pv1_plan_destroy(pv1_plan *p) {
     if (!p) return;
     cudaStreamSynchronize(p->stream);
     if (p->lgnStream) cudaStreamSynchronize(p->lgnStream);
     drop_graph(p);
     release_stimulus_textures(p);
+    if (p->copyStream) cudaStreamSynchronize(p->copyStream);
     if (p->evLgn) cudaEventDestroy(p->evLgn);
     if (p->evFree) cudaEventDestroy(p->evFree);
     if (p->lgnStream) cudaStreamDestroy(p->lgnStream);
+    if (p->evChunk) cudaEventDestroy(p->evChunk);
+    if (p->evCopied) cudaEventDestroy(p->evCopied);
+    if (p->copyStream) cudaStreamDestroy(p->copyStream);
     for (void *ptr : p->allocs) cudaFree(ptr);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
@@ -741,6 +780,8 @@ int pv1_lgn_get_parvo_spatial(pv1_plan *p, float *PS) {
     if (!p || !PS) return PV1_E_ARG;
     if (!p->stimReady) return fail(p, PV1_E_STATE, "no stimulus loaded");
     if (p->nParvo == 0) return fail(p, PV1_E_STATE, "no parvo cells");
+    int r = ensure_all_frames(p);
+    if (r) return r;
     PV1_CUDA(p, cudaStreamSynchronize(p->stream));
     PV1_CUDA(p, cudaMemcpy(PS, p->d_pS, (size_t)(p->nFrame + 1) * 2 * p->nParvo * sizeof(float), cudaMemcpyDeviceToHost));
     return PV1_OK;
@@ -758,6 +799,7 @@ int pv1_lgn_get_tables(pv1_plan *p, float *TW, float *SW, float *SC, float *maxC
     return PV1_OK;
 }
 
+extern "C++" {
 static void release_stimulus_textures(pv1_plan *p) {
     for (int ch = 0; ch < 3; ch++) {
         if (p->stimTex[ch]) cudaDestroyTextureObject(p->stimTex[ch]);
@@ -767,6 +809,29 @@ static void release_stimulus_textures(pv1_plan *p) {
     }
     p->stimW = p->stimH = p->stimL = 0;
 }
+
+// Computes the spatial stage of the movie frames that steps up to `lastStep` read and that
+// are not in the tables yet (frames are computed in order, each once per load).
+static int ensure_frames(pv1_plan *p, long long lastStep) {
+    if (!p->lazyFrames || p->framesDone >= p->nFrame) return PV1_OK;
+    // frames_read_after_step grows with the step; past nFrame frames every frame is needed
+    const long long perFrame = std::max<long long>(1, p->lp.fs.ntPerFrame / std::max(p->lp.fs.denorm, 1));
+    const long long need64 = lastStep < 0 ? 0
+                             : (lastStep >= (long long)(p->nFrame + 1) * (perFrame + 1) ? p->nFrame
+                                                                                        : frames_read_after_step(p->lp.fs, lastStep));
+    const int need = (int)std::min<long long>(need64, p->nFrame);
+    if (need <= p->framesDone) return PV1_OK;
+    const int f0 = p->framesDone, n = need - f0;
+    if (p->nMagno > 0)
+        PV1_CUDA(p, launch_lgn_spatial(p->stimTex[0], p->stimTex[1], p->stimTex[2], p->d_SW, p->d_SC, p->d_coneType,
+                                      p->nMagno, p->mSample, f0, n, f0, p->d_S, p->stream));
+    if (p->nParvo > 0)
+        PV1_CUDA(p, launch_parvo_spatial(p->stimTex[0], p->stimTex[1], p->stimTex[2], p->d_pSW, p->d_pSC, p->d_pCone,
+                                        p->nParvo, p->pSample, f0, n, f0, p->d_pS, p->stream));
+    p->framesDone = need;
+    return PV1_OK;
+}
+}  // extern "C++"
 
 int pv1_stimulus_load(pv1_plan *p, uint32_t nFrame, uint32_t height, uint32_t width,
                       const float init_LMS[3], const float *frames) {
@@ -851,12 +916,16 @@ int pv1_stimulus_load(pv1_plan *p, uint32_t nFrame, uint32_t height, uint32_t wi
             p->stimH = height;
             p->stimL = nl;
         }
+        // a single batch: only the initial-luminance layer now, the movie frames as the steps
+        // that read them are run (ensure_frames); several batches: every layer now
+        const int first = single ? (int)nMovie : 0;
         if (nMagno > 0)
             PV1_CUDA(p, launch_lgn_spatial(tex[0], tex[1], tex[2], p->d_SW, p->d_SC, p->d_coneType, nMagno,
-                                          p->mSample, 0, (int)nl, (int)f0, p->d_S, p->stream));
+                                          p->mSample, first, (int)nl - first, (int)f0 + first, p->d_S, p->stream));
         if (p->nParvo > 0)
             PV1_CUDA(p, launch_parvo_spatial(tex[0], tex[1], tex[2], p->d_pSW, p->d_pSC, p->d_pCone, p->nParvo,
-                                            p->pSample, (int)nl, (int)f0, p->d_pS, p->stream));
+                                            p->pSample, first, (int)nl - first, (int)f0 + first, p->d_pS, p->stream));
+        p->lazyFrames = single;
         PV1_CUDA(p, cudaStreamSynchronize(p->stream));
         if (!single) {
             for (int ch = 0; ch < 3; ch++) {
@@ -866,6 +935,7 @@ int pv1_stimulus_load(pv1_plan *p, uint32_t nFrame, uint32_t height, uint32_t wi
         }
     }
     p->nFrame = (int)nFrame;
+    p->framesDone = p->lazyFrames ? 0 : (int)nFrame;
     p->lp.S = p->d_S;
     p->lp.pS = p->d_pS;
     p->lp.fs.nFrame = (int)nFrame;
@@ -890,6 +960,8 @@ void pv1_host_free(void *ptr) {
 int pv1_lgn_get_spatial(pv1_plan *p, float *S) {
     if (!p || !S) return PV1_E_ARG;
     if (!p->stimReady) return fail(p, PV1_E_STATE, "no stimulus loaded");
+    int r = ensure_all_frames(p);
+    if (r) return r;
     PV1_CUDA(p, cudaStreamSynchronize(p->stream));
     PV1_CUDA(p, cudaMemcpy(S, p->d_S, (size_t)(p->nFrame + 1) * p->nMagno * sizeof(float), cudaMemcpyDeviceToHost));
     return PV1_OK;
@@ -1244,6 +1316,8 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
         return fail(p, PV1_E_ARG, "run longer than the record ring; fetch records in between");
     int r = choose_mode(p);
     if (r) return r;
+    r = ensure_frames(p, p->step + (long long)nsteps - 1);
+    if (r) return r;
     p->launches = 0;
     PV1_CUDA(p, cudaMemcpyAsync(p->d_stepBase, &p->step, sizeof(long long), cudaMemcpyHostToDevice, p->stream));
     uint32_t done = 0;
@@ -1252,6 +1326,8 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
     if (!p->pending && nsteps > 0) {
         int k = (int)std::min<uint32_t>(nsteps, (uint32_t)K);
         r = issue_chunk(p, k, 0, &p->launches);
+        if (r) return r;
+        r = sink_rows(p, p->step + (long long)done, k);
         if (r) return r;
         done += k;
     }
@@ -1282,6 +1358,8 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
                 if (e == cudaSuccess) e = launch_advance_step(p->d_stepBase, K, p->stream);
                 if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("v1_persistent: ") + cudaGetErrorString(e));
                 p->launches += 2;
+                r = sink_rows(p, t0 + (long long)c * K, K);
+                if (r) return r;
                 if (c + 1 < nFull) {
                     PV1_CUDA(p, cudaStreamWaitEvent(p->lgnStream, p->evFree, 0));
                     e = launch_lgn_step(p->lp, p->d_lgnStep, K, p->lgnStream);
@@ -1296,6 +1374,8 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
             // a cooperative launch per chunk: issued directly (4 launches per K steps)
             while (nsteps - done >= (uint32_t)K) {
                 r = issue_chunk(p, K, 1, &p->launches);
+                if (r) return r;
+                r = sink_rows(p, p->step + (long long)done, K);
                 if (r) return r;
                 done += K;
             }
@@ -1315,6 +1395,8 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
             while (nsteps - done >= (uint32_t)K) {
                 PV1_CUDA(p, cudaGraphLaunch(p->graphExec, p->stream));
                 p->launches += p->graphLaunches;
+                r = sink_rows(p, p->step + (long long)done, K);
+                if (r) return r;
                 done += K;
             }
         }
@@ -1322,6 +1404,8 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
     if (done < nsteps) {
         int k = (int)(nsteps - done);
         r = issue_chunk(p, k, 1, &p->launches);
+        if (r) return r;
+        r = sink_rows(p, p->step + (long long)done, k);
         if (r) return r;
         done += k;
     }
@@ -1332,6 +1416,29 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
 }
 
 int64_t pv1_last_launch_count(const pv1_plan *p) { return p ? p->launches : -1; }
+
+int pv1_run_spikes_to_host(pv1_plan *p, uint32_t nsteps, float *out) {
+    if (!p || (!out && nsteps)) return PV1_E_ARG;
+    if (!(p->recFlags & PV1_REC_SPIKES)) return fail(p, PV1_E_STATE, "spike recording is off");
+    if (!p->copyStream) {
+        PV1_CUDA(p, cudaStreamCreateWithFlags(&p->copyStream, cudaStreamNonBlocking));
+        PV1_CUDA(p, cudaEventCreateWithFlags(&p->evChunk, cudaEventDisableTiming));
+        PV1_CUDA(p, cudaEventCreateWithFlags(&p->evCopied, cudaEventDisableTiming));
+    }
+    p->sinkHost = out;
+    p->sinkStep0 = p->step;
+    int r = pv1_run(p, nsteps, 0);
+    p->sinkHost = nullptr;
+    if (r) {
+        cudaStreamSynchronize(p->copyStream);
+        return r;
+    }
+    // the plan's stream continues after the copies (later runs overwrite the ring)
+    PV1_CUDA(p, cudaEventRecord(p->evCopied, p->copyStream));
+    PV1_CUDA(p, cudaStreamWaitEvent(p->stream, p->evCopied, 0));
+    PV1_CUDA(p, cudaStreamSynchronize(p->copyStream));
+    return check_device_error(p);
+}
 
 int pv1_fetch_spikes(pv1_plan *p, uint64_t step0, uint32_t n, float *out) {
     if (!p || !out) return PV1_E_ARG;
@@ -1389,6 +1496,8 @@ int pv1_time_kernels(pv1_plan *p, uint32_t nsteps, float *v1_ms, float *lgn_ms, 
     const int K = p->K;
     const uint32_t nchunk = nsteps / K;
     if (nchunk == 0) return fail(p, PV1_E_ARG, "nsteps < chunk");
+    r = ensure_frames(p, p->step + (long long)nchunk * K - 1);
+    if (r) return r;
     std::vector<cudaEvent_t> ev(3 * nchunk);
     for (auto &e : ev) PV1_CUDA(p, cudaEventCreate(&e));
     PV1_CUDA(p, cudaMemcpyAsync(p->d_stepBase, &p->step, sizeof(long long), cudaMemcpyHostToDevice, p->stream));

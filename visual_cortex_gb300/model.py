@@ -339,6 +339,15 @@ class Simulation:
         N.check(self.plan, N.lib.pv1_run(self.plan, int(nsteps), int(sync)), "pv1_run")
         self.step += nsteps
 
+    def run_spikes_to_host(self, nsteps: int, out: np.ndarray) -> np.ndarray:
+        """Runs nsteps and writes their spike words into out [nsteps][nV1] (float32, best
+        page-locked: N.pinned_empty), the copies overlapping the run."""
+        if out.shape != (nsteps, self.spec.nV1) or out.dtype != f32 or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous float32 array [nsteps][nV1]")
+        N.check(self.plan, N.lib.pv1_run_spikes_to_host(self.plan, int(nsteps), N.fptr(out)), "pv1_run_spikes_to_host")
+        self.step += nsteps
+        return out
+
     def launches(self) -> int:
         return int(N.lib.pv1_last_launch_count(self.plan))
 

@@ -401,3 +401,31 @@ def test_spikes_streamed_to_host_equal_fetched(c1_small):
     finally:
         a.close()
         b.close()
+
+
+@pytest.mark.parametrize("m,persistent", [(24, True), (40, False)])
+def test_ragged_sizes_parity(native, m, persistent):
+    """Ragged shapes: blocks of 640 neurons (3 CTAs per block, the last one half empty), 0..m
+    LGN synapses per neuron (some neurons without feed-forward input), 40 synapses (past the
+    register-held lists: the persistent kernel declines and per-step launches run), far
+    synapses across 3 blocks."""
+    from visual_cortex_gb300 import synth
+    from visual_cortex_gb300.model import Simulation
+    from oracle.parity import run_parity, compare
+    wl = synth.make_workload("ragged", seed=21, nblock=3, n_lgn=512, m=m, m_min=0, width=64, height=64,
+                             nt=800, far_partners=60, adex_inh=True, nFrame=60, blockSize=640, nE=512,
+                             wFF=0.3)
+    assert (wl.net.nLGNperV1 == 0).any()
+    sim = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        assert sim.persistent() == persistent
+        res = run_parity(wl, RASTER_STEPS, cap=8, sim=sim)
+    finally:
+        sim.close()
+    cmp = compare(res, wl.spec)
+    assert res["draw_count_mismatch"] == 0
+    assert cmp["lgn_spike_mismatch"] == 0, cmp
+    assert cmp["v1_spikes_gpu"] > 0, cmp
+    assert_raster_ok(cmp)
+    for k in ("v", "gE", "gI", "gFF"):
+        assert cmp[f"max_rel_{k}"] < 1e-5, cmp

@@ -338,13 +338,14 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
                   noisyDep=(0.0, 0.0), synFail=(0.0, 0.0, 0.0, 0.0), synFailFF=(0.0, 0.0),
                   mSample1D: int = 16, dt: float = 0.125, tjitter: float = 0.0,
                   noDelay: int = 1, n_parvo: int = 0, tau: float | None = None,
-                  nKernelSample: int | None = None) -> Workload:
+                  nKernelSample: int | None = None, blockSize: int = 1024, nE: int = 768,
+                  m_min: int | None = None) -> Workload:
     """Builds one synthetic patch; C1 = 1x1024 V1 / 512 LGN; C2 = 32 blocks / 16384 LGN.
     noDelay = 0: near synapses are delivered after their distance delay (delayMat from the
     neuron positions, mm, at speedOfThought 1 mm/ms)."""
     rng = np.random.default_rng(seed)
-    spec = make_spec(nblock, adex_inh=adex_inh, noisyDep=noisyDep, synFail=synFail,
-                     synFailFF=synFailFF, dt=dt)
+    spec = make_spec(nblock, blockSize=blockSize, nE=nE, adex_inh=adex_inh, noisyDep=noisyDep,
+                     synFail=synFail, synFailFF=synFailFF, dt=dt)
     lgn, extent = make_lgn(n_lgn, rng, patch_deg, dt, mSample1D=mSample1D, tjitter=tjitter,
                            n_parvo=n_parvo, tau=tau, nKernelSample=nKernelSample)
     side = 0.5
@@ -358,6 +359,8 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
         nVec = np.zeros(spec.nV1, u32)
         vecID, conVec, delayVec = np.zeros(0, u32), np.zeros(0, f32), np.zeros(0, f32)
     nLGNperV1, lgnId, sLGN, rfc, rfo = lgn_to_v1(spec, lgn, rng, m, wFF, patch_deg)
+    if m_min is not None:   # ragged LGN lists: m_min..m synapses per neuron (rows past the count unused)
+        nLGNperV1 = rng.integers(m_min, m + 1, size=spec.nV1).astype(u32)
     tonic = np.where(spec.type_of(np.arange(spec.nV1) % spec.blockSize) == 0,
                      rng.uniform(0.3, 0.6, spec.nV1), rng.uniform(0.4, 0.7, spec.nV1)).astype(f32)
     nbId = np.arange(nblock, dtype=u32)[:, None].copy()

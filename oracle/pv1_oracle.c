@@ -75,6 +75,59 @@ static float gauss2(float x, float y, float rx, float ry) {
     return expf(-x * x / (rx * rx) - y * y / (ry * ry));
 }
 
+/* Curved retina (flat_retina = 0): orthPhiRotate3D, axisRotate3D and retina_to_plane of
+ * src/discrete_input_convol.cuh:200-326, in single precision. */
+static void orth_phi_rotate(float theta, float phi, float eta, float *cost, float *sint, float *cosPhi,
+                            float *sinPhi) {
+    const float tan_eta = tanf(eta), sin_phi = sinf(phi);
+    const float r = sqrtf(tan_eta * tan_eta + sin_phi * sin_phi);
+    *cosPhi = cosf(eta) * cosf(phi);
+    *sinPhi = r;
+    float cost1 = sin_phi / r, sint1 = tan_eta / r;
+    if (fabsf(sint1) > 1.0f) sint1 = copysignf(sqrtf(1 - cost1 * cost1), sint1);
+    if (fabsf(cost1) > 1.0f) cost1 = copysignf(sqrtf(1 - sint1 * sint1), cost1);
+    const float cost0 = cosf(theta), sint0 = sinf(theta);
+    float c = cost0 * cost1 - sint0 * sint1, sn = sint0 * cost1 + cost0 * sint1;
+    if (fabsf(sn) > 1.0f) sn = copysignf(sqrtf(1 - c * c), sn);
+    if (fabsf(c) > 1.0f) c = copysignf(sqrtf(1 - sn * sn), c);
+    *cost = c;
+    *sint = sn;
+}
+
+static void axis_rotate(float theta0, float phi0, float ceta, float seta, float *cost, float *sint, float cosPhi,
+                        float sinPhi, float *tanPhi) {
+    const float sinPhi0 = sinf(phi0);
+    const float xr = sinPhi0 * sinf(theta0), yr = sinPhi0 * cosf(theta0), zr = cosf(phi0);
+    const float x = sinPhi * *sint, y = sinPhi * *cost, z = cosPhi;
+    const float zp = (zr * xr * (1 - ceta) + yr * seta) * x + (zr * yr * (1 - ceta) - xr * seta) * y +
+                     (zr * zr * (1 - ceta) + ceta) * z;
+    const float yp = (yr * xr * (1 - ceta) - zr * seta) * x + (yr * yr * (1 - ceta) + ceta) * y +
+                     (yr * zr * (1 - ceta) + xr * seta) * z;
+    const float xp = (xr * xr * (1 - ceta) + ceta) * x + (xr * yr * (1 - ceta) + zr * seta) * y +
+                     (xr * zr * (1 - ceta) - yr * seta) * z;
+    *tanPhi = sqrtf(xp * xp + yp * yp) / zp;
+    const float theta = atan2f(xp, yp);
+    *cost = cosf(theta);
+    *sint = sinf(theta);
+}
+
+/* Texture coordinates of the sample (w, h) of a Gaussian centred at (polar, ecc) with
+ * orientation (coso, sino): flat (a scaled plane) or curved (the sphere projected). */
+static void sample_xy(int flat, float polar, float ecc, float w, float h, float coso, float sino, float nvd, float x0,
+                      float y0, float *x, float *y) {
+    if (flat) {
+        *x = x0 + (ecc * cosf(polar) + w * coso - h * sino) * nvd;
+        *y = y0 + (ecc * sinf(polar) + w * sino + h * coso) * nvd;
+        return;
+    }
+    float cosp, sinp, cosEcc, sinEcc, tanEcc;
+    orth_phi_rotate(polar, ecc + h, w, &cosp, &sinp, &cosEcc, &sinEcc);
+    axis_rotate(polar, ecc, coso, sino, &cosp, &sinp, cosEcc, sinEcc, &tanEcc);
+    const float r = tanEcc * nvd;
+    *x = x0 + r * cosp;
+    *y = y0 + r * sinp;
+}
+
 /* nsig * r / SQRT2: the float product divided in double (SQRT2, src/CONST.h:30). */
 static float parvo_span(float nsig, float r) { return (float)((double)(nsig * r) / 1.4142135623730951); }
 /* Sample coordinate (i + 0.5) * d - span in double, rounded once to float, as the
@@ -165,9 +218,8 @@ int orc_lgn_setup(const pv1_lgn_config *c, const pv1_lgn_params *p, float *TW, f
         for (int s = 0; s < nS; s++) {
             const int tx = s % n1, ty = s / n1;
             const float cx = grid_at(tx, ds, span), cy = grid_at(ty, ds, span);
-            SC[(size_t)m * nS + s] = x0 + (p->ecc[id] * cosf(p->polar[id]) + cx * coso - cy * sino) * c->normViewDistance;
-            SC[(size_t)nMagno * nS + (size_t)m * nS + s] =
-                y0 + (p->ecc[id] * sinf(p->polar[id]) + cx * sino + cy * coso) * c->normViewDistance;
+            sample_xy(c->flat_retina, p->polar[id], p->ecc[id], cx, cy, coso, sino, c->normViewDistance, x0, y0,
+                      &SC[(size_t)m * nS + s], &SC[(size_t)nMagno * nS + (size_t)m * nS + s]);
         }
     }
     free(cw);
@@ -351,8 +403,8 @@ int orc_lgn_parvo_setup(const pv1_lgn_config *c, const pv1_lgn_parvo_config *q, 
             for (int s = 0; s < nS; s++) {
                 const float w = grid_at(s % n1, dw, wSpan), h = grid_at(s / n1, dh, hSpan);
                 const size_t sid = ((size_t)cell * 2 + type) * nS + s;
-                SC[sid] = x0 + (ce * cosf(cp) + w * coso - h * sino) * c->normViewDistance;
-                SC[(size_t)nParvo * 2 * nS + sid] = y0 + (ce * sinf(cp) + w * sino + h * coso) * c->normViewDistance;
+                sample_xy(c->flat_retina, cp, ce, w, h, coso, sino, c->normViewDistance, x0, y0, &SC[sid],
+                          &SC[(size_t)nParvo * 2 * nS + sid]);
             }
         }
     }

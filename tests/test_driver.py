@@ -98,3 +98,25 @@ def test_parvo_cells_read_back():
     for k in ("polar", "ecc", "rw", "rh", "orient", "k", "tauR", "tauD", "delay", "coneType", "covariant",
               "c50", "sharpness"):
         assert np.array_equal(getattr(L, k), getattr(L0, k)), k
+
+
+def test_curved_retina_reads_back():
+    """flat_retina = false: a two-eye stimulus file, the curved geometry of src/patch.cu:
+    1609-1622 (visual centre of the left eye at buffer / (2 extent), view distance from
+    tan(max_ecc))."""
+    import math
+    wl = synth.make_workload("curved", seed=4, nblock=1, n_lgn=256, m=20, width=64, height=64, nt=48,
+                             nFrame=40, flat_retina=False)
+    d = tempfile.mkdtemp()
+    fn = synth.write_reference_files(wl, d, seed=3, nt=48)
+    m = driver.build(cfg.load(["-c", fn]))
+    L = m.lgn
+    assert not L.flat_retina and L.L_y0 == 0.5 and 0 < L.L_x0 < 0.25
+    assert L.R_x0 == np.float32(0.5) + np.float32(L.L_x0)
+    stim = FM.read_stimulus(cfg.resolve_paths(cfg.load(["-c", fn])).stimulus)
+    ext = stim.range + 2 * stim.buffer
+    max_ecc = float(np.max(np.hypot(wl.lgn.xy[:, 0], wl.lgn.xy[:, 1])))
+    assert L.normViewDistance == pytest.approx((max_ecc / (2 * ext)) / math.tan(max_ecc * math.pi / 180), rel=1e-5)
+    assert stim.neye == 2
+    with pytest.raises(cfg.ConfigError, match="one eye"):
+        driver.build(cfg.load(["-c", fn, "--flat_retina", "1"]))

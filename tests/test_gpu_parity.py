@@ -429,3 +429,40 @@ def test_ragged_sizes_parity(native, m, persistent):
     assert_raster_ok(cmp)
     for k in ("v", "gE", "gI", "gFF"):
         assert cmp[f"max_rel_{k}"] < 1e-5, cmp
+
+
+@pytest.fixture(scope="module")
+def curved_wl(native):
+    """A curved retina (sample points on the eye's sphere projected to the plane), magno and
+    parvo cells in the right hemifield of the left eye's half of a binocular texture."""
+    from visual_cortex_gb300 import synth
+    return synth.make_workload("curved", seed=14, nblock=1, n_lgn=512, m=20, width=96, height=96, nt=800,
+                               nFrame=60, n_parvo=64, tau=300.0, nKernelSample=150, flat_retina=False)
+
+
+def test_curved_retina_setup_tables(curved_wl):
+    import oracle
+    from visual_cortex_gb300.model import Simulation
+    wl = curved_wl
+    sim = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        TW, SW, SC, mc = sim.lgn_tables()
+        pTW, pSW, pSC = sim.lgn_parvo_tables()
+    finally:
+        sim.close()
+    lo = oracle.LgnOracle(wl.lgn, wl.stim)
+    np.testing.assert_allclose(SC, lo.SC, rtol=1e-6, atol=2e-6)
+    np.testing.assert_allclose(pSC, lo.pSC, rtol=1e-6, atol=2e-6)
+    assert 0 < SC[0].min() and SC[0].max() < 0.5      # the left eye's half of the texture
+    np.testing.assert_allclose(mc, lo.maxConvol, rtol=1e-5)
+
+
+def test_curved_retina_dynamics_parity(curved_wl):
+    from oracle.parity import run_parity, compare
+    wl = curved_wl
+    res = run_parity(wl, RASTER_STEPS, cap=8)
+    cmp = compare(res, wl.spec)
+    assert res["draw_count_mismatch"] == 0
+    assert cmp["lgn_spike_mismatch"] == 0, cmp
+    assert cmp["lgn_fr_maxrel"] < 1e-5, cmp
+    assert_raster_ok(cmp)

@@ -216,6 +216,7 @@ struct SetupArgs {
 // Parvo store_PM + parvo_maxConvol arguments.
 struct ParvoSetupArgs {
     int nParvo, nLGN, nParvo_I, nMagno_I;
+    int flat;                  // 1: flat retina, 0: curved (sphere projected to the plane)
     int nSample, nSample1D, nKS;
     float kernelSampleDt, kernelSampleT0;
     float normViewDistance, L_x0, L_y0, R_x0, R_y0, nsig;

@@ -65,6 +65,62 @@ __device__ __forceinline__ float grid_coord(int i, float d, float span) {
 
 
 
+// ---- curved-retina geometry (flat_retina = 0): sample points on the eye's sphere projected
+// to the stimulus plane, as orthPhiRotate3D, axisRotate3D and retina_to_plane
+// (src/discrete_input_convol.cuh:200-326) compute them in single precision ----
+
+// The point at angle eta off the meridian through (theta, phi), orthogonal to it: its polar
+// angle (cos, sin) and its eccentricity (cos, sin).
+__device__ __forceinline__ void orth_phi_rotate(float theta, float phi, float eta, float &cost, float &sint,
+                                                float &cosPhi, float &sinPhi) {
+    const float tan_eta = tanf(eta);
+    const float sin_phi = sinf(phi);
+    const float r = sqrtf(tan_eta * tan_eta + sin_phi * sin_phi);
+    cosPhi = cosf(eta) * cosf(phi);
+    sinPhi = r;
+    float cost1 = sin_phi / r, sint1 = tan_eta / r;
+    if (fabsf(sint1) > 1.0f) sint1 = copysignf(sqrtf(1 - cost1 * cost1), sint1);
+    if (fabsf(cost1) > 1.0f) cost1 = copysignf(sqrtf(1 - sint1 * sint1), cost1);
+    const float cost0 = cosf(theta), sint0 = sinf(theta);
+    cost = cost0 * cost1 - sint0 * sint1;
+    sint = sint0 * cost1 + cost0 * sint1;
+    if (fabsf(sint) > 1.0f) sint = copysignf(sqrtf(1 - cost * cost), sint);
+    if (fabsf(cost) > 1.0f) cost = copysignf(sqrtf(1 - sint * sint), cost);
+}
+
+// Rotation of the point (polar cos/sin, eccentricity cos/sin) by (ceta, seta) about the axis
+// through (theta0, phi0); returns the new polar angle's cos/sin and tan(eccentricity).
+__device__ __forceinline__ void axis_rotate(float theta0, float phi0, float ceta, float seta, float &cost, float &sint,
+                                            float cosPhi, float sinPhi, float &tanPhi) {
+    const float sinPhi0 = sinf(phi0);
+    const float x_rot = sinPhi0 * sinf(theta0);
+    const float y_rot = sinPhi0 * cosf(theta0);
+    const float z_rot = cosf(phi0);
+    const float x = sinPhi * sint, y = sinPhi * cost, z = cosPhi;
+    const float z_prime = (z_rot * x_rot * (1 - ceta) + y_rot * seta) * x + (z_rot * y_rot * (1 - ceta) - x_rot * seta) * y +
+                          (z_rot * z_rot * (1 - ceta) + ceta) * z;
+    const float y_prime = (y_rot * x_rot * (1 - ceta) - z_rot * seta) * x + (y_rot * y_rot * (1 - ceta) + ceta) * y +
+                          (y_rot * z_rot * (1 - ceta) + x_rot * seta) * z;
+    const float x_prime = (x_rot * x_rot * (1 - ceta) + ceta) * x + (x_rot * y_rot * (1 - ceta) + z_rot * seta) * y +
+                          (x_rot * z_rot * (1 - ceta) - y_rot * seta) * z;
+    tanPhi = sqrtf(x_prime * x_prime + y_prime * y_prime) / z_prime;
+    const float theta = atan2f(x_prime, y_prime);
+    cost = cosf(theta);
+    sint = sinf(theta);
+}
+
+// Texture coordinates of the sample at (w, h) in the frame of a Gaussian centred at
+// (polar, ecc) with orientation (coso, sino) on a curved retina.
+__device__ __forceinline__ void curved_sample(float polar, float ecc, float w, float h, float coso, float sino,
+                                              float nvd, float x0, float y0, float &x, float &y) {
+    float cosp, sinp, cosEcc, sinEcc, tanEcc;
+    orth_phi_rotate(polar, ecc + h, w, cosp, sinp, cosEcc, sinEcc);
+    axis_rotate(polar, ecc, coso, sino, cosp, sinp, cosEcc, sinEcc, tanEcc);
+    const float r = tanEcc * nvd;
+    x = x0 + r * cosp;
+    y = y0 + r * sinp;
+}
+
 // One CTA per magno cell, one thread per spatial sample (store_PM with PM=1,
 // src/discrete_input_convol.cu:427-744, store_temporalWeight :230-305).
 __global__ void __launch_bounds__(1024) lgn_setup_kernel(SetupArgs A) {
@@ -149,15 +205,16 @@ __global__ void __launch_bounds__(1024) lgn_setup_kernel(SetupArgs A) {
     const bool left = cell < A.nMagno_I;
     const float x0 = left ? A.L_x0 : A.R_x0;
     const float y0 = left ? A.L_y0 : A.R_y0;
+    float x, y;
     if (A.flat) {
-        float x = x0 + (cEcc * cosf(cPolar) + cx * coso - cy * sino) * A.normViewDistance;
-        float y = y0 + (cEcc * sinf(cPolar) + cx * sino + cy * coso) * A.normViewDistance;
-        if (active) {
-            A.SC[(size_t)cell * nSample + tid] = x;
-            A.SC[(size_t)A.nMagno * nSample + (size_t)cell * nSample + tid] = y;
-        }
-    } else if (tid == 0) {
-        atomicOr(A.err, kErrBounds);  // curved-retina geometry is not built (host rejects it)
+        x = x0 + (cEcc * cosf(cPolar) + cx * coso - cy * sino) * A.normViewDistance;
+        y = y0 + (cEcc * sinf(cPolar) + cx * sino + cy * coso) * A.normViewDistance;
+    } else {
+        curved_sample(cPolar, cEcc, cx, cy, coso, sino, A.normViewDistance, x0, y0, x, y);
+    }
+    if (active) {
+        A.SC[(size_t)cell * nSample + tid] = x;
+        A.SC[(size_t)A.nMagno * nSample + (size_t)cell * nSample + tid] = y;
     }
 }
 
@@ -219,8 +276,13 @@ __global__ void __launch_bounds__(1024) lgn_parvo_setup_kernel(ParvoSetupArgs A)
     const bool left = cell < A.nParvo_I;
     const float x0 = left ? A.L_x0 : A.R_x0, y0 = left ? A.L_y0 : A.R_y0;
     if (active) {
-        const float x = x0 + (ecc * cosf(polar) + w * coso - h * sino) * A.normViewDistance;
-        const float y = y0 + (ecc * sinf(polar) + w * sino + h * coso) * A.normViewDistance;
+        float x, y;
+        if (A.flat) {
+            x = x0 + (ecc * cosf(polar) + w * coso - h * sino) * A.normViewDistance;
+            y = y0 + (ecc * sinf(polar) + w * sino + h * coso) * A.normViewDistance;
+        } else {
+            curved_sample(polar, ecc, w, h, coso, sino, A.normViewDistance, x0, y0, x, y);
+        }
         const size_t sid = ((size_t)cell * 2 + type) * nSample + tid;
         A.SC[sid] = x;
         A.SC[(size_t)A.nParvo * 2 * nSample + sid] = y;

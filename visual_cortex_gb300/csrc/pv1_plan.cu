@@ -481,7 +481,6 @@ int lgn_setup_impl(pv1_plan *p, const pv1_lgn_config *lc, const pv1_lgn_parvo_co
     if (nParvo > 0 && !covariant) return fail(p, PV1_E_ARG, "parvo cells need the covariant array");
     if (nParvo > 0 && (pc->nSample1D < 1 || pc->nSample1D > 32 || pc->nKernelSample < 1))
         return fail(p, PV1_E_ARG, "parvo nSample1D must be in [1,32] and nKernelSample >= 1");
-    if (!c.flat_retina) return fail(p, PV1_E_UNSUPPORTED, "curved-retina sample geometry is not built (flat_retina=1 only)");
     if ((int)c.nLGN != nParvo + nMagno) return fail(p, PV1_E_ARG, "nLGN != nParvo + nMagno");
     if (c.mSample1D < 1 || c.mSample1D > 32) return fail(p, PV1_E_ARG, "mSample1D must be in [1,32]");
     if (c.nKernelSample < 1 || c.ntPerFrame < 1 || c.denorm < 1 || c.maxFrame < 1)
@@ -663,6 +662,7 @@ int lgn_setup_impl(pv1_plan *p, const pv1_lgn_config *lc, const pv1_lgn_parvo_co
         if (r) return fail(p, PV1_E_NOMEM, "parvo LGN allocation failed");
         ParvoSetupArgs PA{};
         PA.nParvo = nParvo;
+        PA.flat = c.flat_retina;
         PA.nLGN = nLGN;
         PA.nParvo_I = (int)c.nParvo_I;
         PA.nMagno_I = (int)c.nMagno_I;

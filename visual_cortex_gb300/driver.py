@@ -21,6 +21,7 @@ import numpy as np
 from . import formats as FM
 from .cfg import Config, ConfigError, load, resolve_paths
 from .model import InitState, LgnSpec, Seeds, Stimulus, V1Network, V1Spec, host_init_state
+from .retina import retina_geometry
 from .schedule import make_schedule
 
 f32, u32 = np.float32, np.uint32
@@ -73,8 +74,6 @@ def _check_supported(c: Config):
         bad.append("useNewLGN = true (LGN parameters drawn from distributions)")
     if c.virtual_LGN or c.LGN_switch or c.reverseInput:
         bad.append("virtual_LGN / LGN_switch / reverseInput")
-    if not c.flat_retina:
-        bad.append("flat_retina = false (binocular stimulus)")
     if c.minimal:
         bad.append("minimal = true (sampled output)")
     if c.fSnapshot:
@@ -229,8 +228,11 @@ def build(c: Config) -> Model:
 
     # LGN cells (src/patch.cu:1523-1640, 2505-2530) and the stimulus
     stim_f = FM.read_stimulus(P.stimulus)
-    if stim_f.neye != 1:
-        raise ConfigError("flat retina needs a one-eye stimulus")
+    # src/patch.cu:1457-1468: a flat retina reads a one-eye stimulus, a curved one two eyes
+    if c.flat_retina and stim_f.neye != 1:
+        raise ConfigError("flat retina shall receive one eye stimulus")
+    if not c.flat_retina and stim_f.neye != 2:
+        raise ConfigError("non-flat retina shall receive two eye stimulus")
     nI_, nC_, max_ecc, _, _, LGNtype = FM.read_lgn_vpos(P.lgn_vpos)
     nLGN = nI_ + nC_
     if max_ecc > stim_f.range:
@@ -243,15 +245,14 @@ def build(c: Config) -> Model:
     if nC_ and nParvo_I + nParvo_C:
         raise ConfigError("not supported by this build: parvo cells with a second eye")
     prm = FM.read_lgn_params(P.lgn, nLGN)
-    extent = f32(2) * (f32(stim_f.range) + f32(stim_f.buffer))
-    normEcc = f32(f32(max_ecc) / extent)
-    nvd = float(f32(f32(normEcc / f32(max_ecc)) / f32(DEG)))
+    geo = retina_geometry(max_ecc, stim_f.range, stim_f.buffer, bool(c.flat_retina))
     sched = make_schedule(c.dt, c.frameRate, c.tau, c.mau, c.nKernelSample, c.mKernelSample)
     lgn = LgnSpec(nParvo_I=nParvo_I, nMagno_I=nI_ - nParvo_I, nParvo_C=nParvo_C, nMagno_C=nC_ - nParvo_C,
                   mSample1D=c.mSpatialSample1D, sched=sched,
                   **{k: prm[k] for k in FM.LGN_FIELDS2 + FM.LGN_FIELDS1 + ("coneType",)},
-                  normViewDistance=nvd, L_x0=0.5, L_y0=0.5, R_x0=1.0, R_y0=1.0, nsig=c.nsig,
-                  convolRatio=c.convolRatio, frRatio=c.frRatioLGN, flat_retina=True,
+                  normViewDistance=geo["normViewDistance"], L_x0=geo["L_x0"], L_y0=geo["L_y0"], R_x0=geo["R_x0"],
+                  R_y0=geo["R_y0"], nsig=c.nsig, convolRatio=c.convolRatio, frRatio=c.frRatioLGN,
+                  flat_retina=bool(c.flat_retina),
                   nSample1D=c.nSpatialSample1D, covariant=prm["covariant"])
     stim = Stimulus(frames=stim_f.frames, init_LMS=stim_f.init_LMS)
 
@@ -265,7 +266,7 @@ def build(c: Config) -> Model:
                            tonicMax=float(iTonic.max()))
     seeds = Seeds(lgn=s_lgn, cond=s_sp, trainDepth=max(trainDepth, 1))
     extra = dict(nType=nType, nTypeE=nTypeE, nTypeI=nTypeI, typeAcc=typeAcc, nLGN=nLGN,
-                 normViewDistance=nvd, stimulus_filename=P.stimulus, sRatioV1=sRatioV1,
+                 normViewDistance=geo["normViewDistance"], stimulus_filename=P.stimulus, sRatioV1=sRatioV1,
                  sRatioLGN=sRatioLGN, tonicDep=tonicDep, noisyDep=noisyDep, vR=vR,
                  vThres=vThres, gL=gL, vT=vT, C=Cm, tRef=tRef, a=a, b=b, tau_w=tau_w,
                  deltaT=deltaT, synFail=synFail, synFailFF=synFailFF, paths=P)

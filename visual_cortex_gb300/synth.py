@@ -15,6 +15,7 @@ import numpy as np
 
 from .model import InitState, LgnSpec, Seeds, Stimulus, V1Network, V1Spec, host_init_state
 from .schedule import make_schedule
+from .retina import retina_geometry
 
 f32 = np.float32
 u32 = np.uint32
@@ -83,24 +84,29 @@ def make_lgn(n_lgn: int, rng: np.random.Generator, patch_deg: float, dt: float,
              stim_range_deg: float | None = None, buffer_deg: float = 0.2,
              jitter: float = 0.0, tjitter: float = 0.0, n_parvo: int = 0,
              tau: float | None = None, nKernelSample: int | None = None,
-             nSample1D: int = 8) -> tuple[LgnSpec, float]:
+             nSample1D: int = 8, flat_retina: bool = True) -> tuple[LgnSpec, float]:
     """ON/OFF magno cells with centers uniform in a patch_deg square around the fixation;
     with n_parvo > 0 also parvocellular L/M-opponent cells (LGN ids 0..n_parvo-1, before the
     magno cells as the reference orders them), centre and surround at slightly different
     positions and orientations, each with its own temporal kernel, sampled over `tau` ms with
     nKernelSample taps.
 
-    Returns the spec and the full stimulus extent (deg) the texture spans (flat retina)."""
+    flat_retina = False: the cells sit in the right hemifield of a curved retina whose
+    sample points are projected to the stimulus plane (the left eye's half of a binocular
+    texture).
+
+    Returns the spec and the full stimulus extent (deg) the texture spans."""
     nOn = n_lgn // 2
     xy = rng.uniform(-patch_deg / 2, patch_deg / 2, size=(n_lgn, 2))
+    if not flat_retina:
+        xy[:, 0] = np.abs(xy[:, 0]) + 0.1 * patch_deg
     polar = np.arctan2(xy[:, 1], xy[:, 0])
     ecc = np.hypot(xy[:, 0], xy[:, 1]) * DEG
     max_ecc = float(np.max(np.hypot(xy[:, 0], xy[:, 1])))
     if stim_range_deg is None:
         stim_range_deg = max(max_ecc, patch_deg / 2) * 1.05
-    extent = 2 * (stim_range_deg + buffer_deg)
-    norm_ecc_max = max_ecc / extent
-    normViewDistance = norm_ecc_max / max_ecc / DEG
+    geo = retina_geometry(max_ecc, stim_range_deg, buffer_deg, flat_retina)
+    extent, normViewDistance = geo["extent"], geo["normViewDistance"]
     sc = sigma_c * (1 + jitter * rng.uniform(-1, 1, n_lgn))
     ss = sigma_s * (1 + jitter * rng.uniform(-1, 1, n_lgn))
     two = lambda c, s: np.concatenate([c, s]).astype(f32)
@@ -110,7 +116,7 @@ def make_lgn(n_lgn: int, rng: np.random.Generator, patch_deg: float, dt: float,
                           else nKernelSample, mKernelSample)
     if n_parvo > 0:
         return _with_parvo(n_lgn, n_parvo, rng, patch_deg, sched, mSample1D, nSample1D, sigma_c, sigma_s,
-                           stim_range_deg, buffer_deg, jitter)
+                           stim_range_deg, buffer_deg, jitter, flat_retina)
     spec = LgnSpec(
         nParvo_I=0, nMagno_I=n_lgn, nParvo_C=0, nMagno_C=0, mSample1D=mSample1D, sched=sched,
         polar=two(polar, polar), ecc=two(ecc, ecc), rw=two(sc * DEG, ss * DEG),
@@ -124,18 +130,20 @@ def make_lgn(n_lgn: int, rng: np.random.Generator, patch_deg: float, dt: float,
         spont=np.full(n_lgn, 0.1, f32), c50=np.full(n_lgn, 0.25, f32),
         sharpness=np.full(n_lgn, 3.0, f32),
         coneType=np.full(2 * n_lgn, 3, u32),
-        normViewDistance=normViewDistance, L_x0=0.5, L_y0=0.5, R_x0=1.0, R_y0=1.0,
-        nsig=3.0, convolRatio=1.0, frRatio=1.0, flat_retina=True)
+        normViewDistance=normViewDistance, L_x0=geo["L_x0"], L_y0=geo["L_y0"], R_x0=geo["R_x0"],
+        R_y0=geo["R_y0"], nsig=3.0, convolRatio=1.0, frRatio=1.0, flat_retina=flat_retina)
     spec.types = types
     spec.xy = xy
     return spec, extent
 
 
 def _with_parvo(n_magno, n_parvo, rng, patch_deg, sched, mSample1D, nSample1D, sigma_c, sigma_s,
-                stim_range_deg, buffer_deg, jitter):
+                stim_range_deg, buffer_deg, jitter, flat_retina=True):
     """LGN of n_parvo parvo cells (ids first) and n_magno ON/OFF magno cells, one eye."""
     n = n_parvo + n_magno
     xy = rng.uniform(-patch_deg / 2, patch_deg / 2, size=(n, 2))
+    if not flat_retina:
+        xy[:, 0] = np.abs(xy[:, 0]) + 0.1 * patch_deg
     # surround centres of the parvo cells sit a little off their centres
     sxy = xy.copy()
     sxy[:n_parvo] += rng.normal(0.0, 0.01, size=(n_parvo, 2))
@@ -146,8 +154,8 @@ def _with_parvo(n_magno, n_parvo, rng, patch_deg, sched, mSample1D, nSample1D, s
     max_ecc = float(max(np.max(np.hypot(xy[:, 0], xy[:, 1])), np.max(np.hypot(sxy[:, 0], sxy[:, 1]))))
     if stim_range_deg is None:
         stim_range_deg = max(max_ecc, patch_deg / 2) * 1.05
-    extent = 2 * (stim_range_deg + buffer_deg)
-    normViewDistance = (max_ecc / extent) / max_ecc / DEG
+    geo = retina_geometry(max_ecc, stim_range_deg, buffer_deg, flat_retina)
+    extent, normViewDistance = geo["extent"], geo["normViewDistance"]
     types = np.empty(n, np.int64)
     types[:n_parvo] = np.arange(n_parvo) % 4          # LonMoff, LoffMon, MonLoff, MoffLon
     types[n_parvo:] = np.where(np.arange(n_magno) < n_magno // 2, 4, 5)
@@ -189,8 +197,8 @@ def _with_parvo(n_magno, n_parvo, rng, patch_deg, sched, mSample1D, nSample1D, s
         spont=np.full(n, 0.1, f32), c50=np.where(types < 4, 0.3, 0.25).astype(f32),
         sharpness=np.where(types < 4, 2.5, 3.0).astype(f32),
         coneType=np.concatenate([cone_c, cone_s]).astype(u32),
-        normViewDistance=normViewDistance, L_x0=0.5, L_y0=0.5, R_x0=1.0, R_y0=1.0,
-        nsig=3.0, convolRatio=1.0, frRatio=1.0, flat_retina=True, nSample1D=nSample1D,
+        normViewDistance=normViewDistance, L_x0=geo["L_x0"], L_y0=geo["L_y0"], R_x0=geo["R_x0"],
+        R_y0=geo["R_y0"], nsig=3.0, convolRatio=1.0, frRatio=1.0, flat_retina=flat_retina, nSample1D=nSample1D,
         covariant=np.where(types < 4, 0.53753461391295254, 1.0).astype(f32))
     spec.types = types
     spec.xy = xy
@@ -339,7 +347,7 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
                   mSample1D: int = 16, dt: float = 0.125, tjitter: float = 0.0,
                   noDelay: int = 1, n_parvo: int = 0, tau: float | None = None,
                   nKernelSample: int | None = None, blockSize: int = 1024, nE: int = 768,
-                  m_min: int | None = None) -> Workload:
+                  m_min: int | None = None, flat_retina: bool = True) -> Workload:
     """Builds one synthetic patch; C1 = 1x1024 V1 / 512 LGN; C2 = 32 blocks / 16384 LGN.
     noDelay = 0: near synapses are delivered after their distance delay (delayMat from the
     neuron positions, mm, at speedOfThought 1 mm/ms)."""
@@ -347,7 +355,7 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
     spec = make_spec(nblock, blockSize=blockSize, nE=nE, adex_inh=adex_inh, noisyDep=noisyDep,
                      synFail=synFail, synFailFF=synFailFF, dt=dt)
     lgn, extent = make_lgn(n_lgn, rng, patch_deg, dt, mSample1D=mSample1D, tjitter=tjitter,
-                           n_parvo=n_parvo, tau=tau, nKernelSample=nKernelSample)
+                           n_parvo=n_parvo, tau=tau, nKernelSample=nKernelSample, flat_retina=flat_retina)
     side = 0.5
     pos, nbx = block_positions(nblock, spec.blockSize, side, rng)
     conMat = near_conmat(spec, pos, rng, sigma=0.1, nE_partners=100, nI_partners=50,
@@ -438,7 +446,7 @@ def write_reference_files(wl: Workload, folder: str, seed: int = 0, nt: int | No
     patch = float(np.max(np.abs(lgn.xy))) * 2
     stim_range = max(max_ecc, patch / 2) * 1.05
     FM.write_stimulus(d + "stimulus.bin", wl.stim.frames, wl.stim.init_LMS,
-                      domain=(buffer_deg, stim_range), neye=1)
+                      domain=(buffer_deg, stim_range), neye=1 if lgn.flat_retina else 2)
     FM.write_lgn_vpos(d + "LGN_vpos.bin", lgn.nParvo_I + lgn.nMagno_I, lgn.nParvo_C + lgn.nMagno_C, max_ecc,
                       lgn.xy[:, 0].astype(f32), lgn.xy[:, 1].astype(f32), lgn.types)
     lp = {k: getattr(lgn, k) for k in FM.LGN_FIELDS2 + FM.LGN_FIELDS1 + ("coneType",)}
@@ -452,7 +460,7 @@ def write_reference_files(wl: Workload, folder: str, seed: int = 0, nt: int | No
         mau=s.mRetrace * spec.dt, nKernelSample=s.nKernelSample, mKernelSample=s.mKernelSample,
         mSpatialSample1D=lgn.mSample1D, nSpatialSample1D=lgn.nSample1D or 32, nsig=lgn.nsig,
         convolRatio=lgn.convolRatio,
-        frRatioLGN=lgn.frRatio, flat_retina=True, useNewLGN=False, learning=0,
+        frRatioLGN=lgn.frRatio, flat_retina=bool(lgn.flat_retina), useNewLGN=False, learning=0,
         nTypeHierarchy=[spec.nTypeE, spec.nType - spec.nTypeE], sRatioLGN=[1.0],
         sRatioV1=[1.0], synPerCon=spec.synPerCon, synPerConFF=spec.synPerConFF,
         riseTimeFF=spec.riseFF, decayTimeFF=spec.decayFF, riseTimeE=spec.riseE,

@@ -217,6 +217,36 @@ int pv1_v1_set_state(pv1_plan *plan, const float *v, const float *w, const float
  * (src/coredynamics.cu:5-146) for a network without initial spikes (spE0 = spI0 = 0). */
 int pv1_v1_init_rng(pv1_plan *plan, uint64_t seed, uint32_t trainDepth);
 
+/* What pv1_v1_init_spikes drew and built, for checking it against a restatement.  Host
+ * arrays; any pointer may be NULL. */
+typedef struct pv1_init_record {
+    float *uniforms;     /* [nV1][2*trainDepth] the uniforms each neuron drew, in order */
+    uint32_t *nUniform;  /* [nV1] how many */
+    float *normals;      /* [nV1][normalCap] failure draws of the near delivery before the first step */
+    uint32_t *nNormal;   /* [nV1] how many (more than normalCap: PV1_E_DEVICE) */
+    uint32_t normalCap;
+    float *history;      /* [trainDepth][nV1] spike-word ring after rand_spInit (slot 0: initial spikes) */
+} pv1_init_record;
+
+/* rand_spInit with initial spikes (src/coredynamics.cu:5-146, launched at src/patch.cu:4580)
+ * and the delivery that the reference runs once before its step loop when some spE0/spI0 > 0
+ * (src/patch.cu:5687-5888): replaces pv1_v1_init_rng.  sp0 [nType][2] holds the per-step
+ * spike chances (spE0 then spI0 of the cfg, each times dt/1000: [t][0] for neurons with more
+ * than SCsplit LGN synapses, [t][1] for the rest).  Changes v, w, tBack and the E/I
+ * conductances set by pv1_v1_set_state, so call it after that and after every connectivity
+ * call (pv1_v1_set_near / _near_delayed / _far), before the first step.  Quirks of the
+ * reference that are kept: the initial spike words themselves are never delivered (the first
+ * step overwrites their ring slot); the delivery before the loop takes the history slot
+ * trainDepth-1 as the previous step's spikes and, with noDelay = 1, reads the initial
+ * spikers' compacted output_g/h table at per-neuron offsets (recal_G_mat_nd,
+ * src/coredynamics.cu:2497-2510, after rand_spInit wrote it at :85-116); with noDelay = 0 it
+ * reads the ring with slot 0 as the newest (src/patch.cu:5760-5770) while the loop takes slot
+ * trainDepth-1 as the step before the first.  The reference numbers the initial spikers of a
+ * block in the order of its atomicAdd_block returns; this build numbers them by thread index.
+ * rec may be NULL. */
+int pv1_v1_init_spikes(pv1_plan *plan, uint64_t seed, uint32_t trainDepth, const float *sp0,
+                       uint32_t SCsplit, pv1_init_record *rec);
+
 /* Host initial-state generator of src/patch.cu:4405-4560 (libstdc++ default_random_engine
  * and normal/uniform distributions, same call order).  v0/w0/g0 arrays as in the cfg:
  * v0 [nType][2], w0 [nType][2], gFF0 [nType][ngFF][4], gE0 [nType][ngE][4],

@@ -76,6 +76,7 @@ def lib():
         L.orc_adex_spike.argtypes = [F] * 5 + [FP, FP]
         L.orc_logistic_ab.argtypes = [FP, FP, FP, C.c_int, FP, FP]
         L.orc_v1_deliver_near_delayed.argtypes = [P]
+        L.orc_v1_init_spikes.argtypes = [P, FP, C.c_uint32, C.c_int, FP, UP, C.c_uint32, FP, UP, C.c_uint32, FP]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_num_threads.restype = C.c_int
         _lib = L
@@ -255,6 +256,24 @@ class V1Oracle:
             self.put(name, getattr(init, name))
         if init.w is not None:
             self.put("w", init.w)
+
+    def init_spikes(self, sp0, SCsplit, depth, rec):
+        """rand_spInit with initial spikes and the delivery before the first step, from the
+        device's recorded draws (`rec`: the dict Simulation keeps from pv1_v1_init_spikes).
+        Returns (draw-count mismatches, spike-word history [depth][nV1])."""
+        L = lib()
+        if self.delayed:
+            L.orc_v1_set_delays(self.h, fp(self._keep[-1]), int(depth))
+        u = np.ascontiguousarray(rec["uniforms"], f32)
+        nu = np.ascontiguousarray(rec["nUniform"], np.uint32)
+        z = np.ascontiguousarray(rec["normals"], f32)
+        nz = np.ascontiguousarray(rec["nNormal"], np.uint32)
+        H = np.empty((depth, self.spec.nV1), f32)
+        m = L.orc_v1_init_spikes(self.h, fp(np.ascontiguousarray(sp0, f32)), int(SCsplit), int(depth), fp(u), up(nu),
+                                 u.shape[1], fp(z), up(nz), z.shape[1], fp(H))
+        if m < 0:
+            raise RuntimeError("orc_v1_init_spikes: the delay ring is not set up")
+        return m, H
 
     def step(self, lgn_sInfo, noise=None, ff=None, near=None, cap=0):
         L = lib()

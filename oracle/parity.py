@@ -61,7 +61,11 @@ def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None
 
     close = sim is None
     if sim is None:
-        sim = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+        sim = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds,
+                         record_init=4 * cap if wl.seeds.has_sp0() else 0)
+    init_rec = sim.init_record
+    if wl.seeds.has_sp0() and init_rec is None:
+        raise ValueError("initial spikes: the Simulation must be made with record_init > 0")
     try:
         gpu_tables = sim.lgn_tables()
         gpu_S = sim.lgn_spatial()
@@ -98,12 +102,16 @@ def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None
     lo.ltr[:] = ltr0
     vo = V1Oracle(wl.spec, wl.net)
     vo.set_state(wl.init)
+    mism = 0
+    o_hist = None
+    if wl.seeds.has_sp0():
+        m0, o_hist = vo.init_spikes(wl.seeds.sp0, wl.seeds.SCsplit, wl.seeds.trainDepth, init_rec)
+        mism += m0
     nV1 = wl.spec.nV1
     o_raw = np.zeros_like(raw)
     o_lsp = np.zeros_like(lsp)
     o_lfr = np.zeros_like(lfr)
     lay = record_layout(wl.spec)
-    mism = 0
     for it in range(nsteps):
         conv = lo.convol(it)
         s, fr, m = lo.nonlinear(conv, np.ascontiguousarray(U[it]), np.ascontiguousarray(Uc[it]), cap)
@@ -123,8 +131,10 @@ def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None
                 r[lay[k]:lay[k] + a.size] = a
     o_final = {k: vo.get(k) for k in ("v", "gE", "gI", "gFF", "tBack")}
     vo.close()
-    return dict(gpu=dict(raw=raw, lsp=lsp, lfr=lfr, tables=gpu_tables, S=gpu_S, final=final),
-                ora=dict(raw=o_raw, lsp=o_lsp, lfr=o_lfr, tables=ora_tables, S=ora_S, final=o_final),
+    return dict(gpu=dict(raw=raw, lsp=lsp, lfr=lfr, tables=gpu_tables, S=gpu_S, final=final,
+                         history=None if init_rec is None else init_rec["history"]),
+                ora=dict(raw=o_raw, lsp=o_lsp, lfr=o_lfr, tables=ora_tables, S=ora_S, final=o_final,
+                         history=o_hist),
                 draw_count_mismatch=mism, launches=launches)
 
 

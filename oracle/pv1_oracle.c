@@ -1294,6 +1294,162 @@ int orc_v1_deliver_far(orc_v1 *o) {
     return 0;
 }
 
+/* rand_spInit with initial spikes (src/coredynamics.cu:5-146) and the delivery before the
+ * step loop (src/patch.cu:5687-5888), consuming the uniforms u [nV1][capU] (nu [nV1] of them
+ * each) and the near failure normals z [nV1][capZ] the device drew.  The initial spikers of a
+ * block are numbered by thread index (the device's order).  Writes the spike-word history
+ * [depth][nV1] to H (may be NULL); returns the number of neurons whose draw counts differ. */
+int orc_v1_init_spikes(orc_v1 *o, const float *sp0, uint32_t SCsplit, int depth, const float *u,
+                       const uint32_t *nu, uint32_t capU, const float *z, const uint32_t *nz,
+                       uint32_t capZ, float *Hout) {
+    const pv1_v1_config *c = &o->c;
+    const int nV1 = o->nV1, bs = o->bs, nE = o->nE, nI = o->nI;
+    const float dt = c->dt;
+    int has = 0, mism = 0;
+    for (uint32_t q = 0; q < 2 * c->nType; q++) if (sp0[q] > 0) has = 1;
+    float *H = (float *)calloc((size_t)depth * nV1, sizeof(float));
+    for (int id = 0; id < nV1; id++) {
+        const int itype = otype(o, id % bs);
+        const float *ui = u + (size_t)id * capU;
+        uint32_t k = 0;
+#define ODRAW() (k < nu[id] && k < capU ? ui[k++] : (k++, 2.0f))
+        const float r0 = ODRAW();
+        const float chance = sp0[itype * 2 + (o->nLGN[id] > SCsplit ? 0 : 1)];
+        const float tRef = c->tRef[itype];
+        float v = o->v[id], ref = 0.f, sInfo = v;
+        if (chance > 0 && r0 < chance) {
+            const float tsp = ODRAW();
+            sInfo = 1.0f + tsp;
+            const float tb = tRef - (1 - tsp) * dt;
+            if (tb > 0) o->tBack[id] = tb;
+            const float v0 = c->vR[itype];
+            v = v0;
+            o->v[id] = v0;
+            if (c->iModel == 1) {
+                const float tw = c->tau_w[itype];
+                const float A = c->a[itype] * (v0 - c->vL) * tw;
+                const float w0 = o->w[id] + c->b[itype];
+                o->w[id] = (w0 - A) * expf(-dt * (1 - tsp) / tw) + A;
+            }
+            ref = (1 - tsp) * dt + tRef - dt;
+        }
+        H[id] = sInfo;
+        for (int q = depth - 1; q > 0; q--) {
+            float word;
+            if (ref < dt) {
+                if (ref < 0) ref = 0;
+                if (ODRAW() < chance * (dt - ref) / dt) {
+                    const float tsp = ODRAW() * (dt - ref) / dt;
+                    word = 1.0f + tsp;
+                    ref = tRef + (1 - tsp) * dt;
+                } else {
+                    word = v;
+                }
+            } else {
+                word = c->vR[itype];
+            }
+            H[(size_t)q * nV1 + id] = word;
+            ref -= dt;
+        }
+#undef ODRAW
+        if (k != nu[id]) mism++;
+    }
+    if (Hout) memcpy(Hout, H, (size_t)depth * nV1 * sizeof(float));
+    if (!has) {
+        free(H);
+        return mism;
+    }
+    const float *Hlast = H + (size_t)(depth - 1) * nV1;
+    if (c->noDelay) {
+        /* output_g/h of the initial spikers, compacted per block (rand_spInit :85-116) */
+        const size_t ncb = (size_t)nE * c->ngE + (size_t)nI * c->ngI;
+        float *og = (float *)calloc(ncb * o->nblock, sizeof(float));
+        float *oh = (float *)calloc(ncb * o->nblock, sizeof(float));
+        for (int b = 0; b < o->nblock; b++) {
+            int npE = 0, npI = 0;
+            for (int l = 0; l < bs; l++)
+                if (H[b * bs + l] >= 1) { if (l < nE) npE++; else npI++; }
+            int sE = 0, sI = 0;
+            for (int l = 0; l < bs; l++) {
+                const float w = H[b * bs + l];
+                if (!(w >= 1)) continue;
+                const float tsp = (w - 1) * dt;
+                const int isE = l < nE;
+                const int ng = isE ? (int)c->ngE : (int)c->ngI;
+                const int sid = isE ? sE++ : sI++;
+                for (int ig = 0; ig < ng; ig++) {
+                    float g = 0.f, h = 0.f;
+                    ocond_input(isE ? &o->cE : &o->cI, &g, &h, 1.f, dt - tsp, ig);
+                    const size_t r = isE ? (size_t)ig * npE + sid : (size_t)ig * npI + (size_t)npE * c->ngE + sid;
+                    og[b * ncb + r] = g;
+                    oh[b * ncb + r] = h;
+                }
+            }
+        }
+        /* recal_G_mat_nd on the history slot depth-1 (:2366-2608) */
+        for (int ipost = 0; ipost < nV1; ipost++) {
+            const int b = ipost / bs, local = ipost % bs, itype = otype(o, local);
+            float lgE[PV1_MAX_NG] = {0, 0}, lhE[PV1_MAX_NG] = {0, 0}, lgI[PV1_MAX_NG] = {0, 0}, lhI[PV1_MAX_NG] = {0, 0};
+            uint32_t kz = 0;
+            for (uint32_t ib = 0; ib < o->nNearNB[b]; ib++) {
+                const int bid = (int)o->nbId[(size_t)b * o->nnb + ib];
+                const float *col = o->conMat + ((size_t)(b * o->nnb + ib) * bs) * bs + local;
+                for (int i = 0; i < bs; i++) {
+                    float strength = col[(size_t)i * bs];
+                    if (!(strength != 0 && Hlast[bid * bs + i] > 0)) continue;
+                    const int jtype = otype(o, i);
+                    const float p = c->synFail[jtype * c->nType + itype];
+                    if (p > 0) {
+                        const float nstd = sqrtf(p * (1 - p) / c->synPerCon[jtype * c->nType + itype]);
+                        const float rnd = (z && kz < nz[ipost] && kz < capZ) ? z[(size_t)ipost * capZ + kz] : 0.f;
+                        kz++;
+                        strength *= 1 - p + nstd * rnd;
+                    }
+                    if (strength > 0) {
+                        const int isE = i < nE;
+                        const size_t base = (size_t)bid * ncb + (isE ? (size_t)i * c->ngE : (size_t)nE * c->ngE + (size_t)(i - nE) * c->ngI);
+                        if (isE) {
+                            for (uint32_t ig = 0; ig < c->ngE; ig++) {
+                                const float str = strength * c->pE[itype * c->ngE + ig];
+                                lgE[ig] += str * og[base + ig];
+                                lhE[ig] += str * oh[base + ig];
+                            }
+                        } else {
+                            for (uint32_t ig = 0; ig < c->ngI; ig++) {
+                                const float str = strength * c->pI[itype * c->ngI + ig];
+                                lgI[ig] += str * og[base + ig];
+                                lhI[ig] += str * oh[base + ig];
+                            }
+                        }
+                    }
+                }
+            }
+            if (nz && kz != nz[ipost]) mism++;
+            for (uint32_t ig = 0; ig < c->ngE; ig++) { o->gE[ig * nV1 + ipost] += lgE[ig]; o->hE[ig * nV1 + ipost] += lhE[ig]; }
+            for (uint32_t ig = 0; ig < c->ngI; ig++) { o->gI[ig * nV1 + ipost] += lgI[ig]; o->hI[ig * nV1 + ipost] += lhI[ig]; }
+        }
+        free(og);
+        free(oh);
+    } else {
+        /* recal_G_mat with the ring's current slot 0 (src/patch.cu:5760-5770); the loop then
+         * starts again at slot 0 */
+        if (!o->spikeRing || o->trainDepth != depth) {
+            free(H);
+            return -1;
+        }
+        memcpy(o->spikeRing, H, (size_t)depth * nV1 * sizeof(float));
+        memcpy(o->sInfo, H, (size_t)nV1 * sizeof(float));
+        o->curSlot = 0;
+        orc_v1_deliver_near_delayed(o);
+        o->curSlot = 0;
+    }
+    /* far: fill_fSpikeTrain with the history slot depth-1, recal_G_vec + sum_G */
+    memcpy(o->sInfo, Hlast, (size_t)nV1 * sizeof(float));
+    orc_v1_deliver_far(o);
+    free(H);
+    return mism;
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

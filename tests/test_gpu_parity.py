@@ -466,3 +466,68 @@ def test_curved_retina_dynamics_parity(curved_wl):
     assert cmp["lgn_spike_mismatch"] == 0, cmp
     assert cmp["lgn_fr_maxrel"] < 1e-5, cmp
     assert_raster_ok(cmp)
+
+
+def _sp0_workload(kind, seed):
+    """Initial spikes at high rates (chances 0.12-0.37 per step) so that the history, the
+    compacted output_g/h table and the delivery before the first step all carry many spikes."""
+    from visual_cortex_gb300 import synth
+    rates = dict(spE0=[2000.0, 1000.0], spI0=[3000.0, 1500.0])
+    if kind == "near_failure":     # one block, near synapses with failure draws
+        return synth.config1(seed=seed, synFail=(0.1, 0.1, 0.1, 0.1), **rates)
+    if kind == "far":
+        return synth.make_workload("sp0far", seed=seed, nblock=4, n_lgn=1024, m=20, width=64, height=64,
+                                   nt=800, far_partners=100, adex_inh=True, patch_deg=2.0, nFrame=120,
+                                   wFar=0.01, **rates)
+    return synth.make_workload("sp0delayed", seed=seed, nblock=2, n_lgn=512, m=20, width=64, height=64,
+                               nt=800, far_partners=50, adex_inh=True, nFrame=60, noDelay=0, **rates)
+
+
+@pytest.mark.parametrize("kind", ["near_failure", "far", "delayed"])
+def test_initial_spikes_state(native, kind):
+    """rand_spInit with initial spikes and the delivery before the first step: the device's
+    state after pv1_v1_init_spikes vs the oracle's restatement fed the same draws."""
+    import oracle
+    from visual_cortex_gb300.model import Simulation
+    wl = _sp0_workload(kind, 40 + len(kind))
+    assert wl.seeds.has_sp0()
+    sim = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds, record_init=64)
+    try:
+        rec = sim.init_record
+        st = {k: sim.state(k) for k in ("v", "w", "tBack", "gE", "hE", "gI", "hI")}
+    finally:
+        sim.close()
+    vo = oracle.V1Oracle(wl.spec, wl.net)
+    try:
+        vo.set_state(wl.init)
+        mism, H = vo.init_spikes(wl.seeds.sp0, wl.seeds.SCsplit, wl.seeds.trainDepth, rec)
+        ora = {k: vo.get(k) for k in st}
+    finally:
+        vo.close()
+    assert mism == 0
+    np.testing.assert_array_equal(rec["history"], H)
+    assert (H[0] >= 1).mean() > 0.05 and (H[-1] >= 1).sum() > 0
+    if kind == "near_failure":
+        assert rec["nNormal"].sum() > 0
+    np.testing.assert_array_equal(st["v"], ora["v"])
+    np.testing.assert_array_equal(st["tBack"], ora["tBack"])
+    np.testing.assert_allclose(st["w"], ora["w"], rtol=1e-6, atol=1e-6)
+    for k in ("gE", "hE", "gI", "hI"):
+        np.testing.assert_allclose(st[k], ora[k], rtol=1e-5, atol=1e-7, err_msg=k)
+    assert not np.allclose(st["gE"], wl.init.gE)    # the delivery before the loop added input
+
+
+@pytest.mark.parametrize("kind", ["far", "delayed"])
+def test_initial_spikes_dynamics_parity(native, kind):
+    """From initial spikes on: far rings holding the history's later arrivals, delayed near
+    events of the history slots, then the ordinary steps."""
+    from oracle.parity import run_parity, compare
+    wl = _sp0_workload(kind, 50 + len(kind))
+    res = run_parity(wl, RASTER_STEPS, cap=8)
+    cmp = compare(res, wl.spec)
+    assert res["draw_count_mismatch"] == 0
+    np.testing.assert_array_equal(res["gpu"]["history"], res["ora"]["history"])
+    assert cmp["v1_spikes_gpu"] > 0, cmp
+    assert_raster_ok(cmp)
+    for k in ("v", "gE", "gI"):
+        assert cmp[f"max_rel_{k}"] < 1e-5, cmp

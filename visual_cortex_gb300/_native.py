@@ -77,6 +77,11 @@ class LgnParams(C.Structure):
                [("coneType", _UP)]
 
 
+class InitRecord(C.Structure):
+    _fields_ = [("uniforms", _FP), ("nUniform", _UP), ("normals", _FP), ("nNormal", _UP),
+                ("normalCap", C.c_uint32), ("history", _FP)]
+
+
 def _load() -> C.CDLL:
     import os
     from .build import build_native
@@ -114,6 +119,7 @@ def _load() -> C.CDLL:
         "pv1_v1_set_near_delayed": ([P, C.c_uint32, _UP, _UP, _FP, _FP], C.c_int),
         "pv1_v1_set_state": ([P, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP], C.c_int),
         "pv1_v1_init_rng": ([P, C.c_uint64, C.c_uint32], C.c_int),
+        "pv1_v1_init_spikes": ([P, C.c_uint64, C.c_uint32, _FP, C.c_uint32, C.POINTER(InitRecord)], C.c_int),
         "pv1_host_init_state": ([C.POINTER(V1Config), C.c_uint64, _FP, _UP, C.c_int, C.c_float,
                                  _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP],
                                 C.c_int),

@@ -265,6 +265,17 @@ cudaError_t launch_v1_step(const V1Params &p, const long long *stepBase, int ste
                            cudaStream_t st);
 cudaError_t launch_v1_rng_init(curandStateMRG32k3a *cond, curandStateMRG32k3a *noisy,
                                unsigned long long seed, int nV1, int trainDepth, cudaStream_t st);
+// Initial spikes: per-step spike chance of each type, [type][0] for neurons with more than
+// SCsplit LGN synapses and [type][1] for the rest.
+struct Sp0 { float c[2 * kMaxType]; };
+// rand_spInit with initial spikes (ogTab/ohTab may be null: no output_g/h table).
+cudaError_t launch_v1_sp_init(const V1Params &p, unsigned long long seed, int depth, const Sp0 &sp0, int SCsplit,
+                              float *H, float *ogTab, float *ohTab, float *recU, unsigned *recNU, cudaStream_t st);
+// The near delivery before the first step (noDelay = 1).
+cudaError_t launch_v1_sp_near(const V1Params &p, const float *Hlast, const float *ogTab, const float *ohTab,
+                              float *recZ, unsigned *recNZ, int cap, cudaStream_t st);
+// The delayed events of the history and the delivery of those arriving before the first step.
+cudaError_t launch_v1_sp_events(const V1Params &p, const float *H, int depth, cudaStream_t st);
 int v1_persistent_ctas(const V1Params &p, int device, bool *fits);
 // Evaluates the full-step decay factors of the three conductance kernels on the device and
 // stores them into p (synchronous).

@@ -1235,6 +1235,73 @@ int pv1_v1_init_rng(pv1_plan *p, uint64_t seed, uint32_t trainDepth) {
     return PV1_OK;
 }
 
+int pv1_v1_init_spikes(pv1_plan *p, uint64_t seed, uint32_t trainDepth, const float *sp0, uint32_t SCsplit,
+                       pv1_init_record *rec) {
+    if (!p || trainDepth < 1 || !sp0) return PV1_E_ARG;
+    const pv1_v1_config &c = p->cfg;
+    if (!p->haveState || !p->haveNear) return fail(p, PV1_E_STATE, "set the state and the connectivity first");
+    if (p->step != 0) return fail(p, PV1_E_STATE, "initial spikes are set before the first step");
+    if (c.blockSize > 1024) return fail(p, PV1_E_UNSUPPORTED, "initial spikes need blockSize <= 1024");
+    Sp0 s0{};
+    bool has = false;
+    for (uint32_t q = 0; q < 2 * c.nType; q++) {
+        if (!(sp0[q] >= 0 && sp0[q] <= 1)) return fail(p, PV1_E_ARG, "sp0 holds per-step chances in [0, 1]");
+        s0.c[q] = sp0[q];
+        has = has || sp0[q] > 0;
+    }
+    const V1Params &vp = p->vp;
+    const size_t n = p->nV1;
+    const int depth = (int)trainDepth;
+    const bool nearNd = has && c.noDelay;
+    const size_t ncb = (size_t)p->nE * c.ngE + (size_t)p->nI * c.ngI;
+    const uint32_t cap = rec && rec->normals ? rec->normalCap : 0;
+    float *dH = nullptr, *dOg = nullptr, *dOh = nullptr, *dU = nullptr, *dZ = nullptr;
+    unsigned *dNU = nullptr, *dNZ = nullptr;
+    int r = dev_alloc(p, &dH, (size_t)depth * n);
+    if (!r && nearNd) r = dev_alloc(p, &dOg, ncb * c.nblock);
+    if (!r && nearNd) r = dev_alloc(p, &dOh, ncb * c.nblock);
+    if (!r && rec && rec->uniforms) r = dev_alloc(p, &dU, (size_t)2 * depth * n);
+    if (!r && rec && rec->nUniform) r = dev_alloc(p, &dNU, n);
+    if (!r && cap) r = dev_alloc(p, &dZ, (size_t)cap * n);
+    if (!r && rec && rec->nNormal) r = dev_alloc(p, &dNZ, n);
+    auto cleanup = [&]() {
+        for (void *q : {(void *)dH, (void *)dOg, (void *)dOh, (void *)dU, (void *)dZ, (void *)dNU, (void *)dNZ})
+            if (q) free_one(p, q);
+    };
+    if (r) {
+        cleanup();
+        return r;
+    }
+    cudaError_t e = launch_v1_sp_init(vp, (unsigned long long)seed, depth, s0, (int)SCsplit, dH, dOg, dOh, dU, dNU,
+                                      p->stream);
+    if (e == cudaSuccess && nearNd)
+        e = launch_v1_sp_near(vp, dH + (size_t)(depth - 1) * n, dOg, dOh, dZ, dNZ, (int)cap, p->stream);
+    if (e == cudaSuccess && has && vp.farOn) {
+        e = cudaMemsetAsync(vp.farFlag, 0, 3 * sizeof(int), p->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(vp.farCount, 0, 3 * sizeof(int), p->stream);
+        if (e == cudaSuccess) e = launch_v1_sp_events(vp, dH, depth, p->stream);
+    }
+    auto down = [&](void *dst, const void *src, size_t bytes) {
+        if (e == cudaSuccess && dst && src) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, p->stream);
+    };
+    if (rec) {
+        down(rec->uniforms, dU, (size_t)2 * depth * n * sizeof(float));
+        down(rec->nUniform, dNU, n * sizeof(unsigned));
+        down(rec->normals, dZ, (size_t)cap * n * sizeof(float));
+        down(rec->history, dH, (size_t)depth * n * sizeof(float));
+        if (rec->nNormal) {
+            if (dNZ) down(rec->nNormal, dNZ, n * sizeof(unsigned));
+            else memset(rec->nNormal, 0, n * sizeof(uint32_t));
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    cleanup();
+    if (e != cudaSuccess) return fail(p, PV1_E_CUDA, cudaGetErrorString(e));
+    p->haveRng = true;
+    drop_graph(p);
+    return check_device_error(p);
+}
+
 int pv1_set_record(pv1_plan *p, int flags, uint32_t slots) {
     if (!p) return PV1_E_ARG;
     if (!p->lgnReady) return fail(p, PV1_E_STATE, "call pv1_lgn_setup first");

@@ -947,7 +947,10 @@ __device__ __forceinline__ void far_event(const V1Params &P, long long t, int pr
     const int ng = preE ? P.ngE : P.ngI;
     const int qoff = preE ? 0 : P.ngE;
     const float delta = __fsub_rn(dt, dtsp);
-    unsigned long long *acc = (nearClass ? P.nearAcc : P.farAcc) + (size_t)(tArr % P.farDepth) * ns * 2 * nV1;
+    // tArr >= -1: the only arrival before step 0 is the delivery that precedes the first step
+    // when there are initial spikes (step -1, ring slot farDepth - 1)
+    unsigned long long *acc =
+        (nearClass ? P.nearAcc : P.farAcc) + (size_t)((tArr + P.farDepth) % P.farDepth) * ns * 2 * nV1;
 #pragma unroll
     for (int ig = 0; ig < kMaxNG; ig++) {
         if (ig < ng) {
@@ -1294,6 +1297,269 @@ __global__ void v1_rng_init_kernel(curandStateMRG32k3a *cond, curandStateMRG32k3
     noisy[id] = b;
 }
 
+// ---- initial spikes (spE0/spI0 > 0) ----
+// rand_spInit (src/coredynamics.cu:5-146) with initial spikes, one CTA per block of neurons:
+// neuron id spikes with chance sp0[type][nLGN > SCsplit ? 0 : 1] at a uniform time tsp of the
+// step before the first (v = vR, tBack and the AdEx w advanced over the rest of that step),
+// then the history slots depth-1 .. 1 of the spike-word ring are filled with spikes of the
+// same chance outside the refractory period.  H [depth][nV1] receives the spike words (slot 0:
+// the initial ones).  ogTab/ohTab [nblock][nE*ngE + nI*ngI] receive output_g/h of the initial
+// spikers as the reference writes them for the step's compacted spiker list (E then I, each
+// numbered within its block); the reference numbers them in the order its atomicAdd_block
+// calls return, which the hardware does not fix, and this kernel numbers them by thread index.
+__global__ void __launch_bounds__(1024) v1_sp_init_kernel(V1Params P, unsigned long long seed, int depth, Sp0 sp0,
+                                                          int SCsplit, float *H, float *ogTab, float *ohTab,
+                                                          float *recU, unsigned *recNU) {
+    __shared__ int sCnt[2][32];
+    const int bs = P.blockSize, nV1 = P.nV1;
+    const int b = blockIdx.x, local = threadIdx.x;
+    const bool active = local < bs;
+    const int id = b * bs + (active ? local : 0);
+    const int itype = type_of(P, active ? local : 0);
+    const float dt = P.dt;
+    float sInfo = -1.f;
+    if (active) {
+        curandStateMRG32k3a a, nz;
+        curand_init(seed, id, 0, &a);
+        curand_init(seed, (unsigned long long)nV1 + id, 0, &nz);
+        float *ru = recU ? recU + (size_t)id * 2 * depth : nullptr;
+        int nu = 0;
+        auto draw = [&]() {
+            const float u = curand_uniform(&a);
+            if (ru) ru[nu] = u;
+            nu++;
+            return u;
+        };
+        const float r0 = draw();
+        const float chance = sp0.c[itype * 2 + (P.nLGNperV1[id] > SCsplit ? 0 : 1)];
+        const float tRef = P.tRef[itype];
+        float v = P.v[id];
+        float ref = 0.f;
+        sInfo = v;
+        if (chance > 0 && r0 < chance) {
+            const float tsp = draw();
+            sInfo = 1.0f + tsp;
+            const float tb = tRef - (1 - tsp) * dt;
+            if (tb > 0) P.tBack[id] = tb;
+            const float v0 = P.vR[itype];
+            v = v0;
+            P.v[id] = v0;
+            if (P.iModel == 1) {
+                const float tw = P.tau_w[itype];
+                const float A = P.a[itype] * (v0 - P.vL) * tw;
+                const float w0 = P.w[id] + P.b[itype];
+                P.w[id] = (w0 - A) * expf(-dt * (1 - tsp) / tw) + A;
+            }
+            ref = (1 - tsp) * dt + tRef - dt;
+        }
+        H[id] = sInfo;
+        for (int q = depth - 1; q > 0; q--) {
+            float word;
+            if (ref < dt) {
+                if (ref < 0) ref = 0;
+                if (draw() < chance * (dt - ref) / dt) {
+                    const float tsp = draw() * (dt - ref) / dt;
+                    word = 1.0f + tsp;
+                    ref = tRef + (1 - tsp) * dt;
+                } else {
+                    word = v;
+                }
+            } else {
+                word = P.vR[itype];
+            }
+            H[(size_t)q * nV1 + id] = word;
+            ref -= dt;
+        }
+        P.rGenCond[id] = a;
+        P.rNoisy[id] = nz;
+        if (recNU) recNU[id] = (unsigned)nu;
+    }
+    if (!ogTab) return;
+    // block-wide numbering of the initial E and I spikers in thread order
+    const bool isE = local < P.nE;
+    const bool spk = active && sInfo >= 1.0f;
+    const int lane = local & 31, warp = local >> 5, nw = (blockDim.x + 31) >> 5;
+    const unsigned bE = __ballot_sync(0xffffffffu, spk && isE);
+    const unsigned bI = __ballot_sync(0xffffffffu, spk && !isE);
+    if (lane == 0) {
+        sCnt[0][warp] = __popc(bE);
+        sCnt[1][warp] = __popc(bI);
+    }
+    __syncthreads();
+    int before = 0, nE = 0, nI = 0;
+    for (int w2 = 0; w2 < nw; w2++) {
+        if (w2 < warp) before += isE ? sCnt[0][w2] : sCnt[1][w2];
+        nE += sCnt[0][w2];
+        nI += sCnt[1][w2];
+    }
+    if (!spk) return;
+    const int sid = before + __popc((isE ? bE : bI) & ((1u << lane) - 1u));
+    const size_t base = (size_t)b * (P.nE * P.ngE + P.nI * P.ngI);
+    const float tsp = (sInfo - 1) * dt;
+    const int ng = isE ? P.ngE : P.ngI;
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        if (ig < ng) {
+            float g = 0.f, h = 0.f;
+            if (isE) cond_input_v(P.condE.rise[ig], P.condE.decay[ig], P.condE.dod[ig], g, h, 1.f, dt - tsp);
+            else cond_input_v(P.condI.rise[ig], P.condI.decay[ig], P.condI.dod[ig], g, h, 1.f, dt - tsp);
+            const size_t r = isE ? (size_t)ig * nE + sid : (size_t)ig * nI + (size_t)nE * P.ngE + sid;
+            ogTab[base + r] = g;
+            ohTab[base + r] = h;
+        }
+    }
+}
+
+// The near delivery that runs once before the first step when there are initial spikes
+// (noDelay = 1): recal_G_mat_nd (src/coredynamics.cu:2366-2608) as src/patch.cu:5750-5758
+// launches it, on the history slot depth-1 of the spike-word ring, reading output_g/h at
+// the per-neuron offsets (block, E: i*ngE, I: nE*ngE + (i-nE)*ngI) of the table that
+// v1_sp_init_kernel wrote in the compacted layout; the sums are added to gE/hE/gI/hI.
+__global__ void __launch_bounds__(1024) v1_sp_near_kernel(V1Params P, const float *Hlast, const float *ogTab,
+                                                          const float *ohTab, float *recZ, unsigned *recNZ,
+                                                          int cap) {
+    const int bs = P.blockSize, nV1 = P.nV1;
+    const int b = blockIdx.x, local = threadIdx.x;
+    if (local >= bs) return;
+    const int ipost = b * bs + local;
+    const int itype = type_of(P, local);
+    const int ngE = P.ngE, ngI = P.ngI;
+    const int ncb = P.nE * ngE + P.nI * ngI;
+    float lgE[kMaxNG], lhE[kMaxNG], lgI[kMaxNG], lhI[kMaxNG], ipE[kMaxNG], ipI[kMaxNG];
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        lgE[ig] = lhE[ig] = lgI[ig] = lhI[ig] = 0.f;
+        ipE[ig] = ig < ngE ? P.pE[itype * ngE + ig] : 0.f;
+        ipI[ig] = ig < ngI ? P.pI[itype * ngI + ig] : 0.f;
+    }
+    curandStateMRG32k3a cs = P.rGenCond[ipost];
+    int nz = 0;
+    for (int ib = 0; ib < P.nNearNB[b]; ib++) {
+        const int bid = P.nbId[b * P.nnbMax + ib];
+        const float *col = P.conMat + ((size_t)(b * P.nnbMax + ib) * bs) * bs + local;
+        for (int i = 0; i < bs; i++) {
+            float strength = col[(size_t)i * bs];
+            if (!(strength != 0 && Hlast[(size_t)bid * bs + i] > 0)) continue;
+            const int jtype = type_of(P, i);
+            const float p = P.synFail[jtype * P.nType + itype];
+            if (p > 0) {
+                const float normed_std = sqrtf(p * (1 - p) / P.synPerCon[jtype * P.nType + itype]);
+                const float rnd = curand_normal(&cs);
+                if (recZ) {
+                    if (nz < cap) recZ[(size_t)ipost * cap + nz] = rnd;
+                    else atomicOr(P.err, kErrRecordOverflow);
+                }
+                nz++;
+                strength *= 1 - p + normed_std * rnd;
+            }
+            if (strength > 0) {
+                const bool isE = i < P.nE;
+                const size_t base = (size_t)bid * ncb + (isE ? (size_t)i * ngE : (size_t)P.nE * ngE + (size_t)(i - P.nE) * ngI);
+#pragma unroll
+                for (int ig = 0; ig < kMaxNG; ig++) {
+                    if (isE && ig < ngE) {
+                        const float str = strength * ipE[ig];
+                        lgE[ig] += str * ogTab[base + ig];
+                        lhE[ig] += str * ohTab[base + ig];
+                    }
+                    if (!isE && ig < ngI) {
+                        const float str = strength * ipI[ig];
+                        lgI[ig] += str * ogTab[base + ig];
+                        lhI[ig] += str * ohTab[base + ig];
+                    }
+                }
+            }
+        }
+    }
+    P.rGenCond[ipost] = cs;
+    if (recNZ) recNZ[ipost] = (unsigned)nz;
+#pragma unroll
+    for (int ig = 0; ig < kMaxNG; ig++) {
+        if (ig < ngE) { P.gE[(size_t)ig * nV1 + ipost] += lgE[ig]; P.hE[(size_t)ig * nV1 + ipost] += lhE[ig]; }
+        if (ig < ngI) { P.gI[(size_t)ig * nV1 + ipost] += lgI[ig]; P.hI[(size_t)ig * nV1 + ipost] += lhI[ig]; }
+    }
+}
+
+// Delayed events of the history, one thread per presynaptic neuron.  Far synapses
+// (fill_fSpikeTrain before the loop, src/patch.cu:5806-5846) see the history slot depth-1 as
+// step -1: its events arriving in step -1 go to ring slot farDepth-1 (delivered before the
+// first step), and the neuron joins step -1's far spiker list, from which step 0 pushes the
+// later arrivals.  Delayed near synapses (noDelay = 0) follow recal_G_mat's reads of the
+// ring: before the loop (current slot 0, src/patch.cu:5760-5770) slot 0 is step -1 and slot
+// s >= 1 step s-depth-1, and only arrivals in step -1 count; in the loop slot s is step
+// s-depth until it is overwritten, so slots 1 .. depth-2 push their arrivals in steps >= 0
+// here (slot depth-1's come from step -1's list as above).
+__global__ void v1_sp_push_kernel(V1Params P, const float *H, int depth) {
+    const int nV1 = P.nV1;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nV1) return;
+    const float sLast = H[(size_t)(depth - 1) * nV1 + i];
+    const int e0 = P.farOff[i], deg = P.farOff[i + 1] - e0;
+    if (sLast > 1.0f && P.farPre[i]) P.farFlag[2] = 1;
+    if (sLast >= 1.0f && deg > 0) {
+        const int pos = atomicAdd(P.farCount + 2, 1);
+        P.farList[(size_t)2 * nV1 + pos] = make_int4(i, e0, deg, __float_as_int(sLast));
+    }
+    for (int e = e0; e < e0 + deg; e++) {
+        const int post = P.farPost[e];
+        const float f = P.farStr[e];
+        const int sp = P.farSteps[e];
+        const float frac = P.farFrac[e];
+        const int steps = sp & 0xffff;
+        if (!((sp >> 24) & 1)) {
+            if (sLast >= 1.0f && steps <= 1) far_event(P, -1, i, sLast, post, f, steps, sp, frac, steps);
+            continue;
+        }
+        for (int q = 0; q < depth; q++) {
+            const float w = H[(size_t)q * nV1 + i];
+            if (w < 1.0f) continue;
+            const long long th = q == 0 ? -1 : (long long)q - depth - 1;
+            const long long k = th + steps + 1;
+            if (k == 0 || k == 1) far_event(P, th, i, w, post, f, steps, sp, frac, (int)k);
+        }
+        for (int q = 1; q < depth - 1; q++) {
+            const float w = H[(size_t)q * nV1 + i];
+            if (w < 1.0f) continue;
+            const long long th = (long long)q - depth;
+            for (int k = 0; k < 2; k++)
+                if (k <= steps && th + steps - k >= 0) far_event(P, th, i, w, post, f, steps, sp, frac, k);
+        }
+    }
+}
+
+// Adds ring slot farDepth-1 (arrivals in step -1) to the conductances and clears it: delayed
+// near events as recal_G_mat adds them, then the far events as sum_G does when some far
+// presynaptic neuron spiked in step -1 (src/patch.cu:5806-5846).
+__global__ void v1_sp_consume_kernel(V1Params P) {
+    const int nV1 = P.nV1;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nV1) return;
+    const int ngE = P.ngE, ns = P.ngE + P.ngI;
+    const size_t slot = (size_t)(P.farDepth - 1) * ns * 2 * nV1;
+    for (int pass = 0; pass < 2; pass++) {
+        unsigned long long *acc = pass == 0 ? (P.nearOn ? P.nearAcc : nullptr) : (P.farClass ? P.farAcc : nullptr);
+        if (!acc) continue;
+        const bool add = pass == 0 || P.farFlag[2] != 0;
+        acc += slot;
+        for (int q = 0; q < ns; q++) {
+            unsigned long long *pg = acc + (size_t)(2 * q) * nV1 + i;
+            unsigned long long *ph = acc + (size_t)(2 * q + 1) * nV1 + i;
+            const unsigned long long ug = *pg, uh = *ph;
+            *pg = 0ull;
+            *ph = 0ull;
+            if (!add) continue;
+            const float fg = far_from_fixed(ug), fh = far_from_fixed(uh);
+            if (q < ngE) {
+                P.gE[(size_t)q * nV1 + i] += fg;
+                P.hE[(size_t)q * nV1 + i] += fh;
+            } else {
+                P.gI[(size_t)(q - ngE) * nV1 + i] += fg;
+                P.hI[(size_t)(q - ngE) * nV1 + i] += fh;
+            }
+        }
+    }
+}
+
 __global__ void advance_step_kernel(long long *stepBase, int k) { *stepBase += k; }
 
 // Full-step decay factors, evaluated with the same expressions as cond_decay (one thread).
@@ -1383,6 +1649,29 @@ cudaError_t launch_v1_persistent(const V1Params &p, const long long *stepBase, i
 cudaError_t launch_v1_rng_init(curandStateMRG32k3a *cond, curandStateMRG32k3a *noisy,
                                unsigned long long seed, int nV1, int trainDepth, cudaStream_t st) {
     v1_rng_init_kernel<<<(nV1 + 127) / 128, 128, 0, st>>>(cond, noisy, seed, nV1, trainDepth);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_v1_sp_init(const V1Params &p, unsigned long long seed, int depth, const Sp0 &sp0, int SCsplit,
+                              float *H, float *ogTab, float *ohTab, float *recU, unsigned *recNU, cudaStream_t st) {
+    const int threads = (p.blockSize + 31) / 32 * 32;
+    v1_sp_init_kernel<<<p.nblock, threads, 0, st>>>(p, seed, depth, sp0, SCsplit, H, ogTab, ohTab, recU, recNU);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_v1_sp_near(const V1Params &p, const float *Hlast, const float *ogTab, const float *ohTab,
+                              float *recZ, unsigned *recNZ, int cap, cudaStream_t st) {
+    const int threads = (p.blockSize + 31) / 32 * 32;
+    v1_sp_near_kernel<<<p.nblock, threads, 0, st>>>(p, Hlast, ogTab, ohTab, recZ, recNZ, cap);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_v1_sp_events(const V1Params &p, const float *H, int depth, cudaStream_t st) {
+    const int n = (p.nV1 + 255) / 256;
+    v1_sp_push_kernel<<<n, 256, 0, st>>>(p, H, depth);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    v1_sp_consume_kernel<<<n, 256, 0, st>>>(p);
     return cudaGetLastError();
 }
 

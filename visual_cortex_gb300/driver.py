@@ -84,6 +84,22 @@ def _check_supported(c: Config):
         raise ConfigError("not supported by this build: " + "; ".join(bad))
 
 
+def _sp0(c: Config, nTypeE: int, nTypeI: int):
+    """Initial spike chances per step [type][2] from spE0/spI0 (Hz), src/patch.cu:810-837;
+    None when every one is 0."""
+    from .synth import sp0_chances
+    rates = []
+    for key, nt in (("spE0", nTypeE), ("spI0", nTypeI)):
+        v = getattr(c, key)
+        if v is None:
+            v = [0.0] * (2 * nt)
+        elif len(v) != 2 * nt:
+            raise ConfigError(f"the size of {key} has size of {len(v)} != {nt}x 2")
+        rates += list(v)
+    sp0 = sp0_chances(rates, c.dt)
+    return tuple(sp0) if any(x > 0 for x in sp0) else None
+
+
 def _max_near_distance(conMat, delayMat, nblock, nChunk):
     """maxDistance of src/patch.cu:3808-3812: findDisConMax over each chunk of blocks, always
     over the first remainChunkSize blocks' worth of elements of the chunk (the loop keeps the
@@ -264,7 +280,8 @@ def build(c: Config) -> Model:
     v0 = _exact(c, "v0", nType * 2) if c.use_v0 else None
     init = host_init_state(spec, s_init, iTonic, nL, v0, w0, gFF0, gE0, gI0, use_v0=c.use_v0,
                            tonicMax=float(iTonic.max()))
-    seeds = Seeds(lgn=s_lgn, cond=s_sp, trainDepth=max(trainDepth, 1))
+    seeds = Seeds(lgn=s_lgn, cond=s_sp, trainDepth=max(trainDepth, 1), sp0=_sp0(c, nTypeE, nTypeI),
+                  SCsplit=int(c.SCsplit))
     extra = dict(nType=nType, nTypeE=nTypeE, nTypeI=nTypeI, typeAcc=typeAcc, nLGN=nLGN,
                  normViewDistance=geo["normViewDistance"], stimulus_filename=P.stimulus, sRatioV1=sRatioV1,
                  sRatioLGN=sRatioLGN, tonicDep=tonicDep, noisyDep=noisyDep, vR=vR,

@@ -276,13 +276,20 @@ class Seeds:
     lgn: int          # logRand_init seed
     cond: int         # rand_spInit seed
     trainDepth: int = 2
+    sp0: tuple | None = None   # initial spikes: per-step chance [nType][2] (spE0, spI0 x dt/1000)
+    SCsplit: int = 0
+
+    def has_sp0(self) -> bool:
+        return self.sp0 is not None and any(float(x) > 0 for x in np.ravel(self.sp0))
 
 
 class Simulation:
     """One patch on the current GPU: owns a native plan."""
 
     def __init__(self, spec: V1Spec, net: V1Network, lgn: LgnSpec, stim: Stimulus,
-                 init: InitState, seeds: Seeds):
+                 init: InitState, seeds: Seeds, record_init: int = 0):
+        """record_init > 0 keeps what pv1_v1_init_spikes drew (init_record) with room for that
+        many near failure draws per neuron."""
         self.spec, self.net, self.lgn, self.stim = spec, net, lgn, stim
         self._cfg = spec.to_struct()
         plan = C.c_void_p()
@@ -305,8 +312,29 @@ class Simulation:
         N.check(plan, N.lib.pv1_stimulus_load(plan, nF, h, w, N.fptr(init3), N.fptr(fr)), "pv1_stimulus_load")
         self._set_network(net)
         self.put_initial_state(init)
-        N.check(plan, N.lib.pv1_v1_init_rng(plan, int(seeds.cond), int(seeds.trainDepth)), "pv1_v1_init_rng")
+        self.init_record = None
+        if seeds.has_sp0():
+            self._init_spikes(seeds, record_init)
+        else:
+            N.check(plan, N.lib.pv1_v1_init_rng(plan, int(seeds.cond), int(seeds.trainDepth)), "pv1_v1_init_rng")
         self.step = 0
+
+    def _init_spikes(self, seeds: Seeds, record_init: int):
+        sp0 = np.ascontiguousarray(np.ravel(seeds.sp0), dtype=f32)
+        if sp0.size != 2 * self.spec.nType:
+            raise ValueError("sp0 holds two chances per neuron type")
+        rec = None
+        if record_init:
+            n, d, cap = self.spec.nV1, int(seeds.trainDepth), int(record_init)
+            self.init_record = dict(uniforms=np.zeros((n, 2 * d), f32), nUniform=np.zeros(n, u32),
+                                    normals=np.zeros((n, cap), f32), nNormal=np.zeros(n, u32),
+                                    history=np.zeros((d, n), f32))
+            r = self.init_record
+            rec = N.InitRecord(N.fptr(r["uniforms"]), N.uptr(r["nUniform"]), N.fptr(r["normals"]),
+                               N.uptr(r["nNormal"]), cap, N.fptr(r["history"]))
+        N.check(self.plan, N.lib.pv1_v1_init_spikes(self.plan, int(seeds.cond), int(seeds.trainDepth), N.fptr(sp0),
+                                                    int(seeds.SCsplit), None if rec is None else C.byref(rec)),
+                "pv1_v1_init_spikes")
 
     def _set_network(self, net: V1Network):
         c = lambda a, t: np.ascontiguousarray(a, dtype=t)

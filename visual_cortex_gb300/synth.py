@@ -347,10 +347,13 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
                   mSample1D: int = 16, dt: float = 0.125, tjitter: float = 0.0,
                   noDelay: int = 1, n_parvo: int = 0, tau: float | None = None,
                   nKernelSample: int | None = None, blockSize: int = 1024, nE: int = 768,
-                  m_min: int | None = None, flat_retina: bool = True) -> Workload:
+                  m_min: int | None = None, flat_retina: bool = True, spE0=None, spI0=None,
+                  SCsplit: int = 0) -> Workload:
     """Builds one synthetic patch; C1 = 1x1024 V1 / 512 LGN; C2 = 32 blocks / 16384 LGN.
     noDelay = 0: near synapses are delivered after their distance delay (delayMat from the
-    neuron positions, mm, at speedOfThought 1 mm/ms)."""
+    neuron positions, mm, at speedOfThought 1 mm/ms).  spE0/spI0: initial spike rates in Hz
+    ([type][2] flattened, as in the cfg), converted to per-step chances as
+    src/patch.cu:810-837 does."""
     rng = np.random.default_rng(seed)
     spec = make_spec(nblock, blockSize=blockSize, nE=nE, adex_inh=adex_inh, noisyDep=noisyDep,
                      synFail=synFail, synFailFF=synFailFF, dt=dt)
@@ -393,9 +396,25 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
     init = host_init_state(spec, s_init, tonic, nLGNperV1, None, w0, gFF0, gE0, gI0)
     max_delay = float(delayVec.max()) if delayVec.size else 0.0
     trainDepth = int(math.ceil(max(max_delay, 0.0) / spec.speedOfThought / spec.dt)) + 1
-    seeds = Seeds(lgn=s_lgn, cond=s_sp, trainDepth=max(trainDepth, 2))
+    if delayMat is not None:   # the near spike-word ring (src/patch.cu:3808-3813)
+        conn = conMat != 0
+        maxd = float(delayMat[conn].max()) if conn.any() else 0.0
+        trainDepth = max(trainDepth, int(math.ceil(f32(f32(maxd) / f32(spec.speedOfThought)) / f32(spec.dt))) + 1)
+    sp0 = None
+    if spE0 is not None or spI0 is not None:
+        nTE, nTI = spec.nTypeE, spec.nType - spec.nTypeE
+        rates = list(spE0 if spE0 is not None else [0.0] * 2 * nTE) + list(spI0 if spI0 is not None else [0.0] * 2 * nTI)
+        sp0 = tuple(sp0_chances(rates, spec.dt))
+    seeds = Seeds(lgn=s_lgn, cond=s_sp, trainDepth=max(trainDepth, 2), sp0=sp0, SCsplit=SCsplit)
     return Workload(name=name, spec=spec, net=net, lgn=lgn, stim=stim, init=init, seeds=seeds,
                     nt=nt, pos=pos, rf_center=rfc, rf_orient=rfo)
+
+
+def sp0_chances(rates_hz, dt: float) -> list:
+    """Per-step initial spike chances: each float rate times dt/1000 evaluated in double and
+    stored as float (src/patch.cu:820, 834)."""
+    d = float(f32(dt)) / 1000.0
+    return [float(f32(float(f32(r)) * d)) for r in rates_hz]
 
 
 def config1(seed: int = 0, **kw) -> Workload:

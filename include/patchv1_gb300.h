@@ -195,9 +195,19 @@ int pv1_v1_set_near(pv1_plan *plan, uint32_t nearNeighborBlock, const uint32_t *
  * entries of (vecID, conVec, delayVec) stored back to back.  Strengths already carry
  * sRatioV1.  Builds the outgoing (by pre-neuron) event lists used on the device; replaces
  * the host loop recal_G_vec (src/coredynamics.cu:181-372) with fill_fSpikeTrain
- * (src/stats.cu:114-126) and sum_G (src/coredynamics.cu:2312-2349). */
+ * (src/stats.cu:114-126) and sum_G (src/coredynamics.cu:2312-2349).  With synaptic failure
+ * (some synFail > 0) the far synapses are instead kept by post in vec order and delivered by
+ * the failure path, which then needs pv1_v1_far_failure_engines. */
 int pv1_v1_set_far(pv1_plan *plan, const uint32_t *nVec, const uint32_t *vecID,
                    const float *conVec, const float *delayVec);
+
+/* Host engines of the far synaptic failure (plans with noFarDelay = 0, far synapses and some
+ * synFail > 0): engine i is default_random_engine seeded with seed + i (src/patch.cu:4224-4228,
+ * seed = the logRand_init seed + 1), and the far delivery runs per chunk of blocks (nChunk of
+ * the cfg, split as src/patch.cu:3430-3437), each chunk sharing one normal_distribution as
+ * recal_G_vec does (src/coredynamics.cu:181-372).  Call after pv1_v1_set_far; a no-op for
+ * plans without far failure. */
+int pv1_v1_far_failure_engines(pv1_plan *plan, uint64_t seed, uint32_t nChunk);
 
 /* Near-neighbour connectivity with distance delays, for plans with noDelay = 0: conMat as for
  * pv1_v1_set_near and delayMat of the same layout (distances in mm, src/patch.cu:3450-3460,
@@ -293,6 +303,8 @@ int pv1_fetch_records(pv1_plan *plan, uint64_t step0, uint32_t n, float *raw,
 #define PV1_ST_LGN_LTR 11 /* [nLGN] leftTimeRate  */
 #define PV1_ST_LGN_LNL 12 /* [nLGN] lastNegLogRand */
 #define PV1_ST_LGN_SINFO 13 /* [nLGN] last step's LGN spike word */
+#define PV1_ST_FAR_PULL 14  /* [ngE+ngI][2][nV1] far g, h sums of the last step (far synaptic
+                               failure plans; read only), added at the next step's delivery */
 /* Copies one state array to the host (waits for queued work). */
 int pv1_get_state(pv1_plan *plan, int which, float *out);
 /* Overwrites one state array (PV1_ST_* above). */

@@ -76,6 +76,8 @@ def lib():
         L.orc_adex_spike.argtypes = [F] * 5 + [FP, FP]
         L.orc_logistic_ab.argtypes = [FP, FP, FP, C.c_int, FP, FP]
         L.orc_v1_deliver_near_delayed.argtypes = [P]
+        L.orc_std_normal_draws.argtypes = [C.POINTER(C.c_uint64), C.c_int, IP, C.c_int, FP]
+        L.orc_v1_set_far_failure.argtypes = [P, C.c_uint64, C.c_int]
         L.orc_v1_init_spikes.argtypes = [P, FP, C.c_uint32, C.c_int, FP, UP, C.c_uint32, FP, UP, C.c_uint32, FP]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_num_threads.restype = C.c_int
@@ -256,6 +258,9 @@ class V1Oracle:
             self.put(name, getattr(init, name))
         if init.w is not None:
             self.put("w", init.w)
+
+    def set_far_failure(self, seed, nChunk):
+        lib().orc_v1_set_far_failure(self.h, int(seed), int(nChunk))
 
     def init_spikes(self, sp0, SCsplit, depth, rec):
         """rand_spInit with initial spikes and the delivery before the first step, from the

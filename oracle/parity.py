@@ -102,6 +102,7 @@ def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None
     lo.ltr[:] = ltr0
     vo = V1Oracle(wl.spec, wl.net)
     vo.set_state(wl.init)
+    vo.set_far_failure(wl.seeds.far_engine_seed, wl.seeds.nChunk)
     mism = 0
     o_hist = None
     if wl.seeds.has_sp0():

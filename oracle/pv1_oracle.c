@@ -594,6 +594,9 @@ typedef struct orc_v1 {
     const float *delayMat; /* borrowed, conMat layout */
     float *spikeRing;
     int trainDepth, curSlot;
+    /* far synaptic failure: libstdc++ minstd_rand0 states per post, chunks of blocks */
+    uint32_t *farEng;
+    int nChunk;
 } orc_v1;
 
 static int otype(const orc_v1 *o, int local) {
@@ -678,6 +681,7 @@ void orc_v1_destroy(orc_v1 *o) {
     free(o->nbId); free(o->nVec); free(o->vecOff); free(o->vecID); free(o->conVec);
     free(o->delayVec); free(o->ring); free(o->ringOff); free(o->depth); free(o->slot);
     free(o->spikeRing);
+    free(o->farEng);
     free(o);
 }
 
@@ -1230,14 +1234,132 @@ int orc_v1_deliver_near_delayed(orc_v1 *o) {
     return 0;
 }
 
+/* libstdc++'s <random> as the reference's host code uses it for far synaptic failure
+ * (src/coredynamics.cu:195, 319): default_random_engine is minstd_rand0 (Park-Miller,
+ * x <- 16807 x mod 2^31-1, seeded with s mod m, 0 -> 1); normal_distribution<float> draws
+ * uniforms through generate_canonical<float, 24> (one engine call: (x - 1) / 2^31 as float,
+ * clamped below 1) and uses the Marsaglia polar method, keeping the second value of each pair
+ * for its next call, whichever engine that call is given. */
+typedef struct { int avail; float saved; } onormal;
+
+static uint32_t ostd_seed(uint64_t s) {
+    const uint64_t x = s % 2147483647ull;
+    return x == 0 ? 1u : (uint32_t)x;
+}
+
+static uint32_t ostd_next(uint32_t *x) {
+    *x = (uint32_t)(((uint64_t)*x * 16807ull) % 2147483647ull);
+    return *x;
+}
+
+static float ostd_canonical(uint32_t *x) {
+    const float r = (float)(ostd_next(x) - 1u) / 2147483648.0f;
+    return r >= 1.0f ? nextafterf(1.0f, 0.0f) : r;
+}
+
+static float ostd_normal(onormal *d, uint32_t *x) {
+    if (d->avail) {
+        d->avail = 0;
+        return d->saved;
+    }
+    float a, b, r2;
+    do {
+        a = (float)((double)(2.0f * ostd_canonical(x)) - 1.0);
+        b = (float)((double)(2.0f * ostd_canonical(x)) - 1.0);
+        r2 = a * a + b * b;
+    } while (r2 > 1.0f || r2 == 0.0f);
+    const float mult = sqrtf(-2.0f * logf(r2) / r2);
+    d->saved = a * mult;
+    d->avail = 1;
+    return b * mult * 1.0f + 0.0f;
+}
+
+/* n draws from one shared normal_distribution<float>, draw q from engine who[q] (engines
+ * seeded with seeds[]); for checking the restatement against libstdc++ itself. */
+int orc_std_normal_draws(const uint64_t *seeds, int nEng, const int *who, int n, float *out) {
+    uint32_t *x = (uint32_t *)malloc((size_t)(nEng > 0 ? nEng : 1) * sizeof(uint32_t));
+    for (int q = 0; q < nEng; q++) x[q] = ostd_seed(seeds[q]);
+    onormal d = {0, 0.f};
+    for (int q = 0; q < n; q++) out[q] = ostd_normal(&d, &x[who[q]]);
+    free(x);
+    return 0;
+}
+
+/* Host engines of the far synaptic failure: engine i seeded with seed + i
+ * (src/patch.cu:4224-4228); the far delivery runs per chunk of blocks (nChunk as
+ * src/patch.cu:3430-3437 splits them), each with its own normal_distribution. */
+int orc_v1_set_far_failure(orc_v1 *o, uint64_t seed, int nChunk) {
+    free(o->farEng);
+    o->farEng = (uint32_t *)malloc((size_t)o->nV1 * sizeof(uint32_t));
+    for (int i = 0; i < o->nV1; i++) o->farEng[i] = ostd_seed(seed + (uint64_t)i);
+    o->nChunk = nChunk < 1 ? 1 : nChunk;
+    return 0;
+}
+
+/* recal_G_vec for post neuron i (src/coredynamics.cu:276-333): advance its synapses' ring
+ * slots and, when deliver, add the arrivals (sum_G); dist: the chunk's normal_distribution
+ * (used when some failure rate > 0). */
+static void ofar_post(orc_v1 *o, int i, int deliver, onormal *dist) {
+    const pv1_v1_config *c = &o->c;
+    const int nV1 = o->nV1, bs = o->bs;
+    const float dt = c->dt;
+    const int itype = otype(o, i % bs);
+    float lgE[PV1_MAX_NG] = {0, 0}, lhE[PV1_MAX_NG] = {0, 0}, lgI[PV1_MAX_NG] = {0, 0}, lhI[PV1_MAX_NG] = {0, 0};
+    for (size_t e = o->vecOff[i]; e < o->vecOff[i + 1]; e++) {
+        const uint32_t pre = o->vecID[e];
+        const int tid = (int)(pre % bs);
+        const float strength = o->conVec[e];
+        float time2post = o->delayVec[e] / c->speedOfThought;
+        const int preE = tid < o->nE;
+        const ocond *cd = preE ? &o->cE : &o->cI;
+        const int ng = preE ? (int)c->ngE : (int)c->ngI;
+        float *lg = preE ? lgE : lgI, *lh = preE ? lhE : lhI;
+        const int jtype = otype(o, tid);
+        const float p = c->synFail[jtype * c->nType + itype];
+        const float nSyn = c->synPerCon[jtype * c->nType + itype];
+        const unsigned it2post = (unsigned)ceilf(time2post / dt);
+        time2post = it2post * dt - time2post;
+        int k0 = (int)o->slot[e] - (int)it2post;
+        if (k0 < 0) k0 += (int)o->depth[e];
+        o->slot[e] = (o->slot[e] + 1) % o->depth[e];
+        if (!deliver || c->noFarDelay) continue;
+        for (int k = 0; k < 2; k++) {
+            float dtsp = o->ring[o->ringOff[e] + (size_t)((k0 + k) % (int)o->depth[e])];
+            if (dtsp >= 1.0f) {
+                const unsigned nsp = (unsigned)floorf(dtsp);
+                dtsp = (dtsp - nsp + k) * dt - time2post;
+                if (dtsp < dt && dtsp >= 0) {
+                    float f = strength;
+                    if (p > 0) {
+                        const float normed_std = sqrtf(p * (1 - p) / nSyn);
+                        const float rnd = ostd_normal(dist, &o->farEng[i]);
+                        f *= 1 - p + normed_std * rnd;
+                    }
+                    if (f > 0) {
+                        dtsp = dt - dtsp;
+                        for (int ig = 0; ig < ng; ig++) {
+                            const float ip = preE ? c->pE[itype * c->ngE + ig] : c->pI[itype * c->ngI + ig];
+                            ocond_input(cd, &lg[ig], &lh[ig], nsp * f * ip, dtsp, ig);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (deliver && o->vecOff[i + 1] > o->vecOff[i] && !c->noFarDelay) {
+        for (uint32_t ig = 0; ig < c->ngE; ig++) { o->gE[ig * nV1 + i] += lgE[ig]; o->hE[ig * nV1 + i] += lhE[ig]; }
+        for (uint32_t ig = 0; ig < c->ngI; ig++) { o->gI[ig * nV1 + i] += lgI[ig]; o->hI[ig * nV1 + i] += lhI[ig]; }
+    }
+}
+
 /* Far delivery: fill_fSpikeTrain, then recal_G_vec + sum_G when some far presynaptic neuron
  * spiked (sInfo > 1) this step, else only the ring slots advance (src/patch.cu:6596-6648).
- * noFarDelay = 1 reproduces the reference's empty loop (far input dropped). */
+ * noFarDelay = 1 reproduces the reference's empty loop (far input dropped).  With far
+ * synaptic failure each chunk's posts run in order, sharing the chunk's normal_distribution. */
 int orc_v1_deliver_far(orc_v1 *o) {
     if (!o->anyFar) return 0;
     const pv1_v1_config *c = &o->c;
     const int nV1 = o->nV1, bs = o->bs;
-    const float dt = c->dt;
     int farSpiked = 0;
     for (int i = 0; i < nV1; i++)
         for (size_t e = o->vecOff[i]; e < o->vecOff[i + 1]; e++) {
@@ -1249,47 +1371,22 @@ int orc_v1_deliver_far(orc_v1 *o) {
         for (size_t e = 0; e < o->nFar; e++) o->slot[e] = (o->slot[e] + 1) % o->depth[e];
         return 0;
     }
+    int fail = 0;
+    for (uint32_t q = 0; q < c->nType * c->nType; q++) if (c->synFail[q] > 0) fail = 1;
+    if (!fail || c->noFarDelay) {
 #pragma omp parallel for schedule(static)
-    for (int i = 0; i < nV1; i++) {
-        const int itype = otype(o, i % bs);
-        float lgE[PV1_MAX_NG] = {0, 0}, lhE[PV1_MAX_NG] = {0, 0}, lgI[PV1_MAX_NG] = {0, 0}, lhI[PV1_MAX_NG] = {0, 0};
-        for (size_t e = o->vecOff[i]; e < o->vecOff[i + 1]; e++) {
-            const uint32_t pre = o->vecID[e];
-            const int tid = (int)(pre % bs);
-            const float strength = o->conVec[e];
-            float time2post = o->delayVec[e] / c->speedOfThought;
-            const int preE = tid < o->nE;
-            const ocond *cd = preE ? &o->cE : &o->cI;
-            const int ng = preE ? (int)c->ngE : (int)c->ngI;
-            float *lg = preE ? lgE : lgI, *lh = preE ? lhE : lhI;
-            const unsigned it2post = (unsigned)ceilf(time2post / dt);
-            time2post = it2post * dt - time2post;
-            int k0 = (int)o->slot[e] - (int)it2post;
-            if (k0 < 0) k0 += (int)o->depth[e];
-            o->slot[e] = (o->slot[e] + 1) % o->depth[e];
-            if (c->noFarDelay) continue;
-            for (int k = 0; k < 2; k++) {
-                float dtsp = o->ring[o->ringOff[e] + (size_t)((k0 + k) % (int)o->depth[e])];
-                if (dtsp >= 1.0f) {
-                    const unsigned nsp = (unsigned)floorf(dtsp);
-                    dtsp = (dtsp - nsp + k) * dt - time2post;
-                    if (dtsp < dt && dtsp >= 0) {
-                        const float f = strength;
-                        if (f > 0) {
-                            dtsp = dt - dtsp;
-                            for (int ig = 0; ig < ng; ig++) {
-                                const float ip = preE ? c->pE[itype * c->ngE + ig] : c->pI[itype * c->ngI + ig];
-                                ocond_input(cd, &lg[ig], &lh[ig], nsp * f * ip, dtsp, ig);
-                            }
-                        }
-                    }
-                }
-            }
-        }
-        if (o->vecOff[i + 1] > o->vecOff[i] && !c->noFarDelay) {
-            for (uint32_t ig = 0; ig < c->ngE; ig++) { o->gE[ig * nV1 + i] += lgE[ig]; o->hE[ig * nV1 + i] += lhE[ig]; }
-            for (uint32_t ig = 0; ig < c->ngI; ig++) { o->gI[ig * nV1 + i] += lgI[ig]; o->hI[ig * nV1 + i] += lhI[ig]; }
-        }
+        for (int i = 0; i < nV1; i++) ofar_post(o, i, 1, NULL);
+        return 0;
+    }
+    if (!o->farEng) return -1;
+    const int nCh = o->nChunk > o->nblock ? o->nblock : o->nChunk;
+    const int split = o->nblock % nCh, rem = o->nblock / nCh, maxC = rem + (split > 0);
+#pragma omp parallel for schedule(dynamic)
+    for (int q = 0; q < nCh; q++) {
+        const int b0 = q < split ? q * maxC : split * maxC + (q - split) * rem;
+        const int nb = q < split ? maxC : rem;
+        onormal dist = {0, 0.f};
+        for (int i = b0 * bs; i < (b0 + nb) * bs; i++) ofar_post(o, i, 1, &dist);
     }
     return 0;
 }

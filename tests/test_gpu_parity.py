@@ -531,3 +531,81 @@ def test_initial_spikes_dynamics_parity(native, kind):
     assert_raster_ok(cmp)
     for k in ("v", "gE", "gI"):
         assert cmp[f"max_rel_{k}"] < 1e-5, cmp
+
+
+def _far_failure_workload(seed, **kw):
+    from visual_cortex_gb300 import synth
+    return synth.make_workload("farfail", seed=seed, nblock=4, n_lgn=1024, m=20, width=64, height=64,
+                               nt=800, far_partners=100, adex_inh=True, patch_deg=2.0, nFrame=120, wFar=0.01,
+                               synFail=(0.2, 0.2, 0.2, 0.2), nChunk=3, **kw)
+
+
+@pytest.mark.parametrize("with_sp0", [False, True])
+def test_far_failure_open_loop(native, with_sp0):
+    """Far synaptic failure draw for draw: every step the oracle's recal_G_vec (restating
+    libstdc++'s engines and polar pairs, pinned against libstdc++ itself) is fed the GPU's own
+    spike words, and its far sums are compared with the GPU's, chunks of 2, 1 and 1 blocks.
+    Fed the same spikes the two agree to float rounding for as long as they run; in a closed
+    loop an ulp-level spike-time difference that moves one far event across its arrival window
+    changes that post's draw count and so every later draw of its chunk (a property of the
+    reference's shared distribution), which the closed-loop test below bounds."""
+    import oracle
+    from visual_cortex_gb300.model import Simulation
+    rates = dict(spE0=[2000.0, 1000.0], spI0=[3000.0, 1500.0]) if with_sp0 else {}
+    wl = _far_failure_workload(71 + with_sp0, **rates)
+    spec, n = wl.spec, wl.spec.nV1
+    ngE, ngI = spec.ngE, spec.ngI
+    sim = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds, record_init=64 if with_sp0 else 0)
+    vo = oracle.V1Oracle(wl.spec, wl.net)
+    try:
+        vo.set_state(wl.init)
+        vo.set_far_failure(wl.seeds.far_engine_seed, wl.seeds.nChunk)
+        zero = {k: np.zeros(getattr(spec, "ng" + k[1]) * n, np.float32) for k in ("gE", "hE", "gI", "hI")}
+        if with_sp0:
+            # the delivery before the first step: compare the conductances it leaves
+            m, _ = vo.init_spikes(wl.seeds.sp0, wl.seeds.SCsplit, wl.seeds.trainDepth, sim.init_record)
+            assert m == 0
+            for k in ("gE", "hE", "gI", "hI"):
+                np.testing.assert_allclose(sim.state(k), vo.get(k), rtol=1e-5, atol=1e-8, err_msg=k)
+        drew = 0
+        for t in range(150):
+            sim.run(1)
+            s = sim.state("sInfo")
+            fp = sim.state("farPull").reshape(ngE + ngI, 2, n)
+            for k, a in zero.items():
+                vo.put(k, a)
+            vo.put("sInfo", s)
+            oracle.lib().orc_v1_deliver_far(vo.h)
+            got = {"gE": fp[:ngE, 0].ravel(), "hE": fp[:ngE, 1].ravel(), "gI": fp[ngE:, 0].ravel(), "hI": fp[ngE:, 1].ravel()}
+            for k in ("gE", "hE", "gI", "hI"):
+                # 1e-4 of the population's largest sum: an event arriving late in the step
+                # takes g from exp(-d/decay) - exp(-d/rise) at small d, where an ulp of expf
+                # (device vs host) becomes ~1e-5 of the event; one wrong draw would move its
+                # event by ~10%
+                ref = vo.get(k)
+                scale = max(float(np.abs(ref).max()), 1e-12)
+                assert np.abs(got[k] - ref).max() <= 1e-4 * scale, (t, k)
+            drew += int((fp != 0).any())
+        assert drew > 50
+    finally:
+        sim.close()
+        vo.close()
+
+
+@pytest.mark.parametrize("with_sp0", [False, True])
+def test_far_failure_parity(native, with_sp0):
+    """Closed loop with far synaptic failure: rasters identical over the first 8 ms (64 steps,
+    the far input arriving from step ~11 on) and traces within 1e-5 up to the first spike-time
+    divergence; later the chunk-wide draw sequence makes an ulp-level difference grow (see the
+    open-loop test)."""
+    from oracle.parity import run_parity, compare
+    rates = dict(spE0=[2000.0, 1000.0], spI0=[3000.0, 1500.0]) if with_sp0 else {}
+    wl = _far_failure_workload(61 + with_sp0, **rates)
+    assert wl.net.nVec.sum() > 0
+    res = run_parity(wl, 64, cap=16)
+    cmp = compare(res, wl.spec)
+    assert res["draw_count_mismatch"] == 0
+    assert cmp["v1_spikes_gpu"] > 0, cmp
+    assert cmp["first_raster_divergence"] is None, cmp
+    for k in ("v", "gE", "gI"):
+        assert cmp[f"max_rel_{k}"] < 1e-5, cmp

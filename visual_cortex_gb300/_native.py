@@ -21,7 +21,7 @@ ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "call out of order", -4: "un
 
 REC_RAW, REC_LGN_SP, REC_LGN_FR, REC_SPIKES = 1, 2, 4, 8
 ST = dict(v=0, w=1, tBack=2, dep=3, gFF=4, hFF=5, gE=6, hE=7, gI=8, hI=9, sInfo=10,
-          lgn_ltr=11, lgn_lnl=12, lgn_sInfo=13)
+          lgn_ltr=11, lgn_lnl=12, lgn_sInfo=13, farPull=14)
 
 _f2 = C.c_float * MAX_NG
 _t2 = C.c_float * MAX_NTYPE
@@ -119,6 +119,7 @@ def _load() -> C.CDLL:
         "pv1_v1_set_near_delayed": ([P, C.c_uint32, _UP, _UP, _FP, _FP], C.c_int),
         "pv1_v1_set_state": ([P, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP], C.c_int),
         "pv1_v1_init_rng": ([P, C.c_uint64, C.c_uint32], C.c_int),
+        "pv1_v1_far_failure_engines": ([P, C.c_uint64, C.c_uint32], C.c_int),
         "pv1_v1_init_spikes": ([P, C.c_uint64, C.c_uint32, _FP, C.c_uint32, C.POINTER(InitRecord)], C.c_int),
         "pv1_host_init_state": ([C.POINTER(V1Config), C.c_uint64, _FP, _UP, C.c_int, C.c_float,
                                  _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP],

@@ -191,6 +191,25 @@ struct V1Params {
     int nearOn;                // near-class (delayed) events exist: nearAcc is used
     int farClass;              // far-class events exist: farAcc is used
     unsigned long long *nearAcc;  // [farDepth][ngE+ngI][2][nV1] fixed-point g,h of near-class events
+    // far synapses pulled by post in the reference's vec order (far synaptic failure: recal_G_vec's
+    // per-post host engines and one normal_distribution per chunk of blocks)
+    int farPullOn;
+    const int *pullOff;        // [nV1+1]
+    const int *pullPre;        // [nnz]
+    const float *pullStr;      // [nnz]
+    const int *pullSteps;      // [nnz] it2post
+    const float *pullFrac;     // [nnz] it2post*dt - delay/speed
+    const float *pullP;        // [nnz] failure rate of the (pre type, post type) pair
+    const float *pullStd;      // [nnz] sqrt(p(1-p)/synPerCon)
+    const unsigned char *pullIsPre;  // [nV1] 1 if the neuron is a far presynaptic partner
+    float *sRing; int sDepth;  // [sDepth][nV1] spike words of the last sDepth steps (row = step mod sDepth)
+    unsigned *eng;             // [nV1] minstd_rand0 states
+    int *pullCount, *pullStart, *pullPrev;  // [nV1] draws this step, first draw's index in the chunk, previous drawer
+    float *pullCarry;          // [nV1] the unused second value of a post's last pair
+    float *farPull;            // [ngE+ngI][2][nV1] far sums of the last step (consumed by the next delivery)
+    int *pullFlag;             // [3] some far presynaptic spike (sInfo > 1) in step t%3
+    const int *chunkStart;     // [nChunk+1] first neuron of each chunk
+    int nChunk;
     // records
     float *rec; long long recStride; int recSlots; int hWrite;
     float *recSpk;             // [recSlots][nV1] spike words (PV1_REC_SPIKES)
@@ -276,6 +295,12 @@ cudaError_t launch_v1_sp_near(const V1Params &p, const float *Hlast, const float
                               float *recZ, unsigned *recNZ, int cap, cudaStream_t st);
 // The delayed events of the history and the delivery of those arriving before the first step.
 cudaError_t launch_v1_sp_events(const V1Params &p, const float *H, int depth, cudaStream_t st);
+// Far delivery with synaptic failure for step *stepBase + off (stepBase may be null: step off),
+// after that step's V1 kernel: four launches (count, chunk scan, carries, sums).
+cudaError_t launch_far_pull(const V1Params &p, const long long *stepBase, long long off, cudaStream_t st);
+constexpr int kFarPullLaunches = 4;
+// Adds farPull to the E/I conductances (the far part of the delivery before the first step).
+cudaError_t launch_far_pull_apply(const V1Params &p, cudaStream_t st);
 int v1_persistent_ctas(const V1Params &p, int device, bool *fits);
 // Evaluates the full-step decay factors of the three conductance kernels on the device and
 // stores them into p (synchronous).

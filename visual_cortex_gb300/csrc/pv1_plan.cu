@@ -35,6 +35,7 @@ struct pv1_plan {
     int *d_err = nullptr;
     long long *d_stepBase = nullptr;
     bool haveLGNsyn = false, haveNear = false, haveState = false, haveRng = false;
+    bool haveFarEng = false;    // far failure: engines seeded (pv1_v1_far_failure_engines)
     bool lgnReady = false, stimReady = false;
     pv1_lgn_config lcfg{};
     int nMagno = 0, nLGN = 0, mSample = 0;
@@ -197,6 +198,11 @@ int issue_chunk(pv1_plan *p, int k, int deliverFirst, long long *launches) {
             int deliver = (s == 0) ? deliverFirst : 1;
             e = launch_v1_step(p->vp, p->d_stepBase, s, p->d_lgnRing, p->lgnSlots, deliver, 1, p->stream);
             if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("v1_step: ") + cudaGetErrorString(e));
+            if (p->vp.farPullOn) {
+                e = launch_far_pull(p->vp, p->d_stepBase, s, p->stream);
+                if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("far_pull: ") + cudaGetErrorString(e));
+                n += kFarPullLaunches;
+            }
         }
         n += k;
     }
@@ -263,6 +269,8 @@ int plan_batch_view(pv1_plan *p, PlanBatchView *out) {
     if (er) return er;
     if (!p->haveLGNsyn || !p->haveNear || !p->haveState || !p->haveRng)
         return fail(p, PV1_E_STATE, "V1 synapses/connectivity/state/rng not set");
+    if (p->vp.farPullOn)
+        return fail(p, PV1_E_UNSUPPORTED, "batched trials with far synaptic failure are not built");
     out->vp = p->vp;
     out->lp = p->lp;
     out->lgnRing = p->d_lgnRing;
@@ -1134,6 +1142,122 @@ int rebuild_events(pv1_plan *p) {
 
 extern "C" {
 
+// Far synapses by post in the reference's vec order for the failure path: pre, strength,
+// whole-step delay and offset (as build_event_lists computes them), failure rate and its
+// normed std per (pre type, post type), the spike-word ring and the per-step scratch.
+static int build_far_pull(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, const float *conVec,
+                          const float *delayVec, size_t nnz) {
+    const int nV1 = p->nV1;
+    const pv1_v1_config &c = p->cfg;
+    V1Params &v = p->vp;
+    auto typeOf = [&](int local) {
+        int t = (int)c.nType - 1;
+        for (int j = (int)c.nType - 1; j >= 0; j--)
+            if ((uint32_t)local < c.typeAcc[j]) t = j;
+        return t;
+    };
+    std::vector<int> off(nV1 + 1, 0), pre(nnz), steps(nnz);
+    std::vector<float> str(nnz), frac(nnz), pf(nnz), sd(nnz);
+    std::vector<unsigned char> isPre(nV1, 0);
+    int maxSteps = 0;
+    size_t e = 0;
+    for (int i = 0; i < nV1; i++) {
+        off[i + 1] = off[i] + (int)nVec[i];
+        const int itype = typeOf(i % (int)c.blockSize);
+        for (uint32_t j = 0; j < nVec[i]; j++, e++) {
+            const int q = (int)vecID[e];
+            pre[e] = q;
+            str[e] = conVec[e];
+            float time2post = delayVec[e] / c.speedOfThought;
+            const unsigned it2post = (unsigned)std::ceil(time2post / c.dt);
+            if (it2post > 0xffff) return fail(p, PV1_E_UNSUPPORTED, "synaptic delay longer than 65535 steps");
+            steps[e] = (int)it2post;
+            frac[e] = it2post * c.dt - time2post;
+            maxSteps = std::max(maxSteps, (int)it2post);
+            const int jtype = typeOf(q % (int)c.blockSize);
+            const float fp = c.synFail[jtype * c.nType + itype];
+            pf[e] = fp;
+            sd[e] = fp > 0 ? std::sqrt(fp * (1 - fp) / c.synPerCon[jtype * c.nType + itype]) : 0.f;
+            isPre[q] = 1;
+        }
+    }
+    const int D = maxSteps + 2;
+    const int ns = (int)(c.ngE + c.ngI);
+    int *d_off, *d_pre, *d_steps, *d_cnt, *d_start, *d_prev, *d_flag;
+    float *d_str, *d_frac, *d_p, *d_sd, *d_ring, *d_carry, *d_pull;
+    unsigned char *d_isPre;
+    unsigned *d_eng;
+    int r = 0;
+    r |= dev_upload(p, &d_off, off.data(), off.size());
+    r |= dev_upload(p, &d_pre, pre.data(), nnz);
+    r |= dev_upload(p, &d_steps, steps.data(), nnz);
+    r |= dev_upload(p, &d_str, str.data(), nnz);
+    r |= dev_upload(p, &d_frac, frac.data(), nnz);
+    r |= dev_upload(p, &d_p, pf.data(), nnz);
+    r |= dev_upload(p, &d_sd, sd.data(), nnz);
+    r |= dev_upload(p, &d_isPre, isPre.data(), nV1);
+    r |= dev_alloc(p, &d_ring, (size_t)D * nV1);
+    r |= dev_alloc(p, &d_eng, nV1);
+    r |= dev_alloc(p, &d_cnt, nV1);
+    r |= dev_alloc(p, &d_start, nV1);
+    r |= dev_alloc(p, &d_prev, nV1);
+    r |= dev_alloc(p, &d_carry, nV1);
+    r |= dev_alloc(p, &d_pull, (size_t)ns * 2 * nV1);
+    r |= dev_alloc(p, &d_flag, 3);
+    if (r) return r;
+    v.farPullOn = 1;
+    v.pullOff = d_off;
+    v.pullPre = d_pre;
+    v.pullSteps = d_steps;
+    v.pullStr = d_str;
+    v.pullFrac = d_frac;
+    v.pullP = d_p;
+    v.pullStd = d_sd;
+    v.pullIsPre = d_isPre;
+    v.sRing = d_ring;
+    v.sDepth = D;
+    v.eng = d_eng;
+    v.pullCount = d_cnt;
+    v.pullStart = d_start;
+    v.pullPrev = d_prev;
+    v.pullCarry = d_carry;
+    v.farPull = d_pull;
+    v.pullFlag = d_flag;
+    p->haveFarEng = false;
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    return PV1_OK;
+}
+
+int pv1_v1_far_failure_engines(pv1_plan *p, uint64_t seed, uint32_t nChunk) {
+    if (!p || nChunk < 1) return PV1_E_ARG;
+    const pv1_v1_config &c = p->cfg;
+    V1Params &v = p->vp;
+    if (!v.farPullOn) return PV1_OK;
+    // chunks of blocks as src/patch.cu:3430-3437 splits them: the first nblock % nChunk chunks
+    // one block longer
+    const int nb = (int)c.nblock;
+    const int nCh = std::min<int>((int)nChunk, nb);
+    const int split = nb % nCh, rem = nb / nCh, maxC = rem + (split > 0 ? 1 : 0);
+    std::vector<int> cs(nCh + 1, 0);
+    for (int q = 0; q < nCh; q++) cs[q + 1] = cs[q] + (q < split ? maxC : rem) * (int)c.blockSize;
+    std::vector<unsigned> eng(p->nV1);
+    for (int i = 0; i < p->nV1; i++) {
+        const uint64_t x = (seed + (uint64_t)i) % 2147483647ull;   // minstd_rand0::seed
+        eng[i] = x == 0 ? 1u : (unsigned)x;
+    }
+    if (v.chunkStart) free_one(p, (void *)v.chunkStart);
+    int *d_cs;
+    int r = dev_upload(p, &d_cs, cs.data(), cs.size());
+    if (r) return r;
+    v.chunkStart = d_cs;
+    v.nChunk = nCh;
+    PV1_CUDA(p, cudaMemcpyAsync(v.eng, eng.data(), eng.size() * sizeof(unsigned), cudaMemcpyHostToDevice, p->stream));
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    p->haveFarEng = true;
+    drop_graph(p);
+    return PV1_OK;
+}
+
 int pv1_v1_set_far(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, const float *conVec,
                    const float *delayVec) {
     if (!p || !nVec) return PV1_E_ARG;
@@ -1144,12 +1268,17 @@ int pv1_v1_set_far(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, con
     if (nnz && (!vecID || !conVec || !delayVec)) return PV1_E_ARG;
     p->nFarSyn = (long long)nnz;
     p->farSyn.clear();
-    if (nnz && !c.noFarDelay) {
+    bool failure = false;
+    for (int q = 0; q < (int)(c.nType * c.nType); q++) failure = failure || c.synFail[q] > 0;
+    p->vp.farPullOn = 0;
+    if (nnz && !c.noFarDelay && failure) {
+        // far synaptic failure: pulled by post in vec order (pv1_far_pull.cu)
+        for (size_t e = 0; e < nnz; e++)
+            if (vecID[e] >= (uint32_t)nV1) return fail(p, PV1_E_ARG, "far pre id out of range");
+        int r = build_far_pull(p, nVec, vecID, conVec, delayVec, nnz);
+        if (r) return r;
+    } else if (nnz && !c.noFarDelay) {
         // (noFarDelay = 1 is the reference's path that drops far input)
-        for (int q = 0; q < (int)(c.nType * c.nType); q++)
-            if (c.synFail[q] > 0)
-                return fail(p, PV1_E_UNSUPPORTED,
-                            "synaptic failure on delayed synapses (host std::normal_distribution per post) is not built");
         p->farSyn.resize(nnz);
         size_t e = 0;
         for (int i = 0; i < nV1; i++)
@@ -1241,6 +1370,8 @@ int pv1_v1_init_spikes(pv1_plan *p, uint64_t seed, uint32_t trainDepth, const fl
     const pv1_v1_config &c = p->cfg;
     if (!p->haveState || !p->haveNear) return fail(p, PV1_E_STATE, "set the state and the connectivity first");
     if (p->step != 0) return fail(p, PV1_E_STATE, "initial spikes are set before the first step");
+    if (p->vp.farPullOn && !p->haveFarEng)
+        return fail(p, PV1_E_STATE, "far synaptic failure: call pv1_v1_far_failure_engines first");
     if (c.blockSize > 1024) return fail(p, PV1_E_UNSUPPORTED, "initial spikes need blockSize <= 1024");
     Sp0 s0{};
     bool has = false;
@@ -1280,6 +1411,13 @@ int pv1_v1_init_spikes(pv1_plan *p, uint64_t seed, uint32_t trainDepth, const fl
         e = cudaMemsetAsync(vp.farFlag, 0, 3 * sizeof(int), p->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(vp.farCount, 0, 3 * sizeof(int), p->stream);
         if (e == cudaSuccess) e = launch_v1_sp_events(vp, dH, depth, p->stream);
+    }
+    if (e == cudaSuccess && has && vp.farPullOn) {
+        // far failure path: the history slot depth-1 is step -1 of the spike-word ring
+        e = cudaMemcpyAsync(vp.sRing + (size_t)(vp.sDepth - 1) * n, dH + (size_t)(depth - 1) * n, n * sizeof(float),
+                            cudaMemcpyDeviceToDevice, p->stream);
+        if (e == cudaSuccess) e = launch_far_pull(vp, nullptr, -1, p->stream);
+        if (e == cudaSuccess) e = launch_far_pull_apply(vp, p->stream);
     }
     auto down = [&](void *dst, const void *src, size_t bytes) {
         if (e == cudaSuccess && dst && src) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, p->stream);
@@ -1365,7 +1503,7 @@ static int choose_mode(pv1_plan *p) {
     if (p->modeChosen) return PV1_OK;
     bool fits = false;
     v1_persistent_ctas(p->vp, p->device, &fits);
-    p->persistent = fits && p->allowPersistent && !p->vp.multiSpike;
+    p->persistent = fits && p->allowPersistent && !p->vp.multiSpike && !p->vp.farPullOn;
     if (p->persistent && !p->d_barrier) {
         int r = dev_alloc(p, &p->d_barrier, 2);
         if (r) return r;
@@ -1379,6 +1517,8 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
     if (!p->lgnReady || !p->stimReady) return fail(p, PV1_E_STATE, "LGN/stimulus not loaded");
     if (!p->haveLGNsyn || !p->haveNear || !p->haveState || !p->haveRng)
         return fail(p, PV1_E_STATE, "V1 synapses/connectivity/state/rng not set");
+    if (p->vp.farPullOn && !p->haveFarEng)
+        return fail(p, PV1_E_STATE, "far synaptic failure: call pv1_v1_far_failure_engines first");
     if (p->recFlags && nsteps > (uint32_t)(p->recSlots - 1))
         return fail(p, PV1_E_ARG, "run longer than the record ring; fetch records in between");
     int r = choose_mode(p);
@@ -1687,6 +1827,11 @@ int pv1_get_state(pv1_plan *p, int which, float *out) {
             if (p->step == 0) return fail(p, PV1_E_STATE, "no step run yet");
             src = p->d_lgnRing + (size_t)((p->step - 1) % p->lgnSlots) * p->nLGN;
             cnt = p->nLGN;
+            break;
+        case PV1_ST_FAR_PULL:
+            if (!v.farPullOn) return fail(p, PV1_E_STATE, "no far synaptic failure in this plan");
+            src = v.farPull;
+            cnt = (size_t)(c.ngE + c.ngI) * 2 * n;
             break;
         default: return fail(p, PV1_E_ARG, "unknown state id");
     }

@@ -350,6 +350,21 @@ __device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, in
         st.gE[ig] += lgE[ig]; st.hE[ig] += lhE[ig];
         st.gI[ig] += lgI[ig]; st.hI[ig] += lhI[ig];
     }
+    // far sums of the failure path (already zero when no far presynaptic neuron spiked)
+    if (P.farPullOn && active) {
+#pragma unroll
+        for (int q = 0; q < 2 * kMaxNG; q++) {
+            if (q < ns) {
+                const float fg = __ldcg(P.farPull + (size_t)(2 * q) * nV1 + i);
+                const float fh = __ldcg(P.farPull + (size_t)(2 * q + 1) * nV1 + i);
+#pragma unroll
+                for (int ig = 0; ig < kMaxNG; ig++) {
+                    if (q < ngE && ig == q) { st.gE[ig] += fg; st.hE[ig] += fh; }
+                    if (q >= ngE && ig == q - ngE) { st.gI[ig] += fg; st.hI[ig] += fh; }
+                }
+            }
+        }
+    }
     // far events (sum_G adds them after the near delivery); the ring slot is cleared
     if (acc) {
 #pragma unroll
@@ -1152,6 +1167,7 @@ __device__ __forceinline__ void v1_step_body(const V1Params &P, long long t, int
         if (Rng && P.condRng) P.rGenCond[i] = condState;
         if (Rng && P.noiseRng) P.rNoisy[i] = noisyState;
         if (P.spikeCount && sInfo >= 1.0f) P.spikeCount[i] += (unsigned)floorf(sInfo);
+        if (P.farPullOn) P.sRing[(size_t)(t % P.sDepth) * P.nV1 + i] = sInfo;
     }
     if (P.farOn) {
         const int e0 = active ? P.farOff[i] : 0;

@@ -281,7 +281,7 @@ def build(c: Config) -> Model:
     init = host_init_state(spec, s_init, iTonic, nL, v0, w0, gFF0, gE0, gI0, use_v0=c.use_v0,
                            tonicMax=float(iTonic.max()))
     seeds = Seeds(lgn=s_lgn, cond=s_sp, trainDepth=max(trainDepth, 1), sp0=_sp0(c, nTypeE, nTypeI),
-                  SCsplit=int(c.SCsplit))
+                  SCsplit=int(c.SCsplit), nChunk=int(c.nChunk))
     extra = dict(nType=nType, nTypeE=nTypeE, nTypeI=nTypeI, typeAcc=typeAcc, nLGN=nLGN,
                  normViewDistance=geo["normViewDistance"], stimulus_filename=P.stimulus, sRatioV1=sRatioV1,
                  sRatioLGN=sRatioLGN, tonicDep=tonicDep, noisyDep=noisyDep, vR=vR,

@@ -278,6 +278,12 @@ class Seeds:
     trainDepth: int = 2
     sp0: tuple | None = None   # initial spikes: per-step chance [nType][2] (spE0, spI0 x dt/1000)
     SCsplit: int = 0
+    nChunk: int = 1            # chunks of blocks of the far delivery (far synaptic failure)
+
+    @property
+    def far_engine_seed(self) -> int:
+        """Seed of the first far-failure host engine: the one after logRand_init's."""
+        return int(self.lgn) + 1
 
     def has_sp0(self) -> bool:
         return self.sp0 is not None and any(float(x) > 0 for x in np.ravel(self.sp0))
@@ -311,6 +317,8 @@ class Simulation:
         init3 = np.asarray(stim.init_LMS, dtype=f32)
         N.check(plan, N.lib.pv1_stimulus_load(plan, nF, h, w, N.fptr(init3), N.fptr(fr)), "pv1_stimulus_load")
         self._set_network(net)
+        N.check(plan, N.lib.pv1_v1_far_failure_engines(plan, seeds.far_engine_seed, int(seeds.nChunk)),
+                "pv1_v1_far_failure_engines")
         self.put_initial_state(init)
         self.init_record = None
         if seeds.has_sp0():
@@ -441,7 +449,7 @@ class Simulation:
         n = spec.nV1
         sizes = dict(gFF=spec.ngFF * n, hFF=spec.ngFF * n, gE=spec.ngE * n, hE=spec.ngE * n,
                      gI=spec.ngI * n, hI=spec.ngI * n, lgn_ltr=self.lgn.nLGN, lgn_lnl=self.lgn.nLGN,
-                     lgn_sInfo=self.lgn.nLGN)
+                     lgn_sInfo=self.lgn.nLGN, farPull=(spec.ngE + spec.ngI) * 2 * n)
         out = np.empty(sizes.get(name, n), f32)
         N.check(self.plan, N.lib.pv1_get_state(self.plan, N.ST[name], N.fptr(out)), f"pv1_get_state({name})")
         return out

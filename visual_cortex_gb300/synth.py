@@ -348,7 +348,7 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
                   noDelay: int = 1, n_parvo: int = 0, tau: float | None = None,
                   nKernelSample: int | None = None, blockSize: int = 1024, nE: int = 768,
                   m_min: int | None = None, flat_retina: bool = True, spE0=None, spI0=None,
-                  SCsplit: int = 0) -> Workload:
+                  SCsplit: int = 0, nChunk: int = 1) -> Workload:
     """Builds one synthetic patch; C1 = 1x1024 V1 / 512 LGN; C2 = 32 blocks / 16384 LGN.
     noDelay = 0: near synapses are delivered after their distance delay (delayMat from the
     neuron positions, mm, at speedOfThought 1 mm/ms).  spE0/spI0: initial spike rates in Hz
@@ -405,7 +405,7 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
         nTE, nTI = spec.nTypeE, spec.nType - spec.nTypeE
         rates = list(spE0 if spE0 is not None else [0.0] * 2 * nTE) + list(spI0 if spI0 is not None else [0.0] * 2 * nTI)
         sp0 = tuple(sp0_chances(rates, spec.dt))
-    seeds = Seeds(lgn=s_lgn, cond=s_sp, trainDepth=max(trainDepth, 2), sp0=sp0, SCsplit=SCsplit)
+    seeds = Seeds(lgn=s_lgn, cond=s_sp, trainDepth=max(trainDepth, 2), sp0=sp0, SCsplit=SCsplit, nChunk=nChunk)
     return Workload(name=name, spec=spec, net=net, lgn=lgn, stim=stim, init=init, seeds=seeds,
                     nt=nt, pos=pos, rf_center=rfc, rf_orient=rfo)
 

@@ -120,3 +120,18 @@ def test_curved_retina_reads_back():
     assert stim.neye == 2
     with pytest.raises(cfg.ConfigError, match="one eye"):
         driver.build(cfg.load(["-c", fn, "--flat_retina", "1"]))
+
+
+def test_two_eye_parvo_reads_back():
+    """Parvo and magno cells in both eyes (LGN_vpos nI / nC, cells ordered parvo_I, magno_I,
+    parvo_C, magno_C): the driver splits them as the reference does."""
+    wl = synth.make_workload("twoeye", seed=5, nblock=1, n_lgn=256, m=20, width=64, height=64, nt=48,
+                             nFrame=40, flat_retina=False, n_parvo=32, tau=300.0, nKernelSample=150,
+                             contra=True)
+    d = tempfile.mkdtemp()
+    fn = synth.write_reference_files(wl, d, seed=3, nt=48)
+    m = driver.build(cfg.load(["-c", fn]))
+    L = m.lgn
+    assert (L.nParvo_I, L.nMagno_I, L.nParvo_C, L.nMagno_C) == (16, 128, 16, 128)
+    np.testing.assert_array_equal(L.coneType, wl.lgn.coneType)
+    np.testing.assert_allclose(L.polar, wl.lgn.polar, rtol=1e-6)

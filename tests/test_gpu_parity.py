@@ -457,6 +457,50 @@ def test_curved_retina_setup_tables(curved_wl):
     np.testing.assert_allclose(mc, lo.maxConvol, rtol=1e-5)
 
 
+@pytest.fixture(scope="module")
+def two_eye_wl(native):
+    """Curved retina with parvo and magno cells in both eyes (the second eye's cells sample the
+    right half of the binocular texture from R_x0, R_y0)."""
+    from visual_cortex_gb300 import synth
+    return synth.make_workload("twoeye", seed=16, nblock=1, n_lgn=512, m=20, width=96, height=96, nt=800,
+                               nFrame=60, n_parvo=64, tau=300.0, nKernelSample=150, flat_retina=False, contra=True)
+
+
+def test_two_eye_setup_tables(two_eye_wl):
+    import oracle
+    from visual_cortex_gb300.model import Simulation
+    wl = two_eye_wl
+    assert wl.lgn.nParvo_C > 0 and wl.lgn.nMagno_C > 0
+    sim = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        TW, SW, SC, mc = sim.lgn_tables()
+        pTW, pSW, pSC = sim.lgn_parvo_tables()
+        PS = sim.lgn_parvo_spatial()
+    finally:
+        sim.close()
+    lo = oracle.LgnOracle(wl.lgn, wl.stim)
+    np.testing.assert_allclose(SC, lo.SC, rtol=1e-6, atol=2e-6)
+    np.testing.assert_allclose(pSC, lo.pSC, rtol=1e-6, atol=2e-6)
+    nMI, nPI = wl.lgn.nMagno_I, wl.lgn.nParvo_I
+    assert SC[0][nMI:].min() > 0.5 and pSC[0][nPI:].min() > 0.5     # second eye: right half
+    np.testing.assert_allclose(mc, lo.maxConvol, rtol=1e-5)
+    # the oracle emulates the texture unit's 1/256 filter weights: one weight step times the
+    # steepest neighbouring-texel step of this 96x96 grating bounds the difference
+    ref = lo.parvo_spatial(SW=pSW, SC=pSC)
+    assert np.abs(PS - ref).max() < 5e-4
+
+
+def test_two_eye_dynamics_parity(two_eye_wl):
+    from oracle.parity import run_parity, compare
+    wl = two_eye_wl
+    res = run_parity(wl, RASTER_STEPS, cap=8)
+    cmp = compare(res, wl.spec)
+    assert res["draw_count_mismatch"] == 0
+    assert cmp["lgn_spike_mismatch"] == 0, cmp
+    assert cmp["lgn_fr_maxrel"] < 1e-5, cmp
+    assert_raster_ok(cmp)
+
+
 def test_curved_retina_dynamics_parity(curved_wl):
     from oracle.parity import run_parity, compare
     wl = curved_wl

@@ -258,8 +258,6 @@ def build(c: Config) -> Model:
     nParvo_I, nParvo_C = int(parvo[:nI_].sum()), int(parvo[nI_:].sum())
     if not (np.all(parvo[:nParvo_I]) and np.all(parvo[nI_:nI_ + nParvo_C])):
         raise ConfigError("LGN_vpos: parvo cells must come before the magno cells of each eye")
-    if nC_ and nParvo_I + nParvo_C:
-        raise ConfigError("not supported by this build: parvo cells with a second eye")
     prm = FM.read_lgn_params(P.lgn, nLGN)
     geo = retina_geometry(max_ecc, stim_f.range, stim_f.buffer, bool(c.flat_retina))
     sched = make_schedule(c.dt, c.frameRate, c.tau, c.mau, c.nKernelSample, c.mKernelSample)

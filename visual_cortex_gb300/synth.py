@@ -84,7 +84,7 @@ def make_lgn(n_lgn: int, rng: np.random.Generator, patch_deg: float, dt: float,
              stim_range_deg: float | None = None, buffer_deg: float = 0.2,
              jitter: float = 0.0, tjitter: float = 0.0, n_parvo: int = 0,
              tau: float | None = None, nKernelSample: int | None = None,
-             nSample1D: int = 8, flat_retina: bool = True) -> tuple[LgnSpec, float]:
+             nSample1D: int = 8, flat_retina: bool = True, contra: bool = False) -> tuple[LgnSpec, float]:
     """ON/OFF magno cells with centers uniform in a patch_deg square around the fixation;
     with n_parvo > 0 also parvocellular L/M-opponent cells (LGN ids 0..n_parvo-1, before the
     magno cells as the reference orders them), centre and surround at slightly different
@@ -115,8 +115,10 @@ def make_lgn(n_lgn: int, rng: np.random.Generator, patch_deg: float, dt: float,
     sched = make_schedule(dt, frame_rate, mau if tau is None else tau, mau, mKernelSample if nKernelSample is None
                           else nKernelSample, mKernelSample)
     if n_parvo > 0:
+        if contra and flat_retina:
+            raise ValueError("a second eye needs the curved retina")
         return _with_parvo(n_lgn, n_parvo, rng, patch_deg, sched, mSample1D, nSample1D, sigma_c, sigma_s,
-                           stim_range_deg, buffer_deg, jitter, flat_retina)
+                           stim_range_deg, buffer_deg, jitter, flat_retina, contra)
     spec = LgnSpec(
         nParvo_I=0, nMagno_I=n_lgn, nParvo_C=0, nMagno_C=0, mSample1D=mSample1D, sched=sched,
         polar=two(polar, polar), ecc=two(ecc, ecc), rw=two(sc * DEG, ss * DEG),
@@ -138,8 +140,9 @@ def make_lgn(n_lgn: int, rng: np.random.Generator, patch_deg: float, dt: float,
 
 
 def _with_parvo(n_magno, n_parvo, rng, patch_deg, sched, mSample1D, nSample1D, sigma_c, sigma_s,
-                stim_range_deg, buffer_deg, jitter, flat_retina=True):
-    """LGN of n_parvo parvo cells (ids first) and n_magno ON/OFF magno cells, one eye."""
+                stim_range_deg, buffer_deg, jitter, flat_retina=True, contra=False):
+    """LGN of n_parvo parvo cells (ids first) and n_magno ON/OFF magno cells, one eye; with
+    contra (curved retina only) half of each kind in the second eye."""
     n = n_parvo + n_magno
     xy = rng.uniform(-patch_deg / 2, patch_deg / 2, size=(n, 2))
     if not flat_retina:
@@ -202,7 +205,25 @@ def _with_parvo(n_magno, n_parvo, rng, patch_deg, sched, mSample1D, nSample1D, s
         covariant=np.where(types < 4, 0.53753461391295254, 1.0).astype(f32))
     spec.types = types
     spec.xy = xy
+    if contra:
+        _split_eyes(spec, n_parvo, n_magno)
     return spec, extent
+
+
+def _split_eyes(spec: LgnSpec, n_parvo: int, n_magno: int):
+    """Moves the second half of the parvo and of the magno cells to the second eye, in the
+    reference's order parvo_I, magno_I, parvo_C, magno_C (src/patch.cu:1723-1750)."""
+    n = n_parvo + n_magno
+    pI, mI = n_parvo // 2, n_magno // 2
+    parvo, magno = np.arange(n_parvo), n_parvo + np.arange(n_magno)
+    perm = np.concatenate([parvo[:pI], magno[:mI], parvo[pI:], magno[mI:]])
+    for name, val in list(vars(spec).items()):
+        if isinstance(val, np.ndarray) and val.shape[:1] == (2 * n,):
+            setattr(spec, name, np.concatenate([val[:n][perm], val[n:][perm]]))
+        elif isinstance(val, np.ndarray) and val.shape[:1] == (n,):
+            setattr(spec, name, val[perm])
+    spec.nParvo_I, spec.nMagno_I = pI, mI
+    spec.nParvo_C, spec.nMagno_C = n_parvo - pI, n_magno - mI
 
 
 def near_distances(spec: V1Spec, pos: np.ndarray, nNearNB, nbId) -> np.ndarray:
@@ -348,7 +369,7 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
                   noDelay: int = 1, n_parvo: int = 0, tau: float | None = None,
                   nKernelSample: int | None = None, blockSize: int = 1024, nE: int = 768,
                   m_min: int | None = None, flat_retina: bool = True, spE0=None, spI0=None,
-                  SCsplit: int = 0, nChunk: int = 1) -> Workload:
+                  SCsplit: int = 0, nChunk: int = 1, contra: bool = False) -> Workload:
     """Builds one synthetic patch; C1 = 1x1024 V1 / 512 LGN; C2 = 32 blocks / 16384 LGN.
     noDelay = 0: near synapses are delivered after their distance delay (delayMat from the
     neuron positions, mm, at speedOfThought 1 mm/ms).  spE0/spI0: initial spike rates in Hz
@@ -358,7 +379,8 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
     spec = make_spec(nblock, blockSize=blockSize, nE=nE, adex_inh=adex_inh, noisyDep=noisyDep,
                      synFail=synFail, synFailFF=synFailFF, dt=dt)
     lgn, extent = make_lgn(n_lgn, rng, patch_deg, dt, mSample1D=mSample1D, tjitter=tjitter,
-                           n_parvo=n_parvo, tau=tau, nKernelSample=nKernelSample, flat_retina=flat_retina)
+                           n_parvo=n_parvo, tau=tau, nKernelSample=nKernelSample, flat_retina=flat_retina,
+                           contra=contra)
     side = 0.5
     pos, nbx = block_positions(nblock, spec.blockSize, side, rng)
     conMat = near_conmat(spec, pos, rng, sigma=0.1, nE_partners=100, nI_partners=50,

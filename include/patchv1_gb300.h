@@ -307,6 +307,16 @@ int pv1_fetch_records(pv1_plan *plan, uint64_t step0, uint32_t n, float *raw,
                                failure plans; read only), added at the next step's delivery */
 /* Copies one state array to the host (waits for queued work). */
 int pv1_get_state(pv1_plan *plan, int which, float *out);
+/* Checkpoints: the plan's whole evolving state (neuron state and generators, spike-word
+ * rows, delayed-event rings, far-failure engines, LGN integrals and generators) with the step
+ * count, so that a plan of the same configuration and network that loads it continues bit
+ * for bit (the reference's snapshot, src/patch.cu:6793-6912, also holds the state needed to
+ * resume; its far rings, kept on the host, are not in it).  The last step's delivery is
+ * applied before saving.  size -> save into a host buffer of that size -> load. */
+int pv1_checkpoint_size(pv1_plan *plan, uint64_t *bytes);
+int pv1_checkpoint_save(pv1_plan *plan, void *buf, uint64_t bytes);
+int pv1_checkpoint_load(pv1_plan *plan, const void *buf, uint64_t bytes);
+
 /* Overwrites one state array (PV1_ST_* above). */
 int pv1_put_state(pv1_plan *plan, int which, const float *in);
 

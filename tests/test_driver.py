@@ -135,3 +135,34 @@ def test_two_eye_parvo_reads_back():
     assert (L.nParvo_I, L.nMagno_I, L.nParvo_C, L.nMagno_C) == (16, 128, 16, 128)
     np.testing.assert_array_equal(L.coneType, wl.lgn.coneType)
     np.testing.assert_allclose(L.polar, wl.lgn.polar, rtol=1e-6)
+
+
+@pytest.mark.gpu
+def test_snapshot_resume_continues_the_run(written, native):
+    """A run of 96 steps leaves a snapshot; a second run resumed from it (fSnapshot, asInit =
+    false) for 40 more steps writes the same records as one straight run of 136 steps."""
+    import glob
+    import os
+    import shutil
+    wl, fn = written
+    d = os.path.dirname(fn)
+    out1, out2, out3 = (os.path.join(d, x) + "/" for x in ("o1", "o2", "o3"))
+    lgn = cfg.resolve_paths(cfg.load(["-c", fn])).lgn     # read from the output folder
+    for o in (out1, out2, out3):
+        os.makedirs(o, exist_ok=True)
+        shutil.copy(lgn, o + os.path.basename(lgn))
+    driver.run(cfg.load(["-c", fn, "--outputFolder", out1, "--output_suffix", "s"]), chunk=40, log=lambda *_: None)
+    snaps = glob.glob(out1 + "snapShot_*_s.bin")
+    assert len(snaps) == 1      # the earlier ones of the run were removed (delPrevSnapshot)
+    name = os.path.basename(snaps[0])[:-len("_s.bin")]
+    c2 = cfg.load(["-c", fn, "--outputFolder", out2, "--output_suffix", "s", "--nt", "40",
+                   "--fSnapshot", "!" + out1 + name, "--snapshot_suffix", "s", "--asInit", "false"])
+    driver.run(c2, chunk=40, log=lambda *_: None)
+    driver.run(cfg.load(["-c", fn, "--outputFolder", out3, "--output_suffix", "s", "--nt", "136"]), chunk=40,
+               log=lambda *_: None)
+    _, r2 = FM.read_raw(cfg.resolve_paths(c2).raw)
+    _, r3 = FM.read_raw(cfg.resolve_paths(cfg.load(["-c", fn, "--outputFolder", out3, "--output_suffix", "s"])).raw)
+    np.testing.assert_array_equal(r2, r3[96:])
+    with pytest.raises(cfg.ConfigError, match="asInit"):
+        driver.build(cfg.load(["-c", fn, "--fSnapshot", "!" + out1 + name, "--snapshot_suffix", "s",
+                               "--output_suffix", "s"]))

@@ -653,3 +653,42 @@ def test_far_failure_parity(native, with_sp0):
     assert cmp["first_raster_divergence"] is None, cmp
     for k in ("v", "gE", "gI"):
         assert cmp[f"max_rel_{k}"] < 1e-5, cmp
+
+
+@pytest.mark.parametrize("kind", ["persistent_far", "delayed", "far_failure"])
+def test_checkpoint_resume_bitwise(native, kind):
+    """pv1_checkpoint_save after 150 steps, loaded into a fresh plan: its next 150 steps equal
+    those of the saving plan and of a plan that ran all 300 without stopping."""
+    from visual_cortex_gb300 import synth
+    from visual_cortex_gb300.model import Simulation
+    if kind == "persistent_far":
+        wl = synth.make_workload("ck", seed=81, nblock=4, n_lgn=1024, m=20, width=64, height=64, nt=800,
+                                 far_partners=100, adex_inh=True, nFrame=120, wFar=0.01, noisyDep=(0.1, 0.1))
+    elif kind == "delayed":
+        wl = synth.make_workload("ck", seed=82, nblock=2, n_lgn=512, m=20, width=64, height=64, nt=800,
+                                 far_partners=50, adex_inh=True, nFrame=60, noDelay=0)
+    else:
+        wl = _far_failure_workload(83)
+    sims = [Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds) for _ in range(3)]
+    a, b, c = sims
+    try:
+        a.run(150)
+        ck = a.checkpoint()
+        a.run(150)
+        b.restore(ck)
+        assert b.step == 150
+        b.run(150)
+        c.run(300)
+        for k in ("v", "w", "gE", "hE", "gI", "hI", "gFF", "hFF", "tBack", "lgn_lnl", "lgn_ltr"):
+            np.testing.assert_array_equal(a.state(k), b.state(k), err_msg=k)
+            np.testing.assert_array_equal(a.state(k), c.state(k), err_msg=k)
+        other = synth.make_workload("ck", seed=84, nblock=1, n_lgn=512, m=20, width=64, height=64, nt=800)
+        d = Simulation(other.spec, other.net, other.lgn, other.stim, other.init, other.seeds)
+        try:
+            with pytest.raises(RuntimeError):
+                d.restore(ck)
+        finally:
+            d.close()
+    finally:
+        for s_ in sims:
+            s_.close()

@@ -3,6 +3,7 @@
 // device-side tables (far-delivery event lists, temporal-kernel segment table), and issues
 // the step loop as CUDA graphs of (one LGN launch + K V1 launches + a step-counter bump).
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1762,6 +1763,152 @@ static int flush_delivery(pv1_plan *p) {
     PV1_CUDA(p, launch_v1_step(p->vp, p->d_stepBase, 0, p->d_lgnRing, p->lgnSlots, 1, 0, p->stream));
     p->pending = false;
     return check_device_error(p);
+}
+
+// ---- checkpoints ----
+// Everything that a step reads from the steps before it: the neuron state and generators,
+// the last two spike-word rows, the delayed-event rings with their spiker lists and flags,
+// the far-failure ring and engines, and the LGN cells' integrals and generators.  The
+// delivery of the last step is applied first, so a checkpoint never holds a pending one.
+namespace {
+
+struct CkptHeader {
+    char magic[8];
+    uint32_t version, nV1, nLGN, ngFF, ngE, ngI;
+    int32_t farDepth, sDepth, farOn, farPullOn, nItems, pad;
+    int64_t step;
+    uint64_t cfgHash, bytes;
+};
+static_assert(offsetof(CkptHeader, step) == 56, "the step field sits at byte 56 of a checkpoint");
+
+uint64_t fnv1a(const void *data, size_t n, uint64_t h = 1469598103934665603ull) {
+    const unsigned char *b = (const unsigned char *)data;
+    for (size_t i = 0; i < n; i++) {
+        h ^= b[i];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
+
+void ckpt_items(pv1_plan *p, std::vector<std::pair<void *, size_t>> &items) {
+    const pv1_v1_config &c = p->cfg;
+    V1Params &v = p->vp;
+    const size_t n = p->nV1, f = sizeof(float);
+    items.clear();
+    auto add = [&](void *ptr, size_t bytes) {
+        if (ptr && bytes) items.emplace_back(ptr, bytes);
+    };
+    add(v.v, n * f);
+    add(v.w, n * f);
+    add(v.tBack, n * f);
+    add(v.dep, n * f);
+    add(v.gFF, c.ngFF * n * f);
+    add(v.hFF, c.ngFF * n * f);
+    add(v.gE, c.ngE * n * f);
+    add(v.hE, c.ngE * n * f);
+    add(v.gI, c.ngI * n * f);
+    add(v.hI, c.ngI * n * f);
+    add(v.lastNoise, n * f);
+    add(v.rGenCond, n * sizeof(curandStateMRG32k3a));
+    add(v.rNoisy, n * sizeof(curandStateMRG32k3a));
+    add(v.sInfo, 2 * n * f);
+    const size_t ring = (size_t)v.farDepth * (c.ngE + c.ngI) * 2 * n * sizeof(unsigned long long);
+    if (v.farOn) {
+        add(v.farAcc, ring);
+        if (v.nearOn) add(v.nearAcc, ring);
+        add(v.farFlag, 3 * sizeof(int));
+        add(v.farList, 3 * n * sizeof(int4));
+        add(v.farCount, 3 * sizeof(int));
+    }
+    if (v.farPullOn) {
+        add(v.sRing, (size_t)v.sDepth * n * f);
+        add(v.eng, n * sizeof(unsigned));
+        add(v.farPull, (size_t)(c.ngE + c.ngI) * 2 * n * f);
+        add(v.pullFlag, 3 * sizeof(int));
+    }
+    add(p->lp.leftTimeRate, p->nLGN * f);
+    add(p->lp.lastNegLogRand, p->nLGN * f);
+    add(p->lp.state, p->nLGN * sizeof(curandStateMRG32k3a));
+}
+
+CkptHeader ckpt_header(pv1_plan *p, const std::vector<std::pair<void *, size_t>> &items) {
+    CkptHeader h{};
+    memcpy(h.magic, "PV1CKPT", 8);
+    h.version = 1;
+    h.nV1 = (uint32_t)p->nV1;
+    h.nLGN = (uint32_t)p->nLGN;
+    h.ngFF = p->cfg.ngFF;
+    h.ngE = p->cfg.ngE;
+    h.ngI = p->cfg.ngI;
+    h.farDepth = p->vp.farOn ? p->vp.farDepth : 0;
+    h.sDepth = p->vp.farPullOn ? p->vp.sDepth : 0;
+    h.farOn = p->vp.farOn;
+    h.farPullOn = p->vp.farPullOn;
+    h.nItems = (int32_t)items.size();
+    h.step = p->step;
+    h.cfgHash = fnv1a(&p->cfg, sizeof(p->cfg));
+    uint64_t bytes = sizeof(CkptHeader);
+    for (auto &it : items) bytes += it.second;
+    h.bytes = bytes;
+    return h;
+}
+
+}  // namespace
+
+int pv1_checkpoint_size(pv1_plan *p, uint64_t *bytes) {
+    if (!p || !bytes) return PV1_E_ARG;
+    if (!p->haveState || !p->haveRng || !p->lgnReady) return fail(p, PV1_E_STATE, "plan not initialised");
+    std::vector<std::pair<void *, size_t>> items;
+    ckpt_items(p, items);
+    *bytes = ckpt_header(p, items).bytes;
+    return PV1_OK;
+}
+
+int pv1_checkpoint_save(pv1_plan *p, void *buf, uint64_t bytes) {
+    if (!p || !buf) return PV1_E_ARG;
+    if (!p->haveState || !p->haveRng || !p->lgnReady) return fail(p, PV1_E_STATE, "plan not initialised");
+    int r = flush_delivery(p);
+    if (r) return r;
+    std::vector<std::pair<void *, size_t>> items;
+    ckpt_items(p, items);
+    const CkptHeader h = ckpt_header(p, items);
+    if (bytes < h.bytes) return fail(p, PV1_E_ARG, "checkpoint buffer too small (pv1_checkpoint_size)");
+    char *out = (char *)buf;
+    memcpy(out, &h, sizeof(h));
+    size_t off = sizeof(h);
+    for (auto &it : items) {
+        PV1_CUDA(p, cudaMemcpyAsync(out + off, it.first, it.second, cudaMemcpyDeviceToHost, p->stream));
+        off += it.second;
+    }
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    return PV1_OK;
+}
+
+int pv1_checkpoint_load(pv1_plan *p, const void *buf, uint64_t bytes) {
+    if (!p || !buf || bytes < sizeof(CkptHeader)) return PV1_E_ARG;
+    if (!p->haveState || !p->haveRng || !p->lgnReady) return fail(p, PV1_E_STATE, "plan not initialised");
+    CkptHeader h;
+    memcpy(&h, buf, sizeof(h));
+    std::vector<std::pair<void *, size_t>> items;
+    ckpt_items(p, items);
+    CkptHeader mine = ckpt_header(p, items);
+    if (memcmp(h.magic, "PV1CKPT", 8) != 0 || h.version != 1) return fail(p, PV1_E_ARG, "not a checkpoint");
+    if (h.cfgHash != mine.cfgHash || h.nV1 != mine.nV1 || h.nLGN != mine.nLGN || h.farDepth != mine.farDepth ||
+        h.sDepth != mine.sDepth || h.farOn != mine.farOn || h.farPullOn != mine.farPullOn ||
+        h.nItems != mine.nItems || h.bytes != mine.bytes || bytes < h.bytes)
+        return fail(p, PV1_E_ARG, "checkpoint of a different configuration or network");
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    const char *in = (const char *)buf;
+    size_t off = sizeof(h);
+    for (auto &it : items) {
+        PV1_CUDA(p, cudaMemcpyAsync(it.first, in + off, it.second, cudaMemcpyHostToDevice, p->stream));
+        off += it.second;
+    }
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    p->step = h.step;
+    p->pending = false;
+    drop_graph(p);
+    return PV1_OK;
 }
 
 int pv1_fetch_records(pv1_plan *p, uint64_t step0, uint32_t n, float *raw, float *lgn_sp, float *lgn_fr) {

@@ -6,9 +6,11 @@ rules (src/patch.cu:612-1060 options, 3313-3700 connectivity, 4100-4220 tonic dr
 LGN->V1 lists, 4405-4560 initial state), runs the steps on the GPU and writes rawData,
 LGN_fr, LGN_sp and patchV1_cfg with the reference's headers and record order.
 
-Supported: magno (ON/OFF) LGN read from the LGN parameter file (useNewLGN = false), flat
-retina, learning = 0, no gap junctions, no orientation boost (nOri = 0), no snapshot
-restore, minimal = false.  Anything else raises ConfigError naming the key.
+Supported: magno and parvo LGN cells in one or two eyes read from the LGN parameter file
+(useNewLGN = false), flat or curved retina, initial spikes, synaptic failure (not on
+distance-delayed near synapses), learning = 0, no gap junctions, no orientation boost
+(nOri = 0), snapshots of this build only (resume with asInit = false), minimal = false.
+Anything else raises ConfigError naming the key.
 """
 from __future__ import annotations
 
@@ -76,12 +78,42 @@ def _check_supported(c: Config):
         bad.append("virtual_LGN / LGN_switch / reverseInput")
     if c.minimal:
         bad.append("minimal = true (sampled output)")
-    if c.fSnapshot:
-        bad.append("fSnapshot (restore)")
+    if c.fSnapshot and c.asInit:
+        bad.append("asInit = true (a snapshot as the initial state of a new run; resume with asInit = false)")
+    if c.fSnapshot and (c.snapshot_suffix or "") != (c.output_suffix or ""):
+        raise ConfigError("to use snapshot to resume simulation, it needs to have the same suffix as the output_suffix")
     if c.manual:
         bad.append("manual connections")
     if bad:
         raise ConfigError("not supported by this build: " + "; ".join(bad))
+
+
+def _restore(sim, c: Config) -> int:
+    """Loads the checkpoint named by fSnapshot (inputFolder + name + '_' + snapshot_suffix +
+    '.bin', src/patch.cu:438-445, 611-613) and returns its step."""
+    from .cfg import _prefixed
+    path = _prefixed(c.inputFolder, c.fSnapshot) + "_" + (c.snapshot_suffix or "") + ".bin"
+    buf = np.fromfile(path, np.uint8)
+    if buf[:8].tobytes() != b"PV1CKPT\0":
+        raise ConfigError(f"{path}: not a checkpoint written by this build (the reference's own snapshot "
+                          "layout is not read)")
+    sim.restore(buf)
+    return sim.step
+
+
+def _write_snapshot(sim, c: Config, previous, log):
+    """snapShot_<time><output suffix> in the output folder (the reference writes it in the
+    working directory, src/patch.cu:6793-6912); the previous one is removed when
+    delPrevSnapshot."""
+    import os
+    import time
+    from .cfg import _prefixed
+    name = _prefixed(c.outputFolder, f"snapShot_{int(time.time())}") + "_" + (c.output_suffix or "") + ".bin"
+    sim.checkpoint().tofile(name)
+    if previous and previous != name and c.delPrevSnapshot and os.path.exists(previous):
+        os.remove(previous)
+    log(f"saved a snapshot in {name}")
+    return name
 
 
 def _sp0(c: Config, nTypeE: int, nTypeI: int):
@@ -310,12 +342,18 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
             lsp = FM.LgnSpWriter(P.lgn_sp, spec.dt, m.nt, nLGN)
         if flags:
             sim.set_record(flags, chunk + 1)
+        base = 0
+        if c.fSnapshot:
+            base = _restore(sim, c)
+            log(f"resumed from step {base}")
         done = 0
+        interval = max(int(c.snapshotInterval), 1)
+        last_snap = None
         while done < m.nt:
-            k = min(chunk, m.nt - done)
+            k = min(chunk, m.nt - done, interval - done % interval)
             sim.run(k)
             if flags:
-                r, sp, fr = sim.fetch_records(done, k, raw=raw is not None, lgn_sp=lsp is not None,
+                r, sp, fr = sim.fetch_records(base + done, k, raw=raw is not None, lgn_sp=lsp is not None,
                                               lgn_fr=lfr is not None)
                 if raw is not None:
                     raw.write(r)
@@ -324,6 +362,8 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
                 if lfr is not None:
                     lfr.write(fr)
             done += k
+            if not c.minimal and (done % interval == 0 or done == m.nt):
+                last_snap = _write_snapshot(sim, c, last_snap, log)
         for w in (raw, lsp, lfr):
             if w is not None:
                 w.close()

@@ -454,6 +454,22 @@ class Simulation:
         N.check(self.plan, N.lib.pv1_get_state(self.plan, N.ST[name], N.fptr(out)), f"pv1_get_state({name})")
         return out
 
+    def checkpoint(self) -> np.ndarray:
+        """The plan's evolving state and step count (pv1_checkpoint_save) as bytes."""
+        size = C.c_uint64()
+        N.check(self.plan, N.lib.pv1_checkpoint_size(self.plan, C.byref(size)), "pv1_checkpoint_size")
+        buf = np.empty(size.value, np.uint8)
+        N.check(self.plan, N.lib.pv1_checkpoint_save(self.plan, buf.ctypes.data_as(C.c_void_p), size.value),
+                "pv1_checkpoint_save")
+        return buf
+
+    def restore(self, buf: np.ndarray):
+        """Continues from a checkpoint of a plan of the same configuration and network."""
+        b = np.ascontiguousarray(buf, dtype=np.uint8)
+        N.check(self.plan, N.lib.pv1_checkpoint_load(self.plan, b.ctypes.data_as(C.c_void_p), b.size),
+                "pv1_checkpoint_load")
+        self.step = int(np.frombuffer(b[56:64].tobytes(), np.int64)[0])   # the header's step field
+
     def put_state(self, name: str, arr: np.ndarray):
         a = np.ascontiguousarray(arr, dtype=f32)
         N.check(self.plan, N.lib.pv1_put_state(self.plan, N.ST[name], N.fptr(a)), f"pv1_put_state({name})")

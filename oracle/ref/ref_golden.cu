@@ -9,6 +9,7 @@
 //   ref_golden denorm   in out   find_denorm (src/util/util.h:251-279)
 //   ref_golden far      in out   fill_fSpikeTrain (src/stats.cu:114-126) + recal_G_vec
 //                                (src/coredynamics.cu:181-372) over a spike sequence
+//   ref_golden farfail  in out   the same with synaptic failure (host engines) per chunk
 // Inputs and outputs are raw little-endian arrays; tests/golden/make_golden.py writes and
 // reads them.  The AdEx struct is declared __device__ in the reference; the redefinition
 // below makes its members host-callable without changing their arithmetic.
@@ -105,12 +106,27 @@ static int mode_denorm(const char *in, const char *out) {
     return 0;
 }
 
-static int mode_far(const char *in, const char *out) {
+// far: synaptic failure off, one chunk.  farfail: the header's 8th word is nChunk, followed by
+// the first engine's seed (uint64, engine i seeded seed + i as src/patch.cu:4224-4228),
+// synFail[4] and synPerCon[4]; recal_G_vec is called per chunk of blocks as the step loop
+// does (src/patch.cu:6597-6648, chunks split as :3430-3437).
+static int mode_far(const char *in, const char *out, bool failure) {
     std::ifstream f(in, std::ios::binary);
     int32_t hd[8];
     f.read(reinterpret_cast<char *>(hd), sizeof(hd));
     const Size nV1 = hd[0], bs = hd[1], nE = hd[2], ngE = hd[3], ngI = hd[4], T = hd[5];
     const size_t nnz = (size_t)hd[6];
+    uint64_t seed0 = 0;
+    Float synFail[4] = {0, 0, 0, 0}, synPerCon[4] = {1, 1, 1, 1};
+    const Size nblock = nV1 / bs;
+    Size nChunk = 1;
+    if (failure) {
+        nChunk = hd[7] > 0 ? (Size)hd[7] : 1;
+        if (nChunk > nblock) nChunk = nblock;
+        f.read(reinterpret_cast<char *>(&seed0), sizeof(seed0));
+        f.read(reinterpret_cast<char *>(synFail), sizeof(synFail));
+        f.read(reinterpret_cast<char *>(synPerCon), sizeof(synPerCon));
+    }
     float pr[2 + 8 + 4 + 4];
     f.read(reinterpret_cast<char *>(pr), sizeof(pr));
     const Float dt = pr[0], speed = pr[1];
@@ -142,8 +158,10 @@ static int mode_far(const char *in, const char *out) {
         }
     ConductanceShape condE(rE, dE, ngE), condI(rI, dI, ngI);
     Size typeAcc[2] = {nE, bs};
-    Float synFail[4] = {0, 0, 0, 0}, synPerCon[4] = {1, 1, 1, 1};
     std::vector<std::default_random_engine> gen(nV1);
+    if (failure)
+        for (Size i = 0; i < nV1; i++) gen[i].seed(seed0 + i);
+    const Size split = nblock % nChunk, rem = nblock / nChunk, maxC = rem + (split > 0 ? 1 : 0);
     std::vector<Float> og(nV1 * 2, 0.f), oh(nV1 * 2, 0.f);
     std::vector<float> y;
     std::vector<Float> gE(ngE * nV1), hE(ngE * nV1), gI(ngI * nV1), hI(ngI * nV1);
@@ -154,9 +172,27 @@ static int mode_far(const char *in, const char *out) {
         std::fill(gI.begin(), gI.end(), 0.f);
         std::fill(hI.begin(), hI.end(), 0.f);
         if (farSpiked) {
-            recal_G_vec(fsp, depth, slot, og.data(), oh.data(), nVec, vecID, conVec, delayVec, gE.data(), gI.data(),
-                        hE.data(), hI.data(), pE, pI, typeAcc, gen.data(), synFail, synPerCon, dt, condE, condI, ngE,
-                        ngI, 0, 2, nE, bs - nE, nV1, speed, nV1 / bs, false, t, bs);
+            Size block_offset = 0;
+            for (Size q = 0; q < nChunk; q++) {
+                const Size chunkSize = q < split ? maxC : rem;
+                const size_t cn = (size_t)chunkSize * bs;
+                std::vector<Float> cgE(ngE * cn), chE(ngE * cn), cgI(ngI * cn), chI(ngI * cn);
+                recal_G_vec(fsp, depth, slot, og.data(), oh.data(), nVec, vecID, conVec, delayVec, cgE.data(),
+                            cgI.data(), chE.data(), chI.data(), pE, pI, typeAcc, gen.data(), synFail, synPerCon, dt,
+                            condE, condI, ngE, ngI, block_offset, 2, nE, bs - nE, nV1, speed, chunkSize, false, t, bs);
+                const size_t o = (size_t)block_offset * bs;
+                for (Size ig = 0; ig < ngE; ig++)
+                    for (size_t j = 0; j < cn; j++) {
+                        gE[ig * nV1 + o + j] = cgE[ig * cn + j];
+                        hE[ig * nV1 + o + j] = chE[ig * cn + j];
+                    }
+                for (Size ig = 0; ig < ngI; ig++)
+                    for (size_t j = 0; j < cn; j++) {
+                        gI[ig * nV1 + o + j] = cgI[ig * cn + j];
+                        hI[ig * nV1 + o + j] = chI[ig * cn + j];
+                    }
+                block_offset += chunkSize;
+            }
         } else {
             for (Size i = 0; i < nV1; i++)
                 for (Size j = 0; j < nVec[i]; j++) slot[i][j] = (slot[i][j] + 1) % depth[i][j];
@@ -172,13 +208,14 @@ static int mode_far(const char *in, const char *out) {
 
 int main(int argc, char **argv) {
     if (argc != 4) {
-        fprintf(stderr, "usage: ref_golden cond|adex|logistic|denorm|far in out\n");
+        fprintf(stderr, "usage: ref_golden cond|adex|logistic|denorm|far|farfail in out\n");
         return 2;
     }
     if (!strcmp(argv[1], "cond")) return mode_cond(argv[2], argv[3]);
     if (!strcmp(argv[1], "adex")) return mode_adex(argv[2], argv[3]);
     if (!strcmp(argv[1], "logistic")) return mode_logistic(argv[2], argv[3]);
     if (!strcmp(argv[1], "denorm")) return mode_denorm(argv[2], argv[3]);
-    if (!strcmp(argv[1], "far")) return mode_far(argv[2], argv[3]);
+    if (!strcmp(argv[1], "far")) return mode_far(argv[2], argv[3], false);
+    if (!strcmp(argv[1], "farfail")) return mode_far(argv[2], argv[3], true);
     return 2;
 }

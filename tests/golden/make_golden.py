@@ -2,7 +2,7 @@
 
 The outputs come from oracle/_ref/ref_golden, built by oracle/ref/build_ref.sh from the
 reference's sources (ConductanceShape, the AdEx struct, hStatic_nonlinear, find_denorm,
-fill_fSpikeTrain + recal_G_vec).  Run from the repository root, where the reference's
+fill_fSpikeTrain + recal_G_vec, with and without synaptic failure).  Run from the repository root, where the reference's
 sources are readable:  bash oracle/ref/build_ref.sh && python tests/golden/make_golden.py
 """
 import os
@@ -83,6 +83,29 @@ def main():
     out["far_nVec"], out["far_vecID"], out["far_conVec"], out["far_delayVec"] = nVec, vecID, conVec, delayVec
     out["far_sInfo"] = sInfo
     out["far_out"] = res.reshape(T, (ngE + ngI) * 2, nV1)
+    # far delivery with synaptic failure: 3 blocks x 64 in 2 chunks (2 + 1 blocks), host engines
+    nV1 = 192
+    nVec = rng.integers(0, 25, nV1).astype(u32)
+    ids, strs, dels = [], [], []
+    for i in range(nV1):
+        other = np.setdiff1d(np.arange(nV1), np.arange((i // bs) * bs, (i // bs + 1) * bs))
+        c = rng.choice(other, int(nVec[i]), replace=False)
+        ids.append(c)
+        strs.append(rng.lognormal(0, 0.5, len(c)) * np.where(c % bs < nE, 0.01, 0.04))
+        dels.append(rng.uniform(0.0, 1.5, len(c)))
+    vecID = np.concatenate(ids).astype(u32)
+    conVec = np.concatenate(strs).astype(f32)
+    delayVec = np.concatenate(dels).astype(f32)
+    spk = rng.random((T, nV1)) < 0.03
+    sInfo = np.where(spk, 1.0 + rng.random((T, nV1)), rng.uniform(-70, -51, (T, nV1))).astype(f32)
+    hdr = np.array([nV1, bs, nE, ngE, ngI, T, len(vecID), 2], i32)
+    seed0 = np.array([987654], np.uint64)
+    fail = np.array([0.2, 0.3, 0.25, 0.1, 5.0, 7.5, 4.26, 7.88], f32)    # synFail[4], synPerCon[4]
+    res = run("farfail", [hdr, seed0, fail, prm, nVec, vecID, conVec, delayVec, sInfo], f32)
+    out["farfail_hdr"], out["farfail_seed"], out["farfail_fail"] = hdr, seed0, fail
+    out["farfail_nVec"], out["farfail_vecID"] = nVec, vecID
+    out["farfail_conVec"], out["farfail_delayVec"], out["farfail_sInfo"] = conVec, delayVec, sInfo
+    out["farfail_out"] = res.reshape(T, (ngE + ngI) * 2, nV1)
     np.savez_compressed(os.path.join(ROOT, "tests", "golden", "ref_golden.npz"), **out)
     print({k: v.shape for k, v in out.items()})
 

@@ -76,12 +76,10 @@ def test_find_denorm(gold):
         assert find_denorm(int(u1), int(u2), bool(morn)) == (int(d), int(nrm))
 
 
-def test_far_delivery_matches_recal_G_vec(gold):
-    """fill_fSpikeTrain + recal_G_vec over a 120-step spike sequence: the oracle's
-    restatement gives the same far conductances, bit for bit, every step."""
+def _far_replay(gold, key, synFail=None, synPerCon=None, seed=None, nChunk=1):
     import oracle
     from visual_cortex_gb300.model import V1Network, V1Spec
-    nV1, bs, nE, ngE, ngI, T = [int(v) for v in gold["far_hdr"][:6]]
+    nV1, bs, nE, ngE, ngI, T = [int(v) for v in gold[key + "_hdr"][:6]]
     prm = gold["far_prm"]
     spec = V1Spec(nblock=nV1 // bs, blockSize=bs, typeAcc=[nE, bs], nTypeE=1, ngFF=1, ngE=ngE, ngI=ngI,
                   dt=float(prm[0]), riseFF=[1.0], decayFF=[5.0], riseE=[float(prm[2]), float(prm[3])],
@@ -89,23 +87,40 @@ def test_far_delivery_matches_recal_G_vec(gold):
                   vR=[-60.0] * 2, vThres=[-50.0] * 2, gL=[0.05] * 2, C=[1.0] * 2, tRef=[2.0] * 2,
                   vT=[-50.0] * 2, deltaT=[1.0] * 2, tau_w=[150.0] * 2, a=[0.0] * 2, b=[0.0] * 2,
                   pFF=[1.0, 1.0], pE=[float(v) for v in prm[10:14]], pI=[float(prm[14]), float(prm[15])],
-                  synFail=[0.0] * 4, synPerCon=[1.0] * 4, synFailFF=[0.0] * 2, synPerConFF=[1.0] * 2,
-                  noisyDep=[0.0] * 2, noFarDelay=0, speedOfThought=float(prm[1]))
+                  synFail=synFail or [0.0] * 4, synPerCon=synPerCon or [1.0] * 4, synFailFF=[0.0] * 2,
+                  synPerConFF=[1.0] * 2, noisyDep=[0.0] * 2, noFarDelay=0, speedOfThought=float(prm[1]))
     u32 = np.uint32
     net = V1Network(nLGNperV1=np.zeros(nV1, u32), lgnId=np.zeros((1, nV1), u32), sLGN=np.zeros((1, nV1), f32),
                     nNearNB=np.zeros(spec.nblock, u32), nbId=np.zeros((spec.nblock, 1), u32),
-                    conMat=np.zeros((spec.nblock, 1, bs, bs), f32), nVec=gold["far_nVec"],
-                    vecID=gold["far_vecID"], conVec=gold["far_conVec"], delayVec=gold["far_delayVec"],
+                    conMat=np.zeros((spec.nblock, 1, bs, bs), f32), nVec=gold[key + "_nVec"],
+                    vecID=gold[key + "_vecID"], conVec=gold[key + "_conVec"], delayVec=gold[key + "_delayVec"],
                     tonicDep=np.zeros(nV1, f32))
     vo = oracle.V1Oracle(spec, net)
+    if seed is not None:
+        vo.set_far_failure(seed, nChunk)
     L = oracle.lib()
     zE, zI = np.zeros(ngE * nV1, f32), np.zeros(ngI * nV1, f32)
     for t in range(T):
         for name, z in (("gE", zE), ("hE", zE), ("gI", zI), ("hI", zI)):
             vo.put(name, z)
-        vo.put("sInfo", gold["far_sInfo"][t])
+        vo.put("sInfo", gold[key + "_sInfo"][t])
         L.orc_v1_deliver_far(vo.h)
         got = np.concatenate([vo.get("gE").reshape(ngE, nV1), vo.get("hE").reshape(ngE, nV1),
                               vo.get("gI").reshape(ngI, nV1), vo.get("hI").reshape(ngI, nV1)])
-        np.testing.assert_array_equal(got, gold["far_out"][t], err_msg=f"step {t}")
-    assert np.abs(gold["far_out"]).sum() > 0
+        np.testing.assert_array_equal(got, gold[key + "_out"][t], err_msg=f"step {t}")
+    assert np.abs(gold[key + "_out"]).sum() > 0
+
+
+def test_far_delivery_matches_recal_G_vec(gold):
+    """fill_fSpikeTrain + recal_G_vec over a 120-step spike sequence: the oracle's
+    restatement gives the same far conductances, bit for bit, every step."""
+    _far_replay(gold, "far")
+
+
+def test_far_failure_matches_recal_G_vec(gold):
+    """The same with synaptic failure on every pair: the reference's host engines (seeded
+    seed + i) drawn through one normal_distribution per chunk call, 3 blocks in chunks of 2
+    and 1; the oracle's libstdc++ restatement reproduces every draw, bit for bit."""
+    fail = [float(v) for v in gold["farfail_fail"]]
+    _far_replay(gold, "farfail", synFail=fail[:4], synPerCon=fail[4:], seed=int(gold["farfail_seed"][0]),
+                nChunk=int(gold["farfail_hdr"][7]))

@@ -21,6 +21,7 @@ import argparse
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -51,7 +52,9 @@ class Clocks:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_dev{device}.csv")
+        # the raw samples: PV1_CLOCKS_DIR if set (to keep them), else a temporary folder
+        folder = os.environ.get("PV1_CLOCKS_DIR") or tempfile.mkdtemp(prefix="pv1_clocks_")
+        self.path = os.path.join(folder, f"clocks_dev{device}.csv")
 
     def __enter__(self):
         try:

@@ -252,7 +252,7 @@ typedef struct pv1_init_record {
  * src/coredynamics.cu:2497-2510, after rand_spInit wrote it at :85-116); with noDelay = 0 it
  * reads the ring with slot 0 as the newest (src/patch.cu:5760-5770) while the loop takes slot
  * trainDepth-1 as the step before the first.  The reference numbers the initial spikers of a
- * block in the order of its atomicAdd_block returns; this build numbers them by thread index.
+ * block in the order of its atomicAdd_block returns; this library numbers them by thread index.
  * rec may be NULL. */
 int pv1_v1_init_spikes(pv1_plan *plan, uint64_t seed, uint32_t trainDepth, const float *sp0,
                        uint32_t SCsplit, pv1_init_record *rec);

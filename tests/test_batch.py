@@ -58,7 +58,8 @@ def test_batch_in_pieces_with_noise(native):
     base = synth.make_workload("nz", seed=9, nblock=2, n_lgn=512, width=64, height=64, nt=0,
                                far_partners=50, adex_inh=True, nFrame=60, noisyDep=(0.2, 0.2),
                                synFailFF=(0.1, 0.1), synFail=(0.1, 0.1, 0.1, 0.1))
-    # far synapses cannot fail in this build: drop them for the failure case
+    # batched trials take no far synaptic failure (its host-engine path runs one plan at a time):
+    # drop the far synapses for the failure case
     import dataclasses
     net = dataclasses.replace(base.net, nVec=np.zeros_like(base.net.nVec),
                               vecID=np.zeros(0, np.uint32), conVec=np.zeros(0, np.float32),

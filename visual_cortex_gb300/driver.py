@@ -9,7 +9,7 @@ LGN_fr, LGN_sp and patchV1_cfg with the reference's headers and record order.
 Supported: magno and parvo LGN cells in one or two eyes read from the LGN parameter file
 (useNewLGN = false), flat or curved retina, initial spikes, synaptic failure (not on
 distance-delayed near synapses), learning = 0, no gap junctions, no orientation boost
-(nOri = 0), snapshots of this build only (resume with asInit = false), minimal = false.
+(nOri = 0), snapshots of this library only (resume with asInit = false), minimal = false.
 Anything else raises ConfigError naming the key.
 """
 from __future__ import annotations
@@ -85,7 +85,7 @@ def _check_supported(c: Config):
     if c.manual:
         bad.append("manual connections")
     if bad:
-        raise ConfigError("not supported by this build: " + "; ".join(bad))
+        raise ConfigError("not supported by this library: " + "; ".join(bad))
 
 
 def _restore(sim, c: Config) -> int:
@@ -95,7 +95,7 @@ def _restore(sim, c: Config) -> int:
     path = _prefixed(c.inputFolder, c.fSnapshot) + "_" + (c.snapshot_suffix or "") + ".bin"
     buf = np.fromfile(path, np.uint8)
     if buf[:8].tobytes() != b"PV1CKPT\0":
-        raise ConfigError(f"{path}: not a checkpoint written by this build (the reference's own snapshot "
+        raise ConfigError(f"{path}: not a checkpoint written by this library (the reference's own snapshot "
                           "layout is not read)")
     sim.restore(buf)
     return sim.step

@@ -1,7 +1,7 @@
 """CPU oracle of the patchV1 hot path -- TEST INFRASTRUCTURE, not part of the product.
 
 Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of bench.py use this package,
-as the checker.  pv1_oracle.c restates the reference's kernels on the CPU; this module builds
+as the oracle the GPU results are compared with.  pv1_oracle.c restates the reference's kernels on the CPU; this module builds
 it with gcc and drives it in the reference's own per-step order
 (src/patch.cu:5966-6880): LGN convolution -> LGN spikes -> V1 step -> near delivery -> far
 delivery.  Random draws are supplied by the caller (recorded from the GPU run under test):

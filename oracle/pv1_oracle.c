@@ -1,7 +1,7 @@
 /*
  * pv1_oracle.c -- CPU restatement of the patchV1 simulation hot path.
  *
- * TEST INFRASTRUCTURE: this file is the checker for the GPU library.  Only the tests, the
+ * TEST INFRASTRUCTURE: this file is the oracle of the GPU library.  Only the tests, the
  * smoke check and the CPU-baseline leg of the benchmark load it; the product path never
  * does.  It follows the reference's own structure (one pass per kernel, per-synapse delay
  * rings for the far synapses, the sample-by-sample temporal convolution) rather than the GPU

@@ -1,4 +1,4 @@
-"""Unrolled PyTorch surrogate model: the checker for the CUDA adjoint (test infrastructure).
+"""Unrolled PyTorch surrogate model the CUDA adjoint is tested against (test infrastructure).
 
 The same step as visual_cortex_gb300/csrc/pv1_adjoint.cu, written with the same float32
 operation order (sums over LGN synapses and over spiking I neurons in ascending order), so

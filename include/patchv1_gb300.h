@@ -307,6 +307,18 @@ int pv1_fetch_records(pv1_plan *plan, uint64_t step0, uint32_t n, float *raw,
                                failure plans; read only), added at the next step's delivery */
 /* Copies one state array to the host (waits for queued work). */
 int pv1_get_state(pv1_plan *plan, int which, float *out);
+/* Framed output of the physical V1 sheet (framePhyV1output): pixelizeOutput
+ * (src/stats.cu:4-36) as the step loop runs it (src/patch.cu:6727-6790).  Pixel q holds the
+ * neurons pixIds[pixOff[q] .. pixOff[q+1]) (getUnderlyingID's order, src/stats.cuh:26-60);
+ * frames are ot steps long, counted from the plan's step at setup, and each step adds to a
+ * pixel (sum of floor(sInfo) over its neurons with sInfo >= 0) / (m odt).  Needs the
+ * PV1_REC_SPIKES record.  collect processes steps [step0, step0+n) in order, continuing the
+ * previous call, and writes the frames completed among them to frames [k][nPixel], k in
+ * *nFrames. */
+int pv1_frames_setup(pv1_plan *plan, uint32_t nPixel, const uint32_t *pixOff, const uint32_t *pixIds,
+                     uint32_t ot, float odt);
+int pv1_frames_collect(pv1_plan *plan, uint64_t step0, uint32_t n, float *frames, uint32_t *nFrames);
+
 /* Checkpoints: the plan's whole evolving state (neuron state and generators, spike-word
  * rows, delayed-event rings, far-failure engines, LGN integrals and generators) with the step
  * count, so that a plan of the same configuration and network that loads it continues bit

@@ -166,3 +166,60 @@ def test_snapshot_resume_continues_the_run(written, native):
     with pytest.raises(cfg.ConfigError, match="asInit"):
         driver.build(cfg.load(["-c", fn, "--fSnapshot", "!" + out1 + name, "--snapshot_suffix", "s",
                                "--output_suffix", "s"]))
+
+
+def test_frame_geometry_and_pixels():
+    """getUnderlyingID's pixel lists: every neuron in exactly one pixel, in neuron order, the
+    far edge folded into the last pixel."""
+    x = np.array([0.0, 1.0, 0.5, 0.26, 0.24, 1.0])
+    y = np.array([0.0, 1.0, 0.5, 0.0, 0.99, 0.0])
+    off, ids = FM.underlying_ids(x, y, 4, 2, 0.0, 1.0, 0.0, 1.0)
+    assert off[-1] == 6 and len(off) == 9
+    cells = {q: list(ids[off[q]:off[q + 1]]) for q in range(8) if off[q + 1] > off[q]}
+    assert cells == {0: [0], 1: [3], 3: [5], 4: [4], 6: [2], 7: [1]}
+
+
+@pytest.mark.gpu
+def test_phy_frames_match_the_raster(written, native):
+    """framePhyV1output: the outputFrame of a driver run equals pixelizeOutput's sums
+    recomputed on the host from the run's own rawData spike words."""
+    import os
+    import shutil
+    wl, fn = written
+    d = os.path.join(os.path.dirname(fn), "frames") + "/"
+    os.makedirs(d, exist_ok=True)
+    lgn = cfg.resolve_paths(cfg.load(["-c", fn])).lgn
+    shutil.copy(lgn, d + os.path.basename(lgn))
+    c = cfg.load(["-c", fn, "--outputFolder", d, "--framePhyV1output", "true", "--dot", "1.0",
+                  "--phyWidth_scale", "0.25"])
+    m = driver.run(c, chunk=40, log=lambda *_: None)
+    P = cfg.resolve_paths(c)
+    _, raw = FM.read_raw(P.raw)
+    with open(d + "outputFrame.bin", "rb") as f:
+        dt = np.fromfile(f, np.float32, 1)[0]
+        ot, nkind, W, H = np.fromfile(f, np.uint32, 4)
+        frames = np.fromfile(f, np.float32)
+    assert nkind == 1 and ot == 8 and dt == np.float32(c.dt)
+    frames = frames.reshape(-1, H * W)
+    x0, xs, y0, ys = FM.read_v1_allpos_spans(P.v1_allpos)
+    _, _, pos = FM.read_v1_allpos(P.v1_allpos)
+    off, ids = FM.underlying_ids(pos[:, 0], pos[:, 1], int(W), int(H), x0, xs, y0, ys)
+    odt = np.float32(float(np.float32(np.float32(ot) * np.float32(c.dt))) / 1000.0)
+    sI = raw[:, :m.spec.nV1]
+    want = []
+    acc = np.zeros(H * W, np.float32)
+    for t in range(sI.shape[0]):
+        if t % ot == 0:
+            acc[:] = 0
+        for q in range(H * W):
+            mq = int(off[q + 1] - off[q])
+            if mq:
+                v = np.float32(0)
+                for j in ids[off[q]:off[q + 1]]:
+                    if sI[t, j] >= 0:
+                        v = np.float32(v + np.floor(sI[t, j]))
+                acc[q] = np.float32(acc[q] + np.float32(v / np.float32(np.float32(mq) * odt)))
+        if (t + 1) % ot == 0:
+            want.append(acc.copy())
+    np.testing.assert_array_equal(frames, np.array(want))
+    assert frames.sum() > 0

@@ -37,6 +37,12 @@ struct pv1_plan {
     long long *d_stepBase = nullptr;
     bool haveLGNsyn = false, haveNear = false, haveState = false, haveRng = false;
     bool haveFarEng = false;    // far failure: engines seeded (pv1_v1_far_failure_engines)
+    // framed output of the physical V1 sheet
+    unsigned *d_pixOff = nullptr, *d_pixIds = nullptr;
+    float *d_frameAcc = nullptr, *d_frameOut = nullptr;
+    int nPixel = 0, frameOt = 0, frameOutCap = 0;
+    float frameOdt = 0.f;
+    long long frameT0 = 0;
     bool lgnReady = false, stimReady = false;
     pv1_lgn_config lcfg{};
     int nMagno = 0, nLGN = 0, mSample = 0;
@@ -1763,6 +1769,58 @@ static int flush_delivery(pv1_plan *p) {
     PV1_CUDA(p, launch_v1_step(p->vp, p->d_stepBase, 0, p->d_lgnRing, p->lgnSlots, 1, 0, p->stream));
     p->pending = false;
     return check_device_error(p);
+}
+
+// ---- framed output ----
+int pv1_frames_setup(pv1_plan *p, uint32_t nPixel, const uint32_t *pixOff, const uint32_t *pixIds, uint32_t ot,
+                     float odt) {
+    if (!p || !nPixel || !pixOff || ot < 1 || !(odt > 0)) return PV1_E_ARG;
+    const uint32_t nIds = pixOff[nPixel];
+    if (nIds && !pixIds) return PV1_E_ARG;
+    for (uint32_t q = 0; q < nPixel; q++)
+        if (pixOff[q + 1] < pixOff[q]) return fail(p, PV1_E_ARG, "pixel offsets must not decrease");
+    for (uint32_t j = 0; j < nIds; j++)
+        if (pixIds[j] >= (uint32_t)p->nV1) return fail(p, PV1_E_ARG, "pixel neuron id out of range");
+    for (void *q : {(void *)p->d_pixOff, (void *)p->d_pixIds, (void *)p->d_frameAcc, (void *)p->d_frameOut})
+        if (q) free_one(p, q);
+    p->d_frameOut = nullptr;
+    p->frameOutCap = 0;
+    int r = dev_upload(p, &p->d_pixOff, pixOff, (size_t)nPixel + 1);
+    if (!r) r = dev_upload(p, &p->d_pixIds, nIds ? pixIds : pixOff, nIds ? nIds : 1);
+    if (!r) r = dev_alloc(p, &p->d_frameAcc, nPixel);
+    if (r) return r;
+    p->nPixel = (int)nPixel;
+    p->frameOt = (int)ot;
+    p->frameOdt = odt;
+    p->frameT0 = p->step;
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    return PV1_OK;
+}
+
+int pv1_frames_collect(pv1_plan *p, uint64_t step0, uint32_t n, float *frames, uint32_t *nFrames) {
+    if (!p || !nFrames) return PV1_E_ARG;
+    if (!p->d_pixOff) return fail(p, PV1_E_STATE, "call pv1_frames_setup first");
+    if (!p->vp.recSpk) return fail(p, PV1_E_STATE, "framed output reads the PV1_REC_SPIKES record");
+    if (step0 + n > (uint64_t)p->step) return fail(p, PV1_E_ARG, "steps not run yet");
+    if ((uint64_t)p->step - step0 > (uint64_t)p->recSlots) return fail(p, PV1_E_ARG, "spike records already overwritten");
+    uint32_t k = 0;
+    for (uint32_t s = 0; s < n; s++)
+        if (((long long)(step0 + s) - p->frameT0 + 1) % p->frameOt == 0) k++;
+    if (k > 0 && !frames) return PV1_E_ARG;
+    if ((int)k > p->frameOutCap) {
+        if (p->d_frameOut) free_one(p, p->d_frameOut);
+        int r = dev_alloc(p, &p->d_frameOut, (size_t)k * p->nPixel);
+        if (r) return r;
+        p->frameOutCap = (int)k;
+    }
+    PV1_CUDA(p, launch_frames_phy(p->vp.recSpk, p->recSlots, p->nV1, (long long)step0, (int)n, p->frameOt, p->frameT0,
+                                  p->d_pixOff, p->d_pixIds, p->nPixel, p->frameOdt, p->d_frameAcc,
+                                  p->d_frameOut ? p->d_frameOut : p->d_frameAcc, p->stream));
+    if (k) PV1_CUDA(p, cudaMemcpyAsync(frames, p->d_frameOut, (size_t)k * p->nPixel * sizeof(float),
+                                       cudaMemcpyDeviceToHost, p->stream));
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    *nFrames = k;
+    return PV1_OK;
 }
 
 // ---- checkpoints ----

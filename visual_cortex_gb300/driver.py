@@ -78,6 +78,8 @@ def _check_supported(c: Config):
         bad.append("virtual_LGN / LGN_switch / reverseInput")
     if c.minimal:
         bad.append("minimal = true (sampled output)")
+    if c.frameVisV1output or c.frameVisLGNoutput:
+        bad.append("frameVisV1output / frameVisLGNoutput (visual-field frames; framePhyV1output is built)")
     if c.fSnapshot and c.asInit:
         bad.append("asInit = true (a snapshot as the initial state of a new run; resume with asInit = false)")
     if c.fSnapshot and (c.snapshot_suffix or "") != (c.output_suffix or ""):
@@ -86,6 +88,30 @@ def _check_supported(c: Config):
         bad.append("manual connections")
     if bad:
         raise ConfigError("not supported by this library: " + "; ".join(bad))
+
+
+def _setup_frames(sim, c: Config, m: Model, P):
+    """framePhyV1output: the physical-sheet frame geometry of src/patch.cu:2936-2940 and
+    2959-3037 and the frame interval of :580-584, 5471 (float arithmetic as there); returns
+    the outputFrame writer."""
+    from .cfg import _prefixed, _suffix
+    f32 = np.float32
+    width = int(m.stim.frames.shape[-1])
+    phyWidth = int(f32(f32(width) * f32(c.phyWidth_scale)))
+    x0, xspan, y0, yspan = FM.read_v1_allpos_spans(P.v1_allpos)
+    ratio = f32(yspan / xspan)
+    phyHeight = int(math.ceil(f32(ratio * f32(phyWidth))))
+    if phyHeight % 2 == 1:
+        phyHeight += 1
+    ot = int(f32(c.dot) / f32(c.dt))
+    if ot < 1:
+        raise ConfigError("dot must be at least one time step")
+    odt = f32(float(f32(f32(ot) * f32(c.dt))) / 1000.0)
+    _, _, pos = FM.read_v1_allpos(P.v1_allpos)
+    off, ids = FM.underlying_ids(pos[:, 0], pos[:, 1], phyWidth, phyHeight, x0, xspan, y0, yspan)
+    sim.frames_setup(off, ids, ot, float(odt))
+    fn = _prefixed(c.outputFolder, c.fOutputFrame) + _suffix(c.output_suffix)
+    return FM.OutputFrameWriter(fn, c.dt, ot, phyWidth, phyHeight)
 
 
 def _restore(sim, c: Config) -> int:
@@ -340,6 +366,10 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
                                    spec.nI * spec.nblock, spec.hWrite, spec.ngFF, spec.ngE, spec.ngI)
         if c.getLGN_sp:
             lsp = FM.LgnSpWriter(P.lgn_sp, spec.dt, m.nt, nLGN)
+        frames = None
+        if c.framePhyV1output:
+            flags |= N.REC_SPIKES
+            frames = _setup_frames(sim, c, m, P)
         if flags:
             sim.set_record(flags, chunk + 1)
         base = 0
@@ -361,10 +391,12 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
                     lsp.write(sp)
                 if lfr is not None:
                     lfr.write(fr)
+            if frames is not None:
+                frames.write(sim.frames_collect(base + done, k))
             done += k
             if not c.minimal and (done % interval == 0 or done == m.nt):
                 last_snap = _write_snapshot(sim, c, last_snap, log)
-        for w in (raw, lsp, lfr):
+        for w in (raw, lsp, lfr, frames):
             if w is not None:
                 w.close()
     finally:

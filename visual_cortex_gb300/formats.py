@@ -95,6 +95,49 @@ def read_v1_allpos(fn):
     return nblock, blockSize, np.stack([x, y], 1)
 
 
+def read_v1_allpos_spans(fn):
+    """(x0, xspan, y0, yspan) of the physical V1 sheet from the V1_allpos header
+    (src/patch.cu:2759-2767)."""
+    with open(fn, "rb") as f:
+        _r(f, u32, 3)
+        x0, xspan, y0, yspan = (float(v) for v in _r(f, f64, 4))
+    return x0, xspan, y0, yspan
+
+
+def underlying_ids(x, y, width, height, x0, xspan, y0, yspan):
+    """getUnderlyingID (src/stats.cuh:26-60) for all neurons picked: pixel idx + idy*width
+    of each position (double arithmetic, truncated, the far edge folded into the last pixel);
+    returns (offsets [width*height + 1], ids in neuron order within each pixel)."""
+    x, y = np.asarray(x, f64), np.asarray(y, f64)
+    idx = ((x - x0) / xspan * width).astype(np.int64)
+    idy = ((y - y0) / yspan * height).astype(np.int64)
+    idx[idx == width] -= 1
+    idy[idy == height] -= 1
+    if (idx < 0).any() or (idx >= width).any() or (idy < 0).any() or (idy >= height).any():
+        raise ValueError("a position lies outside the frame's span")
+    pid = idx + idy * width
+    order = np.argsort(pid, kind="stable")
+    off = np.zeros(width * height + 1, np.int64)
+    np.add.at(off, pid + 1, 1)
+    return np.cumsum(off).astype(u32), order.astype(u32)
+
+
+class OutputFrameWriter:
+    """outputFrame: {dt f32, ot u32, iFrameOutput u32, then width, height u32 of each frame
+    kind} then the frames (src/patch.cu:4843-4871, 6778-6786); the physical V1 sheet only."""
+
+    def __init__(self, fn, dt, ot, phyWidth, phyHeight):
+        self.f = open(fn, "wb")
+        _w(self.f, [dt], f32)
+        _w(self.f, [ot, 1, phyWidth, phyHeight], u32)
+
+    def write(self, frames):
+        self.f.write(np.ascontiguousarray(frames, f32).tobytes())
+
+    def close(self):
+        self.f.close()
+
+
 def write_mat(fn, nnb, mat):
     """conMat / delayMat: mat [nblock][nnb][bs][bs]."""
     with open(fn, "wb") as f:

@@ -454,6 +454,22 @@ class Simulation:
         N.check(self.plan, N.lib.pv1_get_state(self.plan, N.ST[name], N.fptr(out)), f"pv1_get_state({name})")
         return out
 
+    def frames_setup(self, pix_off: np.ndarray, pix_ids: np.ndarray, ot: int, odt: float):
+        """Framed output of the physical V1 sheet (pv1_frames_setup); needs REC_SPIKES."""
+        self._pix = (np.ascontiguousarray(pix_off, u32), np.ascontiguousarray(pix_ids, u32))
+        self._npix = len(self._pix[0]) - 1
+        self._ot = int(ot)
+        N.check(self.plan, N.lib.pv1_frames_setup(self.plan, self._npix, N.uptr(self._pix[0]), N.uptr(self._pix[1]),
+                                                  int(ot), float(odt)), "pv1_frames_setup")
+
+    def frames_collect(self, step0: int, n: int) -> np.ndarray:
+        """The frames completed within steps [step0, step0 + n), [k][nPixel]."""
+        out = np.empty((n // self._ot + 1, self._npix), f32)
+        k = C.c_uint32()
+        N.check(self.plan, N.lib.pv1_frames_collect(self.plan, int(step0), int(n), N.fptr(out), C.byref(k)),
+                "pv1_frames_collect")
+        return out[:k.value]
+
     def checkpoint(self) -> np.ndarray:
         """The plan's evolving state and step count (pv1_checkpoint_save) as bytes."""
         size = C.c_uint64()

@@ -307,16 +307,17 @@ int pv1_fetch_records(pv1_plan *plan, uint64_t step0, uint32_t n, float *raw,
                                failure plans; read only), added at the next step's delivery */
 /* Copies one state array to the host (waits for queued work). */
 int pv1_get_state(pv1_plan *plan, int which, float *out);
-/* Framed output of the physical V1 sheet (framePhyV1output): pixelizeOutput
+/* Framed output (framePhyV1output, frameVisV1output, frameVisLGNoutput): pixelizeOutput
  * (src/stats.cu:4-36) as the step loop runs it (src/patch.cu:6727-6790).  Pixel q holds the
- * neurons pixIds[pixOff[q] .. pixOff[q+1]) (getUnderlyingID's order, src/stats.cuh:26-60);
- * frames are ot steps long, counted from the plan's step at setup, and each step adds to a
- * pixel (sum of floor(sInfo) over its neurons with sInfo >= 0) / (m odt).  Needs the
- * PV1_REC_SPIKES record.  collect processes steps [step0, step0+n) in order, continuing the
- * previous call, and writes the frames completed among them to frames [k][nPixel], k in
- * *nFrames. */
-int pv1_frames_setup(pv1_plan *plan, uint32_t nPixel, const uint32_t *pixOff, const uint32_t *pixIds,
-                     uint32_t ot, float odt);
+ * cells pixIds[pixOff[q] .. pixOff[q+1]) (getUnderlyingID's order, src/stats.cuh:26-60): V1
+ * neurons for q < nSpikePixel (each step adds the sum of their spike counts floor(sInfo),
+ * sInfo >= 0), LGN cells after that (the sum of their firing rates); the sum is divided by
+ * m odt and accumulated over frames of ot steps counted from the plan's step at setup.  V1
+ * pixels need the PV1_REC_SPIKES record, LGN pixels PV1_REC_LGN_FR.  collect processes steps
+ * [step0, step0+n) in order, continuing the previous call, and writes the frames completed
+ * among them to frames [k][nPixel], k in *nFrames. */
+int pv1_frames_setup(pv1_plan *plan, uint32_t nPixel, uint32_t nSpikePixel, const uint32_t *pixOff,
+                     const uint32_t *pixIds, uint32_t ot, float odt);
 int pv1_frames_collect(pv1_plan *plan, uint64_t step0, uint32_t n, float *frames, uint32_t *nFrames);
 
 /* Checkpoints: the plan's whole evolving state (neuron state and generators, spike-word

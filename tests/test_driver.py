@@ -180,46 +180,61 @@ def test_frame_geometry_and_pixels():
 
 
 @pytest.mark.gpu
-def test_phy_frames_match_the_raster(written, native):
-    """framePhyV1output: the outputFrame of a driver run equals pixelizeOutput's sums
-    recomputed on the host from the run's own rawData spike words."""
+def test_frames_match_the_raster(native):
+    """framePhyV1output + frameVisV1output + frameVisLGNoutput: the outputFrame of a driver run
+    equals pixelizeOutput's sums recomputed on the host from the run's own rawData spike words
+    and LGN_fr rates, pixel lists from getUnderlyingID."""
     import os
-    import shutil
-    wl, fn = written
-    d = os.path.join(os.path.dirname(fn), "frames") + "/"
-    os.makedirs(d, exist_ok=True)
-    lgn = cfg.resolve_paths(cfg.load(["-c", fn])).lgn
-    shutil.copy(lgn, d + os.path.basename(lgn))
-    c = cfg.load(["-c", fn, "--outputFolder", d, "--framePhyV1output", "true", "--dot", "1.0",
-                  "--phyWidth_scale", "0.25"])
+    wl = synth.make_workload("frames", seed=12, nblock=2, n_lgn=512, m=20, width=64, height=64,
+                             nt=96, far_partners=50, adex_inh=True, nFrame=60)
+    d = tempfile.mkdtemp() + "/"
+    fn = synth.write_reference_files(wl, d, seed=2, nt=96, v1_visual=True)
+    c = cfg.load(["-c", fn, "--framePhyV1output", "true", "--frameVisV1output", "true",
+                  "--frameVisLGNoutput", "true", "--dot", "1.0", "--phyWidth_scale", "0.25",
+                  "--visWidth_scale", "0.25", "--saveLGN_fr", "true"])
     m = driver.run(c, chunk=40, log=lambda *_: None)
     P = cfg.resolve_paths(c)
     _, raw = FM.read_raw(P.raw)
-    with open(d + "outputFrame.bin", "rb") as f:
+    fr = FM.read_lgn_fr(P.lgn_fr)
+    with open(os.path.join(c.outputFolder or os.path.dirname(P.raw), "outputFrame.bin"), "rb") as f:
         dt = np.fromfile(f, np.float32, 1)[0]
-        ot, nkind, W, H = np.fromfile(f, np.uint32, 4)
+        ot, kinds = np.fromfile(f, np.uint32, 2)
+        (pw, ph), (vw, vh), (lw, lh) = np.fromfile(f, np.uint32, 6).reshape(3, 2)
         frames = np.fromfile(f, np.float32)
-    assert nkind == 1 and ot == 8 and dt == np.float32(c.dt)
-    frames = frames.reshape(-1, H * W)
+    assert kinds == 7 and ot == 8 and dt == np.float32(c.dt) and (vw, vh) == (lw, lh)
+    npix = pw * ph + 2 * vw * vh + 2 * lw * lh
+    frames = frames.reshape(-1, npix)
     x0, xs, y0, ys = FM.read_v1_allpos_spans(P.v1_allpos)
     _, _, pos = FM.read_v1_allpos(P.v1_allpos)
-    off, ids = FM.underlying_ids(pos[:, 0], pos[:, 1], int(W), int(H), x0, xs, y0, ys)
+    vx0, vxs, vy0, vys, vx, vy = FM.read_v1_allpos_visual(P.v1_allpos)
+    lx0, lxs, ly0, lys = FM.read_lgn_vpos_spans(P.lgn_vpos)
+    nI, nC, _, lx, ly, _ = FM.read_lgn_vpos(P.lgn_vpos)
+    groups = [(FM.underlying_ids(pos[:, 0], pos[:, 1], int(pw), int(ph), x0, xs, y0, ys), True),
+              (FM.underlying_ids(vx, vy, int(vw), int(vh), vx0, vxs, vy0, vys), True),
+              ((np.zeros(vw * vh + 1, np.uint32), np.zeros(0, np.uint32)), True),
+              (FM.underlying_ids(lx[:nI], ly[:nI], int(lw), int(lh), lx0, lxs, ly0, lys, dtype=np.float32), False),
+              (FM.underlying_ids(lx[nI:], ly[nI:], int(lw), int(lh), lx0, lxs, ly0, lys, dtype=np.float32, n0=nI),
+               False)]
     odt = np.float32(float(np.float32(np.float32(ot) * np.float32(c.dt))) / 1000.0)
     sI = raw[:, :m.spec.nV1]
-    want = []
-    acc = np.zeros(H * W, np.float32)
+    want, acc = [], np.zeros(npix, np.float32)
     for t in range(sI.shape[0]):
         if t % ot == 0:
             acc[:] = 0
-        for q in range(H * W):
-            mq = int(off[q + 1] - off[q])
-            if mq:
-                v = np.float32(0)
-                for j in ids[off[q]:off[q + 1]]:
-                    if sI[t, j] >= 0:
-                        v = np.float32(v + np.floor(sI[t, j]))
-                acc[q] = np.float32(acc[q] + np.float32(v / np.float32(np.float32(mq) * odt)))
+        q0 = 0
+        for (off, ids), spike in groups:
+            src = sI[t] if spike else fr[t]
+            for q in range(len(off) - 1):
+                mq = int(off[q + 1] - off[q])
+                if mq:
+                    v = np.float32(0)
+                    for j in ids[off[q]:off[q + 1]]:
+                        if src[j] >= 0:
+                            v = np.float32(v + (np.floor(src[j]) if spike else src[j]))
+                    acc[q0 + q] = np.float32(acc[q0 + q] + np.float32(v / np.float32(np.float32(mq) * odt)))
+            q0 += len(off) - 1
         if (t + 1) % ot == 0:
             want.append(acc.copy())
     np.testing.assert_array_equal(frames, np.array(want))
-    assert frames.sum() > 0
+    for a, b in ((0, pw * ph), (pw * ph, pw * ph + vw * vh), (npix - 2 * lw * lh, npix)):
+        assert frames[:, a:b].sum() > 0

@@ -299,10 +299,12 @@ cudaError_t launch_v1_sp_events(const V1Params &p, const float *H, int depth, cu
 // after that step's V1 kernel: four launches (count, chunk scan, carries, sums).
 cudaError_t launch_far_pull(const V1Params &p, const long long *stepBase, long long off, cudaStream_t st);
 constexpr int kFarPullLaunches = 4;
-// Framed output of the physical V1 sheet over steps [step0, step0 + n) of the spike record ring.
-cudaError_t launch_frames_phy(const float *recSpk, int recSlots, int nV1, long long step0, int n, int ot,
-                              long long tStart, const unsigned *pixOff, const unsigned *pixIds, int nPixel,
-                              float odt, float *acc, float *out, cudaStream_t st);
+// Framed output over steps [step0, step0 + n): pixels below nSpikePixel from the V1 spike
+// record ring, the others from the LGN firing-rate ring.
+cudaError_t launch_frames(const float *recSpk, int recSlots, int nV1, const float *lgnFr, int lgnSlots, int nLGN,
+                          long long step0, int n, int ot, long long tStart, const unsigned *pixOff,
+                          const unsigned *pixIds, int nPixel, int nSpikePixel, float odt, float *acc, float *out,
+                          cudaStream_t st);
 // Adds farPull to the E/I conductances (the far part of the delivery before the first step).
 cudaError_t launch_far_pull_apply(const V1Params &p, cudaStream_t st);
 int v1_persistent_ctas(const V1Params &p, int device, bool *fits);

@@ -40,7 +40,7 @@ struct pv1_plan {
     // framed output of the physical V1 sheet
     unsigned *d_pixOff = nullptr, *d_pixIds = nullptr;
     float *d_frameAcc = nullptr, *d_frameOut = nullptr;
-    int nPixel = 0, frameOt = 0, frameOutCap = 0;
+    int nPixel = 0, nSpikePixel = 0, frameOt = 0, frameOutCap = 0;
     float frameOdt = 0.f;
     long long frameT0 = 0;
     bool lgnReady = false, stimReady = false;
@@ -1772,15 +1772,17 @@ static int flush_delivery(pv1_plan *p) {
 }
 
 // ---- framed output ----
-int pv1_frames_setup(pv1_plan *p, uint32_t nPixel, const uint32_t *pixOff, const uint32_t *pixIds, uint32_t ot,
-                     float odt) {
-    if (!p || !nPixel || !pixOff || ot < 1 || !(odt > 0)) return PV1_E_ARG;
+int pv1_frames_setup(pv1_plan *p, uint32_t nPixel, uint32_t nSpikePixel, const uint32_t *pixOff,
+                     const uint32_t *pixIds, uint32_t ot, float odt) {
+    if (!p || !nPixel || nSpikePixel > nPixel || !pixOff || ot < 1 || !(odt > 0)) return PV1_E_ARG;
     const uint32_t nIds = pixOff[nPixel];
     if (nIds && !pixIds) return PV1_E_ARG;
-    for (uint32_t q = 0; q < nPixel; q++)
+    for (uint32_t q = 0; q < nPixel; q++) {
         if (pixOff[q + 1] < pixOff[q]) return fail(p, PV1_E_ARG, "pixel offsets must not decrease");
-    for (uint32_t j = 0; j < nIds; j++)
-        if (pixIds[j] >= (uint32_t)p->nV1) return fail(p, PV1_E_ARG, "pixel neuron id out of range");
+        const uint32_t lim = q < nSpikePixel ? (uint32_t)p->nV1 : (uint32_t)p->nLGN;
+        for (uint32_t j = pixOff[q]; j < pixOff[q + 1]; j++)
+            if (pixIds[j] >= lim) return fail(p, PV1_E_ARG, "pixel cell id out of range");
+    }
     for (void *q : {(void *)p->d_pixOff, (void *)p->d_pixIds, (void *)p->d_frameAcc, (void *)p->d_frameOut})
         if (q) free_one(p, q);
     p->d_frameOut = nullptr;
@@ -1790,6 +1792,7 @@ int pv1_frames_setup(pv1_plan *p, uint32_t nPixel, const uint32_t *pixOff, const
     if (!r) r = dev_alloc(p, &p->d_frameAcc, nPixel);
     if (r) return r;
     p->nPixel = (int)nPixel;
+    p->nSpikePixel = (int)nSpikePixel;
     p->frameOt = (int)ot;
     p->frameOdt = odt;
     p->frameT0 = p->step;
@@ -1800,7 +1803,8 @@ int pv1_frames_setup(pv1_plan *p, uint32_t nPixel, const uint32_t *pixOff, const
 int pv1_frames_collect(pv1_plan *p, uint64_t step0, uint32_t n, float *frames, uint32_t *nFrames) {
     if (!p || !nFrames) return PV1_E_ARG;
     if (!p->d_pixOff) return fail(p, PV1_E_STATE, "call pv1_frames_setup first");
-    if (!p->vp.recSpk) return fail(p, PV1_E_STATE, "framed output reads the PV1_REC_SPIKES record");
+    if (p->nSpikePixel > 0 && !p->vp.recSpk) return fail(p, PV1_E_STATE, "V1 frames read the PV1_REC_SPIKES record");
+    if (p->nPixel > p->nSpikePixel && !p->d_lgnFr) return fail(p, PV1_E_STATE, "LGN frames read the PV1_REC_LGN_FR record");
     if (step0 + n > (uint64_t)p->step) return fail(p, PV1_E_ARG, "steps not run yet");
     if ((uint64_t)p->step - step0 > (uint64_t)p->recSlots) return fail(p, PV1_E_ARG, "spike records already overwritten");
     uint32_t k = 0;
@@ -1813,9 +1817,9 @@ int pv1_frames_collect(pv1_plan *p, uint64_t step0, uint32_t n, float *frames, u
         if (r) return r;
         p->frameOutCap = (int)k;
     }
-    PV1_CUDA(p, launch_frames_phy(p->vp.recSpk, p->recSlots, p->nV1, (long long)step0, (int)n, p->frameOt, p->frameT0,
-                                  p->d_pixOff, p->d_pixIds, p->nPixel, p->frameOdt, p->d_frameAcc,
-                                  p->d_frameOut ? p->d_frameOut : p->d_frameAcc, p->stream));
+    PV1_CUDA(p, launch_frames(p->vp.recSpk, p->vp.recSlots, p->nV1, p->d_lgnFr, p->lgnSlots, p->nLGN, (long long)step0,
+                              (int)n, p->frameOt, p->frameT0, p->d_pixOff, p->d_pixIds, p->nPixel, p->nSpikePixel,
+                              p->frameOdt, p->d_frameAcc, p->d_frameOut ? p->d_frameOut : p->d_frameAcc, p->stream));
     if (k) PV1_CUDA(p, cudaMemcpyAsync(frames, p->d_frameOut, (size_t)k * p->nPixel * sizeof(float),
                                        cudaMemcpyDeviceToHost, p->stream));
     PV1_CUDA(p, cudaStreamSynchronize(p->stream));

@@ -78,8 +78,6 @@ def _check_supported(c: Config):
         bad.append("virtual_LGN / LGN_switch / reverseInput")
     if c.minimal:
         bad.append("minimal = true (sampled output)")
-    if c.frameVisV1output or c.frameVisLGNoutput:
-        bad.append("frameVisV1output / frameVisLGNoutput (visual-field frames; framePhyV1output is built)")
     if c.fSnapshot and c.asInit:
         bad.append("asInit = true (a snapshot as the initial state of a new run; resume with asInit = false)")
     if c.fSnapshot and (c.snapshot_suffix or "") != (c.output_suffix or ""):
@@ -91,27 +89,61 @@ def _check_supported(c: Config):
 
 
 def _setup_frames(sim, c: Config, m: Model, P):
-    """framePhyV1output: the physical-sheet frame geometry of src/patch.cu:2936-2940 and
-    2959-3037 and the frame interval of :580-584, 5471 (float arithmetic as there); returns
-    the outputFrame writer."""
+    """Framed output: the frame sizes of src/patch.cu:2936-2956, the pixel lists of
+    getUnderlyingID (physical V1 sheet: src/patch.cu:2959-3037; visual-field V1, all neurons
+    ipsilateral without feature files: 3146-3272; visual-field LGN by eye: 3040-3145) in the
+    order of the frame buffer (physical, visual V1 ipsi then contra, visual LGN ipsi then
+    contra), and the frame interval of :580-584, 5471, with the reference's float arithmetic;
+    returns the outputFrame writer."""
     from .cfg import _prefixed, _suffix
     f32 = np.float32
     width = int(m.stim.frames.shape[-1])
-    phyWidth = int(f32(f32(width) * f32(c.phyWidth_scale)))
-    x0, xspan, y0, yspan = FM.read_v1_allpos_spans(P.v1_allpos)
-    ratio = f32(yspan / xspan)
-    phyHeight = int(math.ceil(f32(ratio * f32(phyWidth))))
-    if phyHeight % 2 == 1:
-        phyHeight += 1
     ot = int(f32(c.dot) / f32(c.dt))
     if ot < 1:
         raise ConfigError("dot must be at least one time step")
     odt = f32(float(f32(f32(ot) * f32(c.dt))) / 1000.0)
-    _, _, pos = FM.read_v1_allpos(P.v1_allpos)
-    off, ids = FM.underlying_ids(pos[:, 0], pos[:, 1], phyWidth, phyHeight, x0, xspan, y0, yspan)
-    sim.frames_setup(off, ids, ot, float(odt))
+    offs, idss, sizes, kinds, nSpike = [], [], [], 0, 0
+
+    def add(off, ids):
+        base = sum(len(x) for x in idss)
+        offs.append((off[1:] if offs else off).astype(np.int64) + base)
+        idss.append(ids)
+
+    if c.framePhyV1output:
+        phyWidth = int(f32(f32(width) * f32(c.phyWidth_scale)))
+        x0, xspan, y0, yspan = FM.read_v1_allpos_spans(P.v1_allpos)
+        phyHeight = int(math.ceil(f32(f32(yspan / xspan) * f32(phyWidth))))
+        phyHeight += phyHeight % 2
+        _, _, pos = FM.read_v1_allpos(P.v1_allpos)
+        add(*FM.underlying_ids(pos[:, 0], pos[:, 1], phyWidth, phyHeight, x0, xspan, y0, yspan))
+        sizes.append((phyWidth, phyHeight))
+        kinds |= 1
+    if c.frameVisV1output or c.frameVisLGNoutput:
+        visWidth = int(f32(f32(width) * f32(c.visWidth_scale)))
+        lx0, lxspan, ly0, lyspan = FM.read_lgn_vpos_spans(P.lgn_vpos)
+        visHeight = int(math.ceil(f32(f32(f32(lyspan) / f32(lxspan)) * f32(visWidth))))
+        visHeight += visHeight % 2
+    if c.frameVisV1output:
+        try:
+            vx0, vxspan, vy0, vyspan, vx, vy = FM.read_v1_allpos_visual(P.v1_allpos)
+        except EOFError as e:
+            raise ConfigError("frameVisV1output needs the visual positions in V1_allpos") from e
+        add(*FM.underlying_ids(vx, vy, visWidth, visHeight, vx0, vxspan, vy0, vyspan))
+        add(np.zeros(visWidth * visHeight + 1, np.uint32), np.zeros(0, np.uint32))   # no contralateral V1
+        sizes.append((visWidth, visHeight))
+        kinds |= 2
+    nSpike = sum(len(o) for o in offs) - (1 if offs else 0)
+    if c.frameVisLGNoutput:
+        nI, nC, _, lx, ly, _ = FM.read_lgn_vpos(P.lgn_vpos)
+        add(*FM.underlying_ids(lx[:nI], ly[:nI], visWidth, visHeight, lx0, lxspan, ly0, lyspan, dtype=f32))
+        add(*FM.underlying_ids(lx[nI:], ly[nI:], visWidth, visHeight, lx0, lxspan, ly0, lyspan, dtype=f32, n0=nI))
+        sizes.append((visWidth, visHeight))
+        kinds |= 4
+    off = np.concatenate(offs).astype(np.uint32)
+    ids = np.concatenate(idss).astype(np.uint32)
+    sim.frames_setup(off, ids, nSpike, ot, float(odt))
     fn = _prefixed(c.outputFolder, c.fOutputFrame) + _suffix(c.output_suffix)
-    return FM.OutputFrameWriter(fn, c.dt, ot, phyWidth, phyHeight)
+    return FM.OutputFrameWriter(fn, c.dt, ot, kinds, sizes)
 
 
 def _restore(sim, c: Config) -> int:
@@ -367,8 +399,11 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
         if c.getLGN_sp:
             lsp = FM.LgnSpWriter(P.lgn_sp, spec.dt, m.nt, nLGN)
         frames = None
-        if c.framePhyV1output:
-            flags |= N.REC_SPIKES
+        if c.framePhyV1output or c.frameVisV1output or c.frameVisLGNoutput:
+            if c.framePhyV1output or c.frameVisV1output:
+                flags |= N.REC_SPIKES
+            if c.frameVisLGNoutput:
+                flags |= N.REC_LGN_FR
             frames = _setup_frames(sim, c, m, P)
         if flags:
             sim.set_record(flags, chunk + 1)

@@ -72,15 +72,17 @@ def read_connectome_cfg(fn):
     return nType, nTypeI, acc
 
 
-def write_v1_allpos(fn, nblock, blockSize, pos):
-    """pos: [nV1][2] in mm."""
+def write_v1_allpos(fn, nblock, blockSize, pos, vpos=None):
+    """pos: [nV1][2] in mm; vpos: optional visual-field positions [nV1][2] in degrees, written
+    after the physical block."""
     pos = np.asarray(pos, dtype=f64)
     with open(fn, "wb") as f:
         _w(f, [nblock, blockSize, 2], u32)
-        x0, y0 = pos[:, 0].min(), pos[:, 1].min()
-        _w(f, [x0, pos[:, 0].max() - x0, y0, pos[:, 1].max() - y0], f64)
-        _w(f, pos[:, 0], f64)
-        _w(f, pos[:, 1], f64)
+        for p in ([pos] if vpos is None else [pos, np.asarray(vpos, dtype=f64)]):
+            x0, y0 = p[:, 0].min(), p[:, 1].min()
+            _w(f, [x0, p[:, 0].max() - x0, y0, p[:, 1].max() - y0], f64)
+            _w(f, p[:, 0], f64)
+            _w(f, p[:, 1], f64)
 
 
 def read_v1_allpos(fn):
@@ -104,13 +106,15 @@ def read_v1_allpos_spans(fn):
     return x0, xspan, y0, yspan
 
 
-def underlying_ids(x, y, width, height, x0, xspan, y0, yspan):
-    """getUnderlyingID (src/stats.cuh:26-60) for all neurons picked: pixel idx + idy*width
-    of each position (double arithmetic, truncated, the far edge folded into the last pixel);
-    returns (offsets [width*height + 1], ids in neuron order within each pixel)."""
-    x, y = np.asarray(x, f64), np.asarray(y, f64)
-    idx = ((x - x0) / xspan * width).astype(np.int64)
-    idy = ((y - y0) / yspan * height).astype(np.int64)
+def underlying_ids(x, y, width, height, x0, xspan, y0, yspan, dtype=f64, n0=0):
+    """getUnderlyingID (src/stats.cuh:26-60) for all cells given: pixel idx + idy*width of
+    each position ((x - x0)/xspan*width in `dtype` -- double for V1, float for LGN --,
+    truncated, the far edge folded into the last pixel); returns (offsets [width*height + 1],
+    ids + n0 in cell order within each pixel)."""
+    t = dtype
+    x, y = np.asarray(x, t), np.asarray(y, t)
+    idx = ((x - t(x0)) / t(xspan) * t(width)).astype(np.int64)
+    idy = ((y - t(y0)) / t(yspan) * t(height)).astype(np.int64)
     idx[idx == width] -= 1
     idy[idy == height] -= 1
     if (idx < 0).any() or (idx >= width).any() or (idy < 0).any() or (idy >= height).any():
@@ -119,17 +123,44 @@ def underlying_ids(x, y, width, height, x0, xspan, y0, yspan):
     order = np.argsort(pid, kind="stable")
     off = np.zeros(width * height + 1, np.int64)
     np.add.at(off, pid + 1, 1)
-    return np.cumsum(off).astype(u32), order.astype(u32)
+    return np.cumsum(off).astype(u32), (order + n0).astype(u32)
+
+
+def read_v1_allpos_visual(fn):
+    """The visual-field block of V1_allpos that follows the physical positions when
+    visual-field V1 frames are asked for (src/patch.cu:2774-2781): (vx0, vxspan, vy0, vyspan,
+    vx, vy)."""
+    with open(fn, "rb") as f:
+        nblock, blockSize, _ = (_r1(f, u32) for _ in range(3))
+        n = nblock * blockSize
+        _r(f, f64, 4 + 2 * n)
+        sp = [float(v) for v in _r(f, f64, 4)]
+        if len(sp) < 4:
+            raise ValueError(f"{fn}: no visual positions after the physical ones")
+        vx = _r(f, f64, n)
+        vy = _r(f, f64, n)
+    return sp[0], sp[1], sp[2], sp[3], vx, vy
+
+
+def read_lgn_vpos_spans(fn):
+    """(x0, xspan, y0, yspan) of the LGN visual positions (src/patch.cu:1688-1701)."""
+    with open(fn, "rb") as f:
+        _r(f, u32, 2)
+        _r(f, f32, 1)
+        return tuple(float(v) for v in _r(f, f32, 4))
 
 
 class OutputFrameWriter:
-    """outputFrame: {dt f32, ot u32, iFrameOutput u32, then width, height u32 of each frame
-    kind} then the frames (src/patch.cu:4843-4871, 6778-6786); the physical V1 sheet only."""
+    """outputFrame: {dt f32, ot u32, iFrameOutput u32 (bits: 1 physical V1, 2 visual-field V1,
+    4 visual-field LGN), then width, height u32 of each kind present} then the frames
+    (src/patch.cu:4843-4871, 6778-6786)."""
 
-    def __init__(self, fn, dt, ot, phyWidth, phyHeight):
+    def __init__(self, fn, dt, ot, kinds, sizes):
         self.f = open(fn, "wb")
         _w(self.f, [dt], f32)
-        _w(self.f, [ot, 1, phyWidth, phyHeight], u32)
+        _w(self.f, [ot, kinds], u32)
+        for w, h in sizes:
+            _w(self.f, [w, h], u32)
 
     def write(self, frames):
         self.f.write(np.ascontiguousarray(frames, f32).tobytes())

@@ -454,13 +454,14 @@ class Simulation:
         N.check(self.plan, N.lib.pv1_get_state(self.plan, N.ST[name], N.fptr(out)), f"pv1_get_state({name})")
         return out
 
-    def frames_setup(self, pix_off: np.ndarray, pix_ids: np.ndarray, ot: int, odt: float):
-        """Framed output of the physical V1 sheet (pv1_frames_setup); needs REC_SPIKES."""
+    def frames_setup(self, pix_off: np.ndarray, pix_ids: np.ndarray, n_spike_pixel: int, ot: int, odt: float):
+        """Framed output (pv1_frames_setup): V1 pixels first (REC_SPIKES), LGN pixels after
+        (REC_LGN_FR)."""
         self._pix = (np.ascontiguousarray(pix_off, u32), np.ascontiguousarray(pix_ids, u32))
         self._npix = len(self._pix[0]) - 1
         self._ot = int(ot)
-        N.check(self.plan, N.lib.pv1_frames_setup(self.plan, self._npix, N.uptr(self._pix[0]), N.uptr(self._pix[1]),
-                                                  int(ot), float(odt)), "pv1_frames_setup")
+        N.check(self.plan, N.lib.pv1_frames_setup(self.plan, self._npix, int(n_spike_pixel), N.uptr(self._pix[0]),
+                                                  N.uptr(self._pix[1]), int(ot), float(odt)), "pv1_frames_setup")
 
     def frames_collect(self, step0: int, n: int) -> np.ndarray:
         """The frames completed within steps [step0, step0 + n), [k][nPixel]."""

@@ -455,11 +455,12 @@ def config2(seed: int = 0, orient: float = 0.0, **kw) -> Workload:
 
 
 def write_reference_files(wl: Workload, folder: str, seed: int = 0, nt: int | None = None,
-                          extra: dict | None = None) -> str:
+                          extra: dict | None = None, v1_visual: bool = False) -> str:
     """Writes a workload as the reference's input files plus a patchV1 cfg; returns the cfg
     path.  The within-block distances of the near tiles go to V1_delayMat, a per-neuron
     feed-forward ratio to conStats (the tonic drive is then derived from it by the reader,
-    CmoreDep = true), and the LGN cells to LGN_vpos + LGN (useNewLGN = false)."""
+    CmoreDep = true), and the LGN cells to LGN_vpos + LGN (useNewLGN = false).  v1_visual: the
+    V1 RF centres follow the physical positions in V1_allpos (visual-field V1 frames)."""
     import os
     from . import formats as FM
     from .cfg import write_cfg
@@ -469,7 +470,7 @@ def write_reference_files(wl: Workload, folder: str, seed: int = 0, nt: int | No
     bs, nb = spec.blockSize, spec.nblock
     FM.write_connectome_cfg(d + "connectome_cfg.bin", spec.nType, spec.nType - spec.nTypeE,
                             spec.typeAcc)
-    FM.write_v1_allpos(d + "V1_allpos.bin", nb, bs, wl.pos)
+    FM.write_v1_allpos(d + "V1_allpos.bin", nb, bs, wl.pos, vpos=wl.rf_center if v1_visual else None)
     FM.write_mat(d + "V1_conMat.bin", net.nnb, net.conMat)
     delay = net.delayMat if net.delayMat is not None else near_distances(spec, wl.pos, net.nNearNB, net.nbId)
     FM.write_mat(d + "V1_delayMat.bin", net.nnb, delay)

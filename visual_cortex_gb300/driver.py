@@ -9,8 +9,9 @@ LGN_fr, LGN_sp and patchV1_cfg with the reference's headers and record order.
 Supported: magno and parvo LGN cells in one or two eyes read from the LGN parameter file
 (useNewLGN = false), flat or curved retina, initial spikes, synaptic failure (not on
 distance-delayed near synapses), learning = 0, no gap junctions, no orientation boost
-(nOri = 0), snapshots of this library only (resume with asInit = false), minimal = false.
-Anything else raises ConfigError naming the key.
+(nOri = 0), snapshots of this library only (resume with asInit = false), framed output
+(physical V1, visual-field V1 and LGN), minimal = false.  Anything else raises ConfigError
+naming the key.
 """
 from __future__ import annotations
 

@@ -307,6 +307,13 @@ int pv1_fetch_records(pv1_plan *plan, uint64_t step0, uint32_t n, float *raw,
                                failure plans; read only), added at the next step's delivery */
 /* Copies one state array to the host (waits for queued work). */
 int pv1_get_state(pv1_plan *plan, int which, float *out);
+/* The excitatory neurons sampled by minimal output (src/patch.cu:4922-4937): all of them in
+ * order when sampleSize exceeds their number, else std::sample over them (block-major) with a
+ * default_random_engine seeded `seed` (the rand_spInit seed + 1).  out holds
+ * min(sampleSize, nblock*nE) ids, the count in *nOut. */
+int pv1_sample_ids(uint64_t seed, uint32_t nblock, uint32_t blockSize, uint32_t nE, uint32_t sampleSize,
+                   uint32_t *out, uint32_t *nOut);
+
 /* Framed output (framePhyV1output, frameVisV1output, frameVisLGNoutput): pixelizeOutput
  * (src/stats.cu:4-36) as the step loop runs it (src/patch.cu:6727-6790).  Pixel q holds the
  * cells pixIds[pixOff[q] .. pixOff[q+1]) (getUnderlyingID's order, src/stats.cuh:26-60): V1

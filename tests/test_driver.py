@@ -238,3 +238,40 @@ def test_frames_match_the_raster(native):
     np.testing.assert_array_equal(frames, np.array(want))
     for a, b in ((0, pw * ph), (pw * ph, pw * ph + vw * vh), (npix - 2 * lw * lh, npix)):
         assert frames[:, a:b].sum() > 0
+
+
+@pytest.mark.gpu
+def test_minimal_sample_file(written, native):
+    """minimal = true writes only the sample file; its LGN rows and sample spike counts equal
+    those of a full run of the same cfg (sample_t0 = 2 ms skips the first 15 steps' rows)."""
+    import os
+    import shutil
+    wl, fn = written
+    d = os.path.join(os.path.dirname(fn), "minimal") + "/"
+    os.makedirs(d, exist_ok=True)
+    lgn = cfg.resolve_paths(cfg.load(["-c", fn])).lgn
+    shutil.copy(lgn, d + os.path.basename(lgn))
+    full = cfg.load(["-c", fn, "--getLGN_sp", "true"])
+    driver.run(full, chunk=40, log=lambda *_: None)
+    P = cfg.resolve_paths(full)
+    _, raw = FM.read_raw(P.raw)
+    _, sp = FM.read_lgn_sp(P.lgn_sp)
+    c = cfg.load(["-c", fn, "--outputFolder", d, "--minimal", "true", "--sampleSize", "300",
+                  "--sample_t0", "2.0"])
+    m = driver.run(c, chunk=40, log=lambda *_: None)
+    assert not os.path.exists(d + "rawData.bin")
+    with open(d + "sample_spikeCount.bin", "rb") as f:
+        k = int(np.fromfile(f, np.uint32, 1)[0])
+        t0, t1 = np.fromfile(f, np.float32, 2)
+        nt, nLGN = (int(v) for v in np.fromfile(f, np.uint32, 2))
+        rest = np.fromfile(f, np.uint8)
+    assert k == 300 and t0 == np.float32(2.0) and nt == 96 and nLGN == sp.shape[1]
+    steps = [s for s in range(nt) if s == nt - 1 or np.float32(np.float32(s + 1) * np.float32(c.dt)) >= t0]
+    rows = rest[:len(steps) * nLGN * 4].view(np.float32).reshape(len(steps), nLGN)
+    ids = rest[len(steps) * nLGN * 4:len(steps) * nLGN * 4 + 4 * k].view(np.uint32)
+    counts = rest[len(steps) * nLGN * 4 + 4 * k:].view(np.uint32)
+    assert len(steps) == nt - 15
+    np.testing.assert_array_equal(rows, sp[steps])
+    sI = raw[steps][:, ids]
+    np.testing.assert_array_equal(counts, np.where(sI >= 1, np.floor(sI), 0).sum(axis=0).astype(np.uint32))
+    assert (ids % m.spec.blockSize < m.spec.typeAcc[m.spec.nTypeE - 1]).all() and counts.sum() > 0

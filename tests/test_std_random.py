@@ -70,3 +70,41 @@ def test_std_normal_one_engine_sequence(stdlib_draws):
     seeds = [42]
     who = np.zeros(3001, np.int64)
     np.testing.assert_array_equal(oracle_draws(seeds, who), stdlib_draws(seeds, who))
+
+
+SAMPLE_CPP = r"""
+#include <algorithm>
+#include <cstdio>
+#include <iterator>
+#include <random>
+#include <vector>
+int main() {
+    unsigned long long seed; unsigned nblock, bs, nE, k;
+    if (scanf("%llu %u %u %u %u", &seed, &nblock, &bs, &nE, &k) != 5) return 1;
+    std::vector<unsigned> exc, ids;
+    for (unsigned i = 0; i < nblock; i++) for (unsigned j = 0; j < nE; j++) exc.push_back(i * bs + j);
+    std::default_random_engine g(seed);
+    std::sample(exc.begin(), exc.end(), std::back_inserter(ids), k, g);
+    for (unsigned v : ids) printf("%u\n", v);
+    return 0;
+}
+"""
+
+
+def test_sample_ids_match_std_sample(tmp_path):
+    """pv1_sample_ids (minimal output's sampled neurons) equals std::sample over the
+    excitatory ids with a default_random_engine, as the reference draws them."""
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    from visual_cortex_gb300 import _native as N
+    src, exe = tmp_path / "s.cpp", tmp_path / "s"
+    src.write_text(SAMPLE_CPP)
+    subprocess.run([gxx, "-O2", "-std=c++17", "-o", str(exe), str(src)], check=True)
+    for seed, nblock, bs, nE, k in ((7, 2, 8, 6, 5), (123456789, 32, 1024, 768, 4000), (3, 4, 64, 48, 100)):
+        ref = subprocess.run([str(exe)], input=f"{seed} {nblock} {bs} {nE} {k}", capture_output=True, text=True,
+                             check=True).stdout.split()
+        out = np.zeros(nblock * nE, np.uint32)
+        n = C.c_uint32()
+        assert N.lib.pv1_sample_ids(seed, nblock, bs, nE, k, N.uptr(out), C.byref(n)) == 0
+        np.testing.assert_array_equal(out[:n.value], np.array(ref, np.uint32))

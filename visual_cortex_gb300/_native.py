@@ -120,6 +120,8 @@ def _load() -> C.CDLL:
         "pv1_v1_set_state": ([P, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP], C.c_int),
         "pv1_v1_init_rng": ([P, C.c_uint64, C.c_uint32], C.c_int),
         "pv1_v1_far_failure_engines": ([P, C.c_uint64, C.c_uint32], C.c_int),
+        "pv1_sample_ids": ([C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _UP, C.POINTER(C.c_uint32)],
+                           C.c_int),
         "pv1_frames_setup": ([P, C.c_uint32, C.c_uint32, _UP, _UP, C.c_uint32, C.c_float], C.c_int),
         "pv1_frames_collect": ([P, C.c_uint64, C.c_uint32, _FP, C.POINTER(C.c_uint32)], C.c_int),
         "pv1_checkpoint_size": ([P, C.POINTER(C.c_uint64)], C.c_int),

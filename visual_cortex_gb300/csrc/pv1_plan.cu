@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <functional>
+#include <iterator>
 #include <random>
 #include <string>
 #include <vector>
@@ -1769,6 +1770,25 @@ static int flush_delivery(pv1_plan *p) {
     PV1_CUDA(p, launch_v1_step(p->vp, p->d_stepBase, 0, p->d_lgnRing, p->lgnSlots, 1, 0, p->stream));
     p->pending = false;
     return check_device_error(p);
+}
+
+// ---- minimal output ----
+int pv1_sample_ids(uint64_t seed, uint32_t nblock, uint32_t blockSize, uint32_t nE, uint32_t sampleSize,
+                   uint32_t *out, uint32_t *nOut) {
+    if (!out || !nOut || nE > blockSize) return PV1_E_ARG;
+    std::vector<unsigned> exc;
+    for (uint32_t i = 0; i < nblock; i++)
+        for (uint32_t j = 0; j < nE; j++) exc.push_back(i * blockSize + j);
+    std::vector<unsigned> ids;
+    if ((uint64_t)sampleSize > exc.size()) {
+        ids = exc;
+    } else {
+        std::default_random_engine gen(seed);
+        std::sample(exc.begin(), exc.end(), std::back_inserter(ids), sampleSize, gen);
+    }
+    std::copy(ids.begin(), ids.end(), out);
+    *nOut = (uint32_t)ids.size();
+    return PV1_OK;
 }
 
 // ---- framed output ----

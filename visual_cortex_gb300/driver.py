@@ -10,11 +10,12 @@ Supported: magno and parvo LGN cells in one or two eyes read from the LGN parame
 (useNewLGN = false), flat or curved retina, initial spikes, synaptic failure (not on
 distance-delayed near synapses), learning = 0, no gap junctions, no orientation boost
 (nOri = 0), snapshots of this library only (resume with asInit = false), framed output
-(physical V1, visual-field V1 and LGN), minimal = false.  Anything else raises ConfigError
-naming the key.
+(physical V1, visual-field V1 and LGN), minimal output (the sample file).  Anything else
+raises ConfigError naming the key.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 import sys
 from dataclasses import dataclass
@@ -77,8 +78,6 @@ def _check_supported(c: Config):
         bad.append("useNewLGN = true (LGN parameters drawn from distributions)")
     if c.virtual_LGN or c.LGN_switch or c.reverseInput:
         bad.append("virtual_LGN / LGN_switch / reverseInput")
-    if c.minimal:
-        bad.append("minimal = true (sampled output)")
     if c.fSnapshot and c.asInit:
         bad.append("asInit = true (a snapshot as the initial state of a new run; resume with asInit = false)")
     if c.fSnapshot and (c.snapshot_suffix or "") != (c.output_suffix or ""):
@@ -87,6 +86,45 @@ def _check_supported(c: Config):
         bad.append("manual connections")
     if bad:
         raise ConfigError("not supported by this library: " + "; ".join(bad))
+
+
+class _SampleWriter:
+    """minimal = true: the sample file (fSample + output suffix).  Header {sampleSize, sample_t0,
+    nt*dt, nt, nLGN}; then, for every step s but the last with (s+1)*dt >= sample_t0, its LGN
+    spike words, the sampled neurons' spike counts accumulating; then the last step's LGN
+    spike words and counts (unconditionally), the sample ids and the counts
+    (src/patch.cu:4916-4946, 6122-6137, 7031-7050)."""
+
+    def __init__(self, c: Config, m: Model, P):
+        from .cfg import _prefixed, _suffix
+        from . import _native as N
+        spec = m.spec
+        f32 = np.float32
+        nE = int(spec.typeAcc[spec.nTypeE - 1])
+        ids = np.zeros(max(spec.nblock * nE, 1), np.uint32)
+        n = ctypes.c_uint32()
+        N.check(None, N.lib.pv1_sample_ids(int(m.seeds.cond) + 1, spec.nblock, spec.blockSize, nE,
+                                           int(c.sampleSize), N.uptr(ids), ctypes.byref(n)), "pv1_sample_ids")
+        self.ids = ids[:n.value]
+        self.counts = np.zeros(len(self.ids), np.uint32)
+        self.nt, self.dt, self.t0 = m.nt, f32(c.dt), f32(c.sample_t0)
+        self.f = open(_prefixed(c.outputFolder, c.fSample) + _suffix(c.output_suffix), "wb")
+        self.f.write(np.array([len(self.ids)], np.uint32).tobytes())
+        self.f.write(np.array([self.t0, f32(f32(self.nt) * self.dt)], f32).tobytes())
+        self.f.write(np.array([self.nt, m.extra["nLGN"]], np.uint32).tobytes())
+
+    def add(self, s0: int, sinfo: np.ndarray, lgn: np.ndarray):
+        for j in range(sinfo.shape[0]):
+            s = s0 + j
+            if s == self.nt - 1 or np.float32(np.float32(s + 1) * self.dt) >= self.t0:
+                w = sinfo[j, self.ids]
+                self.counts += np.where(w >= 1, np.floor(w), 0).astype(np.uint32)
+                self.f.write(np.ascontiguousarray(lgn[j], np.float32).tobytes())
+
+    def close(self):
+        self.f.write(self.ids.astype(np.uint32).tobytes())
+        self.f.write(self.counts.tobytes())
+        self.f.close()
 
 
 def _setup_frames(sim, c: Config, m: Model, P):
@@ -388,19 +426,25 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
     spec = m.spec
     sim = Simulation(m.spec, m.net, m.lgn, m.stim, m.init, m.seeds)
     try:
+        minimal = bool(c.minimal)
         flags = (N.REC_RAW if c.rawData else 0) | (N.REC_LGN_SP if c.getLGN_sp else 0) | \
                 (N.REC_LGN_FR if c.saveLGN_fr else 0)
+        sample = None
+        if minimal:
+            # only the sample file (src/patch.cu:4916-4946): no rawData, LGN_sp, LGN_fr, frames
+            flags = N.REC_RAW | N.REC_LGN_SP
+            sample = _SampleWriter(c, m, P)
         raw = lsp = lfr = None
         nLGN = m.extra["nLGN"]
-        if c.saveLGN_fr:
+        if c.saveLGN_fr and not minimal:
             lfr = FM.LgnFrWriter(P.lgn_fr, m.nt, nLGN)
-        if c.rawData:
+        if c.rawData and not minimal:
             raw = FM.RawDataWriter(P.raw, spec.dt, m.nt, spec.nV1, spec.iModel,
                                    spec.nI * spec.nblock, spec.hWrite, spec.ngFF, spec.ngE, spec.ngI)
-        if c.getLGN_sp:
+        if c.getLGN_sp and not minimal:
             lsp = FM.LgnSpWriter(P.lgn_sp, spec.dt, m.nt, nLGN)
         frames = None
-        if c.framePhyV1output or c.frameVisV1output or c.frameVisLGNoutput:
+        if (c.framePhyV1output or c.frameVisV1output or c.frameVisLGNoutput) and not minimal:
             if c.framePhyV1output or c.frameVisV1output:
                 flags |= N.REC_SPIKES
             if c.frameVisLGNoutput:
@@ -418,7 +462,10 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
         while done < m.nt:
             k = min(chunk, m.nt - done, interval - done % interval)
             sim.run(k)
-            if flags:
+            if sample is not None:
+                r, sp, _ = sim.fetch_records(base + done, k, raw=True, lgn_sp=True, lgn_fr=False)
+                sample.add(done, r[:, :spec.nV1], sp)
+            elif flags:
                 r, sp, fr = sim.fetch_records(base + done, k, raw=raw is not None, lgn_sp=lsp is not None,
                                               lgn_fr=lfr is not None)
                 if raw is not None:
@@ -432,12 +479,15 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
             done += k
             if not c.minimal and (done % interval == 0 or done == m.nt):
                 last_snap = _write_snapshot(sim, c, last_snap, log)
-        for w in (raw, lsp, lfr, frames):
+        for w in (raw, lsp, lfr, frames, sample):
             if w is not None:
                 w.close()
     finally:
         sim.close()
     e = m.extra
+    if c.minimal:
+        log(f"simulation for {c.output_suffix} done: {m.nt} steps of {spec.nV1} V1 neurons (minimal)")
+        return m
     with open(P.patchV1_cfg, "wb") as f:
         vals = dict(c.values)
         vals.update(vR=e["vR"], vThres=e["vThres"], gL=e["gL"], vT=e["vT"], C=e["C"],

@@ -275,3 +275,32 @@ def test_minimal_sample_file(written, native):
     sI = raw[steps][:, ids]
     np.testing.assert_array_equal(counts, np.where(sI >= 1, np.floor(sI), 0).sum(axis=0).astype(np.uint32))
     assert (ids % m.spec.blockSize < m.spec.typeAcc[m.spec.nTypeE - 1]).all() and counts.sum() > 0
+
+
+def test_orientation_boost_of_the_tonic_drive():
+    """nOri > 0 with readFeature: the tonic drive scaled by the von Mises boost of each neuron's
+    preferred orientation (V1_feature) around (iOri % nOri)/nOri + 1/2; boostOri = 1, 0 (the
+    reference's minimal*.cfg) leaves it exactly as without nOri."""
+    import math
+    wl = synth.make_workload("ori", seed=6, nblock=1, n_lgn=256, m=20, width=64, height=64, nt=48, nFrame=40)
+    d = tempfile.mkdtemp()
+    fn = synth.write_reference_files(wl, d, seed=3, nt=48)
+    c0 = cfg.load(["-c", fn])
+    n = wl.spec.nV1
+    rng = np.random.default_rng(0)
+    feat = np.stack([rng.uniform(-1, 1, n), rng.uniform(0, 1, n)]).astype(np.float32)
+    FM.write_v1_feature(cfg._prefixed(c0.resourceFolder, c0.fV1_feature) + cfg._suffix(c0.res_suffix), feat)
+    base = driver.build(c0).net.tonicDep
+    flat = driver.build(cfg.load(["-c", fn, "--nOri", "6", "--iOri", "2", "--boostOri", "1.0",
+                                  "--boostOri", "0.0"])).net.tonicDep
+    np.testing.assert_array_equal(flat, base)
+    m = driver.build(cfg.load(["-c", fn, "--nOri", "6", "--iOri", "2", "--boostOri", "0.5", "--boostOri", "2.0"]))
+    r = m.net.tonicDep.astype(np.float64) / base
+    fOri = math.fmod(2 / 6 + 0.5, 1.0)
+    dd = feat[1].astype(np.float64) - fOri
+    dd = np.where(dd > 0.5, 1 - dd, np.where(dd < -0.5, 1 + dd, dd))
+    A = 1 - math.exp(-4.0)
+    want = 0.5 + 0.5 * (np.exp(2.0 * (np.cos(2 * math.pi * dd) - 1)) - 1 + A) / A
+    np.testing.assert_allclose(r, want, rtol=2e-6, atol=2e-7)
+    assert r.max() <= 1.0 + 1e-6 and r.min() >= 0.5 - 1e-6
+    assert m.extra["feature"] is not None

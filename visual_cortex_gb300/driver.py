@@ -8,8 +8,8 @@ LGN_fr, LGN_sp and patchV1_cfg with the reference's headers and record order.
 
 Supported: magno and parvo LGN cells in one or two eyes read from the LGN parameter file
 (useNewLGN = false), flat or curved retina, initial spikes, synaptic failure (not on
-distance-delayed near synapses), learning = 0, no gap junctions, no orientation boost
-(nOri = 0), snapshots of this library only (resume with asInit = false), framed output
+distance-delayed near synapses), learning = 0, no gap junctions, the orientation boost
+(nOri with readFeature), snapshots of this library only (resume with asInit = false), framed output
 (physical V1, visual-field V1 and LGN), minimal output (the sample file).  Anything else
 raises ConfigError naming the key.
 """
@@ -72,8 +72,6 @@ def _check_supported(c: Config):
         bad.append("learning (LGN->V1 / cortical plasticity)")
     if c.InhGap:
         bad.append("InhGap (gap junctions)")
-    if c.nOri > 0:
-        bad.append("nOri > 0 (orientation boost of the tonic drive)")
     if c.useNewLGN:
         bad.append("useNewLGN = true (LGN parameters drawn from distributions)")
     if c.virtual_LGN or c.LGN_switch or c.reverseInput:
@@ -167,8 +165,10 @@ def _setup_frames(sim, c: Config, m: Model, P):
             vx0, vxspan, vy0, vyspan, vx, vy = FM.read_v1_allpos_visual(P.v1_allpos)
         except EOFError as e:
             raise ConfigError("frameVisV1output needs the visual positions in V1_allpos") from e
-        add(*FM.underlying_ids(vx, vy, visWidth, visHeight, vx0, vxspan, vy0, vyspan))
-        add(np.zeros(visWidth * visHeight + 1, np.uint32), np.zeros(0, np.uint32))   # no contralateral V1
+        feat = m.extra.get("feature")
+        ipsi = np.ones(len(vx), bool) if feat is None else feat[0] < 0      # ocular dominance
+        add(*FM.underlying_ids(vx, vy, visWidth, visHeight, vx0, vxspan, vy0, vyspan, pick=ipsi))
+        add(*FM.underlying_ids(vx, vy, visWidth, visHeight, vx0, vxspan, vy0, vyspan, pick=~ipsi))
         sizes.append((visWidth, visHeight))
         kinds |= 2
     nSpike = sum(len(o) for o in offs) - (1 if offs else 0)
@@ -211,6 +211,43 @@ def _write_snapshot(sim, c: Config, previous, log):
         os.remove(previous)
     log(f"saved a snapshot in {name}")
     return name
+
+
+def _orientation_boost(c: Config, P, nType, nV1, blockSize, ptype):
+    """The orientation boost of the tonic drive (src/patch.cu:2844-2932, 4155-4210): with
+    nOri > 0 and readFeature, neuron i of type t is scaled by base + (1 - base) * (exp(k (cos
+    2 pi dOri - 1)) - 1 + A) / A, A = 1 - exp(-2k), (base, k) = boostOri[t], dOri its preferred
+    orientation (feature 1 of V1_feature) minus (iOri[t] % nOri)/nOri + 1/2 wrapped to
+    [-1/2, 1/2]; 1 otherwise.  Returns (boost [nV1], features or None)."""
+    from .cfg import _prefixed, _suffix
+    if not (c.nOri > 0 and c.readFeature):
+        return np.ones(nV1, f32), None
+    feat = FM.read_v1_feature(_prefixed(c.resourceFolder, c.fV1_feature) + _suffix(c.res_suffix), nV1)
+    bo, io = list(c.boostOri or []), list(c.iOri or [])
+    if len(bo) == 2 and nType > 1:
+        bo = bo * nType
+    if len(io) == 1 and nType > 1:
+        io = io * nType
+    if len(bo) != 2 * nType or len(io) != nType:
+        raise ConfigError("nOri > 0 needs boostOri (2 or 2 x nType values) and iOri (1 or nType values)")
+    fOri = [f32(math.fmod(float(f32(int(io[t]) % int(c.nOri)) / f32(c.nOri)) + 0.5, 1.0)) for t in range(nType)]
+    boost = np.ones(nV1, f32)
+    for i in range(nV1):
+        t = int(ptype[i % blockSize])
+        d = f32(feat[1, i] - fOri[t])
+        if d > 0.5:
+            d = f32(1 - d)
+        if d < -0.5:
+            d = f32(1 + d)
+        base, k = f32(bo[2 * t]), f32(bo[2 * t + 1])
+        amp = f32(1 - base)
+        vm = f32(1 - np.exp(f32(-2 * k)))
+        if vm == 0:
+            boost[i] = base
+        else:
+            cosd = f32(math.cos(float(d) * math.pi * 2))
+            boost[i] = f32(base + amp * f32(f32(f32(np.exp(f32(k * f32(cosd - 1)))) - 1 + vm) / vm))
+    return boost, feat
 
 
 def _sp0(c: Config, nTypeE: int, nTypeI: int):
@@ -356,10 +393,11 @@ def build(c: Config) -> Model:
             if seg.size:
                 mx[j] = max(mx[j], seg.max())
                 mn[j] = min(mn[j], seg.min())
+    boost, feature = _orientation_boost(c, P, nType, nV1, blockSize, ptype)
     iTonic = np.zeros(nV1, f32)
     for i in range(nV1):
         t = int(ptype[i % blockSize])
-        td = f32(tonicDep[t])
+        td = f32(f32(tonicDep[t]) * boost[i])
         if c.CmoreDep and mx[t] > mn[t]:
             rel = f32(1) - ffRatio[i]
             lo, hi = f32(1) - mx[t], f32(1) - mn[t]
@@ -409,7 +447,7 @@ def build(c: Config) -> Model:
                            tonicMax=float(iTonic.max()))
     seeds = Seeds(lgn=s_lgn, cond=s_sp, trainDepth=max(trainDepth, 1), sp0=_sp0(c, nTypeE, nTypeI),
                   SCsplit=int(c.SCsplit), nChunk=int(c.nChunk))
-    extra = dict(nType=nType, nTypeE=nTypeE, nTypeI=nTypeI, typeAcc=typeAcc, nLGN=nLGN,
+    extra = dict(nType=nType, nTypeE=nTypeE, nTypeI=nTypeI, typeAcc=typeAcc, nLGN=nLGN, feature=feature,
                  normViewDistance=geo["normViewDistance"], stimulus_filename=P.stimulus, sRatioV1=sRatioV1,
                  sRatioLGN=sRatioLGN, tonicDep=tonicDep, noisyDep=noisyDep, vR=vR,
                  vThres=vThres, gL=gL, vT=vT, C=Cm, tRef=tRef, a=a, b=b, tau_w=tau_w,

@@ -106,13 +106,33 @@ def read_v1_allpos_spans(fn):
     return x0, xspan, y0, yspan
 
 
-def underlying_ids(x, y, width, height, x0, xspan, y0, yspan, dtype=f64, n0=0):
+def write_v1_feature(fn, values):
+    """V1_feature: nFeature u32, then values [nFeature][nV1] f32 (feature 0: ocular dominance,
+    < 0 ipsilateral; feature 1: preferred orientation in [0, 1))."""
+    v = np.asarray(values, f32)
+    with open(fn, "wb") as f:
+        _w(f, [v.shape[0]], u32)
+        _w(f, v, f32)
+
+
+def read_v1_feature(fn, nV1):
+    """src/patch.cu:2912-2925: [nFeature][nV1]."""
+    with open(fn, "rb") as f:
+        n = _r1(f, u32)
+        return _r(f, f32, n * nV1).reshape(n, nV1)
+
+
+def underlying_ids(x, y, width, height, x0, xspan, y0, yspan, dtype=f64, n0=0, pick=None):
     """getUnderlyingID (src/stats.cuh:26-60) for all cells given: pixel idx + idy*width of
     each position ((x - x0)/xspan*width in `dtype` -- double for V1, float for LGN --,
     truncated, the far edge folded into the last pixel); returns (offsets [width*height + 1],
     ids + n0 in cell order within each pixel)."""
     t = dtype
     x, y = np.asarray(x, t), np.asarray(y, t)
+    index = np.arange(len(x))
+    if pick is not None:      # only the picked cells, under their own indices
+        index = np.nonzero(pick)[0]
+        x, y = x[index], y[index]
     idx = ((x - t(x0)) / t(xspan) * t(width)).astype(np.int64)
     idy = ((y - t(y0)) / t(yspan) * t(height)).astype(np.int64)
     idx[idx == width] -= 1
@@ -123,7 +143,7 @@ def underlying_ids(x, y, width, height, x0, xspan, y0, yspan, dtype=f64, n0=0):
     order = np.argsort(pid, kind="stable")
     off = np.zeros(width * height + 1, np.int64)
     np.add.at(off, pid + 1, 1)
-    return np.cumsum(off).astype(u32), (order + n0).astype(u32)
+    return np.cumsum(off).astype(u32), (index[order] + n0).astype(u32)
 
 
 def read_v1_allpos_visual(fn):

@@ -132,11 +132,23 @@ def algorithmic_bytes_per_neuron_step(wl, rate_hz: float) -> float:
     return 8 * S + 12 + 8 * m + 8 * nlgn_over_n + r_dt * (4 * s.blockSize * n_nb + 16 * k_far)
 
 
-def build_workload(name: str):
+def build_workload(name: str, host_init=None):
+    """The seeded synthetic workload.  host_init: who draws the initial state (the library by
+    default; the reference arm passes the oracle's restatement, so it maps no product code)."""
     from visual_cortex_gb300 import synth
     if name == "C1":
-        return synth.config1(seed=0)
-    return synth.config2(seed=0)
+        return synth.config1(seed=0, host_init=host_init)
+    return synth.config2(seed=0, host_init=host_init)
+
+
+def bench_config(name: str, wl) -> dict:
+    """The `config` object of both arms' JSON lines (identical by construction)."""
+    return {"workload": ("32x1024 V1 (80% LIF E / 20% AdEx I), 16384 magno LGN, 128x128 grating "
+                         "120 Hz, ~400 far partners/neuron, dt 0.125 ms") if name == "C2"
+            else "1x1024 V1, 512 LGN, 64x64 grating, dt 0.125 ms",
+            "nV1": wl.spec.nV1, "nLGN": wl.lgn.nLGN, "seed": 0, "mode": "plain forward",
+            "unit_of_work": "one V1 neuron advanced by one 0.125 ms step (LGN, V1 step, near and far delivery)",
+            "l2": "GPU arm: L2 flushed (512 MiB write) before each timed bench step; CPU arm: not applicable"}
 
 
 def run_gb300(args):
@@ -214,12 +226,8 @@ def run_gb300(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": ("32x1024 V1 (80% LIF E / 20% AdEx I), 16384 magno LGN, 128x128 "
-                                "grating 120 Hz, ~400 far partners/neuron, dt 0.125 ms")
-                   if args.config == "C2" else "1x1024 V1, 512 LGN, 64x64 grating, dt 0.125 ms",
-                   "sim_steps_per_bench_step": S, "nV1": wl.spec.nV1, "nLGN": wl.lgn.nLGN,
-                   "mode": "plain forward", "l2": "flushed (512 MiB write) before each timed bench step",
-                   "v1_rate_hz": rate_hz},
+        "config": bench_config(args.config, wl),
+        "sim_steps_per_bench_step": S, "v1_rate_hz": rate_hz,
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(wl.stim.frames.nbytes),
                 "d2h_bytes_per_step": int(S * wl.spec.nV1 * 4)},
@@ -353,7 +361,8 @@ def bench_lgn_bf16():
     rng = np.random.default_rng(0)
     cells = np.sort(rng.choice(wl.nCells, 1024, replace=False))
     steps = np.arange(0, wl.T, 64)
-    ref = L.oracle_rates(wl, cells, steps)
+    from oracle.lgn_fp64 import oracle_rates, rate_errors
+    ref = oracle_rates(wl, cells, steps)
     work = wl.nCells * wl.T
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
@@ -362,13 +371,13 @@ def bench_lgn_bf16():
     kf = 2.0 * 32 * wl.T * wl.nCells                    # algorithmic: ~32 frames per window
     out_bytes = 4.0 * wl.T * wl.nCells + 4.0 * len(range(0, wl.T, 64)) * wl.nCells
     return {"bf16_tensor": {"value": work / (ms16 * 1e-3), "unit": "LGN cell-steps/s", "ms": ms16,
-                            "err_vs_fp64": L.rate_errors(fr16[:, cells], ref),
+                            "err_vs_fp64": rate_errors(fr16[:, cells], ref),
                             "tensor_tflops": kf / (ms16 * 1e-3) / 1e12,
                             "tensor_frac_of_measured_bf16": kf / (ms16 * 1e-3) / 1e12 / bf16_peak,
                             "mma_tflops_issued": flops / (ms16 * 1e-3) / 1e12,
                             "hbm_gbs_outputs": out_bytes / (ms16 * 1e-3) / 1e9},
             "fp32_cuda_cores": {"value": work / (ms32 * 1e-3), "unit": "LGN cell-steps/s", "ms": ms32,
-                                "err_vs_fp64": L.rate_errors(fr32[:, cells], ref)},
+                                "err_vs_fp64": rate_errors(fr32[:, cells], ref)},
             "speedup_bf16_over_fp32": ms32 / ms16,
             "workload": "16384 ON/OFF cells, 31x31 px DoG (sigma +-20%), 250 taps, 256x256 1/f^2 noise, "
                         "120 Hz, 2 s (16000 steps at 0.125 ms)"}
@@ -421,7 +430,9 @@ def run_reference(args):
     import oracle
     from oracle.baseline import CpuPatch, cpu_model
     oracle.build()
-    wl = build_workload(args.config)
+    wl = build_workload(args.config, host_init=oracle.host_init_state)
+    from visual_cortex_gb300 import _native
+    assert not _native.loaded(), "the reference arm must not map the product library"
     cp = CpuPatch(wl)
     n = args.cpu_sample_steps
     for _ in range(args.warmup):
@@ -434,11 +445,12 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
-        "config": {"workload": "same as the GB300 arm", "sim_steps_per_bench_step": n,
-                   "nV1": wl.spec.nV1},
+        "config": bench_config(args.config, wl),
+        "sim_steps_per_bench_step": n,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cp.threads, "kind": "port",
-                         "sample": f"{n} simulation steps per bench step, CPU restatement of the "
-                                   f"reference kernels + host far delivery ({cpu_model()})"},
+                         "sample": f"{n} simulation steps of the same workload per bench step (a bounded "
+                                   f"sample; the GB300 arm runs 800), CPU restatement of the reference "
+                                   f"kernels + host far delivery, OpenMP ({cpu_model()})"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 

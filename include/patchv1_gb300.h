@@ -382,12 +382,14 @@ int pv1_time_kernels(pv1_plan *plan, uint32_t nsteps, float *v1_ms, float *lgn_m
  * kernels for the plan's next nsteps steps and writes the spike words, and the rates if d_fr
  * is not NULL, to the caller's device buffers [nsteps][nLGN] (magno cells; other entries are
  * left untouched).  The only scratch, the rates passed between the two kernels, lives in a
- * fixed 4 MiB device array of the library: nsteps * nLGN must not exceed 1048576, otherwise
- * PV1_E_ARG.  It calls no cudaMalloc/cudaFree.  Work is queued on the plan's stream.  The
+ * fixed 4 MiB device array of the library: nsteps * nLGN must not exceed 1048576 and nsteps
+ * must not exceed 65535, otherwise PV1_E_ARG.  It calls no cudaMalloc/cudaFree.  Work is queued on the plan's stream.  The
  * first call on a device looks up the array's device address (cudaGetSymbolAddress): make
  * that first call before any stream capture.  Calls share the array, so calls that overlap on
  * the GPU race.  It advances the plan's LGN generators and step counter: a plan stepped this
- * way is an LGN-only plan (do not mix with pv1_run). */
+ * way is an LGN-only plan, and pv1_run, pv1_time_kernels, pv1_checkpoint_save and
+ * pv1_batch_create then return PV1_E_STATE; a plan already stepped by pv1_run or a batch is
+ * refused here with PV1_E_STATE. */
 int pv1_lgn_spikes_noalloc(pv1_plan *plan, uint32_t nsteps, float *d_sinfo, float *d_fr);
 
 /* allow = 1/0 enables/disables the persistent cooperative V1 kernel (one launch per chunk of

@@ -80,6 +80,7 @@ def lib():
         L.orc_v1_set_far_failure.argtypes = [P, C.c_uint64, C.c_int]
         L.orc_v1_init_spikes.argtypes = [P, FP, C.c_uint32, C.c_int, FP, UP, C.c_uint32, FP, UP, C.c_uint32, FP]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_host_init_state.argtypes = [P, C.c_uint64, FP, UP, C.c_int, C.c_float] + [FP] * 12
         L.orc_num_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -107,6 +108,33 @@ def ip(a):
 
 
 ST = dict(v=0, w=1, tBack=2, dep=3, gFF=4, hFF=5, gE=6, hE=7, gI=8, hI=9, sInfo=10)
+
+
+def host_init_state(spec, seed: int, tonicDep, nLGNperV1, v0, w0, gFF0, gE0, gI0,
+                    use_v0=False, tonicMax=None):
+    """The reference's host-drawn initial state (src/patch.cu:4405-4540) restated in C
+    (orc_host_init_state); same arguments and result as the library's host_init_state."""
+    import ctypes as _C
+    from visual_cortex_gb300.model import InitState
+    n = spec.nV1
+    cfg = spec.to_struct()
+    td = np.ascontiguousarray(tonicDep, dtype=f32)
+    nl = np.ascontiguousarray(nLGNperV1, dtype=np.uint32)
+    if tonicMax is None:
+        tonicMax = float(td.max())
+    out = dict(v=np.empty(n, f32), w=np.empty(n, f32), gFF=np.empty(spec.ngFF * n, f32),
+               hFF=np.empty(spec.ngFF * n, f32), gE=np.empty(spec.ngE * n, f32),
+               hE=np.empty(spec.ngE * n, f32), gI=np.empty(spec.ngI * n, f32),
+               hI=np.empty(spec.ngI * n, f32))
+    w0a = np.ascontiguousarray(w0 if w0 is not None else np.zeros(2 * spec.nType), dtype=f32)
+    g = [np.ascontiguousarray(x, dtype=f32) for x in (gFF0, gE0, gI0)]
+    lib().orc_host_init_state(_C.byref(cfg), int(seed), fp(td), up(nl), int(bool(use_v0)), float(tonicMax),
+                              fp(w0a), fp(g[0]), fp(g[1]), fp(g[2]), fp(out["v"]), fp(out["w"]),
+                              fp(out["gFF"]), fp(out["hFF"]), fp(out["gE"]), fp(out["hE"]), fp(out["gI"]),
+                              fp(out["hI"]))
+    if spec.iModel != 1:
+        out["w"] = None
+    return InitState(**out)
 
 
 class LgnOracle:

@@ -1285,6 +1285,91 @@ int orc_std_normal_draws(const uint64_t *seeds, int nEng, const int *who, int n,
     return 0;
 }
 
+/* uniform_real_distribution<float>(a, b) of libstdc++: one generate_canonical<float, 24>
+ * draw u, then u * (b - a) + a in float. */
+static float ostd_uniform(uint32_t *x, float a, float b) {
+    const float u = ostd_canonical(x);
+    return u * (b - a) + a;
+}
+
+/* normal_distribution draw * std + mean, redrawn while below 0 when nonNeg (the sampling
+ * lambda of src/patch.cu:4416-4428 with get_incLowBound(0) or no bound). */
+static float ostd_sample(onormal *d, uint32_t *x, float mean, float sd, int nonNeg) {
+    float r;
+    do {
+        r = ostd_normal(d, x) * sd + mean;
+    } while (nonNeg && r < 0.0f);
+    return r;
+}
+
+/* The initial V1 state the reference draws on the host (src/patch.cu:4405-4540), on one
+ * default_random_engine seeded with seed and one normal_distribution<float> shared by every
+ * draw (the sampling lambda's function-local static): per type, w0 (iModel = 1) then v0
+ * (uniform in [vR, vT) when use_v0 or tonicMax > 1, else vR + (vT - vR) tonicDep), block by
+ * block; then per type and feed-forward species the block's g then its h (zeroed for neurons
+ * without LGN input); then per type the cortical E species and the I species, block by block,
+ * g then h.  Layouts: gFF/hFF [ngFF][nV1], gE/hE [ngE][nV1], gI/hI [ngI][nV1]; w0 [nType][2]
+ * (mean, std), gFF0/gE0/gI0 [nType][ng][4] (g mean, g rel. std, h mean, h rel. std). */
+int orc_host_init_state(const pv1_v1_config *c, uint64_t seed, const float *tonicDep, const uint32_t *nLGNperV1,
+                        int use_v0, float tonicMax, const float *w0, const float *gFF0, const float *gE0,
+                        const float *gI0, float *v, float *w, float *gFF, float *hFF, float *gE, float *hE,
+                        float *gI, float *hI) {
+    const size_t bs = c->blockSize, nblock = c->nblock, nV1 = bs * nblock;
+    const int nType = (int)c->nType;
+    size_t acc[PV1_MAX_NTYPE + 1];
+    acc[0] = 0;
+    for (int j = 0; j < nType; j++) acc[j + 1] = c->typeAcc[j];
+    uint32_t x = ostd_seed(seed);
+    onormal d = {0, 0.f};
+    for (int i = 0; i < nType; i++) {
+        if (c->iModel == 1) {
+            for (size_t b = 0; b < nblock; b++)
+                for (size_t j = acc[i]; j < acc[i + 1]; j++)
+                    w[b * bs + j] = ostd_sample(&d, &x, w0[i * 2 + 0], w0[i * 2 + 1], 0);
+        }
+        if (use_v0 || tonicMax > 1.0f) {
+            for (size_t b = 0; b < nblock; b++)
+                for (size_t j = acc[i]; j < acc[i + 1]; j++) v[b * bs + j] = ostd_uniform(&x, c->vR[i], c->vT[i]);
+        } else {
+            for (size_t b = 0; b < nblock; b++)
+                for (size_t j = acc[i]; j < acc[i + 1]; j++)
+                    v[b * bs + j] = c->vR[i] + (c->vT[i] - c->vR[i]) * tonicDep[b * bs + j];
+        }
+    }
+    if (c->iModel != 1 && w)
+        for (size_t q = 0; q < nV1; q++) w[q] = 0.0f;
+    for (int i = 0; i < nType; i++)
+        for (uint32_t k = 0; k < c->ngFF; k++) {
+            const float *q = gFF0 + ((size_t)i * c->ngFF + k) * 4;
+            for (size_t b = 0; b < nblock; b++) {
+                const size_t off = k * nV1 + b * bs;
+                for (size_t j = acc[i]; j < acc[i + 1]; j++) gFF[off + j] = ostd_sample(&d, &x, q[0], q[0] * q[1], 1);
+                for (size_t j = acc[i]; j < acc[i + 1]; j++) hFF[off + j] = ostd_sample(&d, &x, q[2], q[2] * q[3], 1);
+                for (size_t j = acc[i]; j < acc[i + 1]; j++)
+                    if (nLGNperV1[b * bs + j] == 0) gFF[off + j] = hFF[off + j] = 0.0f;
+            }
+        }
+    for (int i = 0; i < nType; i++) {
+        for (uint32_t k = 0; k < c->ngE; k++) {
+            const float *q = gE0 + ((size_t)i * c->ngE + k) * 4;
+            for (size_t b = 0; b < nblock; b++) {
+                const size_t off = k * nV1 + b * bs;
+                for (size_t j = acc[i]; j < acc[i + 1]; j++) gE[off + j] = ostd_sample(&d, &x, q[0], q[0] * q[1], 1);
+                for (size_t j = acc[i]; j < acc[i + 1]; j++) hE[off + j] = ostd_sample(&d, &x, q[2], q[2] * q[3], 1);
+            }
+        }
+        for (uint32_t k = 0; k < c->ngI; k++) {
+            const float *q = gI0 + ((size_t)i * c->ngI + k) * 4;
+            for (size_t b = 0; b < nblock; b++) {
+                const size_t off = k * nV1 + b * bs;
+                for (size_t j = acc[i]; j < acc[i + 1]; j++) gI[off + j] = ostd_sample(&d, &x, q[0], q[0] * q[1], 1);
+                for (size_t j = acc[i]; j < acc[i + 1]; j++) hI[off + j] = ostd_sample(&d, &x, q[2], q[2] * q[3], 1);
+            }
+        }
+    }
+    return 0;
+}
+
 /* Host engines of the far synaptic failure: engine i seeded with seed + i
  * (src/patch.cu:4224-4228); the far delivery runs per chunk of blocks (nChunk as
  * src/patch.cu:3430-3437 splits them), each with its own normal_distribution. */

@@ -4,7 +4,7 @@
 # use: the reference's kernels are compiled but never launched.
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${REFERENCE_SRC:-/root/reference/src}"
+REF="${REFERENCE_SRC:?set REFERENCE_SRC to the src folder of the reference checkout}"
 OUT="$HERE/../_ref"
 mkdir -p "$OUT"
 FLAGS="-std=c++17 -rdc=true -gencode arch=compute_103a,code=sm_103a -DNDEBUG -w -I $HERE/shim -I $REF -I $REF/util"

@@ -3,7 +3,8 @@
 The outputs come from oracle/_ref/ref_golden, built by oracle/ref/build_ref.sh from the
 reference's sources (ConductanceShape, the AdEx struct, hStatic_nonlinear, find_denorm,
 fill_fSpikeTrain + recal_G_vec, with and without synaptic failure).  Run from the repository root, where the reference's
-sources are readable:  bash oracle/ref/build_ref.sh && python tests/golden/make_golden.py
+sources are readable:
+  REFERENCE_SRC=<reference checkout>/src bash oracle/ref/build_ref.sh && python tests/golden/make_golden.py
 """
 import os
 import subprocess

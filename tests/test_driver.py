@@ -180,18 +180,31 @@ def test_frame_geometry_and_pixels():
 
 
 @pytest.mark.gpu
-def test_frames_match_the_raster(native):
+@pytest.mark.parametrize("features", [False, True])
+def test_frames_match_the_raster(native, features):
     """framePhyV1output + frameVisV1output + frameVisLGNoutput: the outputFrame of a driver run
     equals pixelizeOutput's sums recomputed on the host from the run's own rawData spike words
-    and LGN_fr rates, pixel lists from getUnderlyingID."""
+    and LGN_fr rates, pixel lists from getUnderlyingID.  With a V1 feature file (readFeature
+    forced on by nOri, iOri and boostOri), the visual-field V1 frames split the neurons by the
+    sign of their ocular dominance (src/patch.cu:3157-3170)."""
     import os
     wl = synth.make_workload("frames", seed=12, nblock=2, n_lgn=512, m=20, width=64, height=64,
                              nt=96, far_partners=50, adex_inh=True, nFrame=60)
     d = tempfile.mkdtemp() + "/"
     fn = synth.write_reference_files(wl, d, seed=2, nt=96, v1_visual=True)
+    extra = []
+    od = None
+    if features:
+        c0 = cfg.load(["-c", fn])
+        rng = np.random.default_rng(5)
+        feat = np.stack([rng.uniform(-1, 1, wl.spec.nV1), rng.uniform(0, 1, wl.spec.nV1)]).astype(np.float32)
+        FM.write_v1_feature(cfg._prefixed(c0.resourceFolder, c0.fV1_feature) + cfg._suffix(c0.res_suffix), feat)
+        od = feat[0]
+        # boost (1, 0) leaves the drive unchanged; nOri with iOri forces readFeature on
+        extra = ["--nOri", "6", "--iOri", "2", "--boostOri", "1.0", "--boostOri", "0.0"]
     c = cfg.load(["-c", fn, "--framePhyV1output", "true", "--frameVisV1output", "true",
                   "--frameVisLGNoutput", "true", "--dot", "1.0", "--phyWidth_scale", "0.25",
-                  "--visWidth_scale", "0.25", "--saveLGN_fr", "true"])
+                  "--visWidth_scale", "0.25", "--saveLGN_fr", "true"] + extra)
     m = driver.run(c, chunk=40, log=lambda *_: None)
     P = cfg.resolve_paths(c)
     _, raw = FM.read_raw(P.raw)
@@ -209,9 +222,16 @@ def test_frames_match_the_raster(native):
     vx0, vxs, vy0, vys, vx, vy = FM.read_v1_allpos_visual(P.v1_allpos)
     lx0, lxs, ly0, lys = FM.read_lgn_vpos_spans(P.lgn_vpos)
     nI, nC, _, lx, ly, _ = FM.read_lgn_vpos(P.lgn_vpos)
+    if od is None:
+        vis = [FM.underlying_ids(vx, vy, int(vw), int(vh), vx0, vxs, vy0, vys),
+               (np.zeros(vw * vh + 1, np.uint32), np.zeros(0, np.uint32))]
+    else:
+        ipsi = od < 0
+        vis = [FM.underlying_ids(vx, vy, int(vw), int(vh), vx0, vxs, vy0, vys, pick=ipsi),
+               FM.underlying_ids(vx, vy, int(vw), int(vh), vx0, vxs, vy0, vys, pick=~ipsi)]
+        assert len(vis[0][1]) > 0 and len(vis[1][1]) > 0
     groups = [(FM.underlying_ids(pos[:, 0], pos[:, 1], int(pw), int(ph), x0, xs, y0, ys), True),
-              (FM.underlying_ids(vx, vy, int(vw), int(vh), vx0, vxs, vy0, vys), True),
-              ((np.zeros(vw * vh + 1, np.uint32), np.zeros(0, np.uint32)), True),
+              (vis[0], True), (vis[1], True),
               (FM.underlying_ids(lx[:nI], ly[:nI], int(lw), int(lh), lx0, lxs, ly0, lys, dtype=np.float32), False),
               (FM.underlying_ids(lx[nI:], ly[nI:], int(lw), int(lh), lx0, lxs, ly0, lys, dtype=np.float32, n0=nI),
                False)]
@@ -304,3 +324,31 @@ def test_orientation_boost_of_the_tonic_drive():
     np.testing.assert_allclose(r, want, rtol=2e-6, atol=2e-7)
     assert r.max() <= 1.0 + 1e-6 and r.min() >= 0.5 - 1e-6
     assert m.extra["feature"] is not None
+
+
+def test_read_feature_rules():
+    """readFeature as the reference resolves it (src/patch.cu:2842-2930): forced on by iOri or
+    boostOri when nOri > 0 (so readFeature = false still gets the boost), and once on, the
+    feature file is read and nOri > 0, iOri and boostOri are required (the reference asserts
+    them)."""
+    wl = synth.make_workload("ori", seed=6, nblock=1, n_lgn=256, m=20, width=64, height=64, nt=48, nFrame=40)
+    d = tempfile.mkdtemp()
+    fn = synth.write_reference_files(wl, d, seed=3, nt=48)
+    c0 = cfg.load(["-c", fn])
+    n = wl.spec.nV1
+    rng = np.random.default_rng(1)
+    feat = np.stack([rng.uniform(-1, 1, n), rng.uniform(0, 1, n)]).astype(np.float32)
+    FM.write_v1_feature(cfg._prefixed(c0.resourceFolder, c0.fV1_feature) + cfg._suffix(c0.res_suffix), feat)
+    ori = ["--nOri", "6", "--iOri", "2", "--boostOri", "0.5", "--boostOri", "2.0"]
+    on = driver.build(cfg.load(["-c", fn, "--readFeature", "true"] + ori))
+    forced = driver.build(cfg.load(["-c", fn, "--readFeature", "false"] + ori))
+    np.testing.assert_array_equal(forced.net.tonicDep, on.net.tonicDep)
+    np.testing.assert_array_equal(forced.extra["feature"], feat)
+    assert driver.build(c0).extra["feature"] is None          # readFeature = false, no nOri
+    for bad in (["--readFeature", "true"],                          # nOri = 0
+                ["--nOri", "6", "--iOri", "2"],                      # no boostOri
+                ["--nOri", "6", "--boostOri", "0.5", "--boostOri", "0.0"],   # no iOri
+                ["--nOri", "6", "--iOri", "2", "--boostOri", "0.5", "--boostOri", "0.1",
+                 "--boostOri", "0.2"]):                               # 3 values
+        with pytest.raises(cfg.ConfigError):
+            driver.build(cfg.load(["-c", fn] + bad))

@@ -124,3 +124,31 @@ def test_far_failure_matches_recal_G_vec(gold):
     fail = [float(v) for v in gold["farfail_fail"]]
     _far_replay(gold, "farfail", synFail=fail[:4], synPerCon=fail[4:], seed=int(gold["farfail_seed"][0]),
                 nChunk=int(gold["farfail_hdr"][7]))
+
+
+def test_oracle_host_init_matches_the_library():
+    """The oracle's restatement of the reference's host-drawn initial state (v, w, g, h from
+    one default_random_engine and one shared normal_distribution) equals the library's, which
+    calls libstdc++'s <random> itself: bit for bit, with AdEx w and uniform v0."""
+    from visual_cortex_gb300 import synth
+    from visual_cortex_gb300.model import host_init_state
+    import oracle
+    for kw in (dict(nblock=2, adex_inh=True), dict(nblock=1)):
+        wl = synth.make_workload("init", seed=3, n_lgn=256, nt=16, nFrame=8, **kw)
+        s = wl.spec
+        tonic = wl.net.tonicDep
+        nl = wl.net.nLGNperV1.copy()
+        nl[::7] = 0
+        gFF0 = np.tile([0.01, 0.2, 0.003, 0.3], s.nType * s.ngFF).astype(np.float32)
+        gE0 = np.tile([0.005, 0.2, 0.001, 0.2], s.nType * s.ngE).astype(np.float32)
+        gI0 = np.tile([0.01, 0.25, 0.002, 0.2], s.nType * s.ngI).astype(np.float32)
+        w0 = np.tile([0.01, 0.005], s.nType).astype(np.float32)
+        for use_v0 in (False, True):
+            a = host_init_state(s, 77, tonic, nl, None, w0, gFF0, gE0, gI0, use_v0=use_v0)
+            b = oracle.host_init_state(s, 77, tonic, nl, None, w0, gFF0, gE0, gI0, use_v0=use_v0)
+            for k in ("v", "w", "gFF", "hFF", "gE", "hE", "gI", "hI"):
+                x, y = getattr(a, k), getattr(b, k)
+                if x is None:
+                    assert y is None
+                    continue
+                np.testing.assert_array_equal(x, y, err_msg=k)

@@ -68,3 +68,35 @@ def test_noalloc_rejects_work_beyond_its_scratch(native):
         assert "exceeds the fixed scratch" in native.lib.pv1_last_error(sim.plan).decode()
     finally:
         sim.close()
+
+
+def test_noalloc_limits_and_lgn_only_plans(native):
+    """At most 65535 steps per call; a plan stepped by this entry point is refused by pv1_run
+    and by checkpoints, and a plan stepped by pv1_run is refused here."""
+    import torch
+    from visual_cortex_gb300 import synth
+    from visual_cortex_gb300.model import Simulation
+
+    wl = synth.config1(seed=13)
+    a = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    b = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        buf = torch.zeros((4, wl.lgn.nLGN), dtype=torch.float32, device="cuda")
+        rc = native.lib.pv1_lgn_spikes_noalloc(a.plan, 65536, _fptr(buf), None)
+        assert rc == -1
+        assert "65535" in native.lib.pv1_last_error(a.plan).decode()
+        native.check(a.plan, native.lib.pv1_lgn_spikes_noalloc(a.plan, 4, _fptr(buf), None), "noalloc")
+        assert native.lib.pv1_run(a.plan, 1, 1) == -3
+        assert "LGN only" in native.lib.pv1_last_error(a.plan).decode()
+        n = C.c_uint64()
+        native.check(a.plan, native.lib.pv1_checkpoint_size(a.plan, C.byref(n)), "size")
+        host = np.zeros(n.value, dtype=np.uint8)
+        assert native.lib.pv1_checkpoint_save(a.plan, host.ctypes.data_as(C.c_void_p), n.value) == -3
+
+        b.run(4)
+        rc = native.lib.pv1_lgn_spikes_noalloc(b.plan, 4, _fptr(buf), None)
+        assert rc == -3
+        assert "stepped by pv1_run" in native.lib.pv1_last_error(b.plan).decode()
+    finally:
+        a.close()
+        b.close()

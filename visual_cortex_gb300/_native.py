@@ -1,7 +1,9 @@
 """ctypes binding of the C ABI declared in include/patchv1_gb300.h.
 
-The native library is the product: there is no Python or CPU fallback for the hot path.  If
-the library is missing the import of this module raises.
+The native library is the product: there is no Python or CPU fallback for the hot path.  The
+library is loaded (and built if it is out of date) on the first use of `lib`; if it is missing
+and cannot be built, that first use raises ImportError.  Importing this module alone (for the
+ctypes structures of the model objects) maps nothing.
 """
 from __future__ import annotations
 
@@ -162,7 +164,26 @@ def _load() -> C.CDLL:
     return lib
 
 
-lib = _load()
+_LIB = None
+
+
+def _lib() -> C.CDLL:
+    global _LIB
+    if _LIB is None:
+        _LIB = _load()
+    return _LIB
+
+
+def __getattr__(name):
+    # `N.lib` loads the library on first access (PEP 562)
+    if name == "lib":
+        return _lib()
+    raise AttributeError(f"module {__name__!r} has no attribute {name!r}")
+
+
+def loaded() -> bool:
+    """Whether this process has mapped the native library."""
+    return _LIB is not None
 
 
 class NativeError(RuntimeError):
@@ -185,7 +206,7 @@ def uptr(a):
 
 def check(plan, rc: int, what: str):
     if rc != PV1_OK:
-        msg = lib.pv1_last_error(plan).decode() if plan else ""
+        msg = _lib().pv1_last_error(plan).decode() if plan else ""
         raise NativeError(f"{what} failed ({ERRORS.get(rc, rc)}): {msg}")
 
 
@@ -194,7 +215,7 @@ class _PinnedBlock:
 
     def __init__(self, nbytes: int):
         ptr = C.c_void_p()
-        rc = lib.pv1_host_alloc(nbytes, C.byref(ptr))
+        rc = _lib().pv1_host_alloc(nbytes, C.byref(ptr))
         if rc != 0 or not ptr.value:
             raise MemoryError(f"pv1_host_alloc({nbytes}) failed: {rc}")
         self.ptr = ptr.value
@@ -202,7 +223,7 @@ class _PinnedBlock:
 
     def __del__(self):
         if getattr(self, "ptr", None):
-            lib.pv1_host_free(C.c_void_p(self.ptr))
+            _lib().pv1_host_free(C.c_void_p(self.ptr))
             self.ptr = None
 
 

@@ -275,9 +275,11 @@ struct PlanLgnView {
     cudaStream_t stream;
     long long step;
     int device;
+    bool v1Stepped;   // pv1_run or a batch has stepped the plan (or left a delivery pending)
 };
 int plan_lgn_view(pv1_plan *p, PlanLgnView *out);
 void plan_advance_steps(pv1_plan *p, long long n);
+void plan_mark_lgn_only(pv1_plan *p);
 int plan_fail(pv1_plan *p, int code, const char *msg);
 cudaError_t launch_v1_step(const V1Params &p, const long long *stepBase, int stepOffset,
                            const float *lgnSInfo, int lgnSlots, int deliverPrev, int doStep,

@@ -26,6 +26,8 @@ constexpr size_t kNoAllocRateFloats = size_t(1) << 20;            // 4 MiB of ra
 constexpr size_t kNoAllocHeadBytes = 256;                          // step counter
 constexpr size_t kNoAllocBytes = kNoAllocHeadBytes + kNoAllocRateFloats * sizeof(float);
 constexpr int kMaxDevices = 64;
+// the rate kernel puts the steps of a call on gridDim.y
+constexpr uint32_t kNoAllocMaxSteps = 65535;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -111,6 +113,12 @@ extern "C" int pv1_lgn_spikes_noalloc(pv1_plan *plan, uint32_t nsteps, float *d_
     if (r) return r;
     if (view.lp.nParvo > 0)
         return plan_fail(plan, PV1_E_UNSUPPORTED, "pv1_lgn_spikes_noalloc: plans with parvo cells are not supported");
+    if (view.v1Stepped)
+        return plan_fail(plan, PV1_E_STATE,
+                         "pv1_lgn_spikes_noalloc: the plan was stepped by pv1_run or a batch; LGN-only stepping "
+                         "needs a plan that only this entry point steps");
+    if (nsteps > kNoAllocMaxSteps)
+        return plan_fail(plan, PV1_E_ARG, "pv1_lgn_spikes_noalloc: at most 65535 steps per call");
     const size_t need = (size_t)nsteps * (size_t)view.lp.nLGN;
     if (need > kNoAllocRateFloats)
         return plan_fail(plan, PV1_E_ARG,
@@ -137,5 +145,6 @@ extern "C" int pv1_lgn_spikes_noalloc(pv1_plan *plan, uint32_t nsteps, float *d_
     }
     if (e != cudaSuccess) return plan_fail(plan, PV1_E_CUDA, cudaGetErrorString(e));
     plan_advance_steps(plan, nsteps);
+    plan_mark_lgn_only(plan);
     return PV1_OK;
 }

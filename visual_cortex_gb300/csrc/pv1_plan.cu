@@ -85,6 +85,9 @@ struct pv1_plan {
     // stepping
     long long step = 0;
     bool pending = false;
+    // stepped by pv1_lgn_spikes_noalloc: the LGN generators and the step counter moved
+    // without the V1 state, so pv1_run, batches and checkpoints refuse the plan
+    bool lgnOnly = false;
     // records
     int recFlags = 0;
     int recSlots = 0;
@@ -265,13 +268,17 @@ int plan_lgn_view(pv1_plan *p, PlanLgnView *out) {
     out->stream = p->stream;
     out->step = p->step;
     out->device = p->device;
+    out->v1Stepped = p->pending || (p->step > 0 && !p->lgnOnly);
     return PV1_OK;
 }
 
 void plan_advance_steps(pv1_plan *p, long long n) { p->step += n; }
 
+void plan_mark_lgn_only(pv1_plan *p) { p->lgnOnly = true; }
+
 int plan_batch_view(pv1_plan *p, PlanBatchView *out) {
     if (!p || !out) return PV1_E_ARG;
+    if (p->lgnOnly) return fail(p, PV1_E_STATE, "the plan was stepped by pv1_lgn_spikes_noalloc (LGN only)");
     if (!p->lgnReady || !p->stimReady) return fail(p, PV1_E_STATE, "LGN/stimulus not loaded");
     int er = ensure_all_frames(p);
     if (er) return er;
@@ -1522,6 +1529,7 @@ static int choose_mode(pv1_plan *p) {
 
 int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
     if (!p) return PV1_E_ARG;
+    if (p->lgnOnly) return fail(p, PV1_E_STATE, "the plan was stepped by pv1_lgn_spikes_noalloc (LGN only)");
     if (!p->lgnReady || !p->stimReady) return fail(p, PV1_E_STATE, "LGN/stimulus not loaded");
     if (!p->haveLGNsyn || !p->haveNear || !p->haveState || !p->haveRng)
         return fail(p, PV1_E_STATE, "V1 synapses/connectivity/state/rng not set");
@@ -1704,6 +1712,7 @@ int pv1_run_timed(pv1_plan *p, uint32_t nsteps, uint64_t flush_bytes, float *ms)
 
 int pv1_time_kernels(pv1_plan *p, uint32_t nsteps, float *v1_ms, float *lgn_ms, int *chunk) {
     if (!p || !v1_ms || !lgn_ms) return PV1_E_ARG;
+    if (p->lgnOnly) return fail(p, PV1_E_STATE, "the plan was stepped by pv1_lgn_spikes_noalloc (LGN only)");
     if (!p->lgnReady || !p->stimReady || !p->haveState || !p->haveRng || !p->haveNear || !p->haveLGNsyn)
         return fail(p, PV1_E_STATE, "plan not ready");
     int r = choose_mode(p);
@@ -1948,6 +1957,7 @@ int pv1_checkpoint_size(pv1_plan *p, uint64_t *bytes) {
 
 int pv1_checkpoint_save(pv1_plan *p, void *buf, uint64_t bytes) {
     if (!p || !buf) return PV1_E_ARG;
+    if (p->lgnOnly) return fail(p, PV1_E_STATE, "the plan was stepped by pv1_lgn_spikes_noalloc (LGN only)");
     if (!p->haveState || !p->haveRng || !p->lgnReady) return fail(p, PV1_E_STATE, "plan not initialised");
     int r = flush_delivery(p);
     if (r) return r;

@@ -214,23 +214,50 @@ def _write_snapshot(sim, c: Config, previous, log):
 
 
 def _orientation_boost(c: Config, P, nType, nV1, blockSize, ptype):
-    """The orientation boost of the tonic drive (src/patch.cu:2844-2932, 4155-4210): with
-    nOri > 0 and readFeature, neuron i of type t is scaled by base + (1 - base) * (exp(k (cos
-    2 pi dOri - 1)) - 1 + A) / A, A = 1 - exp(-2k), (base, k) = boostOri[t], dOri its preferred
-    orientation (feature 1 of V1_feature) minus (iOri[t] % nOri)/nOri + 1/2 wrapped to
-    [-1/2, 1/2]; 1 otherwise.  Returns (boost [nV1], features or None)."""
+    """The orientation boost of the tonic drive and the V1 feature file (src/patch.cu:2842-2930,
+    4155-4210).  readFeature is forced on by a non-empty boostOri or iOri when nOri > 0; the
+    feature file is read whenever readFeature ends up on (its ocular dominance also splits the
+    visual-field V1 frames, src/patch.cu:3157-3170), and the reference then asserts nOri > 0,
+    iOri and boostOri (src/patch.cu:2927-2929; its build scripts do not define NDEBUG), which
+    is a ConfigError here.  With boostOri given, readFeature on and nOri > 0, neuron i of type t
+    is scaled by base + (1 - base) * (exp(k (cos 2 pi dOri - 1)) - 1 + A) / A, A = 1 - exp(-2k),
+    (base, k) = boostOri[t], dOri its preferred orientation (feature 1) minus fOri[t] wrapped to
+    [-1/2, 1/2], fOri[t] = (iOri[t] % nOri)/nOri + 1/2 (0 without iOri, when k is forced to 0);
+    1 otherwise.  Returns (boost [nV1], features or None)."""
     from .cfg import _prefixed, _suffix
-    if not (c.nOri > 0 and c.readFeature):
+    nOri = int(c.values.get("nOri") or 0)
+    read_feature = bool(c.readFeature)
+    bo = [float(x) for x in (c.values.get("boostOri") or [])]
+    io = [int(x) for x in (c.values.get("iOri") or [])]
+    fOri = [f32(0.0)] * nType
+    if nOri > 0:
+        if bo:
+            if len(bo) not in (2, 2 * nType):
+                raise ConfigError("boostOri need 2 x nType elements: [baseline, std] x nType")
+            read_feature = True
+            if len(bo) == 2 and nType > 1:
+                bo = bo * nType
+            if any(bo[2 * t + 1] != 0 for t in range(nType)) and not io:
+                raise ConfigError("when boostOri[std] is set, iOri needs to be set")
+        if io:
+            if len(io) not in (1, nType):
+                raise ConfigError("iOri need 1 or nType elements")
+            read_feature = True
+            if len(io) == 1 and nType > 1:
+                io = io * nType
+            fOri = [f32(math.fmod(float(f32(io[t] % nOri) / f32(nOri)) + 0.5, 1.0)) for t in range(nType)]
+        else:
+            for q in range(1, len(bo), 2):
+                bo[q] = 0.0
+    else:
+        for q in range(1, len(bo), 2):
+            bo[q] = 0.0
+    if not read_feature:
         return np.ones(nV1, f32), None
     feat = FM.read_v1_feature(_prefixed(c.resourceFolder, c.fV1_feature) + _suffix(c.res_suffix), nV1)
-    bo, io = list(c.boostOri or []), list(c.iOri or [])
-    if len(bo) == 2 and nType > 1:
-        bo = bo * nType
-    if len(io) == 1 and nType > 1:
-        io = io * nType
-    if len(bo) != 2 * nType or len(io) != nType:
-        raise ConfigError("nOri > 0 needs boostOri (2 or 2 x nType values) and iOri (1 or nType values)")
-    fOri = [f32(math.fmod(float(f32(int(io[t]) % int(c.nOri)) / f32(c.nOri)) + 0.5, 1.0)) for t in range(nType)]
+    if not (nOri > 0 and io and bo):
+        raise ConfigError("readFeature = true needs nOri > 0, iOri and boostOri (the reference asserts them "
+                          "after reading the feature file); set readFeature = false otherwise")
     boost = np.ones(nV1, f32)
     for i in range(nV1):
         t = int(ptype[i % blockSize])

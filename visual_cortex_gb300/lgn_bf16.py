@@ -7,7 +7,8 @@ convol[cell][t] = sum_f S[cell][f] W[t][f] runs as tcgen05 BF16 MMAs with FP32 a
 the time-reversed temporal-kernel samples that read frame f at step t, with the frame
 bookkeeping of the reference's step loop (src/patch.cu:4950-5030, 5395-5422, restated in
 schedule.py); it is built here in FP64 and tiled per 128 steps with a 64-frame window.
-``oracle_rates`` evaluates the same rates in FP64 (numpy) for the error report.
+The FP64 evaluation of the same rates for the error report is test infrastructure and lives
+in oracle/lgn_fp64.py.
 """
 from __future__ import annotations
 
@@ -234,46 +235,6 @@ class LgnTensorCore:
             self.close()
         except Exception:
             pass
-
-
-def spatial64(wl: LgnWorkload, cells: np.ndarray) -> np.ndarray:
-    """FP64 spatial stage of the given cells: [len(cells)][nFext] (column = frame + PAD)."""
-    half = wl.side // 2
-    nF = wl.frames.shape[0]
-    contrast = np.clip(wl.frames.astype(np.float64) / wl.meanLum - 1.0, -1.0, 1.0)
-    out = np.zeros((len(cells), wl.nFext))
-    d = np.arange(wl.side) - half
-    for r, c in enumerate(cells):
-        ys = wl.cy[c] + d
-        xs = wl.cx[c] + d
-        patch = contrast[:, ys[:, None], xs[None, :]].reshape(nF, -1)   # [nF][side*side]
-        s = patch @ wl.SW[c].astype(np.float64)
-        cols = np.arange(PAD, wl.nFext)
-        out[r, PAD:] = s[(cols - PAD) % nF]
-    return out
-
-
-def oracle_rates(wl: LgnWorkload, cells: np.ndarray, steps: np.ndarray) -> np.ndarray:
-    """FP64 LGN rates [len(steps)][len(cells)] of the same workload (spatial stage, frame
-    weights, logistic rate) for the error report of the BF16 and FP32 paths."""
-    S = spatial64(wl, cells)                                   # [cells][nFext]
-    out = np.empty((len(steps), len(cells)))
-    for q, t in enumerate(steps):
-        i, s = divmod(int(t), TILE_N)
-        cols = wl.f0[i] + np.arange(TILE_K)
-        ok = cols < wl.nFext
-        conv = S[:, cols[ok]] @ wl.W[i, s][ok]                 # FP64 weights of the window
-        cur = np.maximum(conv * np.abs(wl.k[cells]).astype(np.float64) * wl.convolRatio, 0.0)
-        mx = wl.maxConvol[cells].astype(np.float64)
-        X = 1.0 / (1.0 + np.exp(wl.sharp[cells] * (wl.c50[cells] - cur / mx)))
-        out[q] = wl.frRatio * mx * (wl.la[cells] * X + wl.lb[cells])
-    return out
-
-
-def rate_errors(fr: np.ndarray, ref: np.ndarray) -> dict:
-    rel = np.abs(fr.astype(np.float64) - ref) / np.abs(ref)
-    return {"max_rel": float(rel.max()), "rms_rel": float(np.sqrt(np.mean(rel ** 2))),
-            "mean_rate_hz": float(ref.mean())}
 
 
 def main(argv=None):

@@ -369,12 +369,13 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
                   noDelay: int = 1, n_parvo: int = 0, tau: float | None = None,
                   nKernelSample: int | None = None, blockSize: int = 1024, nE: int = 768,
                   m_min: int | None = None, flat_retina: bool = True, spE0=None, spI0=None,
-                  SCsplit: int = 0, nChunk: int = 1, contra: bool = False) -> Workload:
+                  SCsplit: int = 0, nChunk: int = 1, contra: bool = False, host_init=None) -> Workload:
     """Builds one synthetic patch; C1 = 1x1024 V1 / 512 LGN; C2 = 32 blocks / 16384 LGN.
     noDelay = 0: near synapses are delivered after their distance delay (delayMat from the
     neuron positions, mm, at speedOfThought 1 mm/ms).  spE0/spI0: initial spike rates in Hz
     ([type][2] flattened, as in the cfg), converted to per-step chances as
-    src/patch.cu:810-837 does."""
+    src/patch.cu:810-837 does.  host_init: the function that draws the initial state (default
+    model.host_init_state, the library's; the oracle's restatement gives the same arrays)."""
     rng = np.random.default_rng(seed)
     spec = make_spec(nblock, blockSize=blockSize, nE=nE, adex_inh=adex_inh, noisyDep=noisyDep,
                      synFail=synFail, synFailFF=synFailFF, dt=dt)
@@ -415,7 +416,7 @@ def make_workload(name: str = "C1", seed: int = 0, nblock: int = 1, n_lgn: int =
     gE0 = np.tile([0.005, 0.2, 0.0, 0.2], spec.nType * spec.ngE).astype(f32)
     gI0 = np.tile([0.01, 0.2, 0.0, 0.2], spec.nType * spec.ngI).astype(f32)
     w0 = np.tile([0.0, 0.0], spec.nType).astype(f32)
-    init = host_init_state(spec, s_init, tonic, nLGNperV1, None, w0, gFF0, gE0, gI0)
+    init = (host_init or host_init_state)(spec, s_init, tonic, nLGNperV1, None, w0, gFF0, gE0, gI0)
     max_delay = float(delayVec.max()) if delayVec.size else 0.0
     trainDepth = int(math.ceil(max(max_delay, 0.0) / spec.speedOfThought / spec.dt)) + 1
     if delayMat is not None:   # the near spike-word ring (src/patch.cu:3808-3813)
@@ -518,7 +519,8 @@ def write_reference_files(wl: Workload, folder: str, seed: int = 0, nt: int | No
         noiseOnTonic=spec.noiseOnTonic, synFail=spec.synFail, synFailFF=spec.synFailFF,
         vR=spec.vR, vThres=spec.vThres, gL=spec.gL, C=spec.C, tRef=spec.tRef, vT=spec.vT,
         deltaT=spec.deltaT, tau_w=spec.tau_w, a=spec.a, b=spec.b, hWrite=spec.hWrite,
-        spE0=[0.0, 0.0], spI0=[0.0, 0.0], getLGN_sp=True, saveLGN_fr=True, rawData=True)
+        spE0=[0.0, 0.0], spI0=[0.0, 0.0], getLGN_sp=True, saveLGN_fr=True, rawData=True,
+        readFeature=False)
     keys.update(extra or {})
     fn = d + "patchV1.cfg"
     with open(fn, "w") as f:

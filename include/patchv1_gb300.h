@@ -305,6 +305,13 @@ int pv1_fetch_records(pv1_plan *plan, uint64_t step0, uint32_t n, float *raw,
 #define PV1_ST_LGN_SINFO 13 /* [nLGN] last step's LGN spike word */
 #define PV1_ST_FAR_PULL 14  /* [ngE+ngI][2][nV1] far g, h sums of the last step (far synaptic
                                failure plans; read only), added at the next step's delivery */
+/* Random generators, read only, as raw bytes: 48 bytes (one curandStateMRG32k3a) per cell or
+ * neuron, so `out` must hold 12 floats' worth per entry.  LGN: one per LGN cell, set up by
+ * logRand_init's curand_init(seed, id, 0) (src/coredynamics.cu:148-177); V1: rGenCond and
+ * rNoisy, curand_init(seed, id, 0) and curand_init(seed, nV1 + id, 0) (:5-146). */
+#define PV1_ST_LGN_RNG 15   /* [nLGN][48 B] */
+#define PV1_ST_V1_RNG_COND 16  /* [nV1][48 B] */
+#define PV1_ST_V1_RNG_NOISY 17 /* [nV1][48 B] */
 /* Copies one state array to the host (waits for queued work). */
 int pv1_get_state(pv1_plan *plan, int which, float *out);
 /* The excitatory neurons sampled by minimal output (src/patch.cu:4922-4937): all of them in
@@ -391,6 +398,13 @@ int pv1_time_kernels(pv1_plan *plan, uint32_t nsteps, float *v1_ms, float *lgn_m
  * pv1_batch_create then return PV1_E_STATE; a plan already stepped by pv1_run or a batch is
  * refused here with PV1_E_STATE. */
 int pv1_lgn_spikes_noalloc(pv1_plan *plan, uint32_t nsteps, float *d_sinfo, float *d_fr);
+
+/* Polls of a barrier wait (the persistent kernel's grid barrier between steps, the batched
+ * kernel's per-trial barrier) before it gives up; spins < 0 restores the default (2e7 polls,
+ * about a second).  A wait that gives up releases every other waiter, the kernel returns, and
+ * the run reports PV1_E_DEVICE ("a barrier wait gave up") instead of hanging: the GPU context
+ * stays usable.  No counterpart in the reference (its kernels never wait on one another). */
+int pv1_set_wait_limit(pv1_plan *plan, int64_t spins);
 
 /* allow = 1/0 enables/disables the persistent cooperative V1 kernel (one launch per chunk of
  * steps, state in registers, bounded grid barrier between steps); allow = -1 only queries.

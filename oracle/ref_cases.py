@@ -1,0 +1,180 @@
+"""Cases on which the reference's own GPU kernels were run -- TEST INFRASTRUCTURE.
+
+tests/golden/make_ref_kernel_golden.py feeds these inputs to oracle/ref/ref_kernel_runner.cu
+(the reference's kernels, src/coredynamics.cu and src/discrete_input_convol.cu, compiled from
+its sources into oracle/_ref/ref_kernels.cubin) and stores inputs and outputs in
+tests/golden/ref_kernels.npz; tests/test_ref_kernels.py rebuilds the same networks from the
+seeds here and holds the oracle (CPU) and the library (GPU) to those outputs.
+
+Bundles are the runner's file format: records {char name[32]; char type[4]; u64 count; data}.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+f32, u32, i32, u64, u8 = np.float32, np.uint32, np.int32, np.uint64, np.uint8
+_CODES = {np.dtype(f32): "f4", np.dtype(u32): "u4", np.dtype(i32): "i4", np.dtype(u64): "u8",
+          np.dtype(u8): "u1"}
+_TYPES = {"f4": f32, "u4": u32, "i4": i32, "u8": u64, "u1": u8}
+
+STATE_BYTES = 48     # curandStateMRG32k3a
+
+
+def write_bundle(path: str, arrays: dict):
+    with open(path, "wb") as f:
+        for name, a in arrays.items():
+            a = np.ascontiguousarray(a)
+            code = _CODES[a.dtype]
+            f.write(name.encode().ljust(32, b"\0")[:32])
+            f.write(code.encode().ljust(4, b"\0"))
+            f.write(np.uint64(a.size).tobytes())
+            f.write(a.tobytes())
+
+
+def read_bundle(path: str) -> dict:
+    out = {}
+    data = open(path, "rb").read()
+    off = 0
+    while off < len(data):
+        name = data[off:off + 32].split(b"\0")[0].decode()
+        code = data[off + 32:off + 34].decode()
+        n = int(np.frombuffer(data, u64, 1, off + 36)[0])
+        off += 44
+        t = np.dtype(_TYPES[code])
+        out[name] = np.frombuffer(data, t, n, off).copy()
+        off += n * t.itemsize
+    return out
+
+
+def scalar(v, t):
+    return np.array([v], dtype=t)
+
+
+# ---- LGN: logRand_init + LGN_nonlinear ----------------------------------------------------
+LGN_N, LGN_K, LGN_NU, LGN_NSX = 512, 48, 24, 32
+LGN_SEED = 1234567
+
+
+def lgn_case() -> dict:
+    """512 cells on a 32 x 16 spike surface, 48 steps of seeded convolutions (a mix of silent,
+    moderate and saturating drive) with per-cell logistic parameters; the draws of the first
+    24 uniforms of every generator are returned by the runner for the oracle's replay."""
+    rng = np.random.default_rng(77)
+    n, K = LGN_N, LGN_K
+    ids = np.arange(n)
+    maxc = rng.uniform(0.5, 2.0, n).astype(f32)
+    convol = (rng.uniform(-0.3, 1.2, (K, n)) * maxc).astype(f32)
+    c50 = rng.uniform(0.2, 0.5, n).astype(f32)
+    sharp = rng.uniform(4.0, 12.0, n).astype(f32)
+    a = rng.uniform(0.9, 1.3, n).astype(f32)
+    b = rng.uniform(0.0, 0.05, n).astype(f32)
+    return dict(seed=scalar(LGN_SEED, u64), n=scalar(n, u32), K=scalar(K, u32), NU=scalar(LGN_NU, u32),
+                nsx=scalar(LGN_NSX, u32), nsy=scalar(n // LGN_NSX, u32),
+                sx=(ids % LGN_NSX).astype(i32), sy=(ids // LGN_NSX).astype(i32),
+                convol=convol.reshape(-1), max_convol=maxc, c50=c50, sharpness=sharp, a=a, b=b,
+                convolRatio=scalar(1.0, f32), frRatio=scalar(80.0, f32), dt=scalar(0.125, f32))
+
+
+# ---- V1: rand_spInit, compute_V_collect_spike_learnFF_fast, recal_G_mat_nd_fast -----------
+V1_T, V1_SNAP = 160, 32
+V1_SEED = 4242
+
+
+def v1_workload(sp: bool = False, host_init=None):
+    """Two blocks of 1024 (768 LIF E / 256 AdEx I), 512 LGN cells, 20 LGN synapses each, no far
+    partners; each block has the other as a second near-neighbour block (its tile is the
+    other block's own tile at half strength), so near delivery crosses blocks."""
+    from visual_cortex_gb300 import synth
+    kw = dict(spE0=[60.0, 20.0], spI0=[80.0, 30.0]) if sp else {}
+    wl = synth.make_workload("ref-pin", seed=21, nblock=2, n_lgn=512, m=20, width=64, height=64,
+                             nt=V1_T, adex_inh=True, nFrame=40, host_init=host_init, **kw)
+    net = wl.net
+    nb, bs = wl.spec.nblock, wl.spec.blockSize
+    own = net.conMat[:, 0]
+    cm = np.empty((nb, 2, bs, bs), f32)
+    cm[:, 0] = own
+    cm[:, 1] = own[::-1] * f32(0.5)
+    net.conMat = cm
+    net.nNearNB = np.full(nb, 2, u32)
+    net.nbId = np.array([[b, (b + 1) % nb] for b in range(nb)], u32)
+    return wl
+
+
+def v1_inputs(wl, sp0=None, lgn_rows=None, T: int = 0) -> dict:
+    """The runner's V1 inputs for a workload (LGN surface 32 wide, cell id = y * 32 + x)."""
+    s, net = wl.spec, wl.net
+    n = s.nV1
+    nsx = 32
+    nl = wl.lgn.nLGN
+    ids = net.lgnId.astype(np.int64)
+    init = wl.init
+    d = dict(
+        nblock=scalar(s.nblock, u32), blockSize=scalar(s.blockSize, u32), nType=scalar(s.nType, u32),
+        nTypeE=scalar(s.nTypeE, u32), nE=scalar(s.nE, u32), ngFF=scalar(s.ngFF, u32), ngE=scalar(s.ngE, u32),
+        ngI=scalar(s.ngI, u32), trainDepth=scalar(wl.seeds.trainDepth, u32), dt=scalar(s.dt, f32),
+        typeAcc=np.asarray(s.typeAcc, u32),
+        v=init.v, w=init.w if init.w is not None else np.zeros(n, f32), tBack=np.zeros(n, f32),
+        gFF=init.gFF, hFF=init.hFF, gE=init.gE, hE=init.hE, gI=init.gI, hI=init.hI,
+        pFF=np.asarray(s.pFF, f32), pE=np.asarray(s.pE, f32), pI=np.asarray(s.pI, f32),
+        vR=np.asarray(s.vR, f32), vThres=np.asarray(s.vThres, f32), gL=np.asarray(s.gL, f32),
+        C=np.asarray(s.C, f32), tRef=np.asarray(s.tRef, f32), vT=np.asarray(s.vT, f32),
+        deltaT=np.asarray(s.deltaT, f32), tau_w=np.asarray(s.tau_w, f32), a=np.asarray(s.a, f32),
+        b=np.asarray(s.b, f32), synFailFF=np.asarray(s.synFailFF, f32),
+        synPerConFF=np.asarray(s.synPerConFF, f32), synFail=np.asarray(s.synFail, f32),
+        synPerCon=np.asarray(s.synPerCon, f32), noisyDep=np.asarray(s.noisyDep, f32),
+        riseFF=np.asarray(s.riseFF, f32), decayFF=np.asarray(s.decayFF, f32),
+        riseE=np.asarray(s.riseE, f32), decayE=np.asarray(s.decayE, f32),
+        riseI=np.asarray(s.riseI, f32), decayI=np.asarray(s.decayI, f32),
+        sp0=np.asarray(sp0 if sp0 is not None else np.zeros(2 * s.nType), f32),
+        tonicDep=net.tonicDep, nLGNperV1=net.nLGNperV1, maxLGN=scalar(net.maxLGN, u32),
+        sLGN=net.sLGN, LGN_idx=(ids % nsx).astype(i32), LGN_idy=(ids // nsx).astype(i32),
+        seed=scalar(wl.seeds.cond, u64), SCsplit=scalar(wl.seeds.SCsplit, u32),
+        noDelay=scalar(1, i32), iModel=scalar(s.iModel, i32), noiseOnTonic=scalar(int(bool(s.noiseOnTonic)), i32))
+    for k in list(d):
+        d[k] = np.ascontiguousarray(d[k])
+    if lgn_rows is not None:
+        cells = np.arange(nl)
+        d.update(T=scalar(T, u32), snapEvery=scalar(V1_SNAP, u32), nLGNcells=scalar(nl, u32),
+                 nsx=scalar(nsx, u32), nsy=scalar((nl + nsx - 1) // nsx, u32),
+                 cell_x=(cells % nsx).astype(i32), cell_y=(cells // nsx).astype(i32),
+                 lgnSInfo=np.ascontiguousarray(lgn_rows[:T], f32).reshape(-1),
+                 nnb=scalar(net.nnb, u32), conMat=np.ascontiguousarray(net.conMat, f32).reshape(-1),
+                 nNearNB=net.nNearNB, nbId=np.ascontiguousarray(net.nbId).reshape(-1))
+    return d
+
+
+STATE_KEYS = ("v", "w", "tBack", "gFF", "hFF", "gE", "hE", "gI", "hI")
+
+
+# ---- LGN convolution: store_PM (magno) + LGN_convol_magno ---------------------------------
+MAGNO_T, MAGNO_STRIDE = 400, 4
+
+
+def magno_workload():
+    """128 ON/OFF magno cells (16 x 16 samples, 250-tap temporal kernels at 1 ms) on 64 x 64
+    grating frames at 120 Hz; 400 steps reach the sixth frame."""
+    from visual_cortex_gb300 import synth
+    return synth.make_workload("magno-pin", seed=5, nblock=1, n_lgn=128, m=20, width=64, height=64,
+                               nt=MAGNO_T, nFrame=8)
+
+
+def magno_inputs(wl) -> dict:
+    lg, s = wl.lgn, wl.lgn.sched
+    assert lg.nParvo == 0 and lg.nMagno_C == 0
+    fr = np.ascontiguousarray(wl.stim.frames, f32)
+    spatial = np.concatenate([np.asarray(getattr(lg, k), f32) for k in ("polar", "rw", "ecc", "rh", "orient", "k")])
+    temporal = np.concatenate([np.asarray(getattr(lg, k), f32) for k in ("tauR", "tauD", "delay", "ratio", "nR", "nD")])
+    return dict(nLGN=scalar(lg.nLGN, u32), mSample1D=scalar(lg.mSample1D, u32),
+                mKernelSample=scalar(s.mKernelSample, u32), kernelSampleDt=scalar(s.mKernelSampleDt, f32),
+                kernelSampleT0=scalar(s.mKernelSampleT0f, f32), spatial=spatial, temporal=temporal,
+                coneType=np.asarray(lg.coneType, u32), L_x0=scalar(lg.L_x0, f32), L_y0=scalar(lg.L_y0, f32),
+                R_x0=scalar(lg.R_x0, f32), R_y0=scalar(lg.R_y0, f32),
+                normViewDistance=scalar(lg.normViewDistance, f32), nsig=scalar(lg.nsig, f32),
+                flat_retina=scalar(int(bool(lg.flat_retina)), i32), width=scalar(fr.shape[3], u32),
+                height=scalar(fr.shape[2], u32), nFrame=scalar(fr.shape[0], u32), frames=fr.reshape(-1),
+                initLMS=np.asarray(wl.stim.init_LMS, f32), maxFrame=scalar(s.maxFrame, u32),
+                ntPerFrame=scalar(s.ntPerFrame, u32), denorm=scalar(s.denorm, u32),
+                magnoComp=scalar(s.magnoComp, u32), frameOffset=scalar(s.dFrame if s.pLongerThanM else 0, u32),
+                kernelSampleInterval=scalar(s.mKernelSampleInterval, u32),
+                iKernelSampleT0=scalar(s.mKernelSampleT0, u32), dt=scalar(s.dt, f32),
+                T=scalar(MAGNO_T, u32), stride=scalar(MAGNO_STRIDE, u32))

@@ -23,7 +23,8 @@ ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "call out of order", -4: "un
 
 REC_RAW, REC_LGN_SP, REC_LGN_FR, REC_SPIKES = 1, 2, 4, 8
 ST = dict(v=0, w=1, tBack=2, dep=3, gFF=4, hFF=5, gE=6, hE=7, gI=8, hI=9, sInfo=10,
-          lgn_ltr=11, lgn_lnl=12, lgn_sInfo=13, farPull=14)
+          lgn_ltr=11, lgn_lnl=12, lgn_sInfo=13, farPull=14, lgn_rng=15, v1_rng_cond=16,
+          v1_rng_noisy=17)
 
 _f2 = C.c_float * MAX_NG
 _t2 = C.c_float * MAX_NTYPE
@@ -146,6 +147,7 @@ def _load() -> C.CDLL:
         "pv1_run_timed": ([P, C.c_uint32, C.c_uint64, _FP], C.c_int),
         "pv1_time_kernels": ([P, C.c_uint32, _FP, _FP, C.POINTER(C.c_int)], C.c_int),
         "pv1_persistent_mode": ([P, C.c_int], C.c_int),
+        "pv1_set_wait_limit": ([P, C.c_int64], C.c_int),
         "pv1_lgn_spikes_noalloc": ([P, C.c_uint32, _FP, _FP], C.c_int),
         "pv1_batch_create": ([C.POINTER(P), C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(P)], C.c_int),
         "pv1_batch_destroy": ([P], None),

@@ -29,6 +29,9 @@ constexpr int kErrNegTsp = 2;           // interpolated spike time < 0 or NaN
 constexpr int kErrFarOverflow = 4;      // far event beyond the delay ring
 constexpr int kErrBounds = 8;           // an index failed its bounds check
 constexpr int kErrBarrier = 16;         // a grid barrier gave up waiting
+// Polls of a grid or trial barrier before it gives up (about 1 s); pv1_set_wait_limit
+// changes it per plan.
+constexpr long long kDefaultWaitSpins = 20000000;
 
 // Two-state (g, h) conductance kernel with rise and decay times: the kinetics of the
 // reference's ConductanceShape (src/condShape.h:13-41).  dod = tr/(td - tr).
@@ -157,6 +160,7 @@ struct V1Params {
     int multiSpike;     // dt > min tRef: several spikes per step (compute_V_collect_spike_learnFF)
     int condRng;        // rGenCond draws can change results (some failure rate > 0)
     int noiseRng;       // some noisyDep > 0
+    long long waitSpins;   // polls of a barrier wait before it gives up and raises kErrBarrier
     // state [nV1] / [ng][nV1]
     float *v, *w, *tBack, *dep, *gFF, *hFF, *gE, *hE, *gI, *hI, *tonicDep, *lastNoise;
     curandStateMRG32k3a *rGenCond, *rNoisy;

@@ -160,6 +160,7 @@ int check_device_error(pv1_plan *p) {
         if (h & kErrNegTsp) m += " negative or NaN spike time;";
         if (h & kErrFarOverflow) m += " far event beyond delay ring;";
         if (h & kErrBounds) m += " bounds check;";
+        if (h & kErrBarrier) m += " a barrier wait gave up (pv1_set_wait_limit);";
         return fail(p, PV1_E_DEVICE, m);
     }
     return PV1_OK;
@@ -438,6 +439,7 @@ int pv1_plan_create(const pv1_v1_config *cfg, pv1_plan **out) {
     }
     v.err = p->d_err;
     v.recSlots = 1;
+    v.waitSpins = kDefaultWaitSpins;
     *out = p;
     PV1_CUDA(p, compute_step_decay(v, p->stream));
     return PV1_OK;
@@ -1527,6 +1529,14 @@ static int choose_mode(pv1_plan *p) {
     return PV1_OK;
 }
 
+int pv1_set_wait_limit(pv1_plan *p, int64_t spins) {
+    if (!p) return PV1_E_ARG;
+    if (spins < 0) spins = kDefaultWaitSpins;
+    p->vp.waitSpins = spins;
+    drop_graph(p);   // captured launches hold the old parameters
+    return PV1_OK;
+}
+
 int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
     if (!p) return PV1_E_ARG;
     if (p->lgnOnly) return fail(p, PV1_E_STATE, "the plan was stepped by pv1_lgn_spikes_noalloc (LGN only)");
@@ -2072,6 +2082,9 @@ int pv1_get_state(pv1_plan *p, int which, float *out) {
             src = v.farPull;
             cnt = (size_t)(c.ngE + c.ngI) * 2 * n;
             break;
+        case PV1_ST_LGN_RNG: src = p->lp.state; cnt = p->nLGN * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
+        case PV1_ST_V1_RNG_COND: src = v.rGenCond; cnt = n * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
+        case PV1_ST_V1_RNG_NOISY: src = v.rNoisy; cnt = n * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
         default: return fail(p, PV1_E_ARG, "unknown state id");
     }
     if (!src) return fail(p, PV1_E_STATE, "state not allocated");

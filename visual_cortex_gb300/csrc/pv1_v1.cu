@@ -34,7 +34,6 @@ constexpr int kMaxBS = 1024;
 constexpr int kLgnBatch = 8;
 constexpr int kMaxLgnReg = 32;        // LGN synapse ids kept in registers by the persistent kernel
 constexpr int kConBatch = 8;          // conMat rows fetched together
-constexpr long long kBarrierSpins = 20000000;  // ~1 s of polling before a barrier gives up
 
 __device__ __forceinline__ int type_of(const V1Params &P, int local) {
     int t = P.nType - 1;
@@ -1208,13 +1207,13 @@ __device__ __forceinline__ void barrier_arrive(unsigned *count, unsigned *s_arri
 }
 
 __device__ __forceinline__ bool barrier_wait(unsigned *count, unsigned target, const unsigned *s_arrived,
-                                             int *err) {
+                                             int *err, long long limit) {
     __shared__ int s_ok;
     if (threadIdx.x == 0) {
         unsigned c = *s_arrived;
         long long spins = 0;
         while ((c & ~kBarrierAbort) < target && !(c & kBarrierAbort)) {
-            if (++spins > kBarrierSpins) {
+            if (++spins > limit) {
                 atomicOr(err, kErrBarrier);
                 atomicOr(count, kBarrierAbort);
                 c = kBarrierAbort;
@@ -1287,7 +1286,8 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
             lgnPre.mask = 0u;
             if (active) lgnPre = lgn_prefetch<1>(P, lgnRing + (size_t)((t + 1) % lgnSlots) * P.lgnN, lgnIds, m, i);
             haveMask = true;
-            if (!barrier_wait(barrier, (unsigned)gridDim.x * (unsigned)(s + 1), &s_arrived, P.err)) break;
+            if (!barrier_wait(barrier, (unsigned)gridDim.x * (unsigned)(s + 1), &s_arrived, P.err, P.waitSpins))
+                break;
         }
     }
     if (active) {
@@ -1787,7 +1787,7 @@ __device__ __forceinline__ void batch_trial_steps(const V1Params &P, long long t
             if (smemIds && active)
                 pre = lgn_prefetch<kCta>(P, lgnRing + (size_t)((t + 1) % lgnSlots) * P.lgnN, sIds + threadIdx.x, m, i);
             havePre = smemIds;
-            if (!barrier_wait(barrier, (unsigned)nCta * (unsigned)(s + 1), s_arrived, P.err)) break;
+            if (!barrier_wait(barrier, (unsigned)nCta * (unsigned)(s + 1), s_arrived, P.err, P.waitSpins)) break;
         }
     }
     if (active) {

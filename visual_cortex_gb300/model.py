@@ -449,9 +449,12 @@ class Simulation:
         n = spec.nV1
         sizes = dict(gFF=spec.ngFF * n, hFF=spec.ngFF * n, gE=spec.ngE * n, hE=spec.ngE * n,
                      gI=spec.ngI * n, hI=spec.ngI * n, lgn_ltr=self.lgn.nLGN, lgn_lnl=self.lgn.nLGN,
-                     lgn_sInfo=self.lgn.nLGN, farPull=(spec.ngE + spec.ngI) * 2 * n)
+                     lgn_sInfo=self.lgn.nLGN, farPull=(spec.ngE + spec.ngI) * 2 * n,
+                     lgn_rng=12 * self.lgn.nLGN, v1_rng_cond=12 * n, v1_rng_noisy=12 * n)
         out = np.empty(sizes.get(name, n), f32)
         N.check(self.plan, N.lib.pv1_get_state(self.plan, N.ST[name], N.fptr(out)), f"pv1_get_state({name})")
+        if name.endswith("_rng") or name.startswith("v1_rng"):
+            return out.view(np.uint8)       # 48 raw bytes (one curandStateMRG32k3a) per entry
         return out
 
     def frames_setup(self, pix_off: np.ndarray, pix_ids: np.ndarray, n_spike_pixel: int, ot: int, odt: float):

@@ -343,8 +343,16 @@ int pv1_frames_collect(pv1_plan *plan, uint64_t step0, uint32_t n, float *frames
 int pv1_checkpoint_size(pv1_plan *plan, uint64_t *bytes);
 int pv1_checkpoint_save(pv1_plan *plan, void *buf, uint64_t bytes);
 int pv1_checkpoint_load(pv1_plan *plan, const void *buf, uint64_t bytes);
+/* The step count of a plan whose state was loaded array by array (pv1_put_state), as a
+ * snapshot in the reference's layout is (src/patch.cu:5489-5685): sets it, drops the pending
+ * delivery (the loaded conductances already hold it) and empties the delayed-event rings and
+ * far spiker lists -- the reference's snapshot holds no far events in flight, its far rings
+ * being host vectors it does not save.  noDelay = 0 plans: PV1_E_UNSUPPORTED. */
+int pv1_set_step(pv1_plan *plan, int64_t step);
 
-/* Overwrites one state array (PV1_ST_* above). */
+/* Overwrites one state array (PV1_ST_* above; the generators as the raw bytes get_state
+ * gives, which is how a snapshot in the reference's layout, src/patch.cu:6793-6912, is loaded;
+ * not the spike words or the far sums). */
 int pv1_put_state(pv1_plan *plan, int which, const float *in);
 
 /* Draw recording for parity tests: when enabled, every uniform/normal the kernels draw is

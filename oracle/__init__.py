@@ -75,7 +75,7 @@ def lib():
         L.orc_adex_rk2.argtypes = [F] * 19 + [FP, FP]
         L.orc_adex_spike.argtypes = [F] * 5 + [FP, FP]
         L.orc_logistic_ab.argtypes = [FP, FP, FP, C.c_int, FP, FP]
-        L.orc_v1_deliver_near_delayed.argtypes = [P]
+        L.orc_v1_deliver_near_delayed.argtypes = [P, FP, C.c_int]
         L.orc_std_normal_draws.argtypes = [C.POINTER(C.c_uint64), C.c_int, IP, C.c_int, FP]
         L.orc_v1_set_far_failure.argtypes = [P, C.c_uint64, C.c_int]
         L.orc_v1_init_spikes.argtypes = [P, FP, C.c_uint32, C.c_int, FP, UP, C.c_uint32, FP, UP, C.c_uint32, FP]
@@ -314,7 +314,7 @@ class V1Oracle:
                                   fp(None if noise is None else np.ascontiguousarray(noise, f32)),
                                   fp(None if ff is None else np.ascontiguousarray(ff, f32)), int(cap))
         if self.delayed:
-            L.orc_v1_deliver_near_delayed(self.h)
+            L.orc_v1_deliver_near_delayed(self.h, fp(None if near is None else np.ascontiguousarray(near, f32)), int(cap))
         else:
             L.orc_v1_deliver_near(self.h, fp(None if near is None else np.ascontiguousarray(near, f32)), int(cap))
         L.orc_v1_deliver_far(self.h)

@@ -98,6 +98,10 @@ def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None
             (pTW, _, _), PS = gpu_parvo
             lo.pTW[:] = pTW
             lo.PS = np.ascontiguousarray(PS)
+    # the initial carried integrals come from the library's LGN generators (the oracle does
+    # not re-derive cuRAND); those generators and lastNegLogRand are held byte for byte to the
+    # reference's own logRand_init (tests/test_ref_kernels.py), so the copy carries no
+    # unchecked state into the comparison
     lo.lnl[:] = lnl0
     lo.ltr[:] = ltr0
     vo = V1Oracle(wl.spec, wl.net)

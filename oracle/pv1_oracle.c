@@ -1180,7 +1180,13 @@ int orc_v1_set_delays(orc_v1 *o, const float *delayMat, int trainDepth) {
     return 0;
 }
 
-int orc_v1_deliver_near_delayed(orc_v1 *o) {
+/* recal_G_mat (src/coredynamics.cu:2063-2309): each post neuron walks its near blocks, every
+ * pre neuron of a block in index order and the two spike-word slots that can hold an event
+ * arriving in this step; with a failure rate p > 0 for the (pre type, post type) pair --
+ * the pre type from the pre neuron's index -- each arriving event scales its strength by
+ * 1 - p + sqrt(p (1-p)/synPerCon) z with z the post's next normal draw (`near`: this step's
+ * recorded draws [nV1][cap], in that order). */
+int orc_v1_deliver_near_delayed(orc_v1 *o, const float *near, int cap) {
     const pv1_v1_config *c = &o->c;
     const int nV1 = o->nV1, bs = o->bs, depth = o->trainDepth;
     const float dt = c->dt;
@@ -1191,6 +1197,7 @@ int orc_v1_deliver_near_delayed(orc_v1 *o) {
         const int b = ipost / bs, local = ipost % bs;
         const int it = otype(o, local);
         float lgE[PV1_MAX_NG] = {0, 0}, lhE[PV1_MAX_NG] = {0, 0}, lgI[PV1_MAX_NG] = {0, 0}, lhI[PV1_MAX_NG] = {0, 0};
+        int ndraw = 0;
         for (uint32_t ib = 0; ib < o->nNearNB[b]; ib++) {
             const size_t local_bid = (size_t)b * o->nnb + ib;
             const int bid = (int)o->nbId[local_bid];
@@ -1199,6 +1206,9 @@ int orc_v1_deliver_near_delayed(orc_v1 *o) {
                 const size_t mid = (local_bid * bs + i) * bs + local;
                 const float strength = o->conMat[mid];
                 if (strength == 0) continue;
+                const int jtype = otype(o, i);
+                const float p = c->synFail[jtype * c->nType + it];
+                const float nSyn = c->synPerCon[jtype * c->nType + it];
                 float time2post = o->delayMat[mid] / c->speedOfThought;
                 const unsigned it2post = (unsigned)ceilf(time2post / dt);
                 time2post = it2post * dt - time2post;
@@ -1211,7 +1221,13 @@ int orc_v1_deliver_near_delayed(orc_v1 *o) {
                         const float nsp = floorf(dtsp);
                         dtsp = (dtsp - nsp + j) * dt - time2post;
                         if (dtsp < dt && dtsp >= 0) {
-                            const float f = strength;
+                            float f = strength;
+                            if (p > 0) {
+                                const float normed_std = sqrtf(p * (1 - p) / nSyn);
+                                const float rnd = (near && ndraw < cap) ? near[(size_t)ipost * cap + ndraw] : 0.f;
+                                ndraw++;
+                                f *= 1 - p + normed_std * rnd;
+                            }
                             if (f > 0) {
                                 dtsp = dt - dtsp;
                                 if (isE) {
@@ -1622,7 +1638,7 @@ int orc_v1_init_spikes(orc_v1 *o, const float *sp0, uint32_t SCsplit, int depth,
         memcpy(o->spikeRing, H, (size_t)depth * nV1 * sizeof(float));
         memcpy(o->sInfo, H, (size_t)nV1 * sizeof(float));
         o->curSlot = 0;
-        orc_v1_deliver_near_delayed(o);
+        orc_v1_deliver_near_delayed(o, z, (int)capZ);
         o->curSlot = 0;
     }
     /* far: fill_fSpikeTrain with the history slot depth-1, recal_G_vec + sum_G */

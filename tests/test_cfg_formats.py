@@ -108,3 +108,38 @@ def test_output_headers_byte_layout():
     s.close()
     dt, sp = FM.read_lgn_sp(os.path.join(d, "sp"))
     assert dt == 0.125 and sp.shape == (1, 3)
+
+
+def test_reference_snapshot_layout_round_trip():
+    """write_reference_snapshot puts the fields in the reference's order and sizes
+    (src/patch.cu:6793-6912: 11 indices, iModel, learning, 7 sizes, the LGN block
+    2 nLGN floats + nLGN generators, rGenCond, rNoisy, tBack, the spike-word ring, then dep, w,
+    v, gFF, hFF, gE, gI, hE, hI, gap); read_reference_snapshot reads them back and returns what
+    follows them."""
+    import tempfile
+    from visual_cortex_gb300 import formats as FM
+    rng = np.random.default_rng(0)
+    n, nl, depth, ngFF, ngE, ngI, nI = 64, 16, 3, 2, 2, 1, 16
+    idx = {k: int(rng.integers(0, 1000)) for k in FM.SNAPSHOT_INDICES}
+    f = lambda k: rng.standard_normal(k).astype(np.float32)
+    lgn = dict(ltr=f(nl), lnl=f(nl), rng=rng.integers(0, 256, 48 * nl).astype(np.uint8))
+    v1 = dict(rng_cond=rng.integers(0, 256, 48 * n).astype(np.uint8),
+              rng_noisy=rng.integers(0, 256, 48 * n).astype(np.uint8), tBack=f(n))
+    ring = f(depth * n).reshape(depth, n)
+    state = dict(dep=f(n), w=f(n), v=f(n), gFF=f(ngFF * n), hFF=f(ngFF * n), gE=f(ngE * n), gI=f(ngI * n),
+                 hE=f(ngE * n), hI=f(ngI * n), gap=f(nI))
+    sizes = dict(nV1=n, nLGN=nl, ngFF=ngFF, ngE=ngE, ngI=ngI, nType=2, trainDepth=depth)
+    with tempfile.TemporaryDirectory() as d:
+        fn = d + "/snap.bin"
+        FM.write_reference_snapshot(fn, idx, 1, 0, sizes, lgn, v1, ring, state, b"TRAILER")
+        size = (11 + 2 + 7) * 4 + (2 * nl * 4 + nl * 48) + 2 * n * 48 + n * 4 + depth * n * 4 + \
+            (n * 3 + 2 * (ngFF + ngE + ngI) * n + nI) * 4 + len(b"TRAILER")
+        import os
+        assert os.path.getsize(fn) == size
+        snap, trailer = FM.read_reference_snapshot(fn, nI)
+    assert trailer == b"TRAILER" and snap["idx"] == idx and snap["sizes"] == sizes and snap["iModel"] == 1
+    for k in state:
+        np.testing.assert_array_equal(snap["state"][k], state[k])
+    np.testing.assert_array_equal(snap["spike_train"], ring)
+    np.testing.assert_array_equal(snap["lgn"]["rng"], lgn["rng"])
+    np.testing.assert_array_equal(snap["v1"]["tBack"], v1["tBack"])

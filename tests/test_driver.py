@@ -163,9 +163,67 @@ def test_snapshot_resume_continues_the_run(written, native):
     _, r2 = FM.read_raw(cfg.resolve_paths(c2).raw)
     _, r3 = FM.read_raw(cfg.resolve_paths(cfg.load(["-c", fn, "--outputFolder", out3, "--output_suffix", "s"])).raw)
     np.testing.assert_array_equal(r2, r3[96:])
-    with pytest.raises(cfg.ConfigError, match="asInit"):
-        driver.build(cfg.load(["-c", fn, "--fSnapshot", "!" + out1 + name, "--snapshot_suffix", "s",
-                               "--output_suffix", "s"]))
+
+
+@pytest.mark.gpu
+def test_reference_layout_snapshot(native):
+    """Snapshots in the reference's layout (src/patch.cu:6793-6912): the indices, sizes and the
+    newest slot of the spike-word ring are where the reference writes them; a snapshot cut to
+    the reference's own fields (as the reference writes it) resumes a run without far synapses
+    bit for bit (src/patch.cu:5489-5685, asInit = false), and with asInit = true it is the
+    initial state of a new run at step 0."""
+    import glob
+    import os
+    from visual_cortex_gb300.model import Simulation
+    wl = synth.make_workload("snap", seed=4, nblock=1, n_lgn=512, m=20, width=64, height=64, nt=64,
+                             adex_inh=True, nFrame=40)
+    d = tempfile.mkdtemp()
+    fn = synth.write_reference_files(wl, d, seed=4, nt=64)
+    outs = [os.path.join(d, x) + "/" for x in ("a", "b", "c")]
+    lgn = cfg.resolve_paths(cfg.load(["-c", fn])).lgn
+    import shutil
+    for o in outs:
+        os.makedirs(o, exist_ok=True)
+        shutil.copy(lgn, o + os.path.basename(lgn))
+    quiet = dict(chunk=16, log=lambda *_: None)
+    driver.run(cfg.load(["-c", fn, "--outputFolder", outs[0], "--output_suffix", "s", "--nt", "32"]), **quiet)
+    snap_fn = glob.glob(outs[0] + "snapShot_*_s.bin")[0]
+    m = driver.build(cfg.load(["-c", fn]))
+    snap, trailer = FM.read_reference_snapshot(snap_fn, m.spec.nI * m.spec.nblock)
+    assert trailer[:8] == b"PV1CKPT\0"
+    depth = int(m.seeds.trainDepth)
+    assert snap["idx"]["step"] == 32 and snap["idx"]["currentTimeSlot"] == 32 % depth
+    assert snap["sizes"]["nV1"] == m.spec.nV1 and snap["sizes"]["trainDepth"] == depth
+    _, raw = FM.read_raw(cfg.resolve_paths(cfg.load(["-c", fn, "--outputFolder", outs[0], "--output_suffix", "s"])).raw)
+    np.testing.assert_array_equal(snap["spike_train"][31 % depth], raw[31, :m.spec.nV1])
+    # the reference's own fields only
+    ref_only = outs[0] + "refsnap_s.bin"
+    with open(snap_fn, "rb") as f:
+        data = f.read()
+    with open(ref_only, "wb") as f:
+        f.write(data[:len(data) - len(trailer)])
+    c2 = cfg.load(["-c", fn, "--outputFolder", outs[1], "--output_suffix", "s", "--nt", "32",
+                   "--fSnapshot", "!" + outs[0] + "refsnap", "--snapshot_suffix", "s", "--asInit", "false"])
+    driver.run(c2, **quiet)
+    driver.run(cfg.load(["-c", fn, "--outputFolder", outs[2], "--output_suffix", "s", "--nt", "64"]), **quiet)
+    _, r2 = FM.read_raw(cfg.resolve_paths(c2).raw)
+    _, r3 = FM.read_raw(cfg.resolve_paths(cfg.load(["-c", fn, "--outputFolder", outs[2], "--output_suffix", "s"])).raw)
+    np.testing.assert_array_equal(r2, r3[32:])
+    # asInit = true: the snapshot's state at step 0
+    c4 = cfg.load(["-c", fn, "--fSnapshot", "!" + outs[0] + "refsnap", "--snapshot_suffix", "s", "--asInit", "true"])
+    m4 = driver.build(c4)
+    sim = Simulation(m4.spec, m4.net, m4.lgn, m4.stim, m4.init, m4.seeds)
+    try:
+        assert driver._restore(sim, c4, m4) == 0 and sim.step == 0
+        for k in ("v", "gE", "gI", "gFF", "hFF"):
+            np.testing.assert_array_equal(sim.state(k), snap["state"][k], err_msg=k)
+        np.testing.assert_array_equal(sim.state("tBack"), snap["v1"]["tBack"])
+        np.testing.assert_array_equal(sim.state("v1_rng_cond"), snap["v1"]["rng_cond"])
+        np.testing.assert_array_equal(sim.state("lgn_rng"), snap["lgn"]["rng"])
+        sim.run(16)
+        assert np.isfinite(sim.state("v")).all()
+    finally:
+        sim.close()
 
 
 def test_frame_geometry_and_pixels():

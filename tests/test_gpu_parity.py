@@ -142,6 +142,29 @@ def test_far_delivery_parity(native):
         assert cmp[f"max_rel_{k}"] < 1e-5, cmp
 
 
+def test_full_patch_workload_parity(native):
+    """The benchmarked workload itself: 32 x 1024 neurons (80% LIF E / 20% AdEx I), 16384
+    LGN cells on 128 x 128 frames, ~400 far partners per neuron with distance delays, run by
+    the persistent kernel (one cooperative launch per 64 steps) for 400 steps (50 ms)
+    against the oracle: LGN spikes identical, rasters identical (or parting at a threshold
+    crossing decided by float rounding), traces within 1e-5 until the first spike-time
+    divergence."""
+    from visual_cortex_gb300 import synth
+    from oracle.parity import run_parity, compare
+    wl = synth.config2(seed=0)
+    assert wl.spec.nV1 == 32768 and wl.lgn.nLGN == 16384 and wl.spec.iModel == 1
+    assert 350 < float(np.mean(wl.net.nVec)) < 450
+    res = run_parity(wl, RASTER_STEPS, cap=8)
+    assert res["launches"] < RASTER_STEPS // 4            # persistent: a launch per chunk, not per step
+    cmp = compare(res, wl.spec)
+    assert res["draw_count_mismatch"] == 0
+    assert cmp["lgn_spike_mismatch"] == 0, cmp
+    assert_raster_ok(cmp)
+    assert cmp["v1_spikes_gpu"] > 10000, cmp
+    for k in ("v", "gE", "gI", "gFF"):
+        assert cmp[f"max_rel_{k}"] < 1e-5, cmp
+
+
 def test_delayed_near_delivery_parity(native):
     """noDelay = 0: recal_G_mat's distance-delayed near delivery (spike-word ring, two slots
     per synapse) vs the GPU's delayed-event ring, with far delivery alongside."""
@@ -154,6 +177,26 @@ def test_delayed_near_delivery_parity(native):
     cmp = compare(res, wl.spec)
     assert cmp["v1_spikes_gpu"] > 0, cmp
     assert_raster_ok(cmp)
+    for k in ("v", "gE", "gI"):
+        assert cmp[f"max_rel_{k}"] < 1e-5, cmp
+
+
+def test_delayed_near_failure_parity(native):
+    """noDelay = 0 with synaptic failure: recal_G_mat's failure draws (a normal from the post's
+    generator per arriving event of a pair with p > 0, in the order near block, pre index,
+    ring slot; src/coredynamics.cu:2138-2224) pulled by post on the GPU, against the oracle's
+    restatement on the same draws; far synapses with failure alongside."""
+    from visual_cortex_gb300 import synth
+    from oracle.parity import run_parity, compare
+    wl = synth.make_workload("delayed-fail", seed=8, nblock=2, n_lgn=512, m=20, width=64, height=64,
+                             nt=800, far_partners=50, adex_inh=True, nFrame=60, noDelay=0,
+                             synFail=(0.2, 0.1, 0.3, 0.15))
+    assert wl.spec.noDelay == 0 and max(wl.spec.synFail) > 0
+    res = run_parity(wl, RASTER_STEPS, cap=16)
+    cmp = compare(res, wl.spec)
+    assert res["draw_count_mismatch"] == 0
+    assert cmp["v1_spikes_gpu"] > 0, cmp
+    assert_raster_ok(cmp, steps=64)
     for k in ("v", "gE", "gI"):
         assert cmp[f"max_rel_{k}"] < 1e-5, cmp
 

@@ -130,6 +130,7 @@ def _load() -> C.CDLL:
         "pv1_checkpoint_size": ([P, C.POINTER(C.c_uint64)], C.c_int),
         "pv1_checkpoint_save": ([P, C.c_void_p, C.c_uint64], C.c_int),
         "pv1_checkpoint_load": ([P, C.c_void_p, C.c_uint64], C.c_int),
+        "pv1_set_step": ([P, C.c_int64], C.c_int),
         "pv1_v1_init_spikes": ([P, C.c_uint64, C.c_uint32, _FP, C.c_uint32, C.POINTER(InitRecord)], C.c_int),
         "pv1_host_init_state": ([C.POINTER(V1Config), C.c_uint64, _FP, _UP, C.c_int, C.c_float,
                                  _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP, _FP],

@@ -207,6 +207,16 @@ struct V1Params {
     const float *pullStd;      // [nnz] sqrt(p(1-p)/synPerCon)
     const unsigned char *pullIsPre;  // [nV1] 1 if the neuron is a far presynaptic partner
     float *sRing; int sDepth;  // [sDepth][nV1] spike words of the last sDepth steps (row = step mod sDepth)
+    // distance-delayed near synapses with synaptic failure (noDelay = 0, some synFail > 0),
+    // pulled by post in recal_G_mat's order: near blocks, then pre neurons by index
+    int nearPullOn;
+    const int *npOff;          // [nV1+1]
+    const int *npPre;          // [nnz]
+    const int *npSteps;        // [nnz] it2post
+    const float *npStr;        // [nnz]
+    const float *npFrac;       // [nnz] it2post*dt - delay/speed
+    const float *npP;          // [nnz] failure rate of the (pre type, post type) pair
+    const float *npStd;        // [nnz] sqrt(p(1-p)/synPerCon)
     unsigned *eng;             // [nV1] minstd_rand0 states
     int *pullCount, *pullStart, *pullPrev;  // [nV1] draws this step, first draw's index in the chunk, previous drawer
     float *pullCarry;          // [nV1] the unused second value of a post's last pair

@@ -285,8 +285,8 @@ int plan_batch_view(pv1_plan *p, PlanBatchView *out) {
     if (er) return er;
     if (!p->haveLGNsyn || !p->haveNear || !p->haveState || !p->haveRng)
         return fail(p, PV1_E_STATE, "V1 synapses/connectivity/state/rng not set");
-    if (p->vp.farPullOn)
-        return fail(p, PV1_E_UNSUPPORTED, "batched trials with far synaptic failure are not built");
+    if (p->vp.farPullOn || p->vp.nearPullOn)
+        return fail(p, PV1_E_UNSUPPORTED, "batched trials with synaptic failure on delayed synapses are not built");
     out->vp = p->vp;
     out->lp = p->lp;
     out->lgnRing = p->d_lgnRing;
@@ -1159,6 +1159,21 @@ int rebuild_events(pv1_plan *p) {
 
 extern "C" {
 
+// The spike-word ring read by the pulled deliveries: at least D rows, zero-filled (no spikes
+// before the first step).
+static int ensure_spike_ring(pv1_plan *p, int D) {
+    V1Params &v = p->vp;
+    if (v.sRing && v.sDepth >= D) return PV1_OK;
+    if (v.sRing) free_one(p, v.sRing);
+    v.sRing = nullptr;
+    float *d = nullptr;
+    int r = dev_alloc(p, &d, (size_t)D * p->nV1);
+    if (r) return r;
+    v.sRing = d;
+    v.sDepth = D;
+    return PV1_OK;
+}
+
 // Far synapses by post in the reference's vec order for the failure path: pre, strength,
 // whole-step delay and offset (as build_event_lists computes them), failure rate and its
 // normed std per (pre type, post type), the spike-word ring and the per-step scratch.
@@ -1201,7 +1216,7 @@ static int build_far_pull(pv1_plan *p, const uint32_t *nVec, const uint32_t *vec
     const int D = maxSteps + 2;
     const int ns = (int)(c.ngE + c.ngI);
     int *d_off, *d_pre, *d_steps, *d_cnt, *d_start, *d_prev, *d_flag;
-    float *d_str, *d_frac, *d_p, *d_sd, *d_ring, *d_carry, *d_pull;
+    float *d_str, *d_frac, *d_p, *d_sd, *d_carry, *d_pull;
     unsigned char *d_isPre;
     unsigned *d_eng;
     int r = 0;
@@ -1213,7 +1228,7 @@ static int build_far_pull(pv1_plan *p, const uint32_t *nVec, const uint32_t *vec
     r |= dev_upload(p, &d_p, pf.data(), nnz);
     r |= dev_upload(p, &d_sd, sd.data(), nnz);
     r |= dev_upload(p, &d_isPre, isPre.data(), nV1);
-    r |= dev_alloc(p, &d_ring, (size_t)D * nV1);
+    r |= ensure_spike_ring(p, D);
     r |= dev_alloc(p, &d_eng, nV1);
     r |= dev_alloc(p, &d_cnt, nV1);
     r |= dev_alloc(p, &d_start, nV1);
@@ -1231,8 +1246,6 @@ static int build_far_pull(pv1_plan *p, const uint32_t *nVec, const uint32_t *vec
     v.pullP = d_p;
     v.pullStd = d_sd;
     v.pullIsPre = d_isPre;
-    v.sRing = d_ring;
-    v.sDepth = D;
     v.eng = d_eng;
     v.pullCount = d_cnt;
     v.pullStart = d_start;
@@ -1313,18 +1326,99 @@ int pv1_v1_set_far(pv1_plan *p, const uint32_t *nVec, const uint32_t *vecID, con
 // (src/coredynamics.cu:2063-2309) delivers every non-zero conMat entry of the near blocks at
 // the arrival step of its delayMat distance.  Here those entries become delayed events of the
 // same event lists as the far synapses (class "near": no far-spike gate on delivery).
+// Distance-delayed near synapses with synaptic failure, by post in recal_G_mat's order (near
+// blocks as listed, then pre neurons by index, src/coredynamics.cu:2138-2170): pre, strength,
+// whole-step delay and offset (ceil(delay/speed/dt) and it2post*dt - delay/speed in float),
+// failure rate and normed std of the (pre type, post type) pair -- the pre type from the pre
+// neuron's index.
+static int build_near_pull(pv1_plan *p, uint32_t nnb, const uint32_t *nNearNB, const uint32_t *nbId,
+                           const float *conMat, const float *delayMat) {
+    const pv1_v1_config &c = p->cfg;
+    const int nV1 = p->nV1, nblock = (int)c.nblock;
+    const size_t bs = c.blockSize;
+    auto typeOf = [&](int local) {
+        int t = (int)c.nType - 1;
+        for (int j = (int)c.nType - 1; j >= 0; j--)
+            if ((uint32_t)local < c.typeAcc[j]) t = j;
+        return t;
+    };
+    std::vector<int> off(nV1 + 1, 0), pre, steps;
+    std::vector<float> str, frac, pf, sd;
+    int maxSteps = 0;
+    for (int b = 0; b < nblock; b++) {
+        if (nNearNB[b] > nnb) return fail(p, PV1_E_ARG, "nNearNeighborBlock > nearNeighborBlock");
+        for (size_t j = 0; j < bs; j++) {
+            const int post = (int)(b * bs + j);
+            const int itype = typeOf((int)j);
+            for (uint32_t k = 0; k < nNearNB[b]; k++) {
+                const uint32_t nb = nbId[(size_t)b * nnb + k];
+                if (nb >= (uint32_t)nblock) return fail(p, PV1_E_ARG, "neighbour block id out of range");
+                const size_t base = ((size_t)b * nnb + k) * bs * bs;
+                for (size_t i = 0; i < bs; i++) {
+                    const float sv = conMat[base + i * bs + j];
+                    if (sv == 0) continue;
+                    float time2post = delayMat[base + i * bs + j] / c.speedOfThought;
+                    const unsigned it2post = (unsigned)std::ceil(time2post / c.dt);
+                    if (it2post > 0xffff) return fail(p, PV1_E_UNSUPPORTED, "synaptic delay longer than 65535 steps");
+                    const int jtype = typeOf((int)i);
+                    const float fp = c.synFail[jtype * c.nType + itype];
+                    pre.push_back((int)(nb * bs + i));
+                    steps.push_back((int)it2post);
+                    str.push_back(sv);
+                    frac.push_back(it2post * c.dt - time2post);
+                    pf.push_back(fp);
+                    sd.push_back(fp > 0 ? std::sqrt(fp * (1 - fp) / c.synPerCon[jtype * c.nType + itype]) : 0.f);
+                    maxSteps = std::max(maxSteps, (int)it2post);
+                }
+            }
+            off[post + 1] = (int)pre.size();
+        }
+    }
+    const size_t nnz = pre.size();
+    int *d_off, *d_pre, *d_steps;
+    float *d_str, *d_frac, *d_p, *d_sd;
+    int r = 0;
+    r |= dev_upload(p, &d_off, off.data(), off.size());
+    r |= dev_upload(p, &d_pre, pre.data(), nnz);
+    r |= dev_upload(p, &d_steps, steps.data(), nnz);
+    r |= dev_upload(p, &d_str, str.data(), nnz);
+    r |= dev_upload(p, &d_frac, frac.data(), nnz);
+    r |= dev_upload(p, &d_p, pf.data(), nnz);
+    r |= dev_upload(p, &d_sd, sd.data(), nnz);
+    if (r) return r;
+    r = ensure_spike_ring(p, maxSteps + 2);
+    if (r) return r;
+    V1Params &v = p->vp;
+    v.nearPullOn = 1;
+    v.npOff = d_off;
+    v.npPre = d_pre;
+    v.npSteps = d_steps;
+    v.npStr = d_str;
+    v.npFrac = d_frac;
+    v.npP = d_p;
+    v.npStd = d_sd;
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    drop_graph(p);
+    return PV1_OK;
+}
+
 int pv1_v1_set_near_delayed(pv1_plan *p, uint32_t nnb, const uint32_t *nNearNB, const uint32_t *nbId,
                             const float *conMat, const float *delayMat) {
     if (!p || !nNearNB || !nbId || !conMat || !delayMat || nnb < 1) return PV1_E_ARG;
     const pv1_v1_config &c = p->cfg;
     if (c.noDelay) return fail(p, PV1_E_STATE, "pv1_v1_set_near_delayed is for noDelay = 0 plans");
-    for (int q = 0; q < (int)(c.nType * c.nType); q++)
-        if (c.synFail[q] > 0)
-            return fail(p, PV1_E_UNSUPPORTED,
-                        "synaptic failure with distance-delayed near delivery is not built");
+    bool failure = false;
+    for (int q = 0; q < (int)(c.nType * c.nType); q++) failure = failure || c.synFail[q] > 0;
     const int nblock = (int)c.nblock;
     const size_t bs = c.blockSize;
     p->nearSyn.clear();
+    p->vp.nearPullOn = 0;
+    if (failure) {
+        int r = build_near_pull(p, nnb, nNearNB, nbId, conMat, delayMat);
+        if (r) return r;
+        p->haveNear = true;
+        return rebuild_events(p);
+    }
     for (int b = 0; b < nblock; b++) {
         if (nNearNB[b] > nnb) return fail(p, PV1_E_ARG, "nNearNeighborBlock > nearNeighborBlock");
         for (uint32_t k = 0; k < nNearNB[b]; k++) {
@@ -1397,6 +1491,9 @@ int pv1_v1_init_spikes(pv1_plan *p, uint64_t seed, uint32_t trainDepth, const fl
         s0.c[q] = sp0[q];
         has = has || sp0[q] > 0;
     }
+    if (has && p->vp.nearPullOn)
+        return fail(p, PV1_E_UNSUPPORTED,
+                    "initial spikes with synaptic failure on distance-delayed near synapses are not built");
     const V1Params &vp = p->vp;
     const size_t n = p->nV1;
     const int depth = (int)trainDepth;
@@ -1520,7 +1617,7 @@ static int choose_mode(pv1_plan *p) {
     if (p->modeChosen) return PV1_OK;
     bool fits = false;
     v1_persistent_ctas(p->vp, p->device, &fits);
-    p->persistent = fits && p->allowPersistent && !p->vp.multiSpike && !p->vp.farPullOn;
+    p->persistent = fits && p->allowPersistent && !p->vp.multiSpike && !p->vp.farPullOn && !p->vp.nearPullOn;
     if (p->persistent && !p->d_barrier) {
         int r = dev_alloc(p, &p->d_barrier, 2);
         if (r) return r;
@@ -1921,6 +2018,7 @@ void ckpt_items(pv1_plan *p, std::vector<std::pair<void *, size_t>> &items) {
         add(v.farList, 3 * n * sizeof(int4));
         add(v.farCount, 3 * sizeof(int));
     }
+    if (v.nearPullOn && !v.farPullOn) add(v.sRing, (size_t)v.sDepth * n * f);
     if (v.farPullOn) {
         add(v.sRing, (size_t)v.sDepth * n * f);
         add(v.eng, n * sizeof(unsigned));
@@ -1942,7 +2040,7 @@ CkptHeader ckpt_header(pv1_plan *p, const std::vector<std::pair<void *, size_t>>
     h.ngE = p->cfg.ngE;
     h.ngI = p->cfg.ngI;
     h.farDepth = p->vp.farOn ? p->vp.farDepth : 0;
-    h.sDepth = p->vp.farPullOn ? p->vp.sDepth : 0;
+    h.sDepth = (p->vp.farPullOn || p->vp.nearPullOn) ? p->vp.sDepth : 0;
     h.farOn = p->vp.farOn;
     h.farPullOn = p->vp.farPullOn;
     h.nItems = (int32_t)items.size();
@@ -1983,6 +2081,39 @@ int pv1_checkpoint_save(pv1_plan *p, void *buf, uint64_t bytes) {
         off += it.second;
     }
     PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    return PV1_OK;
+}
+
+int pv1_set_step(pv1_plan *p, int64_t step) {
+    if (!p || step < 0) return PV1_E_ARG;
+    if (!p->haveState || !p->haveRng || !p->lgnReady) return fail(p, PV1_E_STATE, "plan not initialised");
+    if (p->lgnOnly) return fail(p, PV1_E_STATE, "the plan was stepped by pv1_lgn_spikes_noalloc (LGN only)");
+    if (!p->cfg.noDelay)
+        return fail(p, PV1_E_UNSUPPORTED,
+                    "state loaded array by array with distance-delayed near synapses (noDelay = 0): the "
+                    "events in flight would need the spike-word history");
+    V1Params &v = p->vp;
+    const size_t n = p->nV1, ns = p->cfg.ngE + p->cfg.ngI;
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    auto zero = [&](void *ptr, size_t bytes) {
+        return ptr ? cudaMemsetAsync(ptr, 0, bytes, p->stream) : cudaSuccess;
+    };
+    if (v.farOn) {
+        const size_t ring = (size_t)v.farDepth * ns * 2 * n * sizeof(unsigned long long);
+        PV1_CUDA(p, zero(v.farAcc, ring));
+        PV1_CUDA(p, zero(v.nearAcc, ring));
+        PV1_CUDA(p, zero(v.farCount, 3 * sizeof(int)));
+        PV1_CUDA(p, zero(v.farFlag, 3 * sizeof(int)));
+    }
+    if (v.farPullOn) {
+        PV1_CUDA(p, zero(v.farPull, ns * 2 * n * sizeof(float)));
+        PV1_CUDA(p, zero(v.pullFlag, 3 * sizeof(int)));
+    }
+    PV1_CUDA(p, zero(v.sRing, (size_t)v.sDepth * n * sizeof(float)));
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    p->step = step;
+    p->pending = false;
+    drop_graph(p);
     return PV1_OK;
 }
 
@@ -2111,8 +2242,12 @@ int pv1_put_state(pv1_plan *p, int which, const float *in) {
         case PV1_ST_HE: dst = v.hE; cnt = c.ngE * n; break;
         case PV1_ST_GI: dst = v.gI; cnt = c.ngI * n; break;
         case PV1_ST_HI: dst = v.hI; cnt = c.ngI * n; break;
+        case PV1_ST_DEP: dst = v.dep; break;
         case PV1_ST_LGN_LTR: dst = p->lp.leftTimeRate; cnt = p->nLGN; break;
         case PV1_ST_LGN_LNL: dst = p->lp.lastNegLogRand; cnt = p->nLGN; break;
+        case PV1_ST_LGN_RNG: dst = p->lp.state; cnt = p->nLGN * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
+        case PV1_ST_V1_RNG_COND: dst = v.rGenCond; cnt = n * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
+        case PV1_ST_V1_RNG_NOISY: dst = v.rNoisy; cnt = n * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
         default: return fail(p, PV1_E_ARG, "state id cannot be written");
     }
     if (!dst) return fail(p, PV1_E_STATE, "state not allocated");

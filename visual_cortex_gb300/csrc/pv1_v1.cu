@@ -244,6 +244,60 @@ __device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, in
             farH[q] = q < ns ? __ldcg(acc + (size_t)(2 * q + 1) * nV1 + i) : 0ull;
         }
     }
+    float *recNear = nullptr;
+    int nNearDraw = 0;
+    if (Rng && P.recNear && active) {
+        long long rs = tp - P.recStep0;
+        if (rs >= 0 && rs < P.recSteps) recNear = P.recNear + ((size_t)rs * nV1 + i) * P.recCap;
+    }
+    // delayed near events with synaptic failure: recal_G_mat (src/coredynamics.cu:2138-2224)
+    // restated per post -- its near synapses in the reference's order, the two spike-word
+    // slots that can deliver in step tp, a normal draw from the post's generator for each
+    // arriving event of a pair with failure rate p > 0, float sums in that order
+    if constexpr (Rng) {
+        if (P.nearPullOn && active) {
+            const float dt = P.dt;
+            for (int e = P.npOff[i]; e < P.npOff[i + 1]; e++) {
+                const int pre = P.npPre[e];
+                const int steps = P.npSteps[e];
+                const float frac = P.npFrac[e];
+                const bool preE = (pre % bs) < P.nE;
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const long long ts = tp - steps + k;
+                    const long long row = ((ts % P.sDepth) + P.sDepth) % P.sDepth;
+                    const float sI = __ldcg(P.sRing + (size_t)row * nV1 + pre);
+                    if (!(sI >= 1.0f)) continue;
+                    const float nsp = floorf(sI);
+                    const float dtsp = (sI - nsp + (float)k) * dt - frac;
+                    if (!(dtsp < dt && dtsp >= 0)) continue;
+                    float f = P.npStr[e];
+                    const float pf = P.npP[e];
+                    if (pf > 0) {
+                        const float rnd = curand_normal(&condState);
+                        if (recNear) {
+                            if (nNearDraw < P.recCap) recNear[nNearDraw] = rnd;
+                            else atomicOr(P.err, kErrRecordOverflow);
+                        }
+                        nNearDraw++;
+                        f *= 1 - pf + P.npStd[e] * rnd;
+                    }
+                    if (f > 0) {
+                        const float delta = dt - dtsp;
+#pragma unroll
+                        for (int ig = 0; ig < kMaxNG; ig++) {
+                            if (preE && ig < ngE)
+                                cond_input_v(P.condE.rise[ig], P.condE.decay[ig], P.condE.dod[ig], lgE[ig], lhE[ig],
+                                             nsp * f * ipE[ig], delta);
+                            if (!preE && ig < ngI)
+                                cond_input_v(P.condI.rise[ig], P.condI.decay[ig], P.condI.dod[ig], lgI[ig], lhI[ig],
+                                             nsp * f * ipI[ig], delta);
+                        }
+                    }
+                }
+            }
+        }
+    }
     // delayed near events (noDelay = 0): recal_G_mat sums them into the same step's
     // conductance update; here they were pushed into their own ring
     if (!P.noDelay) {
@@ -270,12 +324,6 @@ __device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, in
         }
     }
     const int nnb = P.noDelay ? P.nNearNB[b] : 0;
-    float *recNear = nullptr;
-    int nNearDraw = 0;
-    if (Rng && P.recNear && active) {
-        long long rs = tp - P.recStep0;
-        if (rs >= 0 && rs < P.recSteps) recNear = P.recNear + ((size_t)rs * nV1 + i) * P.recCap;
-    }
     for (int ib = 0; ib < nnb; ib++) {
         const int nb = P.nbId[b * P.nnbMax + ib];
         int cntE;
@@ -1166,7 +1214,7 @@ __device__ __forceinline__ void v1_step_body(const V1Params &P, long long t, int
         if (Rng && P.condRng) P.rGenCond[i] = condState;
         if (Rng && P.noiseRng) P.rNoisy[i] = noisyState;
         if (P.spikeCount && sInfo >= 1.0f) P.spikeCount[i] += (unsigned)floorf(sInfo);
-        if (P.farPullOn) P.sRing[(size_t)(t % P.sDepth) * P.nV1 + i] = sInfo;
+        if (P.farPullOn || P.nearPullOn) P.sRing[(size_t)(t % P.sDepth) * P.nV1 + i] = sInfo;
     }
     if (P.farOn) {
         const int e0 = active ? P.farOff[i] : 0;

@@ -9,7 +9,8 @@ LGN_fr, LGN_sp and patchV1_cfg with the reference's headers and record order.
 Supported: magno and parvo LGN cells in one or two eyes read from the LGN parameter file
 (useNewLGN = false), flat or curved retina, initial spikes, synaptic failure (not on
 distance-delayed near synapses), learning = 0, no gap junctions, the orientation boost
-(nOri with readFeature), snapshots of this library only (resume with asInit = false), framed output
+(nOri with readFeature), snapshots in the reference's layout (resumed, or the initial state with
+asInit = true), framed output
 (physical V1, visual-field V1 and LGN), minimal output (the sample file).  Anything else
 raises ConfigError naming the key.
 """
@@ -76,9 +77,7 @@ def _check_supported(c: Config):
         bad.append("useNewLGN = true (LGN parameters drawn from distributions)")
     if c.virtual_LGN or c.LGN_switch or c.reverseInput:
         bad.append("virtual_LGN / LGN_switch / reverseInput")
-    if c.fSnapshot and c.asInit:
-        bad.append("asInit = true (a snapshot as the initial state of a new run; resume with asInit = false)")
-    if c.fSnapshot and (c.snapshot_suffix or "") != (c.output_suffix or ""):
+    if c.fSnapshot and not c.asInit and (c.snapshot_suffix or "") != (c.output_suffix or ""):
         raise ConfigError("to use snapshot to resume simulation, it needs to have the same suffix as the output_suffix")
     if c.manual:
         bad.append("manual connections")
@@ -185,28 +184,88 @@ def _setup_frames(sim, c: Config, m: Model, P):
     return FM.OutputFrameWriter(fn, c.dt, ot, kinds, sizes)
 
 
-def _restore(sim, c: Config) -> int:
-    """Loads the checkpoint named by fSnapshot (inputFolder + name + '_' + snapshot_suffix +
-    '.bin', src/patch.cu:438-445, 611-613) and returns its step."""
+def _restore(sim, c: Config, m) -> int:
+    """Loads the snapshot named by fSnapshot (inputFolder + name + '_' + snapshot_suffix +
+    '.bin', src/patch.cu:438-445, 611-613) and returns the step the run starts at.  A snapshot
+    in the reference's layout (src/patch.cu:5489-5685) sets the neuron state, tBack, the
+    generators and the LGN integrals; with asInit = true it is the initial state of a new run
+    (step 0, frame bookkeeping from the start), otherwise the run resumes at its step, whose
+    frame bookkeeping must be the one this configuration reaches there.  Its far events in
+    flight are not in it (the reference keeps them in host vectors it does not save).  When
+    this library wrote the snapshot, its own checkpoint follows the reference's fields, and
+    resuming (asInit = false) loads that instead: bit for bit, far events included."""
+    from . import _native as N
     from .cfg import _prefixed
     path = _prefixed(c.inputFolder, c.fSnapshot) + "_" + (c.snapshot_suffix or "") + ".bin"
-    buf = np.fromfile(path, np.uint8)
-    if buf[:8].tobytes() != b"PV1CKPT\0":
-        raise ConfigError(f"{path}: not a checkpoint written by this library (the reference's own snapshot "
-                          "layout is not read)")
-    sim.restore(buf)
-    return sim.step
+    head = np.fromfile(path, np.uint8, 8)
+    if head.tobytes() == b"PV1CKPT\0":           # a bare checkpoint of this library
+        if c.asInit:
+            raise ConfigError(f"{path}: a checkpoint of this library resumes a run (asInit = false)")
+        sim.restore(np.fromfile(path, np.uint8))
+        return sim.step
+    spec = m.spec
+    try:
+        snap, trailer = FM.read_reference_snapshot(path, spec.nI * spec.nblock)
+    except ValueError as e:
+        raise ConfigError(str(e)) from None
+    sz = snap["sizes"]
+    if (snap["iModel"] != spec.iModel or sz["nV1"] != spec.nV1 or sz["nLGN"] != m.lgn.nLGN or
+            sz["ngFF"] != spec.ngFF or sz["ngE"] != spec.ngE or sz["ngI"] != spec.ngI):
+        raise ConfigError(f"{path}: patchV1 config is incompatible with the restore file config")
+    if not c.asInit and trailer[:8] == b"PV1CKPT\0":
+        sim.restore(np.frombuffer(trailer, np.uint8).copy())
+        return sim.step
+    step = 0 if c.asInit else snap["idx"]["step"]
+    if not c.asInit:
+        want = m.lgn.sched.snapshot_indices(step, sz["trainDepth"])
+        diff = [k for k in FM.SNAPSHOT_INDICES[:-2] if want[k] != snap["idx"][k]]
+        if diff:
+            raise ConfigError(f"{path}: the snapshot's frame bookkeeping ({', '.join(diff)}) is not this "
+                              "configuration's at its step")
+    st = snap["state"]
+    for k in ("v", "gFF", "hFF", "gE", "hE", "gI", "hI", "dep"):
+        sim.put_state(k, st[k])
+    if spec.iModel == 1:
+        sim.put_state("w", st["w"])
+    sim.put_state("tBack", snap["v1"]["tBack"])
+    sim.put_state("v1_rng_cond", snap["v1"]["rng_cond"])
+    sim.put_state("v1_rng_noisy", snap["v1"]["rng_noisy"])
+    sim.put_state("lgn_ltr", snap["lgn"]["ltr"])
+    sim.put_state("lgn_lnl", snap["lgn"]["lnl"])
+    sim.put_state("lgn_rng", snap["lgn"]["rng"])
+    N.check(sim.plan, N.lib.pv1_set_step(sim.plan, int(step)), "pv1_set_step")
+    sim.step = int(step)
+    return int(step)
 
 
-def _write_snapshot(sim, c: Config, previous, log):
-    """snapShot_<time><output suffix> in the output folder (the reference writes it in the
-    working directory, src/patch.cu:6793-6912); the previous one is removed when
-    delPrevSnapshot."""
+def _write_snapshot(sim, c: Config, m, history, previous, log):
+    """snapShot_<time>_<output suffix>.bin in the output folder (the reference writes it in the
+    working directory, src/patch.cu:6793-6912), in the reference's layout -- `history` holds the
+    spike words of the last steps for its spike-word ring -- followed by this library's own
+    checkpoint; the previous one is removed when delPrevSnapshot."""
     import os
     import time
     from .cfg import _prefixed
     name = _prefixed(c.outputFolder, f"snapShot_{int(time.time())}") + "_" + (c.output_suffix or "") + ".bin"
-    sim.checkpoint().tofile(name)
+    trailer = sim.checkpoint().tobytes()        # applies the last step's delivery first
+    spec, depth = m.spec, int(m.seeds.trainDepth)
+    q = int(sim.step)
+    ring = np.empty((depth, spec.nV1), np.float32)
+    for slot in range(depth):
+        # slot s holds the newest step t < q with t % depth == s (the initial v before step 0)
+        t = q - 1 - ((q - 1 - slot) % depth)
+        ring[slot] = history.get(t, m.init.v)
+    state = {k: sim.state(k) for k in ("dep", "v", "gFF", "hFF", "gE", "gI", "hE", "hI")}
+    if spec.iModel == 1:
+        state["w"] = sim.state("w")
+    state["gap"] = np.zeros(spec.nI * spec.nblock, np.float32)
+    FM.write_reference_snapshot(
+        name, m.lgn.sched.snapshot_indices(q, depth), spec.iModel, 0,
+        dict(nV1=spec.nV1, nLGN=m.lgn.nLGN, ngFF=spec.ngFF, ngE=spec.ngE, ngI=spec.ngI, nType=spec.nType,
+             trainDepth=depth),
+        dict(ltr=sim.state("lgn_ltr"), lnl=sim.state("lgn_lnl"), rng=sim.state("lgn_rng")),
+        dict(rng_cond=sim.state("v1_rng_cond"), rng_noisy=sim.state("v1_rng_noisy"), tBack=sim.state("tBack")),
+        ring, state, trailer)
     if previous and previous != name and c.delPrevSnapshot and os.path.exists(previous):
         os.remove(previous)
     log(f"saved a snapshot in {name}")
@@ -515,18 +574,29 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
             if c.frameVisLGNoutput:
                 flags |= N.REC_LGN_FR
             frames = _setup_frames(sim, c, m, P)
+        snaps = not minimal
+        if snaps:
+            flags |= N.REC_SPIKES          # the spike-word ring of the snapshots
         if flags:
             sim.set_record(flags, chunk + 1)
         base = 0
         if c.fSnapshot:
-            base = _restore(sim, c)
-            log(f"resumed from step {base}")
+            base = _restore(sim, c, m)
+            log(("initial state from" if c.asInit else "resumed from") + f" step {base}")
         done = 0
         interval = max(int(c.snapshotInterval), 1)
         last_snap = None
+        history = {}
+        depth = int(m.seeds.trainDepth)
         while done < m.nt:
             k = min(chunk, m.nt - done, interval - done % interval)
             sim.run(k)
+            if snaps:
+                first = base + done + max(0, k - depth)
+                for q, row in enumerate(sim.fetch_spikes(first, min(k, depth))):
+                    history[first + q] = row
+                for t in [t for t in history if t < base + done + k - depth]:
+                    del history[t]
             if sample is not None:
                 r, sp, _ = sim.fetch_records(base + done, k, raw=True, lgn_sp=True, lgn_fr=False)
                 sample.add(done, r[:, :spec.nV1], sp)
@@ -543,7 +613,7 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
                 frames.write(sim.frames_collect(base + done, k))
             done += k
             if not c.minimal and (done % interval == 0 or done == m.nt):
-                last_snap = _write_snapshot(sim, c, last_snap, log)
+                last_snap = _write_snapshot(sim, c, m, history, last_snap, log)
         for w in (raw, lsp, lfr, frames, sample):
             if w is not None:
                 w.close()

@@ -506,3 +506,69 @@ def patchv1_cfg_bytes(c, *, vL, vE, vI, nType, nTypeE, nTypeI, typeAcc, stimulus
     _w(b, _pad(c["synFail"], nType * nType), f32)
     _w(b, _pad(c["synFailFF"], nType), f32)
     return b.getvalue()
+
+
+# ------------------------------------------------------------------ snapshots (reference layout)
+
+SNAPSHOT_INDICES = ("step", "frameCycle", "iFrameHead", "oldFrameHead", "currentFrame", "iFramePhaseHead",
+                    "iFramePhaseTail", "mFramePhaseHead", "mFramePhaseTail", "iStatus", "currentTimeSlot")
+
+
+def write_reference_snapshot(fn, idx: dict, iModel: int, learning: int, sizes: dict, lgn: dict, v1: dict,
+                             spike_train, state: dict, trailer: bytes | None = None):
+    """A snapshot in the reference's layout (src/patch.cu:6793-6912): 11 u32 indices (steps
+    done, frame bookkeeping, iStatus, the next spike-word slot), iModel and learning (i32),
+    nV1 nLGN ngFF ngE ngI nType trainDepth (u32); the LGN block (leftTimeRate, lastNegLogRand,
+    the generators, 48 bytes each); rGenCond, rNoisy (48 bytes per neuron), tBack; the
+    spike-word ring [trainDepth][nV1]; the state block dep, (w,) v, gFF, hFF, gE, gI, hE, hI,
+    gap.  `trailer` (this build's own checkpoint) is appended after it: the reference's reader
+    stops before it."""
+    with open(fn, "wb") as f:
+        _w(f, [idx[k] for k in SNAPSHOT_INDICES], u32)
+        _w(f, [iModel, learning], i32)
+        _w(f, [sizes[k] for k in ("nV1", "nLGN", "ngFF", "ngE", "ngI", "nType", "trainDepth")], u32)
+        _w(f, lgn["ltr"], f32)
+        _w(f, lgn["lnl"], f32)
+        f.write(np.ascontiguousarray(lgn["rng"], np.uint8).tobytes())
+        f.write(np.ascontiguousarray(v1["rng_cond"], np.uint8).tobytes())
+        f.write(np.ascontiguousarray(v1["rng_noisy"], np.uint8).tobytes())
+        _w(f, v1["tBack"], f32)
+        _w(f, np.ravel(spike_train), f32)
+        keys = ["dep"] + (["w"] if iModel == 1 else []) + ["v", "gFF", "hFF", "gE", "gI", "hE", "hI", "gap"]
+        for k in keys:
+            _w(f, np.ravel(state[k]), f32)
+        if trailer is not None:
+            f.write(trailer)
+
+
+def read_reference_snapshot(fn, nI_total: int):
+    """Reads a snapshot written by the reference (or by write_reference_snapshot); returns the
+    fields and the bytes that follow them (this build's checkpoint, if it wrote the file)."""
+    data = open(fn, "rb").read()
+    off = 0
+
+    def take(dtype, count):
+        nonlocal off
+        a = np.frombuffer(data, dtype, count, off)
+        off += a.nbytes
+        return a.copy()
+
+    idx = dict(zip(SNAPSHOT_INDICES, (int(x) for x in take(u32, 11))))
+    iModel, learning = (int(x) for x in take(i32, 2))
+    sizes = dict(zip(("nV1", "nLGN", "ngFF", "ngE", "ngI", "nType", "trainDepth"), (int(x) for x in take(u32, 7))))
+    n, nl = sizes["nV1"], sizes["nLGN"]
+    if learning:
+        raise ValueError(f"{fn}: a snapshot of a run with learning = {learning} (plasticity) is not read")
+    lgn = dict(ltr=take(f32, nl), lnl=take(f32, nl), rng=take(np.uint8, 48 * nl))
+    v1 = dict(rng_cond=take(np.uint8, 48 * n), rng_noisy=take(np.uint8, 48 * n), tBack=take(f32, n))
+    spike_train = take(f32, sizes["trainDepth"] * n).reshape(sizes["trainDepth"], n)
+    state = dict(dep=take(f32, n))
+    if iModel == 1:
+        state["w"] = take(f32, n)
+    state["v"] = take(f32, n)
+    for k, c in (("gFF", sizes["ngFF"]), ("hFF", sizes["ngFF"]), ("gE", sizes["ngE"]), ("gI", sizes["ngI"]),
+                 ("hE", sizes["ngE"]), ("hI", sizes["ngI"])):
+        state[k] = take(f32, c * n)
+    state["gap"] = take(f32, nI_total)
+    return dict(idx=idx, iModel=iModel, learning=learning, sizes=sizes, lgn=lgn, v1=v1,
+                spike_train=spike_train, state=state), data[off:]

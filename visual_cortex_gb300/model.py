@@ -491,7 +491,10 @@ class Simulation:
         self.step = int(np.frombuffer(b[56:64].tobytes(), np.int64)[0])   # the header's step field
 
     def put_state(self, name: str, arr: np.ndarray):
-        a = np.ascontiguousarray(arr, dtype=f32)
+        if name.endswith("_rng") or name.startswith("v1_rng"):
+            a = np.ascontiguousarray(arr, dtype=np.uint8).view(f32)     # raw generator bytes
+        else:
+            a = np.ascontiguousarray(arr, dtype=f32)
         N.check(self.plan, N.lib.pv1_put_state(self.plan, N.ST[name], N.fptr(a)), f"pv1_put_state({name})")
 
     def lgn_tables(self):

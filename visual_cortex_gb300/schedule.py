@@ -79,6 +79,20 @@ class FrameSchedule:
         """Frames read from the stimulus file once step `it` started (src/patch.cu:5969)."""
         return -(-((it + 1) * self.denorm) // self.ntPerFrame)
 
+    def snapshot_indices(self, steps_done: int, trainDepth: int) -> dict:
+        """The frame bookkeeping of the step loop after steps_done steps (src/patch.cu:
+        5395-5412, 5966-6057): frames read, the ring head, its previous value and wraps, the
+        four phases; the next spike-word slot; iStatus 0 (no LGN switching)."""
+        q = int(steps_done)
+        cur = -(-(q * self.denorm) // self.ntPerFrame)
+        return dict(step=q, frameCycle=cur // self.maxFrame, iFrameHead=cur % self.maxFrame,
+                    oldFrameHead=(cur - 1) % self.maxFrame if cur > 0 else 0, currentFrame=cur,
+                    iFramePhaseHead=(q * self.denorm) % self.ntPerFrame,
+                    iFramePhaseTail=(self.parvoComp + q * self.denorm) % self.ntPerFrame,
+                    mFramePhaseHead=(q * self.denorm) % self.ntPerFrame,
+                    mFramePhaseTail=(self.magnoComp + q * self.denorm) % self.ntPerFrame,
+                    iStatus=0, currentTimeSlot=q % int(trainDepth))
+
     def magno_tail(self, it: int) -> tuple[int, int]:
         """(frame tail layer offset from the newest frame's layer, phase) at step it."""
         phase = (self.magnoComp + (it + 1) * self.denorm) % self.ntPerFrame

@@ -350,6 +350,40 @@ int pv1_checkpoint_load(pv1_plan *plan, const void *buf, uint64_t bytes);
  * being host vectors it does not save.  noDelay = 0 plans: PV1_E_UNSUPPORTED. */
 int pv1_set_step(pv1_plan *plan, int64_t step);
 
+/* LGN->V1 plasticity, learning = 3 of the reference ("only FF_E learning is active",
+ * src/patch.cu:1166-1171): the triplet rule on every LGN->excitatory synapse inside the V1
+ * step (compute_V_collect_spike_learnFF_fast, src/coredynamics.cu:1631-1993: LTD at each LGN
+ * spike from the post LTD trace, LTP at each V1 spike from the presynaptic trace and the post
+ * triplet trace, weights clipped to [gmin, gmax], the filtered post rate vAvgE scaling LTD
+ * when targetFR > 0, optional homeostasis of each neuron's total LGN weight), and the
+ * presynaptic LTP traces updated in the LGN stage (LGN_nonlinear, src/discrete_input_convol.cu:
+ * 1774-1820).  The fields are the cfg values the reference reads (src/patch.cu:221-256:
+ * element [0] of tauLTP, tauLTD, tauTrip, tauAvg, targetFR, A_LGN, r_LTD, gmaxLGN, gminLGN and
+ * sRatioLGN); the derived rates are computed as learnFF_post does (src/condShape.h:137-152)
+ * and exp_homeo as expf(-dt / decayTimeHomeoFF) (src/patch.cu:1330).  The per-neuron totals of
+ * the homeostasis start from the current weights (src/patch.cu:4335-4352).  Plans with
+ * learning run one launch per step (no persistent kernel, no batches) and one spike per
+ * step at most; PV1_E_UNSUPPORTED otherwise. */
+typedef struct pv1_ff_learning {
+    int32_t learning;            /* 3 */
+    float tauLTP, tauLTD, tauTrip, tauAvg, targetFR;
+    float A_LGN, r_LTD, gmaxLGN, gminLGN, sRatioLGN;
+    float decayTimeHomeoFF, FF_InfRatio;
+    int32_t applyHomeo;          /* 0 none, 1 multiplicative, 2 additive */
+    int32_t symmetricHomeo, rebound;
+} pv1_ff_learning;
+int pv1_set_ff_learning(pv1_plan *plan, const pv1_ff_learning *cfg);
+
+/* Learning state (plans with learning): the LGN->V1 weights [maxLGN][nV1] (the reference's
+ * LGN_V1_s, synapse-major), the post variables in the reference's learnVar layout
+ * (src/patch.cu:4365-4385: vLTD_FF_E [nblock*nE], vTrip_FF_E [nblock*nE], vAvgE [nblock*nE][2],
+ * vAvgI [nblock*nI]), the presynaptic LTP trace of each LGN cell at the end of the last step
+ * [nLGN], and the homeostasis totals [2][nV1] (total, target). */
+#define PV1_ST_SLGN     18
+#define PV1_ST_FF_POST  19
+#define PV1_ST_FF_PRE   20
+#define PV1_ST_TOTAL_FF 21
+
 /* Overwrites one state array (PV1_ST_* above; the generators as the raw bytes get_state
  * gives, which is how a snapshot in the reference's layout, src/patch.cu:6793-6912, is loaded;
  * not the spike words or the far sums). */

@@ -54,6 +54,10 @@ def lib():
         L.orc_lgn_spatial.argtypes = [C.c_int, C.c_int, FP, FP, UP, FP, C.c_int, C.c_int, C.c_int, C.c_int, FP]
         L.orc_lgn_convol.argtypes = [P, C.c_int, C.c_int, C.c_longlong, FP, FP, FP, FP]
         L.orc_lgn_nonlinear.argtypes = [P, FP, FP, FP, FP, FP, FP, FP, FP, FP, IP, C.c_int, FP, FP]
+        L.orc_lgn_nonlinear_ex.argtypes = [P, FP, FP, FP, FP, FP, FP, FP, FP, FP, IP, C.c_int, FP, FP, UP, FP]
+        L.orc_lgn_ff_pre.argtypes = [C.c_int, C.c_float, C.c_float, UP, FP, FP, FP, FP, FP]
+        L.orc_v1_set_ff_learning.argtypes = [P, P]
+        L.orc_v1_learn_ff.argtypes = [P, FP, FP, FP]
         L.orc_parvo_max_sample1d.argtypes = [P, P, C.c_int]
         L.orc_lgn_parvo_setup.argtypes = [P, P, P, FP, FP, FP, FP, FP]
         L.orc_lgn_parvo_spatial.argtypes = [C.c_int, C.c_int, FP, FP, UP, FP, C.c_int, C.c_int, C.c_int,
@@ -107,7 +111,8 @@ def ip(a):
     return a.ctypes.data_as(C.POINTER(C.c_int32))
 
 
-ST = dict(v=0, w=1, tBack=2, dep=3, gFF=4, hFF=5, gE=6, hE=7, gI=8, hI=9, sInfo=10)
+ST = dict(v=0, w=1, tBack=2, dep=3, gFF=4, hFF=5, gE=6, hE=7, gI=8, hI=9, sInfo=10, sLGN=18, ff_post=19,
+          total_ff=21)
 
 
 def host_init_state(spec, seed: int, tonicDep, nLGNperV1, v0, w0, gFF0, gE0, gI0,
@@ -239,10 +244,26 @@ class LgnOracle:
     def nonlinear(self, convol, u, ucount, cap):
         sInfo = np.zeros(self.lgn.nLGN, f32)
         fr = np.zeros(self.lgn.nLGN, f32)
-        mism = lib().orc_lgn_nonlinear(C.byref(self.cfg), fp(convol), fp(self.maxConvol), fp(self.c50),
-                                       fp(self.sharp), fp(self.la), fp(self.lb), fp(self.ltr), fp(self.lnl),
-                                       fp(u), ip(ucount), int(cap), fp(sInfo), fp(fr))
+        self.nsp = np.zeros(self.lgn.nLGN, np.uint32)
+        self.tsp = np.zeros(self.lgn.nLGN, f32)
+        mism = lib().orc_lgn_nonlinear_ex(C.byref(self.cfg), fp(convol), fp(self.maxConvol), fp(self.c50),
+                                          fp(self.sharp), fp(self.la), fp(self.lb), fp(self.ltr), fp(self.lnl),
+                                          fp(u), ip(ucount), int(cap), fp(sInfo), fp(fr), up(self.nsp),
+                                          fp(self.tsp))
+        self.last_sInfo = sInfo
         return sInfo, fr, mism
+
+    def ff_pre(self, tauLTP: float):
+        """The presynaptic learning trace over the step just computed by `nonlinear`
+        (self.ff_var carries it): returns (trace at the step start, right after the spikes)."""
+        n = self.lgn.nLGN
+        if getattr(self, "ff_var", None) is None:
+            self.ff_var = np.zeros(n, f32)
+        start = np.zeros(n, f32)
+        at = np.zeros(n, f32)
+        lib().orc_lgn_ff_pre(n, f32(self.cfg.dt), f32(tauLTP), up(self.nsp), fp(self.tsp), fp(self.last_sInfo),
+                             fp(self.ff_var), fp(start), fp(at))
+        return start, at
 
 
 class V1Oracle:
@@ -276,7 +297,8 @@ class V1Oracle:
         s = self.spec
         n = s.nV1
         size = dict(gFF=s.ngFF * n, hFF=s.ngFF * n, gE=s.ngE * n, hE=s.ngE * n, gI=s.ngI * n,
-                    hI=s.ngI * n).get(name, n)
+                    hI=s.ngI * n, sLGN=self._keep[1].shape[0] * n,
+                    ff_post=4 * s.nE * s.nblock + (s.blockSize - s.nE) * s.nblock, total_ff=2 * n).get(name, n)
         out = np.empty(size, f32)
         lib().orc_v1_get(self.h, ST[name], fp(out))
         return out
@@ -289,6 +311,22 @@ class V1Oracle:
 
     def set_far_failure(self, seed, nChunk):
         lib().orc_v1_set_far_failure(self.h, int(seed), int(nChunk))
+
+    def set_ff_learning(self, learning):
+        """LGN->V1 plasticity with the parameters of a model.FFLearning."""
+        from visual_cortex_gb300 import _native as N
+        self._ffl = N.FFLearning(learning=int(learning.learning), tauLTP=learning.tauLTP, tauLTD=learning.tauLTD,
+                                 tauTrip=learning.tauTrip, tauAvg=learning.tauAvg, targetFR=learning.targetFR,
+                                 A_LGN=learning.A_LGN, r_LTD=learning.r_LTD, gmaxLGN=learning.gmaxLGN,
+                                 gminLGN=learning.gminLGN, sRatioLGN=learning.sRatioLGN,
+                                 decayTimeHomeoFF=learning.decayTimeHomeoFF, FF_InfRatio=learning.FF_InfRatio,
+                                 applyHomeo=int(learning.applyHomeo), symmetricHomeo=int(learning.symmetricHomeo),
+                                 rebound=int(learning.rebound))
+        if lib().orc_v1_set_ff_learning(self.h, C.byref(self._ffl)) != 0:
+            raise ValueError("the oracle restates learning = 3 only")
+
+    def learn_ff(self, lgn_sInfo, pre_start, pre_spike):
+        lib().orc_v1_learn_ff(self.h, fp(np.ascontiguousarray(lgn_sInfo, f32)), fp(pre_start), fp(pre_spike))
 
     def init_spikes(self, sp0, SCsplit, depth, rec):
         """rand_spInit with initial spikes and the delivery before the first step, from the

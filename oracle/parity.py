@@ -55,7 +55,13 @@ def split_record(spec, rec):
     return {k: rec[..., v:v + sizes[k]] for k, v in o.items()}
 
 
-def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None):
+LEARN_KEYS = ("sLGN", "ff_post", "total_ff")
+
+
+def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None, learning=None):
+    """learning: a model.FFLearning to run with LGN->V1 plasticity on both sides; the final
+    weights, post variables, homeostasis totals and presynaptic traces come back under
+    gpu/oracle "learn"."""
     from visual_cortex_gb300.model import Simulation
     from visual_cortex_gb300 import _native as N
 
@@ -67,6 +73,8 @@ def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None
     if wl.seeds.has_sp0() and init_rec is None:
         raise ValueError("initial spikes: the Simulation must be made with record_init > 0")
     try:
+        if learning is not None:
+            sim.set_ff_learning(learning)
         gpu_tables = sim.lgn_tables()
         gpu_S = sim.lgn_spatial()
         gpu_parvo = (sim.lgn_parvo_tables(), sim.lgn_parvo_spatial()) if wl.lgn.nParvo else None
@@ -81,6 +89,10 @@ def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None
         ff, _ = sim.fetch_draws(2)
         near, _ = sim.fetch_draws(3)
         final = {k: sim.state(k) for k in ("v", "gE", "gI", "gFF", "tBack")}
+        learn = None
+        if learning is not None:
+            learn = {k: sim.state(k) for k in LEARN_KEYS}
+            learn["ff_pre"] = sim.state("ff_pre")
         launches = sim.launches()
     finally:
         if close:
@@ -107,6 +119,8 @@ def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None
     vo = V1Oracle(wl.spec, wl.net)
     vo.set_state(wl.init)
     vo.set_far_failure(wl.seeds.far_engine_seed, wl.seeds.nChunk)
+    if learning is not None:
+        vo.set_ff_learning(learning)
     mism = 0
     o_hist = None
     if wl.seeds.has_sp0():
@@ -123,7 +137,11 @@ def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None
         mism += m
         o_lsp[it] = s
         o_lfr[it] = fr
+        if learning is not None:
+            pre_start, pre_spike = lo.ff_pre(learning.tauLTP)
         vo.step(s, noise=noise[it], ff=np.ascontiguousarray(ff[it]), near=np.ascontiguousarray(near[it]), cap=cap)
+        if learning is not None:
+            vo.learn_ff(s, pre_start, pre_spike)
         r = o_raw[it]
         r[lay["sInfo"]:lay["sInfo"] + nV1] = vo.get("sInfo")
         r[lay["dep"]:lay["dep"] + nV1] = vo.get("dep")
@@ -135,11 +153,15 @@ def run_parity(wl, nsteps: int, cap: int = 8, own_tables: bool = False, sim=None
                 a = vo.get(k)
                 r[lay[k]:lay[k] + a.size] = a
     o_final = {k: vo.get(k) for k in ("v", "gE", "gI", "gFF", "tBack")}
+    o_learn = None
+    if learning is not None:
+        o_learn = {k: vo.get(k) for k in LEARN_KEYS}
+        o_learn["ff_pre"] = lo.ff_var.copy()
     vo.close()
     return dict(gpu=dict(raw=raw, lsp=lsp, lfr=lfr, tables=gpu_tables, S=gpu_S, final=final,
-                         history=None if init_rec is None else init_rec["history"]),
+                         history=None if init_rec is None else init_rec["history"], learn=learn),
                 ora=dict(raw=o_raw, lsp=o_lsp, lfr=o_lfr, tables=ora_tables, S=ora_S, final=o_final,
-                         history=o_hist),
+                         history=o_hist, learn=o_learn),
                 draw_count_mismatch=mism, launches=launches)
 
 

@@ -528,10 +528,13 @@ int orc_lgn_parvo_convol(const pv1_lgn_config *c, const pv1_lgn_parvo_config *q,
  * entries already times |k|).  u: recorded uniforms [nLGN][cap] of this step, ucount [nLGN].
  * Returns the number of cells whose draw count disagrees with the record (0 when the CPU and
  * GPU took the same branches). */
-int orc_lgn_nonlinear(const pv1_lgn_config *c, const float *convol, const float *maxConvol,
-                      const float *c50, const float *sharp, const float *la, const float *lb,
-                      float *ltr, float *lnl, const float *u, const int32_t *ucount, int cap,
-                      float *sInfo_out, float *fr_out) {
+/* LGN_nonlinear (src/discrete_input_convol.cu:1637-1821): logistic rate and get_spike on
+ * the given uniforms; nsp_out/tsp_out (may be NULL) receive the spike count and mean spike
+ * time the presynaptic learning trace uses. */
+int orc_lgn_nonlinear_ex(const pv1_lgn_config *c, const float *convol, const float *maxConvol,
+                         const float *c50, const float *sharp, const float *la, const float *lb,
+                         float *ltr, float *lnl, const float *u, const int32_t *ucount, int cap,
+                         float *sInfo_out, float *fr_out, uint32_t *nsp_out, float *tsp_out) {
     int mismatch = 0;
     for (int id = 0; id < (int)c->nLGN; id++) {
         const float mx = maxConvol[id];
@@ -562,8 +565,41 @@ int orc_lgn_nonlinear(const pv1_lgn_config *c, const float *convol, const float 
         if (ucount && (int)nsp != ucount[id]) mismatch++;
         sInfo_out[id] = nsp + tsp / dt;
         if (fr_out) fr_out[id] = fr;
+        if (nsp_out) nsp_out[id] = nsp;
+        if (tsp_out) tsp_out[id] = tsp;
     }
     return mismatch;
+}
+
+int orc_lgn_nonlinear(const pv1_lgn_config *c, const float *convol, const float *maxConvol,
+                      const float *c50, const float *sharp, const float *la, const float *lb,
+                      float *ltr, float *lnl, const float *u, const int32_t *ucount, int cap,
+                      float *sInfo_out, float *fr_out) {
+    return orc_lgn_nonlinear_ex(c, convol, maxConvol, c50, sharp, la, lb, ltr, lnl, u, ucount, cap, sInfo_out,
+                                fr_out, NULL, NULL);
+}
+
+/* The presynaptic LTP trace of each LGN cell over one step (the learning block of
+ * LGN_nonlinear, src/discrete_input_convol.cu:1774-1808, one learning type): `start` gets the
+ * trace at the step start; a cell that spiked adds its spike count, decays to the spike time
+ * tsp and leaves that value in `at_spike`; every trace then decays to the step end. */
+void orc_lgn_ff_pre(int nLGN, float dt, float tauLTP, const uint32_t *nsp, const float *tsp, const float *sInfo,
+                    float *var, float *start, float *at_spike) {
+    for (int id = 0; id < nLGN; id++) {
+        float x = var[id];
+        start[id] = x;
+        float delta_t = dt;
+        if (sInfo[id] > 0) {
+            x += (float)nsp[id];
+            x *= expf(-tsp[id] / tauLTP);
+            at_spike[id] = x;
+            delta_t = dt - tsp[id];
+        } else {
+            at_spike[id] = 0.f;
+        }
+        x *= expf(-delta_t / tauLTP);
+        var[id] = x;
+    }
 }
 
 /* ================================================================== V1 ============= */
@@ -597,6 +633,12 @@ typedef struct orc_v1 {
     /* far synaptic failure: libstdc++ minstd_rand0 states per post, chunks of blocks */
     uint32_t *farEng;
     int nChunk;
+    /* LGN->V1 plasticity (learning = 3) */
+    int learn;
+    float lTauLTP, lTauLTD, lTauTrip, lTauAvg, lTargetFR, lA_LTP, lA_ratio, lGmax, lGmin, lExpHomeo;
+    int applyHomeo, symmetricHomeo, rebound;
+    float *ffPost;   /* vLTD_FF_E [nblock*nE], vTrip_FF_E [nblock*nE], vAvgE [nblock*nE][2], vAvgI [nblock*nI] */
+    float *totalFF;  /* [2][nV1] */
 } orc_v1;
 
 static int otype(const orc_v1 *o, int local) {
@@ -682,6 +724,8 @@ void orc_v1_destroy(orc_v1 *o) {
     free(o->delayVec); free(o->ring); free(o->ringOff); free(o->depth); free(o->slot);
     free(o->spikeRing);
     free(o->farEng);
+    free(o->ffPost);
+    free(o->totalFF);
     free(o);
 }
 
@@ -701,6 +745,9 @@ static float *oarr(orc_v1 *o, int which, size_t *cnt) {
         case PV1_ST_GI: *cnt = o->c.ngI * n; return o->gI;
         case PV1_ST_HI: *cnt = o->c.ngI * n; return o->hI;
         case PV1_ST_SINFO: return o->sInfo;
+        case PV1_ST_SLGN: *cnt = (size_t)o->maxLGN * n; return o->sLGN;
+        case PV1_ST_FF_POST: *cnt = 4 * (size_t)o->nE * o->nblock + (size_t)o->nI * o->nblock; return o->ffPost;
+        case PV1_ST_TOTAL_FF: *cnt = 2 * n; return o->totalFF;
         default: return NULL;
     }
 }
@@ -1646,6 +1693,124 @@ int orc_v1_init_spikes(orc_v1 *o, const float *sp0, uint32_t SCsplit, int depth,
     orc_v1_deliver_far(o);
     free(H);
     return mism;
+}
+
+/* LGN->V1 plasticity, learning = 3.  Derived rates as learnFF_post computes them
+ * (src/condShape.h:137-152; Float = float with its double literals), exp_homeo =
+ * exp(-dt/decayTimeHomeoFF) (src/patch.cu:1330), the homeostasis totals from the current
+ * weights (src/patch.cu:4335-4352).  Returns -1 for other learning modes. */
+int orc_v1_set_ff_learning(orc_v1 *o, const pv1_ff_learning *l) {
+    if (l->learning != 3) return -1;
+    const float ALTP = l->A_LGN * l->sRatioLGN;
+    const float tas = (float)((double)l->tauAvg / 1000.0);
+    float Ar = l->r_LTD * ALTP;
+    if (l->targetFR > 0) {
+        const float q = l->tauTrip / (l->tauLTD * (tas * tas));
+        Ar = (float)((double)Ar * ((double)q / 1000.0 / (double)l->targetFR));
+    }
+    o->learn = 1;
+    o->lTauLTP = l->tauLTP; o->lTauLTD = l->tauLTD; o->lTauTrip = l->tauTrip; o->lTauAvg = l->tauAvg;
+    o->lTargetFR = l->targetFR; o->lA_LTP = ALTP; o->lA_ratio = Ar;
+    o->lGmax = l->gmaxLGN * l->sRatioLGN; o->lGmin = l->gminLGN * l->sRatioLGN;
+    o->lExpHomeo = expf(-o->c.dt / l->decayTimeHomeoFF);
+    o->applyHomeo = l->applyHomeo; o->symmetricHomeo = l->symmetricHomeo != 0; o->rebound = l->rebound != 0;
+    const size_t n = (size_t)o->nV1;
+    free(o->ffPost);
+    free(o->totalFF);
+    o->ffPost = (float *)calloc(4 * (size_t)o->nE * o->nblock + (size_t)o->nI * o->nblock + 1, sizeof(float));
+    o->totalFF = (float *)calloc(2 * n, sizeof(float));
+    for (size_t i = 0; i < n; i++) {
+        float t = 0.f;
+        for (uint32_t j = 0; j < o->nLGN[i]; j++) t += o->sLGN[(size_t)j * n + i];
+        o->totalFF[i] = t;
+        o->totalFF[n + i] = t * l->FF_InfRatio;
+    }
+    return 0;
+}
+
+static inline float odecay(float x, float tau, float dt) { return x * expf(-dt / tau); }
+
+/* The learning block of compute_V_collect_spike_learnFF_fast (src/coredynamics.cu:1631-1993)
+ * for learning = 3, every excitatory neuron, after orc_v1_compute_v (whose spike words it
+ * reads): lgnSInfo are the step's LGN spike words, pre_start / pre_spike the presynaptic
+ * traces at the step start and right after each LGN cell's spikes (orc_lgn_ff_pre). */
+int orc_v1_learn_ff(orc_v1 *o, const float *lgnSInfo, const float *pre_start, const float *pre_spike) {
+    if (!o->learn) return -1;
+    const size_t n = (size_t)o->nV1;
+    const float dt = o->c.dt;
+    const int nEt = o->nE * o->nblock;
+    float *vLTD = o->ffPost, *vTrip = o->ffPost + nEt, *vAvgE = o->ffPost + 2 * nEt;
+    for (int b = 0; b < o->nblock; b++) {
+        for (int j = 0; j < o->nE; j++) {
+            const size_t i = (size_t)b * o->bs + j;
+            const int eid = b * o->nE + j;
+            const float sI = o->sInfo[i];
+            float nsp, tsp;
+            if (sI > 0) { nsp = floorf(sI); tsp = (sI - nsp) * dt; }
+            else { nsp = 0; tsp = dt; }
+            float LTD[2] = {vLTD[eid], 0.f}, Trip[2] = {vTrip[eid], 0.f}, Avg[2] = {vAvgE[2 * eid], 0.f};
+            if (nsp > 0) {
+                LTD[1] = odecay(LTD[0], o->lTauLTD, tsp);
+                Trip[1] = odecay(Trip[0], o->lTauTrip, tsp);
+                Avg[1] = odecay(Avg[0], o->lTauAvg, tsp);
+            }
+            const uint32_t m = o->nLGN[i];
+            float new0 = 0.f, ch = 0.f, dsum = 0.f;
+            if (o->applyHomeo) {
+                const float f0 = o->totalFF[i], finf = o->totalFF[n + i];
+                const float d = f0 - finf;
+                if (d > 0 || o->symmetricHomeo) {
+                    new0 = d * o->lExpHomeo + finf;
+                    ch = o->applyHomeo == 1 ? new0 / f0 : (new0 - f0) / (float)m;
+                } else {
+                    new0 = f0;
+                    ch = o->applyHomeo == 1 ? 1.f : 0.f;
+                }
+            }
+            for (uint32_t q = 0; q < m; q++) {
+                const size_t lid = (size_t)q * n + i;
+                float f = o->sLGN[lid];
+                if (f == 0 && !o->rebound) continue;
+                if (o->applyHomeo == 1) f *= ch;
+                else if (o->applyHomeo == 2) f += ch;
+                const uint32_t id = o->lgnId[lid];
+                const float sFF = lgnSInfo[id];
+                const uint32_t nspFF = (uint32_t)floorf(sFF);
+                const float tspFF = (sFF > 0 ? sFF - (float)nspFF : 1.f) * dt;
+                if (nspFF > 0) {
+                    const int c = tspFF < tsp ? 0 : 1;
+                    const float delta_t = c == 0 ? tspFF : tspFF - tsp;
+                    float A = o->lA_ratio;
+                    if (o->lTargetFR > 0) A *= o->lTauLTP * Avg[c] * Avg[c];
+                    const float df = odecay(LTD[c], o->lTauLTD, delta_t) * A;
+                    f -= df;
+                    if (o->applyHomeo) dsum -= df;
+                }
+                if (nsp > 0) {
+                    const int early = tspFF < tsp;
+                    const float lpre = early ? pre_spike[id] : pre_start[id];
+                    const float delta_t = early ? tsp - tspFF : tsp;
+                    const float df = odecay(lpre, o->lTauLTP, delta_t) * Trip[1] * o->lA_LTP;
+                    if (o->applyHomeo) dsum += df;
+                    f += df;
+                }
+                if (f < o->lGmin) { if (o->applyHomeo) dsum += o->lGmin - f; f = o->lGmin; }
+                if (f > o->lGmax) { if (o->applyHomeo) dsum -= f - o->lGmax; f = o->lGmax; }
+                o->sLGN[lid] = f;
+            }
+            if (o->applyHomeo) o->totalFF[i] = new0 + dsum;
+            const int c = nsp > 0 ? 1 : 0;
+            float delta_t = dt;
+            if (nsp > 0) delta_t -= tsp;
+            LTD[c] = odecay(LTD[c] + nsp, o->lTauLTD, delta_t);
+            Trip[c] = odecay(Trip[c] + nsp, o->lTauTrip, delta_t);
+            Avg[c] = odecay(Avg[c] + nsp, o->lTauAvg, delta_t);
+            vLTD[eid] = LTD[c];
+            vTrip[eid] = Trip[c];
+            vAvgE[2 * eid] = Avg[c];
+        }
+    }
+    return 0;
 }
 
 int orc_num_threads(void) {

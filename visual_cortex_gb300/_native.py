@@ -24,7 +24,7 @@ ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "call out of order", -4: "un
 REC_RAW, REC_LGN_SP, REC_LGN_FR, REC_SPIKES = 1, 2, 4, 8
 ST = dict(v=0, w=1, tBack=2, dep=3, gFF=4, hFF=5, gE=6, hE=7, gI=8, hI=9, sInfo=10,
           lgn_ltr=11, lgn_lnl=12, lgn_sInfo=13, farPull=14, lgn_rng=15, v1_rng_cond=16,
-          v1_rng_noisy=17)
+          v1_rng_noisy=17, sLGN=18, ff_post=19, ff_pre=20, total_ff=21)
 
 _f2 = C.c_float * MAX_NG
 _t2 = C.c_float * MAX_NTYPE
@@ -48,6 +48,15 @@ class V1Config(C.Structure):
         ("noDelay", C.c_int32), ("noFarDelay", C.c_int32), ("speedOfThought", C.c_float),
         ("hWrite", C.c_int32),
     ]
+
+
+class FFLearning(C.Structure):
+    """pv1_ff_learning: the cfg values of LGN->V1 plasticity (learning = 3)."""
+    _fields_ = [("learning", C.c_int32), ("tauLTP", C.c_float), ("tauLTD", C.c_float), ("tauTrip", C.c_float),
+                ("tauAvg", C.c_float), ("targetFR", C.c_float), ("A_LGN", C.c_float), ("r_LTD", C.c_float),
+                ("gmaxLGN", C.c_float), ("gminLGN", C.c_float), ("sRatioLGN", C.c_float),
+                ("decayTimeHomeoFF", C.c_float), ("FF_InfRatio", C.c_float), ("applyHomeo", C.c_int32),
+                ("symmetricHomeo", C.c_int32), ("rebound", C.c_int32)]
 
 
 class LgnConfig(C.Structure):
@@ -149,6 +158,7 @@ def _load() -> C.CDLL:
         "pv1_time_kernels": ([P, C.c_uint32, _FP, _FP, C.POINTER(C.c_int)], C.c_int),
         "pv1_persistent_mode": ([P, C.c_int], C.c_int),
         "pv1_set_wait_limit": ([P, C.c_int64], C.c_int),
+        "pv1_set_ff_learning": ([P, C.POINTER(FFLearning)], C.c_int),
         "pv1_lgn_spikes_noalloc": ([P, C.c_uint32, _FP, _FP], C.c_int),
         "pv1_batch_create": ([C.POINTER(P), C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(P)], C.c_int),
         "pv1_batch_destroy": ([P], None),

@@ -280,6 +280,8 @@ class Paths:
     lgn_fr: str
     raw: str
     lgn_sp: str
+    slgn: str
+    dslgn: str
 
 
 def resolve_paths(c: Config) -> Paths:
@@ -304,6 +306,8 @@ def resolve_paths(c: Config) -> Paths:
         lgn_fr=_prefixed(out, c.fLGN_fr) + outs,
         raw=_prefixed(out, c.fRawData) + outs,
         lgn_sp=_prefixed(out, c.fLGN_sp) + outs,
+        slgn=_prefixed(out, c.f_sLGN) + outs,
+        dslgn=_prefixed(out, c.f_dsLGN) + outs,
     )
 
 

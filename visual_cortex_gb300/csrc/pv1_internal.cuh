@@ -140,6 +140,11 @@ struct LgnParams {
     const double *pctw;        // [2][pKS+1][nParvo] cumulative temporal weights (centre, surround)
     const float *pS;           // [nFrame+1][2][nParvo] spatial stage per frame
     const float *pk;           // [2][nParvo] amplitude k of centre and surround
+    // LGN->V1 plasticity: presynaptic LTP trace per cell (0 types: none)
+    int nFF;
+    float tauLTP;
+    float *ffPre;              // [nLGN] trace at the end of the last computed step
+    float *outPre;             // [outSlots][2][nLGN] trace at the start of the step, right after its spikes
 };
 
 struct V1Params {
@@ -161,6 +166,16 @@ struct V1Params {
     int condRng;        // rGenCond draws can change results (some failure rate > 0)
     int noiseRng;       // some noisyDep > 0
     long long waitSpins;   // polls of a barrier wait before it gives up and raises kErrBarrier
+    int pushCta;           // far-push CTAs appended to the persistent grid (0: the neuron CTAs push)
+    // LGN->V1 plasticity (learning = 3): triplet rule on the LGN->E synapses
+    int ffLearn;
+    float ffTauLTP, ffTauLTD, ffTauTrip, ffTauAvg, ffTargetFR, ffA_LTP, ffA_ratio, ffGmax, ffGmin;
+    int applyHomeo, symmetricHomeo, rebound;
+    float expHomeo;
+    float *ffPost;         // the reference's learnVar FF block: vLTD_FF_E, vTrip_FF_E, vAvgE[2], vAvgI
+    float *totalFF;        // [2][nV1] total LGN weight and its target
+    float *sLGNw;          // the weights, written by the learning (same array as sLGN)
+    const float *ffPreRing;  // the LGN stage's outPre ring (row = step % lgn slots)
     // state [nV1] / [ng][nV1]
     float *v, *w, *tBack, *dep, *gFF, *hFF, *gE, *hE, *gI, *hI, *tonicDep, *lastNoise;
     curandStateMRG32k3a *rGenCond, *rNoisy;
@@ -176,6 +191,8 @@ struct V1Params {
     const int *nNearNB;        // [nblock]
     const int *nbId;           // [nblock][nnbMax]
     const float *conMat;       // [nblock][nnbMax][bs][bs]
+    const int *nearRevOff;     // [nblock+1] near tiles that read block b's rows: nearRev[off[b]..off[b+1])
+    const int *nearRev;        //            tile index (post block * nnbMax + position in its list)
     // far delivery (outgoing lists by pre-neuron)
     int farOn;                 // 0: no far input at all (noFarDelay=1 or no far synapses)
     const int *farOff;         // [nV1+1]
@@ -189,7 +206,7 @@ struct V1Params {
     int *farFlag;              // [3] any far-pre spike (sInfo > 1) in step t%3
     const int *farN1;          // [nV1] leading synapses of each list with whole-step delay <= 1
     int4 *farList;             // [3][nV1] step t%3's far spikers: (pre, first synapse, count, sInfo bits)
-    int *farCount;             // [3] length of each list
+    unsigned long long *farCount;  // [3] each list's spikers (high 32 bits) and synapses (low 32 bits)
     unsigned *spikeCount;      // [nV1] spikes per neuron since the counters were cleared (may be null)
     int noDelay;               // 1: near delivery from this step's spikes (conMat); 0: delayed events
     int nearOn;                // near-class (delayed) events exist: nearAcc is used
@@ -323,7 +340,9 @@ cudaError_t launch_frames(const float *recSpk, int recSlots, int nV1, const floa
                           cudaStream_t st);
 // Adds farPull to the E/I conductances (the far part of the delivery before the first step).
 cudaError_t launch_far_pull_apply(const V1Params &p, cudaStream_t st);
-int v1_persistent_ctas(const V1Params &p, int device, bool *fits);
+// Neuron CTAs of the persistent kernel; *fits: all can be resident at once; *pushCtas: the
+// far-push CTAs that fit beside them on the device (0 without far synapses).
+int v1_persistent_ctas(const V1Params &p, int device, bool *fits, int *pushCtas);
 // Evaluates the full-step decay factors of the three conductance kernels on the device and
 // stores them into p (synchronous).
 cudaError_t compute_step_decay(V1Params &p, cudaStream_t st);

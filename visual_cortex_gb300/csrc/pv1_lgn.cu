@@ -559,6 +559,30 @@ __device__ __forceinline__ int frame_number(const FrameSched &fs, int currentFra
 
 constexpr int kClassCta = 128;
 
+// Presynaptic LTP trace of LGN cell id over step it (LGN_nonlinear with learning 1-3,
+// src/discrete_input_convol.cu:1774-1808): the value at the start of the step and, when the
+// cell spiked, the value right after its spikes (the spike count added, then decayed from the
+// step start to the spike time tsp) go to the step's row of outPre; var leaves decayed to the
+// end of the step.
+__device__ __forceinline__ void ff_pre_step(const LgnParams &P, long long it, int id, unsigned nsp, float tsp,
+                                            float sInfo, float &var) {
+    float *row = P.outPre + (size_t)(it % P.outSlots) * 2 * P.nLGN;
+    row[id] = var;
+    float delta_t;
+    if (sInfo > 0) {
+        delta_t = tsp;
+        var += (float)nsp;
+        var *= expf(-delta_t / P.tauLTP);
+        row[P.nLGN + id] = var;
+        delta_t = P.dt - delta_t;
+    } else {
+        delta_t = P.dt;
+    }
+    var *= expf(-delta_t / P.tauLTP);
+}
+
+
+
 // The whole LGN step for a chunk of K steps when every magno cell has the same temporal
 // weights (one temporal kernel class): the window segment weights W[s][q] (differences of the
 // shared cumulative weights) and the frame slot of every segment are computed once per CTA;
@@ -626,6 +650,7 @@ __device__ __forceinline__ void lgn_class_body(const LgnParams &P, long long t0,
     float ltr = P.leftTimeRate[id];
     float lnl = P.lastNegLogRand[id];
     curandStateMRG32k3a st = P.state[id];
+    float ffVar = P.nFF ? P.ffPre[id] : 0.f;
     const float dt = P.dt;
     for (int s = 0; s < K; s++) {
         const long long it = t0 + s;
@@ -667,11 +692,14 @@ __device__ __forceinline__ void lgn_class_body(const LgnParams &P, long long t0,
             ltr = rT - old_rT;
             tsp = old_rT / (rate * nsp);
         }
-        P.outSInfo[(size_t)(it % P.outSlots) * P.nLGN + id] = nsp + tsp / dt;
+        const float sInfo = nsp + tsp / dt;
+        P.outSInfo[(size_t)(it % P.outSlots) * P.nLGN + id] = sInfo;
+        if (P.nFF) ff_pre_step(P, it, id, nsp, tsp, sInfo, ffVar);
     }
     P.leftTimeRate[id] = ltr;
     P.lastNegLogRand[id] = lnl;
     P.state[id] = st;
+    if (P.nFF) P.ffPre[id] = ffVar;
 }
 
 __global__ void __launch_bounds__(kClassCta) lgn_class_kernel(LgnParams P, const long long *stepBase, int K) {
@@ -808,6 +836,7 @@ __global__ void __launch_bounds__(256) lgn_spike_kernel(LgnParams P, const long 
     float ltr = P.leftTimeRate[id];
     float lnl = P.lastNegLogRand[id];
     curandStateMRG32k3a st = P.state[id];
+    float ffVar = P.nFF ? P.ffPre[id] : 0.f;
     const float dt = P.dt;
     const long long step0 = *stepBase;
     for (int s = 0; s < K; s++) {
@@ -843,10 +872,12 @@ __global__ void __launch_bounds__(256) lgn_spike_kernel(LgnParams P, const long 
         }
         const float sInfo = nsp + tsp / dt;
         P.outSInfo[(size_t)(it % P.outSlots) * P.nLGN + id] = sInfo;
+        if (P.nFF) ff_pre_step(P, it, id, nsp, tsp, sInfo, ffVar);
     }
     P.leftTimeRate[id] = ltr;
     P.lastNegLogRand[id] = lnl;
     P.state[id] = st;
+    if (P.nFF) P.ffPre[id] = ffVar;
 }
 
 }  // namespace pv1

@@ -113,6 +113,9 @@ extern "C" int pv1_lgn_spikes_noalloc(pv1_plan *plan, uint32_t nsteps, float *d_
     if (r) return r;
     if (view.lp.nParvo > 0)
         return plan_fail(plan, PV1_E_UNSUPPORTED, "pv1_lgn_spikes_noalloc: plans with parvo cells are not supported");
+    if (view.lp.nFF > 0)
+        return plan_fail(plan, PV1_E_UNSUPPORTED,
+                         "pv1_lgn_spikes_noalloc: plans with LGN->V1 plasticity are not supported");
     if (view.v1Stepped)
         return plan_fail(plan, PV1_E_STATE,
                          "pv1_lgn_spikes_noalloc: the plan was stepped by pv1_run or a batch; LGN-only stepping "

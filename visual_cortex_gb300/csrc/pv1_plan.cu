@@ -287,6 +287,7 @@ int plan_batch_view(pv1_plan *p, PlanBatchView *out) {
         return fail(p, PV1_E_STATE, "V1 synapses/connectivity/state/rng not set");
     if (p->vp.farPullOn || p->vp.nearPullOn)
         return fail(p, PV1_E_UNSUPPORTED, "batched trials with synaptic failure on delayed synapses are not built");
+    if (p->vp.ffLearn) return fail(p, PV1_E_UNSUPPORTED, "batched trials with LGN->V1 plasticity are not built");
     out->vp = p->vp;
     out->lp = p->lp;
     out->lgnRing = p->d_lgnRing;
@@ -1017,7 +1018,88 @@ int pv1_v1_set_lgn_synapses(pv1_plan *p, uint32_t maxLGN, const uint32_t *nLGNpe
     p->vp.nLGNperV1 = d_n;
     p->vp.lgnId = d_id;
     p->vp.sLGN = d_s;
+    p->vp.sLGNw = d_s;
     p->haveLGNsyn = true;
+    drop_graph(p);
+    return PV1_OK;
+}
+
+// The LGN stage's trace ring of a plan with learning: one row pair per LGN ring row.
+static int ensure_ff_ring(pv1_plan *p) {
+    if (!p->vp.ffLearn) return PV1_OK;
+    if (p->lp.outPre) free_one(p, p->lp.outPre);
+    p->lp.outPre = nullptr;
+    float *d = nullptr;
+    int r = dev_alloc(p, &d, (size_t)p->lgnSlots * 2 * p->nLGN);
+    if (r) return r;
+    p->lp.outPre = d;
+    p->vp.ffPreRing = d;
+    return PV1_OK;
+}
+
+int pv1_set_ff_learning(pv1_plan *p, const pv1_ff_learning *l) {
+    if (!p || !l) return PV1_E_ARG;
+    if (l->learning != 3)
+        return fail(p, PV1_E_UNSUPPORTED, "only learning = 3 (LGN->E plasticity) is built");
+    if (!p->lgnReady || !p->haveLGNsyn) return fail(p, PV1_E_STATE, "set up the LGN and the LGN->V1 synapses first");
+    if (p->vp.multiSpike)
+        return fail(p, PV1_E_UNSUPPORTED, "plasticity with several spikes per step (dt > min tRef) is not built");
+    if (!(l->tauLTP > 0 && l->tauLTD > 0 && l->tauTrip > 0 && l->tauAvg > 0 && l->decayTimeHomeoFF > 0))
+        return fail(p, PV1_E_ARG, "learning time constants must be > 0");
+    if (l->applyHomeo < 0 || l->applyHomeo > 2) return fail(p, PV1_E_ARG, "applyHomeo is 0, 1 or 2");
+    const pv1_v1_config &c = p->cfg;
+    const float dt = c.dt;
+    // learnFF_post (src/condShape.h:137-152), Float = float, with its double literals
+    const float A_LTP = l->A_LGN * l->sRatioLGN;
+    const float tauAvg_in_sec = (float)((double)l->tauAvg / 1000.0);
+    float A_ratio = l->r_LTD * A_LTP;
+    if (l->targetFR > 0) {
+        const float q = l->tauTrip / (l->tauLTD * (tauAvg_in_sec * tauAvg_in_sec));
+        A_ratio = (float)((double)A_ratio * ((double)q / 1000.0 / (double)l->targetFR));
+    }
+    V1Params &v = p->vp;
+    const size_t n = p->nV1, nEt = (size_t)p->nE * c.nblock, nIt = (size_t)p->nI * c.nblock;
+    // the homeostasis totals: each neuron's LGN weights summed in synapse order, and that
+    // times FF_InfRatio (src/patch.cu:4335-4352)
+    std::vector<float> s((size_t)v.maxLGN * n), tot(2 * n, 0.f);
+    std::vector<int> m(n);
+    PV1_CUDA(p, cudaStreamSynchronize(p->stream));
+    if (!s.empty()) PV1_CUDA(p, cudaMemcpy(s.data(), v.sLGN, s.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    PV1_CUDA(p, cudaMemcpy(m.data(), v.nLGNperV1, n * sizeof(int), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; i++) {
+        float t = 0.f;
+        for (int j = 0; j < m[i]; j++) t += s[(size_t)j * n + i];
+        tot[i] = t;
+        tot[n + i] = t * l->FF_InfRatio;
+    }
+    float *d_post = nullptr, *d_tot = nullptr, *d_pre = nullptr;
+    int r = 0;
+    r |= dev_alloc(p, &d_post, 4 * nEt + nIt);
+    r |= dev_upload(p, &d_tot, tot.data(), tot.size());
+    r |= dev_alloc(p, &d_pre, (size_t)p->nLGN);
+    if (r) return r;
+    v.ffLearn = 1;
+    v.ffTauLTP = l->tauLTP;
+    v.ffTauLTD = l->tauLTD;
+    v.ffTauTrip = l->tauTrip;
+    v.ffTauAvg = l->tauAvg;
+    v.ffTargetFR = l->targetFR;
+    v.ffA_LTP = A_LTP;
+    v.ffA_ratio = A_ratio;
+    v.ffGmax = l->gmaxLGN * l->sRatioLGN;
+    v.ffGmin = l->gminLGN * l->sRatioLGN;
+    v.applyHomeo = l->applyHomeo;
+    v.symmetricHomeo = l->symmetricHomeo != 0;
+    v.rebound = l->rebound != 0;
+    v.expHomeo = expf(-dt / l->decayTimeHomeoFF);
+    v.ffPost = d_post;
+    v.totalFF = d_tot;
+    v.sLGNw = const_cast<float *>(v.sLGN);
+    p->lp.nFF = 1;
+    p->lp.tauLTP = l->tauLTP;
+    p->lp.ffPre = d_pre;
+    r = ensure_ff_ring(p);
+    if (r) return r;
     drop_graph(p);
     return PV1_OK;
 }
@@ -1032,17 +1114,30 @@ int pv1_v1_set_near(pv1_plan *p, uint32_t nnb, const uint32_t *nNearNB, const ui
             if (nbId[(size_t)b * nnb + q] >= (uint32_t)nblock) return fail(p, PV1_E_ARG, "neighbour block id out of range");
     }
     const size_t bs = p->cfg.blockSize;
-    int *d_n, *d_id;
+    // for each pre block, the tiles whose rows its spikers' deliveries read (the kernels send
+    // those rows to L2 when the spike happens, a step before the delivery)
+    std::vector<int> revOff(nblock + 1, 0), rev;
+    for (int pb = 0; pb < nblock; pb++) {
+        for (int b = 0; b < nblock; b++)
+            for (uint32_t q = 0; q < nNearNB[b]; q++)
+                if ((int)nbId[(size_t)b * nnb + q] == pb) rev.push_back(b * (int)nnb + (int)q);
+        revOff[pb + 1] = (int)rev.size();
+    }
+    int *d_n, *d_id, *d_ro, *d_rev = nullptr;
     float *d_c;
     int r = 0;
     r |= dev_upload(p, &d_n, (const int *)nNearNB, nblock);
     r |= dev_upload(p, &d_id, (const int *)nbId, (size_t)nblock * nnb);
     r |= dev_upload(p, &d_c, conMat, (size_t)nblock * nnb * bs * bs);
+    r |= dev_upload(p, &d_ro, revOff.data(), revOff.size());
+    if (!rev.empty()) r |= dev_upload(p, &d_rev, rev.data(), rev.size());
     if (r) return r;
     p->vp.nnbMax = (int)nnb;
     p->vp.nNearNB = d_n;
     p->vp.nbId = d_id;
     p->vp.conMat = d_c;
+    p->vp.nearRevOff = d_ro;
+    p->vp.nearRev = d_rev;
     p->haveNear = true;
     drop_graph(p);
     return PV1_OK;
@@ -1107,7 +1202,8 @@ int build_event_lists(pv1_plan *p, const std::vector<EvSyn> &syn) {
         anyNear |= syn[e].near != 0;
         maxSteps = std::max(maxSteps, (int)it2post);
     }
-    int *d_off, *d_post, *d_steps, *d_n1, *d_count;
+    int *d_off, *d_post, *d_steps, *d_n1;
+    unsigned long long *d_count;
     float *d_str, *d_frac;
     unsigned char *d_pre;
     unsigned long long *d_acc, *d_nacc = nullptr;
@@ -1523,7 +1619,7 @@ int pv1_v1_init_spikes(pv1_plan *p, uint64_t seed, uint32_t trainDepth, const fl
         e = launch_v1_sp_near(vp, dH + (size_t)(depth - 1) * n, dOg, dOh, dZ, dNZ, (int)cap, p->stream);
     if (e == cudaSuccess && has && vp.farOn) {
         e = cudaMemsetAsync(vp.farFlag, 0, 3 * sizeof(int), p->stream);
-        if (e == cudaSuccess) e = cudaMemsetAsync(vp.farCount, 0, 3 * sizeof(int), p->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(vp.farCount, 0, 3 * sizeof(unsigned long long), p->stream);
         if (e == cudaSuccess) e = launch_v1_sp_events(vp, dH, depth, p->stream);
     }
     if (e == cudaSuccess && has && vp.farPullOn) {
@@ -1591,6 +1687,10 @@ int pv1_set_record(pv1_plan *p, int flags, uint32_t slots) {
     p->lp.outSInfo = p->d_lgnRing;
     p->lp.outFr = p->d_lgnFr;
     p->lp.outSlots = p->lgnSlots;
+    {
+        int r = ensure_ff_ring(p);
+        if (r) return r;
+    }
     p->vp.rec = p->d_rec;
     p->vp.recStride = p->recStride;
     p->vp.recSlots = (flags & (PV1_REC_RAW | PV1_REC_SPIKES)) ? (int)slots : 1;
@@ -1616,8 +1716,11 @@ int64_t pv1_raw_record_floats(const pv1_plan *p) {
 static int choose_mode(pv1_plan *p) {
     if (p->modeChosen) return PV1_OK;
     bool fits = false;
-    v1_persistent_ctas(p->vp, p->device, &fits);
-    p->persistent = fits && p->allowPersistent && !p->vp.multiSpike && !p->vp.farPullOn && !p->vp.nearPullOn;
+    int push = 0;
+    v1_persistent_ctas(p->vp, p->device, &fits, &push);
+    p->persistent = fits && p->allowPersistent && !p->vp.multiSpike && !p->vp.farPullOn && !p->vp.nearPullOn &&
+                    !p->vp.ffLearn;
+    p->vp.pushCta = p->persistent ? push : 0;
     if (p->persistent && !p->d_barrier) {
         int r = dev_alloc(p, &p->d_barrier, 2);
         if (r) return r;
@@ -2016,7 +2119,7 @@ void ckpt_items(pv1_plan *p, std::vector<std::pair<void *, size_t>> &items) {
         if (v.nearOn) add(v.nearAcc, ring);
         add(v.farFlag, 3 * sizeof(int));
         add(v.farList, 3 * n * sizeof(int4));
-        add(v.farCount, 3 * sizeof(int));
+        add(v.farCount, 3 * sizeof(unsigned long long));
     }
     if (v.nearPullOn && !v.farPullOn) add(v.sRing, (size_t)v.sDepth * n * f);
     if (v.farPullOn) {
@@ -2028,6 +2131,13 @@ void ckpt_items(pv1_plan *p, std::vector<std::pair<void *, size_t>> &items) {
     add(p->lp.leftTimeRate, p->nLGN * f);
     add(p->lp.lastNegLogRand, p->nLGN * f);
     add(p->lp.state, p->nLGN * sizeof(curandStateMRG32k3a));
+    if (v.ffLearn) {
+        const size_t nEt = (size_t)p->nE * c.nblock, nIt = (size_t)p->nI * c.nblock;
+        add(v.sLGNw, (size_t)v.maxLGN * n * f);
+        add(v.ffPost, (4 * nEt + nIt) * f);
+        add(v.totalFF, 2 * n * f);
+        add(p->lp.ffPre, p->nLGN * f);
+    }
 }
 
 CkptHeader ckpt_header(pv1_plan *p, const std::vector<std::pair<void *, size_t>> &items) {
@@ -2102,7 +2212,7 @@ int pv1_set_step(pv1_plan *p, int64_t step) {
         const size_t ring = (size_t)v.farDepth * ns * 2 * n * sizeof(unsigned long long);
         PV1_CUDA(p, zero(v.farAcc, ring));
         PV1_CUDA(p, zero(v.nearAcc, ring));
-        PV1_CUDA(p, zero(v.farCount, 3 * sizeof(int)));
+        PV1_CUDA(p, zero(v.farCount, 3 * sizeof(unsigned long long)));
         PV1_CUDA(p, zero(v.farFlag, 3 * sizeof(int)));
     }
     if (v.farPullOn) {
@@ -2216,6 +2326,10 @@ int pv1_get_state(pv1_plan *p, int which, float *out) {
         case PV1_ST_LGN_RNG: src = p->lp.state; cnt = p->nLGN * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
         case PV1_ST_V1_RNG_COND: src = v.rGenCond; cnt = n * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
         case PV1_ST_V1_RNG_NOISY: src = v.rNoisy; cnt = n * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
+        case PV1_ST_SLGN: src = v.sLGN; cnt = (size_t)v.maxLGN * n; break;
+        case PV1_ST_FF_POST: src = v.ffPost; cnt = 4 * (size_t)p->nE * c.nblock + (size_t)p->nI * c.nblock; break;
+        case PV1_ST_FF_PRE: src = p->lp.ffPre; cnt = p->nLGN; break;
+        case PV1_ST_TOTAL_FF: src = v.totalFF; cnt = 2 * n; break;
         default: return fail(p, PV1_E_ARG, "unknown state id");
     }
     if (!src) return fail(p, PV1_E_STATE, "state not allocated");
@@ -2248,6 +2362,10 @@ int pv1_put_state(pv1_plan *p, int which, const float *in) {
         case PV1_ST_LGN_RNG: dst = p->lp.state; cnt = p->nLGN * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
         case PV1_ST_V1_RNG_COND: dst = v.rGenCond; cnt = n * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
         case PV1_ST_V1_RNG_NOISY: dst = v.rNoisy; cnt = n * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
+        case PV1_ST_SLGN: dst = v.sLGNw; cnt = (size_t)v.maxLGN * n; break;
+        case PV1_ST_FF_POST: dst = v.ffPost; cnt = 4 * (size_t)p->nE * c.nblock + (size_t)p->nI * c.nblock; break;
+        case PV1_ST_FF_PRE: dst = p->lp.ffPre; cnt = p->nLGN; break;
+        case PV1_ST_TOTAL_FF: dst = v.totalFF; cnt = 2 * n; break;
         default: return fail(p, PV1_E_ARG, "state id cannot be written");
     }
     if (!dst) return fail(p, PV1_E_STATE, "state not allocated");

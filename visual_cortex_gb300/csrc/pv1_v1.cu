@@ -24,6 +24,7 @@
 // steps.  Both are instantiated with and without the random-number paths (noise, synaptic
 // failure); the host picks the variant.  Per-species arrays use compile-time indices so that
 // they stay in registers.
+#include <algorithm>
 #include "pv1_internal.cuh"
 
 namespace pv1 {
@@ -212,6 +213,28 @@ __device__ __forceinline__ int compact_spikers(const V1Params &P, const float *_
     }
     __syncthreads();
     return total;
+}
+
+// Sends to L2 what the next step reads because neuron i (local index `local` of block b)
+// spiked: its rows of the near tiles that list block b (read by the delivery, whole 16-byte
+// aligned rows), and the whole 16-byte chunks of its far synapse list (read by the push).
+// Hints only: nothing waits on them.
+__device__ __forceinline__ void prefetch_spiker(const V1Params &P, int b, int local, int farE0, int farDeg) {
+    if (P.noDelay && P.nearRevOff && (P.blockSize & 3) == 0) {
+        const unsigned bytes = (unsigned)P.blockSize * 4u;
+        for (int e = __ldg(P.nearRevOff + b); e < __ldg(P.nearRevOff + b + 1); e++) {
+            const float *row = P.conMat + ((size_t)__ldg(P.nearRev + e) * P.blockSize + local) * P.blockSize;
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(row), "r"(bytes) : "memory");
+        }
+    }
+    const int a = (farE0 + 3) & ~3, z = (farE0 + farDeg) & ~3;
+    if (z > a) {
+        const unsigned bytes = (unsigned)(z - a) * 4u;
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(P.farPost + a), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(P.farStr + a), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(P.farSteps + a), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(P.farFrac + a), "r"(bytes) : "memory");
+    }
 }
 
 // Phase A: delivery of step tp's spikes to this thread's neuron (all threads of the CTA
@@ -751,6 +774,125 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
     return sInfo;
 }
 
+// LGN->V1 plasticity after the membrane step of neuron i (learning = 3, only the LGN->E
+// synapses learn): compute_V_collect_spike_learnFF_fast's learning block (src/coredynamics.cu:
+// 1631-1993) with one FF_E learning type.  The post LTD and triplet traces and the filtered
+// rate are read at the step start and, when the neuron spiked, decayed to its spike time tsp;
+// each LGN synapse (in synapse order) takes the homeostatic factor, LTD when its LGN cell
+// spiked (from the post LTD trace at the earlier of the two spike times, scaled by the
+// squared filtered rate when targetFR > 0), LTP when the neuron spiked (the presynaptic trace
+// at the step start or right after the LGN spike, whichever precedes tsp, decayed to tsp, times
+// the post triplet trace), and is clipped to [gmin, gmax]; the post traces then take the spike
+// count and decay to the end of the step.  Float arithmetic in the reference's order.
+__device__ __noinline__ void learn_ff(const V1Params &P, long long t, int i, int local, int m, float sInfo,
+                                      const float *__restrict__ lgnSInfo, const float *__restrict__ preRow,
+                                      int nLGN) {
+    if (local >= P.nE) return;
+    const float dt = P.dt;
+    float nsp, tsp;
+    if (sInfo > 0) {
+        nsp = floorf(sInfo);
+        tsp = (sInfo - nsp) * dt;
+    } else {
+        nsp = 0;
+        tsp = dt;
+    }
+    const int nV1 = P.nV1;
+    const int nEt = P.nE * P.nblock;
+    const int eid = (i / P.blockSize) * P.nE + local;
+    float *vLTD = P.ffPost, *vTrip = P.ffPost + nEt, *vAvgE = P.ffPost + 2 * nEt;
+    // row 0: the step start; row 1: the spike time
+    float lLTD[2], lTrip[2], lAvg[2];
+    lLTD[0] = vLTD[eid];
+    lTrip[0] = vTrip[eid];
+    lAvg[0] = vAvgE[2 * eid];
+    lLTD[1] = lTrip[1] = lAvg[1] = 0.f;
+    if (nsp > 0) {
+        lLTD[1] = lLTD[0];
+        lTrip[1] = lTrip[0];
+        lLTD[1] *= expf(-tsp / P.ffTauLTD);
+        lTrip[1] *= expf(-tsp / P.ffTauTrip);
+        lAvg[1] = lAvg[0];
+        lAvg[1] *= expf(-tsp / P.ffTauAvg);
+    }
+    float new0 = 0.f, change = 0.f, delta_f = 0.f;
+    if (P.applyHomeo) {
+        const float f0 = P.totalFF[i];
+        const float finf = P.totalFF[nV1 + i];
+        const float d = f0 - finf;
+        if (d > 0 || P.symmetricHomeo) {
+            new0 = d * P.expHomeo + finf;
+            change = P.applyHomeo == 1 ? new0 / f0 : (new0 - f0) / (float)m;
+        } else {
+            new0 = f0;
+            change = P.applyHomeo == 1 ? 1.f : 0.f;
+        }
+    }
+    for (int q = 0; q < m; q++) {
+        const size_t lid = (size_t)q * nV1 + i;
+        float f = P.sLGNw[lid];
+        if (f == 0 && !P.rebound) continue;
+        if (P.applyHomeo == 1) f *= change;
+        else if (P.applyHomeo == 2) f += change;
+        const int id = __ldg(P.lgnId + lid);
+        const float sFF = __ldcg(lgnSInfo + id);
+        const unsigned nspFF = (unsigned)floorf(sFF);
+        const float tspFF = (sFF > 0 ? sFF - (float)nspFF : 1.f) * dt;
+        if (nspFF > 0) {  // LTD, whether or not the neuron spiked
+            int cPick;
+            float delta_t;
+            if (tspFF < tsp) {
+                cPick = 0;
+                delta_t = tspFF;
+            } else {
+                cPick = 1;
+                delta_t = tspFF - tsp;
+            }
+            float A_LTD = P.ffA_ratio;
+            if (P.ffTargetFR > 0) A_LTD *= P.ffTauLTP * lAvg[cPick] * lAvg[cPick];
+            const float df = lLTD[cPick] * expf(-delta_t / P.ffTauLTD) * A_LTD;
+            f -= df;
+            if (P.applyHomeo) delta_f -= df;
+        }
+        if (nsp > 0) {  // LTP, whether or not the LGN cell spiked
+            float lpre, delta_t;
+            if (tspFF < tsp) {
+                lpre = __ldcg(preRow + nLGN + id);
+                delta_t = tsp - tspFF;
+            } else {
+                lpre = __ldcg(preRow + id);
+                delta_t = tsp;
+            }
+            const float df = lpre * expf(-delta_t / P.ffTauLTP) * lTrip[1] * P.ffA_LTP;
+            if (P.applyHomeo) delta_f += df;
+            f += df;
+        }
+        if (f < P.ffGmin) {
+            if (P.applyHomeo) delta_f += P.ffGmin - f;
+            f = P.ffGmin;
+        }
+        if (f > P.ffGmax) {
+            if (P.applyHomeo) delta_f -= f - P.ffGmax;
+            f = P.ffGmax;
+        }
+        P.sLGNw[lid] = f;
+    }
+    if (P.applyHomeo) P.totalFF[i] = new0 + delta_f;
+    // the post traces take this step's spikes and decay to its end
+    float delta_t = dt;
+    const int cPick = nsp > 0 ? 1 : 0;
+    if (nsp > 0) delta_t -= tsp;
+    lLTD[cPick] += nsp;
+    lTrip[cPick] += nsp;
+    lLTD[cPick] *= expf(-delta_t / P.ffTauLTD);
+    lTrip[cPick] *= expf(-delta_t / P.ffTauTrip);
+    lAvg[cPick] += nsp;
+    lAvg[cPick] *= expf(-delta_t / P.ffTauAvg);
+    vLTD[eid] = lLTD[cPick];
+    vTrip[eid] = lTrip[cPick];
+    vAvgE[2 * eid] = lAvg[cPick];
+}
+
 // Phase B when dt exceeds the shortest refractory period: a neuron may fire several times in
 // one step (compute_V_collect_spike_learnFF, src/coredynamics.cu:427-845, without learning).
 // After each spike whose refractory period ends inside the step the membrane is integrated
@@ -988,7 +1130,7 @@ __device__ __noinline__ float step_neuron_multi(const V1Params &P, long long t, 
 // and recal_G_mat (2163-2200) compute them, with explicitly rounded operations.  `code` is the
 // synapse's packed word: post type in bits 16-23, class in bit 24 (1: near block, delivered
 // through nearAcc; 0: far, through farAcc).
-__device__ __forceinline__ void far_event(const V1Params &P, long long t, int pre, float sI, int post,
+__device__ __forceinline__ void far_event(const V1Params &P, long long t, int tSlot, int pre, float sI, int post,
                                           float f, int steps, int code, float frac, int kk) {
     const int ptype = (code >> 16) & 0xff;
     const bool nearClass = (code >> 24) & 1;
@@ -1009,10 +1151,12 @@ __device__ __forceinline__ void far_event(const V1Params &P, long long t, int pr
     const int ng = preE ? P.ngE : P.ngI;
     const int qoff = preE ? 0 : P.ngE;
     const float delta = __fsub_rn(dt, dtsp);
-    // tArr >= -1: the only arrival before step 0 is the delivery that precedes the first step
-    // when there are initial spikes (step -1, ring slot farDepth - 1)
-    unsigned long long *acc =
-        (nearClass ? P.nearAcc : P.farAcc) + (size_t)((tArr + P.farDepth) % P.farDepth) * ns * 2 * nV1;
+    // ring slot of tArr: tSlot is step t's (t mod farDepth, in [0, farDepth)) and 0 <= tArr - t
+    // < farDepth - 1 (the only arrival before step 0 is the delivery that precedes the first
+    // step when there are initial spikes: step -1, slot farDepth - 1)
+    int aSlot = tSlot + (int)(tArr - t);
+    if (aSlot >= P.farDepth) aSlot -= P.farDepth;
+    unsigned long long *acc = (nearClass ? P.nearAcc : P.farAcc) + (size_t)aSlot * ns * 2 * nV1;
 #pragma unroll
     for (int ig = 0; ig < kMaxNG; ig++) {
         if (ig < ng) {
@@ -1060,26 +1204,39 @@ __device__ __forceinline__ int owner_of(const Smem &sm, int cnt, int w) {
     return lo;
 }
 
+// Ring slot of step t in the far/near event rings.
+__device__ __forceinline__ int far_ring_slot(const V1Params &P, long long t) {
+    const long long r = t % P.farDepth;
+    return (int)(r < 0 ? r + P.farDepth : r);
+}
+
+// Spiker count (high 32 bits) and synapse work (low 32 bits) of step tl's far list.
+__device__ __forceinline__ unsigned long long far_list_size(const V1Params &P, long long tl) {
+    return __ldcg(P.farCount + (int)((tl + 3) % 3));
+}
+
 // Phase C, part 1 (runs in step tl + 1): the far events of step tl's spikes that arrive after
-// step tl, from the step's global spiker list.  The (spiker, synapse) work is flattened over
-// every thread of the grid, so one CTA's burst of spikers no longer serialises on that CTA;
-// the fixed-point ring makes the sums independent of the order of the atomic appends.
-__device__ __forceinline__ void far_push_list(const V1Params &P, long long tl, Smem &sm, int cta, int nCta) {
+// step tl, from the step's global spiker list.  The (spiker, synapse) work items are numbered
+// in list order; the items [lo, hi) are shared by the nCta CTAs given, thread gt of them
+// taking lo + gt, lo + gt + G, ... (G their threads), U items per pass with their synapse
+// loads issued together.  The fixed-point ring makes the sums independent of which thread
+// appends which event, and in which order.
+template <int U = 1>
+__device__ __forceinline__ void far_push_range(const V1Params &P, long long tl, Smem &sm, int cta, int nCta,
+                                               unsigned long long size, int lo, int hi) {
+    const int n = (int)(size >> 32);
+    if (n == 0 || lo >= hi) return;
     const int slot = (int)((tl + 3) % 3);  // tl >= -1
     const int4 *list = P.farList + (size_t)slot * P.nV1;
-    // the first chunk's entries are fetched together with the count (entries past the count
-    // are stale and not used)
-    const int4 first = (int)threadIdx.x < P.nV1 ? __ldcg(list + threadIdx.x) : make_int4(0, 0, 0, 0);
-    const int n = __ldcg(P.farCount + slot);
-    if (n == 0) return;
+    const int tSlot = far_ring_slot(P, tl);
     const int G = nCta * kCta;
     const int gt = cta * kCta + threadIdx.x;
-    int W0 = 0;  // work of the earlier chunks, modulo G
-    for (int c0 = 0; c0 < n; c0 += kCta) {
+    int base = 0;  // items of the earlier chunks
+    for (int c0 = 0; c0 < n && base < hi; c0 += kCta) {
         const int cnt = min(kCta, n - c0);
         __syncthreads();
         if (threadIdx.x < cnt) {
-            const int4 e = c0 == 0 ? first : __ldcg(list + c0 + threadIdx.x);
+            const int4 e = __ldcg(list + c0 + threadIdx.x);
             sm.fpre[threadIdx.x] = e.x;
             sm.fe0[threadIdx.x] = e.y;
             sm.fdeg[threadIdx.x] = e.z;
@@ -1089,25 +1246,48 @@ __device__ __forceinline__ void far_push_list(const V1Params &P, long long tl, S
         scan_degrees(sm, cnt);
         __syncthreads();
         const int work = sm.fpref[cnt];
-        // this thread takes the items whose global index is congruent to gt modulo G
-        int w = gt - W0;
-        if (w < 0) w += G;
-        for (; w < work; w += G) {
-            const int r = owner_of(sm, cnt, w);
-            const int e = sm.fe0[r] + (w - sm.fpref[r]);
-            const int post = __ldg(P.farPost + e);
-            const float f = __ldg(P.farStr + e);
-            const int sp = __ldg(P.farSteps + e);
-            const float frac = __ldg(P.farFrac + e);
-            const int steps = sp & 0xffff;
-            const int pre = sm.fpre[r];
-            const float sI = sm.fsi[r];
-            // the slot arriving in step tl itself (steps == k) was pushed in step tl
-            if (steps != 0) far_event(P, tl, pre, sI, post, f, steps, sp, frac, 0);
-            if (steps != 1) far_event(P, tl, pre, sI, post, f, steps, sp, frac, 1);
+        // this chunk's items [base, base + work) within [lo, hi): the first of this thread's
+        // items at or after max(base, lo)
+        const int a = max(base, lo), z = min(base + work, hi);
+        int w = lo + gt;
+        if (w < a) w += (a - w + G - 1) / G * G;
+        for (; w < z; w += U * G) {
+            int rr[U], post[U], sp[U];
+            float f[U], frac[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int wu = w + u * G - base;
+                rr[u] = -1;
+                if (w + u * G < z) {
+                    const int r = owner_of(sm, cnt, wu);
+                    const int e = sm.fe0[r] + (wu - sm.fpref[r]);
+                    rr[u] = r;
+                    post[u] = __ldg(P.farPost + e);
+                    f[u] = __ldg(P.farStr + e);
+                    sp[u] = __ldg(P.farSteps + e);
+                    frac[u] = __ldg(P.farFrac + e);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (rr[u] < 0) continue;
+                const int steps = sp[u] & 0xffff;
+                const int pre = sm.fpre[rr[u]];
+                const float sI = sm.fsi[rr[u]];
+                // the slot arriving in step tl itself (steps == k) was pushed in step tl
+                if (steps != 0) far_event(P, tl, tSlot, pre, sI, post[u], f[u], steps, sp[u], frac[u], 0);
+                if (steps != 1) far_event(P, tl, tSlot, pre, sI, post[u], f[u], steps, sp[u], frac[u], 1);
+            }
         }
-        W0 = (int)(((long long)W0 + work) % G);
+        base += work;
     }
+}
+
+// All of step tl's far push, shared by nCta CTAs.
+template <int U = 1>
+__device__ __forceinline__ void far_push_list(const V1Params &P, long long tl, Smem &sm, int cta, int nCta) {
+    const unsigned long long size = far_list_size(P, tl);
+    far_push_range<U>(P, tl, sm, cta, nCta, size, 0, (int)(size & 0xffffffffu));
 }
 
 // Phase C, part 2 (runs in step t): appends this CTA's far presynaptic spikers to step t's
@@ -1118,7 +1298,7 @@ __device__ __forceinline__ void far_phase(const V1Params &P, long long t, int i,
                                           bool isFarPre, int e0, int deg, int n1, Smem &sm, int cta) {
     if (cta == 0 && threadIdx.x == 0) {
         P.farFlag[(t + 1) % 3] = 0;
-        P.farCount[(t + 1) % 3] = 0;
+        P.farCount[(t + 1) % 3] = 0ull;
     }
     if (active && sInfo > 1.0f && isFarPre) P.farFlag[t % 3] = 1;
     const bool spk = active && sInfo >= 1.0f;
@@ -1127,8 +1307,11 @@ __device__ __forceinline__ void far_phase(const V1Params &P, long long t, int i,
     const unsigned ab = __ballot_sync(0xffffffffu, app);
     if (ab) {
         const int leader = __ffs(ab) - 1;
+        // one atomic per warp adds its spikers (high half) and their synapses (low half)
+        const unsigned wsum = __reduce_add_sync(0xffffffffu, app ? (unsigned)deg : 0u);
         int base = 0;
-        if (lane == leader) base = atomicAdd(P.farCount + t % 3, __popc(ab));
+        if (lane == leader)
+            base = (int)(atomicAdd(P.farCount + t % 3, ((unsigned long long)__popc(ab) << 32) | wsum) >> 32);
         base = __shfl_sync(0xffffffffu, base, leader);
         if (app)
             P.farList[(size_t)(t % 3) * P.nV1 + base + __popc(ab & ((1u << lane) - 1u))] =
@@ -1158,6 +1341,7 @@ __device__ __forceinline__ void far_phase(const V1Params &P, long long t, int i,
     scan_degrees(sm, cnt);
     __syncthreads();
     const int work = sm.fpref[cnt];
+    const int tSlot = far_ring_slot(P, t);
     for (int w = threadIdx.x; w < work; w += kCta) {
         const int r = owner_of(sm, cnt, w);
         const int e = sm.fe0[r] + (w - sm.fpref[r]);
@@ -1167,7 +1351,7 @@ __device__ __forceinline__ void far_phase(const V1Params &P, long long t, int i,
         const float frac = __ldg(P.farFrac + e);
         const int steps = sp & 0xffff;
         // steps is 0 or 1 here: the slot with tArr == t
-        far_event(P, t, sm.fpre[r], sm.fsi[r], post, f, steps, sp, frac, steps);
+        far_event(P, t, tSlot, sm.fpre[r], sm.fsi[r], post, f, steps, sp, frac, steps);
     }
 }
 
@@ -1215,6 +1399,9 @@ __device__ __forceinline__ void v1_step_body(const V1Params &P, long long t, int
         if (Rng && P.noiseRng) P.rNoisy[i] = noisyState;
         if (P.spikeCount && sInfo >= 1.0f) P.spikeCount[i] += (unsigned)floorf(sInfo);
         if (P.farPullOn || P.nearPullOn) P.sRing[(size_t)(t % P.sDepth) * P.nV1 + i] = sInfo;
+        if (P.ffLearn)
+            learn_ff(P, t, i, local, P.nLGNperV1[i], sInfo, lgnSInfo,
+                     P.ffPreRing + (size_t)(t % lgnSlots) * 2 * P.lgnN, P.lgnN);
     }
     if (P.farOn) {
         const int e0 = active ? P.farOff[i] : 0;
@@ -1245,6 +1432,7 @@ __global__ void __launch_bounds__(kCta) v1_step_kernel(V1Params P, const long lo
 // must not read what other CTAs write in the step (the next step's LGN spike words are
 // written before the launch).
 constexpr unsigned kBarrierAbort = 0x80000000u;
+constexpr int kPushBatch = 8;   // far-push items per thread and pass of a far-push CTA
 
 __device__ __forceinline__ void barrier_arrive(unsigned *count, unsigned *s_arrived) {
     __syncthreads();
@@ -1287,9 +1475,32 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
                                                                  int lgnSlots, int deliverFirst,
                                                                  unsigned *barrier) {
     __shared__ Smem sm;
+    __shared__ unsigned s_arrived;
     const long long t0 = *stepBase;
     const int bs = P.blockSize;
     const int nq = (bs + kCta - 1) / kCta;
+    const int nNeuron = (int)gridDim.x - P.pushCta;
+    // the far-push CTAs take the first items of each step's push (one batch per thread), the
+    // neuron CTAs the rest after their own step work
+    const int pushShare = P.pushCta * kCta * kPushBatch;
+    if ((int)blockIdx.x >= nNeuron) {
+        // far-push CTA: in step t it pushes the far events of step t - 1's spikers (those that
+        // arrive after step t - 1) while the neuron CTAs deliver and step; the grid barrier
+        // that ends step t orders them before the delivery that reads them
+        for (int s = 0; s < K; s++) {
+            if (P.farOn) {
+                const unsigned long long size = far_list_size(P, t0 + s - 1);
+                far_push_range<kPushBatch>(P, t0 + s - 1, sm, (int)blockIdx.x - nNeuron, P.pushCta, size, 0,
+                                           min((int)(size & 0xffffffffu), pushShare));
+            }
+            if (s + 1 < K) {
+                barrier_arrive(barrier, &s_arrived);
+                if (!barrier_wait(barrier, (unsigned)gridDim.x * (unsigned)(s + 1), &s_arrived, P.err, P.waitSpins))
+                    break;
+            }
+        }
+        return;
+    }
     const int b = blockIdx.x / nq;
     const int local = (blockIdx.x % nq) * kCta + threadIdx.x;
     const bool active = local < bs;
@@ -1312,11 +1523,11 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
     const int farDeg = (P.farOn && active) ? P.farOff[i + 1] - farE0 : 0;
     const int farN1 = (P.farOn && active) ? P.farN1[i] : 0;
     const bool isFarPre = P.farOn && active && P.farPre[i];
-    __shared__ unsigned s_arrived;
     LgnPre lgnPre{0u, 0.f, 0.f};
     bool haveMask = false;
     for (int s = 0; s < K; s++) {
         const long long t = t0 + s;
+        const unsigned long long farSize = P.farOn ? far_list_size(P, t - 1) : 0ull;
         if (s > 0 || deliverFirst) deliver_prev<Rng>(P, t - 1, b, local, i, active, itype, st, condState, sm);
         float sInfo = 0.f;
         if (active) {
@@ -1324,9 +1535,10 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
             sInfo = step_neuron<Rng, true>(P, t, i, itype, tonic, depC, m, lgnIds, lgnSInfo, st, condState,
                                            noisyState, haveMask ? &lgnPre : nullptr);
             if (P.spikeCount && sInfo >= 1.0f) P.spikeCount[i] += (unsigned)floorf(sInfo);
+            if (sInfo >= 1.0f) prefetch_spiker(P, b, local, farE0, farDeg);
         }
         if (P.farOn) {
-            far_push_list(P, t - 1, sm, blockIdx.x, gridDim.x);
+            far_push_range(P, t - 1, sm, blockIdx.x, nNeuron, farSize, pushShare, (int)(farSize & 0xffffffffu));
             far_phase(P, t, i, active, sInfo, isFarPre, farE0, farDeg, farN1, sm, blockIdx.x);
         }
         if (s + 1 < K) {
@@ -1561,7 +1773,7 @@ __global__ void v1_sp_push_kernel(V1Params P, const float *H, int depth) {
     const int e0 = P.farOff[i], deg = P.farOff[i + 1] - e0;
     if (sLast > 1.0f && P.farPre[i]) P.farFlag[2] = 1;
     if (sLast >= 1.0f && deg > 0) {
-        const int pos = atomicAdd(P.farCount + 2, 1);
+        const int pos = (int)(atomicAdd(P.farCount + 2, (1ull << 32) | (unsigned)deg) >> 32);
         P.farList[(size_t)2 * nV1 + pos] = make_int4(i, e0, deg, __float_as_int(sLast));
     }
     for (int e = e0; e < e0 + deg; e++) {
@@ -1571,7 +1783,7 @@ __global__ void v1_sp_push_kernel(V1Params P, const float *H, int depth) {
         const float frac = P.farFrac[e];
         const int steps = sp & 0xffff;
         if (!((sp >> 24) & 1)) {
-            if (sLast >= 1.0f && steps <= 1) far_event(P, -1, i, sLast, post, f, steps, sp, frac, steps);
+            if (sLast >= 1.0f && steps <= 1) far_event(P, -1, far_ring_slot(P, -1), i, sLast, post, f, steps, sp, frac, steps);
             continue;
         }
         for (int q = 0; q < depth; q++) {
@@ -1579,14 +1791,14 @@ __global__ void v1_sp_push_kernel(V1Params P, const float *H, int depth) {
             if (w < 1.0f) continue;
             const long long th = q == 0 ? -1 : (long long)q - depth - 1;
             const long long k = th + steps + 1;
-            if (k == 0 || k == 1) far_event(P, th, i, w, post, f, steps, sp, frac, (int)k);
+            if (k == 0 || k == 1) far_event(P, th, far_ring_slot(P, th), i, w, post, f, steps, sp, frac, (int)k);
         }
         for (int q = 1; q < depth - 1; q++) {
             const float w = H[(size_t)q * nV1 + i];
             if (w < 1.0f) continue;
             const long long th = (long long)q - depth;
             for (int k = 0; k < 2; k++)
-                if (k <= steps && th + steps - k >= 0) far_event(P, th, i, w, post, f, steps, sp, frac, k);
+                if (k <= steps && th + steps - k >= 0) far_event(P, th, far_ring_slot(P, th), i, w, post, f, steps, sp, frac, k);
         }
     }
 }
@@ -1673,9 +1885,10 @@ cudaError_t launch_v1_step(const V1Params &p, const long long *stepBase, int ste
 }
 
 // Number of CTAs of the persistent kernel and whether they can all be resident at once.
-int v1_persistent_ctas(const V1Params &p, int device, bool *fits) {
+int v1_persistent_ctas(const V1Params &p, int device, bool *fits, int *pushCtas) {
     const int nq = (p.blockSize + kCta - 1) / kCta;
     const int n = p.nblock * nq;
+    *pushCtas = 0;
     int perSM = 0, sms = 0;
     if (needs_rng(p))
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_persistent_kernel<true>, kCta, 0);
@@ -1685,6 +1898,9 @@ int v1_persistent_ctas(const V1Params &p, int device, bool *fits) {
     int coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
     *fits = coop && perSM > 0 && n <= perSM * sms && p.maxLGN <= kMaxLgnReg;
+    // far-push CTAs on the SMs the neuron CTAs leave free (at most a quarter of the neuron
+    // CTAs, at least 8 when that many are free: each one more CTA at every grid barrier)
+    if (*fits && p.farOn) *pushCtas = std::min(perSM * sms - n, std::max(8, n / 4));
     return n;
 }
 
@@ -1692,7 +1908,7 @@ cudaError_t launch_v1_persistent(const V1Params &p, const long long *stepBase, i
                                  int lgnSlots, int deliverFirst, unsigned *barrier, cudaStream_t st) {
     const int nq = (p.blockSize + kCta - 1) / kCta;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(p.nblock * nq);
+    cfg.gridDim = dim3(p.nblock * nq + p.pushCta);
     cfg.blockDim = dim3(kCta);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;

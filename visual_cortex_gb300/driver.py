@@ -69,8 +69,13 @@ class Model:
 
 def _check_supported(c: Config):
     bad = []
-    if c.learning != 0:
-        bad.append("learning (LGN->V1 / cortical plasticity)")
+    if c.learning not in (0, 3):
+        bad.append(f"learning = {c.learning} (cortical E/Q plasticity, LGN->I plasticity; learning = 3, "
+                   "LGN->E plasticity, is built)")
+    if c.learning == 3 and int(c.values.get("nLearnTypeFF_E", 1)) != 1:
+        bad.append("learning = 3 with nLearnTypeFF_E != 1")
+    if c.learning == 3 and int(c.learnData_FF) > 1:
+        bad.append("learnData_FF = 2 (per-step learning dumps)")
     if c.InhGap:
         bad.append("InhGap (gap junctions)")
     if c.useNewLGN:
@@ -205,12 +210,13 @@ def _restore(sim, c: Config, m) -> int:
         return sim.step
     spec = m.spec
     try:
-        snap, trailer = FM.read_reference_snapshot(path, spec.nI * spec.nblock)
+        snap, trailer = FM.read_reference_snapshot(path, spec.nI * spec.nblock, maxLGN=m.net.maxLGN,
+                                                   nE_total=spec.nE * spec.nblock)
     except ValueError as e:
         raise ConfigError(str(e)) from None
     sz = snap["sizes"]
-    if (snap["iModel"] != spec.iModel or sz["nV1"] != spec.nV1 or sz["nLGN"] != m.lgn.nLGN or
-            sz["ngFF"] != spec.ngFF or sz["ngE"] != spec.ngE or sz["ngI"] != spec.ngI):
+    if (snap["learning"] != int(c.learning) or snap["iModel"] != spec.iModel or sz["nV1"] != spec.nV1 or
+            sz["nLGN"] != m.lgn.nLGN or sz["ngFF"] != spec.ngFF or sz["ngE"] != spec.ngE or sz["ngI"] != spec.ngI):
         raise ConfigError(f"{path}: patchV1 config is incompatible with the restore file config")
     if not c.asInit and trailer[:8] == b"PV1CKPT\0":
         sim.restore(np.frombuffer(trailer, np.uint8).copy())
@@ -233,9 +239,65 @@ def _restore(sim, c: Config, m) -> int:
     sim.put_state("lgn_ltr", snap["lgn"]["ltr"])
     sim.put_state("lgn_lnl", snap["lgn"]["lnl"])
     sim.put_state("lgn_rng", snap["lgn"]["rng"])
+    if snap["learn"] is not None:
+        # the weights and learning variables; the homeostasis totals stay those of the
+        # connectome's weights, as the reference computes them before it restores
+        for k in ("sLGN", "ff_post", "ff_pre"):
+            sim.put_state(k, snap["learn"][k])
     N.check(sim.plan, N.lib.pv1_set_step(sim.plan, int(step)), "pv1_set_step")
     sim.step = int(step)
     return int(step)
+
+
+def _ff_learning(c: Config, sRatioLGN):
+    """The FFLearning of learning = 3 from the cfg (src/patch.cu:1092-1330): element [0] of the
+    triplet-rule arrays; tauAvg and targetFR of size 1 or 2 ([0]: E); the Q arrays must agree in
+    size even though Q learning is off; gmaxLGN and gminLGN must be given."""
+    from .model import FFLearning
+    v = c.values
+
+    def first(key, required=True):
+        a = v.get(key)
+        if not a:
+            if required:
+                raise ConfigError(f"learning = 3 needs '{key}'")
+            return None
+        return float(a[0])
+
+    for key in ("tauAvg", "targetFR"):
+        a = v.get(key) or []
+        if len(a) not in (1, 2):
+            raise ConfigError(f"{key} must have 1 or 2 values (E, I), not {len(a)}")
+    sizes = [len(v.get(k) or []) for k in ("tauQ", "A_Q", "gmaxQ", "gminQ")]
+    if len(set(sizes)) != 1:
+        raise ConfigError(f"size of tauQ: {sizes[0]} should be the same as A_Q: {sizes[1]}")
+    nTrip = len(v.get("tauTrip") or [])
+    for key in ("r_LTD", "tauLTD", "tauLTP"):
+        if len(v.get(key) or []) != nTrip:
+            raise ConfigError(f"the size of {key} should be the same as tauTrip: {nTrip}")
+    return FFLearning(tauLTP=first("tauLTP"), tauLTD=first("tauLTD"), tauTrip=first("tauTrip"),
+                      tauAvg=first("tauAvg"), targetFR=first("targetFR"), A_LGN=first("A_LGN"),
+                      r_LTD=first("r_LTD"), gmaxLGN=first("gmaxLGN"), gminLGN=first("gminLGN"),
+                      sRatioLGN=float(sRatioLGN[0]), decayTimeHomeoFF=float(c.decayTimeHomeoFF),
+                      FF_InfRatio=float(c.FF_InfRatio), applyHomeo=int(c.applyHomeo),
+                      symmetricHomeo=bool(c.symmetricHomeo), rebound=bool(c.rebound))
+
+
+def _ltd_ratio(learn):
+    """A_ratio * tauLTP of the FF_E type, the dsLGN header's LTD ratio (src/patch.cu:4804-4806):
+    learnFF_post's A_ratio (src/condShape.h:137-152) in float with its double literals."""
+    f = np.float32
+    A_LTP = f(f(learn.A_LGN) * f(learn.sRatioLGN))
+    A_ratio = f(f(learn.r_LTD) * A_LTP)
+    if learn.targetFR > 0:
+        tas = f(float(f(learn.tauAvg)) / 1000.0)
+        q = f(f(learn.tauTrip) / f(f(learn.tauLTD) * f(tas * tas)))
+        A_ratio = f(float(A_ratio) * (float(q) / 1000.0 / float(f(learn.targetFR))))
+    return float(f(A_ratio * f(learn.tauLTP)))
+
+
+def _learn_state(sim, m):
+    return dict(sLGN=sim.state("sLGN"), ff_post=sim.state("ff_post"), ff_pre=sim.state("ff_pre"))
 
 
 def _write_snapshot(sim, c: Config, m, history, previous, log):
@@ -259,13 +321,14 @@ def _write_snapshot(sim, c: Config, m, history, previous, log):
     if spec.iModel == 1:
         state["w"] = sim.state("w")
     state["gap"] = np.zeros(spec.nI * spec.nblock, np.float32)
+    learning = int(c.learning)
     FM.write_reference_snapshot(
-        name, m.lgn.sched.snapshot_indices(q, depth), spec.iModel, 0,
+        name, m.lgn.sched.snapshot_indices(q, depth), spec.iModel, learning,
         dict(nV1=spec.nV1, nLGN=m.lgn.nLGN, ngFF=spec.ngFF, ngE=spec.ngE, ngI=spec.ngI, nType=spec.nType,
              trainDepth=depth),
         dict(ltr=sim.state("lgn_ltr"), lnl=sim.state("lgn_lnl"), rng=sim.state("lgn_rng")),
         dict(rng_cond=sim.state("v1_rng_cond"), rng_noisy=sim.state("v1_rng_noisy"), tBack=sim.state("tBack")),
-        ring, state, trailer)
+        ring, state, trailer, learn=_learn_state(sim, m) if learning else None)
     if previous and previous != name and c.delPrevSnapshot and os.path.exists(previous):
         os.remove(previous)
     log(f"saved a snapshot in {name}")
@@ -550,6 +613,10 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
     spec = m.spec
     sim = Simulation(m.spec, m.net, m.lgn, m.stim, m.init, m.seeds)
     try:
+        learn = None
+        if c.learning == 3:
+            learn = _ff_learning(c, m.extra["sRatioLGN"])
+            sim.set_ff_learning(learn)
         minimal = bool(c.minimal)
         flags = (N.REC_RAW if c.rawData else 0) | (N.REC_LGN_SP if c.getLGN_sp else 0) | \
                 (N.REC_LGN_FR if c.saveLGN_fr else 0)
@@ -574,6 +641,16 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
             if c.frameVisLGNoutput:
                 flags |= N.REC_LGN_FR
             frames = _setup_frames(sim, c, m, P)
+        slgn = dslgn = None
+        sample_every = max(int(c.sampleInterval_LGN_V1), 1)
+        if learn is not None and int(c.learnData_FF) == 1 and not minimal:
+            sr2 = (list(m.extra["sRatioLGN"]) * 2)[:2]
+            slgn = FM.SLgnWriter(P.slgn, m.nt, sample_every, spec.dt, spec.nV1, m.net.maxLGN, sr2, 1, 0,
+                                 c.values.get("gmaxLGN"), float(c.FF_InfRatio))
+            if c.store_dsLGN:
+                tfr = (list(c.values.get("targetFR")) * 2)[:2]
+                dslgn = FM.DsLgnWriter(P.dslgn, m.nt, sample_every, spec.dt, spec.nV1, m.net.maxLGN, sr2, 1, 0,
+                                       c.values.get("A_LGN"), [_ltd_ratio(learn)], tfr, int(c.learnData_FF))
         snaps = not minimal
         if snaps:
             flags |= N.REC_SPIKES          # the spike-word ring of the snapshots
@@ -590,6 +667,8 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
         depth = int(m.seeds.trainDepth)
         while done < m.nt:
             k = min(chunk, m.nt - done, interval - done % interval)
+            if slgn is not None:
+                k = min(k, sample_every - done % sample_every)
             sim.run(k)
             if snaps:
                 first = base + done + max(0, k - depth)
@@ -612,9 +691,15 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
             if frames is not None:
                 frames.write(sim.frames_collect(base + done, k))
             done += k
+            if slgn is not None and done % sample_every == 0:
+                slgn.write(sim.state("sLGN"))
+                if dslgn is not None:
+                    post = sim.state("ff_post")
+                    nEt = spec.nE * spec.nblock
+                    dslgn.write(post[2 * nEt:4 * nEt], post[4 * nEt:])
             if not c.minimal and (done % interval == 0 or done == m.nt):
                 last_snap = _write_snapshot(sim, c, m, history, last_snap, log)
-        for w in (raw, lsp, lfr, frames, sample):
+        for w in (raw, lsp, lfr, frames, sample, slgn, dslgn):
             if w is not None:
                 w.close()
     finally:

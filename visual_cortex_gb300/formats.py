@@ -444,6 +444,77 @@ class LgnFrWriter(LgnSpWriter):
         _w(self.f, [nt, nLGN], u32)
 
 
+class SLgnWriter:
+    """f_sLGN (learnData_FF = 1): header {nt, sampleInterval_LGN_V1 (u32), dt (f32), nV1,
+    max_LGNperV1 (u32), sRatioLGN[0..1] (f32), nLearnTypeFF_E, nLearnTypeFF_I (u32), gmaxLGN
+    [nLearnTypeFF] (f32), FF_InfRatio (f32)} (src/patch.cu:4767-4776), then the LGN->V1 weights
+    [max_LGNperV1][nV1] after every sampleInterval_LGN_V1 steps (src/patch.cu:6196-6200,
+    6937-6938)."""
+
+    def __init__(self, fn, nt, interval, dt, nV1, maxLGN, sRatioLGN2, nFF_E, nFF_I, gmaxLGN, FF_InfRatio):
+        self.f = open(fn, "wb")
+        _w(self.f, [nt, interval], u32)
+        _w(self.f, [dt], f32)
+        _w(self.f, [nV1, maxLGN], u32)
+        _w(self.f, list(sRatioLGN2)[:2], f32)
+        _w(self.f, [nFF_E, nFF_I], u32)
+        _w(self.f, list(gmaxLGN)[:nFF_E + nFF_I], f32)
+        _w(self.f, [FF_InfRatio], f32)
+
+    def write(self, sLGN):
+        self.f.write(np.ascontiguousarray(sLGN, f32).tobytes())
+
+    def close(self):
+        self.f.close()
+
+
+class DsLgnWriter:
+    """f_dsLGN (store_dsLGN with learnData_FF = 1): header {nt, sampleInterval_LGN_V1 (u32), dt
+    (f32), nV1, max_LGNperV1 (u32), sRatioLGN[0..1] (f32), nLearnTypeFF_E, nLearnTypeFF_I
+    (u32), A_LGN[nLearnTypeFF] (f32), the LTD ratio A_ratio * tauLTP of each type (f32),
+    targetFR[0..1] (f32), learnData_FF (i32)} (src/patch.cu:4795-4810), then at each sample the
+    filtered rates vAvgE [nblock*nE][2] when targetFR[0] > 0 and vAvgI [nblock*nI] when
+    targetFR[1] > 0 (src/patch.cu:6201-6208)."""
+
+    def __init__(self, fn, nt, interval, dt, nV1, maxLGN, sRatioLGN2, nFF_E, nFF_I, A_LGN, ltd_ratio, targetFR2,
+                 learnData_FF):
+        self.f = open(fn, "wb")
+        _w(self.f, [nt, interval], u32)
+        _w(self.f, [dt], f32)
+        _w(self.f, [nV1, maxLGN], u32)
+        _w(self.f, list(sRatioLGN2)[:2], f32)
+        _w(self.f, [nFF_E, nFF_I], u32)
+        _w(self.f, list(A_LGN)[:nFF_E + nFF_I], f32)
+        _w(self.f, list(ltd_ratio), f32)
+        _w(self.f, list(targetFR2)[:2], f32)
+        _w(self.f, [learnData_FF], i32)
+        self.targetFR = list(targetFR2)[:2]
+
+    def write(self, avgE, avgI):
+        if self.targetFR[0] > 0:
+            self.f.write(np.ascontiguousarray(avgE, f32).tobytes())
+        if self.targetFR[1] > 0:
+            self.f.write(np.ascontiguousarray(avgI, f32).tobytes())
+
+    def close(self):
+        self.f.close()
+
+
+def read_slgn(fn, nFF: int = 1):
+    """Header dict and the sampled weights [samples][max_LGNperV1][nV1] of an sLGN file."""
+    with open(fn, "rb") as f:
+        nt, interval = (_r1(f, u32) for _ in range(2))
+        dt = float(_r1(f, f32))
+        nV1, maxLGN = (_r1(f, u32) for _ in range(2))
+        sr = _r(f, f32, 2)
+        nE, nI = (_r1(f, u32) for _ in range(2))
+        gmax = _r(f, f32, nE + nI)
+        inf = float(_r1(f, f32))
+        d = np.frombuffer(f.read(), f32)
+    return (dict(nt=nt, interval=interval, dt=dt, nV1=nV1, maxLGN=maxLGN, sRatioLGN=sr, nLearnTypeFF_E=nE,
+                 nLearnTypeFF_I=nI, gmaxLGN=gmax, FF_InfRatio=inf), d.reshape(-1, maxLGN, nV1))
+
+
 def read_lgn_sp(fn):
     with open(fn, "rb") as f:
         dt = float(_r1(f, f32))
@@ -515,7 +586,7 @@ SNAPSHOT_INDICES = ("step", "frameCycle", "iFrameHead", "oldFrameHead", "current
 
 
 def write_reference_snapshot(fn, idx: dict, iModel: int, learning: int, sizes: dict, lgn: dict, v1: dict,
-                             spike_train, state: dict, trailer: bytes | None = None):
+                             spike_train, state: dict, trailer: bytes | None = None, learn: dict | None = None):
     """A snapshot in the reference's layout (src/patch.cu:6793-6912): 11 u32 indices (steps
     done, frame bookkeeping, iStatus, the next spike-word slot), iModel and learning (i32),
     nV1 nLGN ngFF ngE ngI nType trainDepth (u32); the LGN block (leftTimeRate, lastNegLogRand,
@@ -530,6 +601,12 @@ def write_reference_snapshot(fn, idx: dict, iModel: int, learning: int, sizes: d
         _w(f, lgn["ltr"], f32)
         _w(f, lgn["lnl"], f32)
         f.write(np.ascontiguousarray(lgn["rng"], np.uint8).tobytes())
+        if learning:
+            # the LGN->V1 weights, the post learning variables and the presynaptic traces
+            # (src/patch.cu:6844-6850)
+            _w(f, np.ravel(learn["sLGN"]), f32)
+            _w(f, np.ravel(learn["ff_post"]), f32)
+            _w(f, np.ravel(learn["ff_pre"]), f32)
         f.write(np.ascontiguousarray(v1["rng_cond"], np.uint8).tobytes())
         f.write(np.ascontiguousarray(v1["rng_noisy"], np.uint8).tobytes())
         _w(f, v1["tBack"], f32)
@@ -541,9 +618,12 @@ def write_reference_snapshot(fn, idx: dict, iModel: int, learning: int, sizes: d
             f.write(trailer)
 
 
-def read_reference_snapshot(fn, nI_total: int):
+def read_reference_snapshot(fn, nI_total: int, maxLGN: int = 0, nE_total: int = 0, nFF: int = 1):
     """Reads a snapshot written by the reference (or by write_reference_snapshot); returns the
-    fields and the bytes that follow them (this build's checkpoint, if it wrote the file)."""
+    fields and the bytes that follow them (this build's checkpoint, if it wrote the file).  A
+    snapshot of a learning run also holds the LGN->V1 weights [maxLGN][nV1], the post learning
+    variables (learnVar's FF block, 4 nE_total + nI_total floats for one FF_E type) and the
+    presynaptic traces [nFF][nLGN]."""
     data = open(fn, "rb").read()
     off = 0
 
@@ -557,9 +637,15 @@ def read_reference_snapshot(fn, nI_total: int):
     iModel, learning = (int(x) for x in take(i32, 2))
     sizes = dict(zip(("nV1", "nLGN", "ngFF", "ngE", "ngI", "nType", "trainDepth"), (int(x) for x in take(u32, 7))))
     n, nl = sizes["nV1"], sizes["nLGN"]
-    if learning:
-        raise ValueError(f"{fn}: a snapshot of a run with learning = {learning} (plasticity) is not read")
+    if learning and learning != 3:
+        raise ValueError(f"{fn}: a snapshot of a run with learning = {learning} is not read (learning = 3 only)")
     lgn = dict(ltr=take(f32, nl), lnl=take(f32, nl), rng=take(np.uint8, 48 * nl))
+    learn = None
+    if learning:
+        if not maxLGN:
+            raise ValueError(f"{fn}: a snapshot of a learning run needs max_LGNperV1 to be read")
+        learn = dict(sLGN=take(f32, maxLGN * n), ff_post=take(f32, 4 * nE_total + nI_total),
+                     ff_pre=take(f32, nFF * nl))
     v1 = dict(rng_cond=take(np.uint8, 48 * n), rng_noisy=take(np.uint8, 48 * n), tBack=take(f32, n))
     spike_train = take(f32, sizes["trainDepth"] * n).reshape(sizes["trainDepth"], n)
     state = dict(dep=take(f32, n))
@@ -571,4 +657,4 @@ def read_reference_snapshot(fn, nI_total: int):
         state[k] = take(f32, c * n)
     state["gap"] = take(f32, nI_total)
     return dict(idx=idx, iModel=iModel, learning=learning, sizes=sizes, lgn=lgn, v1=v1,
-                spike_train=spike_train, state=state), data[off:]
+                spike_train=spike_train, state=state, learn=learn), data[off:]

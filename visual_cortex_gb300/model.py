@@ -272,6 +272,28 @@ class InitState:
 
 
 @dataclass
+class FFLearning:
+    """LGN->V1 plasticity parameters as the reference's cfg gives them (learning = 3: one
+    LGN->E triplet-rule type; element [0] of the cfg arrays, gmax/gmin before sRatioLGN)."""
+    tauLTP: float
+    tauLTD: float
+    tauTrip: float
+    tauAvg: float
+    targetFR: float
+    A_LGN: float
+    r_LTD: float
+    gmaxLGN: float
+    gminLGN: float
+    sRatioLGN: float
+    decayTimeHomeoFF: float = 250.0
+    FF_InfRatio: float = 1.0
+    applyHomeo: int = 0
+    symmetricHomeo: bool = True
+    rebound: bool = False
+    learning: int = 3
+
+
+@dataclass
 class Seeds:
     lgn: int          # logRand_init seed
     cond: int         # rand_spInit seed
@@ -404,6 +426,17 @@ class Simulation:
         self.step += (int(nsteps) // k.value) * k.value
         return float(v1.value), float(lgn.value), int(k.value)
 
+    def set_ff_learning(self, learning: "FFLearning"):
+        """LGN->V1 plasticity (learning = 3) with the cfg values of `learning` (pv1_set_ff_learning)."""
+        c = N.FFLearning(learning=int(learning.learning), tauLTP=learning.tauLTP, tauLTD=learning.tauLTD,
+                         tauTrip=learning.tauTrip, tauAvg=learning.tauAvg, targetFR=learning.targetFR,
+                         A_LGN=learning.A_LGN, r_LTD=learning.r_LTD, gmaxLGN=learning.gmaxLGN,
+                         gminLGN=learning.gminLGN, sRatioLGN=learning.sRatioLGN,
+                         decayTimeHomeoFF=learning.decayTimeHomeoFF, FF_InfRatio=learning.FF_InfRatio,
+                         applyHomeo=int(learning.applyHomeo), symmetricHomeo=int(learning.symmetricHomeo),
+                         rebound=int(learning.rebound))
+        N.check(self.plan, N.lib.pv1_set_ff_learning(self.plan, C.byref(c)), "pv1_set_ff_learning")
+
     def persistent(self, allow: int = -1) -> bool:
         """Queries (allow=-1) or sets whether V1 steps run as one cooperative launch per
         chunk of steps."""
@@ -450,7 +483,10 @@ class Simulation:
         sizes = dict(gFF=spec.ngFF * n, hFF=spec.ngFF * n, gE=spec.ngE * n, hE=spec.ngE * n,
                      gI=spec.ngI * n, hI=spec.ngI * n, lgn_ltr=self.lgn.nLGN, lgn_lnl=self.lgn.nLGN,
                      lgn_sInfo=self.lgn.nLGN, farPull=(spec.ngE + spec.ngI) * 2 * n,
-                     lgn_rng=12 * self.lgn.nLGN, v1_rng_cond=12 * n, v1_rng_noisy=12 * n)
+                     lgn_rng=12 * self.lgn.nLGN, v1_rng_cond=12 * n, v1_rng_noisy=12 * n,
+                     sLGN=self.net.maxLGN * n,
+                     ff_post=4 * spec.nE * spec.nblock + (spec.blockSize - spec.nE) * spec.nblock,
+                     ff_pre=self.lgn.nLGN, total_ff=2 * n)
         out = np.empty(sizes.get(name, n), f32)
         N.check(self.plan, N.lib.pv1_get_state(self.plan, N.ST[name], N.fptr(out)), f"pv1_get_state({name})")
         if name.endswith("_rng") or name.startswith("v1_rng"):

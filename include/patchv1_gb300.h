@@ -373,6 +373,11 @@ typedef struct pv1_ff_learning {
     int32_t symmetricHomeo, rebound;
 } pv1_ff_learning;
 int pv1_set_ff_learning(pv1_plan *plan, const pv1_ff_learning *cfg);
+/* The derived constants pv1_set_ff_learning uses, for a step dt (host only, no device work):
+ * out[0] A_LTP = A_LGN * sRatioLGN, out[1] A_ratio (the LTD rate; with targetFR > 0 scaled by
+ * tauTrip / (tauLTD tauAvg_s^2) / 1000 / targetFR), out[2] gmax and out[3] gmin scaled by
+ * sRatioLGN, out[4] exp_homeo -- learnFF_post (src/condShape.h:137-152) and src/patch.cu:1330. */
+int pv1_ff_learning_rates(const pv1_ff_learning *cfg, float dt, float *out5);
 
 /* Learning state (plans with learning): the LGN->V1 weights [maxLGN][nV1] (the reference's
  * LGN_V1_s, synapse-major), the post variables in the reference's learnVar layout

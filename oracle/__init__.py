@@ -58,6 +58,7 @@ def lib():
         L.orc_lgn_ff_pre.argtypes = [C.c_int, C.c_float, C.c_float, UP, FP, FP, FP, FP, FP]
         L.orc_v1_set_ff_learning.argtypes = [P, P]
         L.orc_v1_learn_ff.argtypes = [P, FP, FP, FP]
+        L.orc_ff_learning_rates.argtypes = [P, C.c_float, FP]
         L.orc_parvo_max_sample1d.argtypes = [P, P, C.c_int]
         L.orc_lgn_parvo_setup.argtypes = [P, P, P, FP, FP, FP, FP, FP]
         L.orc_lgn_parvo_spatial.argtypes = [C.c_int, C.c_int, FP, FP, UP, FP, C.c_int, C.c_int, C.c_int,

@@ -1699,8 +1699,7 @@ int orc_v1_init_spikes(orc_v1 *o, const float *sp0, uint32_t SCsplit, int depth,
  * (src/condShape.h:137-152; Float = float with its double literals), exp_homeo =
  * exp(-dt/decayTimeHomeoFF) (src/patch.cu:1330), the homeostasis totals from the current
  * weights (src/patch.cu:4335-4352).  Returns -1 for other learning modes. */
-int orc_v1_set_ff_learning(orc_v1 *o, const pv1_ff_learning *l) {
-    if (l->learning != 3) return -1;
+void orc_ff_learning_rates(const pv1_ff_learning *l, float dt, float *out) {
     const float ALTP = l->A_LGN * l->sRatioLGN;
     const float tas = (float)((double)l->tauAvg / 1000.0);
     float Ar = l->r_LTD * ALTP;
@@ -1708,11 +1707,22 @@ int orc_v1_set_ff_learning(orc_v1 *o, const pv1_ff_learning *l) {
         const float q = l->tauTrip / (l->tauLTD * (tas * tas));
         Ar = (float)((double)Ar * ((double)q / 1000.0 / (double)l->targetFR));
     }
+    out[0] = ALTP;
+    out[1] = Ar;
+    out[2] = l->gmaxLGN * l->sRatioLGN;
+    out[3] = l->gminLGN * l->sRatioLGN;
+    out[4] = expf(-dt / l->decayTimeHomeoFF);
+}
+
+int orc_v1_set_ff_learning(orc_v1 *o, const pv1_ff_learning *l) {
+    if (l->learning != 3) return -1;
+    float r[5];
+    orc_ff_learning_rates(l, o->c.dt, r);
     o->learn = 1;
     o->lTauLTP = l->tauLTP; o->lTauLTD = l->tauLTD; o->lTauTrip = l->tauTrip; o->lTauAvg = l->tauAvg;
-    o->lTargetFR = l->targetFR; o->lA_LTP = ALTP; o->lA_ratio = Ar;
-    o->lGmax = l->gmaxLGN * l->sRatioLGN; o->lGmin = l->gminLGN * l->sRatioLGN;
-    o->lExpHomeo = expf(-o->c.dt / l->decayTimeHomeoFF);
+    o->lTargetFR = l->targetFR; o->lA_LTP = r[0]; o->lA_ratio = r[1];
+    o->lGmax = r[2]; o->lGmin = r[3];
+    o->lExpHomeo = r[4];
     o->applyHomeo = l->applyHomeo; o->symmetricHomeo = l->symmetricHomeo != 0; o->rebound = l->rebound != 0;
     const size_t n = (size_t)o->nV1;
     free(o->ffPost);

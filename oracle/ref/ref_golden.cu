@@ -10,6 +10,8 @@
 //   ref_golden far      in out   fill_fSpikeTrain (src/stats.cu:114-126) + recal_G_vec
 //                                (src/coredynamics.cu:181-372) over a spike sequence
 //   ref_golden farfail  in out   the same with synaptic failure (host engines) per chunk
+//   ref_golden learnff  in out   learnFF_pre/learnFF_post (src/condShape.h:94-152) and
+//                                exp_homeo (src/patch.cu:1330): LGN->V1 learning constants
 // Inputs and outputs are raw little-endian arrays; tests/golden/make_golden.py writes and
 // reads them.  The AdEx struct is declared __device__ in the reference; the redefinition
 // below makes its members host-callable without changing their arithmetic.
@@ -206,9 +208,36 @@ static int mode_far(const char *in, const char *out, bool failure) {
     return 0;
 }
 
+// learnFF_pre / learnFF_post (src/condShape.h:94-152) and exp_homeo (src/patch.cu:1330) for
+// rows {tauLTP, tauLTD, tauTrip, tauAvg, targetFR, A_LGN, r_LTD, gmaxLGN, gminLGN, sRatioLGN,
+// dt, decayTimeHomeoFF}; per row the bytes of LearnVarShapeFF_E_pre, of LearnVarShapeFF_E_post
+// and of exp_homeo.
+static int mode_learnff(const char *in, const char *out) {
+    auto x = read_all<float>(in);
+    std::vector<unsigned char> y;
+    for (size_t r = 0; r + 12 <= x.size(); r += 12) {
+        const float *q = &x[r];
+        Float tauLTP[1] = {q[0]}, tauLTD[1] = {q[1]}, tauTrip[1] = {q[2]}, A[1] = {q[5]}, rLTD[1] = {q[6]};
+        LearnVarShapeFF_E_pre pre = {};
+        LearnVarShapeFF_E_post post = {};
+        learnFF_pre<LearnVarShapeFF_E_pre>(pre, tauLTP, 1);
+        learnFF_post<LearnVarShapeFF_E_post>(post, tauLTD, tauTrip, rLTD, q[3], q[4], A, q[7], q[8], 1, q[9]);
+        const Float dt = q[10], hdFF = q[11];
+        const Float expHomeo = exponential(-dt / hdFF);
+        const unsigned char *a = reinterpret_cast<const unsigned char *>(&pre);
+        const unsigned char *b = reinterpret_cast<const unsigned char *>(&post);
+        const unsigned char *c = reinterpret_cast<const unsigned char *>(&expHomeo);
+        y.insert(y.end(), a, a + sizeof(pre));
+        y.insert(y.end(), b, b + sizeof(post));
+        y.insert(y.end(), c, c + sizeof(expHomeo));
+    }
+    write_all(out, y);
+    return 0;
+}
+
 int main(int argc, char **argv) {
     if (argc != 4) {
-        fprintf(stderr, "usage: ref_golden cond|adex|logistic|denorm|far|farfail in out\n");
+        fprintf(stderr, "usage: ref_golden cond|adex|logistic|denorm|far|farfail|learnff in out\n");
         return 2;
     }
     if (!strcmp(argv[1], "cond")) return mode_cond(argv[2], argv[3]);
@@ -217,5 +246,6 @@ int main(int argc, char **argv) {
     if (!strcmp(argv[1], "denorm")) return mode_denorm(argv[2], argv[3]);
     if (!strcmp(argv[1], "far")) return mode_far(argv[2], argv[3], false);
     if (!strcmp(argv[1], "farfail")) return mode_far(argv[2], argv[3], true);
+    if (!strcmp(argv[1], "learnff")) return mode_learnff(argv[2], argv[3]);
     return 2;
 }

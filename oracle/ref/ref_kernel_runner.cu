@@ -164,7 +164,7 @@ struct Launch {
     size_t idx = 0;
     const char *name;
     explicit Launch(const char *kname) : f(find_kernel(kname)), name(kname) {}
-    void raw(const void *p, size_t n) {
+    Launch &raw(const void *p, size_t n) {
         size_t off = 0, sz = 0;
         if (cuFuncGetParamInfo(f, idx, &off, &sz) != CUDA_SUCCESS) {
             fprintf(stderr, "%s: more arguments than parameters (%zu)\n", name, idx);
@@ -177,6 +177,7 @@ struct Launch {
         if (buf.size() < off + sz) buf.resize(off + sz, 0);
         memcpy(&buf[off], p, n);
         idx++;
+        return *this;
     }
     template <class T>
     Launch &a(const T &v) {
@@ -322,6 +323,68 @@ static void mode_lgn(const Bundle &in, Writer &out) {
     out.putv("lnl", "f4", host(lnl, n));
     out.putv("ltr", "f4", host(ltr, n));
     out.putv("state", "u1", host(reinterpret_cast<u8 *>(st), n * kState));
+}
+
+// ---- lgnlearn: logRand_init + K steps of LGN_nonlinear with learning = 3 ----
+// One FF_E learning type: the surface holds the spike words (layer 0) and the presynaptic
+// trace in three slots (layers 1-3: the start of the step by varSlot = k % 2, the next slot,
+// and the value right after the step's spikes).  Per step: the trace at the end of the step
+// (lVar, learnData_FF on) and layer 3 at each cell.
+struct LearnPre {     // LearnVarShapeFF_E_pre / _I_pre with one type (src/condShape.h:85-92)
+    unsigned n;
+    float tauLTP[1];
+};
+static void mode_lgnlearn(const Bundle &in, Writer &out) {
+    const unsigned n = scalar<unsigned>(in, "n"), K = scalar<unsigned>(in, "K");
+    const unsigned nsx = scalar<unsigned>(in, "nsx"), nsy = scalar<unsigned>(in, "nsy");
+    const uint64_t seed = scalar<uint64_t>(in, "seed");
+    auto sx = get<int>(in, "sx"), sy = get<int>(in, "sy");
+    auto convol = get<float>(in, "convol");
+    Surface surf(nsx, nsy, 4);
+    float *lnl = dev<float>(n), *ltr = dev<float>(n);
+    int *dsx = dev_from(sx), *dsy = dev_from(sy);
+    curandStateMRG32k3a *st = dev<curandStateMRG32k3a>(n);
+    {
+        Launch L("logRand_init");
+        L.a(lnl).a(ltr).a(dsx).a(dsy).a(st).a(surf.obj).a((unsigned long)seed).a(n).a((unsigned)0);
+        L.go((n + 1023) / 1024, 1, 1024, 1);
+    }
+    auto c50 = get<float>(in, "c50"), sh = get<float>(in, "sharpness"), la = get<float>(in, "a"), lb = get<float>(in, "b");
+    std::vector<float> blk;
+    for (auto *v : {&c50, &sh, &la, &lb}) blk.insert(blk.end(), v->begin(), v->end());
+    float *dblk = dev_from(blk);
+    std::vector<float *> logi = {dblk, dblk, dblk + n, dblk + 2 * n, dblk + 3 * n};
+    float **dlogi = dev_from(logi);
+    float *maxc = dev_from(get<float>(in, "max_convol"));
+    float *cur = dev<float>(n), *fr = dev<float>(n), *sinfo = dev<float>(n);
+    float *switchv = dev<float>(n), *lvar = dev<float>(4 * n);
+    int *ltype = dev<int>(n);
+    const float convolRatio = scalar<float>(in, "convolRatio"), frRatio = scalar<float>(in, "frRatio");
+    const float dt = scalar<float>(in, "dt");
+    LearnPre lE{1u, {scalar<float>(in, "tauLTP")}}, lI{0u, {0.f}};
+    std::vector<float> all_si, all_var, all_spk, all_start;
+    for (unsigned k = 0; k < K; k++) {
+        CK(cudaMemcpy(cur, convol.data() + (size_t)k * n, n * sizeof(float), cudaMemcpyHostToDevice));
+        Launch L("LGN_nonlinear");
+        L.a(n).a(dlogi).a(maxc).a(cur).a(convolRatio).a(fr).a(sinfo).a(dsx).a(dsy).a(ltr).a(lnl).a(st);
+        L.a(ltype).a(switchv).zero().a(lvar).a(surf.obj).a(frRatio).a((int)(k % 2)).a(lE).a(lI).a((unsigned)1).a(dt);
+        L.a((int)3).a(true).a(false).a(true).a(false).a((int)0);
+        L.go((n + 1023) / 1024, 1, 1024, 1);
+        auto b = host(sinfo, n), v = host(lvar, n);
+        all_si.insert(all_si.end(), b.begin(), b.end());
+        all_var.insert(all_var.end(), v.begin(), v.end());
+        auto s = surf.copy_out();
+        const size_t plane = (size_t)nsx * nsy;
+        for (unsigned i = 0; i < n; i++) {
+            const size_t at = (size_t)sy[i] * nsx + sx[i];
+            all_spk.push_back(s[3 * plane + at]);
+            all_start.push_back(s[(1 + k % 2) * plane + at]);
+        }
+    }
+    out.putv("sInfo", "f4", all_si);
+    out.putv("ffvar", "f4", all_var);
+    out.putv("ffspk", "f4", all_spk);
+    out.putv("ffstart", "f4", all_start);
 }
 
 // ---- V1: the shared network description ----
@@ -543,6 +606,100 @@ static void mode_v1run(const Bundle &in, Writer &out) {
     out.putv("rGenCond", "u1", host(reinterpret_cast<u8 *>(m.rGenCond), n * kState));
 }
 
+// ---- v1learn: rand_spInit, then T steps of compute_V_collect_spike_learnFF_fast with
+// learning = 3 + recal_G_mat_nd_fast, the presynaptic traces given per step (surface layer
+// 1 + varSlot: the step start, layer 3: right after the LGN spikes); the learning structs
+// come as bytes ("lFF_E_pre", "lFF_E_post", in the reference's layout) ----
+static void mode_v1learn(const Bundle &in, Writer &out) {
+    V1 m = make_v1(in);
+    const size_t n = m.nV1;
+    rand_sp_init(m, in);
+    const unsigned T = scalar<unsigned>(in, "T");
+    const unsigned nLGNcells = scalar<unsigned>(in, "nLGNcells");
+    const unsigned nsx = scalar<unsigned>(in, "nsx"), nsy = scalar<unsigned>(in, "nsy");
+    auto cx = get<int>(in, "cell_x"), cy = get<int>(in, "cell_y");
+    auto lgnRows = get<float>(in, "lgnSInfo");   // [T][nLGNcells]
+    auto preStart = get<float>(in, "preStart");  // [T][nLGNcells]
+    auto preSpk = get<float>(in, "preSpk");      // [T][nLGNcells]
+    auto ePre = get<u8>(in, "lFF_E_pre"), ePost = get<u8>(in, "lFF_E_post");
+    const float expHomeo = scalar<float>(in, "expHomeo");
+    const int applyHomeo = scalar<int>(in, "applyHomeo");
+    const bool symmetricHomeo = scalar<int>(in, "symmetricHomeo") != 0, rebound = scalar<int>(in, "rebound") != 0;
+    Surface surf(nsx, nsy, 4);
+    m.nnb = scalar<unsigned>(in, "nnb");
+    m.conMat = dev_from(get<float>(in, "conMat"));
+    m.gapMat = dev<float>(16);
+    m.nNB = dev_from(get<unsigned>(in, "nNearNB"));
+    m.nbId = dev_from(get<unsigned>(in, "nbId"));
+    const int iModel = scalar<int>(in, "iModel");
+    const unsigned nTypeE = scalar<unsigned>(in, "nTypeE");
+    const size_t nEt = (size_t)m.nE * m.nblock, nIt = (size_t)m.nI * m.nblock;
+    float *vLTD = dev<float>(nEt), *vTrip = dev<float>(nEt), *vAvgE = dev<float>(2 * nEt), *vAvgI = dev<float>(nIt + 1);
+    float *none = dev<float>(64);
+    auto tot = get<float>(in, "totalFF");        // [2][nV1]
+    CK(cudaMemcpy(m.totalFF, tot.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(m.totalFF_inf, tot.data() + n, n * sizeof(float), cudaMemcpyHostToDevice));
+    std::vector<unsigned char> zE(60, 0), zQ(28, 0), zIpost(36, 0), zIpre(8, 0);
+    std::vector<float> raster;
+    const size_t plane = (size_t)nsx * nsy;
+    std::vector<float> layers(4 * plane, 0.f);
+    for (unsigned it = 0; it < T; it++) {
+        const unsigned varSlot = it % 2;
+        for (unsigned c = 0; c < nLGNcells; c++) {
+            const size_t at = (size_t)cy[c] * nsx + cx[c], q = (size_t)it * nLGNcells + c;
+            layers[at] = lgnRows[q];
+            layers[(1 + varSlot) * plane + at] = preStart[q];
+            layers[3 * plane + at] = preSpk[q];
+        }
+        surf.copy_in(layers);
+        const unsigned slot = it % m.trainDepth;
+        {
+            Launch L("compute_V_collect_spike_learnFF_fast");
+            L.a(m.v).a(m.dep).a(m.w).a(m.gapS).a(m.gFF).a(m.hFF).a(m.ddgE).a(m.ddgI).a(m.ddhE).a(m.ddhI).a(m.ddgap);
+            L.a(m.nLGN).a(m.sLGN).a(m.lgnx).a(m.lgny).a(m.tBack).a(m.spikeTrain);
+            L.a(vLTD).a(vTrip).a(none).a(none).a(vAvgE).a(vAvgI).a(none).a(none).a(none).a(none).a(none);
+            L.a(m.pFF).a(m.vR).a(m.vThres).a(m.gL).a(m.C).a(m.tRef).a(m.tonic).a(m.vT).a(m.deltaT).a(m.tau_w);
+            L.a(m.a).a(m.b).a(m.dTypeAcc).a(m.rGenCond).a(m.synFailFF).a(m.synPerConFF).a(m.rNoisy).a(m.noisyDep);
+            L.a(m.last_noise).a(m.ipre).a(m.npre).a(m.og).a(m.oh).a(m.totalFF).a(m.totalFF_inf);
+            L.a(0.0f).a(slot).a(m.trainDepth).a(m.maxLGN).a(m.ngFF).a(m.ngE).a(m.ngI);
+            L.raw(m.condFF.data(), m.condFF.size());
+            L.raw(m.condE.data(), m.condE.size());
+            L.raw(m.condI.data(), m.condI.size());
+            L.a(m.dt).a(m.nblock).a(m.nblock).a((unsigned)1).a((unsigned)1).a(m.nE).a(m.nI).a(m.nV1);
+            L.a((int)3).a((int)varSlot).a(m.nType).a(surf.obj);
+            L.raw(ePre.data(), ePre.size()).raw(zIpre.data(), zIpre.size());
+            L.raw(ePost.data(), ePost.size()).raw(zIpost.data(), zIpost.size());
+            L.raw(zE.data(), zE.size()).raw(zQ.data(), zQ.size());
+            L.a(expHomeo).a(iModel).a((int)1).a(applyHomeo).a(symmetricHomeo).a(false).a(rebound);
+            L.a(scalar<int>(in, "noiseOnTonic") != 0);
+            L.go(m.nblock, 1, m.bs, 1);
+        }
+        {
+            const unsigned shmem = m.nnb * 2 * 4 + std::max(m.nE, m.nI) * 4 +
+                                   std::max(m.nE * m.ngE, m.nI * m.ngI) * 2 * 4;
+            Launch L("recal_G_mat_nd_fast");
+            L.a(m.spikeTrain + (size_t)m.nV1 * slot).a(m.ipre).a(m.npre).a(m.og).a(m.oh).a(m.conMat).a(m.gapMat);
+            L.a(m.nNB).a(m.nbId).a(m.gE).a(m.gI).a(m.hE).a(m.hI).a(m.gap);
+            L.a(vAvgE).a(none).a(none).a(none).a(none).a(none);
+            L.a(m.pE).a(m.pI).a(m.dTypeAcc).a(m.rGenCond).a(m.synFail).a(m.synPerCon).a(m.vThres);
+            L.a(m.dt);
+            L.raw(m.condE.data(), m.condE.size());
+            L.raw(m.condI.data(), m.condI.size());
+            L.a(m.ngE).a(m.ngI).a(m.nnb).a(m.nE).a(m.nI).a(m.nV1).a((int)3).a((unsigned)0).a(m.nType);
+            L.a(nTypeE).a(m.nType - nTypeE).a(m.nblock).zero().zero().a((unsigned)0).a(it).a(false);
+            L.go(m.nblock, 1, m.bs, 1, shmem);
+        }
+        auto row = host(m.spikeTrain + (size_t)m.nV1 * slot, n);
+        raster.insert(raster.end(), row.begin(), row.end());
+    }
+    out.putv("raster", "f4", raster);
+    out.putv("sLGN", "f4", host(m.sLGN, (size_t)m.maxLGN * n));
+    out.putv("vLTD", "f4", host(vLTD, nEt));
+    out.putv("vTrip", "f4", host(vTrip, nEt));
+    out.putv("vAvgE", "f4", host(vAvgE, 2 * nEt));
+    out.putv("totalFF", "f4", host(m.totalFF, n));
+}
+
 // ---- magno: store_PM (PM = 1) once, then T steps of LGN_convol_magno ----
 // Stimulus textures as src/patch.h:95-109 sets them up: one layered float array per cone
 // channel with maxFrame layers, border addressing, linear filtering, normalised coordinates;
@@ -654,7 +811,7 @@ static void mode_magno(const Bundle &in, Writer &out) {
 
 int main(int argc, char **argv) {
     if (argc != 5) {
-        fprintf(stderr, "usage: %s <ref_kernels.cubin> <lgn|v1init|v1run|magno> <in.bundle> <out.bundle>\n", argv[0]);
+        fprintf(stderr, "usage: %s <ref_kernels.cubin> <lgn|lgnlearn|v1init|v1run|v1learn|magno> <in.bundle> <out.bundle>\n", argv[0]);
         return 1;
     }
     CK(cudaFree(0));  // primary context current for the driver API too
@@ -670,6 +827,10 @@ int main(int argc, char **argv) {
         mode_v1run(in, out);
     else if (mode == "magno")
         mode_magno(in, out);
+    else if (mode == "lgnlearn")
+        mode_lgnlearn(in, out);
+    else if (mode == "v1learn")
+        mode_v1learn(in, out);
     else {
         fprintf(stderr, "unknown mode %s\n", mode.c_str());
         return 1;

@@ -178,3 +178,86 @@ def magno_inputs(wl) -> dict:
                 kernelSampleInterval=scalar(s.mKernelSampleInterval, u32),
                 iKernelSampleT0=scalar(s.mKernelSampleT0, u32), dt=scalar(s.dt, f32),
                 T=scalar(MAGNO_T, u32), stride=scalar(MAGNO_STRIDE, u32))
+
+
+# ---- LGN->V1 plasticity (learning = 3) ---------------------------------------------------
+LEARN_T = 120
+
+
+def learning_params():
+    """The FFLearning of the pinned learning cases (multiplicative homeostasis, targetFR > 0)."""
+    from visual_cortex_gb300.model import FFLearning
+    return FFLearning(tauLTP=16.8, tauLTD=33.7, tauTrip=114.0, tauAvg=1000.0, targetFR=2.0, A_LGN=0.02,
+                      r_LTD=1.0, gmaxLGN=0.6, gminLGN=0.0, sRatioLGN=1.0, decayTimeHomeoFF=250.0,
+                      FF_InfRatio=0.9, applyHomeo=1)
+
+
+def learning_structs(L, dt: float):
+    """The bytes of LearnVarShapeFF_E_pre and LearnVarShapeFF_E_post (src/condShape.h:85-126)
+    for one FF_E type, with the derived constants of pv1_ff_learning_rates (held bit for bit
+    to learnFF_post by tests/test_golden.py), and exp_homeo."""
+    import ctypes as C
+    from visual_cortex_gb300 import _native as N
+    cfg = N.FFLearning(learning=3, tauLTP=L.tauLTP, tauLTD=L.tauLTD, tauTrip=L.tauTrip, tauAvg=L.tauAvg,
+                       targetFR=L.targetFR, A_LGN=L.A_LGN, r_LTD=L.r_LTD, gmaxLGN=L.gmaxLGN, gminLGN=L.gminLGN,
+                       sRatioLGN=L.sRatioLGN, decayTimeHomeoFF=L.decayTimeHomeoFF, FF_InfRatio=L.FF_InfRatio,
+                       applyHomeo=int(L.applyHomeo), symmetricHomeo=int(L.symmetricHomeo), rebound=int(L.rebound))
+    r = np.zeros(5, f32)
+    assert N.lib.pv1_ff_learning_rates(C.byref(cfg), f32(dt), N.fptr(r)) == 0
+    pre = np.array([1], u32).tobytes() + np.array([L.tauLTP], f32).tobytes()
+    post = np.array([1], u32).tobytes() + np.array([L.tauLTD, L.tauTrip, L.tauAvg, r[0], r[1], L.targetFR, r[2], r[3]],
+                                                   f32).tobytes()
+    return np.frombuffer(pre, u8).copy(), np.frombuffer(post, u8).copy(), f32(r[4])
+
+
+def lgn_learn_case() -> dict:
+    """The LGN case above with the presynaptic trace of one FF_E type (tauLTP of
+    learning_params())."""
+    d = lgn_case()
+    d["tauLTP"] = scalar(learning_params().tauLTP, f32)
+    return d
+
+
+def pre_traces(lgn_rows, dt: float, tauLTP: float):
+    """Presynaptic traces for given LGN spike words (the oracle's trace step, nsp and tsp taken
+    from the words): ([T][n] at the step start, [T][n] right after the step's spikes)."""
+    import oracle
+    T, n = lgn_rows.shape
+    var = np.zeros(n, f32)
+    start = np.zeros((T, n), f32)
+    spk = np.zeros((T, n), f32)
+    for t in range(T):
+        s = np.ascontiguousarray(lgn_rows[t], f32)
+        nsp = np.floor(s).clip(0).astype(u32)
+        tsp = np.where(s > 0, (s - nsp.astype(f32)) * f32(dt), 0).astype(f32)
+        a, b = np.zeros(n, f32), np.zeros(n, f32)
+        oracle.lib().orc_lgn_ff_pre(n, f32(dt), f32(tauLTP), oracle.up(nsp), oracle.fp(tsp), oracle.fp(s),
+                                    oracle.fp(var), oracle.fp(a), oracle.fp(b))
+        start[t], spk[t] = a, b
+    return start, spk
+
+
+def learning_totals(net):
+    """The homeostasis totals of src/patch.cu:4335-4352: each neuron's LGN weights summed in
+    synapse order (float), and that times FF_InfRatio."""
+    n = net.sLGN.shape[1]
+    tot = np.zeros(2 * n, f32)
+    L = learning_params()
+    for i in range(n):
+        t = f32(0)
+        for j in range(int(net.nLGNperV1[i])):
+            t = f32(t + net.sLGN[j, i])
+        tot[i] = t
+        tot[n + i] = f32(t * f32(L.FF_InfRatio))
+    return tot
+
+
+def v1_learn_inputs(wl, lgn_rows, T: int) -> dict:
+    L = learning_params()
+    d = v1_inputs(wl, lgn_rows=lgn_rows, T=T)
+    pre, post, eh = learning_structs(L, wl.spec.dt)
+    start, spk = pre_traces(np.asarray(lgn_rows[:T], f32), wl.spec.dt, L.tauLTP)
+    d.update(lFF_E_pre=pre, lFF_E_post=post, expHomeo=scalar(eh, f32), applyHomeo=scalar(int(L.applyHomeo), i32),
+             symmetricHomeo=scalar(int(L.symmetricHomeo), i32), rebound=scalar(int(L.rebound), i32),
+             preStart=start.reshape(-1), preSpk=spk.reshape(-1), totalFF=learning_totals(wl.net))
+    return d

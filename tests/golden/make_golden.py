@@ -2,7 +2,7 @@
 
 The outputs come from oracle/_ref/ref_golden, built by oracle/ref/build_ref.sh from the
 reference's sources (ConductanceShape, the AdEx struct, hStatic_nonlinear, find_denorm,
-fill_fSpikeTrain + recal_G_vec, with and without synaptic failure).  Run from the repository root, where the reference's
+fill_fSpikeTrain + recal_G_vec, with and without synaptic failure, learnFF_pre/learnFF_post).  Run from the repository root, where the reference's
 sources are readable:
   REFERENCE_SRC=<reference checkout>/src bash oracle/ref/build_ref.sh && python tests/golden/make_golden.py
 """
@@ -107,6 +107,17 @@ def main():
     out["farfail_nVec"], out["farfail_vecID"] = nVec, vecID
     out["farfail_conVec"], out["farfail_delayVec"], out["farfail_sInfo"] = conVec, delayVec, sInfo
     out["farfail_out"] = res.reshape(T, (ngE + ngI) * 2, nV1)
+    # LGN->V1 learning constants: learnFF_pre/learnFF_post and exp_homeo for parameter rows
+    # {tauLTP, tauLTD, tauTrip, tauAvg, targetFR, A_LGN, r_LTD, gmaxLGN, gminLGN, sRatioLGN, dt,
+    # decayTimeHomeoFF}
+    m = 64
+    lf = np.stack([rng.uniform(5, 40, m), rng.uniform(10, 60, m), rng.uniform(50, 200, m),
+                   rng.uniform(200, 3000, m), np.where(rng.random(m) < 0.3, 0.0, rng.uniform(0.5, 20, m)),
+                   rng.uniform(1e-4, 5e-2, m), rng.uniform(0.2, 2, m), rng.uniform(0.1, 2, m),
+                   rng.uniform(0, 0.05, m), rng.uniform(0.5, 3, m), rng.choice([0.0625, 0.1, 0.125, 0.25], m),
+                   rng.uniform(50, 1000, m)], 1).astype(f32)
+    out["learnff_in"] = lf
+    out["learnff_out"] = run("learnff", lf, np.uint8).reshape(m, -1)
     np.savez_compressed(os.path.join(ROOT, "tests", "golden", "ref_golden.npz"), **out)
     print({k: v.shape for k, v in out.items()})
 

@@ -8,6 +8,7 @@ Run from the repository root on a machine with a GPU:
 
   REFERENCE_SRC=<reference checkout>/src bash oracle/ref/build_ref_kernels.sh   # where the sources are
   python tests/golden/make_ref_kernel_golden.py [out.npz]                        # on the GPU machine
+  python tests/golden/make_ref_kernel_golden.py --learning [out.npz]             # ref_learning.npz
 
 Cases:
   lgn_*    logRand_init + 48 steps of LGN_nonlinear (512 cells, seeded drive)
@@ -48,7 +49,46 @@ def run(mode, inputs):
         return RC.read_bundle(fo)
 
 
+def learning(out_path):
+    """ref_learning.npz: LGN_nonlinear with learning = 3 (the presynaptic trace of each cell per
+    step: at the end, at the start, right after its spikes) on the LGN case, and 120 V1 steps of
+    compute_V_collect_spike_learnFF_fast with learning = 3 + recal_G_mat_nd_fast on the LGN
+    spike words of the library's own run, the presynaptic traces given per step."""
+    res = {}
+    lo = run("lgnlearn", RC.lgn_learn_case())
+    for k, v in lo.items():
+        res["lgn_" + k] = v
+    wl = RC.v1_workload(sp=False)
+    from visual_cortex_gb300 import _native as N
+    from visual_cortex_gb300.model import Simulation
+    sim = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        sim.set_record(N.REC_LGN_SP, RC.LEARN_T + 1)
+        sim.run(RC.LEARN_T)
+        _, lsp, _ = sim.fetch_records(0, RC.LEARN_T, raw=False, lgn_sp=True, lgn_fr=False)
+    finally:
+        sim.close()
+    vi = RC.v1_learn_inputs(wl, np.asarray(lsp, np.float32), RC.LEARN_T)
+    o = run("v1learn", vi)
+    res["v1_lgnSInfo"] = np.asarray(lsp, np.float32)
+    res["v1_preStart"] = vi["preStart"].reshape(RC.LEARN_T, -1)
+    res["v1_preSpk"] = vi["preSpk"].reshape(RC.LEARN_T, -1)
+    for k in RC.STATE_KEYS:
+        res["v1_in_" + k] = vi[k]
+    for k, v in o.items():
+        res["v1_" + k] = v
+    np.savez_compressed(out_path, **res)
+    print(f"wrote {out_path}: {len(res)} arrays; v1: {(o['raster'] >= 1).sum()} V1 spikes, "
+          f"max |dw| {np.abs(o['sLGN'] - wl.net.sLGN.reshape(-1)).max():.3g}")
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "--learning":
+        if not os.path.exists(CUBIN):
+            raise SystemExit(f"{CUBIN} is missing: run oracle/ref/build_ref_kernels.sh where the reference's sources are")
+        build_runner()
+        learning(sys.argv[2] if len(sys.argv) > 2 else os.path.join(ROOT, "tests", "golden", "ref_learning.npz"))
+        return
     out_path = sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "tests", "golden", "ref_kernels.npz")
     if not os.path.exists(CUBIN):
         raise SystemExit(f"{CUBIN} is missing: run oracle/ref/build_ref_kernels.sh where the reference's sources are")

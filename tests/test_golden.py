@@ -152,3 +152,36 @@ def test_oracle_host_init_matches_the_library():
                     assert y is None
                     continue
                 np.testing.assert_array_equal(x, y, err_msg=k)
+
+
+def _ff_rows(gold):
+    """The learnff rows as pv1_ff_learning structs and the reference's derived constants
+    (LearnVarShapeFF_E_pre: n, tauLTP; LearnVarShapeFF_E_post: n, tau[3], A_LTP, A_ratio,
+    targetFR, gmax, gmin; then exp_homeo)."""
+    from visual_cortex_gb300 import _native as N
+    rows = gold["learnff_in"]
+    out = gold["learnff_out"]
+    for r, b in zip(rows, out):
+        cfg = N.FFLearning(learning=3, tauLTP=r[0], tauLTD=r[1], tauTrip=r[2], tauAvg=r[3], targetFR=r[4],
+                           A_LGN=r[5], r_LTD=r[6], gmaxLGN=r[7], gminLGN=r[8], sRatioLGN=r[9],
+                           decayTimeHomeoFF=r[11], FF_InfRatio=1.0, applyHomeo=0, symmetricHomeo=1, rebound=0)
+        pre = np.frombuffer(b[:8].tobytes(), np.uint32)
+        post = np.frombuffer(b[8:44].tobytes(), f32)
+        assert pre[0] == 1 and np.frombuffer(b[8:12].tobytes(), np.uint32)[0] == 1
+        want = np.array([post[4], post[5], post[7], post[8], np.frombuffer(b[44:48].tobytes(), f32)[0]], f32)
+        yield cfg, r, want, np.frombuffer(b[4:8].tobytes(), f32)[0], post
+
+
+def test_learning_constants_match_learnFF_post(gold, L):
+    """The oracle's and the library's derived LGN->V1 learning constants (A_LTP, the LTD rate
+    A_ratio with its targetFR scaling, gmax, gmin, exp_homeo) equal the reference's learnFF_post
+    and exp_homeo bit for bit, and its tau fields are the cfg's."""
+    from visual_cortex_gb300 import _native as N
+    for cfg, r, want, tauLTP, post in _ff_rows(gold):
+        assert tauLTP == r[0] and post[1] == r[1] and post[2] == r[2] and post[3] == r[3] and post[6] == r[4]
+        a = np.zeros(5, f32)
+        L.orc_ff_learning_rates(C.byref(cfg), f32(r[10]), fp(a))
+        np.testing.assert_array_equal(a, want)
+        b = np.zeros(5, f32)
+        assert N.lib.pv1_ff_learning_rates(C.byref(cfg), f32(r[10]), N.fptr(b)) == 0
+        np.testing.assert_array_equal(b, want)

@@ -291,3 +291,92 @@ def _rates(L, lo, conv):
                         oracle.fp(lo.sharp), oracle.fp(lo.la), oracle.fp(lo.lb), oracle.fp(ltr), oracle.fp(lnl),
                         oracle.fp(np.zeros((n, 1), f32)), None, 1, oracle.fp(si), oracle.fp(fr))
     return fr, si
+
+
+GOLD_LEARN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_learning.npz")
+
+
+@pytest.fixture(scope="module")
+def gold_learn():
+    return dict(np.load(GOLD_LEARN))
+
+
+def test_oracle_lgn_trace_matches_reference_kernel(gold, gold_learn):
+    """LGN_nonlinear with learning = 3 (src/discrete_input_convol.cu:1774-1808) on the LGN case:
+    the oracle's presynaptic trace at the start of each step, right after each cell's spikes,
+    and at the end of the step (lVar) within 1e-5 of the reference's over 48 steps."""
+    import oracle
+    case = RC.lgn_case()
+    n, K, NU = RC.LGN_N, RC.LGN_K, RC.LGN_NU
+    L = oracle.lib()
+    cfg = _lgn_cfg(n, 1.0, 80.0, 0.125)
+    tau = RC.learning_params().tauLTP
+    u0 = gold["lgn_u0"].reshape(n, NU)
+    ltr = gold["lgn_ltr0"].copy()
+    lnl = gold["lgn_lnl0"].copy()
+    used = np.zeros(n, np.int64)
+    conv = case["convol"].reshape(K, n)
+    var = np.zeros(n, f32)
+    ref_end = gold_learn["lgn_ffvar"].reshape(K, n)
+    ref_start = gold_learn["lgn_ffstart"].reshape(K, n)
+    ref_spk = gold_learn["lgn_ffspk"].reshape(K, n)
+    np.testing.assert_array_equal(gold_learn["lgn_sInfo"].reshape(K, n), gold["lgn_sInfo"].reshape(K, n))
+    cap = 8
+    spiked = 0
+    for k in range(K):
+        u = np.zeros((n, cap), f32)
+        for i in range(n):
+            take = u0[i, used[i]:used[i] + cap]
+            u[i, :take.size] = take
+        si, fr, tsp = np.zeros(n, f32), np.zeros(n, f32), np.zeros(n, f32)
+        nsp = np.zeros(n, np.uint32)
+        L.orc_lgn_nonlinear_ex(C.byref(cfg), oracle.fp(conv[k]), oracle.fp(case["max_convol"]), oracle.fp(case["c50"]),
+                               oracle.fp(case["sharpness"]), oracle.fp(case["a"]), oracle.fp(case["b"]), oracle.fp(ltr),
+                               oracle.fp(lnl), oracle.fp(u), None, cap, oracle.fp(si), oracle.fp(fr), oracle.up(nsp),
+                               oracle.fp(tsp))
+        start, at = np.zeros(n, f32), np.zeros(n, f32)
+        L.orc_lgn_ff_pre(n, f32(0.125), f32(tau), oracle.up(nsp), oracle.fp(tsp), oracle.fp(si), oracle.fp(var),
+                         oracle.fp(start), oracle.fp(at))
+        np.testing.assert_allclose(start, ref_start[k], rtol=1e-5, atol=1e-7)
+        np.testing.assert_allclose(var, ref_end[k], rtol=1e-5, atol=1e-7)
+        s = si > 0
+        np.testing.assert_allclose(at[s], ref_spk[k][s], rtol=1e-5, atol=1e-7)
+        spiked += int(s.sum())
+        used += np.floor(si).astype(np.int64)
+    assert spiked > 200 and ref_end.max() > 0.5
+
+
+def test_oracle_v1_learning_matches_reference_kernels(gold_learn):
+    """120 steps of the reference's compute_V_collect_spike_learnFF_fast with learning = 3
+    (multiplicative homeostasis, targetFR > 0) + recal_G_mat_nd_fast on recorded LGN spike
+    words and presynaptic traces: the oracle's rasters are identical, and the LGN->V1 weights,
+    the post LTD and triplet traces, the filtered rates and the homeostasis totals agree to
+    1e-5 of each array's largest value (the weights change by several percent)."""
+    import oracle
+    wl = RC.v1_workload(sp=False, host_init=oracle.host_init_state)
+    g = gold_learn
+    vo = oracle.V1Oracle(wl.spec, wl.net)
+    for k in ("v", "w", "gFF", "hFF", "gE", "hE", "gI", "hI"):
+        vo.put(k, g["v1_in_" + k])
+    vo.set_ff_learning(RC.learning_params())
+    T, n = RC.LEARN_T, wl.spec.nV1
+    lgn = g["v1_lgnSInfo"]
+    raster = np.zeros((T, n), f32)
+    for it in range(T):
+        vo.step(lgn[it])
+        vo.learn_ff(lgn[it], np.ascontiguousarray(g["v1_preStart"][it]), np.ascontiguousarray(g["v1_preSpk"][it]))
+        raster[it] = vo.get("sInfo")
+    ref = g["v1_raster"].reshape(T, n)
+    np.testing.assert_array_equal(raster >= 1, ref >= 1)
+    assert (ref >= 1).sum() > 50
+    s1 = vo.get("sLGN")
+    rel = lambda a, b: float(np.max(np.abs(a.astype(np.float64) - b)) / np.max(np.abs(b)))
+    assert rel(s1, g["v1_sLGN"]) < 1e-5
+    assert np.abs(g["v1_sLGN"] - wl.net.sLGN.reshape(-1)).max() > 0.01 * wl.net.sLGN.max()
+    post = vo.get("ff_post")
+    nEt = wl.spec.nE * wl.spec.nblock
+    assert rel(post[:nEt], g["v1_vLTD"]) < 1e-5
+    assert rel(post[nEt:2 * nEt], g["v1_vTrip"]) < 1e-5
+    assert rel(post[2 * nEt:4 * nEt], g["v1_vAvgE"]) < 1e-5
+    assert rel(vo.get("total_ff")[:n], g["v1_totalFF"]) < 1e-5
+    vo.close()

@@ -1037,6 +1037,24 @@ static int ensure_ff_ring(pv1_plan *p) {
     return PV1_OK;
 }
 
+int pv1_ff_learning_rates(const pv1_ff_learning *l, float dt, float *out) {
+    if (!l || !out) return PV1_E_ARG;
+    // learnFF_post (src/condShape.h:137-152), Float = float, with its double literals
+    const float A_LTP = l->A_LGN * l->sRatioLGN;
+    const float tauAvg_in_sec = (float)((double)l->tauAvg / 1000.0);
+    float A_ratio = l->r_LTD * A_LTP;
+    if (l->targetFR > 0) {
+        const float q = l->tauTrip / (l->tauLTD * (tauAvg_in_sec * tauAvg_in_sec));
+        A_ratio = (float)((double)A_ratio * ((double)q / 1000.0 / (double)l->targetFR));
+    }
+    out[0] = A_LTP;
+    out[1] = A_ratio;
+    out[2] = l->gmaxLGN * l->sRatioLGN;
+    out[3] = l->gminLGN * l->sRatioLGN;
+    out[4] = expf(-dt / l->decayTimeHomeoFF);
+    return PV1_OK;
+}
+
 int pv1_set_ff_learning(pv1_plan *p, const pv1_ff_learning *l) {
     if (!p || !l) return PV1_E_ARG;
     if (l->learning != 3)
@@ -1048,15 +1066,8 @@ int pv1_set_ff_learning(pv1_plan *p, const pv1_ff_learning *l) {
         return fail(p, PV1_E_ARG, "learning time constants must be > 0");
     if (l->applyHomeo < 0 || l->applyHomeo > 2) return fail(p, PV1_E_ARG, "applyHomeo is 0, 1 or 2");
     const pv1_v1_config &c = p->cfg;
-    const float dt = c.dt;
-    // learnFF_post (src/condShape.h:137-152), Float = float, with its double literals
-    const float A_LTP = l->A_LGN * l->sRatioLGN;
-    const float tauAvg_in_sec = (float)((double)l->tauAvg / 1000.0);
-    float A_ratio = l->r_LTD * A_LTP;
-    if (l->targetFR > 0) {
-        const float q = l->tauTrip / (l->tauLTD * (tauAvg_in_sec * tauAvg_in_sec));
-        A_ratio = (float)((double)A_ratio * ((double)q / 1000.0 / (double)l->targetFR));
-    }
+    float rates[5];
+    pv1_ff_learning_rates(l, c.dt, rates);
     V1Params &v = p->vp;
     const size_t n = p->nV1, nEt = (size_t)p->nE * c.nblock, nIt = (size_t)p->nI * c.nblock;
     // the homeostasis totals: each neuron's LGN weights summed in synapse order, and that
@@ -1084,14 +1095,14 @@ int pv1_set_ff_learning(pv1_plan *p, const pv1_ff_learning *l) {
     v.ffTauTrip = l->tauTrip;
     v.ffTauAvg = l->tauAvg;
     v.ffTargetFR = l->targetFR;
-    v.ffA_LTP = A_LTP;
-    v.ffA_ratio = A_ratio;
-    v.ffGmax = l->gmaxLGN * l->sRatioLGN;
-    v.ffGmin = l->gminLGN * l->sRatioLGN;
+    v.ffA_LTP = rates[0];
+    v.ffA_ratio = rates[1];
+    v.ffGmax = rates[2];
+    v.ffGmin = rates[3];
     v.applyHomeo = l->applyHomeo;
     v.symmetricHomeo = l->symmetricHomeo != 0;
     v.rebound = l->rebound != 0;
-    v.expHomeo = expf(-dt / l->decayTimeHomeoFF);
+    v.expHomeo = rates[4];
     v.ffPost = d_post;
     v.totalFF = d_tot;
     v.sLGNw = const_cast<float *>(v.sLGN);

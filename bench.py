@@ -347,15 +347,36 @@ def bench_lgn_bf16():
     cores, each followed by the logistic rate and Poisson spikes; rates against an FP64 oracle
     on 1024 cells x 250 steps."""
     from visual_cortex_gb300 import lgn_bf16 as L
+    from visual_cortex_gb300 import _native as N
+    from visual_cortex_gb300.model import Simulation
     wl = L.make_workload(seed=0)
     tc = L.LgnTensorCore(wl, fr_every=64)
     try:
         tc.run(tensor_cores=True)
         tc.run(tensor_cores=False)
-        ms16 = float(np.median([tc.run(tensor_cores=True) for _ in range(3)]))
-        _, _, fr16 = tc.fetch()
         ms32 = float(np.median([tc.run(tensor_cores=False) for _ in range(3)]))
         _, _, fr32 = tc.fetch()
+        ms16 = float(np.median([tc.run(tensor_cores=True) for _ in range(3)]))
+        _, _, fr16 = tc.fetch()
+        # the full-patch V1 (16384 LGN cells, as the stage) driven by the BF16 stage's spike
+        # words for the whole 2 s (pv1_set_lgn_source)
+        v1 = build_workload("C2")
+        sim = Simulation(v1.spec, v1.net, v1.lgn, v1.stim, v1.init, v1.seeds)
+        try:
+            sim.set_lgn_source(tc.device_spikes(), 0, wl.T)
+            sim.set_record(N.REC_SPIKES, 4097)
+            drv_ms = sim.run_timed(4000, 0)
+            counts = sim.fetch_spikes(0, 4000)
+            sim.set_record(0, 2)
+            drv_ms += sim.run_timed(wl.T - 4000, 0)
+            driven = {"value": v1.spec.nV1 * wl.T / (drv_ms * 1e-3), "unit": UNIT, "ms": drv_ms,
+                      "v1_rate_hz_first_500ms": float(np.floor(np.where(counts >= 1, counts, 0)).sum()) /
+                      (v1.spec.nV1 * 4000 * wl.dt * 1e-3),
+                      "e2e_stage_plus_v1_ms": ms16 + drv_ms,
+                      "what": "the 32x1024 V1 of the headline workload stepped for the stage's 16000 steps on its "
+                              "BF16 spike words (one device-to-device copy of each chunk's rows into the LGN ring)"}
+        finally:
+            sim.close()
     finally:
         tc.close()
     rng = np.random.default_rng(0)
@@ -379,6 +400,7 @@ def bench_lgn_bf16():
             "fp32_cuda_cores": {"value": work / (ms32 * 1e-3), "unit": "LGN cell-steps/s", "ms": ms32,
                                 "err_vs_fp64": rate_errors(fr32[:, cells], ref)},
             "speedup_bf16_over_fp32": ms32 / ms16,
+            "v1_driven_by_bf16_stage": driven,
             "workload": "16384 ON/OFF cells, 31x31 px DoG (sigma +-20%), 250 taps, 256x256 1/f^2 noise, "
                         "120 Hz, 2 s (16000 steps at 0.125 ms)"}
 

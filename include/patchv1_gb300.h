@@ -284,6 +284,16 @@ int64_t pv1_raw_record_floats(const pv1_plan *plan);
  * Returns after the work is queued when `sync` is 0. */
 int pv1_run(pv1_plan *plan, uint32_t nsteps, int sync);
 
+/* Feeds the V1 steps [step0, step0 + nsteps) from LGN spike words the caller computed
+ * (d_sInfo: device memory of the plan's device, [nsteps][nLGN] rows in the plan's LGN cell
+ * order, spike words nsp + tsp/dt as LGN_nonlinear writes them, src/discrete_input_convol.cu:
+ * 1766-1771) instead of the plan's own LGN stage; each run copies the rows of its steps into
+ * the LGN ring, and a run outside the range fails.  The buffer must stay valid while it is
+ * set; d_sInfo = NULL returns to the plan's own LGN stage.  Not with plasticity
+ * (PV1_E_UNSUPPORTED).  For instance the BF16 tensor-core LGN stage below
+ * (pv1_lgn_tc_device_spikes) can drive a simulation this way. */
+int pv1_set_lgn_source(pv1_plan *plan, const float *d_sInfo, int64_t step0, int64_t nsteps);
+
 /* Copies finished records [step0, step0+n) to host buffers (any may be NULL):
  * raw: n * pv1_raw_record_floats floats; lgn_sp, lgn_fr: n * nLGN floats. */
 int pv1_fetch_records(pv1_plan *plan, uint64_t step0, uint32_t n, float *raw,
@@ -569,6 +579,8 @@ int pv1_lgn_tc_run(pv1_lgn_tc *p, int tensorCores, uint64_t seed, float *ms);
 /* S [nCells][nFext] (FP32 spatial stage), spike words [T][nCells], rates
  * [ceil(T/frEvery)][nCells]; any may be null. */
 int pv1_lgn_tc_fetch(pv1_lgn_tc *p, float *S, float *sInfo, float *fr);
+/* The device array of the spike words [T][nCells] the last run wrote (valid until destroy). */
+const float *pv1_lgn_tc_device_spikes(const pv1_lgn_tc *p);
 void pv1_lgn_tc_destroy(pv1_lgn_tc *p);
 const char *pv1_lgn_tc_last_error(const pv1_lgn_tc *p);
 

@@ -49,3 +49,75 @@ def test_bf16_tensor_core_rates_against_fp64(native):
     # spikes are produced on both paths at similar counts
     n16, n32 = int((sp16 >= 1).sum()), int((sp32 >= 1).sum())
     assert n32 > 0 and abs(n16 - n32) < 0.1 * n32 + 10
+
+
+@pytest.mark.gpu
+def test_external_lgn_source_reproduces_the_plans_own_lgn(native):
+    """A plan fed its own LGN spike words from a device array (pv1_set_lgn_source) steps exactly
+    as the plan that computed them: the V1 rasters are equal bit for bit over 200 steps (the
+    first chunk, full persistent chunks with the overlapped LGN copies, and a partial chunk);
+    a run past the source's steps fails."""
+    torch = pytest.importorskip("torch")
+    from visual_cortex_gb300 import _native as N
+    from visual_cortex_gb300 import synth
+    from visual_cortex_gb300.model import Simulation
+    wl = synth.make_workload("ext-lgn", seed=12, nblock=4, n_lgn=1024, m=20, width=64, height=64, nt=400,
+                             far_partners=100, adex_inh=True, nFrame=60)
+    T = 200
+    a = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        a.set_record(N.REC_SPIKES | N.REC_LGN_SP, T + 1)
+        a.run(T)
+        sa = a.fetch_spikes(0, T)
+        _, lsp, _ = a.fetch_records(0, T, raw=False, lgn_sp=True, lgn_fr=False)
+    finally:
+        a.close()
+    d = torch.from_numpy(np.ascontiguousarray(lsp, np.float32)).to("cuda:0")
+    b = Simulation(wl.spec, wl.net, wl.lgn, wl.stim, wl.init, wl.seeds)
+    try:
+        b.set_lgn_source(d.data_ptr(), 0, T)
+        b.set_record(N.REC_SPIKES, T + 1)
+        b.run(T)
+        np.testing.assert_array_equal(b.fetch_spikes(0, T), sa)
+        assert (sa >= 1).sum() > 100
+        with pytest.raises(RuntimeError, match="external LGN source"):
+            b.run(8)
+    finally:
+        b.close()
+    torch.cuda.synchronize()
+
+
+@pytest.mark.gpu
+def test_simulation_driven_by_the_bf16_lgn_stage(native):
+    """V1 steps driven by the BF16 tensor-core LGN stage through pv1_set_lgn_source, and by the
+    FP32 CUDA-core form of the same stage: both runs spike, and their V1 rates agree within 10%
+    (the BF16 rates differ from FP32 by a fraction of a percent; the spike draws are the same
+    generators)."""
+    from visual_cortex_gb300 import _native as N
+    from visual_cortex_gb300 import lgn_bf16 as L
+    from visual_cortex_gb300 import synth
+    from visual_cortex_gb300.model import Simulation
+    wl = L.make_workload(nCells=1024, size=64, nFrame=24, side=15, T=640, seed=3)
+    v1 = synth.make_workload("bf16-driven", seed=13, nblock=2, n_lgn=1024, m=20, width=64, height=64, nt=640,
+                             adex_inh=True, nFrame=40)
+    assert v1.lgn.nLGN == wl.nCells
+    tc = L.LgnTensorCore(wl, fr_every=64)
+    rates, lgn = {}, {}
+    try:
+        for cores in (True, False):
+            tc.run(tensor_cores=cores)
+            lgn[cores] = int((tc.fetch(spikes=True, rates=False)[1] >= 1).sum())
+            sim = Simulation(v1.spec, v1.net, v1.lgn, v1.stim, v1.init, v1.seeds)
+            try:
+                sim.set_lgn_source(tc.device_spikes(), 0, wl.T)
+                sim.set_record(N.REC_SPIKES, wl.T + 1)
+                sim.run(wl.T)
+                sp = sim.fetch_spikes(0, wl.T)
+            finally:
+                sim.close()
+            rates[cores] = float(np.floor(np.where(sp >= 1, sp, 0)).sum()) / (v1.spec.nV1 * wl.T * wl.dt * 1e-3)
+    finally:
+        tc.close()
+    assert lgn[True] > 300 and lgn[False] > 300, lgn
+    assert rates[True] > 0.5 and rates[False] > 0.5, rates
+    assert abs(rates[True] - rates[False]) < 0.1 * rates[False], rates

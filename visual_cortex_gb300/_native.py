@@ -159,6 +159,8 @@ def _load() -> C.CDLL:
         "pv1_persistent_mode": ([P, C.c_int], C.c_int),
         "pv1_set_wait_limit": ([P, C.c_int64], C.c_int),
         "pv1_set_ff_learning": ([P, C.POINTER(FFLearning)], C.c_int),
+        "pv1_set_lgn_source": ([P, C.c_void_p, C.c_int64, C.c_int64], C.c_int),
+        "pv1_lgn_tc_device_spikes": ([P], C.c_void_p),
         "pv1_ff_learning_rates": ([C.POINTER(FFLearning), C.c_float, _FP], C.c_int),
         "pv1_lgn_spikes_noalloc": ([P, C.c_uint32, _FP, _FP], C.c_int),
         "pv1_batch_create": ([C.POINTER(P), C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(P)], C.c_int),

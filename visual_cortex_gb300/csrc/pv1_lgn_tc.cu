@@ -54,15 +54,38 @@ struct TcArgs {
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
 // The rate of LGN_nonlinear (src/discrete_input_convol.cu:1660-1730) for this form: the same
-// logistic, evaluated in single precision with reciprocals (the reference divides in double;
-// this form's accuracy is stated against the FP64 oracle instead).  Independent across steps,
-// so a chunk of steps is evaluated with full instruction-level parallelism.
+// logistic, evaluated in single precision with the hardware exponential and reciprocal (the
+// reference divides in double; this form's accuracy is stated against the FP64 oracle, and
+// the BF16 operands dominate that error).  Independent across steps, so a chunk of steps is
+// evaluated with full instruction-level parallelism.
 __device__ __forceinline__ float lgn_rate(const TcArgs &A, float convol, float absk, float mx, float rmx, float C50,
                                           float Kc, float LA, float LB) {
     float current = (convol * absk) * A.convolRatio;
     if (current < 0) current = 0;
-    const float X = 1.0f / (1.0f + expf(Kc * (C50 - current * rmx)));
+    const float X = __fdividef(1.0f, 1.0f + __expf(Kc * (C50 - current * rmx)));
     return A.frRatio * mx * (LA * X + LB);
+}
+
+// Steps t0..t0+n-1 of one cell through get_spike from rT values in shared memory (stride
+// kTcM floats), spike words to out (stride nCells floats); four steps per pass with their
+// shared-memory loads issued together.
+__device__ __forceinline__ float lgn_poisson(float rT, float &ltr, float &lnl, curandStateMRG32k3a &st);
+__device__ __forceinline__ void lgn_poisson_run(const float *rT, int stride, int n, float *out, size_t nCells,
+                                                float &ltr, float &lnl, curandStateMRG32k3a &st) {
+    int c = 0;
+    for (; c + 4 <= n; c += 4) {
+        const float r0 = rT[(c + 0) * stride], r1 = rT[(c + 1) * stride];
+        const float r2 = rT[(c + 2) * stride], r3 = rT[(c + 3) * stride];
+        out[0] = lgn_poisson(r0, ltr, lnl, st);
+        out[nCells] = lgn_poisson(r1, ltr, lnl, st);
+        out[2 * nCells] = lgn_poisson(r2, ltr, lnl, st);
+        out[3 * nCells] = lgn_poisson(r3, ltr, lnl, st);
+        out += 4 * nCells;
+    }
+    for (; c < n; c++) {
+        out[0] = lgn_poisson(rT[c * stride], ltr, lnl, st);
+        out += nCells;
+    }
 }
 
 // get_spike (src/discrete_input_convol.cu:1589-1619) for one step given rT = dt * rate: the
@@ -93,17 +116,23 @@ __device__ __forceinline__ void lgn_epilogue32(const TcArgs &A, int cell, int t0
                                                float &ltr, float &lnl, curandStateMRG32k3a &st) {
     float rT[32];
     const float scale = A.dt * 1e-3f;   // rate in spikes/ms times dt
+    int ph = t0 % A.frEvery;            // steps since the last recorded rate
 #pragma unroll
     for (int j = 0; j < 32; j++) {
         const float fr = lgn_rate(A, conv[j], absk, mx, rmx, C50, Kc, LA, LB);
         const int t = t0 + j;
-        if (A.fr && t < A.T && t % A.frEvery == 0) A.fr[(size_t)(t / A.frEvery) * A.nCells + cell] = fr;
+        if (A.fr && ph == 0 && t < A.T) A.fr[(size_t)(t / A.frEvery) * A.nCells + cell] = fr;
+        ph = ph + 1 == A.frEvery ? 0 : ph + 1;
         rT[j] = fr * scale;
     }
+    const int n = min(32, A.T - t0);
+    float *out = A.sInfo + (size_t)t0 * A.nCells + cell;
 #pragma unroll
     for (int j = 0; j < 32; j++) {
-        const int t = t0 + j;
-        if (t < A.T) A.sInfo[(size_t)t * A.nCells + cell] = lgn_poisson(rT[j], ltr, lnl, st);
+        if (j < n) {
+            *out = lgn_poisson(rT[j], ltr, lnl, st);
+            out += A.nCells;
+        }
     }
 }
 
@@ -264,11 +293,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) lgn_tc_kernel(TcArgs A, const _
             float v[32];
             tmem_ld32(tmem + ((unsigned)(quad * 32) << 16) + (unsigned)c0, v);
             if (on) {
+                int ph = (i * kTcN + c0) % A.frEvery;   // steps since the last recorded rate
 #pragma unroll
                 for (int j = 0; j < 32; j++) {
                     const float fr = lgn_rate(A, v[j], absk, mx, rmx, C50, Kc, LA, LB);
                     const int t = i * kTcN + c0 + j;
-                    if (A.fr && t < A.T && t % A.frEvery == 0) A.fr[(size_t)(t / A.frEvery) * A.nCells + cell] = fr;
+                    if (A.fr && ph == 0 && t < A.T) A.fr[(size_t)(t / A.frEvery) * A.nCells + cell] = fr;
+                    ph = ph + 1 == A.frEvery ? 0 : ph + 1;
                     R[(c0 + j) * kTcM + cl] = fr * scale;
                 }
             }
@@ -276,12 +307,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) lgn_tc_kernel(TcArgs A, const _
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();   // R holds the tile; tensor memory and both tiles are free
         if (threadIdx.x == issuer && i + 1 < A.nTiles) load_and_multiply(i + 1);
-        if (half == 0 && on) {
-            for (int c = 0; c < kTcN; c++) {
-                const int t = i * kTcN + c;
-                if (t < A.T) A.sInfo[(size_t)t * A.nCells + cell] = lgn_poisson(R[c * kTcM + cl], ltr, lnl, st);
-            }
-        }
+        if (half == 0 && on)
+            lgn_poisson_run(R + cl, kTcM, min(kTcN, A.T - i * kTcN), A.sInfo + (size_t)i * kTcN * A.nCells + cell,
+                            (size_t)A.nCells, ltr, lnl, st);
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();   // R is read; the next tile is in tensor memory
     }
@@ -587,5 +615,7 @@ void pv1_lgn_tc_destroy(pv1_lgn_tc *p) {
 }
 
 const char *pv1_lgn_tc_last_error(const pv1_lgn_tc *p) { return p ? p->err.c_str() : "null"; }
+
+const float *pv1_lgn_tc_device_spikes(const pv1_lgn_tc *p) { return p ? p->a.sInfo : nullptr; }
 
 }  // extern "C"

@@ -67,6 +67,9 @@ struct pv1_plan {
     // LGN spike ring
     float *d_lgnRing = nullptr, *d_lgnFr = nullptr;
     int lgnSlots = 0;
+    // an external LGN source (pv1_set_lgn_source): rows [extStep0, extStep0 + extSteps)
+    const float *extLgn = nullptr;
+    long long extStep0 = 0, extSteps = 0;
     int K = 64;  // steps per LGN launch / per persistent V1 launch / per graph
     bool persistent = false;     // V1 steps run as one cooperative launch per chunk
     // the LGN of chunk c+1 runs on its own stream while the persistent V1 kernel runs chunk c
@@ -193,13 +196,39 @@ int sink_rows(pv1_plan *p, long long a, long long n) {
     return PV1_OK;
 }
 
-// Issues k steps on the plan's stream: the LGN rate+spike pair for the k steps, then either
-// one persistent cooperative V1 launch for all k steps or k per-step V1 launches, then the
-// step-counter bump.  Returns the number of kernel launches through *launches.
-int issue_chunk(pv1_plan *p, int k, int deliverFirst, long long *launches) {
-    cudaError_t e = launch_lgn_step(p->lp, p->d_stepBase, k, p->stream);
-    if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("lgn_step: ") + cudaGetErrorString(e));
-    long long n = lgn_step_launches(p->lp, k);
+// The LGN spike words of steps [t0, t0 + k) into the LGN ring on stream st: the LGN kernels
+// (their step counter at d_step), or, with an external source, copies of its rows.  Returns
+// the kernel launches through *launches.
+int lgn_stage(pv1_plan *p, long long t0, int k, const long long *d_step, cudaStream_t st, long long *launches) {
+    if (!p->extLgn) {
+        cudaError_t e = launch_lgn_step(p->lp, d_step, k, st);
+        if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("lgn_step: ") + cudaGetErrorString(e));
+        if (launches) *launches += lgn_step_launches(p->lp, k);
+        return PV1_OK;
+    }
+    if (t0 < p->extStep0 || t0 + k > p->extStep0 + p->extSteps)
+        return fail(p, PV1_E_ARG, "the steps run are not all in the external LGN source");
+    const size_t row = (size_t)p->nLGN * sizeof(float);
+    long long done = 0;
+    while (done < k) {
+        const long long t = t0 + done;
+        const long long slot = t % p->lgnSlots;
+        const long long cnt = std::min<long long>(k - done, p->lgnSlots - slot);
+        PV1_CUDA(p, cudaMemcpyAsync(p->d_lgnRing + (size_t)slot * p->nLGN, p->extLgn + (size_t)(t - p->extStep0) * p->nLGN,
+                                    (size_t)cnt * row, cudaMemcpyDeviceToDevice, st));
+        done += cnt;
+    }
+    return PV1_OK;
+}
+
+// Issues k steps (from host step t0) on the plan's stream: the LGN stage for the k steps,
+// then either one persistent cooperative V1 launch for all k steps or k per-step V1 launches,
+// then the step-counter bump.  Returns the number of kernel launches through *launches.
+int issue_chunk(pv1_plan *p, long long t0, int k, int deliverFirst, long long *launches) {
+    long long n = 0;
+    int r = lgn_stage(p, t0, k, p->d_stepBase, p->stream, &n);
+    if (r) return r;
+    cudaError_t e = cudaSuccess;
     if (p->persistent) {
         e = launch_v1_persistent(p->vp, p->d_stepBase, k, p->d_lgnRing, p->lgnSlots, deliverFirst, p->d_barrier,
                                  p->stream);
@@ -1060,6 +1089,8 @@ int pv1_set_ff_learning(pv1_plan *p, const pv1_ff_learning *l) {
     if (l->learning != 3)
         return fail(p, PV1_E_UNSUPPORTED, "only learning = 3 (LGN->E plasticity) is built");
     if (!p->lgnReady || !p->haveLGNsyn) return fail(p, PV1_E_STATE, "set up the LGN and the LGN->V1 synapses first");
+    if (p->extLgn)
+        return fail(p, PV1_E_UNSUPPORTED, "plasticity needs the plan's own LGN stage (its presynaptic traces)");
     if (p->vp.multiSpike)
         return fail(p, PV1_E_UNSUPPORTED, "plasticity with several spikes per step (dt > min tRef) is not built");
     if (!(l->tauLTP > 0 && l->tauLTD > 0 && l->tauTrip > 0 && l->tauAvg > 0 && l->decayTimeHomeoFF > 0))
@@ -1740,6 +1771,30 @@ static int choose_mode(pv1_plan *p) {
     return PV1_OK;
 }
 
+int pv1_set_lgn_source(pv1_plan *p, const float *d_sInfo, int64_t step0, int64_t nsteps) {
+    if (!p) return PV1_E_ARG;
+    if (!d_sInfo) {
+        p->extLgn = nullptr;
+        p->extSteps = 0;
+        drop_graph(p);
+        return PV1_OK;
+    }
+    if (!p->lgnReady) return fail(p, PV1_E_STATE, "call pv1_lgn_setup first (it gives the LGN cell count)");
+    if (step0 < 0 || nsteps <= 0) return fail(p, PV1_E_ARG, "bad step range");
+    if (p->vp.ffLearn)
+        return fail(p, PV1_E_UNSUPPORTED, "an external LGN source has no presynaptic learning traces (learning = 3)");
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, d_sInfo) != cudaSuccess || a.type != cudaMemoryTypeDevice || a.device != p->device) {
+        cudaGetLastError();
+        return fail(p, PV1_E_ARG, "the LGN source must be device memory of the plan's device");
+    }
+    p->extLgn = d_sInfo;
+    p->extStep0 = step0;
+    p->extSteps = nsteps;
+    drop_graph(p);
+    return PV1_OK;
+}
+
 int pv1_set_wait_limit(pv1_plan *p, int64_t spins) {
     if (!p) return PV1_E_ARG;
     if (spins < 0) spins = kDefaultWaitSpins;
@@ -1769,7 +1824,7 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
     // the first chunk of a run without a pending delivery differs from the captured one
     if (!p->pending && nsteps > 0) {
         int k = (int)std::min<uint32_t>(nsteps, (uint32_t)K);
-        r = issue_chunk(p, k, 0, &p->launches);
+        r = issue_chunk(p, p->step, k, 0, &p->launches);
         if (r) return r;
         r = sink_rows(p, p->step + (long long)done, k);
         if (r) return r;
@@ -1790,10 +1845,11 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
             const int nFull = (int)((nsteps - done) / (uint32_t)K);
             const long long t0 = p->step + (long long)done;
             PV1_CUDA(p, cudaMemcpyAsync(p->d_lgnStep, &t0, sizeof(long long), cudaMemcpyHostToDevice, p->stream));
-            cudaError_t e = launch_lgn_step(p->lp, p->d_lgnStep, K, p->stream);
-            if (e == cudaSuccess) e = launch_advance_step(p->d_lgnStep, K, p->stream);
+            r = lgn_stage(p, t0, K, p->d_lgnStep, p->stream, &p->launches);
+            if (r) return r;
+            cudaError_t e = launch_advance_step(p->d_lgnStep, K, p->stream);
             if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("lgn_step: ") + cudaGetErrorString(e));
-            p->launches += lgn_step_launches(p->lp, K) + 1;
+            p->launches += 1;
             for (int c = 0; c < nFull; c++) {
                 if (c > 0) PV1_CUDA(p, cudaStreamWaitEvent(p->stream, p->evLgn, 0));
                 PV1_CUDA(p, cudaEventRecord(p->evFree, p->stream));   // chunk c-1's V1 is done
@@ -1806,18 +1862,28 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
                 if (r) return r;
                 if (c + 1 < nFull) {
                     PV1_CUDA(p, cudaStreamWaitEvent(p->lgnStream, p->evFree, 0));
-                    e = launch_lgn_step(p->lp, p->d_lgnStep, K, p->lgnStream);
-                    if (e == cudaSuccess) e = launch_advance_step(p->d_lgnStep, K, p->lgnStream);
+                    r = lgn_stage(p, t0 + (long long)(c + 1) * K, K, p->d_lgnStep, p->lgnStream, &p->launches);
+                    if (r) return r;
+                    e = launch_advance_step(p->d_lgnStep, K, p->lgnStream);
                     if (e != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("lgn_step: ") + cudaGetErrorString(e));
                     PV1_CUDA(p, cudaEventRecord(p->evLgn, p->lgnStream));
-                    p->launches += lgn_step_launches(p->lp, K) + 1;
+                    p->launches += 1;
                 }
                 done += K;
             }
         } else if (p->persistent) {
             // a cooperative launch per chunk: issued directly (4 launches per K steps)
             while (nsteps - done >= (uint32_t)K) {
-                r = issue_chunk(p, K, 1, &p->launches);
+                r = issue_chunk(p, p->step + (long long)done, K, 1, &p->launches);
+                if (r) return r;
+                r = sink_rows(p, p->step + (long long)done, K);
+                if (r) return r;
+                done += K;
+            }
+        } else if (p->extLgn) {
+            // the copies of an external source differ chunk by chunk: issued directly
+            while (nsteps - done >= (uint32_t)K) {
+                r = issue_chunk(p, p->step + (long long)done, K, 1, &p->launches);
                 if (r) return r;
                 r = sink_rows(p, p->step + (long long)done, K);
                 if (r) return r;
@@ -1828,7 +1894,7 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
             if (!p->graphExec) {
                 cudaGraph_t g;
                 PV1_CUDA(p, cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
-                r = issue_chunk(p, K, 1, &per);
+                r = issue_chunk(p, p->step + (long long)done, K, 1, &per);
                 cudaError_t e2 = cudaStreamEndCapture(p->stream, &g);
                 if (r) return r;
                 if (e2 != cudaSuccess) return fail(p, PV1_E_CUDA, std::string("capture: ") + cudaGetErrorString(e2));
@@ -1847,7 +1913,7 @@ int pv1_run(pv1_plan *p, uint32_t nsteps, int sync) {
     }
     if (done < nsteps) {
         int k = (int)(nsteps - done);
-        r = issue_chunk(p, k, 1, &p->launches);
+        r = issue_chunk(p, p->step + (long long)done, k, 1, &p->launches);
         if (r) return r;
         r = sink_rows(p, p->step + (long long)done, k);
         if (r) return r;
@@ -1933,6 +1999,7 @@ int pv1_run_timed(pv1_plan *p, uint32_t nsteps, uint64_t flush_bytes, float *ms)
 
 int pv1_time_kernels(pv1_plan *p, uint32_t nsteps, float *v1_ms, float *lgn_ms, int *chunk) {
     if (!p || !v1_ms || !lgn_ms) return PV1_E_ARG;
+    if (p->extLgn) return fail(p, PV1_E_STATE, "pv1_time_kernels times the plan's own LGN stage");
     if (p->lgnOnly) return fail(p, PV1_E_STATE, "the plan was stepped by pv1_lgn_spikes_noalloc (LGN only)");
     if (!p->lgnReady || !p->stimReady || !p->haveState || !p->haveRng || !p->haveNear || !p->haveLGNsyn)
         return fail(p, PV1_E_STATE, "plan not ready");

@@ -225,6 +225,11 @@ class LgnTensorCore:
             raise RuntimeError(f"pv1_lgn_tc_fetch failed: {N.lib.pv1_lgn_tc_last_error(self.h).decode()}")
         return s, sp, fr
 
+    def device_spikes(self) -> int:
+        """Device address of the last run's spike words [T][nCells] (pv1_lgn_tc_device_spikes),
+        for Simulation.set_lgn_source."""
+        return int(N.lib.pv1_lgn_tc_device_spikes(self.h) or 0)
+
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:
             N.lib.pv1_lgn_tc_destroy(self.h)

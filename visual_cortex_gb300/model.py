@@ -437,6 +437,14 @@ class Simulation:
                          rebound=int(learning.rebound))
         N.check(self.plan, N.lib.pv1_set_ff_learning(self.plan, C.byref(c)), "pv1_set_ff_learning")
 
+    def set_lgn_source(self, device_ptr: int | None, step0: int = 0, nsteps: int = 0):
+        """Feed steps [step0, step0 + nsteps) from caller-computed LGN spike words: device_ptr
+        is the address of a device array [nsteps][nLGN] on the plan's device (e.g. a torch CUDA
+        tensor's data_ptr(), or LgnTensorCore.device_spikes()); None returns to the plan's own
+        LGN stage (pv1_set_lgn_source)."""
+        N.check(self.plan, N.lib.pv1_set_lgn_source(self.plan, device_ptr, int(step0), int(nsteps)),
+                "pv1_set_lgn_source")
+
     def persistent(self, allow: int = -1) -> bool:
         """Queries (allow=-1) or sets whether V1 steps run as one cooperative launch per
         chunk of steps."""

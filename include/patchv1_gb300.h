@@ -360,40 +360,55 @@ int pv1_checkpoint_load(pv1_plan *plan, const void *buf, uint64_t bytes);
  * being host vectors it does not save.  noDelay = 0 plans: PV1_E_UNSUPPORTED. */
 int pv1_set_step(pv1_plan *plan, int64_t step);
 
-/* LGN->V1 plasticity, learning = 3 of the reference ("only FF_E learning is active",
- * src/patch.cu:1166-1171): the triplet rule on every LGN->excitatory synapse inside the V1
- * step (compute_V_collect_spike_learnFF_fast, src/coredynamics.cu:1631-1993: LTD at each LGN
- * spike from the post LTD trace, LTP at each V1 spike from the presynaptic trace and the post
- * triplet trace, weights clipped to [gmin, gmax], the filtered post rate vAvgE scaling LTD
- * when targetFR > 0, optional homeostasis of each neuron's total LGN weight), and the
- * presynaptic LTP traces updated in the LGN stage (LGN_nonlinear, src/discrete_input_convol.cu:
- * 1774-1820).  The fields are the cfg values the reference reads (src/patch.cu:221-256:
- * element [0] of tauLTP, tauLTD, tauTrip, tauAvg, targetFR, A_LGN, r_LTD, gmaxLGN, gminLGN and
- * sRatioLGN); the derived rates are computed as learnFF_post does (src/condShape.h:137-152)
- * and exp_homeo as expf(-dt / decayTimeHomeoFF) (src/patch.cu:1330).  The per-neuron totals of
- * the homeostasis start from the current weights (src/patch.cu:4335-4352).  Plans with
- * learning run one launch per step (no persistent kernel, no batches) and one spike per
- * step at most; PV1_E_UNSUPPORTED otherwise. */
+/* LGN->V1 plasticity, the reference's learning modes 1-4 (src/patch.cu:1160-1175): the
+ * triplet rule on the LGN->excitatory synapses (learning 1, 2, 3) and on the LGN->inhibitory
+ * ones (learning 2) inside the V1 step (compute_V_collect_spike_learnFF_fast,
+ * src/coredynamics.cu:1631-1993: LTD at each LGN spike from the post LTD trace, LTP at each V1
+ * spike from the presynaptic trace and the post triplet trace, weights clipped to
+ * [gmin, gmax], the filtered post rate scaling LTD when targetFR > 0, optional homeostasis of
+ * each neuron's total LGN weight), the presynaptic LTP traces in the LGN stage (LGN_nonlinear,
+ * src/discrete_input_convol.cu:1774-1820), and, with learning 1, 2 and 4, the excitatory
+ * filtered rate vAvgE taken through the near delivery with the cortical E types' tauAvg
+ * (recal_G_mat_nd_fast, src/coredynamics.cu:2866-2890) instead of inside the V1 step.  The
+ * reference keeps cortical E->E and I->E learning variables as well, but no kernel of it
+ * changes a cortical weight with them and none of its outputs holds them; they are not kept.
+ * The fields are the cfg values the reference reads (src/patch.cu:221-256): the FF->E type's
+ * tauLTP..sRatioLGN (element [0] of the arrays; sRatioLGN[0]), the FF->I type's (element
+ * [nLearnTypeFF_E]; tauAvg[1], targetFR[1], sRatioLGN[1]) and the cortical E types' tauAvg
+ * (tauAvg[0] when nLearnTypeE > 0; 0 reproduces the zeroed struct the reference passes
+ * otherwise).  Derived rates as learnFF_post computes them (src/condShape.h:137-152),
+ * exp_homeo = expf(-dt / decayTimeHomeoFF) (src/patch.cu:1330); the homeostasis totals start
+ * from the current weights (src/patch.cu:4335-4352).  Plans with learning run one launch per
+ * step (no persistent kernel, no batches) and one spike per step at most;
+ * PV1_E_UNSUPPORTED otherwise. */
 typedef struct pv1_ff_learning {
-    int32_t learning;            /* 3 */
-    float tauLTP, tauLTD, tauTrip, tauAvg, targetFR;
+    int32_t learning;            /* 1, 2, 3 or 4 */
+    float tauLTP, tauLTD, tauTrip, tauAvg, targetFR;    /* FF->E type */
     float A_LGN, r_LTD, gmaxLGN, gminLGN, sRatioLGN;
     float decayTimeHomeoFF, FF_InfRatio;
     int32_t applyHomeo;          /* 0 none, 1 multiplicative, 2 additive */
     int32_t symmetricHomeo, rebound;
+    int32_t nLearnTypeFF_E;      /* 0 or 1; 0 with learning 4 */
+    int32_t nLearnTypeFF_I;      /* 0 or 1; 1 only with learning 2 */
+    float tauLTP_I, tauLTD_I, tauTrip_I, tauAvg_I, targetFR_I;   /* FF->I type */
+    float A_LGN_I, r_LTD_I, gmaxLGN_I, gminLGN_I, sRatioLGN_I;
+    float tauAvgCortical;        /* vAvgE's time constant in the delivery (learning 1, 2, 4) */
 } pv1_ff_learning;
 int pv1_set_ff_learning(pv1_plan *plan, const pv1_ff_learning *cfg);
-/* The derived constants pv1_set_ff_learning uses, for a step dt (host only, no device work):
- * out[0] A_LTP = A_LGN * sRatioLGN, out[1] A_ratio (the LTD rate; with targetFR > 0 scaled by
- * tauTrip / (tauLTD tauAvg_s^2) / 1000 / targetFR), out[2] gmax and out[3] gmin scaled by
- * sRatioLGN, out[4] exp_homeo -- learnFF_post (src/condShape.h:137-152) and src/patch.cu:1330. */
+/* The derived constants pv1_set_ff_learning uses for the FF->E type, for a step dt (host only,
+ * no device work): out[0] A_LTP = A_LGN * sRatioLGN, out[1] A_ratio (the LTD rate; with
+ * targetFR > 0 scaled by tauTrip / (tauLTD tauAvg_s^2) / 1000 / targetFR), out[2] gmax and
+ * out[3] gmin scaled by sRatioLGN, out[4] exp_homeo -- learnFF_post (src/condShape.h:137-152)
+ * and src/patch.cu:1330.  The FF->I type's come from the same function given its values in
+ * the FF->E fields. */
 int pv1_ff_learning_rates(const pv1_ff_learning *cfg, float dt, float *out5);
 
 /* Learning state (plans with learning): the LGN->V1 weights [maxLGN][nV1] (the reference's
- * LGN_V1_s, synapse-major), the post variables in the reference's learnVar layout
- * (src/patch.cu:4365-4385: vLTD_FF_E [nblock*nE], vTrip_FF_E [nblock*nE], vAvgE [nblock*nE][2],
- * vAvgI [nblock*nI]), the presynaptic LTP trace of each LGN cell at the end of the last step
- * [nLGN], and the homeostasis totals [2][nV1] (total, target). */
+ * LGN_V1_s, synapse-major), the post variables in the reference's learnVar FF layout
+ * (src/patch.cu:4365-4385: vLTD_FF_E [nE types][nblock*nE], vTrip_FF_E, vLTD_FF_I
+ * [nI types][nblock*nI], vTrip_FF_I, vAvgE [nblock*nE][2], vAvgI [nblock*nI]), the presynaptic
+ * LTP traces of each LGN cell at the end of the last step [nLearnTypeFF_E + nLearnTypeFF_I][nLGN],
+ * and the homeostasis totals [2][nV1] (total, target). */
 #define PV1_ST_SLGN     18
 #define PV1_ST_FF_POST  19
 #define PV1_ST_FF_PRE   20

@@ -59,6 +59,7 @@ def lib():
         L.orc_v1_set_ff_learning.argtypes = [P, P]
         L.orc_v1_learn_ff.argtypes = [P, FP, FP, FP]
         L.orc_ff_learning_rates.argtypes = [P, C.c_float, FP]
+        L.orc_v1_learn_avg.argtypes = [P]
         L.orc_parvo_max_sample1d.argtypes = [P, P, C.c_int]
         L.orc_lgn_parvo_setup.argtypes = [P, P, P, FP, FP, FP, FP, FP]
         L.orc_lgn_parvo_spatial.argtypes = [C.c_int, C.c_int, FP, FP, UP, FP, C.c_int, C.c_int, C.c_int,
@@ -254,17 +255,22 @@ class LgnOracle:
         self.last_sInfo = sInfo
         return sInfo, fr, mism
 
-    def ff_pre(self, tauLTP: float):
-        """The presynaptic learning trace over the step just computed by `nonlinear`
-        (self.ff_var carries it): returns (trace at the step start, right after the spikes)."""
+    def ff_pre(self, tauLTP: float, k: int = 0):
+        """Presynaptic learning trace k (0: the FF->E type's, 1: the FF->I type's) over the step
+        just computed by `nonlinear` (self.ff_vars[k] carries it): returns (trace at the step
+        start, right after the spikes)."""
         n = self.lgn.nLGN
-        if getattr(self, "ff_var", None) is None:
-            self.ff_var = np.zeros(n, f32)
+        if getattr(self, "ff_vars", None) is None:
+            self.ff_vars = [np.zeros(n, f32), np.zeros(n, f32)]
         start = np.zeros(n, f32)
         at = np.zeros(n, f32)
         lib().orc_lgn_ff_pre(n, f32(self.cfg.dt), f32(tauLTP), up(self.nsp), fp(self.tsp), fp(self.last_sInfo),
-                             fp(self.ff_var), fp(start), fp(at))
+                             fp(self.ff_vars[k]), fp(start), fp(at))
         return start, at
+
+    @property
+    def ff_var(self):
+        return self.ff_vars[0]
 
 
 class V1Oracle:
@@ -299,7 +305,9 @@ class V1Oracle:
         n = s.nV1
         size = dict(gFF=s.ngFF * n, hFF=s.ngFF * n, gE=s.ngE * n, hE=s.ngE * n, gI=s.ngI * n,
                     hI=s.ngI * n, sLGN=self._keep[1].shape[0] * n,
-                    ff_post=4 * s.nE * s.nblock + (s.blockSize - s.nE) * s.nblock, total_ff=2 * n).get(name, n)
+                    ff_post=((0 if getattr(self, "_ff_mode", 3) == 4 else 2 * s.nE * s.nblock) + 2 * s.nE * s.nblock +
+                             (1 + 2 * getattr(self, "_ff_i", 0)) * (s.blockSize - s.nE) * s.nblock),
+                    total_ff=2 * n).get(name, n)
         out = np.empty(size, f32)
         lib().orc_v1_get(self.h, ST[name], fp(out))
         return out
@@ -315,19 +323,17 @@ class V1Oracle:
 
     def set_ff_learning(self, learning):
         """LGN->V1 plasticity with the parameters of a model.FFLearning."""
-        from visual_cortex_gb300 import _native as N
-        self._ffl = N.FFLearning(learning=int(learning.learning), tauLTP=learning.tauLTP, tauLTD=learning.tauLTD,
-                                 tauTrip=learning.tauTrip, tauAvg=learning.tauAvg, targetFR=learning.targetFR,
-                                 A_LGN=learning.A_LGN, r_LTD=learning.r_LTD, gmaxLGN=learning.gmaxLGN,
-                                 gminLGN=learning.gminLGN, sRatioLGN=learning.sRatioLGN,
-                                 decayTimeHomeoFF=learning.decayTimeHomeoFF, FF_InfRatio=learning.FF_InfRatio,
-                                 applyHomeo=int(learning.applyHomeo), symmetricHomeo=int(learning.symmetricHomeo),
-                                 rebound=int(learning.rebound))
+        self._ffl = learning.to_struct()
+        self._ff_mode = int(learning.learning)
+        self._ff_i = int(learning.nLearnTypeFF_I) if self._ff_mode == 2 else 0
         if lib().orc_v1_set_ff_learning(self.h, C.byref(self._ffl)) != 0:
-            raise ValueError("the oracle restates learning = 3 only")
+            raise ValueError("learning modes 1-4 with nLearnTypeFF_E = 1 (0 with learning 4) are restated")
 
     def learn_ff(self, lgn_sInfo, pre_start, pre_spike):
         lib().orc_v1_learn_ff(self.h, fp(np.ascontiguousarray(lgn_sInfo, f32)), fp(pre_start), fp(pre_spike))
+
+    def learn_avg(self):
+        lib().orc_v1_learn_avg(self.h)
 
     def init_spikes(self, sp0, SCsplit, depth, rec):
         """rand_spInit with initial spikes and the delivery before the first step, from the

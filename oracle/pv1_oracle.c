@@ -633,11 +633,15 @@ typedef struct orc_v1 {
     /* far synaptic failure: libstdc++ minstd_rand0 states per post, chunks of blocks */
     uint32_t *farEng;
     int nChunk;
-    /* LGN->V1 plasticity (learning = 3) */
-    int learn;
-    float lTauLTP, lTauLTD, lTauTrip, lTauAvg, lTargetFR, lA_LTP, lA_ratio, lGmax, lGmin, lExpHomeo;
+    /* LGN->V1 plasticity (learning 1-4) */
+    int learn;       /* the reference's `learning` (0: off) */
+    int ffI;         /* FF->I type on (learning 2) */
+    float lt[2][9];  /* per type (FF->E, FF->I): tauLTP, tauLTD, tauTrip, tauAvg, targetFR, A_LTP, A_ratio, gmax, gmin */
+    float lExpHomeo, tauAvgCortical;
     int applyHomeo, symmetricHomeo, rebound;
-    float *ffPost;   /* vLTD_FF_E [nblock*nE], vTrip_FF_E [nblock*nE], vAvgE [nblock*nE][2], vAvgI [nblock*nI] */
+    float *ffPost;   /* vLTD_FF_E, vTrip_FF_E [nblock*nE], vLTD_FF_I, vTrip_FF_I [nblock*nI] (with FF->I),
+                        vAvgE [nblock*nE][2], vAvgI [nblock*nI] */
+    size_t offI, offAvgE, offAvgI;
     float *totalFF;  /* [2][nV1] */
 } orc_v1;
 
@@ -746,7 +750,7 @@ static float *oarr(orc_v1 *o, int which, size_t *cnt) {
         case PV1_ST_HI: *cnt = o->c.ngI * n; return o->hI;
         case PV1_ST_SINFO: return o->sInfo;
         case PV1_ST_SLGN: *cnt = (size_t)o->maxLGN * n; return o->sLGN;
-        case PV1_ST_FF_POST: *cnt = 4 * (size_t)o->nE * o->nblock + (size_t)o->nI * o->nblock; return o->ffPost;
+        case PV1_ST_FF_POST: *cnt = o->offAvgI + (size_t)o->nI * o->nblock; return o->ffPost;
         case PV1_ST_TOTAL_FF: *cnt = 2 * n; return o->totalFF;
         default: return NULL;
     }
@@ -1715,19 +1719,35 @@ void orc_ff_learning_rates(const pv1_ff_learning *l, float dt, float *out) {
 }
 
 int orc_v1_set_ff_learning(orc_v1 *o, const pv1_ff_learning *l) {
-    if (l->learning != 3) return -1;
-    float r[5];
-    orc_ff_learning_rates(l, o->c.dt, r);
-    o->learn = 1;
-    o->lTauLTP = l->tauLTP; o->lTauLTD = l->tauLTD; o->lTauTrip = l->tauTrip; o->lTauAvg = l->tauAvg;
-    o->lTargetFR = l->targetFR; o->lA_LTP = r[0]; o->lA_ratio = r[1];
-    o->lGmax = r[2]; o->lGmin = r[3];
-    o->lExpHomeo = r[4];
+    if (l->learning < 1 || l->learning > 4) return -1;
+    const int nE_ = l->learning == 4 ? 0 : l->nLearnTypeFF_E;
+    const int nI_ = l->learning == 2 ? l->nLearnTypeFF_I : 0;
+    if (l->learning != 4 && nE_ != 1) return -1;
+    for (int k = 0; k < 2; k++) {
+        pv1_ff_learning q = *l;
+        if (k) {
+            q.tauLTP = l->tauLTP_I; q.tauLTD = l->tauLTD_I; q.tauTrip = l->tauTrip_I; q.tauAvg = l->tauAvg_I;
+            q.targetFR = l->targetFR_I; q.A_LGN = l->A_LGN_I; q.r_LTD = l->r_LTD_I; q.gmaxLGN = l->gmaxLGN_I;
+            q.gminLGN = l->gminLGN_I; q.sRatioLGN = l->sRatioLGN_I;
+        }
+        float r[5];
+        orc_ff_learning_rates(&q, o->c.dt, r);
+        const float t[9] = {q.tauLTP, q.tauLTD, q.tauTrip, q.tauAvg, q.targetFR, r[0], r[1], r[2], r[3]};
+        memcpy(o->lt[k], t, sizeof(t));
+        if (!k) o->lExpHomeo = r[4];
+    }
+    o->learn = l->learning;
+    o->ffI = nI_;
+    o->tauAvgCortical = l->tauAvgCortical;
     o->applyHomeo = l->applyHomeo; o->symmetricHomeo = l->symmetricHomeo != 0; o->rebound = l->rebound != 0;
-    const size_t n = (size_t)o->nV1;
+    const size_t n = (size_t)o->nV1, nEt = (size_t)o->nE * o->nblock, nIt = (size_t)o->nI * o->nblock;
+    /* learnVar's FF block (src/patch.cu:4367-4392): learning 4 has no FF->E traces */
+    o->offI = l->learning == 4 ? 0 : 2 * nEt;
+    o->offAvgE = o->offI + 2 * (size_t)nI_ * nIt;
+    o->offAvgI = o->offAvgE + 2 * nEt;
     free(o->ffPost);
     free(o->totalFF);
-    o->ffPost = (float *)calloc(4 * (size_t)o->nE * o->nblock + (size_t)o->nI * o->nblock + 1, sizeof(float));
+    o->ffPost = (float *)calloc(o->offAvgI + nIt + 1, sizeof(float));
     o->totalFF = (float *)calloc(2 * n, sizeof(float));
     for (size_t i = 0; i < n; i++) {
         float t = 0.f;
@@ -1741,28 +1761,40 @@ int orc_v1_set_ff_learning(orc_v1 *o, const pv1_ff_learning *l) {
 static inline float odecay(float x, float tau, float dt) { return x * expf(-dt / tau); }
 
 /* The learning block of compute_V_collect_spike_learnFF_fast (src/coredynamics.cu:1631-1993)
- * for learning = 3, every excitatory neuron, after orc_v1_compute_v (whose spike words it
- * reads): lgnSInfo are the step's LGN spike words, pre_start / pre_spike the presynaptic
- * traces at the step start and right after each LGN cell's spikes (orc_lgn_ff_pre). */
+ * for learning 1-3, after orc_v1_compute_v (whose spike words it reads): every excitatory
+ * neuron with the FF->E type, and with learning 2 every inhibitory neuron with the FF->I type.
+ * lgnSInfo are the step's LGN spike words, pre_start / pre_spike presynaptic trace 0 at the
+ * step start and right after each LGN cell's spikes (orc_lgn_ff_pre): the inhibitory posts'
+ * LTP reads trace 0 as the reference's does (its surface layer 1 + 3j with j from 0).  With
+ * learning != 3 the excitatory filtered rate is left to orc_v1_learn_avg, its value at the
+ * spike time stored in the second slot. */
 int orc_v1_learn_ff(orc_v1 *o, const float *lgnSInfo, const float *pre_start, const float *pre_spike) {
-    if (!o->learn) return -1;
+    if (!o->learn || o->learn == 4) return -1;
     const size_t n = (size_t)o->nV1;
     const float dt = o->c.dt;
-    const int nEt = o->nE * o->nblock;
-    float *vLTD = o->ffPost, *vTrip = o->ffPost + nEt, *vAvgE = o->ffPost + 2 * nEt;
+    const size_t nEt = (size_t)o->nE * o->nblock, nIt = (size_t)o->nI * o->nblock;
     for (int b = 0; b < o->nblock; b++) {
-        for (int j = 0; j < o->nE; j++) {
+        for (int j = 0; j < o->bs; j++) {
+            const int isE = j < o->nE;
+            if (!isE && !o->ffI) continue;
+            const float *T = o->lt[isE ? 0 : 1];
+            const float tLTP = T[0], tLTD = T[1], tTrip = T[2], tAvg = T[3], tFR = T[4], ALTP = T[5], Ar = T[6];
+            const float gmax = T[7], gmin = T[8];
             const size_t i = (size_t)b * o->bs + j;
-            const int eid = b * o->nE + j;
+            const size_t id = isE ? (size_t)b * o->nE + j : (size_t)b * o->nI + (j - o->nE);
+            float *vLTD = isE ? o->ffPost : o->ffPost + o->offI;
+            float *vTrip = isE ? o->ffPost + nEt : o->ffPost + o->offI + nIt;
+            float *vAvg = isE ? o->ffPost + o->offAvgE + 2 * id : o->ffPost + o->offAvgI + id;
             const float sI = o->sInfo[i];
             float nsp, tsp;
             if (sI > 0) { nsp = floorf(sI); tsp = (sI - nsp) * dt; }
             else { nsp = 0; tsp = dt; }
-            float LTD[2] = {vLTD[eid], 0.f}, Trip[2] = {vTrip[eid], 0.f}, Avg[2] = {vAvgE[2 * eid], 0.f};
+            float LTD[2] = {vLTD[id], 0.f}, Trip[2] = {vTrip[id], 0.f}, Avg[2] = {vAvg[0], 0.f};
             if (nsp > 0) {
-                LTD[1] = odecay(LTD[0], o->lTauLTD, tsp);
-                Trip[1] = odecay(Trip[0], o->lTauTrip, tsp);
-                Avg[1] = odecay(Avg[0], o->lTauAvg, tsp);
+                LTD[1] = odecay(LTD[0], tLTD, tsp);
+                Trip[1] = odecay(Trip[0], tTrip, tsp);
+                Avg[1] = odecay(Avg[0], tAvg, tsp);
+                if (isE && o->learn != 3) vAvg[1] = Avg[1];
             }
             const uint32_t m = o->nLGN[i];
             float new0 = 0.f, ch = 0.f, dsum = 0.f;
@@ -1783,41 +1815,60 @@ int orc_v1_learn_ff(orc_v1 *o, const float *lgnSInfo, const float *pre_start, co
                 if (f == 0 && !o->rebound) continue;
                 if (o->applyHomeo == 1) f *= ch;
                 else if (o->applyHomeo == 2) f += ch;
-                const uint32_t id = o->lgnId[lid];
-                const float sFF = lgnSInfo[id];
+                const uint32_t cell = o->lgnId[lid];
+                const float sFF = lgnSInfo[cell];
                 const uint32_t nspFF = (uint32_t)floorf(sFF);
                 const float tspFF = (sFF > 0 ? sFF - (float)nspFF : 1.f) * dt;
                 if (nspFF > 0) {
                     const int c = tspFF < tsp ? 0 : 1;
                     const float delta_t = c == 0 ? tspFF : tspFF - tsp;
-                    float A = o->lA_ratio;
-                    if (o->lTargetFR > 0) A *= o->lTauLTP * Avg[c] * Avg[c];
-                    const float df = odecay(LTD[c], o->lTauLTD, delta_t) * A;
+                    float A = Ar;
+                    if (tFR > 0) A *= tLTP * Avg[c] * Avg[c];
+                    const float df = odecay(LTD[c], tLTD, delta_t) * A;
                     f -= df;
                     if (o->applyHomeo) dsum -= df;
                 }
                 if (nsp > 0) {
                     const int early = tspFF < tsp;
-                    const float lpre = early ? pre_spike[id] : pre_start[id];
+                    const float lpre = early ? pre_spike[cell] : pre_start[cell];
                     const float delta_t = early ? tsp - tspFF : tsp;
-                    const float df = odecay(lpre, o->lTauLTP, delta_t) * Trip[1] * o->lA_LTP;
+                    const float df = odecay(lpre, tLTP, delta_t) * Trip[1] * ALTP;
                     if (o->applyHomeo) dsum += df;
                     f += df;
                 }
-                if (f < o->lGmin) { if (o->applyHomeo) dsum += o->lGmin - f; f = o->lGmin; }
-                if (f > o->lGmax) { if (o->applyHomeo) dsum -= f - o->lGmax; f = o->lGmax; }
+                if (f < gmin) { if (o->applyHomeo) dsum += gmin - f; f = gmin; }
+                if (f > gmax) { if (o->applyHomeo) dsum -= f - gmax; f = gmax; }
                 o->sLGN[lid] = f;
             }
             if (o->applyHomeo) o->totalFF[i] = new0 + dsum;
             const int c = nsp > 0 ? 1 : 0;
             float delta_t = dt;
             if (nsp > 0) delta_t -= tsp;
-            LTD[c] = odecay(LTD[c] + nsp, o->lTauLTD, delta_t);
-            Trip[c] = odecay(Trip[c] + nsp, o->lTauTrip, delta_t);
-            Avg[c] = odecay(Avg[c] + nsp, o->lTauAvg, delta_t);
-            vLTD[eid] = LTD[c];
-            vTrip[eid] = Trip[c];
-            vAvgE[2 * eid] = Avg[c];
+            vLTD[id] = odecay(LTD[c] + nsp, tLTD, delta_t);
+            vTrip[id] = odecay(Trip[c] + nsp, tTrip, delta_t);
+            if (!isE || o->learn == 3) vAvg[0] = odecay(Avg[c] + nsp, tAvg, delta_t);
+        }
+    }
+    return 0;
+}
+
+/* The excitatory filtered rate of learning 1, 2 and 4 advanced over the step just computed,
+ * as recal_G_mat_nd_fast does after its conductance sums (src/coredynamics.cu:2866-2890): from
+ * the spike-time value (second slot) when the neuron spiked, else the step start value, plus
+ * the spike count, decayed by dt (1 - tsp/dt) or dt with the cortical E types' tauAvg. */
+int orc_v1_learn_avg(orc_v1 *o) {
+    if (!o->learn || o->learn == 3) return -1;
+    const float dt = o->c.dt;
+    for (int b = 0; b < o->nblock; b++) {
+        for (int j = 0; j < o->nE; j++) {
+            const float ps = o->sInfo[(size_t)b * o->bs + j];
+            const float postNsp = floorf(ps);
+            const float postTsp = ps > 0 ? ps - postNsp : 1.f;
+            const int c = postNsp > 0 ? 1 : 0;
+            float *vAvg = o->ffPost + o->offAvgE + 2 * ((size_t)b * o->nE + j);
+            float delta_t = dt;
+            if (postNsp > 0) delta_t = dt * (1 - postTsp);
+            vAvg[0] = odecay(vAvg[c] + postNsp, o->tauAvgCortical, delta_t);
         }
     }
     return 0;

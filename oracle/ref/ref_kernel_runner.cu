@@ -607,9 +607,10 @@ static void mode_v1run(const Bundle &in, Writer &out) {
 }
 
 // ---- v1learn: rand_spInit, then T steps of compute_V_collect_spike_learnFF_fast with
-// learning = 3 + recal_G_mat_nd_fast, the presynaptic traces given per step (surface layer
-// 1 + varSlot: the step start, layer 3: right after the LGN spikes); the learning structs
-// come as bytes ("lFF_E_pre", "lFF_E_post", in the reference's layout) ----
+// learning 1-3 + recal_G_mat_nd_fast, the presynaptic traces given per step (surface layer
+// 1 + varSlot: the step start, layer 3: right after the LGN spikes -- the only trace layers the
+// V1 kernel reads); the learning structs come as bytes in the reference's layout ("lFF_E_pre",
+// "lFF_E_post", "lFF_I_pre", "lFF_I_post", "lE") ----
 static void mode_v1learn(const Bundle &in, Writer &out) {
     V1 m = make_v1(in);
     const size_t n = m.nV1;
@@ -622,6 +623,8 @@ static void mode_v1learn(const Bundle &in, Writer &out) {
     auto preStart = get<float>(in, "preStart");  // [T][nLGNcells]
     auto preSpk = get<float>(in, "preSpk");      // [T][nLGNcells]
     auto ePre = get<u8>(in, "lFF_E_pre"), ePost = get<u8>(in, "lFF_E_post");
+    auto iPre = get<u8>(in, "lFF_I_pre"), iPost = get<u8>(in, "lFF_I_post"), lEs = get<u8>(in, "lE");
+    const int learning = scalar<int>(in, "learning");
     const float expHomeo = scalar<float>(in, "expHomeo");
     const int applyHomeo = scalar<int>(in, "applyHomeo");
     const bool symmetricHomeo = scalar<int>(in, "symmetricHomeo") != 0, rebound = scalar<int>(in, "rebound") != 0;
@@ -635,11 +638,15 @@ static void mode_v1learn(const Bundle &in, Writer &out) {
     const unsigned nTypeE = scalar<unsigned>(in, "nTypeE");
     const size_t nEt = (size_t)m.nE * m.nblock, nIt = (size_t)m.nI * m.nblock;
     float *vLTD = dev<float>(nEt), *vTrip = dev<float>(nEt), *vAvgE = dev<float>(2 * nEt), *vAvgI = dev<float>(nIt + 1);
+    float *vLTDi = dev<float>(nIt), *vTripi = dev<float>(nIt);
+    // the cortical learning variables (read and written at spikes by the V1 kernel, used by
+    // nothing else): zeroed, generously sized
+    float *cort = dev<float>((size_t)8 * m.trainDepth * n + 64);
     float *none = dev<float>(64);
     auto tot = get<float>(in, "totalFF");        // [2][nV1]
     CK(cudaMemcpy(m.totalFF, tot.data(), n * sizeof(float), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(m.totalFF_inf, tot.data() + n, n * sizeof(float), cudaMemcpyHostToDevice));
-    std::vector<unsigned char> zE(60, 0), zQ(28, 0), zIpost(36, 0), zIpre(8, 0);
+    std::vector<unsigned char> zQ(28, 0);
     std::vector<float> raster;
     const size_t plane = (size_t)nsx * nsy;
     std::vector<float> layers(4 * plane, 0.f);
@@ -657,7 +664,7 @@ static void mode_v1learn(const Bundle &in, Writer &out) {
             Launch L("compute_V_collect_spike_learnFF_fast");
             L.a(m.v).a(m.dep).a(m.w).a(m.gapS).a(m.gFF).a(m.hFF).a(m.ddgE).a(m.ddgI).a(m.ddhE).a(m.ddhI).a(m.ddgap);
             L.a(m.nLGN).a(m.sLGN).a(m.lgnx).a(m.lgny).a(m.tBack).a(m.spikeTrain);
-            L.a(vLTD).a(vTrip).a(none).a(none).a(vAvgE).a(vAvgI).a(none).a(none).a(none).a(none).a(none);
+            L.a(vLTD).a(vTrip).a(vLTDi).a(vTripi).a(vAvgE).a(vAvgI).a(cort).a(cort).a(cort).a(cort).a(cort);
             L.a(m.pFF).a(m.vR).a(m.vThres).a(m.gL).a(m.C).a(m.tRef).a(m.tonic).a(m.vT).a(m.deltaT).a(m.tau_w);
             L.a(m.a).a(m.b).a(m.dTypeAcc).a(m.rGenCond).a(m.synFailFF).a(m.synPerConFF).a(m.rNoisy).a(m.noisyDep);
             L.a(m.last_noise).a(m.ipre).a(m.npre).a(m.og).a(m.oh).a(m.totalFF).a(m.totalFF_inf);
@@ -666,10 +673,10 @@ static void mode_v1learn(const Bundle &in, Writer &out) {
             L.raw(m.condE.data(), m.condE.size());
             L.raw(m.condI.data(), m.condI.size());
             L.a(m.dt).a(m.nblock).a(m.nblock).a((unsigned)1).a((unsigned)1).a(m.nE).a(m.nI).a(m.nV1);
-            L.a((int)3).a((int)varSlot).a(m.nType).a(surf.obj);
-            L.raw(ePre.data(), ePre.size()).raw(zIpre.data(), zIpre.size());
-            L.raw(ePost.data(), ePost.size()).raw(zIpost.data(), zIpost.size());
-            L.raw(zE.data(), zE.size()).raw(zQ.data(), zQ.size());
+            L.a(learning).a((int)varSlot).a(m.nType).a(surf.obj);
+            L.raw(ePre.data(), ePre.size()).raw(iPre.data(), iPre.size());
+            L.raw(ePost.data(), ePost.size()).raw(iPost.data(), iPost.size());
+            L.raw(lEs.data(), lEs.size()).raw(zQ.data(), zQ.size());
             L.a(expHomeo).a(iModel).a((int)1).a(applyHomeo).a(symmetricHomeo).a(false).a(rebound);
             L.a(scalar<int>(in, "noiseOnTonic") != 0);
             L.go(m.nblock, 1, m.bs, 1);
@@ -680,13 +687,14 @@ static void mode_v1learn(const Bundle &in, Writer &out) {
             Launch L("recal_G_mat_nd_fast");
             L.a(m.spikeTrain + (size_t)m.nV1 * slot).a(m.ipre).a(m.npre).a(m.og).a(m.oh).a(m.conMat).a(m.gapMat);
             L.a(m.nNB).a(m.nbId).a(m.gE).a(m.gI).a(m.hE).a(m.hI).a(m.gap);
-            L.a(vAvgE).a(none).a(none).a(none).a(none).a(none);
+            L.a(vAvgE).a(cort).a(cort).a(cort).a(cort).a(cort);
             L.a(m.pE).a(m.pI).a(m.dTypeAcc).a(m.rGenCond).a(m.synFail).a(m.synPerCon).a(m.vThres);
             L.a(m.dt);
             L.raw(m.condE.data(), m.condE.size());
             L.raw(m.condI.data(), m.condI.size());
-            L.a(m.ngE).a(m.ngI).a(m.nnb).a(m.nE).a(m.nI).a(m.nV1).a((int)3).a((unsigned)0).a(m.nType);
-            L.a(nTypeE).a(m.nType - nTypeE).a(m.nblock).zero().zero().a((unsigned)0).a(it).a(false);
+            L.a(m.ngE).a(m.ngI).a(m.nnb).a(m.nE).a(m.nI).a(m.nV1).a(learning).a((unsigned)0).a(m.nType);
+            L.a(nTypeE).a(m.nType - nTypeE).a(m.nblock).raw(lEs.data(), lEs.size()).raw(zQ.data(), zQ.size());
+            L.a((unsigned)0).a(it).a(false);
             L.go(m.nblock, 1, m.bs, 1, shmem);
         }
         auto row = host(m.spikeTrain + (size_t)m.nV1 * slot, n);
@@ -696,7 +704,10 @@ static void mode_v1learn(const Bundle &in, Writer &out) {
     out.putv("sLGN", "f4", host(m.sLGN, (size_t)m.maxLGN * n));
     out.putv("vLTD", "f4", host(vLTD, nEt));
     out.putv("vTrip", "f4", host(vTrip, nEt));
+    out.putv("vLTDi", "f4", host(vLTDi, nIt));
+    out.putv("vTripi", "f4", host(vTripi, nIt));
     out.putv("vAvgE", "f4", host(vAvgE, 2 * nEt));
+    out.putv("vAvgI", "f4", host(vAvgI, nIt));
     out.putv("totalFF", "f4", host(m.totalFF, n));
 }
 

@@ -192,22 +192,75 @@ def learning_params():
                       FF_InfRatio=0.9, applyHomeo=1)
 
 
-def learning_structs(L, dt: float):
-    """The bytes of LearnVarShapeFF_E_pre and LearnVarShapeFF_E_post (src/condShape.h:85-126)
-    for one FF_E type, with the derived constants of pv1_ff_learning_rates (held bit for bit
-    to learnFF_post by tests/test_golden.py), and exp_homeo."""
+def learning_params2():
+    """The FFLearning of the learning = 2 case: both FF types (FF->I with its own constants,
+    targetFR[1] > 0), one cortical E type (its tauAvg filters vAvgE in the delivery), additive
+    homeostasis.  targetFR[0] is 0: with learning != 3 the delivery adds floor(spike word) --
+    the membrane potential, about -60, when the neuron did not spike -- to vAvgE every step
+    (src/coredynamics.cu:2548-2560), so vAvgE runs to about -7000 within 100 steps, and with
+    targetFR[0] > 0 the LTD factor tauLTP vAvgE^2 clips every active FF->E weight to gmin at
+    its first LGN spike; the homeostasis total is then the difference of terms of that size
+    and carries their rounding (ulps of 1e4), the same on no two machines."""
+    from visual_cortex_gb300.model import FFLearning
+    return FFLearning(tauLTP=16.8, tauLTD=33.7, tauTrip=114.0, tauAvg=1000.0, targetFR=0.0, A_LGN=0.02,
+                      r_LTD=1.0, gmaxLGN=0.6, gminLGN=0.0, sRatioLGN=1.0, decayTimeHomeoFF=250.0,
+                      FF_InfRatio=0.9, applyHomeo=2, learning=2, nLearnTypeFF_E=1, nLearnTypeFF_I=1,
+                      tauLTP_I=20.0, tauLTD_I=40.0, tauTrip_I=90.0, tauAvg_I=800.0, targetFR_I=5.0, A_LGN_I=0.015,
+                      r_LTD_I=0.8, gmaxLGN_I=0.8, gminLGN_I=0.0, sRatioLGN_I=1.2, tauAvgCortical=1000.0)
+
+
+def learning_params4():
+    """The FFLearning of the learning = 4 case: no FF learning (the LGN->V1 weights stay), the
+    excitatory filtered rate in the delivery with one cortical E type's tauAvg."""
+    from visual_cortex_gb300.model import FFLearning
+    return FFLearning(tauLTP=16.8, tauLTD=33.7, tauTrip=114.0, tauAvg=1000.0, targetFR=2.0, A_LGN=0.02,
+                      r_LTD=1.0, gmaxLGN=0.6, gminLGN=0.0, sRatioLGN=1.0, decayTimeHomeoFF=250.0,
+                      FF_InfRatio=1.0, applyHomeo=0, learning=4, tauAvgCortical=700.0)
+
+
+def _type_structs(tauLTP, tauLTD, tauTrip, tauAvg, targetFR, A_LGN, r_LTD, gmax, gmin, ratio, L, dt):
     import ctypes as C
     from visual_cortex_gb300 import _native as N
-    cfg = N.FFLearning(learning=3, tauLTP=L.tauLTP, tauLTD=L.tauLTD, tauTrip=L.tauTrip, tauAvg=L.tauAvg,
-                       targetFR=L.targetFR, A_LGN=L.A_LGN, r_LTD=L.r_LTD, gmaxLGN=L.gmaxLGN, gminLGN=L.gminLGN,
-                       sRatioLGN=L.sRatioLGN, decayTimeHomeoFF=L.decayTimeHomeoFF, FF_InfRatio=L.FF_InfRatio,
-                       applyHomeo=int(L.applyHomeo), symmetricHomeo=int(L.symmetricHomeo), rebound=int(L.rebound))
+    cfg = N.FFLearning(learning=3, tauLTP=tauLTP, tauLTD=tauLTD, tauTrip=tauTrip, tauAvg=tauAvg, targetFR=targetFR,
+                       A_LGN=A_LGN, r_LTD=r_LTD, gmaxLGN=gmax, gminLGN=gmin, sRatioLGN=ratio,
+                       decayTimeHomeoFF=L.decayTimeHomeoFF, FF_InfRatio=L.FF_InfRatio)
     r = np.zeros(5, f32)
     assert N.lib.pv1_ff_learning_rates(C.byref(cfg), f32(dt), N.fptr(r)) == 0
-    pre = np.array([1], u32).tobytes() + np.array([L.tauLTP], f32).tobytes()
-    post = np.array([1], u32).tobytes() + np.array([L.tauLTD, L.tauTrip, L.tauAvg, r[0], r[1], L.targetFR, r[2], r[3]],
+    pre = np.array([1], u32).tobytes() + np.array([tauLTP], f32).tobytes()
+    post = np.array([1], u32).tobytes() + np.array([tauLTD, tauTrip, tauAvg, r[0], r[1], targetFR, r[2], r[3]],
                                                    f32).tobytes()
     return np.frombuffer(pre, u8).copy(), np.frombuffer(post, u8).copy(), f32(r[4])
+
+
+def learning_structs(L, dt: float):
+    """The bytes of LearnVarShapeFF_E_pre and LearnVarShapeFF_E_post (src/condShape.h:85-126)
+    for the FF->E type, with the derived constants of pv1_ff_learning_rates (held bit for bit
+    to learnFF_post by tests/test_golden.py), and exp_homeo."""
+    return _type_structs(L.tauLTP, L.tauLTD, L.tauTrip, L.tauAvg, L.targetFR, L.A_LGN, L.r_LTD, L.gmaxLGN,
+                         L.gminLGN, L.sRatioLGN, L, dt)
+
+
+def learning_structs_i(L, dt: float):
+    """LearnVarShapeFF_I_pre / _post of the FF->I type (zeroed when it is off)."""
+    if not (L.learning == 2 and L.nLearnTypeFF_I):
+        return np.zeros(8, u8), np.zeros(36, u8)
+    pre, post, _ = _type_structs(L.tauLTP_I, L.tauLTD_I, L.tauTrip_I, L.tauAvg_I, L.targetFR_I, L.A_LGN_I, L.r_LTD_I,
+                                 L.gmaxLGN_I, L.gminLGN_I, L.sRatioLGN_I, L, dt)
+    return pre, post
+
+
+def cortical_struct(L):
+    """LearnVarShapeE (src/condShape.h:159-167) with one cortical E type whose tauAvg is
+    L.tauAvgCortical (learnE, src/condShape.cu:22-36; the other fields only shape variables no
+    output holds), or zeroed when L.tauAvgCortical is 0."""
+    if not L.tauAvgCortical:
+        return np.zeros(60, u8)
+    tau = np.zeros(7, f32)
+    tau[0:3] = (L.tauLTP, L.tauLTD, L.tauTrip)
+    tau[3] = L.tauAvgCortical
+    b = (np.array([1], u32).tobytes() + tau.tobytes() + np.zeros(2, f32).tobytes() + np.zeros(2, f32).tobytes() +
+         np.array([L.targetFR, L.gmaxLGN, L.gminLGN], f32).tobytes())
+    return np.frombuffer(b, u8).copy()
 
 
 def lgn_learn_case() -> dict:
@@ -237,12 +290,12 @@ def pre_traces(lgn_rows, dt: float, tauLTP: float):
     return start, spk
 
 
-def learning_totals(net):
+def learning_totals(net, L=None):
     """The homeostasis totals of src/patch.cu:4335-4352: each neuron's LGN weights summed in
     synapse order (float), and that times FF_InfRatio."""
     n = net.sLGN.shape[1]
     tot = np.zeros(2 * n, f32)
-    L = learning_params()
+    L = learning_params() if L is None else L
     for i in range(n):
         t = f32(0)
         for j in range(int(net.nLGNperV1[i])):
@@ -252,12 +305,17 @@ def learning_totals(net):
     return tot
 
 
-def v1_learn_inputs(wl, lgn_rows, T: int) -> dict:
-    L = learning_params()
+def v1_learn_inputs(wl, lgn_rows, T: int, L=None) -> dict:
+    L = learning_params() if L is None else L
     d = v1_inputs(wl, lgn_rows=lgn_rows, T=T)
     pre, post, eh = learning_structs(L, wl.spec.dt)
+    if L.learning == 4:
+        # nLearnTypeFF_E = 0: the reference passes zeroed FF_E structs (src/patch.cu:1174, 1281-1300)
+        pre, post = np.zeros_like(pre), np.zeros_like(post)
+    ipre, ipost = learning_structs_i(L, wl.spec.dt)
     start, spk = pre_traces(np.asarray(lgn_rows[:T], f32), wl.spec.dt, L.tauLTP)
-    d.update(lFF_E_pre=pre, lFF_E_post=post, expHomeo=scalar(eh, f32), applyHomeo=scalar(int(L.applyHomeo), i32),
+    d.update(learning=scalar(int(L.learning), i32), lFF_E_pre=pre, lFF_E_post=post, lFF_I_pre=ipre, lFF_I_post=ipost,
+             lE=cortical_struct(L), expHomeo=scalar(eh, f32), applyHomeo=scalar(int(L.applyHomeo), i32),
              symmetricHomeo=scalar(int(L.symmetricHomeo), i32), rebound=scalar(int(L.rebound), i32),
-             preStart=start.reshape(-1), preSpk=spk.reshape(-1), totalFF=learning_totals(wl.net))
+             preStart=start.reshape(-1), preSpk=spk.reshape(-1), totalFF=learning_totals(wl.net, L))
     return d

@@ -52,8 +52,9 @@ def run(mode, inputs):
 def learning(out_path):
     """ref_learning.npz: LGN_nonlinear with learning = 3 (the presynaptic trace of each cell per
     step: at the end, at the start, right after its spikes) on the LGN case, and 120 V1 steps of
-    compute_V_collect_spike_learnFF_fast with learning = 3 + recal_G_mat_nd_fast on the LGN
-    spike words of the library's own run, the presynaptic traces given per step."""
+    compute_V_collect_spike_learnFF_fast + recal_G_mat_nd_fast with learning = 3 (v1_*), learning = 2
+    (v2_*) and learning = 4 (v4_*) on the LGN spike words of the library's own run, the presynaptic traces
+    given per step."""
     res = {}
     lo = run("lgnlearn", RC.lgn_learn_case())
     for k, v in lo.items():
@@ -77,6 +78,15 @@ def learning(out_path):
         res["v1_in_" + k] = vi[k]
     for k, v in o.items():
         res["v1_" + k] = v
+    # learning = 2: both FF types, vAvgE through the delivery with a cortical E type's tauAvg
+    v2 = RC.v1_learn_inputs(wl, np.asarray(lsp, np.float32), RC.LEARN_T, RC.learning_params2())
+    o2 = run("v1learn", v2)
+    for k, v in o2.items():
+        res["v2_" + k] = v
+    # learning = 4: no FF learning, vAvgE through the delivery only
+    o4 = run("v1learn", RC.v1_learn_inputs(wl, np.asarray(lsp, np.float32), RC.LEARN_T, RC.learning_params4()))
+    for k, v in o4.items():
+        res["v4_" + k] = v
     np.savez_compressed(out_path, **res)
     print(f"wrote {out_path}: {len(res)} arrays; v1: {(o['raster'] >= 1).sum()} V1 spikes, "
           f"max |dw| {np.abs(o['sLGN'] - wl.net.sLGN.reshape(-1)).max():.3g}")

@@ -48,7 +48,7 @@ def test_scaling_rules(written):
 def test_unsupported_keys_fail_loudly(written):
     _, fn = written
     with pytest.raises(cfg.ConfigError, match="learning"):
-        driver.build(cfg.load(["-c", fn, "--learning", "1"]))
+        driver.build(cfg.load(["-c", fn, "--learning", "1", "--learnData_FF", "2"]))
     with pytest.raises(cfg.ConfigError, match="noFarDelay"):
         driver.build(cfg.load(["-c", fn, "--noDelay", "0", "--noFarDelay", "1"]))
     m = driver.build(cfg.load(["-c", fn, "--noDelay", "0", "--noFarDelay", "0"]))
@@ -412,13 +412,66 @@ def test_read_feature_rules():
             driver.build(cfg.load(["-c", fn] + bad))
 
 
+LEARN_CFG = dict(tauLTP=[16.8], tauLTD=[33.7], tauTrip=[114.0], tauAvg=[1000.0, 800.0], targetFR=[2.0, 5.0],
+                 A_LGN=[0.02, 0.015], r_LTD=[1.0], gmaxLGN=[0.6, 0.8], gminLGN=[0.0], applyHomeo=1,
+                 FF_InfRatio=0.95, sampleInterval_LGN_V1=32, store_dsLGN=True, gmaxE=[1.0], gminE=[0.0], A_V1=[0.01])
+
+
+def _learn_cfg(tmp, learning, **kw):
+    wl = synth.make_workload("learnc", seed=3, nblock=1, n_lgn=256, m=10, width=32, height=32, nt=8,
+                             adex_inh=True, nFrame=8)
+    # the reference refuses more gmaxLGN values than FF types
+    extra = dict(LEARN_CFG, learning=learning, gmaxLGN=[0.6, 0.8] if learning == 2 else [0.6])
+    extra.update(kw)
+    fn = synth.write_reference_files(wl, tmp, seed=3, nt=8, extra=extra)
+    return cfg.load(["-c", fn])
+
+
+def test_learning_modes_from_the_cfg(tmp_path):
+    """The cfg rules of src/patch.cu:1092-1330 for learning 1-4: the mode's overrides of the
+    type counts, the FF->I type from element [nLearnTypeFF_E] with tauAvg[1], targetFR[1] and
+    sRatioLGN[1], the delivery's filtered-rate time constant tauAvg[0] while cortical E types
+    exist, and the reference's refusals."""
+    c = _learn_cfg(str(tmp_path / "a"), 2)
+    m = driver.build(c)
+    sr = m.extra["sRatioLGN"]
+    L = driver._ff_learning(c, sr)
+    assert (L.learning, L.nLearnTypeFF_E, L.nLearnTypeFF_I) == (2, 1, 1)
+    assert L.A_LGN == 0.02 and L.A_LGN_I == 0.015 and L.gmaxLGN_I == 0.8 and L.gminLGN_I == 0.0
+    assert L.tauAvg == 1000.0 and L.tauAvg_I == 800.0 and L.targetFR_I == 5.0 and L.sRatioLGN_I == float(sr[1])
+    assert L.tauLTP_I == 16.8 and L.tauAvgCortical == 1000.0
+    assert driver._learn_types(c) == (1, 1, 1)
+    assert len(driver._ltd_ratio(L, 1, 1)) == 2
+    c1 = _learn_cfg(str(tmp_path / "b"), 1)
+    L1 = driver._ff_learning(c1, sr)
+    assert L1.nLearnTypeFF_I == 0 and L1.tauAvgCortical == 1000.0
+    c1e = _learn_cfg(str(tmp_path / "b2"), 1, nLearnTypeE=0)
+    assert driver._ff_learning(c1e, sr).tauAvgCortical == 0.0
+    c3 = _learn_cfg(str(tmp_path / "c"), 3)
+    L3 = driver._ff_learning(c3, sr)
+    assert L3.nLearnTypeFF_I == 0 and L3.tauAvgCortical == 0.0
+    c4 = _learn_cfg(str(tmp_path / "d"), 4)
+    assert driver._learn_types(c4) == (0, 0, 1)
+    assert driver._ff_learning(c4, sr).tauAvgCortical == 1000.0
+    # the reference's refusals
+    for kw in (dict(tauAvg=[1.0, 2.0, 3.0]), dict(gmaxLGN=[0.6, 0.7, 0.8]), dict(tauLTD=[1.0, 2.0]),
+               dict(A_LGN=[0.02]), dict(gmaxE=[])):
+        with pytest.raises(cfg.ConfigError):
+            driver._ff_learning(_learn_cfg(str(tmp_path / "e"), 2, **kw), sr)
+    with pytest.raises(cfg.ConfigError):
+        driver.build(_learn_cfg(str(tmp_path / "f"), 2, nLearnTypeFF_I=2))
+    with pytest.raises(cfg.ConfigError):
+        driver.build(_learn_cfg(str(tmp_path / "g"), 5))
+
+
 @pytest.mark.gpu
-def test_learning_outputs_and_snapshot(native):
-    """learning = 3 from a cfg: the sLGN file holds the header of src/patch.cu:4767-4776 and the
-    weights after every sampleInterval_LGN_V1 steps (equal to the weights of a Simulation run
-    with the same FFLearning); the snapshot carries the weights and learning variables where
-    the reference puts them (src/patch.cu:6844-6850); a run resumed from the snapshot cut to
-    the reference's fields continues the weights and the records bit for bit."""
+@pytest.mark.parametrize("learning", [3, 2])
+def test_learning_outputs_and_snapshot(native, learning):
+    """learning 3 and 2 from a cfg: the sLGN file holds the header of src/patch.cu:4767-4776
+    and the weights after every sampleInterval_LGN_V1 steps (equal to the weights of a
+    Simulation run with the same FFLearning); the snapshot carries the weights and learning
+    variables where the reference puts them (src/patch.cu:6844-6850); a run resumed from the
+    snapshot cut to the reference's fields continues the weights and the records bit for bit."""
     import glob
     import os
     import shutil
@@ -427,9 +480,8 @@ def test_learning_outputs_and_snapshot(native):
     wl = synth.make_workload("learn", seed=6, nblock=1, n_lgn=512, m=20, width=64, height=64, nt=96,
                              adex_inh=True, nFrame=40)
     d = tempfile.mkdtemp()
-    extra = dict(learning=3, tauLTP=[16.8], tauLTD=[33.7], tauTrip=[114.0], tauAvg=[1000.0, 1000.0],
-                 targetFR=[2.0, 2.0], A_LGN=[0.02], r_LTD=[1.0], gmaxLGN=[0.6], gminLGN=[0.0],
-                 applyHomeo=1, FF_InfRatio=0.95, sampleInterval_LGN_V1=32, store_dsLGN=True)
+    nFI = 1 if learning == 2 else 0
+    extra = dict(LEARN_CFG, learning=learning, gmaxLGN=[0.6, 0.8][:1 + nFI])
     fn = synth.write_reference_files(wl, d, seed=6, nt=96, extra=extra)
     outs = [os.path.join(d, x) + "/" for x in ("a", "b", "c")]
     lgn = cfg.resolve_paths(cfg.load(["-c", fn])).lgn
@@ -441,7 +493,8 @@ def test_learning_outputs_and_snapshot(native):
     driver.run(ca, **quiet)
     h, W = FM.read_slgn(cfg.resolve_paths(ca).slgn)
     assert h["nt"] == 64 and h["interval"] == 32 and h["maxLGN"] == wl.net.maxLGN and W.shape[0] == 2
-    assert abs(h["FF_InfRatio"] - 0.95) < 1e-7 and h["nLearnTypeFF_E"] == 1 and h["nLearnTypeFF_I"] == 0
+    assert abs(h["FF_InfRatio"] - 0.95) < 1e-7 and h["nLearnTypeFF_E"] == 1 and h["nLearnTypeFF_I"] == nFI
+    np.testing.assert_array_equal(h["gmaxLGN"], np.float32([0.6, 0.8][:1 + nFI]))
     m = driver.build(ca)
     sim = Simulation(m.spec, m.net, m.lgn, m.stim, m.init, m.seeds)
     try:
@@ -455,8 +508,9 @@ def test_learning_outputs_and_snapshot(native):
         sim.close()
     snap_fn = glob.glob(outs[0] + "snapShot_*_s.bin")[0]
     snap, trailer = FM.read_reference_snapshot(snap_fn, m.spec.nI * m.spec.nblock, maxLGN=m.net.maxLGN,
-                                               nE_total=m.spec.nE * m.spec.nblock)
-    assert snap["learning"] == 3
+                                               nE_total=m.spec.nE * m.spec.nblock, nFF_I=nFI)
+    assert snap["learning"] == learning
+    assert snap["learn"]["ff_pre"].size == (1 + nFI) * m.lgn.nLGN
     np.testing.assert_array_equal(snap["learn"]["sLGN"].reshape(W[1].shape), W[1])
     # resumed from the reference's fields only
     ref_only = outs[0] + "refsnap_s.bin"

@@ -380,3 +380,87 @@ def test_oracle_v1_learning_matches_reference_kernels(gold_learn):
     assert rel(post[2 * nEt:4 * nEt], g["v1_vAvgE"]) < 1e-5
     assert rel(vo.get("total_ff")[:n], g["v1_totalFF"]) < 1e-5
     vo.close()
+
+
+def test_oracle_v1_learning2_matches_reference_kernels(gold_learn):
+    """The same 120 steps with learning = 2: an FF->I type beside the FF->E one (its own
+    constants; the reference's inhibitory posts read presynaptic trace 0), additive homeostasis,
+    and the excitatory filtered rate advanced by recal_G_mat_nd_fast with the cortical E type's
+    tauAvg (src/coredynamics.cu:2326-2346).  Rasters identical; weights, the E and I post
+    traces, both filtered rates and the totals within 1e-5 of each array's largest value."""
+    import oracle
+    wl = RC.v1_workload(sp=False, host_init=oracle.host_init_state)
+    g = gold_learn
+    L = RC.learning_params2()
+    vo = oracle.V1Oracle(wl.spec, wl.net)
+    for k in ("v", "w", "gFF", "hFF", "gE", "hE", "gI", "hI"):
+        vo.put(k, g["v1_in_" + k])
+    vo.set_ff_learning(L)
+    T, n = RC.LEARN_T, wl.spec.nV1
+    lgn = g["v1_lgnSInfo"]
+    raster = np.zeros((T, n), f32)
+    for it in range(T):
+        vo.step(lgn[it])
+        vo.learn_ff(lgn[it], np.ascontiguousarray(g["v1_preStart"][it]), np.ascontiguousarray(g["v1_preSpk"][it]))
+        vo.learn_avg()
+        raster[it] = vo.get("sInfo")
+    ref = g["v2_raster"].reshape(T, n)
+    np.testing.assert_array_equal(raster >= 1, ref >= 1)
+    E = np.arange(n) % wl.spec.blockSize < wl.spec.nE
+    assert (ref.reshape(T, n)[:, E] >= 1).sum() > 50 and (ref.reshape(T, n)[:, ~E] >= 1).sum() > 20
+    rel = lambda a, b: float(np.max(np.abs(a.astype(np.float64) - b)) / np.max(np.abs(b)))
+    s1 = vo.get("sLGN")
+    assert rel(s1, g["v2_sLGN"]) < 1e-5
+    s0 = wl.net.sLGN.reshape(-1, n)
+    dI = np.abs(g["v2_sLGN"].reshape(-1, n) - s0)[:, ~E].max()
+    assert dI > 0.01 * s0.max(), "the FF->I weights did not learn"
+    post = vo.get("ff_post")
+    nEt, nIt = wl.spec.nE * wl.spec.nblock, wl.spec.nI * wl.spec.nblock
+    o = 2 * nEt
+    for name, a, b in (("vLTD", 0, nEt), ("vTrip", nEt, 2 * nEt), ("vLTDi", o, o + nIt), ("vTripi", o + nIt, o + 2 * nIt),
+                       ("vAvgI", o + 2 * nIt + 2 * nEt, post.size)):
+        assert np.abs(g["v2_" + name]).max() > 0, name
+        assert rel(post[a:b], g["v2_" + name]) < 1e-5, (name, rel(post[a:b], g["v2_" + name]))
+    # vAvgE adds floor(spike word) every step -- the membrane potential when the neuron did not
+    # spike -- so a potential within an ulp of an integer moves it by 1 on one side only
+    from oracle.parity import avg_floor_flips, compare_avg
+    flips = avg_floor_flips(wl.spec, raster, ref)
+    assert (flips > 0).sum() <= 0.01 * nEt
+    assert compare_avg(post[o + 2 * nIt:o + 2 * nIt + 2 * nEt], g["v2_vAvgE"], flips) < 1e-5
+    assert rel(vo.get("total_ff")[:n], g["v2_totalFF"]) < 1e-5
+    vo.close()
+
+
+def test_oracle_v1_learning4_matches_reference_kernels(gold_learn):
+    """The same 120 steps with learning = 4: the V1 kernel skips the FF learning block, so the
+    LGN->V1 weights stay bit for bit and the spike-time slot of vAvgE stays 0; the delivery
+    advances vAvgE with the cortical E type's tauAvg.  Rasters identical, vAvgE as in the
+    learning = 2 case (floor flips counted)."""
+    import oracle
+    from oracle.parity import avg_floor_flips, compare_avg
+    wl = RC.v1_workload(sp=False, host_init=oracle.host_init_state)
+    g = gold_learn
+    vo = oracle.V1Oracle(wl.spec, wl.net)
+    for k in ("v", "w", "gFF", "hFF", "gE", "hE", "gI", "hI"):
+        vo.put(k, g["v1_in_" + k])
+    vo.set_ff_learning(RC.learning_params4())
+    T, n = RC.LEARN_T, wl.spec.nV1
+    lgn = g["v1_lgnSInfo"]
+    raster = np.zeros((T, n), f32)
+    for it in range(T):
+        vo.step(lgn[it])
+        vo.learn_avg()
+        raster[it] = vo.get("sInfo")
+    ref = g["v4_raster"].reshape(T, n)
+    np.testing.assert_array_equal(raster >= 1, ref >= 1)
+    assert (ref >= 1).sum() > 50
+    np.testing.assert_array_equal(g["v4_sLGN"], wl.net.sLGN.reshape(-1))
+    np.testing.assert_array_equal(vo.get("sLGN"), wl.net.sLGN.reshape(-1))
+    nEt = wl.spec.nE * wl.spec.nblock
+    post = vo.get("ff_post")
+    assert post.size == 2 * nEt + wl.spec.nI * wl.spec.nblock
+    flips = avg_floor_flips(wl.spec, raster, ref)
+    assert (flips > 0).sum() <= 0.01 * nEt
+    assert np.abs(g["v4_vAvgE"]).max() > 100
+    assert compare_avg(post[:2 * nEt], g["v4_vAvgE"], flips) < 1e-5
+    vo.close()

@@ -56,7 +56,11 @@ class FFLearning(C.Structure):
                 ("tauAvg", C.c_float), ("targetFR", C.c_float), ("A_LGN", C.c_float), ("r_LTD", C.c_float),
                 ("gmaxLGN", C.c_float), ("gminLGN", C.c_float), ("sRatioLGN", C.c_float),
                 ("decayTimeHomeoFF", C.c_float), ("FF_InfRatio", C.c_float), ("applyHomeo", C.c_int32),
-                ("symmetricHomeo", C.c_int32), ("rebound", C.c_int32)]
+                ("symmetricHomeo", C.c_int32), ("rebound", C.c_int32), ("nLearnTypeFF_E", C.c_int32),
+                ("nLearnTypeFF_I", C.c_int32), ("tauLTP_I", C.c_float), ("tauLTD_I", C.c_float),
+                ("tauTrip_I", C.c_float), ("tauAvg_I", C.c_float), ("targetFR_I", C.c_float), ("A_LGN_I", C.c_float),
+                ("r_LTD_I", C.c_float), ("gmaxLGN_I", C.c_float), ("gminLGN_I", C.c_float),
+                ("sRatioLGN_I", C.c_float), ("tauAvgCortical", C.c_float)]
 
 
 class LgnConfig(C.Structure):

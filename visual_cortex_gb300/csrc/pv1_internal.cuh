@@ -140,11 +140,16 @@ struct LgnParams {
     const double *pctw;        // [2][pKS+1][nParvo] cumulative temporal weights (centre, surround)
     const float *pS;           // [nFrame+1][2][nParvo] spatial stage per frame
     const float *pk;           // [2][nParvo] amplitude k of centre and surround
-    // LGN->V1 plasticity: presynaptic LTP trace per cell (0 types: none)
+    // LGN->V1 plasticity: presynaptic LTP traces per cell (FF->E type first; 0 types: none)
     int nFF;
-    float tauLTP;
-    float *ffPre;              // [nLGN] trace at the end of the last computed step
-    float *outPre;             // [outSlots][2][nLGN] trace at the start of the step, right after its spikes
+    float tauLTP[2];
+    float *ffPre;              // [nFF][nLGN] traces at the end of the last computed step
+    float *outPre;             // [outSlots][nFF][2][nLGN] traces at the start of the step, right after its spikes
+};
+
+// One LGN->V1 learning type (learnFF_pre/learnFF_post, src/condShape.h:85-152, derived).
+struct FFType {
+    float tauLTP, tauLTD, tauTrip, tauAvg, targetFR, A_LTP, A_ratio, gmax, gmin;
 };
 
 struct V1Params {
@@ -167,12 +172,18 @@ struct V1Params {
     int noiseRng;       // some noisyDep > 0
     long long waitSpins;   // polls of a barrier wait before it gives up and raises kErrBarrier
     int pushCta;           // far-push CTAs appended to the persistent grid (0: the neuron CTAs push)
-    // LGN->V1 plasticity (learning = 3): triplet rule on the LGN->E synapses
-    int ffLearn;
-    float ffTauLTP, ffTauLTD, ffTauTrip, ffTauAvg, ffTargetFR, ffA_LTP, ffA_ratio, ffGmax, ffGmin;
+    // LGN->V1 plasticity (the reference's learning 1-4): triplet rule on the LGN->E synapses
+    // (type 0) and, with learning 2, on the LGN->I synapses (type 1)
+    int ffMode;            // the reference's `learning` (0: off)
+    int ffLearn;           // the V1 step runs the learning block (learning 1-3)
+    int ffTypes;           // traces the LGN stage keeps (FF->E, then FF->I)
+    int ffI;               // FF->I learning on
+    FFType ffT[2];         // FF->E, FF->I
     int applyHomeo, symmetricHomeo, rebound;
     float expHomeo;
-    float *ffPost;         // the reference's learnVar FF block: vLTD_FF_E, vTrip_FF_E, vAvgE[2], vAvgI
+    float tauAvgCortical;  // vAvgE through the delivery (learning 1, 2, 4)
+    float *ffPost;         // learnVar's FF block: vLTD_FF_E, vTrip_FF_E, vLTD_FF_I, vTrip_FF_I, vAvgE[2], vAvgI
+    int ffOffI, ffOffAvgE, ffOffAvgI;   // offsets of vLTD_FF_I, vAvgE and vAvgI in it
     float *totalFF;        // [2][nV1] total LGN weight and its target
     float *sLGNw;          // the weights, written by the learning (same array as sLGN)
     const float *ffPreRing;  // the LGN stage's outPre ring (row = step % lgn slots)

@@ -559,26 +559,32 @@ __device__ __forceinline__ int frame_number(const FrameSched &fs, int currentFra
 
 constexpr int kClassCta = 128;
 
-// Presynaptic LTP trace of LGN cell id over step it (LGN_nonlinear with learning 1-3,
-// src/discrete_input_convol.cu:1774-1808): the value at the start of the step and, when the
-// cell spiked, the value right after its spikes (the spike count added, then decayed from the
-// step start to the spike time tsp) go to the step's row of outPre; var leaves decayed to the
-// end of the step.
+// Presynaptic LTP traces of LGN cell id over step it (LGN_nonlinear with learning 1-3,
+// src/discrete_input_convol.cu:1774-1808), one per learning type (FF->E, then FF->I), each with
+// its own tauLTP: the value at the start of the step and, when the cell spiked, the value right
+// after its spikes (the spike count added, then decayed from the step start to the spike time
+// tsp) go to the step's row of outPre; var leaves decayed to the end of the step.
 __device__ __forceinline__ void ff_pre_step(const LgnParams &P, long long it, int id, unsigned nsp, float tsp,
-                                            float sInfo, float &var) {
-    float *row = P.outPre + (size_t)(it % P.outSlots) * 2 * P.nLGN;
-    row[id] = var;
-    float delta_t;
-    if (sInfo > 0) {
-        delta_t = tsp;
-        var += (float)nsp;
-        var *= expf(-delta_t / P.tauLTP);
-        row[P.nLGN + id] = var;
-        delta_t = P.dt - delta_t;
-    } else {
-        delta_t = P.dt;
+                                            float sInfo, float *var) {
+    float *row = P.outPre + (size_t)(it % P.outSlots) * P.nFF * 2 * P.nLGN;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        if (k < P.nFF) {
+            float *r = row + (size_t)k * 2 * P.nLGN;
+            r[id] = var[k];
+            float delta_t;
+            if (sInfo > 0) {
+                delta_t = tsp;
+                var[k] += (float)nsp;
+                var[k] *= expf(-delta_t / P.tauLTP[k]);
+                r[P.nLGN + id] = var[k];
+                delta_t = P.dt - delta_t;
+            } else {
+                delta_t = P.dt;
+            }
+            var[k] *= expf(-delta_t / P.tauLTP[k]);
+        }
     }
-    var *= expf(-delta_t / P.tauLTP);
 }
 
 
@@ -650,7 +656,7 @@ __device__ __forceinline__ void lgn_class_body(const LgnParams &P, long long t0,
     float ltr = P.leftTimeRate[id];
     float lnl = P.lastNegLogRand[id];
     curandStateMRG32k3a st = P.state[id];
-    float ffVar = P.nFF ? P.ffPre[id] : 0.f;
+    float ffVar[2] = {P.nFF > 0 ? P.ffPre[id] : 0.f, P.nFF > 1 ? P.ffPre[(size_t)P.nLGN + id] : 0.f};
     const float dt = P.dt;
     for (int s = 0; s < K; s++) {
         const long long it = t0 + s;
@@ -699,7 +705,8 @@ __device__ __forceinline__ void lgn_class_body(const LgnParams &P, long long t0,
     P.leftTimeRate[id] = ltr;
     P.lastNegLogRand[id] = lnl;
     P.state[id] = st;
-    if (P.nFF) P.ffPre[id] = ffVar;
+    if (P.nFF > 0) P.ffPre[id] = ffVar[0];
+    if (P.nFF > 1) P.ffPre[(size_t)P.nLGN + id] = ffVar[1];
 }
 
 __global__ void __launch_bounds__(kClassCta) lgn_class_kernel(LgnParams P, const long long *stepBase, int K) {
@@ -836,7 +843,7 @@ __global__ void __launch_bounds__(256) lgn_spike_kernel(LgnParams P, const long 
     float ltr = P.leftTimeRate[id];
     float lnl = P.lastNegLogRand[id];
     curandStateMRG32k3a st = P.state[id];
-    float ffVar = P.nFF ? P.ffPre[id] : 0.f;
+    float ffVar[2] = {P.nFF > 0 ? P.ffPre[id] : 0.f, P.nFF > 1 ? P.ffPre[(size_t)P.nLGN + id] : 0.f};
     const float dt = P.dt;
     const long long step0 = *stepBase;
     for (int s = 0; s < K; s++) {
@@ -877,7 +884,8 @@ __global__ void __launch_bounds__(256) lgn_spike_kernel(LgnParams P, const long 
     P.leftTimeRate[id] = ltr;
     P.lastNegLogRand[id] = lnl;
     P.state[id] = st;
-    if (P.nFF) P.ffPre[id] = ffVar;
+    if (P.nFF > 0) P.ffPre[id] = ffVar[0];
+    if (P.nFF > 1) P.ffPre[(size_t)P.nLGN + id] = ffVar[1];
 }
 
 }  // namespace pv1

@@ -316,7 +316,7 @@ int plan_batch_view(pv1_plan *p, PlanBatchView *out) {
         return fail(p, PV1_E_STATE, "V1 synapses/connectivity/state/rng not set");
     if (p->vp.farPullOn || p->vp.nearPullOn)
         return fail(p, PV1_E_UNSUPPORTED, "batched trials with synaptic failure on delayed synapses are not built");
-    if (p->vp.ffLearn) return fail(p, PV1_E_UNSUPPORTED, "batched trials with LGN->V1 plasticity are not built");
+    if (p->vp.ffMode) return fail(p, PV1_E_UNSUPPORTED, "batched trials with LGN->V1 plasticity are not built");
     out->vp = p->vp;
     out->lp = p->lp;
     out->lgnRing = p->d_lgnRing;
@@ -1055,11 +1055,11 @@ int pv1_v1_set_lgn_synapses(pv1_plan *p, uint32_t maxLGN, const uint32_t *nLGNpe
 
 // The LGN stage's trace ring of a plan with learning: one row pair per LGN ring row.
 static int ensure_ff_ring(pv1_plan *p) {
-    if (!p->vp.ffLearn) return PV1_OK;
+    if (!p->vp.ffMode || p->lp.nFF == 0) return PV1_OK;
     if (p->lp.outPre) free_one(p, p->lp.outPre);
     p->lp.outPre = nullptr;
     float *d = nullptr;
-    int r = dev_alloc(p, &d, (size_t)p->lgnSlots * 2 * p->nLGN);
+    int r = dev_alloc(p, &d, (size_t)p->lgnSlots * p->lp.nFF * 2 * p->nLGN);
     if (r) return r;
     p->lp.outPre = d;
     p->vp.ffPreRing = d;
@@ -1084,23 +1084,58 @@ int pv1_ff_learning_rates(const pv1_ff_learning *l, float dt, float *out) {
     return PV1_OK;
 }
 
+// Floats of learnVar's FF block (src/patch.cu:4365-4377): the post traces of each type, then
+// vAvgE [nblock*nE][2] and vAvgI [nblock*nI].
+static size_t ff_post_floats(const pv1_plan *p) {
+    const size_t nEt = (size_t)p->nE * p->cfg.nblock, nIt = (size_t)p->nI * p->cfg.nblock;
+    const V1Params &v = p->vp;
+    // learnVar's FF block (src/patch.cu:4367-4392): the FF->E post traces (none with
+    // learning 4), the FF->I ones, vAvgE [nEt][2], vAvgI
+    return (v.ffMode == 4 ? 0 : 2 * nEt) + 2 * (size_t)v.ffI * nIt + 2 * nEt + nIt;
+}
+
 int pv1_set_ff_learning(pv1_plan *p, const pv1_ff_learning *l) {
     if (!p || !l) return PV1_E_ARG;
-    if (l->learning != 3)
-        return fail(p, PV1_E_UNSUPPORTED, "only learning = 3 (LGN->E plasticity) is built");
+    const int mode = l->learning;
+    if (mode < 1 || mode > 4) return fail(p, PV1_E_ARG, "learning is 1, 2, 3 or 4");
     if (!p->lgnReady || !p->haveLGNsyn) return fail(p, PV1_E_STATE, "set up the LGN and the LGN->V1 synapses first");
     if (p->extLgn)
         return fail(p, PV1_E_UNSUPPORTED, "plasticity needs the plan's own LGN stage (its presynaptic traces)");
     if (p->vp.multiSpike)
         return fail(p, PV1_E_UNSUPPORTED, "plasticity with several spikes per step (dt > min tRef) is not built");
-    if (!(l->tauLTP > 0 && l->tauLTD > 0 && l->tauTrip > 0 && l->tauAvg > 0 && l->decayTimeHomeoFF > 0))
-        return fail(p, PV1_E_ARG, "learning time constants must be > 0");
+    // learning 1: FF->E (+ cortical variables); 2: FF->E and FF->I; 3: FF->E only; 4: cortical
+    // variables only (src/patch.cu:1160-1175)
+    const int nE_ = mode == 4 ? 0 : l->nLearnTypeFF_E;
+    const int nI_ = mode == 2 ? l->nLearnTypeFF_I : 0;
+    if (mode != 4 && nE_ != 1)
+        return fail(p, PV1_E_UNSUPPORTED,
+                    "learning 1-3 with nLearnTypeFF_E != 1 (0 would clip every LGN->E weight to the zeroed "
+                    "struct's [0, 0]; the reference allows at most 1)");
+    if (nI_ < 0 || nI_ > 1) return fail(p, PV1_E_UNSUPPORTED, "nLearnTypeFF_I is 0 or 1 (the reference's maximum)");
+    if (mode != 4 && !(l->tauLTP > 0 && l->tauLTD > 0 && l->tauTrip > 0 && l->tauAvg > 0))
+        return fail(p, PV1_E_ARG, "FF->E learning time constants must be > 0");
+    if (nI_ && !(l->tauLTP_I > 0 && l->tauLTD_I > 0 && l->tauTrip_I > 0 && l->tauAvg_I > 0))
+        return fail(p, PV1_E_ARG, "FF->I learning time constants must be > 0");
+    if (!(l->decayTimeHomeoFF > 0) || l->tauAvgCortical < 0) return fail(p, PV1_E_ARG, "bad time constant");
     if (l->applyHomeo < 0 || l->applyHomeo > 2) return fail(p, PV1_E_ARG, "applyHomeo is 0, 1 or 2");
     const pv1_v1_config &c = p->cfg;
-    float rates[5];
-    pv1_ff_learning_rates(l, c.dt, rates);
     V1Params &v = p->vp;
-    const size_t n = p->nV1, nEt = (size_t)p->nE * c.nblock, nIt = (size_t)p->nI * c.nblock;
+    auto type_of = [&](bool inh, FFType &T, float *expHomeo) {
+        pv1_ff_learning q = *l;
+        if (inh) {
+            q.tauLTP = l->tauLTP_I; q.tauLTD = l->tauLTD_I; q.tauTrip = l->tauTrip_I; q.tauAvg = l->tauAvg_I;
+            q.targetFR = l->targetFR_I; q.A_LGN = l->A_LGN_I; q.r_LTD = l->r_LTD_I; q.gmaxLGN = l->gmaxLGN_I;
+            q.gminLGN = l->gminLGN_I; q.sRatioLGN = l->sRatioLGN_I;
+        }
+        float r[5];
+        pv1_ff_learning_rates(&q, c.dt, r);
+        T = FFType{q.tauLTP, q.tauLTD, q.tauTrip, q.tauAvg, q.targetFR, r[0], r[1], r[2], r[3]};
+        if (expHomeo) *expHomeo = r[4];
+    };
+    float expHomeo = 0.f;
+    type_of(false, v.ffT[0], &expHomeo);
+    type_of(true, v.ffT[1], nullptr);
+    const size_t n = p->nV1;
     // the homeostasis totals: each neuron's LGN weights summed in synapse order, and that
     // times FF_InfRatio (src/patch.cu:4335-4352)
     std::vector<float> s((size_t)v.maxLGN * n), tot(2 * n, 0.f);
@@ -1114,31 +1149,31 @@ int pv1_set_ff_learning(pv1_plan *p, const pv1_ff_learning *l) {
         tot[i] = t;
         tot[n + i] = t * l->FF_InfRatio;
     }
+    v.ffMode = mode;
+    v.ffLearn = mode <= 3;
+    v.ffI = nI_;
+    v.ffTypes = nE_ + nI_;
+    const size_t nEt = (size_t)p->nE * c.nblock, nIt = (size_t)p->nI * c.nblock;
+    v.ffOffI = (int)(mode == 4 ? 0 : 2 * nEt);
+    v.ffOffAvgE = v.ffOffI + (int)(2 * (size_t)nI_ * nIt);
+    v.ffOffAvgI = v.ffOffAvgE + (int)(2 * nEt);
     float *d_post = nullptr, *d_tot = nullptr, *d_pre = nullptr;
     int r = 0;
-    r |= dev_alloc(p, &d_post, 4 * nEt + nIt);
+    r |= dev_alloc(p, &d_post, ff_post_floats(p));
     r |= dev_upload(p, &d_tot, tot.data(), tot.size());
-    r |= dev_alloc(p, &d_pre, (size_t)p->nLGN);
+    r |= dev_alloc(p, &d_pre, (size_t)std::max(v.ffTypes, 1) * p->nLGN);
     if (r) return r;
-    v.ffLearn = 1;
-    v.ffTauLTP = l->tauLTP;
-    v.ffTauLTD = l->tauLTD;
-    v.ffTauTrip = l->tauTrip;
-    v.ffTauAvg = l->tauAvg;
-    v.ffTargetFR = l->targetFR;
-    v.ffA_LTP = rates[0];
-    v.ffA_ratio = rates[1];
-    v.ffGmax = rates[2];
-    v.ffGmin = rates[3];
     v.applyHomeo = l->applyHomeo;
     v.symmetricHomeo = l->symmetricHomeo != 0;
     v.rebound = l->rebound != 0;
-    v.expHomeo = rates[4];
+    v.expHomeo = expHomeo;
+    v.tauAvgCortical = l->tauAvgCortical;
     v.ffPost = d_post;
     v.totalFF = d_tot;
     v.sLGNw = const_cast<float *>(v.sLGN);
-    p->lp.nFF = 1;
-    p->lp.tauLTP = l->tauLTP;
+    p->lp.nFF = v.ffTypes;
+    p->lp.tauLTP[0] = nE_ ? v.ffT[0].tauLTP : v.ffT[1].tauLTP;
+    p->lp.tauLTP[1] = v.ffT[1].tauLTP;
     p->lp.ffPre = d_pre;
     r = ensure_ff_ring(p);
     if (r) return r;
@@ -1761,7 +1796,7 @@ static int choose_mode(pv1_plan *p) {
     int push = 0;
     v1_persistent_ctas(p->vp, p->device, &fits, &push);
     p->persistent = fits && p->allowPersistent && !p->vp.multiSpike && !p->vp.farPullOn && !p->vp.nearPullOn &&
-                    !p->vp.ffLearn;
+                    !p->vp.ffMode;
     p->vp.pushCta = p->persistent ? push : 0;
     if (p->persistent && !p->d_barrier) {
         int r = dev_alloc(p, &p->d_barrier, 2);
@@ -1781,8 +1816,8 @@ int pv1_set_lgn_source(pv1_plan *p, const float *d_sInfo, int64_t step0, int64_t
     }
     if (!p->lgnReady) return fail(p, PV1_E_STATE, "call pv1_lgn_setup first (it gives the LGN cell count)");
     if (step0 < 0 || nsteps <= 0) return fail(p, PV1_E_ARG, "bad step range");
-    if (p->vp.ffLearn)
-        return fail(p, PV1_E_UNSUPPORTED, "an external LGN source has no presynaptic learning traces (learning = 3)");
+    if (p->vp.ffMode)
+        return fail(p, PV1_E_UNSUPPORTED, "an external LGN source has no presynaptic learning traces");
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, d_sInfo) != cudaSuccess || a.type != cudaMemoryTypeDevice || a.device != p->device) {
         cudaGetLastError();
@@ -2209,12 +2244,11 @@ void ckpt_items(pv1_plan *p, std::vector<std::pair<void *, size_t>> &items) {
     add(p->lp.leftTimeRate, p->nLGN * f);
     add(p->lp.lastNegLogRand, p->nLGN * f);
     add(p->lp.state, p->nLGN * sizeof(curandStateMRG32k3a));
-    if (v.ffLearn) {
-        const size_t nEt = (size_t)p->nE * c.nblock, nIt = (size_t)p->nI * c.nblock;
+    if (v.ffMode) {
         add(v.sLGNw, (size_t)v.maxLGN * n * f);
-        add(v.ffPost, (4 * nEt + nIt) * f);
+        add(v.ffPost, ff_post_floats(p) * f);
         add(v.totalFF, 2 * n * f);
-        add(p->lp.ffPre, p->nLGN * f);
+        add(p->lp.ffPre, (size_t)p->lp.nFF * p->nLGN * f);
     }
 }
 
@@ -2405,8 +2439,8 @@ int pv1_get_state(pv1_plan *p, int which, float *out) {
         case PV1_ST_V1_RNG_COND: src = v.rGenCond; cnt = n * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
         case PV1_ST_V1_RNG_NOISY: src = v.rNoisy; cnt = n * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
         case PV1_ST_SLGN: src = v.sLGN; cnt = (size_t)v.maxLGN * n; break;
-        case PV1_ST_FF_POST: src = v.ffPost; cnt = 4 * (size_t)p->nE * c.nblock + (size_t)p->nI * c.nblock; break;
-        case PV1_ST_FF_PRE: src = p->lp.ffPre; cnt = p->nLGN; break;
+        case PV1_ST_FF_POST: src = v.ffPost; cnt = ff_post_floats(p); break;
+        case PV1_ST_FF_PRE: src = p->lp.ffPre; cnt = (size_t)p->lp.nFF * p->nLGN; break;
         case PV1_ST_TOTAL_FF: src = v.totalFF; cnt = 2 * n; break;
         default: return fail(p, PV1_E_ARG, "unknown state id");
     }
@@ -2441,8 +2475,8 @@ int pv1_put_state(pv1_plan *p, int which, const float *in) {
         case PV1_ST_V1_RNG_COND: dst = v.rGenCond; cnt = n * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
         case PV1_ST_V1_RNG_NOISY: dst = v.rNoisy; cnt = n * (sizeof(curandStateMRG32k3a) / sizeof(float)); break;
         case PV1_ST_SLGN: dst = v.sLGNw; cnt = (size_t)v.maxLGN * n; break;
-        case PV1_ST_FF_POST: dst = v.ffPost; cnt = 4 * (size_t)p->nE * c.nblock + (size_t)p->nI * c.nblock; break;
-        case PV1_ST_FF_PRE: dst = p->lp.ffPre; cnt = p->nLGN; break;
+        case PV1_ST_FF_POST: dst = v.ffPost; cnt = ff_post_floats(p); break;
+        case PV1_ST_FF_PRE: dst = p->lp.ffPre; cnt = (size_t)p->lp.nFF * p->nLGN; break;
         case PV1_ST_TOTAL_FF: dst = v.totalFF; cnt = 2 * n; break;
         default: return fail(p, PV1_E_ARG, "state id cannot be written");
     }

@@ -237,6 +237,24 @@ __device__ __forceinline__ void prefetch_spiker(const V1Params &P, int b, int lo
     }
 }
 
+// The excitatory filtered rate of learning 1, 2 and 4, advanced over step tp in the near
+// delivery as recal_G_mat_nd_fast does (src/coredynamics.cu:2866-2890): from the value stored
+// at the spike time when the neuron spiked (slot 1), else the step start (slot 0), plus the
+// spike count, decayed over the rest of the step with the cortical E types' tauAvg.
+__device__ __forceinline__ void learn_avg_delivery(const V1Params &P, float postSInfo, int b, int local) {
+    const float dt = P.dt;
+    const float postNsp = floorf(postSInfo);
+    const float postTsp = postSInfo > 0 ? postSInfo - postNsp : 1.f;
+    const int cPick = postNsp > 0 ? 1 : 0;
+    float *vAvg = P.ffPost + P.ffOffAvgE + 2 * (b * P.nE + local);
+    float lAvgE = vAvg[cPick];
+    float delta_t = dt;
+    if (postNsp > 0) delta_t = dt * (1 - postTsp);
+    lAvgE += postNsp;
+    lAvgE *= expf(-delta_t / P.tauAvgCortical);
+    vAvg[0] = lAvgE;
+}
+
 // Phase A: delivery of step tp's spikes to this thread's neuron (all threads of the CTA
 // must call it; `active` masks the neuron work).
 template <bool Rng>
@@ -415,6 +433,7 @@ __device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, in
         __syncthreads();
     }
     if (recNear) P.recNearCount[(size_t)(tp - P.recStep0) * nV1 + i] = nNearDraw;
+    if (P.ffMode && P.ffMode != 3 && active && local < P.nE) learn_avg_delivery(P, __ldcg(sPrev + i), b, local);
 #pragma unroll
     for (int ig = 0; ig < kMaxNG; ig++) {
         st.gE[ig] += lgE[ig]; st.hE[ig] += lhE[ig];
@@ -774,20 +793,28 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
     return sInfo;
 }
 
-// LGN->V1 plasticity after the membrane step of neuron i (learning = 3, only the LGN->E
-// synapses learn): compute_V_collect_spike_learnFF_fast's learning block (src/coredynamics.cu:
-// 1631-1993) with one FF_E learning type.  The post LTD and triplet traces and the filtered
-// rate are read at the step start and, when the neuron spiked, decayed to its spike time tsp;
-// each LGN synapse (in synapse order) takes the homeostatic factor, LTD when its LGN cell
-// spiked (from the post LTD trace at the earlier of the two spike times, scaled by the
-// squared filtered rate when targetFR > 0), LTP when the neuron spiked (the presynaptic trace
-// at the step start or right after the LGN spike, whichever precedes tsp, decayed to tsp, times
-// the post triplet trace), and is clipped to [gmin, gmax]; the post traces then take the spike
-// count and decay to the end of the step.  Float arithmetic in the reference's order.
+// LGN->V1 plasticity after the membrane step of neuron i (learning 1-3): the learning block
+// of compute_V_collect_spike_learnFF_fast (src/coredynamics.cu:1631-1993) with one FF->E type
+// for excitatory posts and, with learning 2, one FF->I type for inhibitory posts.  The post
+// LTD and triplet traces and the filtered rate are read at the step start and, when the neuron
+// spiked, decayed to its spike time tsp; each LGN synapse (in synapse order) takes the
+// homeostatic factor, LTD when its LGN cell spiked (from the post LTD trace at the earlier of
+// the two spike times, scaled by the squared filtered rate when targetFR > 0), LTP when the
+// neuron spiked (the presynaptic trace at the step start or right after the LGN spike,
+// whichever precedes tsp, decayed to tsp, times the post triplet trace), and is clipped to
+// [gmin, gmax]; the post traces then take the spike count and decay to the end of the step.
+// The reference's choices kept: with learning != 3 the excitatory filtered rate is not
+// advanced here but stored at tsp into its second slot for the delivery to advance
+// (vAvgE[2*eid+1], src/coredynamics.cu:1746-1748); the inhibitory posts' LTP reads
+// presynaptic trace 0 (layer 1 + 3j of the LGN surface with j counting from 0,
+// src/coredynamics.cu:1905-1912), which is the FF->E type's trace when both types learn.
+// Float arithmetic in the reference's order.
 __device__ __noinline__ void learn_ff(const V1Params &P, long long t, int i, int local, int m, float sInfo,
                                       const float *__restrict__ lgnSInfo, const float *__restrict__ preRow,
                                       int nLGN) {
-    if (local >= P.nE) return;
+    const bool isE = local < P.nE;
+    if (!isE && !P.ffI) return;
+    const FFType &T = P.ffT[isE ? 0 : 1];
     const float dt = P.dt;
     float nsp, tsp;
     if (sInfo > 0) {
@@ -798,22 +825,26 @@ __device__ __noinline__ void learn_ff(const V1Params &P, long long t, int i, int
         tsp = dt;
     }
     const int nV1 = P.nV1;
-    const int nEt = P.nE * P.nblock;
-    const int eid = (i / P.blockSize) * P.nE + local;
-    float *vLTD = P.ffPost, *vTrip = P.ffPost + nEt, *vAvgE = P.ffPost + 2 * nEt;
+    const int nEt = P.nE * P.nblock, nIt = P.nI * P.nblock;
+    const int b = i / P.blockSize;
+    const int id = isE ? b * P.nE + local : b * P.nI + (local - P.nE);   // eid / iid
+    float *vLTD = isE ? P.ffPost : P.ffPost + P.ffOffI;
+    float *vTrip = isE ? P.ffPost + nEt : P.ffPost + P.ffOffI + nIt;
+    float *vAvg = isE ? P.ffPost + P.ffOffAvgE + 2 * id : P.ffPost + P.ffOffAvgI + id;
     // row 0: the step start; row 1: the spike time
     float lLTD[2], lTrip[2], lAvg[2];
-    lLTD[0] = vLTD[eid];
-    lTrip[0] = vTrip[eid];
-    lAvg[0] = vAvgE[2 * eid];
+    lLTD[0] = vLTD[id];
+    lTrip[0] = vTrip[id];
+    lAvg[0] = vAvg[0];
     lLTD[1] = lTrip[1] = lAvg[1] = 0.f;
     if (nsp > 0) {
         lLTD[1] = lLTD[0];
         lTrip[1] = lTrip[0];
-        lLTD[1] *= expf(-tsp / P.ffTauLTD);
-        lTrip[1] *= expf(-tsp / P.ffTauTrip);
+        lLTD[1] *= expf(-tsp / T.tauLTD);
+        lTrip[1] *= expf(-tsp / T.tauTrip);
         lAvg[1] = lAvg[0];
-        lAvg[1] *= expf(-tsp / P.ffTauAvg);
+        lAvg[1] *= expf(-tsp / T.tauAvg);
+        if (isE && P.ffMode != 3) vAvg[1] = lAvg[1];
     }
     float new0 = 0.f, change = 0.f, delta_f = 0.f;
     if (P.applyHomeo) {
@@ -834,8 +865,8 @@ __device__ __noinline__ void learn_ff(const V1Params &P, long long t, int i, int
         if (f == 0 && !P.rebound) continue;
         if (P.applyHomeo == 1) f *= change;
         else if (P.applyHomeo == 2) f += change;
-        const int id = __ldg(P.lgnId + lid);
-        const float sFF = __ldcg(lgnSInfo + id);
+        const int cell = __ldg(P.lgnId + lid);
+        const float sFF = __ldcg(lgnSInfo + cell);
         const unsigned nspFF = (unsigned)floorf(sFF);
         const float tspFF = (sFF > 0 ? sFF - (float)nspFF : 1.f) * dt;
         if (nspFF > 0) {  // LTD, whether or not the neuron spiked
@@ -848,32 +879,32 @@ __device__ __noinline__ void learn_ff(const V1Params &P, long long t, int i, int
                 cPick = 1;
                 delta_t = tspFF - tsp;
             }
-            float A_LTD = P.ffA_ratio;
-            if (P.ffTargetFR > 0) A_LTD *= P.ffTauLTP * lAvg[cPick] * lAvg[cPick];
-            const float df = lLTD[cPick] * expf(-delta_t / P.ffTauLTD) * A_LTD;
+            float A_LTD = T.A_ratio;
+            if (T.targetFR > 0) A_LTD *= T.tauLTP * lAvg[cPick] * lAvg[cPick];
+            const float df = lLTD[cPick] * expf(-delta_t / T.tauLTD) * A_LTD;
             f -= df;
             if (P.applyHomeo) delta_f -= df;
         }
         if (nsp > 0) {  // LTP, whether or not the LGN cell spiked
             float lpre, delta_t;
             if (tspFF < tsp) {
-                lpre = __ldcg(preRow + nLGN + id);
+                lpre = __ldcg(preRow + nLGN + cell);
                 delta_t = tsp - tspFF;
             } else {
-                lpre = __ldcg(preRow + id);
+                lpre = __ldcg(preRow + cell);
                 delta_t = tsp;
             }
-            const float df = lpre * expf(-delta_t / P.ffTauLTP) * lTrip[1] * P.ffA_LTP;
+            const float df = lpre * expf(-delta_t / T.tauLTP) * lTrip[1] * T.A_LTP;
             if (P.applyHomeo) delta_f += df;
             f += df;
         }
-        if (f < P.ffGmin) {
-            if (P.applyHomeo) delta_f += P.ffGmin - f;
-            f = P.ffGmin;
+        if (f < T.gmin) {
+            if (P.applyHomeo) delta_f += T.gmin - f;
+            f = T.gmin;
         }
-        if (f > P.ffGmax) {
-            if (P.applyHomeo) delta_f -= f - P.ffGmax;
-            f = P.ffGmax;
+        if (f > T.gmax) {
+            if (P.applyHomeo) delta_f -= f - T.gmax;
+            f = T.gmax;
         }
         P.sLGNw[lid] = f;
     }
@@ -884,13 +915,15 @@ __device__ __noinline__ void learn_ff(const V1Params &P, long long t, int i, int
     if (nsp > 0) delta_t -= tsp;
     lLTD[cPick] += nsp;
     lTrip[cPick] += nsp;
-    lLTD[cPick] *= expf(-delta_t / P.ffTauLTD);
-    lTrip[cPick] *= expf(-delta_t / P.ffTauTrip);
-    lAvg[cPick] += nsp;
-    lAvg[cPick] *= expf(-delta_t / P.ffTauAvg);
-    vLTD[eid] = lLTD[cPick];
-    vTrip[eid] = lTrip[cPick];
-    vAvgE[2 * eid] = lAvg[cPick];
+    lLTD[cPick] *= expf(-delta_t / T.tauLTD);
+    lTrip[cPick] *= expf(-delta_t / T.tauTrip);
+    vLTD[id] = lLTD[cPick];
+    vTrip[id] = lTrip[cPick];
+    if (!isE || P.ffMode == 3) {
+        lAvg[cPick] += nsp;
+        lAvg[cPick] *= expf(-delta_t / T.tauAvg);
+        vAvg[0] = lAvg[cPick];
+    }
 }
 
 // Phase B when dt exceeds the shortest refractory period: a neuron may fire several times in
@@ -1401,7 +1434,7 @@ __device__ __forceinline__ void v1_step_body(const V1Params &P, long long t, int
         if (P.farPullOn || P.nearPullOn) P.sRing[(size_t)(t % P.sDepth) * P.nV1 + i] = sInfo;
         if (P.ffLearn)
             learn_ff(P, t, i, local, P.nLGNperV1[i], sInfo, lgnSInfo,
-                     P.ffPreRing + (size_t)(t % lgnSlots) * 2 * P.lgnN, P.lgnN);
+                     P.ffPreRing + (size_t)(t % lgnSlots) * P.ffTypes * 2 * P.lgnN, P.lgnN);
     }
     if (P.farOn) {
         const int e0 = active ? P.farOff[i] : 0;

@@ -69,12 +69,13 @@ class Model:
 
 def _check_supported(c: Config):
     bad = []
-    if c.learning not in (0, 3):
-        bad.append(f"learning = {c.learning} (cortical E/Q plasticity, LGN->I plasticity; learning = 3, "
-                   "LGN->E plasticity, is built)")
-    if c.learning == 3 and int(c.values.get("nLearnTypeFF_E", 1)) != 1:
-        bad.append("learning = 3 with nLearnTypeFF_E != 1")
-    if c.learning == 3 and int(c.learnData_FF) > 1:
+    if c.learning not in (0, 1, 2, 3, 4):
+        bad.append(f"learning = {c.learning} (learning 0-4 are read)")
+    if c.learning in (1, 2, 3) and int(c.values.get("nLearnTypeFF_E", 1)) != 1:
+        bad.append(f"learning = {c.learning} with nLearnTypeFF_E != 1")
+    if c.learning == 2 and int(c.values.get("nLearnTypeFF_I", 1)) > 1:
+        bad.append("learning = 2 with nLearnTypeFF_I > 1")
+    if c.learning and int(c.learnData_FF) > 1:
         bad.append("learnData_FF = 2 (per-step learning dumps)")
     if c.InhGap:
         bad.append("InhGap (gap junctions)")
@@ -210,8 +211,9 @@ def _restore(sim, c: Config, m) -> int:
         return sim.step
     spec = m.spec
     try:
+        nFE, nFI, _ = _learn_types(c) if c.learning else (0, 0, 0)
         snap, trailer = FM.read_reference_snapshot(path, spec.nI * spec.nblock, maxLGN=m.net.maxLGN,
-                                                   nE_total=spec.nE * spec.nblock)
+                                                   nE_total=spec.nE * spec.nblock, nFF_E=nFE, nFF_I=nFI)
     except ValueError as e:
         raise ConfigError(str(e)) from None
     sz = snap["sizes"]
@@ -249,51 +251,126 @@ def _restore(sim, c: Config, m) -> int:
     return int(step)
 
 
+def _learn_types(c: Config):
+    """(nLearnTypeFF_E, nLearnTypeFF_I, nLearnTypeE) after the learning mode's overrides
+    (src/patch.cu:1160-1176): 1 drops FF->I, 3 keeps FF->E alone, 4 drops both FF types."""
+    v, mode = c.values, int(c.learning)
+    nE = int(v.get("nLearnTypeFF_E", 1))
+    nI = int(v.get("nLearnTypeFF_I", 1))
+    nC = int(v.get("nLearnTypeE", 1))
+    if mode in (1, 3):
+        nI = 0
+    if mode == 3:
+        nC = 0
+    if mode == 4:
+        nE = nI = 0
+    return nE, nI, nC
+
+
 def _ff_learning(c: Config, sRatioLGN):
-    """The FFLearning of learning = 3 from the cfg (src/patch.cu:1092-1330): element [0] of the
-    triplet-rule arrays; tauAvg and targetFR of size 1 or 2 ([0]: E); the Q arrays must agree in
-    size even though Q learning is off; gmaxLGN and gminLGN must be given."""
+    """The FFLearning of learning 1-4 from the cfg (src/patch.cu:1092-1330): the FF->E type is
+    element [0] of the triplet-rule arrays (a single value stands for every type), the FF->I
+    type element [nLearnTypeFF_E] with tauAvg[1], targetFR[1] and sRatioLGN[1]; tauAvg and
+    targetFR have 1 or 2 values (E, I); the Q arrays must agree in size even though Q learning
+    is off; with cortical E types (nLearnTypeE > 0) the excitatory filtered rate of the delivery
+    decays with tauAvg[0] (learnE's tau[3 n]), with none it is zeroed each step."""
     from .model import FFLearning
-    v = c.values
+    v, mode = c.values, int(c.learning)
+    nE, nI, nC = _learn_types(c)
+    nFF = nE + nI
 
-    def first(key, required=True):
-        a = v.get(key)
-        if not a:
-            if required:
-                raise ConfigError(f"learning = 3 needs '{key}'")
-            return None
-        return float(a[0])
+    def arr(key, required=True):
+        a = [float(x) for x in (v.get(key) or [])]
+        if not a and required:
+            raise ConfigError(f"learning = {mode} needs '{key}'")
+        return a
 
-    for key in ("tauAvg", "targetFR"):
-        a = v.get(key) or []
+    tauAvg, targetFR = arr("tauAvg"), arr("targetFR")
+    for key, a in (("tauAvg", tauAvg), ("targetFR", targetFR)):
         if len(a) not in (1, 2):
             raise ConfigError(f"{key} must have 1 or 2 values (E, I), not {len(a)}")
+        a += a[:1] * (2 - len(a))
     sizes = [len(v.get(k) or []) for k in ("tauQ", "A_Q", "gmaxQ", "gminQ")]
     if len(set(sizes)) != 1:
         raise ConfigError(f"size of tauQ: {sizes[0]} should be the same as A_Q: {sizes[1]}")
-    nTrip = len(v.get("tauTrip") or [])
-    for key in ("r_LTD", "tauLTD", "tauLTP"):
-        if len(v.get(key) or []) != nTrip:
+    if not bool(v.get("symQ", True)) and sizes[0] % 2:
+        raise ConfigError(f"size of array tauQ: {sizes[0]} must be even (or single-value)")
+    tauTrip = arr("tauTrip", nFF + nC > 0)
+    nTrip = len(tauTrip)
+    trip = {k: arr(k, False) for k in ("r_LTD", "tauLTD", "tauLTP")}
+    for key, a in trip.items():
+        if len(a) != nTrip:
             raise ConfigError(f"the size of {key} should be the same as tauTrip: {nTrip}")
-    return FFLearning(tauLTP=first("tauLTP"), tauLTD=first("tauLTD"), tauTrip=first("tauTrip"),
-                      tauAvg=first("tauAvg"), targetFR=first("targetFR"), A_LGN=first("A_LGN"),
-                      r_LTD=first("r_LTD"), gmaxLGN=first("gmaxLGN"), gminLGN=first("gminLGN"),
-                      sRatioLGN=float(sRatioLGN[0]), decayTimeHomeoFF=float(c.decayTimeHomeoFF),
-                      FF_InfRatio=float(c.FF_InfRatio), applyHomeo=int(c.applyHomeo),
-                      symmetricHomeo=bool(c.symmetricHomeo), rebound=bool(c.rebound))
+    if nTrip == 1:
+        if nE > 1 or nI > 1 or nC > 1:
+            raise ConfigError(f"tauLTP, tauLTD, tauTrip have size 1, but nLearnTypeFF_E: {nE}, nLearnTypeFF_I: "
+                              f"{nI}, nLearnTypeE: {nC} are inconsistent")
+    elif nC + nFF > nTrip:
+        raise ConfigError(f"nLearnTypeE {nC} + nLearnTypeFF {nFF} exceed the {nTrip} triplet rules")
+    if nC > 0:
+        for key in ("gmaxE", "gminE"):
+            a = v.get(key) or []
+            if len(a) > nC or 1 < len(a) < nC:
+                raise ConfigError(f"{key} either has size 1 or size {nC}")
+            if not a:
+                raise ConfigError(f"learning = {mode} with nLearnTypeE > 0 needs '{key}'")
+        if not v.get("A_V1"):
+            raise ConfigError(f"learning = {mode} with nLearnTypeE > 0 needs 'A_V1'")
+    gmax, gmin, A = arr("gmaxLGN", nFF > 0), arr("gminLGN", nFF > 0), arr("A_LGN", nFF > 0)
+    for key, a in (("gmaxLGN", gmax), ("gminLGN", gmin)):
+        if len(a) > nFF and nFF:
+            raise ConfigError(f"array size of {key} cannot be bigger than nLearnTypeFF {nFF}")
+        if 1 < len(a) < nFF:
+            raise ConfigError(f"{key} either has size 1 or size {nFF}")
+        a += a[:1] * (nFF - len(a))
+    if len(A) < nFF:
+        raise ConfigError(f"A_LGN needs {nFF} values")
+    for key in ("r_LTD", "tauLTD", "tauLTP"):
+        trip[key] += trip[key][:1] * (max(nFF, 1) - len(trip[key]))
+    tauTrip = tauTrip + tauTrip[:1] * (max(nFF, 1) - len(tauTrip))
+    sr = [float(x) for x in sRatioLGN]
+    kw = {}
+    if nE:
+        kw.update(tauLTP=trip["tauLTP"][0], tauLTD=trip["tauLTD"][0], tauTrip=tauTrip[0], A_LGN=A[0],
+                  r_LTD=trip["r_LTD"][0], gmaxLGN=gmax[0], gminLGN=gmin[0])
+    else:
+        kw.update(tauLTP=0.0, tauLTD=0.0, tauTrip=0.0, A_LGN=0.0, r_LTD=0.0, gmaxLGN=0.0, gminLGN=0.0)
+    if nI:
+        if len(sr) < 2:
+            raise ConfigError("learning = 2 with nLearnTypeFF_I = 1 reads sRatioLGN[1]")
+        k = nE
+        kw.update(tauLTP_I=trip["tauLTP"][k], tauLTD_I=trip["tauLTD"][k], tauTrip_I=tauTrip[k],
+                  tauAvg_I=tauAvg[1], targetFR_I=targetFR[1], A_LGN_I=A[k], r_LTD_I=trip["r_LTD"][k],
+                  gmaxLGN_I=gmax[k], gminLGN_I=gmin[k], sRatioLGN_I=sr[1])
+    return FFLearning(tauAvg=tauAvg[0], targetFR=targetFR[0], sRatioLGN=sr[0],
+                      decayTimeHomeoFF=float(c.decayTimeHomeoFF), FF_InfRatio=float(c.FF_InfRatio),
+                      applyHomeo=int(c.applyHomeo), symmetricHomeo=bool(c.symmetricHomeo),
+                      rebound=bool(c.rebound), learning=mode, nLearnTypeFF_E=max(nE, 1), nLearnTypeFF_I=nI,
+                      tauAvgCortical=tauAvg[0] if (mode != 3 and nC > 0) else 0.0, **kw)
 
 
-def _ltd_ratio(learn):
-    """A_ratio * tauLTP of the FF_E type, the dsLGN header's LTD ratio (src/patch.cu:4804-4806):
-    learnFF_post's A_ratio (src/condShape.h:137-152) in float with its double literals."""
+def _ltd_ratio1(A_LGN, sRatio, r_LTD, tauAvg, tauTrip, tauLTD, targetFR, tauLTP):
     f = np.float32
-    A_LTP = f(f(learn.A_LGN) * f(learn.sRatioLGN))
-    A_ratio = f(f(learn.r_LTD) * A_LTP)
-    if learn.targetFR > 0:
-        tas = f(float(f(learn.tauAvg)) / 1000.0)
-        q = f(f(learn.tauTrip) / f(f(learn.tauLTD) * f(tas * tas)))
-        A_ratio = f(float(A_ratio) * (float(q) / 1000.0 / float(f(learn.targetFR))))
-    return float(f(A_ratio * f(learn.tauLTP)))
+    A_LTP = f(f(A_LGN) * f(sRatio))
+    A_ratio = f(f(r_LTD) * A_LTP)
+    if targetFR > 0:
+        tas = f(float(f(tauAvg)) / 1000.0)
+        q = f(f(tauTrip) / f(f(tauLTD) * f(tas * tas)))
+        A_ratio = f(float(A_ratio) * (float(q) / 1000.0 / float(f(targetFR))))
+    return float(f(A_ratio * f(tauLTP)))
+
+
+def _ltd_ratio(learn, nE: int = 1, nI: int = 0):
+    """A_ratio * tauLTP of each FF type, the dsLGN header's LTD ratios (src/patch.cu:4804-4811):
+    learnFF_post's A_ratio (src/condShape.h:137-152) in float with its double literals."""
+    out = []
+    if nE:
+        out.append(_ltd_ratio1(learn.A_LGN, learn.sRatioLGN, learn.r_LTD, learn.tauAvg, learn.tauTrip, learn.tauLTD,
+                               learn.targetFR, learn.tauLTP))
+    if nI:
+        out.append(_ltd_ratio1(learn.A_LGN_I, learn.sRatioLGN_I, learn.r_LTD_I, learn.tauAvg_I, learn.tauTrip_I,
+                               learn.tauLTD_I, learn.targetFR_I, learn.tauLTP_I))
+    return out
 
 
 def _learn_state(sim, m):
@@ -614,7 +691,7 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
     sim = Simulation(m.spec, m.net, m.lgn, m.stim, m.init, m.seeds)
     try:
         learn = None
-        if c.learning == 3:
+        if c.learning:
             learn = _ff_learning(c, m.extra["sRatioLGN"])
             sim.set_ff_learning(learn)
         minimal = bool(c.minimal)
@@ -644,13 +721,17 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
         slgn = dslgn = None
         sample_every = max(int(c.sampleInterval_LGN_V1), 1)
         if learn is not None and int(c.learnData_FF) == 1 and not minimal:
+            nFE, nFI, _ = _learn_types(c)
             sr2 = (list(m.extra["sRatioLGN"]) * 2)[:2]
-            slgn = FM.SLgnWriter(P.slgn, m.nt, sample_every, spec.dt, spec.nV1, m.net.maxLGN, sr2, 1, 0,
-                                 c.values.get("gmaxLGN"), float(c.FF_InfRatio))
+            gm = [float(x) for x in (c.values.get("gmaxLGN") or [])]
+            gm += gm[:1] * (nFE + nFI - len(gm))
+            slgn = FM.SLgnWriter(P.slgn, m.nt, sample_every, spec.dt, spec.nV1, m.net.maxLGN, sr2, nFE, nFI,
+                                 gm, float(c.FF_InfRatio))
             if c.store_dsLGN:
                 tfr = (list(c.values.get("targetFR")) * 2)[:2]
-                dslgn = FM.DsLgnWriter(P.dslgn, m.nt, sample_every, spec.dt, spec.nV1, m.net.maxLGN, sr2, 1, 0,
-                                       c.values.get("A_LGN"), [_ltd_ratio(learn)], tfr, int(c.learnData_FF))
+                dslgn = FM.DsLgnWriter(P.dslgn, m.nt, sample_every, spec.dt, spec.nV1, m.net.maxLGN, sr2, nFE, nFI,
+                                       c.values.get("A_LGN") or [], _ltd_ratio(learn, nFE, nFI), tfr,
+                                       int(c.learnData_FF))
         snaps = not minimal
         if snaps:
             flags |= N.REC_SPIKES          # the spike-word ring of the snapshots
@@ -694,9 +775,11 @@ def run(c: Config, chunk: int = 512, log=print) -> Model:
             if slgn is not None and done % sample_every == 0:
                 slgn.write(sim.state("sLGN"))
                 if dslgn is not None:
+                    # vAvgE [nEt][2] and vAvgI follow the FF types' post traces
                     post = sim.state("ff_post")
-                    nEt = spec.nE * spec.nblock
-                    dslgn.write(post[2 * nEt:4 * nEt], post[4 * nEt:])
+                    nEt, nIt = spec.nE * spec.nblock, spec.nI * spec.nblock
+                    a = post.size - 2 * nEt - nIt
+                    dslgn.write(post[a:a + 2 * nEt], post[a + 2 * nEt:])
             if not c.minimal and (done % interval == 0 or done == m.nt):
                 last_snap = _write_snapshot(sim, c, m, history, last_snap, log)
         for w in (raw, lsp, lfr, frames, sample, slgn, dslgn):

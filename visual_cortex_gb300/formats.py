@@ -500,7 +500,7 @@ class DsLgnWriter:
         self.f.close()
 
 
-def read_slgn(fn, nFF: int = 1):
+def read_slgn(fn):
     """Header dict and the sampled weights [samples][max_LGNperV1][nV1] of an sLGN file."""
     with open(fn, "rb") as f:
         nt, interval = (_r1(f, u32) for _ in range(2))
@@ -618,12 +618,14 @@ def write_reference_snapshot(fn, idx: dict, iModel: int, learning: int, sizes: d
             f.write(trailer)
 
 
-def read_reference_snapshot(fn, nI_total: int, maxLGN: int = 0, nE_total: int = 0, nFF: int = 1):
+def read_reference_snapshot(fn, nI_total: int, maxLGN: int = 0, nE_total: int = 0, nFF_E: int = 1,
+                            nFF_I: int = 0):
     """Reads a snapshot written by the reference (or by write_reference_snapshot); returns the
     fields and the bytes that follow them (this build's checkpoint, if it wrote the file).  A
     snapshot of a learning run also holds the LGN->V1 weights [maxLGN][nV1], the post learning
-    variables (learnVar's FF block, 4 nE_total + nI_total floats for one FF_E type) and the
-    presynaptic traces [nFF][nLGN]."""
+    variables (learnVar's FF block, src/patch.cu:4367-4369: 2 nE_total nFF_E + 2 nI_total nFF_I
+    post traces, then vAvgE [nE_total][2] and vAvgI [nI_total]) and the presynaptic traces
+    [nFF_E + nFF_I][nLGN]."""
     data = open(fn, "rb").read()
     off = 0
 
@@ -637,15 +639,13 @@ def read_reference_snapshot(fn, nI_total: int, maxLGN: int = 0, nE_total: int = 
     iModel, learning = (int(x) for x in take(i32, 2))
     sizes = dict(zip(("nV1", "nLGN", "ngFF", "ngE", "ngI", "nType", "trainDepth"), (int(x) for x in take(u32, 7))))
     n, nl = sizes["nV1"], sizes["nLGN"]
-    if learning and learning != 3:
-        raise ValueError(f"{fn}: a snapshot of a run with learning = {learning} is not read (learning = 3 only)")
     lgn = dict(ltr=take(f32, nl), lnl=take(f32, nl), rng=take(np.uint8, 48 * nl))
     learn = None
     if learning:
         if not maxLGN:
             raise ValueError(f"{fn}: a snapshot of a learning run needs max_LGNperV1 to be read")
-        learn = dict(sLGN=take(f32, maxLGN * n), ff_post=take(f32, 4 * nE_total + nI_total),
-                     ff_pre=take(f32, nFF * nl))
+        post = 2 * nE_total * nFF_E + 2 * nI_total * nFF_I + 2 * nE_total + nI_total
+        learn = dict(sLGN=take(f32, maxLGN * n), ff_post=take(f32, post), ff_pre=take(f32, (nFF_E + nFF_I) * nl))
     v1 = dict(rng_cond=take(np.uint8, 48 * n), rng_noisy=take(np.uint8, 48 * n), tBack=take(f32, n))
     spike_train = take(f32, sizes["trainDepth"] * n).reshape(sizes["trainDepth"], n)
     state = dict(dep=take(f32, n))

@@ -273,8 +273,11 @@ class InitState:
 
 @dataclass
 class FFLearning:
-    """LGN->V1 plasticity parameters as the reference's cfg gives them (learning = 3: one
-    LGN->E triplet-rule type; element [0] of the cfg arrays, gmax/gmin before sRatioLGN)."""
+    """LGN->V1 plasticity parameters as the reference's cfg gives them: `learning` 1 (FF->E
+    triplet rule, the excitatory filtered rate advanced in the delivery), 2 (FF->E and FF->I),
+    3 (FF->E alone) or 4 (the filtered rate alone).  The plain fields are the FF->E type's
+    (element [0] of the cfg arrays, gmax/gmin before sRatioLGN), the *_I fields the FF->I
+    type's (element [nLearnTypeFF_E])."""
     tauLTP: float
     tauLTD: float
     tauTrip: float
@@ -291,6 +294,36 @@ class FFLearning:
     symmetricHomeo: bool = True
     rebound: bool = False
     learning: int = 3
+    nLearnTypeFF_E: int = 1
+    nLearnTypeFF_I: int = 0
+    # the FF->I type (learning = 2 with nLearnTypeFF_I = 1)
+    tauLTP_I: float = 0.0
+    tauLTD_I: float = 0.0
+    tauTrip_I: float = 0.0
+    tauAvg_I: float = 0.0
+    targetFR_I: float = 0.0
+    A_LGN_I: float = 0.0
+    r_LTD_I: float = 0.0
+    gmaxLGN_I: float = 0.0
+    gminLGN_I: float = 0.0
+    sRatioLGN_I: float = 1.0
+    # vAvgE's time constant in the delivery (learning 1, 2, 4): tauAvg[0] with cortical E types
+    tauAvgCortical: float = 0.0
+
+    def to_struct(self):
+        from . import _native as N
+        import dataclasses
+        kw = {f.name: getattr(self, f.name) for f in dataclasses.fields(self)}
+        for k in ("learning", "applyHomeo", "symmetricHomeo", "rebound", "nLearnTypeFF_E", "nLearnTypeFF_I"):
+            kw[k] = int(kw[k])
+        return N.FFLearning(**kw)
+
+
+def ff_post_size(spec: V1Spec, mode: int, ff_i: int) -> int:
+    """Floats of learnVar's FF block (src/patch.cu:4367-4369): the FF->E post traces (none with
+    learning 4), the FF->I ones (ff_i types), vAvgE [nE_total][2] and vAvgI [nI_total]."""
+    nEt, nIt = spec.nE * spec.nblock, (spec.blockSize - spec.nE) * spec.nblock
+    return (0 if mode == 4 else 2 * nEt) + 2 * ff_i * nIt + 2 * nEt + nIt
 
 
 @dataclass
@@ -427,15 +460,13 @@ class Simulation:
         return float(v1.value), float(lgn.value), int(k.value)
 
     def set_ff_learning(self, learning: "FFLearning"):
-        """LGN->V1 plasticity (learning = 3) with the cfg values of `learning` (pv1_set_ff_learning)."""
-        c = N.FFLearning(learning=int(learning.learning), tauLTP=learning.tauLTP, tauLTD=learning.tauLTD,
-                         tauTrip=learning.tauTrip, tauAvg=learning.tauAvg, targetFR=learning.targetFR,
-                         A_LGN=learning.A_LGN, r_LTD=learning.r_LTD, gmaxLGN=learning.gmaxLGN,
-                         gminLGN=learning.gminLGN, sRatioLGN=learning.sRatioLGN,
-                         decayTimeHomeoFF=learning.decayTimeHomeoFF, FF_InfRatio=learning.FF_InfRatio,
-                         applyHomeo=int(learning.applyHomeo), symmetricHomeo=int(learning.symmetricHomeo),
-                         rebound=int(learning.rebound))
+        """LGN->V1 plasticity (learning 1-4) with the cfg values of `learning` (pv1_set_ff_learning)."""
+        c = learning.to_struct()
         N.check(self.plan, N.lib.pv1_set_ff_learning(self.plan, C.byref(c)), "pv1_set_ff_learning")
+        mode = int(learning.learning)
+        self.ff_mode = mode
+        self.ff_i = int(learning.nLearnTypeFF_I) if mode == 2 else 0
+        self.ff_types = 0 if mode == 4 else 1 + self.ff_i
 
     def set_lgn_source(self, device_ptr: int | None, step0: int = 0, nsteps: int = 0):
         """Feed steps [step0, step0 + nsteps) from caller-computed LGN spike words: device_ptr
@@ -493,8 +524,8 @@ class Simulation:
                      lgn_sInfo=self.lgn.nLGN, farPull=(spec.ngE + spec.ngI) * 2 * n,
                      lgn_rng=12 * self.lgn.nLGN, v1_rng_cond=12 * n, v1_rng_noisy=12 * n,
                      sLGN=self.net.maxLGN * n,
-                     ff_post=4 * spec.nE * spec.nblock + (spec.blockSize - spec.nE) * spec.nblock,
-                     ff_pre=self.lgn.nLGN, total_ff=2 * n)
+                     ff_post=ff_post_size(spec, getattr(self, "ff_mode", 3), getattr(self, "ff_i", 0)),
+                     ff_pre=getattr(self, "ff_types", 1) * self.lgn.nLGN, total_ff=2 * n)
         out = np.empty(sizes.get(name, n), f32)
         N.check(self.plan, N.lib.pv1_get_state(self.plan, N.ST[name], N.fptr(out)), f"pv1_get_state({name})")
         if name.endswith("_rng") or name.startswith("v1_rng"):

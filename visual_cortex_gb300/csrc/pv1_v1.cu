@@ -73,6 +73,19 @@ struct LgnPre {
     float s0, f0;
 };
 
+// Starts the copies of one step's LGN spike words of a neuron's m synapses into shared memory
+// (ids and destinations [synapse][kCta] from this thread's column); lgn_words_wait completes
+// them.  Each thread reads back only what it copied, so no CTA barrier is needed.
+__device__ __forceinline__ void lgn_words_async(const float *__restrict__ ring, const int *ids, float *dst, int m) {
+    for (int q = 0; q < m; q++) {
+        const unsigned d = (unsigned)__cvta_generic_to_shared(dst + q * kCta);
+        const float *src = ring + ids[q * kCta];
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void lgn_words_wait() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Fetches the spike words of a neuron's (at most kMaxLgnReg) LGN synapses for one step: ids
 // at ids[q * Stride] (registers: Stride 1; shared memory: Stride kCta).
 template <int Stride>
@@ -534,17 +547,19 @@ __device__ __forceinline__ void lgn_input(const V1Params &P, int itype, float sF
     }
 }
 
-// Phase B: one membrane step of neuron i.  With RegSyn the synapse ids are the register
-// array lgnIds (up to kMaxLgnReg of them) and the weights are read only for synapses that
-// received a spike; otherwise ids and weights are loaded batch by batch.  Returns the
-// spike word.
-template <bool Rng, bool RegSyn>
+// Phase B: one membrane step of neuron i.  With SmemSyn the spike words and weights of the
+// neuron's synapses are in shared memory (smS, smW: [synapse][kCta] from the thread's column);
+// with RegSyn the synapse ids are the register array lgnIds (up to kMaxLgnReg of them) and
+// the weights are read only for synapses that received a spike; otherwise ids and weights are
+// loaded batch by batch.  Returns the spike word.
+template <bool Rng, bool RegSyn, bool SmemSyn = false>
 __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int i, int itype,
                                              float tonic, float depC, int m, const int *lgnIds,
                                              const float *__restrict__ lgnSInfo,
                                              NState &st, curandStateMRG32k3a &condState,
                                              curandStateMRG32k3a &noisyState,
-                                             const LgnPre *pre = nullptr) {
+                                             const LgnPre *pre = nullptr, const float *smW = nullptr,
+                                             const float *smS = nullptr) {
     const int nV1 = P.nV1;
     const float dt = P.dt;
     const int ngE = P.ngE, ngI = P.ngI, ngFF = P.ngFF;
@@ -632,7 +647,20 @@ __device__ __forceinline__ float step_neuron(const V1Params &P, long long t, int
         long long rs = t - P.recStep0;
         if (rs >= 0 && rs < P.recSteps) recFF = P.recFF + ((size_t)rs * nV1 + i) * P.recCap;
     }
-    if constexpr (RegSyn) {
+    if constexpr (SmemSyn) {
+        // the step's spike words (copied in by lgn_words_async) and the weights in shared
+        // memory, [synapse][kCta] from this thread's column: no global load
+        unsigned mask = 0u;
+#pragma unroll
+        for (int q = 0; q < kMaxLgnReg; q++)
+            if (q < m) mask |= (smS[q * kCta] >= 1.0f ? 1u : 0u) << q;
+        while (mask) {
+            const int q = __ffs(mask) - 1;
+            mask &= mask - 1;
+            lgn_input<Rng>(P, itype, smS[q * kCta], smW[q * kCta], backingUp, tBack, pf, nSynFF, g0, h0, g1, h1,
+                           condState, recFF, nFF);
+        }
+    } else if constexpr (RegSyn) {
         // synapses that received a spike, as a bit mask; they are visited in synapse order
         unsigned mask = 0u;
         if (pre) {
@@ -1498,10 +1526,10 @@ __device__ __forceinline__ bool barrier_wait(unsigned *count, unsigned target, c
     return s_ok != 0;
 }
 
-// K steps in one cooperative launch.  Neuron state, generators and up to kMaxLgnReg LGN
-// synapse ids stay in registers; one grid barrier separates consecutive steps, and while a CTA
-// waits at it the spike words of its neurons' LGN synapses for the next step are already
-// fetched (as a bit mask of the synapses that received spikes).
+// K steps in one cooperative launch.  Neuron state and generators stay in registers, the LGN
+// synapses of each thread's neuron (up to kMaxLgnReg: ids, weights, the step's spike words) in
+// shared memory; one grid barrier separates consecutive steps, and while a CTA waits at it the
+// spike words of its neurons' LGN synapses for the next step are copied in.
 template <bool Rng>
 __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, const long long *stepBase,
                                                                  int K, const float *__restrict__ lgnRing,
@@ -1548,16 +1576,23 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
     const float tonic = active ? P.tonicDep[i] : 0.f;
     const float depC = tonic_current(P, itype, tonic);
     const int m = active ? P.nLGNperV1[i] : 0;
-    int lgnIds[kMaxLgnReg];
-#pragma unroll
-    for (int q = 0; q < kMaxLgnReg; q++) lgnIds[q] = q < m ? __ldg(P.lgnId + (size_t)q * P.nV1 + i) : 0;
+    // this neuron's LGN synapses in shared memory, [synapse][kCta] per array: weights, the
+    // current step's spike words (copied in asynchronously a step ahead), cell ids
+    extern __shared__ __align__(16) float lgnSm[];
+    const int mx = P.maxLGN;
+    float *smW = lgnSm + threadIdx.x;
+    float *smS = lgnSm + (size_t)mx * kCta + threadIdx.x;
+    int *smI = reinterpret_cast<int *>(lgnSm + (size_t)2 * mx * kCta) + threadIdx.x;
+    for (int q = 0; q < m; q++) {
+        smI[q * kCta] = __ldg(P.lgnId + (size_t)q * P.nV1 + i);
+        smW[q * kCta] = __ldg(P.sLGN + (size_t)q * P.nV1 + i);
+    }
+    if (active) lgn_words_async(lgnRing + (size_t)(t0 % lgnSlots) * P.lgnN, smI, smS, m);
     // this neuron's outgoing far list (static for the run)
     const int farE0 = (P.farOn && active) ? P.farOff[i] : 0;
     const int farDeg = (P.farOn && active) ? P.farOff[i + 1] - farE0 : 0;
     const int farN1 = (P.farOn && active) ? P.farN1[i] : 0;
     const bool isFarPre = P.farOn && active && P.farPre[i];
-    LgnPre lgnPre{0u, 0.f, 0.f};
-    bool haveMask = false;
     for (int s = 0; s < K; s++) {
         const long long t = t0 + s;
         const unsigned long long farSize = P.farOn ? far_list_size(P, t - 1) : 0ull;
@@ -1565,8 +1600,9 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
         float sInfo = 0.f;
         if (active) {
             const float *lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
-            sInfo = step_neuron<Rng, true>(P, t, i, itype, tonic, depC, m, lgnIds, lgnSInfo, st, condState,
-                                           noisyState, haveMask ? &lgnPre : nullptr);
+            lgn_words_wait();
+            sInfo = step_neuron<Rng, false, true>(P, t, i, itype, tonic, depC, m, nullptr, lgnSInfo, st, condState,
+                                                  noisyState, nullptr, smW, smS);
             if (P.spikeCount && sInfo >= 1.0f) P.spikeCount[i] += (unsigned)floorf(sInfo);
             if (sInfo >= 1.0f) prefetch_spiker(P, b, local, farE0, farDeg);
         }
@@ -1576,13 +1612,14 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
         }
         if (s + 1 < K) {
             barrier_arrive(barrier, &s_arrived);
-            lgnPre.mask = 0u;
-            if (active) lgnPre = lgn_prefetch<1>(P, lgnRing + (size_t)((t + 1) % lgnSlots) * P.lgnN, lgnIds, m, i);
-            haveMask = true;
+            // the next step's LGN rows are complete before the launch: their copies run while
+            // this CTA waits at the barrier
+            if (active) lgn_words_async(lgnRing + (size_t)((t + 1) % lgnSlots) * P.lgnN, smI, smS, m);
             if (!barrier_wait(barrier, (unsigned)gridDim.x * (unsigned)(s + 1), &s_arrived, P.err, P.waitSpins))
                 break;
         }
     }
+    lgn_words_wait();
     if (active) {
         store_state(P, i, st);
         if (Rng && P.condRng) P.rGenCond[i] = condState;
@@ -1918,15 +1955,25 @@ cudaError_t launch_v1_step(const V1Params &p, const long long *stepBase, int ste
 }
 
 // Number of CTAs of the persistent kernel and whether they can all be resident at once.
+// Dynamic shared memory of the persistent kernel: weights, spike words and ids of up to maxLGN
+// LGN synapses per thread.
+static size_t v1_persistent_smem(const V1Params &p) {
+    return (size_t)3 * std::max(p.maxLGN, 1) * kCta * sizeof(float);
+}
+
 int v1_persistent_ctas(const V1Params &p, int device, bool *fits, int *pushCtas) {
     const int nq = (p.blockSize + kCta - 1) / kCta;
     const int n = p.nblock * nq;
     *pushCtas = 0;
     int perSM = 0, sms = 0;
+    const int maxDyn = (int)((size_t)3 * kMaxLgnReg * kCta * sizeof(float));
+    cudaFuncSetAttribute(v1_persistent_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxDyn);
+    cudaFuncSetAttribute(v1_persistent_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxDyn);
+    const size_t dyn = v1_persistent_smem(p);
     if (needs_rng(p))
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_persistent_kernel<true>, kCta, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_persistent_kernel<true>, kCta, dyn);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_persistent_kernel<false>, kCta, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_persistent_kernel<false>, kCta, dyn);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     int coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
@@ -1943,7 +1990,7 @@ cudaError_t launch_v1_persistent(const V1Params &p, const long long *stepBase, i
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(p.nblock * nq + p.pushCta);
     cfg.blockDim = dim3(kCta);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = v1_persistent_smem(p);
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;

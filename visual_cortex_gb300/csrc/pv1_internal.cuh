@@ -211,6 +211,7 @@ struct V1Params {
     const float *farStr;       // [nnz]
     const int *farSteps;       // [nnz] it2post
     const float *farFrac;      // [nnz] it2post*dt - delay/speed
+    const int4 *farRec;        // [nnz] the four above in one record: post, str, steps, frac
     const unsigned char *farPre;  // [nV1] 1 if the neuron is a far presynaptic partner
     unsigned long long *farAcc;   // [farDepth][ngE+ngI][2][nV1] fixed-point g,h
     int farDepth;

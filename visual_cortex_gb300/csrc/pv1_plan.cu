@@ -1296,6 +1296,17 @@ int build_event_lists(pv1_plan *p, const std::vector<EvSyn> &syn) {
     r |= dev_upload(p, &d_steps, steps.data(), nnz);
     r |= dev_upload(p, &d_str, str.data(), nnz);
     r |= dev_upload(p, &d_frac, frac.data(), nnz);
+    // the same four values packed per synapse (one 16-byte load in the push)
+    std::vector<int4> rec(nnz);
+    for (size_t e = 0; e < nnz; e++) {
+        float fs = str[e], ff = frac[e];
+        int bs_, bf_;
+        memcpy(&bs_, &fs, 4);
+        memcpy(&bf_, &ff, 4);
+        rec[e] = make_int4(post[e], bs_, steps[e], bf_);
+    }
+    int4 *d_rec;
+    r |= dev_upload(p, &d_rec, rec.data(), nnz);
     r |= dev_upload(p, &d_pre, isPre.data(), nV1);
     r |= dev_alloc(p, &d_acc, ringLen);
     if (anyNear) r |= dev_alloc(p, &d_nacc, ringLen);
@@ -1308,6 +1319,7 @@ int build_event_lists(pv1_plan *p, const std::vector<EvSyn> &syn) {
     v.farSteps = d_steps;
     v.farStr = d_str;
     v.farFrac = d_frac;
+    v.farRec = d_rec;
     v.farPre = d_pre;
     v.farAcc = d_acc;
     v.nearAcc = d_nacc;

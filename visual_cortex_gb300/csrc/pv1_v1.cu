@@ -240,13 +240,9 @@ __device__ __forceinline__ void prefetch_spiker(const V1Params &P, int b, int lo
             asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(row), "r"(bytes) : "memory");
         }
     }
-    const int a = (farE0 + 3) & ~3, z = (farE0 + farDeg) & ~3;
-    if (z > a) {
-        const unsigned bytes = (unsigned)(z - a) * 4u;
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(P.farPost + a), "r"(bytes) : "memory");
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(P.farStr + a), "r"(bytes) : "memory");
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(P.farSteps + a), "r"(bytes) : "memory");
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(P.farFrac + a), "r"(bytes) : "memory");
+    if (farDeg > 0) {
+        const unsigned bytes = (unsigned)farDeg * 16u;
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(P.farRec + farE0), "r"(bytes) : "memory");
     }
 }
 
@@ -268,13 +264,17 @@ __device__ __forceinline__ void learn_avg_delivery(const V1Params &P, float post
     vAvg[0] = lAvgE;
 }
 
+__device__ __forceinline__ int far_ring_slot(const V1Params &P, long long t);
+
 // Phase A: delivery of step tp's spikes to this thread's neuron (all threads of the CTA
 // must call it; `active` masks the neuron work).
 template <bool Rng>
 __device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, int b, int local, int i,
                                              bool active, int itype, NState &st,
-                                             curandStateMRG32k3a &condState, Smem &sm) {
+                                             curandStateMRG32k3a &condState, Smem &sm, int farSlot = -1) {
     const int bs = P.blockSize, nV1 = P.nV1;
+    // the far ring slot of step tp (tp mod farDepth; passed in by the persistent kernel)
+    if (farSlot < 0) farSlot = far_ring_slot(P, tp);
     const int ngE = P.ngE, ngI = P.ngI;
     const float *sPrev = P.sInfo + (size_t)(tp & 1) * nV1;
     float lgE[kMaxNG], lhE[kMaxNG], lgI[kMaxNG], lhI[kMaxNG], ipE[kMaxNG], ipI[kMaxNG];
@@ -290,7 +290,7 @@ __device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, in
     unsigned long long *acc = nullptr;
     bool farSpiked = false;
     if (P.farClass && active) {
-        acc = P.farAcc + (size_t)(tp % P.farDepth) * ns * 2 * nV1;
+        acc = P.farAcc + (size_t)farSlot * ns * 2 * nV1;
         farSpiked = __ldcg(P.farFlag + tp % 3) != 0;
 #pragma unroll
         for (int q = 0; q < 2 * kMaxNG; q++) {
@@ -356,7 +356,7 @@ __device__ __forceinline__ void deliver_prev(const V1Params &P, long long tp, in
     // conductance update; here they were pushed into their own ring
     if (!P.noDelay) {
         if (P.nearOn && active) {
-            unsigned long long *nacc = P.nearAcc + (size_t)(tp % P.farDepth) * ns * 2 * nV1;
+            unsigned long long *nacc = P.nearAcc + (size_t)farSlot * ns * 2 * nV1;
 #pragma unroll
             for (int q = 0; q < 2 * kMaxNG; q++) {
                 if (q < ns) {
@@ -1284,12 +1284,12 @@ __device__ __forceinline__ unsigned long long far_list_size(const V1Params &P, l
 // appends which event, and in which order.
 template <int U = 1>
 __device__ __forceinline__ void far_push_range(const V1Params &P, long long tl, Smem &sm, int cta, int nCta,
-                                               unsigned long long size, int lo, int hi) {
+                                               unsigned long long size, int lo, int hi, int tSlot = -1) {
     const int n = (int)(size >> 32);
     if (n == 0 || lo >= hi) return;
     const int slot = (int)((tl + 3) % 3);  // tl >= -1
     const int4 *list = P.farList + (size_t)slot * P.nV1;
-    const int tSlot = far_ring_slot(P, tl);
+    if (tSlot < 0) tSlot = far_ring_slot(P, tl);
     const int G = nCta * kCta;
     const int gt = cta * kCta + threadIdx.x;
     int base = 0;  // items of the earlier chunks
@@ -1323,10 +1323,11 @@ __device__ __forceinline__ void far_push_range(const V1Params &P, long long tl, 
                     const int r = owner_of(sm, cnt, wu);
                     const int e = sm.fe0[r] + (wu - sm.fpref[r]);
                     rr[u] = r;
-                    post[u] = __ldg(P.farPost + e);
-                    f[u] = __ldg(P.farStr + e);
-                    sp[u] = __ldg(P.farSteps + e);
-                    frac[u] = __ldg(P.farFrac + e);
+                    const int4 rc = __ldg(P.farRec + e);
+                    post[u] = rc.x;
+                    f[u] = __int_as_float(rc.y);
+                    sp[u] = rc.z;
+                    frac[u] = __int_as_float(rc.w);
                 }
             }
 #pragma unroll
@@ -1356,7 +1357,8 @@ __device__ __forceinline__ void far_push_list(const V1Params &P, long long tl, S
 // (whole-step delay 0 or 1: the first n1 synapses of each list), which must be in the ring
 // before the next step delivers it.  All threads of the CTA call it.
 __device__ __forceinline__ void far_phase(const V1Params &P, long long t, int i, bool active, float sInfo,
-                                          bool isFarPre, int e0, int deg, int n1, Smem &sm, int cta) {
+                                          bool isFarPre, int e0, int deg, int n1, Smem &sm, int cta,
+                                          int tSlot = -1) {
     if (cta == 0 && threadIdx.x == 0) {
         P.farFlag[(t + 1) % 3] = 0;
         P.farCount[(t + 1) % 3] = 0ull;
@@ -1402,14 +1404,15 @@ __device__ __forceinline__ void far_phase(const V1Params &P, long long t, int i,
     scan_degrees(sm, cnt);
     __syncthreads();
     const int work = sm.fpref[cnt];
-    const int tSlot = far_ring_slot(P, t);
+    if (tSlot < 0) tSlot = far_ring_slot(P, t);
     for (int w = threadIdx.x; w < work; w += kCta) {
         const int r = owner_of(sm, cnt, w);
         const int e = sm.fe0[r] + (w - sm.fpref[r]);
-        const int post = __ldg(P.farPost + e);
-        const float f = __ldg(P.farStr + e);
-        const int sp = __ldg(P.farSteps + e);
-        const float frac = __ldg(P.farFrac + e);
+        const int4 rc = __ldg(P.farRec + e);
+        const int post = rc.x;
+        const float f = __int_as_float(rc.y);
+        const int sp = rc.z;
+        const float frac = __int_as_float(rc.w);
         const int steps = sp & 0xffff;
         // steps is 0 or 1 here: the slot with tArr == t
         far_event(P, t, tSlot, sm.fpre[r], sm.fsi[r], post, f, steps, sp, frac, steps);
@@ -1548,12 +1551,14 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
         // far-push CTA: in step t it pushes the far events of step t - 1's spikers (those that
         // arrive after step t - 1) while the neuron CTAs deliver and step; the grid barrier
         // that ends step t orders them before the delivery that reads them
+        int fsPrev = far_ring_slot(P, t0 - 1);  // far ring slot of step t0 + s - 1
         for (int s = 0; s < K; s++) {
             if (P.farOn) {
                 const unsigned long long size = far_list_size(P, t0 + s - 1);
                 far_push_range<kPushBatch>(P, t0 + s - 1, sm, (int)blockIdx.x - nNeuron, P.pushCta, size, 0,
-                                           min((int)(size & 0xffffffffu), pushShare));
+                                           min((int)(size & 0xffffffffu), pushShare), fsPrev);
             }
+            if (++fsPrev == P.farDepth) fsPrev = 0;
             if (s + 1 < K) {
                 barrier_arrive(barrier, &s_arrived);
                 if (!barrier_wait(barrier, (unsigned)gridDim.x * (unsigned)(s + 1), &s_arrived, P.err, P.waitSpins))
@@ -1587,7 +1592,10 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
         smI[q * kCta] = __ldg(P.lgnId + (size_t)q * P.nV1 + i);
         smW[q * kCta] = __ldg(P.sLGN + (size_t)q * P.nV1 + i);
     }
-    if (active) lgn_words_async(lgnRing + (size_t)(t0 % lgnSlots) * P.lgnN, smI, smS, m);
+    // ring slots kept incrementally (t mod lgnSlots, t mod farDepth)
+    int lgnSlot = (int)(t0 % lgnSlots);
+    int fsT = far_ring_slot(P, t0), fsPrev = far_ring_slot(P, t0 - 1);
+    if (active) lgn_words_async(lgnRing + (size_t)lgnSlot * P.lgnN, smI, smS, m);
     // this neuron's outgoing far list (static for the run)
     const int farE0 = (P.farOn && active) ? P.farOff[i] : 0;
     const int farDeg = (P.farOn && active) ? P.farOff[i + 1] - farE0 : 0;
@@ -1596,10 +1604,11 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
     for (int s = 0; s < K; s++) {
         const long long t = t0 + s;
         const unsigned long long farSize = P.farOn ? far_list_size(P, t - 1) : 0ull;
-        if (s > 0 || deliverFirst) deliver_prev<Rng>(P, t - 1, b, local, i, active, itype, st, condState, sm);
+        if (s > 0 || deliverFirst) deliver_prev<Rng>(P, t - 1, b, local, i, active, itype, st, condState, sm, fsPrev);
+        const int lgnNext = lgnSlot + 1 == lgnSlots ? 0 : lgnSlot + 1;
         float sInfo = 0.f;
         if (active) {
-            const float *lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
+            const float *lgnSInfo = lgnRing + (size_t)lgnSlot * P.lgnN;
             lgn_words_wait();
             sInfo = step_neuron<Rng, false, true>(P, t, i, itype, tonic, depC, m, nullptr, lgnSInfo, st, condState,
                                                   noisyState, nullptr, smW, smS);
@@ -1607,17 +1616,21 @@ __global__ void __launch_bounds__(kCta, 1) v1_persistent_kernel(V1Params P, cons
             if (sInfo >= 1.0f) prefetch_spiker(P, b, local, farE0, farDeg);
         }
         if (P.farOn) {
-            far_push_range(P, t - 1, sm, blockIdx.x, nNeuron, farSize, pushShare, (int)(farSize & 0xffffffffu));
-            far_phase(P, t, i, active, sInfo, isFarPre, farE0, farDeg, farN1, sm, blockIdx.x);
+            far_push_range(P, t - 1, sm, blockIdx.x, nNeuron, farSize, pushShare, (int)(farSize & 0xffffffffu),
+                           fsPrev);
+            far_phase(P, t, i, active, sInfo, isFarPre, farE0, farDeg, farN1, sm, blockIdx.x, fsT);
         }
+        fsPrev = fsT;
+        if (++fsT == P.farDepth) fsT = 0;
         if (s + 1 < K) {
             barrier_arrive(barrier, &s_arrived);
             // the next step's LGN rows are complete before the launch: their copies run while
             // this CTA waits at the barrier
-            if (active) lgn_words_async(lgnRing + (size_t)((t + 1) % lgnSlots) * P.lgnN, smI, smS, m);
+            if (active) lgn_words_async(lgnRing + (size_t)lgnNext * P.lgnN, smI, smS, m);
             if (!barrier_wait(barrier, (unsigned)gridDim.x * (unsigned)(s + 1), &s_arrived, P.err, P.waitSpins))
                 break;
         }
+        lgnSlot = lgnNext;
     }
     lgn_words_wait();
     if (active) {

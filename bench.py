@@ -260,8 +260,9 @@ def run_gb300(args):
 
 def bench_batched(n_trials: int):
     """The batched sweep: n_trials instances of an 8 x 1024 patch, 12 orientations, contrast
-    U[0.1, 1], durations U[250, 2000] ms, all run to their ends by one Batch (autotuned).
-    Value = sum over trials of neurons x steps / device time of the whole sweep."""
+    U[0.1, 1], durations U[250, 2000] ms, all run to their ends by one Batch, twice: in
+    autotuned chunks, and as one graph with one cooperative V1 launch (pv1_batch_sweep, the
+    line's value).  Value = sum over trials of neurons x steps / device time of the sweep."""
     from visual_cortex_gb300 import synth
     from visual_cortex_gb300.batch import Batch
     from visual_cortex_gb300.model import Simulation
@@ -278,13 +279,31 @@ def bench_batched(n_trials: int):
     for s in sims:
         s.close()
     work = sum(t.steps * t.wl.spec.nV1 for t in trials)
-    return {"value": work / (ms * 1e-3), "unit": UNIT, "device_ms": ms,
-            "e2e": {"value": work / e2e_s, "unit": UNIT,
+    # the same trials as one graph of three launches (pv1_batch_sweep): the LGN stage of every
+    # step, ONE cooperative V1 launch (slots run their trials longest first), the advance
+    t0 = time.perf_counter()
+    sims = [Simulation(t.wl.spec, t.wl.net, t.wl.lgn, t.wl.stim, t.wl.init, t.wl.seeds) for t in trials]
+    b = Batch(sims, [t.steps for t in trials], autotune=False)
+    sweep_ms = b.sweep()
+    sweep_rates = [b.stats(q)[1] for q in range(len(trials))]
+    sweep_e2e_s = time.perf_counter() - t0
+    sweep_launches = b.launches()
+    b.close()
+    for s in sims:
+        s.close()
+    sweep = {"value": work / (sweep_ms * 1e-3), "unit": UNIT, "device_ms": sweep_ms,
+             "gpu_launches": sweep_launches, "e2e": {"value": work / sweep_e2e_s, "unit": UNIT},
+             "mean_rate_hz": float(np.mean(sweep_rates)),
+             "same_rates_as_chunked": bool(np.array_equal(np.float64(rates), np.float64(sweep_rates)))}
+    chunked = {"value": work / (ms * 1e-3), "unit": UNIT, "device_ms": ms, "gpu_launches": launches,
+               "tuning": tuning, "e2e": {"value": work / e2e_s, "unit": UNIT}}
+    return {"value": sweep["value"], "unit": UNIT, "device_ms": sweep_ms,
+            "e2e": {"value": work / sweep_e2e_s, "unit": UNIT,
                     "note": "plan creation with all host->device uploads, the sweep and the FP64 rate read-back"},
             "workload": f"{n_trials} trials x 8x1024 V1 / 4096 LGN, 128x128 gratings at 12 orientations, "
                         "contrast U[0.1,1], durations U[250,2000] ms, dt 0.125 ms",
-            "neuron_steps": work, "trial_steps": [t.steps for t in trials], "gpu_launches": launches,
-            "tuning": tuning, "mean_rate_hz": float(np.mean(rates))}
+            "neuron_steps": work, "trial_steps": [t.steps for t in trials], "gpu_launches": sweep_launches,
+            "one_launch_sweep": sweep, "chunked_autotuned": chunked, "mean_rate_hz": float(np.mean(rates))}
 
 
 def bench_adjoint(reps: int = 3):

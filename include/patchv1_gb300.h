@@ -518,8 +518,18 @@ int pv1_batch_tuning(const pv1_batch *batch, int *K, int *minB, float *times);
  * null) and their mean, from spike counters kept by the V1 kernel since pv1_batch_create. */
 int pv1_batch_stats(pv1_batch *batch, uint32_t trial, double *simTimeMs, double *rates,
                     double *meanRate);
-/* Kernel launches issued by the last pv1_batch_run. */
+/* Kernel launches issued by the last pv1_batch_run or pv1_batch_sweep. */
 int64_t pv1_batch_launch_count(const pv1_batch *batch);
+/* Runs the rest of every trial as one CUDA graph of three launches: the LGN stage of every
+ * remaining step of every trial (into per-trial buffers of one row per step, allocated for
+ * the call: remaining steps x nLGN floats per trial), ONE cooperative V1 launch in which each
+ * slot of CTAs runs its trials one after the other, each for all its remaining steps (trials
+ * assigned to slots longest first, each to the least loaded slot), and the advance.  Each
+ * trial computes exactly what pv1_run computes for it alone.  Needs the persistent variant
+ * (the largest trial co-resident) and single-class LGN cells; otherwise PV1_E_UNSUPPORTED.
+ * Returns 0 (every trial done) or a negative error code; *ms (may be null) receives the
+ * device time of the graph. */
+int pv1_batch_sweep(pv1_batch *batch, float *ms);
 
 /* ---- Surrogate-gradient adjoint ----------------------------------------------------------
  * No counterpart in the reference (it has no gradient code).  The differentiable form of the

@@ -51,6 +51,45 @@ def test_batch_equals_trials_alone(native, autotune):
             s.close()
 
 
+def test_batch_sweep_in_one_launch(native):
+    """pv1_batch_sweep: the rest of every trial (uneven durations and sizes) as one graph of
+    three launches -- the LGN stage of every remaining step, one cooperative V1 launch with the
+    trials scheduled longest first on the slots, the advance -- after a chunked start; every
+    trial ends bit-identical to the same trial run alone."""
+    from visual_cortex_gb300.batch import Batch
+    from visual_cortex_gb300 import synth
+    trials = _trials(n_trials=5, dur_ms=(6.0, 30.0))
+    big = synth.batch_trials(n_trials=1, seed=7, nblock=3, n_lgn=512, width=64, height=64, nFrame=60,
+                             far_partners=50, dur_ms=(20.0, 20.0))
+    trials = trials + big
+    alone, batched = [], []
+    try:
+        for tr in trials:
+            s = _sim(tr.wl)
+            s.persistent(0)
+            s.run(tr.steps)
+            alone.append(s)
+        batched = [_sim(tr.wl) for tr in trials]
+        b = Batch(batched, [tr.steps for tr in trials], autotune=False)
+        try:
+            b.run(max_steps=20)
+            ms = b.sweep()
+            assert ms > 0 and b.launches() == 3
+            for q, tr in enumerate(trials):
+                assert batched[q].step == tr.steps
+                for k in STATE:
+                    np.testing.assert_array_equal(batched[q].state(k), alone[q].state(k),
+                                                  err_msg=f"trial {q} {k}")
+                t, mean, rates = b.stats(q, rates=True)
+                assert t == pytest.approx(tr.steps * tr.wl.spec.dt, rel=1e-12)
+            assert b.sweep() == 0.0
+        finally:
+            b.close()
+    finally:
+        for s in alone + batched:
+            s.close()
+
+
 def test_batch_in_pieces_with_noise(native):
     """maxSteps slices, a trial continuing after the batch, noise and failure draws."""
     from visual_cortex_gb300.batch import Batch

@@ -176,6 +176,7 @@ def _load() -> C.CDLL:
         "pv1_batch_stats": ([P, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                              C.POINTER(C.c_double)], C.c_int),
         "pv1_batch_launch_count": ([P], C.c_int64),
+        "pv1_batch_sweep": ([P, _FP], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -57,6 +57,17 @@ class Batch:
             self.remaining[q] -= k
         return int(left), float(ms.value)
 
+    def sweep(self) -> float:
+        """Runs the rest of every trial as one graph: the LGN stage of all remaining steps, one
+        cooperative V1 launch (each slot runs its trials for all their steps, longest trials
+        first), the advance (pv1_batch_sweep).  Returns the device ms."""
+        ms = C.c_float()
+        self._check(N.lib.pv1_batch_sweep(self.h, C.byref(ms)), "pv1_batch_sweep")
+        for q, s in enumerate(self.sims):
+            s.step += self.remaining[q]
+            self.remaining[q] = 0
+        return float(ms.value)
+
     def tuning(self):
         K, mb = C.c_int(), C.c_int()
         t = np.empty(12, np.float32)

@@ -395,6 +395,126 @@ int64_t pv1_batch_run(pv1_batch *b, uint64_t maxSteps, float *ms) {
     return left;
 }
 
+int pv1_batch_sweep(pv1_batch *b, float *ms) {
+    if (!b) return PV1_E_ARG;
+    if (!b->allClass || b->nSlots <= 0)
+        return bfail(b, PV1_E_UNSUPPORTED,
+                     "the one-launch sweep needs single-class LGN cells and every trial co-resident in a slot");
+    std::vector<long long> left(b->n);
+    long long maxLeft = 0;
+    for (int q = 0; q < b->n; q++) {
+        left[q] = std::max(0LL, b->end[q] - b->step[q]);
+        maxLeft = std::max(maxLeft, left[q]);
+    }
+    b->launches = 0;
+    if (maxLeft == 0) {
+        if (ms) *ms = 0.f;
+        return 0;
+    }
+    if (maxLeft > (1LL << 30)) return bfail(b, PV1_E_ARG, "too many steps for one launch");
+    // per-trial LGN buffers of one row per remaining step (row = step mod rows, distinct for the
+    // trial's remaining steps), in copies of the trial blocks
+    std::vector<BatchTrial> T = b->hT;
+    std::vector<BatchLgn> L = b->hL;
+    std::vector<void *> bufs;
+    auto release = [&]() {
+        for (void *ptr : bufs) cudaFree(ptr);
+        bufs.clear();
+    };
+    auto fresh = [&](float **ptr, size_t n) {
+        if (cudaMalloc((void **)ptr, n * sizeof(float)) != cudaSuccess) return false;
+        bufs.push_back(*ptr);
+        return true;
+    };
+    for (int q = 0; q < b->n; q++) {
+        if (!left[q]) continue;
+        const int rows = (int)left[q];
+        const size_t cells = (size_t)L[q].p.nLGN;
+        float *sp = nullptr, *fr = nullptr;
+        if (!fresh(&sp, (size_t)rows * cells) || (L[q].p.outFr && !fresh(&fr, (size_t)rows * cells))) {
+            release();
+            return bfail(b, PV1_E_NOMEM, "cudaMalloc of the sweep's LGN buffers");
+        }
+        L[q].p.outSInfo = sp;
+        if (L[q].p.outFr) L[q].p.outFr = fr;
+        L[q].p.outSlots = rows;
+        T[q].lgnRing = sp;
+        T[q].lgnSlots = rows;
+    }
+    // slot schedule: longest trial first, each to the least loaded slot; the kernel's slot s
+    // takes list entries s, s + nSlots, ... (-1: nothing)
+    std::vector<int> order(b->n);
+    for (int q = 0; q < b->n; q++) order[q] = q;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return left[x] > left[y]; });
+    std::vector<std::vector<int>> per(b->nSlots);
+    std::vector<long long> load(b->nSlots, 0);
+    for (int q : order) {
+        if (!left[q]) continue;
+        const int sl = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        per[sl].push_back(q);
+        load[sl] += left[q];
+    }
+    size_t depth = 0;
+    for (auto &v : per) depth = std::max(depth, v.size());
+    std::vector<int> list(depth * b->nSlots, -1);
+    for (int sl = 0; sl < b->nSlots; sl++)
+        for (size_t k = 0; k < per[sl].size(); k++) list[k * b->nSlots + sl] = per[sl][k];
+    const int nList = (int)list.size();
+    BatchTrial *dTs = nullptr;
+    BatchLgn *dLs = nullptr;
+    int *dList = nullptr, *dNList = nullptr;
+    bool ok = cudaMalloc((void **)&dTs, b->n * sizeof(BatchTrial)) == cudaSuccess;
+    if (ok) bufs.push_back(dTs);
+    ok = ok && cudaMalloc((void **)&dLs, b->n * sizeof(BatchLgn)) == cudaSuccess;
+    if (ok) bufs.push_back(dLs);
+    ok = ok && cudaMalloc((void **)&dList, list.size() * sizeof(int)) == cudaSuccess;
+    if (ok) bufs.push_back(dList);
+    ok = ok && cudaMalloc((void **)&dNList, sizeof(int)) == cudaSuccess;
+    if (ok) bufs.push_back(dNList);
+    if (!ok) {
+        release();
+        return bfail(b, PV1_E_NOMEM, "cudaMalloc of the sweep's tables");
+    }
+    cudaError_t e = cudaMemcpyAsync(dTs, T.data(), b->n * sizeof(BatchTrial), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dLs, L.data(), b->n * sizeof(BatchLgn), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dList, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dNList, &nList, sizeof(int), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    // the sweep as one graph: LGN stage, one cooperative V1 launch, advance
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ex = nullptr;
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t e1 = launch_lgn_class_batch(dLs, b->n, b->maxCellCtas, (int)maxLeft, b->stream);
+        if (e1 == cudaSuccess)
+            e1 = launch_v1_batch_persistent(dTs, dList, dNList, b->slotCtas, b->nSlots, (int)maxLeft, b->dBar, b->n,
+                                            b->rng, b->stream);
+        if (e1 == cudaSuccess) e1 = launch_batch_advance(dTs, b->n, (int)maxLeft, b->dSimTime, b->stream);
+        cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+        e = e1 != cudaSuccess ? e1 : e2;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&ex, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev0, b->stream);
+    if (e == cudaSuccess) e = cudaGraphLaunch(ex, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev1, b->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b->ev1);
+    if (ex) cudaGraphExecDestroy(ex);
+    if (e == cudaSuccess && ms) e = cudaEventElapsedTime(ms, b->ev0, b->ev1);
+    release();
+    if (e != cudaSuccess) return bfail(b, PV1_E_CUDA, std::string("sweep: ") + cudaGetErrorString(e));
+    b->launches = 3;
+    int r = check_errors(b);
+    if (r) return r;
+    for (int q = 0; q < b->n; q++) {
+        b->step[q] = b->end[q];
+        plan_batch_finish(b->plans[q], b->step[q]);
+    }
+    return 0;
+}
+
 int pv1_batch_stats(pv1_batch *b, uint32_t trial, double *simTimeMs, double *rates, double *meanRate) {
     if (!b || trial >= (uint32_t)b->n) return PV1_E_ARG;
     const int nV1 = b->hT[trial].v.nV1;

@@ -713,9 +713,9 @@ __global__ void __launch_bounds__(kClassCta) lgn_class_kernel(LgnParams P, const
     lgn_class_body(P, *stepBase, K, blockIdx.x * kClassCta);
 }
 
-// The single-class LGN chunk for every trial of a batch: grid (cell CTAs, trials); each CTA
+// The single-class LGN stage for every trial of a batch: grid (cell CTAs, trials); each CTA
 // copies its trial's parameters to shared memory and runs the same body for the steps the
-// trial still has in this chunk.
+// trial still has among the next K (in pieces of at most kClassMaxK steps).
 __global__ void __launch_bounds__(kClassCta) lgn_class_batch_kernel(const BatchLgn *__restrict__ trials, int K) {
     __shared__ __align__(16) BatchLgn sT;
     const int *src = reinterpret_cast<const int *>(trials + blockIdx.y);
@@ -726,7 +726,12 @@ __global__ void __launch_bounds__(kClassCta) lgn_class_batch_kernel(const BatchL
     const long long left = sT.tEnd - t0;
     const int k = left < K ? (int)left : K;
     if (k <= 0 || (int)blockIdx.x * kClassCta >= sT.p.nMagno) return;
-    lgn_class_body(sT.p, t0, k, blockIdx.x * kClassCta);
+    // chunks of at most kClassMaxK steps (the shared tables of one chunk's frames); the cells'
+    // carried state passes from one chunk to the next through global memory
+    for (int off = 0; off < k; off += kClassMaxK) {
+        if (off) __syncthreads();
+        lgn_class_body(sT.p, t0 + off, min(kClassMaxK, k - off), blockIdx.x * kClassCta);
+    }
 }
 
 // Temporal contraction and logistic rate for (cell, step) pairs of a chunk of K steps: grid
@@ -994,7 +999,7 @@ cudaError_t launch_lgn_step(const LgnParams &p, const long long *stepBase, int K
 
 cudaError_t launch_lgn_class_batch(const BatchLgn *trials, int nTrials, int maxCellCtas, int K, cudaStream_t st) {
     if (nTrials <= 0 || maxCellCtas <= 0) return cudaSuccess;
-    if (K > kClassMaxK) return cudaErrorInvalidValue;
+    if (K <= 0) return cudaErrorInvalidValue;
     const size_t smem = (size_t)kClassMaxSlots * kClassCta * sizeof(float);
     static bool attrSet = false;
     if (!attrSet) {

@@ -2179,6 +2179,7 @@ __global__ void __launch_bounds__(kCta, 2) v1_batch_persistent_kernel(const Batc
     const int na = *nActive;
     for (int j = slot; j < na; j += nSlots) {
         const int q = activeList[j];
+        if (q < 0) continue;  // a slot's schedule ended (one-launch sweep)
         __syncthreads();
         const int *src = reinterpret_cast<const int *>(trials + q);
         int *dst = reinterpret_cast<int *>(&sT);

@@ -1223,21 +1223,17 @@ __device__ __forceinline__ void far_event(const V1Params &P, long long t, int tS
         if (ig < ng) {
             const float ip = preE ? P.pE[ptype * P.ngE + ig] : P.pI[ptype * P.ngI + ig];
             const float fv = __fmul_rn(__fmul_rn((float)nsp, f), ip);
-            // conductance input of the arrival (cond_input of src/condShape.h:42-51).  Far
-            // arrivals use the hardware exponential and division: the reference computes them
-            // on the host, so no device expression reproduces its bits, and these are within a
-            // few ulp; delayed near events (device code in the reference) keep expf and '/'
+            // conductance input of the arrival (cond_input of src/condShape.h:42-51) with the
+            // hardware exponential and division (within a few ulp): the reference computes far
+            // arrivals on the host, so no device expression reproduces its bits, and the
+            // fixed-point ring already sums delayed near events in another order than its
+            // recal_G_mat; the precise forms cost 14% of the step here
             const float rise = preE ? P.condE.rise[ig] : P.condI.rise[ig];
             const float dec = preE ? P.condE.decay[ig] : P.condI.decay[ig];
             const float dod = preE ? P.condE.dod[ig] : P.condI.dod[ig];
-            float g = 0.f, h = 0.f;
-            if (nearClass) {
-                cond_input_v(rise, dec, dod, g, h, fv, delta);
-            } else {
-                const float etr = __expf(-__fdividef(delta, rise));
-                g = fv * dod * (__expf(-__fdividef(delta, dec)) - etr);
-                h = fv * etr;
-            }
+            const float etr = __expf(-__fdividef(delta, rise));
+            const float g = fv * dod * (__expf(-__fdividef(delta, dec)) - etr);
+            const float h = fv * etr;
             atomicAdd(&acc[(size_t)(2 * (qoff + ig)) * nV1 + post], (unsigned long long)far_to_fixed(g));
             atomicAdd(&acc[(size_t)(2 * (qoff + ig) + 1) * nV1 + post], (unsigned long long)far_to_fixed(h));
         }

@@ -33,7 +33,8 @@ constexpr int kCta = 256;
 constexpr int kWarps = kCta / 32;
 constexpr int kMaxBS = 1024;
 constexpr int kLgnBatch = 8;
-constexpr int kMaxLgnReg = 32;        // LGN synapse ids kept in registers by the persistent kernel
+constexpr int kMaxLgnReg = 32;        // LGN synapses kept in shared memory by the persistent kernel
+constexpr int kBatchLgn = 24;         // the same in the batched persistent kernel (two blocks per SM)
 constexpr int kConBatch = 8;          // conMat rows fetched together
 
 __device__ __forceinline__ int type_of(const V1Params &P, int local) {
@@ -1355,9 +1356,10 @@ __device__ __forceinline__ void far_push_range(const V1Params &P, long long tl, 
 
 // All of step tl's far push, shared by nCta CTAs.
 template <int U = 1>
-__device__ __forceinline__ void far_push_list(const V1Params &P, long long tl, Smem &sm, int cta, int nCta) {
+__device__ __forceinline__ void far_push_list(const V1Params &P, long long tl, Smem &sm, int cta, int nCta,
+                                              int tSlot = -1) {
     const unsigned long long size = far_list_size(P, tl);
-    far_push_range<U>(P, tl, sm, cta, nCta, size, 0, (int)(size & 0xffffffffu));
+    far_push_range<U>(P, tl, sm, cta, nCta, size, 0, (int)(size & 0xffffffffu), tSlot);
 }
 
 // Phase C, part 2 (runs in step t): appends this CTA's far presynaptic spikers to step t's
@@ -2095,7 +2097,7 @@ template <bool Rng>
 __device__ __forceinline__ void batch_trial_steps(const V1Params &P, long long t0, int steps, int cta, int nCta,
                                                   const float *__restrict__ lgnRing, int lgnSlots, bool deliverFirst,
                                                   unsigned *barrier, Smem &sm, unsigned *s_arrived,
-                                                  int *sIds) {
+                                                  float *dyn) {
     const int bs = P.blockSize;
     const int nq = (bs + kCta - 1) / kCta;
     const int b = cta / nq;
@@ -2115,28 +2117,37 @@ __device__ __forceinline__ void batch_trial_steps(const V1Params &P, long long t
     const int farDeg = (P.farOn && active) ? P.farOff[i + 1] - farE0 : 0;
     const int farN1 = (P.farOn && active) ? P.farN1[i] : 0;
     const bool isFarPre = P.farOn && active && P.farPre[i];
-    // short LGN lists: ids in shared memory (column per thread) for the trial's steps, and each
-    // step's spike words fetched while the trial's CTAs meet at the barrier
-    const bool smemIds = sIds && P.maxLGN <= kMaxLgnReg && !P.multiSpike;
-    if (smemIds) {
-#pragma unroll
-        for (int q = 0; q < kMaxLgnReg; q++)
-            sIds[q * kCta + threadIdx.x] = (active && q < m) ? __ldg(P.lgnId + (size_t)q * P.nV1 + i) : 0;
+    // short LGN lists: ids, weights and the step's spike words in shared memory ([synapse][kCta]
+    // from the thread's column), the next step's words copied in while the trial's CTAs meet at
+    // the barrier -- as the single-patch persistent kernel does
+    const bool smemSyn = dyn && P.maxLGN <= kBatchLgn && !P.multiSpike;
+    float *smW = dyn + threadIdx.x;
+    float *smS = dyn + (size_t)kBatchLgn * kCta + threadIdx.x;
+    int *smI = reinterpret_cast<int *>(dyn + (size_t)2 * kBatchLgn * kCta) + threadIdx.x;
+    // ring slots kept incrementally (t mod lgnSlots, t mod farDepth)
+    int lgnSlot = (int)(t0 % lgnSlots);
+    int fsT = P.farOn ? far_ring_slot(P, t0) : 0, fsPrev = P.farOn ? far_ring_slot(P, t0 - 1) : 0;
+    if (smemSyn) {
+        for (int q = 0; q < m; q++) {
+            smI[q * kCta] = __ldg(P.lgnId + (size_t)q * P.nV1 + i);
+            smW[q * kCta] = __ldg(P.sLGN + (size_t)q * P.nV1 + i);
+        }
+        if (active) lgn_words_async(lgnRing + (size_t)lgnSlot * P.lgnN, smI, smS, m);
     }
-    LgnPre pre{0u, 0.f, 0.f};
-    bool havePre = false;
     for (int s = 0; s < steps; s++) {
         const long long t = t0 + s;
-        if (s > 0 || deliverFirst) deliver_prev<Rng>(P, t - 1, b, local, i, active, itype, st, condState, sm);
+        if (s > 0 || deliverFirst)
+            deliver_prev<Rng>(P, t - 1, b, local, i, active, itype, st, condState, sm, P.farOn ? fsPrev : -1);
+        const int lgnNext = lgnSlot + 1 == lgnSlots ? 0 : lgnSlot + 1;
         float sInfo = 0.f;
         if (active) {
-            const float *lgnSInfo = lgnRing + (size_t)(t % lgnSlots) * P.lgnN;
+            const float *lgnSInfo = lgnRing + (size_t)lgnSlot * P.lgnN;
             if (P.multiSpike) {
                 sInfo = step_neuron_multi<Rng>(P, t, i, itype, tonic, depC, m, lgnSInfo, st, condState, noisyState);
-            } else if (smemIds) {
-                if (!havePre) pre = lgn_prefetch<kCta>(P, lgnSInfo, sIds + threadIdx.x, m, i);
-                sInfo = step_neuron<Rng, true>(P, t, i, itype, tonic, depC, m, nullptr, lgnSInfo, st, condState,
-                                               noisyState, &pre);
+            } else if (smemSyn) {
+                lgn_words_wait();
+                sInfo = step_neuron<Rng, false, true>(P, t, i, itype, tonic, depC, m, nullptr, lgnSInfo, st,
+                                                      condState, noisyState, nullptr, smW, smS);
             } else {
                 sInfo = step_neuron<Rng, false>(P, t, i, itype, tonic, depC, m, nullptr, lgnSInfo, st, condState,
                                                 noisyState);
@@ -2144,17 +2155,19 @@ __device__ __forceinline__ void batch_trial_steps(const V1Params &P, long long t
             if (P.spikeCount && sInfo >= 1.0f) P.spikeCount[i] += (unsigned)floorf(sInfo);
         }
         if (P.farOn) {
-            far_push_list(P, t - 1, sm, cta, nCta);
-            far_phase(P, t, i, active, sInfo, isFarPre, farE0, farDeg, farN1, sm, cta);
+            far_push_list(P, t - 1, sm, cta, nCta, fsPrev);
+            far_phase(P, t, i, active, sInfo, isFarPre, farE0, farDeg, farN1, sm, cta, fsT);
+            fsPrev = fsT;
+            if (++fsT == P.farDepth) fsT = 0;
         }
         if (s + 1 < steps) {
             barrier_arrive(barrier, s_arrived);
-            if (smemIds && active)
-                pre = lgn_prefetch<kCta>(P, lgnRing + (size_t)((t + 1) % lgnSlots) * P.lgnN, sIds + threadIdx.x, m, i);
-            havePre = smemIds;
+            if (smemSyn && active) lgn_words_async(lgnRing + (size_t)lgnNext * P.lgnN, smI, smS, m);
             if (!barrier_wait(barrier, (unsigned)nCta * (unsigned)(s + 1), s_arrived, P.err, P.waitSpins)) break;
         }
+        lgnSlot = lgnNext;
     }
+    if (smemSyn) lgn_words_wait();
     if (active) {
         store_state(P, i, st);
         if (Rng && P.condRng) P.rGenCond[i] = condState;
@@ -2170,7 +2183,7 @@ __global__ void __launch_bounds__(kCta, 2) v1_batch_persistent_kernel(const Batc
     __shared__ Smem sm;
     __shared__ __align__(16) BatchTrial sT;
     __shared__ unsigned s_arrived;
-    extern __shared__ int sIds[];   // [kMaxLgnReg][kCta] LGN synapse ids (dynamic)
+    extern __shared__ __align__(16) float dyn[];   // LGN synapses: weights, words, ids [kBatchLgn][kCta] each
     const int slot = blockIdx.x / slotCtas, c = blockIdx.x % slotCtas;
     const int na = *nActive;
     for (int j = slot; j < na; j += nSlots) {
@@ -2187,16 +2200,17 @@ __global__ void __launch_bounds__(kCta, 2) v1_batch_persistent_kernel(const Batc
         const int steps = left < K ? (int)left : K;
         if (steps <= 0) continue;
         batch_trial_steps<Rng>(sT.v, t0, steps, c, sT.nCta, sT.lgnRing, sT.lgnSlots, t0 >= sT.tDeliverFrom,
-                               barriers + q, sm, &s_arrived, sIds);
+                               barriers + q, sm, &s_arrived, dyn);
     }
 }
 
-// The kernel's shared memory (Smem, the trial block and 32 KB of ids) passes the 48 KB a
-// block gets without opting in.
+// The kernel's shared memory (Smem, the trial block and 72 KB of LGN synapses) passes the
+// 48 KB a block gets without opting in; two blocks still fit an SM.
+constexpr size_t kBatchDyn = (size_t)3 * kBatchLgn * kCta * sizeof(float);
 static cudaError_t batch_persistent_smem_optin() {
     static cudaError_t done = cudaErrorNotReady;
     if (done == cudaErrorNotReady) {
-        const int dyn = kMaxLgnReg * kCta * (int)sizeof(int);
+        const int dyn = (int)kBatchDyn;
         done = cudaFuncSetAttribute(v1_batch_persistent_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
         if (done == cudaSuccess)
             done = cudaFuncSetAttribute(v1_batch_persistent_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2208,7 +2222,7 @@ static cudaError_t batch_persistent_smem_optin() {
 int v1_batch_persistent_capacity(bool rng, int device) {
     int perSM = 0, sms = 0;
     if (batch_persistent_smem_optin() != cudaSuccess) return 0;
-    const size_t dyn = (size_t)kMaxLgnReg * kCta * sizeof(int);
+    const size_t dyn = kBatchDyn;
     cudaError_t e = rng ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_batch_persistent_kernel<true>, kCta, dyn)
                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, v1_batch_persistent_kernel<false>, kCta, dyn);
     if (e != cudaSuccess) return 0;
@@ -2227,7 +2241,7 @@ cudaError_t launch_v1_batch_persistent(const BatchTrial *trials, const int *acti
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nSlots * slotCtas);
     cfg.blockDim = dim3(kCta);
-    cfg.dynamicSmemBytes = (size_t)kMaxLgnReg * kCta * sizeof(int);
+    cfg.dynamicSmemBytes = kBatchDyn;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;

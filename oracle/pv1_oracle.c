@@ -1699,10 +1699,11 @@ int orc_v1_init_spikes(orc_v1 *o, const float *sp0, uint32_t SCsplit, int depth,
     return mism;
 }
 
-/* LGN->V1 plasticity, learning = 3.  Derived rates as learnFF_post computes them
- * (src/condShape.h:137-152; Float = float with its double literals), exp_homeo =
- * exp(-dt/decayTimeHomeoFF) (src/patch.cu:1330), the homeostasis totals from the current
- * weights (src/patch.cu:4335-4352).  Returns -1 for other learning modes. */
+/* LGN->V1 plasticity, learning 1-4.  Derived rates of one FF type as learnFF_post computes
+ * them (src/condShape.h:137-152; Float = float with its double literals) and exp_homeo =
+ * exp(-dt/decayTimeHomeoFF) (src/patch.cu:1330); orc_v1_set_ff_learning below takes the
+ * homeostasis totals from the current weights (src/patch.cu:4335-4352) and returns -1 for
+ * modes outside 1-4 or type counts the reference does not allow. */
 void orc_ff_learning_rates(const pv1_ff_learning *l, float dt, float *out) {
     const float ALTP = l->A_LGN * l->sRatioLGN;
     const float tas = (float)((double)l->tauAvg / 1000.0);

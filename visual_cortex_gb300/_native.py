@@ -51,7 +51,7 @@ class V1Config(C.Structure):
 
 
 class FFLearning(C.Structure):
-    """pv1_ff_learning: the cfg values of LGN->V1 plasticity (learning = 3)."""
+    """pv1_ff_learning: the cfg values of LGN->V1 plasticity (learning 1-4)."""
     _fields_ = [("learning", C.c_int32), ("tauLTP", C.c_float), ("tauLTD", C.c_float), ("tauTrip", C.c_float),
                 ("tauAvg", C.c_float), ("targetFR", C.c_float), ("A_LGN", C.c_float), ("r_LTD", C.c_float),
                 ("gmaxLGN", C.c_float), ("gminLGN", C.c_float), ("sRatioLGN", C.c_float),

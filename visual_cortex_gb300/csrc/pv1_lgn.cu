@@ -415,12 +415,23 @@ __global__ void __launch_bounds__(256) lgn_spatial_kernel(
     int nMagno, int nSample, int layer0, int nLayer, int row0, float *__restrict__ S) {
     const int lane = threadIdx.x & 31;
     const int cell = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int li = blockIdx.y;
-    if (cell >= nMagno || li >= nLayer) return;
-    const int layer = layer0 + li;
+    if (cell >= nMagno) return;
     const float *sc_x = SC + (size_t)cell * nSample;
     const float *sc_y = SC + (size_t)nMagno * nSample + (size_t)cell * nSample;
     const int type = coneType[cell];
+    // the cell's sample coordinates and weights, loaded once for all the layers of the launch
+    float X[kSpatialReg], Y[kSpatialReg], Wt[kSpatialReg];
+    if (nSample <= 32 * kSpatialReg) {
+#pragma unroll
+        for (int k = 0; k < kSpatialReg; k++) {
+            const int s = lane + 32 * k;
+            X[k] = s < nSample ? sc_x[s] : 0.f;
+            Y[k] = s < nSample ? sc_y[s] : 0.f;
+            Wt[k] = s < nSample ? SW[(size_t)cell * nSample + s] : 0.f;
+        }
+    }
+    for (int li = blockIdx.y; li < nLayer; li += gridDim.y) {
+    const int layer = layer0 + li;
     float sum = 0.f, acc = 0.f;
     if (nSample <= 32 * kSpatialReg) {
         // each texel is fetched once: the cell's intensities stay in registers between the mean
@@ -431,7 +442,7 @@ __global__ void __launch_bounds__(256) lgn_spatial_kernel(
             const int s = lane + 32 * k;
             Iv[k] = 0.f;
             if (s < nSample) {
-                const float x = sc_x[s], y = sc_y[s];
+                const float x = X[k], y = Y[k];
                 const float L = tex2DLayered<float>(texL, x, y, layer), M = tex2DLayered<float>(texM, x, y, layer);
                 sum += (L + M) / 2.0f;
                 if (type == 3) Iv[k] = (L + M) / 2.0f;
@@ -451,7 +462,7 @@ __global__ void __launch_bounds__(256) lgn_spatial_kernel(
                 if (mean > 0) c = Iv[k] / mean - 1.0f;
                 else c = Iv[k];
                 if (fabsf(c) > 1.0f) c = copysignf(1.0f, c);
-                acc += SW[(size_t)cell * nSample + s] * c;
+                acc += Wt[k] * c;
             }
         }
     } else {
@@ -469,6 +480,7 @@ __global__ void __launch_bounds__(256) lgn_spatial_kernel(
     }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (lane == 0) S[(size_t)(row0 + li) * nMagno + cell] = acc;
+    }
 }
 
 // Parvo spatial stage, once per (frame, cell): the mean luminances of the centre and the
@@ -914,7 +926,8 @@ cudaError_t launch_lgn_spatial(cudaTextureObject_t L, cudaTextureObject_t M, cud
                                const float *SW, const float *SC, const int *coneType, int nMagno,
                                int nSample, int layer0, int nLayer, int row0, float *out,
                                cudaStream_t st) {
-    dim3 grid((nMagno + 7) / 8, nLayer);
+    // each warp runs its cell over up to 8 layers (the cell's coordinates and weights loaded once)
+    dim3 grid((nMagno + 7) / 8, (nLayer + 7) / 8);
     lgn_spatial_kernel<<<grid, 256, 0, st>>>(L, M, S, SW, SC, coneType, nMagno, nSample, layer0,
                                              nLayer, row0, out);
     return cudaGetLastError();

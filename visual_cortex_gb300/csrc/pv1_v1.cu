@@ -180,34 +180,32 @@ __device__ __forceinline__ int compact_spikers(const V1Params &P, const float *_
         if (k * kCta < bs && lane == 0) sm.ball[k * kWarps + warp] = bal;
     }
     __syncthreads();
-    if (warp == 0) {
-        const unsigned bal = lane < nw ? sm.ball[lane] : 0u;
-        const int c = __popc(bal);
-        int below = 0;
-        if ((lane + 1) * 32 <= nE) below = c;
-        else if (lane * 32 < nE) below = __popc(bal & ((1u << (nE - lane * 32)) - 1u));
-        int incl = c;
+    // every warp scans the block's ballot words itself (no second barrier): lane l holds word l
+    const unsigned wb = lane < nw ? sm.ball[lane] : 0u;
+    const int c = __popc(wb);
+    int below = 0;
+    if ((lane + 1) * 32 <= nE) below = c;
+    else if (lane * 32 < nE) below = __popc(wb & ((1u << (nE - lane * 32)) - 1u));
+    int incl = c;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) below += __shfl_xor_sync(0xffffffffu, below, o);
-        if (lane < nw) sm.pref[lane] = incl - c;
-        if (lane == 31) sm.total = incl;
-        if (lane == 0) sm.below = below;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
     }
-    __syncthreads();
-    const int total = sm.total;
-    *cntE = sm.below;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) below += __shfl_xor_sync(0xffffffffu, below, o);
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    *cntE = below;
     if (total == 0) return 0;
+    const int excl = incl - c;
 #pragma unroll
     for (int k = 0; k < kMaxBS / kCta; k++) {
         const int j = k * kCta + threadIdx.x;
+        // word k * kWarps + warp holds this warp's lanes for pass k (j >> 5)
+        const int wbase = __shfl_sync(0xffffffffu, excl, (k * kWarps + warp) & 31);
+        const unsigned wbits = __shfl_sync(0xffffffffu, wb, (k * kWarps + warp) & 31);
         if (j < bs && vals[k] >= 1.0f) {
-            const int w = j >> 5;
-            const int pos = sm.pref[w] + __popc(sm.ball[w] & ((1u << lane) - 1u));
+            const int pos = wbase + __popc(wbits & ((1u << lane) - 1u));
             sm.pre[pos] = j;
             const float sI = vals[k];
             const float nsp = floorf(sI);

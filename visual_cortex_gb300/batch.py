@@ -111,14 +111,15 @@ def main(argv=None):
     ap.add_argument("--trials", type=int, default=64)
     ap.add_argument("--dur-ms", type=float, nargs=2, default=(250.0, 2000.0))
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--sweep", action="store_true", help="one graph with one cooperative V1 launch (pv1_batch_sweep)")
     a = ap.parse_args(argv)
     trials = synth.batch_trials(n_trials=a.trials, seed=0, dur_ms=tuple(a.dur_ms))
     sims = [Simulation(t.wl.spec, t.wl.net, t.wl.lgn, t.wl.stim, t.wl.init, t.wl.seeds) for t in trials]
-    b = Batch(sims, [t.steps for t in trials], autotune=not a.no_autotune)
-    _, ms = b.run()
+    b = Batch(sims, [t.steps for t in trials], autotune=not (a.no_autotune or a.sweep))
+    ms = b.sweep() if a.sweep else b.run()[1]
     work = sum(t.steps * t.wl.spec.nV1 for t in trials)
-    print(f"{a.trials} trials, {work} neuron-steps in {ms:.2f} ms: {work / (ms * 1e-3):.4g} neuron-steps/s; "
-          f"tuning {b.tuning()}")
+    how = "one-launch sweep" if a.sweep else f"tuning {b.tuning()}"
+    print(f"{a.trials} trials, {work} neuron-steps in {ms:.2f} ms: {work / (ms * 1e-3):.4g} neuron-steps/s; {how}")
     b.close()
     for s in sims:
         s.close()
